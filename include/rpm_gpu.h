@@ -1,0 +1,168 @@
+/*
+ * rpm_gpu.h -- C ABI of the GB300 collision and distance engine for
+ * RPMPLv2's RealVectorSpace path.
+ *
+ * The engine replaces the link x obstacle loops behind
+ *   base::RealVectorSpace::isValid(q)              src/state_spaces/real_vector_space/RealVectorSpace.cpp:277-309
+ *   base::RealVectorSpace::isValid(q1, q2)         RealVectorSpace.cpp:261-275 (+ interpolateEdge :75-88)
+ *   base::RealVectorSpace::computeDistance(q, ..)  RealVectorSpace.cpp:318-392
+ * and the forward kinematics / skeleton recipes they call
+ *   robots::xArm6::computeForwardKinematics/computeSkeleton    src/robots/xArm6.cpp:107-134, 209-235
+ *   robots::Planar2DOF::computeForwardKinematics/computeSkeleton src/robots/Planar2DOF.cpp:82-130
+ * Obstacles reach the path as fcl world AABBs (src/environments/objects/Box.cpp:3-14).
+ *
+ * Conventions: every entry point returns an int status (RPM_OK == 0, negative
+ * on error) and never throws.  rpm_last_error_string() returns a message for
+ * the last failing call on the calling thread.  Pointers named *_dev are
+ * device pointers owned by the caller; pointers named *_host are ordinary or
+ * pinned host pointers owned by the caller.  Robots and scenes are owned by
+ * the context.  A context may be used from several host threads as long as
+ * each thread passes its own stream.
+ */
+#ifndef RPM_GPU_H
+#define RPM_GPU_H
+
+#include <stdint.h>
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define RPM_MAX_DOF 32
+
+enum rpm_status_code {
+    RPM_OK = 0,
+    RPM_ERR_INVALID = -1,     /* bad argument, unknown handle, unsupported robot */
+    RPM_ERR_CUDA = -2,        /* a CUDA runtime call failed */
+    RPM_ERR_NOMEM = -3,       /* device or pinned allocation failed */
+    RPM_ERR_TIMEOUT = -4,     /* a bounded device-side wait gave up */
+    RPM_ERR_ADMISSION = -5,   /* request rejected by the memory budget */
+    RPM_ERR_RANGE = -6        /* size beyond a stated maximum */
+};
+
+/* Robot families of the reference.  CHAIN is robots::Planar2DOF and the
+ * classes derived from it (Planar10DOF, Spatial10/14/18/22DOF): skeleton point
+ * k is the origin of chain segment k, k = 0..D (Planar2DOF.cpp:125-126).
+ * XARM6 is robots::xArm6 with its 7-point skeleton recipe and gripper offset
+ * (xArm6.cpp:130, 215-231). */
+enum rpm_robot_kind { RPM_ROBOT_CHAIN = 0, RPM_ROBOT_XARM6 = 1 };
+
+/* Kinematic description of a serial chain as kdl_parser builds it from the
+ * URDF: joint k (0-based) has a fixed origin (origin_xyz[k], origin_rot[k])
+ * in its parent frame followed by a revolute rotation q_k about the unit axis
+ * joint_axis[k] (0 = x, 1 = y, 2 = z) of the joint frame.  Entry D of the
+ * origin arrays is the fixed tool joint ("ee" / "joint_eef").  origin_rot is
+ * row-major and is used as given, so the URDF rpy values (e.g. -1.5708, not
+ * -pi/2) are preserved. */
+typedef struct rpm_robot_desc {
+    int32_t kind;                          /* enum rpm_robot_kind */
+    int32_t num_dofs;                      /* D; also the number of capsule links */
+    int32_t ground_included;               /* links i < ground_included ignore "ground" obstacles */
+    float   gripper_length;                /* XARM6 only (xArm6.cpp:130, 231) */
+    int32_t joint_axis[RPM_MAX_DOF];
+    double  origin_xyz[RPM_MAX_DOF + 1][3];
+    double  origin_rot[RPM_MAX_DOF + 1][9];
+    float   capsule_radius[RPM_MAX_DOF];   /* AbstractRobot::getCapsuleRadius(i) */
+    float   limits[RPM_MAX_DOF][2];        /* joint limits (lower, upper); informational */
+} rpm_robot_desc;
+
+/* Obstacle flags (per obstacle). */
+#define RPM_OBS_GROUND  0x1u   /* label == "ground": skipped for links i < ground_included (RealVectorSpace.cpp:285, 336) */
+#define RPM_OBS_DYNAMIC 0x2u   /* label == "dynamic_obstacle" (moved by incremental updates) */
+
+/* RealVectorSpaceConfig constants as the YAML sets them
+ * (data/configurations/configuration_realvectorspace.yaml:1-3). */
+typedef struct rpm_params {
+    double equality_threshold;   /* EQUALITY_THRESHOLD, 1e-4 */
+    double max_distance;         /* MAX_DISTANCE, 1000 */
+} rpm_params;
+
+/* Arithmetic forms of the check. */
+enum rpm_precision {
+    RPM_PREC_FP64 = 0,          /* FP64 FK and narrow phase ("plain form") */
+    RPM_PREC_FP32_RECHECK = 1,  /* FP32 bulk pass; configs near any decision boundary are recomputed in FP64 */
+    RPM_PREC_FP32_REF = 2       /* the reference's own numerics: FP64 FK rounded to FP32, FP32 narrow phase */
+};
+
+typedef struct rpm_ctx rpm_ctx;
+
+/* Statistics of the last check issued on a context (read after a sync). */
+typedef struct rpm_check_stats {
+    int64_t configs;           /* configurations (or edge checks) in the call */
+    int64_t rechecked;         /* configurations recomputed in FP64 by the recheck pass */
+    int64_t overflow;          /* recheck entries that did not fit the recheck list (must be 0) */
+    int32_t device_status;     /* 0, or an RPM_ERR_* recorded by a kernel */
+    int32_t pad;
+} rpm_check_stats;
+
+/* ---- errors ---------------------------------------------------------------- */
+const char *rpm_last_error_string(void);
+int rpm_version(void);
+
+/* ---- context ----------------------------------------------------------------
+ * Replaces nothing in the reference (it has no device); holds the device
+ * robots, scenes and reusable scratch. */
+int rpm_ctx_create(int device, rpm_ctx **out);
+int rpm_ctx_destroy(rpm_ctx *ctx);
+int rpm_ctx_set_params(rpm_ctx *ctx, const rpm_params *params);
+
+/* ---- robots -----------------------------------------------------------------
+ * Replaces the robot construction from URDF (xArm6.cpp:7-76, Planar2DOF.cpp:7-64,
+ * Spatial10DOF.cpp:5-9) plus AbstractRobot::setCapsulesRadius / setGroundIncluded. */
+int rpm_robot_upload(rpm_ctx *ctx, const rpm_robot_desc *desc, int32_t *robot_id);
+
+/* ---- scenes (device-resident obstacle sets) ----------------------------------
+ * Replaces env::Environment's object list as the hot path sees it
+ * (Environment.cpp:13-56; fcl AABB per Box.cpp:6-7).  aabb_host is n x 6
+ * floats (xmin, ymin, zmin, xmax, ymax, zmax) per obstacle, exactly the
+ * 'obs' vector of RealVectorSpace.cpp:293-295; min_dist_tol_host is
+ * Object::getMinDistTol (Box.cpp:13, YAML min_dist_tol); flags_host holds
+ * RPM_OBS_* bits.  min_dist_tol_host and flags_host may be NULL (MAX_DISTANCE, 0). */
+int rpm_scene_create(rpm_ctx *ctx, int32_t robot_id, const float *aabb_host, const float *min_dist_tol_host,
+                     const uint8_t *flags_host, int32_t n, int32_t *scene_id);
+/* Replace the AABBs of obstacles idx[0..m) (Object::setPosition, Object.cpp:21-26;
+ * Environment::updateEnvironment moves).  The new version is visible to every
+ * check issued on any stream after this call returns; checks already issued
+ * keep the version they started with. */
+int rpm_scene_update(rpm_ctx *ctx, int32_t scene_id, const int32_t *idx_host, const float *aabb_host, int32_t m,
+                     uint64_t *version_out);
+int rpm_scene_destroy(rpm_ctx *ctx, int32_t scene_id);
+int rpm_scene_info(rpm_ctx *ctx, int32_t scene_id, int32_t *robot_id, int32_t *num_obstacles, uint64_t *version);
+
+/* fcl 0.7 world AABB of a box (Box.cpp:6-7): identity rotation gives
+ * pos +- dim/2; any other rotation gives the cube pos +- |dim/2|. */
+int rpm_box_aabb(const float dim[3], const float pos[3], const float quat_xyzw[4], float aabb_out[6]);
+
+/* ---- batched checks ------------------------------------------------------------
+ * For configurations q_dev (C x D floats, row-major, one RealVectorSpaceState
+ * coordinate vector per row) compute
+ *   valid_dev[c]   = isValid(q_c)                     (1 valid, 0 in collision)  nullable
+ *   dist_dev[c]    = computeDistance(q_c, true)        (0 on collision)          nullable
+ *   profile_dev[c*L+i] = d_c_profile[i] after computeDistance, including its
+ *                    early-exit shape (RealVectorSpace.cpp:370-378)            nullable
+ * All work is queued on 'stream' (a cudaStream_t, NULL = legacy default). */
+int rpm_check_configs(rpm_ctx *ctx, int32_t scene_id, int32_t precision, const float *q_dev, int64_t num_configs,
+                      uint8_t *valid_dev, double *dist_dev, float *profile_dev, void *stream);
+
+/* Same as rpm_check_configs with host buffers: stages through context-owned
+ * pinned memory, overlaps copies with compute and returns after the results
+ * are in the host buffers. */
+int rpm_check_configs_host(rpm_ctx *ctx, int32_t scene_id, int32_t precision, const float *q_host, int64_t num_configs,
+                           uint8_t *valid_host, double *dist_host, float *profile_host);
+
+/* Skeleton points (L+1 points x 3) per configuration, in FP64
+ * (computeSkeleton of the robot in the scene; xArm6.cpp:209-235). */
+int rpm_skeleton(rpm_ctx *ctx, int32_t robot_id, int32_t precision, const float *q_dev, int64_t num_configs,
+                 double *points_dev, void *stream);
+
+/* Statistics of the last check on this context; synchronises 'stream'. */
+int rpm_last_stats(rpm_ctx *ctx, void *stream, rpm_check_stats *out);
+
+/* Synchronise a stream and report any device-side error status. */
+int rpm_sync(rpm_ctx *ctx, void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* RPM_GPU_H */

@@ -1,0 +1,52 @@
+"""ctypes mirror of include/rpm_gpu.h (structs and constants only)."""
+import ctypes
+
+RPM_MAX_DOF = 32
+
+RPM_OK = 0
+RPM_ERR_INVALID = -1
+RPM_ERR_CUDA = -2
+RPM_ERR_NOMEM = -3
+RPM_ERR_TIMEOUT = -4
+RPM_ERR_ADMISSION = -5
+RPM_ERR_RANGE = -6
+
+RPM_ROBOT_CHAIN = 0
+RPM_ROBOT_XARM6 = 1
+
+RPM_OBS_GROUND = 0x1
+RPM_OBS_DYNAMIC = 0x2
+
+RPM_PREC_FP64 = 0
+RPM_PREC_FP32_RECHECK = 1
+RPM_PREC_FP32_REF = 2
+
+PRECISIONS = {"fp64": RPM_PREC_FP64, "fp32_recheck": RPM_PREC_FP32_RECHECK, "fp32_ref": RPM_PREC_FP32_REF}
+
+
+class RobotDesc(ctypes.Structure):
+    _fields_ = [
+        ("kind", ctypes.c_int32),
+        ("num_dofs", ctypes.c_int32),
+        ("ground_included", ctypes.c_int32),
+        ("gripper_length", ctypes.c_float),
+        ("joint_axis", ctypes.c_int32 * RPM_MAX_DOF),
+        ("origin_xyz", (ctypes.c_double * 3) * (RPM_MAX_DOF + 1)),
+        ("origin_rot", (ctypes.c_double * 9) * (RPM_MAX_DOF + 1)),
+        ("capsule_radius", ctypes.c_float * RPM_MAX_DOF),
+        ("limits", (ctypes.c_float * 2) * RPM_MAX_DOF),
+    ]
+
+
+class Params(ctypes.Structure):
+    _fields_ = [("equality_threshold", ctypes.c_double), ("max_distance", ctypes.c_double)]
+
+
+class CheckStats(ctypes.Structure):
+    _fields_ = [
+        ("configs", ctypes.c_int64),
+        ("rechecked", ctypes.c_int64),
+        ("overflow", ctypes.c_int64),
+        ("device_status", ctypes.c_int32),
+        ("pad", ctypes.c_int32),
+    ]

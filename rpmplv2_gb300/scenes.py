@@ -1,0 +1,167 @@
+"""Seeded synthetic workloads with the reference's shapes and distributions.
+
+The reference has no public benchmark for this path; its random-obstacle
+experiments (apps/CommonFunctions.h:77-177) place boxes in a workspace sphere
+and reject boxes that make the start configuration invalid.  These
+generators produce the same kinds of scenes with fixed seeds:
+
+* ``planar_2dof_workload``   planar_2dof, 4 AABBs in a 2 m disk, 65,536 configs
+* ``xarm6_workload``         xarm6 capsules (r 0.05, gripper 0.1, ground from
+                             link 2), 50 cubes of 0.05 m in a 1 m ball around
+                             (0, 0, 0.267) rejected if they touch q = 0,
+                             1,048,576 configs in [-pi, pi]^6
+* ``spatial10_edge_workload`` spatial_10dof (r 0.03), 200 rotated boxes turned
+                             into fcl world AABBs, 262,144 edges discretised
+                             at 0.05 rad
+* ``mixed_dof_workload``     spatial 14/18/22 (r 0.03), 500 AABBs in a 1.5 m
+                             ball, 32,768/49,152/49,152 configs
+
+Every array is float32 (the reference's State coordinates are
+Eigen::VectorXf, include/state_spaces/State.h:27).
+"""
+import math
+
+import numpy as np
+
+from . import robots as _robots
+from ._abi import RPM_OBS_GROUND, RPM_OBS_DYNAMIC
+
+MAX_DISTANCE = 1000.0
+
+
+class Scene:
+    """An obstacle set as the hot path sees it: fcl world AABBs (n, 6) float32,
+    min_dist_tol (n,) float32 and RPM_OBS_* flags (n,) uint8."""
+
+    def __init__(self, aabb, tol=None, flags=None, labels=None):
+        self.aabb = np.ascontiguousarray(aabb, dtype=np.float32).reshape(-1, 6)
+        n = self.aabb.shape[0]
+        self.tol = (np.full(n, MAX_DISTANCE, np.float32) if tol is None
+                    else np.ascontiguousarray(tol, dtype=np.float32))
+        self.flags = np.zeros(n, np.uint8) if flags is None else np.ascontiguousarray(flags, dtype=np.uint8)
+        self.labels = labels
+
+    @property
+    def n(self):
+        return self.aabb.shape[0]
+
+
+def box_aabb(dim, pos, quat_xyzw=(0.0, 0.0, 0.0, 1.0)):
+    """fcl 0.7 world AABB of a box (src/environments/objects/Box.cpp:6-7):
+    identity rotation -> (-dim/2) + pos .. dim/2 + pos, any other rotation ->
+    the cube pos -/+ |dim/2|.  float32 arithmetic."""
+    dim = np.asarray(dim, np.float32)
+    pos = np.asarray(pos, np.float32)
+    x, y, z, w = [np.float32(v) for v in quat_xyzw]
+    h = np.float32(0.5) * dim
+    if x == 0 and y == 0 and z == 0 and abs(w) == 1:
+        return np.concatenate([(-h) + pos, h + pos]).astype(np.float32)
+    rad = np.sqrt(h[0] * h[0] + (h[1] * h[1] + h[2] * h[2])).astype(np.float32)
+    return np.concatenate([pos - rad, pos + rad]).astype(np.float32)
+
+
+def ground_box():
+    """The 'ground' obstacle of the xarm6 scenarios (data/xarm6/scenario1/scenario1.yaml:2-6)."""
+    return box_aabb([1.5, 1.5, 0.1], [0.0, 0.0, -0.05]), np.float32(0.05)
+
+
+def _ball(rng, n, center, radius):
+    pts = []
+    while len(pts) < n:
+        p = rng.uniform(-1.0, 1.0, 3)
+        if p @ p <= 1.0:
+            pts.append(np.asarray(center) + radius * p)
+    return np.array(pts)
+
+
+def _seg_aabb_dist(a, b, box, samples=65):
+    t = np.linspace(0.0, 1.0, samples)[:, None]
+    p = a[None, :] + t * (b - a)[None, :]
+    d = np.maximum(np.maximum(box[:3] - p, p - box[3:]), 0.0)
+    return float(np.sqrt((d * d).sum(1)).min()), float(np.linalg.norm(b - a)) / (samples - 1)
+
+
+def touches(robot, q, box, margin=0.01):
+    """Conservative host test: True if the capsule skeleton at q comes within
+    radius + margin of the box (used to reject obstacles at q = 0)."""
+    sk = robot.skeleton_np(q)
+    r = robot.capsule_radius
+    for i in range(robot.num_links):
+        d, h = _seg_aabb_dist(sk[i], sk[i + 1], box.astype(np.float64))
+        if d <= r[i] + margin + h:
+            return True
+    return False
+
+
+def uniform_configs(rng, n, dofs, lo=-math.pi, hi=math.pi):
+    return rng.uniform(lo, hi, (n, dofs)).astype(np.float32)
+
+
+def planar_2dof_workload(num_configs=65536, seed=0):
+    rng = np.random.default_rng(seed)
+    robot = _robots.planar_2dof(radius=0.0)
+    boxes = []
+    for _ in range(4):
+        dx, dy = rng.uniform(0.1, 0.5, 2)
+        rr, th = 2.0 * math.sqrt(rng.uniform()), rng.uniform(0, 2 * math.pi)
+        boxes.append(box_aabb([dx, dy, 0.1], [rr * math.cos(th), rr * math.sin(th), 0.0]))
+    scene = Scene(np.array(boxes))
+    q = uniform_configs(rng, num_configs, 2)
+    return robot, scene, q
+
+
+def xarm6_workload(num_configs=1 << 20, num_obstacles=50, seed=1, gripper_length=0.1, radius=0.05):
+    rng = np.random.default_rng(seed)
+    robot = _robots.xarm6(radius=radius, gripper_length=gripper_length, ground_included=2)
+    g_aabb, g_tol = ground_box()
+    aabb = [g_aabb]
+    tol = [g_tol]
+    flags = [RPM_OBS_GROUND]
+    q0 = np.zeros(6)
+    while len(aabb) < num_obstacles + 1:
+        c = _ball(rng, 1, (0.0, 0.0, 0.267), 1.0)[0]
+        box = box_aabb([0.05, 0.05, 0.05], c)
+        if touches(robot, q0, box):
+            continue
+        aabb.append(box)
+        tol.append(np.float32(MAX_DISTANCE))
+        flags.append(0)
+    scene = Scene(np.array(aabb), np.array(tol, np.float32), np.array(flags, np.uint8))
+    q = uniform_configs(rng, num_configs, 6)
+    return robot, scene, q
+
+
+def random_obb_scene(rng, n, dim_lo, dim_hi, center, radius, rotated=True):
+    boxes = []
+    for _ in range(n):
+        dim = rng.uniform(dim_lo, dim_hi, 3)
+        c = _ball(rng, 1, center, radius)[0]
+        if rotated:
+            qv = rng.normal(size=4)
+            qv = qv / np.linalg.norm(qv)
+        else:
+            qv = np.array([0.0, 0.0, 0.0, 1.0])
+        boxes.append(box_aabb(dim, c, qv))
+    return Scene(np.array(boxes))
+
+
+def spatial10_edge_workload(num_edges=1 << 18, seed=2, step=0.05):
+    rng = np.random.default_rng(seed)
+    robot = _robots.spatial(10, radius=0.03)
+    scene = random_obb_scene(rng, 200, 0.02, 0.1, (0.0, 0.0, 0.0), 1.2, rotated=True)
+    q1 = uniform_configs(rng, num_edges, 10)
+    u = rng.normal(size=(num_edges, 10))
+    u /= np.linalg.norm(u, axis=1, keepdims=True)
+    length = rng.uniform(0.01, 2.0, (num_edges, 1))
+    q2 = (q1 + u * length).astype(np.float32)
+    return robot, scene, q1, q2, np.float32(step)
+
+
+def mixed_dof_workload(counts=(32768, 49152, 49152), seed=3):
+    rng = np.random.default_rng(seed)
+    scene = random_obb_scene(rng, 500, 0.02, 0.15, (0.0, 0.0, 0.0), 1.5, rotated=False)
+    parts = []
+    for dofs, n in zip((14, 18, 22), counts):
+        robot = _robots.spatial(dofs, radius=0.03)
+        parts.append((robot, uniform_configs(rng, n, dofs)))
+    return scene, parts
