@@ -151,8 +151,10 @@ int rpm_check_configs(rpm_ctx *ctx, int32_t scene_id, int32_t precision, const f
 int rpm_check_configs_host(rpm_ctx *ctx, int32_t scene_id, int32_t precision, const float *q_host, int64_t num_configs,
                            uint8_t *valid_host, double *dist_host, float *profile_host);
 
-/* Skeleton points (L+1 points x 3) per configuration, in FP64
- * (computeSkeleton of the robot in the scene; xArm6.cpp:209-235). */
+/* Skeleton points (L+1 points x 3) per configuration, widened to double
+ * (computeSkeleton; xArm6.cpp:209-235, Planar2DOF.cpp:117-130): RPM_PREC_FP64
+ * gives the FP64 points, RPM_PREC_FP32_REF the reference's float skeleton,
+ * RPM_PREC_FP32_RECHECK the FP32 FK of the bulk pass. */
 int rpm_skeleton(rpm_ctx *ctx, int32_t robot_id, int32_t precision, const float *q_dev, int64_t num_configs,
                  double *points_dev, void *stream);
 

@@ -1,0 +1,75 @@
+"""Builds the CUDA library librpm_gb300.so in-tree for sm_103a.
+
+rpm_exact.cu is compiled with --fmad=false (no contracted multiply-add, so the
+exact forms round like the CPU restatement); rpm_fast.cu and rpm_api.cu with
+the default contraction.  Translation units compile in parallel.
+"""
+import concurrent.futures as cf
+import os
+import subprocess
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+CSRC = os.path.join(HERE, "csrc")
+OUT_DIR = os.path.join(HERE, "_build")
+LIB = os.path.join(OUT_DIR, "librpm_gb300.so")
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+COMMON = ["-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off"]
+UNITS = {"rpm_exact.cu": ["--fmad=false"], "rpm_fast.cu": ["--fmad=true"], "rpm_api.cu": []}
+
+
+def _deps():
+    files = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".cu", ".cuh"))]
+    files.append(os.path.join(HERE, "..", "include", "rpm_gpu.h"))
+    return files
+
+
+def _up_to_date():
+    if not os.path.exists(LIB):
+        return False
+    t = os.path.getmtime(LIB)
+    return all(os.path.getmtime(f) <= t for f in _deps())
+
+
+def nvcc():
+    cand = os.environ.get("NVCC")
+    if cand:
+        return cand
+    for p in ("/usr/local/cuda/bin/nvcc",):
+        if os.path.exists(p):
+            return p
+    return "nvcc"
+
+
+def build(force=False, verbose=False):
+    if not force and _up_to_date():
+        return LIB
+    os.makedirs(OUT_DIR, exist_ok=True)
+
+    def compile_one(item):
+        src, extra = item
+        obj = os.path.join(OUT_DIR, src.replace(".cu", ".o"))
+        cmd = [nvcc(), *ARCH, *COMMON, *extra, "-c", os.path.join(CSRC, src), "-o", obj]
+        if verbose:
+            cmd.insert(1, "-Xptxas=-v")
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError("nvcc failed for %s:\n%s%s" % (src, r.stdout, r.stderr))
+        return obj, r.stderr
+
+    with cf.ThreadPoolExecutor(max_workers=len(UNITS)) as ex:
+        results = list(ex.map(compile_one, UNITS.items()))
+    if verbose:
+        for _, log in results:
+            print(log)
+    tmp = LIB + ".tmp%d" % os.getpid()
+    cmd = [nvcc(), *ARCH, "-shared", "-o", tmp] + [o for o, _ in results]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("link failed:\n%s%s" % (r.stdout, r.stderr))
+    os.replace(tmp, LIB)
+    return LIB
+
+
+if __name__ == "__main__":
+    import sys
+    print(build(force="-f" in sys.argv, verbose="-v" in sys.argv))

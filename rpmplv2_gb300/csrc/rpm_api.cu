@@ -1,0 +1,553 @@
+// rpm_api.cu -- the C ABI declared in include/rpm_gpu.h.
+//
+// Ownership: the context owns device robots (DevRobot), scenes (a small ring
+// of versioned obstacle buffers per scene) and per-stream scratch (FP32 ->
+// FP64 recheck list, counters, device status word).  Callers own every
+// q / output pointer they pass.
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "rpm_launch.cuh"
+
+using namespace rpm;
+
+namespace {
+
+thread_local std::string g_err;
+
+int fail(int code, const char *fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    g_err = buf;
+    return code;
+}
+
+#define CK(x)                                                                                   \
+    do {                                                                                        \
+        cudaError_t e_ = (x);                                                                   \
+        if (e_ != cudaSuccess) return fail(RPM_ERR_CUDA, "%s: %s", #x, cudaGetErrorString(e_)); \
+    } while (0)
+
+constexpr int kRing = 4;   // versions kept per scene
+
+struct RobotRec {
+    rpm_robot_desc desc;
+    DevRobot *dev = nullptr;
+};
+
+struct SceneBuf {
+    void *mem = nullptr;
+    float *f = nullptr;
+    double *d = nullptr;
+    std::vector<cudaEvent_t> users;   // checks that may still read this buffer
+};
+
+struct SceneRec {
+    int robot = 0;
+    int n = 0, n_pad = 16;
+    std::vector<float> aabb, tol;
+    std::vector<uint8_t> flags;
+    int cur = 0;
+    SceneBuf bufs[kRing];
+    uint64_t version = 0;
+};
+
+struct Scratch {
+    uint64_t *recheck = nullptr;
+    size_t cap = 0;
+    uint32_t *counters = nullptr;   // [0] recheck count
+    int32_t *status = nullptr;
+    int64_t last_configs = 0;
+};
+
+}  // namespace
+
+struct rpm_ctx {
+    int device = 0;
+    int num_sms = 0;
+    rpm_params params{1e-4, 1000.0};
+    std::mutex mu;
+    std::vector<RobotRec> robots;
+    std::map<int, SceneRec *> scenes;
+    int next_scene = 0;
+    std::map<cudaStream_t, Scratch *> scratch;
+    std::vector<cudaEvent_t> event_pool;
+    // host-buffer pipeline
+    cudaStream_t hs[2] = {nullptr, nullptr};
+    float *hq[2] = {nullptr, nullptr};
+    uint8_t *hv[2] = {nullptr, nullptr};
+    double *hd[2] = {nullptr, nullptr};
+    float *hp[2] = {nullptr, nullptr};
+    size_t hcap_cfg = 0, hcap_prof = 0;
+};
+
+namespace {
+
+int set_device(rpm_ctx *ctx) {
+    CK(cudaSetDevice(ctx->device));
+    return RPM_OK;
+}
+
+cudaEvent_t get_event(rpm_ctx *ctx) {
+    if (!ctx->event_pool.empty()) {
+        cudaEvent_t e = ctx->event_pool.back();
+        ctx->event_pool.pop_back();
+        return e;
+    }
+    cudaEvent_t e = nullptr;
+    cudaEventCreateWithFlags(&e, cudaEventDisableTiming);
+    return e;
+}
+
+// Drop completed user events of a buffer back into the pool.
+void prune_users(rpm_ctx *ctx, SceneBuf &b) {
+    std::vector<cudaEvent_t> keep;
+    for (cudaEvent_t e : b.users) {
+        if (cudaEventQuery(e) == cudaSuccess) ctx->event_pool.push_back(e);
+        else keep.push_back(e);
+    }
+    b.users.swap(keep);
+}
+
+void wait_users(rpm_ctx *ctx, SceneBuf &b) {
+    for (cudaEvent_t e : b.users) {
+        cudaEventSynchronize(e);
+        ctx->event_pool.push_back(e);
+    }
+    b.users.clear();
+}
+
+int upload_scene(rpm_ctx *ctx, SceneRec &s, SceneBuf &b) {
+    const int np = s.n_pad;
+    if (!b.mem) {
+        const size_t bytes = (size_t)kFRows * np * sizeof(float) + (size_t)kDRows * np * sizeof(double);
+        if (cudaMalloc(&b.mem, bytes) != cudaSuccess) return fail(RPM_ERR_NOMEM, "scene allocation of %zu bytes failed", bytes);
+        b.f = reinterpret_cast<float *>(b.mem);
+        b.d = reinterpret_cast<double *>(reinterpret_cast<char *>(b.mem) + (size_t)kFRows * np * sizeof(float));
+    }
+    std::vector<float> f((size_t)kFRows * np, 0.f);
+    std::vector<double> d((size_t)kDRows * np, 0.0);
+    for (int j = 0; j < s.n; ++j) {
+        for (int k = 0; k < 6; ++k) f[(size_t)k * np + j] = s.aabb[6 * (size_t)j + k];
+        f[(size_t)kRowTol * np + j] = s.tol[j];
+        f[(size_t)kRowGround * np + j] = (s.flags[j] & RPM_OBS_GROUND) ? 1.f : 0.f;
+        for (int k = 0; k < 7; ++k) d[(size_t)k * np + j] = (double)f[(size_t)k * np + j];
+    }
+    (void)ctx;
+    CK(cudaMemcpy(b.f, f.data(), f.size() * sizeof(float), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(b.d, d.data(), d.size() * sizeof(double), cudaMemcpyHostToDevice));
+    return RPM_OK;
+}
+
+int get_scratch(rpm_ctx *ctx, cudaStream_t st, int64_t need, Scratch **out) {
+    Scratch *s = ctx->scratch[st];
+    if (!s) {
+        s = new Scratch();
+        ctx->scratch[st] = s;
+        if (cudaMalloc(&s->counters, 64) != cudaSuccess || cudaMalloc(&s->status, 64) != cudaSuccess)
+            return fail(RPM_ERR_NOMEM, "scratch allocation failed");
+        CK(cudaMemset(s->counters, 0, 64));
+        CK(cudaMemset(s->status, 0, 64));
+    }
+    if ((int64_t)s->cap < need) {
+        if (s->recheck) {
+            CK(cudaStreamSynchronize(st));
+            cudaFree(s->recheck);
+            s->recheck = nullptr;
+        }
+        size_t cap = std::max<size_t>((size_t)need, 1u << 16);
+        if (cudaMalloc(&s->recheck, cap * sizeof(uint64_t)) != cudaSuccess)
+            return fail(RPM_ERR_NOMEM, "recheck list allocation failed");
+        s->cap = cap;
+    }
+    *out = s;
+    return RPM_OK;
+}
+
+int build_dev_robot(const rpm_robot_desc &d, DevRobot &r) {
+    if (d.kind != RPM_ROBOT_CHAIN && d.kind != RPM_ROBOT_XARM6) return fail(RPM_ERR_INVALID, "unknown robot kind %d", d.kind);
+    if (d.num_dofs < 1 || d.num_dofs > RPM_MAX_DOF) return fail(RPM_ERR_INVALID, "num_dofs %d out of range", d.num_dofs);
+    if (d.kind == RPM_ROBOT_XARM6 && d.num_dofs != 6) return fail(RPM_ERR_INVALID, "xArm6 needs num_dofs == 6");
+    std::memset(&r, 0, sizeof r);
+    r.kind = d.kind;
+    r.D = d.num_dofs;
+    r.ground_included = d.ground_included;
+    for (int k = 0; k < d.num_dofs; ++k) {
+        if (d.joint_axis[k] < 0 || d.joint_axis[k] > 2) return fail(RPM_ERR_INVALID, "joint %d axis must be 0, 1 or 2", k);
+        const float rad = d.capsule_radius[k];
+        if (!(rad >= 0.f) || !std::isfinite(rad)) return fail(RPM_ERR_INVALID, "capsule radius %d invalid", k);
+        r.axis[k] = d.joint_axis[k];
+        r.radius_f[k] = rad;
+        r.radius_d[k] = (double)rad;
+        r.rnew_d[k] = (double)rad * std::sqrt(3.0) / 3;
+        r.rnew_f[k] = (float)r.rnew_d[k];
+    }
+    for (int k = 0; k <= d.num_dofs; ++k) {
+        bool ident = true;
+        for (int i = 0; i < 9; ++i) {
+            double v = d.origin_rot[k][i];
+            if (v != ((i % 4 == 0) ? 1.0 : 0.0)) ident = false;
+            r.orot[k][i] = v;
+            r.orot_f[k][i] = (float)v;
+        }
+        if (ident && k < 32) r.rot_identity_mask |= (1 << k);
+        for (int i = 0; i < 3; ++i) {
+            r.oxyz[k][i] = d.origin_xyz[k][i];
+            r.oxyz_f[k][i] = (float)d.origin_xyz[k][i];
+        }
+    }
+    r.gripper_d = (double)d.gripper_length;
+    r.gripper_f = d.gripper_length;
+    r.grip03_f = (float)(0.3 * (double)d.gripper_length);
+    return RPM_OK;
+}
+
+SceneRec *find_scene(rpm_ctx *ctx, int id) {
+    auto it = ctx->scenes.find(id);
+    return it == ctx->scenes.end() ? nullptr : it->second;
+}
+
+// Queue one check of C configurations on 'st'; the caller holds ctx->mu.
+int enqueue_check(rpm_ctx *ctx, SceneRec *s, int prec, const float *q, int64_t C, uint8_t *valid, double *dist,
+                  float *profile, cudaStream_t st) {
+    const RobotRec &rb = ctx->robots[s->robot];
+    SceneBuf &buf = s->bufs[s->cur];
+    KParams p;
+    std::memset(&p, 0, sizeof p);
+    p.nseg = 1;
+    Seg &g = p.segs[0];
+    g.robot = rb.dev;
+    g.obs_f = buf.f;
+    g.obs_d = buf.d;
+    g.q = q;
+    g.valid = valid;
+    g.dist = dist;
+    g.profile = profile;
+    g.count = C;
+    g.first_block = 0;
+    g.n = s->n;
+    g.n_pad = s->n_pad;
+    p.nmd.eq = ctx->params.equality_threshold;
+    p.nmd.maxd = ctx->params.max_distance;
+    p.nmf.eq = (float)ctx->params.equality_threshold;
+    p.nmf.maxd = (float)ctx->params.max_distance;
+    Scratch *sc = nullptr;
+    int rc = get_scratch(ctx, st, prec == RPM_PREC_FP32_RECHECK ? C : 0, &sc);
+    if (rc) return rc;
+    p.recheck = sc->recheck;
+    p.recheck_count = sc->counters;
+    p.status = sc->status;
+    sc->last_configs = C;
+    const int64_t blocks = (C + kThreads - 1) / kThreads;
+    CK(cudaMemsetAsync(sc->counters, 0, sizeof(uint32_t), st));
+    if (blocks > 0) {
+        if (prec == RPM_PREC_FP32_RECHECK) {
+            CK(launch_check_fp32(p, blocks, smem_bytes(RPM_PREC_FP32_REF, s->n_pad), st));
+            CK(launch_recheck(p, ctx->num_sms * 4, st));
+        } else {
+            CK(launch_check_exact(prec, p, blocks, smem_bytes(prec, s->n_pad), st));
+        }
+    }
+    prune_users(ctx, buf);
+    cudaEvent_t e = get_event(ctx);
+    CK(cudaEventRecord(e, st));
+    buf.users.push_back(e);
+    return RPM_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char *rpm_last_error_string(void) { return g_err.c_str(); }
+int rpm_version(void) { return 1; }
+
+int rpm_ctx_create(int device, rpm_ctx **out) {
+    if (!out) return fail(RPM_ERR_INVALID, "out is NULL");
+    int n = 0;
+    CK(cudaGetDeviceCount(&n));
+    if (device < 0 || device >= n) return fail(RPM_ERR_INVALID, "device %d not present (%d devices)", device, n);
+    rpm_ctx *ctx = new rpm_ctx();
+    ctx->device = device;
+    CK(cudaSetDevice(device));
+    CK(cudaDeviceGetAttribute(&ctx->num_sms, cudaDevAttrMultiProcessorCount, device));
+    *out = ctx;
+    return RPM_OK;
+}
+
+int rpm_ctx_destroy(rpm_ctx *ctx) {
+    if (!ctx) return RPM_OK;
+    cudaSetDevice(ctx->device);
+    cudaDeviceSynchronize();
+    for (auto &kv : ctx->scenes) {
+        for (auto &b : kv.second->bufs) {
+            for (cudaEvent_t e : b.users) cudaEventDestroy(e);
+            if (b.mem) cudaFree(b.mem);
+        }
+        delete kv.second;
+    }
+    for (auto &r : ctx->robots) cudaFree(r.dev);
+    for (auto &kv : ctx->scratch) {
+        cudaFree(kv.second->recheck);
+        cudaFree(kv.second->counters);
+        cudaFree(kv.second->status);
+        delete kv.second;
+    }
+    for (int i = 0; i < 2; ++i) {
+        if (ctx->hs[i]) cudaStreamDestroy(ctx->hs[i]);
+        cudaFree(ctx->hq[i]); cudaFree(ctx->hv[i]); cudaFree(ctx->hd[i]); cudaFree(ctx->hp[i]);
+    }
+    for (cudaEvent_t e : ctx->event_pool) cudaEventDestroy(e);
+    delete ctx;
+    return RPM_OK;
+}
+
+int rpm_ctx_set_params(rpm_ctx *ctx, const rpm_params *params) {
+    if (!ctx || !params) return fail(RPM_ERR_INVALID, "NULL argument");
+    if (!(params->max_distance > 0) || !(params->equality_threshold >= 0))
+        return fail(RPM_ERR_INVALID, "invalid RealVectorSpaceConfig constants");
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    ctx->params = *params;
+    return RPM_OK;
+}
+
+int rpm_robot_upload(rpm_ctx *ctx, const rpm_robot_desc *desc, int32_t *robot_id) {
+    if (!ctx || !desc || !robot_id) return fail(RPM_ERR_INVALID, "NULL argument");
+    DevRobot r;
+    int rc = build_dev_robot(*desc, r);
+    if (rc) return rc;
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    if (set_device(ctx)) return RPM_ERR_CUDA;
+    RobotRec rec;
+    rec.desc = *desc;
+    if (cudaMalloc(&rec.dev, sizeof(DevRobot)) != cudaSuccess) return fail(RPM_ERR_NOMEM, "robot allocation failed");
+    CK(cudaMemcpy(rec.dev, &r, sizeof r, cudaMemcpyHostToDevice));
+    ctx->robots.push_back(rec);
+    *robot_id = (int32_t)ctx->robots.size() - 1;
+    return RPM_OK;
+}
+
+int rpm_scene_create(rpm_ctx *ctx, int32_t robot_id, const float *aabb_host, const float *min_dist_tol_host,
+                     const uint8_t *flags_host, int32_t n, int32_t *scene_id) {
+    if (!ctx || !scene_id || (n > 0 && !aabb_host)) return fail(RPM_ERR_INVALID, "NULL argument");
+    if (n < 0) return fail(RPM_ERR_INVALID, "negative obstacle count");
+    if (n > kMaxObstacles) return fail(RPM_ERR_RANGE, "%d obstacles exceed the maximum of %d per scene", n, kMaxObstacles);
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    if (robot_id < 0 || robot_id >= (int)ctx->robots.size()) return fail(RPM_ERR_INVALID, "unknown robot %d", robot_id);
+    if (set_device(ctx)) return RPM_ERR_CUDA;
+    SceneRec *s = new SceneRec();
+    s->robot = robot_id;
+    s->n = n;
+    s->n_pad = std::max(16, (n + 15) / 16 * 16);
+    s->aabb.assign(aabb_host, aabb_host + 6 * (size_t)n);
+    s->tol.resize(n);
+    s->flags.resize(n);
+    for (int j = 0; j < n; ++j) {
+        s->tol[j] = min_dist_tol_host ? min_dist_tol_host[j] : (float)ctx->params.max_distance;
+        s->flags[j] = flags_host ? flags_host[j] : 0;
+    }
+    int rc = upload_scene(ctx, *s, s->bufs[0]);
+    if (rc) { delete s; return rc; }
+    s->cur = 0;
+    s->version = 1;
+    *scene_id = ctx->next_scene++;
+    ctx->scenes[*scene_id] = s;
+    return RPM_OK;
+}
+
+int rpm_scene_update(rpm_ctx *ctx, int32_t scene_id, const int32_t *idx_host, const float *aabb_host, int32_t m,
+                     uint64_t *version_out) {
+    if (!ctx || (m > 0 && (!idx_host || !aabb_host))) return fail(RPM_ERR_INVALID, "NULL argument");
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    SceneRec *s = find_scene(ctx, scene_id);
+    if (!s) return fail(RPM_ERR_INVALID, "unknown scene %d", scene_id);
+    for (int k = 0; k < m; ++k)
+        if (idx_host[k] < 0 || idx_host[k] >= s->n) return fail(RPM_ERR_INVALID, "obstacle index %d out of range", idx_host[k]);
+    if (set_device(ctx)) return RPM_ERR_CUDA;
+    for (int k = 0; k < m; ++k)
+        for (int c = 0; c < 6; ++c) s->aabb[6 * (size_t)idx_host[k] + c] = aabb_host[6 * (size_t)k + c];
+    const int nxt = (s->cur + 1) % kRing;
+    wait_users(ctx, s->bufs[nxt]);
+    int rc = upload_scene(ctx, *s, s->bufs[nxt]);
+    if (rc) return rc;
+    s->cur = nxt;
+    s->version++;
+    if (version_out) *version_out = s->version;
+    return RPM_OK;
+}
+
+int rpm_scene_destroy(rpm_ctx *ctx, int32_t scene_id) {
+    if (!ctx) return fail(RPM_ERR_INVALID, "NULL argument");
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    SceneRec *s = find_scene(ctx, scene_id);
+    if (!s) return fail(RPM_ERR_INVALID, "unknown scene %d", scene_id);
+    for (auto &b : s->bufs) {
+        wait_users(ctx, b);
+        if (b.mem) cudaFree(b.mem);
+    }
+    ctx->scenes.erase(scene_id);
+    delete s;
+    return RPM_OK;
+}
+
+int rpm_scene_info(rpm_ctx *ctx, int32_t scene_id, int32_t *robot_id, int32_t *num_obstacles, uint64_t *version) {
+    if (!ctx) return fail(RPM_ERR_INVALID, "NULL argument");
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    SceneRec *s = find_scene(ctx, scene_id);
+    if (!s) return fail(RPM_ERR_INVALID, "unknown scene %d", scene_id);
+    if (robot_id) *robot_id = s->robot;
+    if (num_obstacles) *num_obstacles = s->n;
+    if (version) *version = s->version;
+    return RPM_OK;
+}
+
+int rpm_box_aabb(const float dim[3], const float pos[3], const float quat_xyzw[4], float aabb_out[6]) {
+    if (!dim || !pos || !quat_xyzw || !aabb_out) return fail(RPM_ERR_INVALID, "NULL argument");
+    const float x = quat_xyzw[0], y = quat_xyzw[1], z = quat_xyzw[2], w = quat_xyzw[3];
+    const bool ident = x == 0.f && y == 0.f && z == 0.f && (w == 1.f || w == -1.f);
+    const float h[3] = {0.5f * dim[0], 0.5f * dim[1], 0.5f * dim[2]};
+    if (ident) {
+        for (int k = 0; k < 3; ++k) { aabb_out[k] = (-h[k]) + pos[k]; aabb_out[3 + k] = h[k] + pos[k]; }
+    } else {
+        const float rad = std::sqrt(h[0] * h[0] + (h[1] * h[1] + h[2] * h[2]));
+        for (int k = 0; k < 3; ++k) { aabb_out[k] = pos[k] - rad; aabb_out[3 + k] = pos[k] + rad; }
+    }
+    return RPM_OK;
+}
+
+int rpm_check_configs(rpm_ctx *ctx, int32_t scene_id, int32_t precision, const float *q_dev, int64_t num_configs,
+                      uint8_t *valid_dev, double *dist_dev, float *profile_dev, void *stream) {
+    if (!ctx) return fail(RPM_ERR_INVALID, "NULL context");
+    if (num_configs < 0) return fail(RPM_ERR_INVALID, "negative configuration count");
+    if (num_configs > 0 && !q_dev) return fail(RPM_ERR_INVALID, "q is NULL");
+    if (precision < RPM_PREC_FP64 || precision > RPM_PREC_FP32_REF) return fail(RPM_ERR_INVALID, "unknown precision %d", precision);
+    if (num_configs >= (int64_t)1 << 40) return fail(RPM_ERR_RANGE, "too many configurations in one call");
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    SceneRec *s = find_scene(ctx, scene_id);
+    if (!s) return fail(RPM_ERR_INVALID, "unknown scene %d", scene_id);
+    if (set_device(ctx)) return RPM_ERR_CUDA;
+    return enqueue_check(ctx, s, precision, q_dev, num_configs, valid_dev, dist_dev, profile_dev, (cudaStream_t)stream);
+}
+
+int rpm_check_configs_host(rpm_ctx *ctx, int32_t scene_id, int32_t precision, const float *q_host, int64_t num_configs,
+                           uint8_t *valid_host, double *dist_host, float *profile_host) {
+    if (!ctx) return fail(RPM_ERR_INVALID, "NULL context");
+    if (num_configs < 0 || (num_configs > 0 && !q_host)) return fail(RPM_ERR_INVALID, "bad configuration buffer");
+    if (precision < RPM_PREC_FP64 || precision > RPM_PREC_FP32_REF) return fail(RPM_ERR_INVALID, "unknown precision %d", precision);
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    SceneRec *s = find_scene(ctx, scene_id);
+    if (!s) return fail(RPM_ERR_INVALID, "unknown scene %d", scene_id);
+    if (set_device(ctx)) return RPM_ERR_CUDA;
+    const int D = ctx->robots[s->robot].desc.num_dofs;
+    const int64_t chunk = 1 << 18;
+    if (ctx->hcap_cfg < (size_t)chunk) {
+        for (int i = 0; i < 2; ++i) {
+            if (!ctx->hs[i]) CK(cudaStreamCreateWithFlags(&ctx->hs[i], cudaStreamNonBlocking));
+            cudaFree(ctx->hq[i]); cudaFree(ctx->hv[i]); cudaFree(ctx->hd[i]);
+            if (cudaMalloc(&ctx->hq[i], chunk * RPM_MAX_DOF * sizeof(float)) != cudaSuccess ||
+                cudaMalloc(&ctx->hv[i], chunk) != cudaSuccess || cudaMalloc(&ctx->hd[i], chunk * sizeof(double)) != cudaSuccess)
+                return fail(RPM_ERR_NOMEM, "staging allocation failed");
+        }
+        ctx->hcap_cfg = chunk;
+    }
+    if (profile_host && ctx->hcap_prof < (size_t)chunk) {
+        for (int i = 0; i < 2; ++i) {
+            cudaFree(ctx->hp[i]);
+            if (cudaMalloc(&ctx->hp[i], chunk * RPM_MAX_DOF * sizeof(float)) != cudaSuccess)
+                return fail(RPM_ERR_NOMEM, "staging allocation failed");
+        }
+        ctx->hcap_prof = chunk;
+    }
+    int k = 0;
+    for (int64_t off = 0; off < num_configs; off += chunk, ++k) {
+        const int i = k & 1;
+        cudaStream_t st = ctx->hs[i];
+        const int64_t n = std::min(chunk, num_configs - off);
+        CK(cudaMemcpyAsync(ctx->hq[i], q_host + off * D, n * D * sizeof(float), cudaMemcpyHostToDevice, st));
+        int rc = enqueue_check(ctx, s, precision, ctx->hq[i], n, valid_host ? ctx->hv[i] : nullptr,
+                               dist_host ? ctx->hd[i] : nullptr, profile_host ? ctx->hp[i] : nullptr, st);
+        if (rc) return rc;
+        if (valid_host) CK(cudaMemcpyAsync(valid_host + off, ctx->hv[i], n, cudaMemcpyDeviceToHost, st));
+        if (dist_host) CK(cudaMemcpyAsync(dist_host + off, ctx->hd[i], n * sizeof(double), cudaMemcpyDeviceToHost, st));
+        if (profile_host)
+            CK(cudaMemcpyAsync(profile_host + off * D, ctx->hp[i], n * D * sizeof(float), cudaMemcpyDeviceToHost, st));
+    }
+    for (int i = 0; i < 2; ++i)
+        if (ctx->hs[i]) CK(cudaStreamSynchronize(ctx->hs[i]));
+    for (int i = 0; i < 2; ++i) {
+        auto it = ctx->scratch.find(ctx->hs[i]);
+        if (it == ctx->scratch.end()) continue;
+        int32_t st = 0;
+        CK(cudaMemcpy(&st, it->second->status, sizeof st, cudaMemcpyDeviceToHost));
+        if (st) {
+            cudaMemset(it->second->status, 0, sizeof(int32_t));
+            return fail(RPM_ERR_TIMEOUT, "a bounded device-side wait gave up (status %d)", st);
+        }
+    }
+    return RPM_OK;
+}
+
+int rpm_skeleton(rpm_ctx *ctx, int32_t robot_id, int32_t precision, const float *q_dev, int64_t num_configs,
+                 double *points_dev, void *stream) {
+    if (!ctx || (num_configs > 0 && (!q_dev || !points_dev))) return fail(RPM_ERR_INVALID, "NULL argument");
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    if (robot_id < 0 || robot_id >= (int)ctx->robots.size()) return fail(RPM_ERR_INVALID, "unknown robot %d", robot_id);
+    if (set_device(ctx)) return RPM_ERR_CUDA;
+    const RobotRec &r = ctx->robots[robot_id];
+    if (precision < RPM_PREC_FP64 || precision > RPM_PREC_FP32_REF) return fail(RPM_ERR_INVALID, "unknown precision %d", precision);
+    CK(launch_skeleton(precision, r.dev, r.desc.num_dofs, q_dev, num_configs, points_dev, (cudaStream_t)stream));
+    return RPM_OK;
+}
+
+int rpm_last_stats(rpm_ctx *ctx, void *stream, rpm_check_stats *out) {
+    if (!ctx || !out) return fail(RPM_ERR_INVALID, "NULL argument");
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    if (set_device(ctx)) return RPM_ERR_CUDA;
+    cudaStream_t st = (cudaStream_t)stream;
+    std::memset(out, 0, sizeof *out);
+    auto it = ctx->scratch.find(st);
+    if (it == ctx->scratch.end()) return RPM_OK;
+    CK(cudaStreamSynchronize(st));
+    uint32_t cnt = 0;
+    int32_t status = 0;
+    CK(cudaMemcpy(&cnt, it->second->counters, sizeof cnt, cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(&status, it->second->status, sizeof status, cudaMemcpyDeviceToHost));
+    out->configs = it->second->last_configs;
+    out->rechecked = cnt;
+    out->overflow = 0;
+    out->device_status = status;
+    return RPM_OK;
+}
+
+int rpm_sync(rpm_ctx *ctx, void *stream) {
+    if (!ctx) return fail(RPM_ERR_INVALID, "NULL context");
+    cudaStream_t st = (cudaStream_t)stream;
+    {
+        std::lock_guard<std::mutex> lk(ctx->mu);
+        if (set_device(ctx)) return RPM_ERR_CUDA;
+    }
+    CK(cudaStreamSynchronize(st));
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    auto it = ctx->scratch.find(st);
+    if (it != ctx->scratch.end()) {
+        int32_t status = 0;
+        CK(cudaMemcpy(&status, it->second->status, sizeof status, cudaMemcpyDeviceToHost));
+        if (status) {
+            cudaMemset(it->second->status, 0, sizeof(int32_t));
+            return fail(RPM_ERR_TIMEOUT, "a bounded device-side wait gave up (status %d)", status);
+        }
+    }
+    return RPM_OK;
+}
+
+}  // extern "C"

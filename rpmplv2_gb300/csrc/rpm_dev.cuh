@@ -1,0 +1,392 @@
+// rpm_dev.cuh -- device data layout, FK and obstacle staging shared by the
+// kernels of the GB300 RealVectorSpace engine.
+//
+// Layout in HBM
+//   robot   : DevRobot (one struct per uploaded robot, ~6 KB)
+//   scene   : one allocation per obstacle-set version, n padded to n_pad
+//             (a multiple of 16) so every row starts 16-byte aligned:
+//               float  rows [8][n_pad] : xmin ymin zmin xmax ymax zmax tol ground(0/1)
+//               double rows [7][n_pad] : xmin ymin zmin xmax ymax zmax tol (exact widening)
+//   configs : float [C][D] row-major (one RealVectorSpaceState coordinate vector per row)
+// Each CTA copies its scene into shared memory with one bulk-async (TMA)
+// copy per row block and reads obstacles from there as warp-uniform broadcasts.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "../../include/rpm_gpu.h"
+
+#define RPM_HD __host__ __device__ __forceinline__
+
+namespace rpm {
+
+// Round-to-nearest multiply / add that are never contracted into an FMA.
+RPM_HD double dmul(double a, double b) {
+#ifdef __CUDA_ARCH__
+    return __dmul_rn(a, b);
+#else
+    return a * b;
+#endif
+}
+RPM_HD double dadd(double a, double b) {
+#ifdef __CUDA_ARCH__
+    return __dadd_rn(a, b);
+#else
+    return a + b;
+#endif
+}
+RPM_HD float fmul(float a, float b) {
+#ifdef __CUDA_ARCH__
+    return __fmul_rn(a, b);
+#else
+    return a * b;
+#endif
+}
+RPM_HD float fadd(float a, float b) {
+#ifdef __CUDA_ARCH__
+    return __fadd_rn(a, b);
+#else
+    return a + b;
+#endif
+}
+
+constexpr int kMaxDof = RPM_MAX_DOF;
+constexpr int kMaxObstacles = 2048;     // per scene, shared-memory resident
+constexpr int kFRows = 8;               // float rows per scene
+constexpr int kDRows = 7;               // double rows per scene
+constexpr int kRowTol = 6;
+constexpr int kRowGround = 7;
+// FP32 + FP64-recheck thresholds.  The FP32 skeleton differs from the FP64
+// one by at most ~2e-7 m on the reference's robots, so an FP32 branch decision
+// whose (error-amplification-scaled) margin is at least kDecide = 1e-5 m takes
+// the same branch in FP64.  Clearances within the contact band kBand = 1e-4 m
+// of zero (or of an obstacle's min_dist_tol) always go to FP64.
+constexpr float kDecide = 1e-5f;
+constexpr float kBand = 1e-4f;
+constexpr unsigned kWaitLimit = 1u << 22;   // bounded spin on an mbarrier
+
+// device status codes (written to the context's status word)
+constexpr int kStatusTimeout = 1;
+
+struct DevRobot {
+    int32_t kind, D, ground_included, rot_identity_mask;
+    int32_t axis[kMaxDof];
+    float radius_f[kMaxDof];
+    float rnew_f[kMaxDof];       // (float)((double)r * sqrt(3) / 3)  CollisionAndDistance.cpp:7
+    double radius_d[kMaxDof];
+    double rnew_d[kMaxDof];      // r * sqrt(3) / 3 in double
+    double gripper_d;            // (double)gripper_length
+    float gripper_f;
+    float grip03_f;              // (float)(0.3 * (double)gripper_length)   xArm6.cpp:231
+    double oxyz[kMaxDof + 1][3];
+    double orot[kMaxDof + 1][9];
+    float oxyz_f[kMaxDof + 1][3];
+    float orot_f[kMaxDof + 1][9];
+};
+// The robot is bulk-copied to shared memory ahead of 16-byte aligned rows.
+static_assert(sizeof(DevRobot) % 16 == 0, "DevRobot must be a multiple of 16 bytes");
+
+// One contiguous run of configurations checked against one scene.
+struct Seg {
+    const DevRobot *robot;
+    const float *obs_f;      // [8][n_pad]
+    const double *obs_d;     // [7][n_pad]
+    const float *q;          // [count][D]
+    uint8_t *valid;          // nullable
+    double *dist;            // nullable
+    float *profile;          // nullable, [count][L]
+    int64_t count;
+    int64_t first_block;     // first CTA of this segment in the launch
+    int32_t n, n_pad;
+};
+
+struct LaunchCtl {
+    const Seg *segs;
+    int32_t nseg;
+    int32_t pad;
+    uint64_t *recheck;       // FP32 pass: (seg << 40 | config) of configs to recompute in FP64
+    uint32_t *recheck_count;
+    uint32_t recheck_cap;
+    int32_t *status;
+};
+
+// ------------------------------------------------------------------ sincos --
+// Cody-Waite reduction by pi/2 (three-part split; P1, P2 carry 33 significant
+// bits) and Taylor series on [-pi/4, pi/4] through r^17 / r^18.  Every
+// operation is an IEEE-754 round-to-nearest add or multiply, so with
+// contraction disabled the result is bit-identical on any IEEE host.
+RPM_HD void taylor_sincos(double x, double *so, double *co) {
+    const double kTwoOverPi = 0x1.45f306dc9c883p-1;
+    const double kP1 = 0x1.921fb54400000p+0;
+    const double kP2 = 0x1.0b4611a600000p-34;
+    const double kP3 = 0x1.3198a2e037073p-69;
+    double kd = rint(dmul(x, kTwoOverPi));
+    double r = dadd(x, -dmul(kd, kP1));
+    r = dadd(r, -dmul(kd, kP2));
+    r = dadd(r, -dmul(kd, kP3));
+    double z = dmul(r, r);
+    double ps = 0x1.952c77030ad4ap-49;
+    ps = dadd(-0x1.ae7f3e733b81fp-41, dmul(z, ps));
+    ps = dadd(0x1.6124613a86d09p-33, dmul(z, ps));
+    ps = dadd(-0x1.ae64567f544e4p-26, dmul(z, ps));
+    ps = dadd(0x1.71de3a556c734p-19, dmul(z, ps));
+    ps = dadd(-0x1.a01a01a01a01ap-13, dmul(z, ps));
+    ps = dadd(0x1.1111111111111p-7, dmul(z, ps));
+    ps = dadd(-0x1.5555555555555p-3, dmul(z, ps));
+    double s = dadd(r, dmul(dmul(r, z), ps));
+    double pc = -0x1.6827863b97d97p-53;
+    pc = dadd(0x1.ae7f3e733b81fp-45, dmul(z, pc));
+    pc = dadd(-0x1.93974a8c07c9dp-37, dmul(z, pc));
+    pc = dadd(0x1.1eed8eff8d898p-29, dmul(z, pc));
+    pc = dadd(-0x1.27e4fb7789f5cp-22, dmul(z, pc));
+    pc = dadd(0x1.a01a01a01a01ap-16, dmul(z, pc));
+    pc = dadd(-0x1.6c16c16c16c17p-10, dmul(z, pc));
+    pc = dadd(0x1.5555555555555p-5, dmul(z, pc));
+    pc = dadd(-0x1.0000000000000p-1, dmul(z, pc));
+    double c = dadd(1.0, dmul(z, pc));
+    long long k = (long long)kd;
+    switch (k & 3) {
+        case 0: *so = s; *co = c; break;
+        case 1: *so = c; *co = -s; break;
+        case 2: *so = -s; *co = -c; break;
+        default: *so = -c; *co = s; break;
+    }
+}
+
+// --------------------------------------------------------------------- FK --
+// F <- F * origin_k * Rot(axis_k, q_k) (KDL's root-to-tip composition).
+template <typename F> struct Fk {
+    F R[9];
+    F p[3];
+    RPM_HD void init() {
+#pragma unroll
+        for (int i = 0; i < 9; ++i) R[i] = (i % 4 == 0) ? F(1) : F(0);
+        p[0] = p[1] = p[2] = F(0);
+    }
+};
+
+RPM_HD void fk_step_d(Fk<double> &f, const DevRobot &rb, int k, double q) {
+    const double *o = rb.oxyz[k];
+    double np[3];
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+        np[i] = dadd(dadd(dadd(dmul(f.R[3 * i + 0], o[0]), dmul(f.R[3 * i + 1], o[1])),
+                                    dmul(f.R[3 * i + 2], o[2])),
+                          f.p[i]);
+#pragma unroll
+    for (int i = 0; i < 3; ++i) f.p[i] = np[i];
+    if (!((rb.rot_identity_mask >> k) & 1)) {
+        const double *M = rb.orot[k];
+        double nR[9];
+#pragma unroll
+        for (int i = 0; i < 3; ++i)
+#pragma unroll
+            for (int j = 0; j < 3; ++j)
+                nR[3 * i + j] = dadd(dadd(dmul(f.R[3 * i + 0], M[j]), dmul(f.R[3 * i + 1], M[3 + j])),
+                                          dmul(f.R[3 * i + 2], M[6 + j]));
+#pragma unroll
+        for (int i = 0; i < 9; ++i) f.R[i] = nR[i];
+    }
+    double s, c;
+    taylor_sincos(q, &s, &c);
+    const int ax = rb.axis[k];
+    const int ia = (ax == 0) ? 1 : (ax == 1 ? 2 : 0);
+    const int ib = (ax == 0) ? 2 : (ax == 1 ? 0 : 1);
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+        double a = f.R[3 * i + ia], b = f.R[3 * i + ib];
+        f.R[3 * i + ia] = dadd(dmul(a, c), dmul(b, s));
+        f.R[3 * i + ib] = dadd(dmul(b, c), -dmul(a, s));
+    }
+}
+
+RPM_HD void fk_step_f(Fk<float> &f, const DevRobot &rb, int k, float q) {
+    const float *o = rb.oxyz_f[k];
+    float np[3];
+#pragma unroll
+    for (int i = 0; i < 3; ++i) np[i] = f.R[3 * i + 0] * o[0] + f.R[3 * i + 1] * o[1] + f.R[3 * i + 2] * o[2] + f.p[i];
+#pragma unroll
+    for (int i = 0; i < 3; ++i) f.p[i] = np[i];
+    if (!((rb.rot_identity_mask >> k) & 1)) {
+        const float *M = rb.orot_f[k];
+        float nR[9];
+#pragma unroll
+        for (int i = 0; i < 3; ++i)
+#pragma unroll
+            for (int j = 0; j < 3; ++j) nR[3 * i + j] = f.R[3 * i + 0] * M[j] + f.R[3 * i + 1] * M[3 + j] + f.R[3 * i + 2] * M[6 + j];
+#pragma unroll
+        for (int i = 0; i < 9; ++i) f.R[i] = nR[i];
+    }
+    float s, c;
+    sincosf(q, &s, &c);
+    const int ax = rb.axis[k];
+    const int ia = (ax == 0) ? 1 : (ax == 1 ? 2 : 0);
+    const int ib = (ax == 0) ? 2 : (ax == 1 ? 0 : 1);
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+        float a = f.R[3 * i + ia], b = f.R[3 * i + ib];
+        f.R[3 * i + ia] = a * c + b * s;
+        f.R[3 * i + ib] = b * c - a * s;
+    }
+}
+
+// Walks the skeleton points 0..L of one configuration in order, advancing the
+// FK only as far as the next point needs (so an early exit also skips FK).
+//   CHAIN : point k = origin of chain segment k; point D = tool
+//           (Planar2DOF.cpp:125-126)
+//   XARM6 : 0, F1.p, F2.p, F3.p - 0.25 z3, F4.p, F4.p + 0.076 x4,
+//           F5.p + g z5 - 0.3 g z5   (xArm6.cpp:130, 215-231)
+// MODE 0: FP64 points.  MODE 1: the reference's float skeleton (FP64 FK,
+// rounded, line (*) of xArm6.cpp:231 in float).  MODE 2: FP32 FK.
+template <int MODE> struct SkelWalker;
+
+template <> struct SkelWalker<0> {
+    Fk<double> f;
+    RPM_HD void begin() { f.init(); }
+    RPM_HD void point(const DevRobot &rb, const float *q, int k, double *out) {
+        if (rb.kind == RPM_ROBOT_CHAIN) {
+            if (k < rb.D) {
+                fk_step_d(f, rb, k, (double)q[k]);
+                out[0] = f.p[0]; out[1] = f.p[1]; out[2] = f.p[2];
+            } else {
+                const double *o = rb.oxyz[rb.D];
+#pragma unroll
+                for (int i = 0; i < 3; ++i)
+                    out[i] = dadd(dadd(dadd(dmul(f.R[3 * i], o[0]), dmul(f.R[3 * i + 1], o[1])),
+                                                 dmul(f.R[3 * i + 2], o[2])),
+                                       f.p[i]);
+            }
+            return;
+        }
+        switch (k) {
+            case 0: out[0] = out[1] = out[2] = 0.0; break;
+            case 1: fk_step_d(f, rb, 0, (double)q[0]); fk_step_d(f, rb, 1, (double)q[1]);
+                    out[0] = f.p[0]; out[1] = f.p[1]; out[2] = f.p[2]; break;
+            case 2: fk_step_d(f, rb, 2, (double)q[2]); out[0] = f.p[0]; out[1] = f.p[1]; out[2] = f.p[2]; break;
+            case 3: fk_step_d(f, rb, 3, (double)q[3]);
+#pragma unroll
+                    for (int i = 0; i < 3; ++i) out[i] = dadd(f.p[i], -dmul(f.R[3 * i + 2], 0.25));
+                    break;
+            case 4: fk_step_d(f, rb, 4, (double)q[4]); out[0] = f.p[0]; out[1] = f.p[1]; out[2] = f.p[2]; break;
+            case 5:
+#pragma unroll
+                    for (int i = 0; i < 3; ++i) out[i] = dadd(f.p[i], dmul(f.R[3 * i + 0], 0.076));
+                    break;
+            default: {
+                fk_step_d(f, rb, 5, (double)q[5]);
+                const double g = rb.gripper_d, g3 = dmul(0.3, rb.gripper_d);
+#pragma unroll
+                for (int i = 0; i < 3; ++i) {
+                    double z = f.R[3 * i + 2];
+                    double ps = dadd(f.p[i], dmul(g, z));
+                    out[i] = dadd(ps, -dmul(g3, z));
+                }
+            }
+        }
+    }
+};
+
+template <> struct SkelWalker<1> {
+    SkelWalker<0> w;
+    RPM_HD void begin() { w.begin(); }
+    RPM_HD void point(const DevRobot &rb, const float *q, int k, float *out) {
+        if (rb.kind == RPM_ROBOT_XARM6 && k == 6) {
+            fk_step_d(w.f, rb, 5, (double)q[5]);
+            const double g = rb.gripper_d;
+#pragma unroll
+            for (int i = 0; i < 3; ++i) {
+                double z = w.f.R[3 * i + 2];
+                float ps = (float)dadd(w.f.p[i], dmul(g, z));
+                out[i] = fadd(ps, -fmul(rb.grip03_f, (float)z));
+            }
+            return;
+        }
+        double d[3];
+        w.point(rb, q, k, d);
+        out[0] = (float)d[0]; out[1] = (float)d[1]; out[2] = (float)d[2];
+    }
+};
+
+template <> struct SkelWalker<2> {
+    Fk<float> f;
+    RPM_HD void begin() { f.init(); }
+    RPM_HD void point(const DevRobot &rb, const float *q, int k, float *out) {
+        if (rb.kind == RPM_ROBOT_CHAIN) {
+            if (k < rb.D) {
+                fk_step_f(f, rb, k, q[k]);
+                out[0] = f.p[0]; out[1] = f.p[1]; out[2] = f.p[2];
+            } else {
+                const float *o = rb.oxyz_f[rb.D];
+#pragma unroll
+                for (int i = 0; i < 3; ++i) out[i] = f.R[3 * i] * o[0] + f.R[3 * i + 1] * o[1] + f.R[3 * i + 2] * o[2] + f.p[i];
+            }
+            return;
+        }
+        switch (k) {
+            case 0: out[0] = out[1] = out[2] = 0.f; break;
+            case 1: fk_step_f(f, rb, 0, q[0]); fk_step_f(f, rb, 1, q[1]);
+                    out[0] = f.p[0]; out[1] = f.p[1]; out[2] = f.p[2]; break;
+            case 2: fk_step_f(f, rb, 2, q[2]); out[0] = f.p[0]; out[1] = f.p[1]; out[2] = f.p[2]; break;
+            case 3: fk_step_f(f, rb, 3, q[3]);
+#pragma unroll
+                    for (int i = 0; i < 3; ++i) out[i] = f.p[i] - f.R[3 * i + 2] * 0.25f;
+                    break;
+            case 4: fk_step_f(f, rb, 4, q[4]); out[0] = f.p[0]; out[1] = f.p[1]; out[2] = f.p[2]; break;
+            case 5:
+#pragma unroll
+                    for (int i = 0; i < 3; ++i) out[i] = f.p[i] + f.R[3 * i + 0] * 0.076f;
+                    break;
+            default: {
+                fk_step_f(f, rb, 5, q[5]);
+                const float g7 = 0.7f * rb.gripper_f;
+#pragma unroll
+                for (int i = 0; i < 3; ++i) out[i] = f.p[i] + g7 * f.R[3 * i + 2];
+            }
+        }
+    }
+};
+
+// --------------------------------------------------- shared-memory staging --
+__device__ __forceinline__ uint32_t smem_addr(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+// Bulk-async (TMA) copies global -> shared completed on an mbarrier.  Sizes
+// are multiples of 16 bytes and both addresses 16-byte aligned.  Thread 0
+// arms the barrier with the total byte count and issues the copies; every
+// thread then waits with a bounded spin, which on expiry records
+// kStatusTimeout and returns false instead of hanging.
+__device__ __forceinline__ void bulk_init(uint64_t *bar) {
+    if (threadIdx.x == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(1));
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+}
+
+__device__ __forceinline__ void bulk_expect(uint64_t *bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes) : "memory");
+}
+
+__device__ __forceinline__ void bulk_copy(uint64_t *bar, void *dst, const void *src, uint32_t bytes) {
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                     smem_addr(dst)),
+                 "l"(src), "r"(bytes), "r"(smem_addr(bar))
+                 : "memory");
+}
+
+__device__ __forceinline__ bool bulk_wait(uint64_t *bar, uint32_t parity, int32_t *status) {
+    uint32_t done = 0;
+    for (unsigned it = 0; it < kWaitLimit; ++it) {
+        asm volatile(
+            "{\n\t.reg .pred p;\n\t"
+            "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+            "selp.u32 %0, 1, 0, p;\n\t}"
+            : "=r"(done)
+            : "r"(smem_addr(bar)), "r"(parity)
+            : "memory");
+        if (done) return true;
+    }
+    if (status) atomicCAS(status, 0, kStatusTimeout);
+    return false;
+}
+
+}  // namespace rpm

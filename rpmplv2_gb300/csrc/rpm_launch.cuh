@@ -1,0 +1,33 @@
+// rpm_launch.cuh -- kernel parameter block and host-side launchers.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "rpm_dev.cuh"
+#include "rpm_tree.cuh"
+
+namespace rpm {
+
+constexpr int kThreads = 128;     // configurations per CTA
+constexpr int kMaxSegs = 32;      // segments per launch (passed by value)
+
+struct KParams {
+    Seg segs[kMaxSegs];
+    int32_t nseg;
+    int32_t pad;
+    Num<double> nmd;
+    Num<float> nmf;
+    uint64_t *recheck;          // FP32 pass -> FP64 recheck list: (segment << 40) | config
+    uint32_t *recheck_count;
+    int32_t *status;
+};
+
+// Dynamic shared memory of one CTA: robot + obstacle rows of its scene.
+size_t smem_bytes(int mode, int n_pad);
+
+cudaError_t launch_check_exact(int mode, const KParams &p, int64_t blocks, size_t smem, cudaStream_t st);
+cudaError_t launch_check_fp32(const KParams &p, int64_t blocks, size_t smem, cudaStream_t st);
+cudaError_t launch_recheck(const KParams &p, int grid, cudaStream_t st);
+cudaError_t launch_skeleton(int mode, const DevRobot *rb, int D, const float *q, int64_t C, double *out, cudaStream_t st);
+
+}  // namespace rpm

@@ -1,0 +1,178 @@
+"""ctypes binding of librpm_gb300.so (include/rpm_gpu.h).
+
+There is no CPU fallback: constructing an Engine without the CUDA library or
+without a GPU raises.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+from . import _abi
+from ._abi import CheckStats, Params, PRECISIONS
+
+_LIB = None
+
+_vp = ctypes.c_void_p
+_i32 = ctypes.c_int32
+_i64 = ctypes.c_int64
+_pi32 = ctypes.POINTER(ctypes.c_int32)
+
+
+class RpmError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__("rpm error %d: %s" % (code, msg))
+        self.code = code
+
+
+def lib_path():
+    from . import build as _b
+    return _b.LIB
+
+
+def load(build_if_missing=False):
+    """Load the CUDA library (building it first if asked)."""
+    global _LIB
+    if _LIB is not None:
+        return _LIB
+    path = lib_path()
+    if not os.path.exists(path):
+        if not build_if_missing:
+            raise RuntimeError("librpm_gb300.so is not built; run __graft_entry__.build() (no CPU fallback)")
+        from . import build as _b
+        _b.build()
+    L = ctypes.CDLL(path)
+    L.rpm_last_error_string.restype = ctypes.c_char_p
+    L.rpm_ctx_create.argtypes = [ctypes.c_int, ctypes.POINTER(_vp)]
+    L.rpm_ctx_destroy.argtypes = [_vp]
+    L.rpm_ctx_set_params.argtypes = [_vp, ctypes.POINTER(Params)]
+    L.rpm_robot_upload.argtypes = [_vp, ctypes.c_void_p, _pi32]
+    L.rpm_scene_create.argtypes = [_vp, _i32, _vp, _vp, _vp, _i32, _pi32]
+    L.rpm_scene_update.argtypes = [_vp, _i32, _vp, _vp, _i32, ctypes.POINTER(ctypes.c_uint64)]
+    L.rpm_scene_destroy.argtypes = [_vp, _i32]
+    L.rpm_scene_info.argtypes = [_vp, _i32, _pi32, _pi32, ctypes.POINTER(ctypes.c_uint64)]
+    L.rpm_box_aabb.argtypes = [_vp, _vp, _vp, _vp]
+    L.rpm_check_configs.argtypes = [_vp, _i32, _i32, _vp, _i64, _vp, _vp, _vp, _vp]
+    L.rpm_check_configs_host.argtypes = [_vp, _i32, _i32, _vp, _i64, _vp, _vp, _vp]
+    L.rpm_skeleton.argtypes = [_vp, _i32, _i32, _vp, _i64, _vp, _vp]
+    L.rpm_last_stats.argtypes = [_vp, _vp, ctypes.POINTER(CheckStats)]
+    L.rpm_sync.argtypes = [_vp, _vp]
+    _LIB = L
+    return L
+
+
+def _check(rc):
+    if rc != 0:
+        raise RpmError(rc, _LIB.rpm_last_error_string().decode())
+
+
+def _ptr(x):
+    """Device pointer of a torch tensor, host pointer of a numpy array, or None."""
+    if x is None:
+        return None
+    if isinstance(x, np.ndarray):
+        return x.ctypes.data
+    return x.data_ptr()
+
+
+class Engine:
+    """A device context: robots and scenes resident in HBM."""
+
+    def __init__(self, device=0, equality_threshold=1e-4, max_distance=1000.0):
+        self.lib = load()
+        self.ctx = _vp()
+        _check(self.lib.rpm_ctx_create(int(device), ctypes.byref(self.ctx)))
+        self.device = device
+        self.set_params(equality_threshold, max_distance)
+        self._robots = {}
+        self._scene_robot = {}
+
+    def close(self):
+        if self.ctx:
+            self.lib.rpm_ctx_destroy(self.ctx)
+            self.ctx = _vp()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_params(self, equality_threshold=1e-4, max_distance=1000.0):
+        p = Params(equality_threshold, max_distance)
+        _check(self.lib.rpm_ctx_set_params(self.ctx, ctypes.byref(p)))
+
+    def upload_robot(self, robot):
+        rid = _i32()
+        _check(self.lib.rpm_robot_upload(self.ctx, ctypes.addressof(robot.desc), ctypes.byref(rid)))
+        self._robots[rid.value] = robot
+        return rid.value
+
+    def create_scene(self, robot_id, scene):
+        sid = _i32()
+        _check(self.lib.rpm_scene_create(self.ctx, robot_id, scene.aabb.ctypes.data, scene.tol.ctypes.data,
+                                         scene.flags.ctypes.data, scene.n, ctypes.byref(sid)))
+        self._scene_robot[sid.value] = robot_id
+        return sid.value
+
+    def update_scene(self, scene_id, idx, aabb):
+        idx = np.ascontiguousarray(idx, np.int32)
+        aabb = np.ascontiguousarray(aabb, np.float32).reshape(-1, 6)
+        ver = ctypes.c_uint64()
+        _check(self.lib.rpm_scene_update(self.ctx, scene_id, idx.ctypes.data, aabb.ctypes.data, idx.size,
+                                         ctypes.byref(ver)))
+        return ver.value
+
+    def destroy_scene(self, scene_id):
+        _check(self.lib.rpm_scene_destroy(self.ctx, scene_id))
+
+    def robot_of(self, scene_id):
+        return self._robots[self._scene_robot[scene_id]]
+
+    # ---- device-buffer calls (torch CUDA tensors) ----
+    def check_configs(self, scene_id, q, precision="fp64", valid=None, dist=None, profile=None, stream=None):
+        prec = PRECISIONS[precision] if isinstance(precision, str) else int(precision)
+        n = int(q.shape[0])
+        _check(self.lib.rpm_check_configs(self.ctx, scene_id, prec, _ptr(q), n, _ptr(valid), _ptr(dist),
+                                          _ptr(profile), stream))
+
+    def skeleton(self, robot_id, q, points, precision="fp64", stream=None):
+        prec = PRECISIONS[precision] if isinstance(precision, str) else int(precision)
+        _check(self.lib.rpm_skeleton(self.ctx, robot_id, prec, _ptr(q), int(q.shape[0]), _ptr(points), stream))
+
+    def stats(self, stream=None):
+        s = CheckStats()
+        _check(self.lib.rpm_last_stats(self.ctx, stream, ctypes.byref(s)))
+        return {"configs": s.configs, "rechecked": s.rechecked, "overflow": s.overflow,
+                "device_status": s.device_status}
+
+    def sync(self, stream=None):
+        _check(self.lib.rpm_sync(self.ctx, stream))
+
+    # ---- host-buffer call (numpy) ----
+    def check_configs_host(self, scene_id, q, precision="fp64", want=("valid", "dist")):
+        prec = PRECISIONS[precision] if isinstance(precision, str) else int(precision)
+        q = np.ascontiguousarray(q, np.float32)
+        C = q.shape[0]
+        L = self.robot_of(scene_id).num_links
+        valid = np.zeros(C, np.uint8) if "valid" in want else None
+        dist = np.zeros(C, np.float64) if "dist" in want else None
+        prof = np.zeros((C, L), np.float32) if "profile" in want else None
+        _check(self.lib.rpm_check_configs_host(self.ctx, scene_id, prec, q.ctypes.data, C, _ptr(valid), _ptr(dist),
+                                               _ptr(prof)))
+        return valid, dist, prof
+
+
+def box_aabb(dim, pos, quat_xyzw=(0.0, 0.0, 0.0, 1.0)):
+    L = load()
+    dim, pos, quat = (np.ascontiguousarray(v, np.float32) for v in (dim, pos, quat_xyzw))
+    out = np.zeros(6, np.float32)
+    _check(L.rpm_box_aabb(dim.ctypes.data, pos.ctypes.data, quat.ctypes.data, out.ctypes.data))
+    return out
+
+
+ABI_SYMBOLS = [
+    "rpm_last_error_string", "rpm_version", "rpm_ctx_create", "rpm_ctx_destroy", "rpm_ctx_set_params",
+    "rpm_robot_upload", "rpm_scene_create", "rpm_scene_update", "rpm_scene_destroy", "rpm_scene_info",
+    "rpm_box_aabb", "rpm_check_configs", "rpm_check_configs_host", "rpm_skeleton", "rpm_last_stats", "rpm_sync",
+]

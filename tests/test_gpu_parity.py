@@ -1,0 +1,83 @@
+"""GPU parity: the CUDA forms against the oracle on the same seeded inputs.
+
+Bars (per form):
+  fp64          isValid bit-equal to ref64; distance within 1e-9 m of ref64
+                (and, with the shared-bits sincos and no contraction, bit-equal)
+  fp32_ref      bit-equal to ref32 (the reference's own numerics)
+  fp32_recheck  isValid bit-equal to ref64 (0 flips); distance within 1e-5 m
+"""
+import numpy as np
+import pytest
+import torch
+
+from oracle import oracle as O
+from rpmplv2_gb300 import scenes
+
+pytestmark = pytest.mark.gpu
+
+DIST_TOL = {"fp64": 1e-9, "fp32_ref": 0.0, "fp32_recheck": 1e-5}
+ORACLE_OF = {"fp64": "ref64", "fp32_ref": "ref32", "fp32_recheck": "ref64"}
+
+
+def run_gpu(engine, robot, scene, q, prec, profile=True):
+    rid = engine.upload_robot(robot)
+    sid = engine.create_scene(rid, scene)
+    qd = torch.from_numpy(q).cuda()
+    C, L = q.shape[0], robot.num_links
+    valid = torch.zeros(C, dtype=torch.uint8, device="cuda")
+    dist = torch.zeros(C, dtype=torch.float64, device="cuda")
+    prof = torch.zeros((C, L), dtype=torch.float32, device="cuda") if profile else None
+    engine.check_configs(sid, qd, prec, valid, dist, prof)
+    engine.sync()
+    st = engine.stats()
+    engine.destroy_scene(sid)
+    return valid.cpu().numpy(), dist.cpu().numpy(), (prof.cpu().numpy() if profile else None), st
+
+
+def compare(engine, robot, scene, q, prec):
+    v, d, p, st = run_gpu(engine, robot, scene, q, prec)
+    rv, rd, rp = O.check_configs(robot, scene, q, prec=ORACLE_OF[prec])
+    flips = int((v != rv).sum())
+    derr = float(np.abs(d - rd).max())
+    assert flips == 0, "%s: %d isValid mismatches" % (prec, flips)
+    assert derr <= DIST_TOL[prec], "%s: max distance error %g" % (prec, derr)
+    if prec != "fp32_recheck":
+        perr = float(np.abs(p.astype(np.float64) - rp).max())
+        assert perr <= max(DIST_TOL[prec], 0.0) + (0 if prec == "fp32_ref" else 1e-7), "%s profile err %g" % (prec, perr)
+    else:
+        perr = float(np.abs(p.astype(np.float64) - rp).max())
+        assert perr <= 2e-5, "profile err %g" % perr
+    return st, derr
+
+
+@pytest.mark.parametrize("prec", ["fp64", "fp32_ref", "fp32_recheck"])
+def test_planar_2dof(engine, prec):
+    robot, scene, q = scenes.planar_2dof_workload(65536, seed=0)
+    compare(engine, robot, scene, q, prec)
+
+
+@pytest.mark.parametrize("prec", ["fp64", "fp32_ref", "fp32_recheck"])
+def test_xarm6(engine, prec):
+    robot, scene, q = scenes.xarm6_workload(65536, seed=1)
+    st, derr = compare(engine, robot, scene, q, prec)
+    if prec == "fp32_recheck":
+        assert st["rechecked"] < 0.5 * q.shape[0]
+
+
+def test_fp64_bits(engine):
+    robot, scene, q = scenes.xarm6_workload(16384, seed=5)
+    v, d, p, _ = run_gpu(engine, robot, scene, q, "fp64")
+    rv, rd, rp = O.check_configs(robot, scene, q, prec="ref64")
+    assert np.array_equal(v, rv)
+    assert np.array_equal(d.view(np.uint64), rd.view(np.uint64))
+
+
+def test_skeleton_fp64_bits(engine):
+    robot, scene, q = scenes.xarm6_workload(4096, seed=7)
+    rid = engine.upload_robot(robot)
+    qd = torch.from_numpy(q).cuda()
+    out = torch.zeros((q.shape[0], robot.num_links + 1, 3), dtype=torch.float64, device="cuda")
+    engine.skeleton(rid, qd, out, "fp64")
+    engine.sync()
+    ref = O.skeleton(robot, q, prec="ref64")
+    assert np.array_equal(out.cpu().numpy().view(np.uint64), ref.view(np.uint64))
