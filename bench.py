@@ -1,0 +1,305 @@
+#!/usr/bin/env python
+"""Benchmark of the RealVectorSpace collision + distance path on GB300.
+
+Headline workload (one "step" = one pass over the batch): xarm6 capsule model
+(radius 0.05 m, gripper 0.1 m, ground from link 2) against 50 cubes of 0.05 m
+plus the ground box, 1,048,576 configurations uniform in [-pi, pi]^6; outputs
+per configuration are isValid and computeDistance.
+
+  value    configs/s of the FP32 + FP64-recheck form, inputs resident in HBM
+  e2e      the same through rpm_check_configs_host with pinned host buffers
+           (host->device copy of q and device->host copy of both outputs timed)
+  fp64     configs/s of the plain FP64 form on the same batch, with the number
+           of isValid flips and the max distance difference between the forms
+
+python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+"""
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "xarm6 configs/s FP32+recheck vs FP64 GPU (0 flips); p50/p99 serve latency"
+NUM_CONFIGS = 1 << 20
+D = 6
+PAIRS = 6 * 50 + 4                       # link x obstacle pairs not skipped by the ground rule
+FLOP_PER_CONFIG = 60 * D + 100 * PAIRS   # fixed work convention: 30,760 FLOP per configuration
+BYTES_PER_CONFIG = 4 * D + 1 + 8         # q in, isValid + distance out
+WORKLOAD = ("xarm6 capsules (r 0.05 m, gripper 0.1 m, ground from link 2) vs 50 cubes of 0.05 m + ground, "
+            "1,048,576 configs in [-pi, pi]^6; isValid + computeDistance")
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--configs", type=int, default=NUM_CONFIGS)
+    return ap.parse_args()
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.path = os.path.join(ROOT, "gpurun_out", "clocks_bench.csv")
+
+    def __enter__(self):
+        try:
+            os.makedirs(os.path.dirname(self.path), exist_ok=True)
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.FIELDS,
+                                          "--format=csv,noheader,nounits", "-lms", "100"], stdout=self.f,
+                                         stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+            self.f.close()
+
+    def summary(self):
+        if self.proc is None or not os.path.exists(self.path):
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        sm, smax, reasons = [], [], set()
+        names = ["active", "hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            p = [x.strip() for x in line.split(",")]
+            if len(p) < 9:
+                continue
+            try:
+                sm.append(float(p[1]))
+                smax.append(float(p[2]))
+            except ValueError:
+                continue
+            for name, v in zip(names[1:], p[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def cpu_baseline(robot, scene, q, sample):
+    """The oracle (a restatement of the reference's FP32 path) on every host core."""
+    from oracle import oracle as O
+    cores = os.cpu_count() or 1
+    qs = np.ascontiguousarray(q[:sample])
+    O.check_configs(robot, scene, qs[:4096], prec="ref32", nthreads=cores)   # warm-up
+    t0 = time.perf_counter()
+    O.check_configs(robot, scene, qs, prec="ref32", nthreads=cores)
+    dt = time.perf_counter() - t0
+    return {"value": sample / dt, "unit": "configs/s", "cores": cores, "kind": "port",
+            "sample": "%d configs of the same workload, isValid + computeDistance, ref32 oracle, OpenMP" % sample}
+
+
+def traffic_per_launch():
+    path = os.path.join(ROOT, "profiles", "k_check_fp32_xarm6.json")
+    if not os.path.exists(path):
+        return None
+    try:
+        with open(path) as f:
+            return json.load(f).get("dram_bytes_per_launch_full")
+    except Exception:
+        return None
+
+
+def run_reference(args, ws, rank):
+    if rank != 0:
+        return
+    from rpmplv2_gb300 import scenes
+    robot, scene, q = scenes.xarm6_workload(args.configs, seed=1)
+    from oracle import oracle as O
+    cores = os.cpu_count() or 1
+    sample = min(args.configs, 1 << 18)
+    for w in range(args.warmup):
+        O.check_configs(robot, scene, q[:4096], prec="ref32", nthreads=cores)
+    times = []
+    for k in range(args.steps):
+        qs = np.ascontiguousarray(q[(k * sample) % args.configs:][:sample])
+        t0 = time.perf_counter()
+        O.check_configs(robot, scene, qs, prec="ref32", nthreads=cores)
+        times.append(time.perf_counter() - t0)
+    value = sample * len(times) / sum(times)
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "configs/s", "n_gpus": ws,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * sum(times) / len(times),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "sample_per_step": sample,
+                       "implementation": "CPU restatement of the reference's RealVectorSpace path (ref32)"},
+            "cpu_baseline": {"value": value, "unit": "configs/s", "cores": cores, "kind": "port",
+                             "sample": "%d configs per step, isValid + computeDistance" % sample},
+            "e2e": {"value": value, "unit": "configs/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args, ws, rank, local):
+    import torch
+    from rpmplv2_gb300 import scenes
+    from rpmplv2_gb300.engine import Engine
+
+    torch.cuda.set_device(local)
+    dist = None
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    C = args.configs
+    robot, scene, q = scenes.xarm6_workload(C, seed=1 + rank)
+    eng = Engine(local)
+    rid = eng.upload_robot(robot)
+    sid = eng.create_scene(rid, scene)
+    qd = torch.from_numpy(q).cuda()
+    valid = torch.zeros(C, dtype=torch.uint8, device="cuda")
+    distv = torch.zeros(C, dtype=torch.float64, device="cuda")
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")   # > 129 MB L2
+
+    def timed(prec, steps, warmup):
+        for _ in range(warmup):
+            eng.check_configs(sid, qd, prec, valid, distv)
+        eng.set_timing(True)
+        barrier()
+        step_ms, bulk_ms, re_ms, rechecked = [], [], [], []
+        for _ in range(steps):
+            flush.zero_()
+            a = torch.cuda.Event(enable_timing=True)
+            b = torch.cuda.Event(enable_timing=True)
+            a.record()
+            eng.check_configs(sid, qd, prec, valid, distv)
+            b.record()
+            b.synchronize()
+            step_ms.append(a.elapsed_time(b))
+            bm, rm = eng.last_timing()
+            bulk_ms.append(bm)
+            re_ms.append(rm)
+            rechecked.append(eng.stats()["rechecked"])
+        barrier()
+        eng.set_timing(False)
+        return step_ms, bulk_ms, re_ms, rechecked
+
+    # ---- headline: FP32 + FP64 recheck, inputs resident in HBM
+    peak_fp32 = eng.fp32_peak_tflops()
+    with ClockSampler(local) as clk:
+        step_ms, bulk_ms, re_ms, rechecked = timed("fp32_recheck", args.steps, args.warmup)
+    clocks = clk.summary()
+    v32, d32 = valid.clone(), distv.clone()
+    # ---- the plain FP64 form on the same batch
+    step64, bulk64, _, _ = timed("fp64", max(2, min(args.steps, 3)), 1)
+    v64, d64 = valid.clone(), distv.clone()
+    flips = int((v32 != v64).sum().item())
+    max_derr = float((d32 - d64).abs().max().item())
+
+    t_local = sum(step_ms) / 1e3
+    if dist is not None:
+        t = torch.tensor([t_local], dtype=torch.float64, device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        t_local = float(t.item())
+    value = ws * C * args.steps / t_local
+    fp64_value = C / (statistics.median(step64) / 1e3)
+
+    # ---- end to end through the host-buffer C ABI call, pinned host memory
+    qh = torch.from_numpy(q).pin_memory().numpy()
+    vh = torch.zeros(C, dtype=torch.uint8).pin_memory().numpy()
+    dh = torch.zeros(C, dtype=torch.float64).pin_memory().numpy()
+    import ctypes
+    lib = eng.lib
+    for _ in range(2):
+        lib.rpm_check_configs_host(eng.ctx, sid, 1, qh.ctypes.data, C, vh.ctypes.data, dh.ctypes.data, None)
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        rc = lib.rpm_check_configs_host(eng.ctx, sid, 1, qh.ctypes.data, C, vh.ctypes.data, dh.ctypes.data, None)
+        if rc != 0:
+            raise RuntimeError("rpm_check_configs_host failed: %s" % lib.rpm_last_error_string().decode())
+    e2e_s = time.perf_counter() - t0
+    barrier()
+    e2e_ok = bool(np.array_equal(vh, v32.cpu().numpy()))
+
+    # ---- roofline of the dominant kernel (the FP32 bulk pass)
+    bulk_s = statistics.median(bulk_ms) / 1e3
+    achieved = FLOP_PER_CONFIG * C / bulk_s / 1e12
+    peaks = {}
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            peaks = json.load(f)
+    except Exception:
+        pass
+    hbm_peak = peaks.get("hbm_gbs")
+    hbm_achieved = BYTES_PER_CONFIG * C / bulk_s / 1e9
+
+    if rank != 0:
+        return
+    line = {
+        "metric": METRIC, "value": value, "unit": "configs/s", "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": statistics.mean(step_ms), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32 (f64 recheck)", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "global_batch": C * ws, "precision": "fp32_recheck",
+                   "l2": "flushed (256 MB write) between timed steps", "parallelism": "replicas, configs sharded"},
+        "fp64": {"value": fp64_value, "unit": "configs/s", "ms_per_step": statistics.median(step64),
+                 "speedup_fp32_recheck_over_fp64": value / ws / fp64_value, "isvalid_flips": flips,
+                 "max_distance_diff_m": max_derr},
+        "recheck": {"configs_per_step": int(statistics.median(rechecked)),
+                    "fraction": statistics.median(rechecked) / C, "kernel_ms": statistics.median(re_ms)},
+        "clocks": clocks,
+        "e2e": {"value": C * args.steps / e2e_s, "unit": "configs/s", "h2d_bytes_per_step": C * D * 4,
+                "d2h_bytes_per_step": C * (1 + 8), "call": "rpm_check_configs_host", "matches_device_run": e2e_ok},
+        "gpu_launches": 2 * args.steps,
+        "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak_fp32, "unit": "TFLOP/s",
+                     "frac": achieved / peak_fp32 if peak_fp32 else None, "traffic": traffic_per_launch(),
+                     "kernel": "k_check_fp32", "kernel_ms": statistics.median(bulk_ms),
+                     "flop_per_config": FLOP_PER_CONFIG,
+                     "peak_source": "FFMA probe measured in this run (rpm_probe_fp32_peak)",
+                     "hbm": {"achieved": hbm_achieved, "peak": hbm_peak, "unit": "GB/s",
+                             "frac": (hbm_achieved / hbm_peak) if hbm_peak else None,
+                             "bytes_per_config": BYTES_PER_CONFIG, "peak_source": "MEASURED_PEAKS.json hbm_gbs"}},
+    }
+    if ws == 1 or rank == 0:
+        line["cpu_baseline"] = cpu_baseline(robot, scene, q, min(C, 1 << 20))
+    print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+def main():
+    args = parse()
+    ws, rank, local = dist_env()
+    if args.impl == "reference":
+        run_reference(args, ws, rank)
+    else:
+        run_ours(args, ws, rank, local)
+
+
+if __name__ == "__main__":
+    main()

@@ -161,6 +161,16 @@ int rpm_skeleton(rpm_ctx *ctx, int32_t robot_id, int32_t precision, const float 
 /* Statistics of the last check on this context; synchronises 'stream'. */
 int rpm_last_stats(rpm_ctx *ctx, void *stream, rpm_check_stats *out);
 
+/* Per-kernel timing of later checks (CUDA events on the caller's stream).
+ * rpm_last_timing returns the bulk kernel's and the recheck kernel's duration
+ * of the last check on 'stream' (synchronises it). */
+int rpm_ctx_set_timing(rpm_ctx *ctx, int enable);
+int rpm_last_timing(rpm_ctx *ctx, void *stream, float *bulk_ms, float *recheck_ms);
+
+/* FP32 FMA throughput of the device (TFLOP/s), measured with independent FMA
+ * chains: the denominator of the FP32 roofline. */
+int rpm_probe_fp32_peak(rpm_ctx *ctx, double *tflops);
+
 /* Synchronise a stream and report any device-side error status. */
 int rpm_sync(rpm_ctx *ctx, void *stream);
 

@@ -68,6 +68,8 @@ struct Scratch {
     uint32_t *counters = nullptr;   // [0] recheck count
     int32_t *status = nullptr;
     int64_t last_configs = 0;
+    cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};   // bulk start, bulk end / recheck start, recheck end
+    bool timed = false, had_recheck = false;
 };
 
 }  // namespace
@@ -89,6 +91,7 @@ struct rpm_ctx {
     double *hd[2] = {nullptr, nullptr};
     float *hp[2] = {nullptr, nullptr};
     size_t hcap_cfg = 0, hcap_prof = 0;
+    bool timing = false;
 };
 
 namespace {
@@ -250,13 +253,21 @@ int enqueue_check(rpm_ctx *ctx, SceneRec *s, int prec, const float *q, int64_t C
     sc->last_configs = C;
     const int64_t blocks = (C + kThreads - 1) / kThreads;
     CK(cudaMemsetAsync(sc->counters, 0, sizeof(uint32_t), st));
+    sc->timed = ctx->timing && blocks > 0;
+    sc->had_recheck = prec == RPM_PREC_FP32_RECHECK;
+    if (sc->timed && !sc->ev[0])
+        for (int i = 0; i < 3; ++i) CK(cudaEventCreate(&sc->ev[i]));
     if (blocks > 0) {
+        if (sc->timed) CK(cudaEventRecord(sc->ev[0], st));
         if (prec == RPM_PREC_FP32_RECHECK) {
             CK(launch_check_fp32(p, blocks, smem_bytes(RPM_PREC_FP32_REF, s->n_pad), st));
+            if (sc->timed) CK(cudaEventRecord(sc->ev[1], st));
             CK(launch_recheck(p, ctx->num_sms * 4, st));
         } else {
             CK(launch_check_exact(prec, p, blocks, smem_bytes(prec, s->n_pad), st));
+            if (sc->timed) CK(cudaEventRecord(sc->ev[1], st));
         }
+        if (sc->timed) CK(cudaEventRecord(sc->ev[2], st));
     }
     prune_users(ctx, buf);
     cudaEvent_t e = get_event(ctx);
@@ -526,6 +537,58 @@ int rpm_last_stats(rpm_ctx *ctx, void *stream, rpm_check_stats *out) {
     out->rechecked = cnt;
     out->overflow = 0;
     out->device_status = status;
+    return RPM_OK;
+}
+
+int rpm_ctx_set_timing(rpm_ctx *ctx, int enable) {
+    if (!ctx) return fail(RPM_ERR_INVALID, "NULL context");
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    ctx->timing = enable != 0;
+    return RPM_OK;
+}
+
+int rpm_last_timing(rpm_ctx *ctx, void *stream, float *bulk_ms, float *recheck_ms) {
+    if (!ctx) return fail(RPM_ERR_INVALID, "NULL context");
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    if (set_device(ctx)) return RPM_ERR_CUDA;
+    cudaStream_t st = (cudaStream_t)stream;
+    auto it = ctx->scratch.find(st);
+    if (it == ctx->scratch.end() || !it->second->timed) return fail(RPM_ERR_INVALID, "no timed check on this stream");
+    Scratch *sc = it->second;
+    CK(cudaEventSynchronize(sc->ev[2]));
+    float a = 0.f, b = 0.f;
+    CK(cudaEventElapsedTime(&a, sc->ev[0], sc->ev[1]));
+    CK(cudaEventElapsedTime(&b, sc->ev[1], sc->ev[2]));
+    if (bulk_ms) *bulk_ms = a;
+    if (recheck_ms) *recheck_ms = b;
+    return RPM_OK;
+}
+
+int rpm_probe_fp32_peak(rpm_ctx *ctx, double *tflops) {
+    if (!ctx || !tflops) return fail(RPM_ERR_INVALID, "NULL argument");
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    if (set_device(ctx)) return RPM_ERR_CUDA;
+    float *buf = nullptr;
+    const int blocks = ctx->num_sms * 8, threads = 256, iters = 4096;
+    CK(cudaMalloc(&buf, (size_t)blocks * threads * sizeof(float)));
+    cudaEvent_t a, b;
+    CK(cudaEventCreate(&a));
+    CK(cudaEventCreate(&b));
+    double best = 0.0;
+    for (int rep = 0; rep < 5; ++rep) {
+        CK(cudaEventRecord(a, 0));
+        CK(launch_ffma_probe(buf, blocks, threads, iters, 0));
+        CK(cudaEventRecord(b, 0));
+        CK(cudaEventSynchronize(b));
+        float ms = 0.f;
+        CK(cudaEventElapsedTime(&ms, a, b));
+        const double flops = 2.0 * kProbeChains * (double)iters * blocks * threads;
+        if (rep > 0) best = std::max(best, flops / (ms * 1e-3) / 1e12);
+    }
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    cudaFree(buf);
+    *tflops = best;
     return RPM_OK;
 }
 

@@ -54,10 +54,17 @@ inline int g_dbg_site_b = 0, g_dbg_site_d = 0;   // host debugging only
 #define RPM_DBG_D(pol) ((void)0)
 #endif
 
-// Exact forms: MODE 0 = FP64 (T double), MODE 1 = the reference's numerics (T float).
+#ifdef __CUDACC__
+// One warp per configuration (used for the few configurations the FP32 pass
+// leaves unsettled, so latency matters more than throughput).  Lanes split
+// the obstacles of each link; the isValid OR, the per-link minimum and the
+// first hit (lowest obstacle index with d <= 0) are warp reductions, which
+// give exactly the sequential i-major / j-minor result.
 template <int MODE, typename T>
-__host__ __device__ void config_exact(const DevRobot &rb, const ObsView<T> &ob, const float *q, const Num<T> &nm, Want w,
-                             uint8_t *valid_out, double *dist_out, float *prof_out) {
+__device__ void config_exact_warp(const DevRobot &rb, const ObsView<T> &ob, const float *q, const Num<T> &nm, Want w,
+                                  uint8_t *valid_out, double *dist_out, float *prof_out) {
+    const unsigned full = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
     SkelWalker<MODE> sw;
     sw.begin();
     T A[3], B[3];
@@ -66,110 +73,318 @@ __host__ __device__ void config_exact(const DevRobot &rb, const ObsView<T> &ob, 
     bool collided = false;
     T best = nm.maxd;
     int hit = -1;
-    T hit_val = T(0);
     const int L = rb.D;
     for (int i = 0; i < L && (need_b || need_d); ++i) {
         sw.point(rb, q, i + 1, B);
         const T r = LinkConst<T>::r(rb, i), rn = LinkConst<T>::rn(rb, i);
         const bool ground_skip = i < rb.ground_included;
-        const bool dist_link = need_d;
-        T link_best = nm.maxd;
-        for (int j = 0; j < ob.n && (need_b || need_d); ++j) {
-            if (ground_skip && ob.is_ground(j)) continue;   // :285 (bool) and :336-341 (d = MAX)
-            T o[6];
-            ob.box(j, o);
-            if (need_b) {
+        if (need_b) {
+            bool mine = false;
+            for (int j = lane; j < ob.n && !mine; j += 32) {
+                if (ground_skip && ob.is_ground(j)) continue;
+                T o[6];
+                ob.box(j, o);
                 ExactPol pol;
-                if (coll_box(pol, nm, A, B, r, rn, o)) { collided = true; need_b = false; }
+                mine = coll_box(pol, nm, A, B, r, rn, o);
             }
-            if (need_d) {
+            if (__any_sync(full, mine)) { collided = true; need_b = false; }
+        }
+        if (need_d) {
+            T lb = nm.maxd, hv = T(0);
+            int hj = 0x7fffffff;
+            for (int j = lane; j < ob.n; j += 32) {
+                if (ground_skip && ob.is_ground(j)) continue;
+                T o[6];
+                ob.box(j, o);
                 const T tol = ob.tol(j);
-                T thr = w.profile ? link_best : smin(best, link_best);
+                T thr = w.profile ? lb : smin(best, lb);
                 thr = smin(thr, tol);
                 const T s = thr + r + nm.eq + LinkConst<T>::margin();
                 if (s > T(0) && gap2(A, B, o) > s * s) continue;
                 ExactPol pol;
                 T d = capsule_box(pol, nm, A, B, r, o).v;
-                if (d > tol) d = nm.maxd;                     // :367-368
-                link_best = smin(link_best, d);               // :370
-                if (link_best <= T(0)) { hit = i; hit_val = link_best; need_d = false; }   // :371-378
+                if (d > tol) d = nm.maxd;
+                lb = smin(lb, d);
+                if (d <= T(0)) { hj = j; hv = d; break; }
+            }
+            int fj = hj;
+#pragma unroll
+            for (int off = 16; off > 0; off >>= 1) fj = min(fj, __shfl_xor_sync(full, fj, off));
+            T lmin = lb;
+#pragma unroll
+            for (int off = 16; off > 0; off >>= 1) {
+                const T other = __shfl_xor_sync(full, lmin, off);
+                lmin = (other < lmin) ? other : lmin;
+            }
+            if (fj != 0x7fffffff) {
+                const int owner = __ffs(__ballot_sync(full, hj == fj)) - 1;
+                const T hval = __shfl_sync(full, hv, owner);
+                hit = i;
+                need_d = false;
+                if (w.profile && lane == 0) prof_out[i] = (float)hval;
+            } else {
+                if (w.profile && lane == 0) prof_out[i] = (float)lmin;
+                best = smin(best, lmin);
             }
         }
-        if (w.profile && dist_link) prof_out[i] = (hit == i) ? (float)hit_val : (float)link_best;
-        if (hit < 0) best = smin(best, link_best);
         A[0] = B[0]; A[1] = B[1]; A[2] = B[2];
     }
-    if (w.profile && hit >= 0)
-        for (int k = hit + 1; k < L; ++k) prof_out[k] = 0.f;   // d_c_profile is zero-initialised (:325)
-    if (w.valid) *valid_out = collided ? 0 : 1;
-    if (w.dist) *dist_out = (hit >= 0) ? 0.0 : (double)best;
+    if (lane == 0) {
+        if (w.profile && hit >= 0)
+            for (int k = hit + 1; k < L; ++k) prof_out[k] = 0.f;
+        if (w.valid) *valid_out = collided ? 0 : 1;
+        if (w.dist) *dist_out = (hit >= 0) ? 0.0 : (double)best;
+    }
+}
+#endif
+
+#ifdef __CUDACC__
+// ---------------------------------------------------------------------------
+// Warp-cooperative driver used by the batched kernels.
+//
+// A warp owns 32 configurations (lane = configuration) and walks the links in
+// lockstep.  For link i every lane classifies obstacle j of its own
+// configuration with the bounding-box gap alone:
+//   * isValid : the reference's tree can return true only when some point of
+//     the segment is within r*sqrt(2) of the box (the inner test reaches r,
+//     the corner tests of :69-72 reach r*sqrt(2)), so a larger gap is a
+//     settled 'no collision' and the tree is skipped;
+//   * distance: a gap above min(best, min_dist_tol) + r + EQUALITY_THRESHOLD
+//     cannot lower the minimum or be a hit (pruned).
+// Pairs that need a tree go into one of two per-warp queues in shared memory;
+// a queue is drained 32 entries at a time with every lane evaluating one
+// pair, and results are combined per owner with shared-memory atomics:
+// isValid by OR, the link minimum by an order-preserving integer min, the
+// first hit by the minimum obstacle index.  These combine exactly as the
+// sequential i-major / j-minor scan, so outputs are bit-identical to it.
+// Order-preserving integer keys of T (for shared-memory atomicMin).
+template <typename T> struct Key;
+template <> struct Key<double> {
+    typedef long long type;
+    __device__ static long long of(double x) {
+        const long long i = __double_as_longlong(x);
+        return i >= 0 ? i : i ^ 0x7fffffffffffffffLL;
+    }
+    __device__ static double value(long long i) { return __longlong_as_double(i >= 0 ? i : i ^ 0x7fffffffffffffffLL); }
+};
+template <> struct Key<float> {
+    typedef int type;
+    __device__ static int of(float x) {
+        const int i = __float_as_int(x);
+        return i >= 0 ? i : i ^ 0x7fffffff;
+    }
+    __device__ static float value(int i) { return __int_as_float(i >= 0 ? i : i ^ 0x7fffffff); }
+};
+
+template <typename T> struct WarpShared {
+    T a[32][3], b[32][3];                // current link's segment per owner lane
+    typename Key<T>::type lmin[32];      // ordered key of the link minimum of d'
+    int hitj[32];                        // lowest obstacle index with a settled d' <= 0
+    T hitv[32];                          // d' at that index
+    int flags[32];                       // bit0 collision, bit1 isValid unsettled, bit2 distance unsettled
+    uint32_t qb[64], qd[64];             // queues: owner | j << 5
+};
+
+template <int MODE> struct PolOf { typedef ExactPol type; };
+template <> struct PolOf<2> { typedef RobustPol type; };
+
+template <int MODE, typename T> struct BoolMargin;
+template <int MODE> struct BoolMargin<MODE, double> { __device__ static double m() { return 1e-9; } };
+template <int MODE> struct BoolMargin<MODE, float> { __device__ static float m() { return MODE == 2 ? kDecide : 1e-5f; } };
+
+template <int MODE, typename T>
+__device__ __forceinline__ void drain_bool(WarpShared<T> &sh, const DevRobot &rb, const ObsView<T> &ob, const Num<T> &nm,
+                                           int i, int nitems) {
+    typedef typename PolOf<MODE>::type P;
+    const int lane = threadIdx.x & 31;
+    if (lane < nitems) {
+        const uint32_t e = sh.qb[lane];
+        const int owner = (int)(e & 31u), j = (int)(e >> 5);
+        T o[6];
+        ob.box(j, o);
+        P pol;
+        const bool c = coll_box(pol, nm, sh.a[owner], sh.b[owner], LinkConst<T>::r(rb, i), LinkConst<T>::rn(rb, i), o);
+        if (P::robust && pol.m < kDecide) atomicOr(&sh.flags[owner], 2);
+        else if (c) atomicOr(&sh.flags[owner], 1);
+    }
 }
 
-// FP32 bulk pass.  Returns true when every decision that shaped the requested
-// outputs was settled (branch margins >= kDecide, clearances outside the
-// contact band kBand).  Returns false when the configuration must be
-// recomputed in FP64; the outputs it wrote are then provisional and the FP64
-// recheck overwrites every one of them.
-static __host__ __device__ bool config_fp32(const DevRobot &rb, const ObsView<float> &ob, const float *q,
-                                            const Num<float> &nm, Want w, uint8_t *valid_out, double *dist_out,
-                                            float *prof_out) {
-    SkelWalker<2> sw;
+template <int MODE, typename T>
+__device__ __forceinline__ T pair_distance(const DevRobot &rb, const ObsView<T> &ob, const Num<T> &nm, const T *A,
+                                           const T *B, int i, int j, bool &settled) {
+    typedef typename PolOf<MODE>::type P;
+    T o[6];
+    ob.box(j, o);
+    P pol;
+    Val<T> dv = capsule_box(pol, nm, A, B, LinkConst<T>::r(rb, i), o);
+    const T tol = ob.tol(j);
+    T d = dv.v;
+    if (P::robust) {
+        const float band = dv.ia * (kDecide / kBand);
+        RPM_NOTE(pol, fabsf((float)(d - tol)) * band);
+        if (d != T(0)) RPM_NOTE(pol, fabsf((float)(d > tol ? nm.maxd : d)) * band);
+    }
+    if (d > tol) d = nm.maxd;   // :367-368
+    settled = !P::robust || pol.m >= kDecide;
+    return d;
+}
+
+template <int MODE, typename T>
+__device__ __forceinline__ void drain_dist(WarpShared<T> &sh, const DevRobot &rb, const ObsView<T> &ob, const Num<T> &nm,
+                                           int i, int nitems) {
+    const int lane = threadIdx.x & 31;
+    if (lane < nitems) {
+        const uint32_t e = sh.qd[lane];
+        const int owner = (int)(e & 31u), j = (int)(e >> 5);
+        bool settled;
+        const T d = pair_distance<MODE, T>(rb, ob, nm, sh.a[owner], sh.b[owner], i, j, settled);
+        if (!settled) atomicOr(&sh.flags[owner], 4);
+        if (d == d) {   // the reference's std::min ignores NaN
+            atomicMin(&sh.lmin[owner], Key<T>::of(d));
+            if (d <= T(0) && settled) atomicMin(&sh.hitj[owner], j);
+        }
+        __syncwarp(__activemask());
+        if (d <= T(0) && settled && sh.hitj[owner] == j) sh.hitv[owner] = d;   // one entry per (owner, j)
+    }
+}
+
+// Lower bound of the segment-box distance from the segment's bounding box
+// (lo, hi) and the box: the same arithmetic as gap2.
+template <typename T> __device__ __forceinline__ T gap2_bb(const T *lo, const T *hi, const T *o) {
+    T g2 = T(0);
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+        T g = o[c] - hi[c];
+        const T g2b = lo[c] - o[3 + c];
+        g = g > g2b ? g : g2b;
+        g = g > T(0) ? g : T(0);
+        g2 = g2 + g * g;
+    }
+    return g2;
+}
+
+// Append this lane's item to a warp queue (positions by ballot rank) and
+// drain the queue 32 entries at a time.
+#define RPM_PUSH_AND_DRAIN(Q, N, want, item, DRAIN)                                    \
+    do {                                                                               \
+        const unsigned m_ = __ballot_sync(0xffffffffu, (want));                         \
+        if (want) sh.Q[(N) + __popc(m_ & lt_mask)] = (item);                           \
+        (N) += __popc(m_);                                                             \
+        __syncwarp();                                                                  \
+        if ((N) >= 32) {                                                               \
+            DRAIN<MODE, T>(sh, rb, ob, nm, i, 32);                                     \
+            __syncwarp();                                                              \
+            if (lane < (N) - 32) sh.Q[lane] = sh.Q[32 + lane];                         \
+            (N) -= 32;                                                                 \
+            __syncwarp();                                                              \
+        }                                                                              \
+    } while (0)
+
+// Returns, per lane, whether the configuration is settled (always true for
+// the exact forms).  Outputs of unsettled configurations are provisional.
+// Once a lane has a settled hit it only looks for an earlier hit (lower
+// obstacle index), which is all the profile's first-hit semantics need.
+template <int MODE, typename T>
+__device__ bool warp_check(WarpShared<T> &sh, const DevRobot &rb, const ObsView<T> &ob, const float *q, bool active,
+                           const Num<T> &nm, Want w, uint8_t *valid_out, double *dist_out, float *prof_out) {
+    const unsigned full = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    const unsigned lt_mask = (1u << lane) - 1u;
+    SkelWalker<MODE> sw;
     sw.begin();
-    float A[3], B[3];
-    sw.point(rb, q, 0, A);
-    bool need_b = w.valid, need_d = w.dist || w.profile;
+    T A[3] = {T(0), T(0), T(0)}, B[3] = {T(0), T(0), T(0)};
+    if (active) sw.point(rb, q, 0, A);
+    bool need_b = active && w.valid, need_d = active && (w.dist || w.profile);
     bool collided = false, unc_b = false, unc_d = false;
-    float best = nm.maxd;
+    T best = nm.maxd;
     int hit = -1;
     const int L = rb.D;
-    for (int i = 0; i < L && (need_b || need_d); ++i) {
-        sw.point(rb, q, i + 1, B);
-        const float r = rb.radius_f[i], rn = rb.rnew_f[i];
+    const T dmargin = (MODE == 2) ? T(kBand) : LinkConst<T>::margin();
+    sh.flags[lane] = 0;
+    for (int i = 0; i < L; ++i) {
+        if (!__any_sync(full, need_b || need_d)) break;
+        if (active) sw.point(rb, q, i + 1, B);
+        const T r = LinkConst<T>::r(rb, i);
+        const T tb = r * T(1.41421356237309515) + BoolMargin<MODE, T>::m();
+        const T tb2 = tb * tb;
+        const T hunt = r + nm.eq + dmargin;          // a gap above this cannot be a hit
         const bool ground_skip = i < rb.ground_included;
         const bool dist_link = need_d;
-        float link_best = nm.maxd;
-        for (int j = 0; j < ob.n && (need_b || need_d); ++j) {
-            if (ground_skip && ob.is_ground(j)) continue;
-            float o[6];
-            ob.box(j, o);
-            if (need_b) {
-                RobustPol pol;
-                bool c = coll_box(pol, nm, A, B, r, rn, o);
-                if (pol.m < kDecide) { unc_b = true; RPM_DBG_B(pol); }
-                else if (c) { collided = true; need_b = false; }
+        T lo[3], hi[3];
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            lo[k] = A[k] < B[k] ? A[k] : B[k];
+            hi[k] = A[k] < B[k] ? B[k] : A[k];
+            sh.a[lane][k] = A[k];
+            sh.b[lane][k] = B[k];
+        }
+        sh.lmin[lane] = Key<T>::of(nm.maxd);
+        sh.hitj[lane] = 0x7fffffff;
+        sh.hitv[lane] = T(0);
+        __syncwarp();
+        int nb = 0, nd = 0;
+        for (int j = 0; j < ob.n; ++j) {
+            const bool wb = need_b && !(sh.flags[lane] & 1);
+            const int hj = sh.hitj[lane];
+            const bool wd = need_d && (hj == 0x7fffffff || (w.profile && j < hj));
+            bool qb = false, qd = false;
+            if ((wb || wd) && !(ground_skip && ob.is_ground(j))) {
+                T o[6];
+                ob.box(j, o);
+                const T g2 = gap2_bb(lo, hi, o);
+                qb = wb && !(g2 > tb2);
+                if (wd) {
+                    if (hj != 0x7fffffff) {
+                        qd = !(g2 > hunt * hunt);
+                    } else {
+                        const T cur = Key<T>::value(sh.lmin[lane]);
+                        T thr = w.profile ? cur : smin(best, cur);
+                        thr = smin(thr, ob.tol(j));
+                        const T s = thr + r + nm.eq + dmargin;
+                        qd = !(s > T(0) && g2 > s * s);
+                    }
+                }
             }
-            if (need_d) {
-                const float tol = ob.tol(j);
-                float thr = w.profile ? link_best : fminf(best, link_best);
-                thr = fminf(thr, tol);
-                const float s = thr + r + nm.eq + kBand;
-                if (s > 0.f && gap2(A, B, o) > s * s) continue;
-                RobustPol pol;
-                Val<float> dv = capsule_box(pol, nm, A, B, r, o);
-                float d = dv.v;
-                // clearance decisions use the contact band (scaled onto kDecide)
-                const float band = dv.ia * (kDecide / kBand);
-                RPM_NOTE(pol, fabsf(d - tol) * band);
-                if (d > tol) d = nm.maxd;
-                if (d != 0.f) RPM_NOTE(pol, fabsf(d) * band);   // exact zeros come from settled branches
-                if (pol.m < kDecide) { unc_d = true; RPM_DBG_D(pol); }
-                link_best = (d < link_best) ? d : link_best;
-                if (link_best <= 0.f) { hit = i; need_d = false; }
+            const uint32_t item = (uint32_t)lane | ((uint32_t)j << 5);
+            RPM_PUSH_AND_DRAIN(qb, nb, qb, item, drain_bool);
+            RPM_PUSH_AND_DRAIN(qd, nd, qd, item, drain_dist);
+        }
+        if (nb > 0) drain_bool<MODE, T>(sh, rb, ob, nm, i, nb);
+        if (nd > 0) drain_dist<MODE, T>(sh, rb, ob, nm, i, nd);
+        __syncwarp();
+        // ---- fold this link's results into the lane's configuration
+        const int fl = sh.flags[lane];
+        if (need_b) {
+            if (fl & 1) { collided = true; need_b = false; }
+            if (fl & 2) unc_b = true;
+        }
+        if (dist_link) {
+            if (fl & 4) unc_d = true;
+            const int hj = sh.hitj[lane];
+            const T lmin = Key<T>::value(sh.lmin[lane]);
+            if (hj != 0x7fffffff) {
+                // the partial minimum at the first hit is the hit's own value
+                hit = i;
+                need_d = false;
+                if (w.profile) prof_out[i] = (float)sh.hitv[lane];
+            } else {
+                if (w.profile) prof_out[i] = (float)lmin;
+                best = smin(best, lmin);
             }
         }
-        if (w.profile && dist_link) prof_out[i] = link_best;   // the hit value when hit == i
-        if (hit < 0) best = fminf(best, link_best);
+        sh.flags[lane] = fl & ~7;   // the per-link bits have been folded
+        __syncwarp();
         A[0] = B[0]; A[1] = B[1]; A[2] = B[2];
     }
+    if (!active) return true;
     if (w.profile && hit >= 0)
         for (int k = hit + 1; k < L; ++k) prof_out[k] = 0.f;
     if (w.valid) *valid_out = collided ? 0 : 1;
     if (w.dist) *dist_out = (hit >= 0) ? 0.0 : (double)best;
-    // A settled collision decides isValid; a settled hit decides the scalar
-    // distance (0), but not the profile's first-hit position.
     const bool bad_b = w.valid && !collided && unc_b;
     const bool bad_d = (w.dist || w.profile) && unc_d && (w.profile || hit < 0);
     return !(bad_b || bad_d);
 }
+#endif
 
 }  // namespace rpm

@@ -165,6 +165,25 @@ template <typename F> struct Fk {
     }
 };
 
+// Right-multiplication of R by a rotation about the joint axis: columns
+// (IA, IB) become (a c + b s, b c - a s).
+template <int IA, int IB> RPM_HD void rot_cols_d(double *R, double c, double s) {
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+        const double a = R[3 * i + IA], b = R[3 * i + IB];
+        R[3 * i + IA] = dadd(dmul(a, c), dmul(b, s));
+        R[3 * i + IB] = dadd(dmul(b, c), -dmul(a, s));
+    }
+}
+template <int IA, int IB> RPM_HD void rot_cols_f(float *R, float c, float s) {
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+        const float a = R[3 * i + IA], b = R[3 * i + IB];
+        R[3 * i + IA] = a * c + b * s;
+        R[3 * i + IB] = b * c - a * s;
+    }
+}
+
 RPM_HD void fk_step_d(Fk<double> &f, const DevRobot &rb, int k, double q) {
     const double *o = rb.oxyz[k];
     double np[3];
@@ -189,14 +208,10 @@ RPM_HD void fk_step_d(Fk<double> &f, const DevRobot &rb, int k, double q) {
     }
     double s, c;
     taylor_sincos(q, &s, &c);
-    const int ax = rb.axis[k];
-    const int ia = (ax == 0) ? 1 : (ax == 1 ? 2 : 0);
-    const int ib = (ax == 0) ? 2 : (ax == 1 ? 0 : 1);
-#pragma unroll
-    for (int i = 0; i < 3; ++i) {
-        double a = f.R[3 * i + ia], b = f.R[3 * i + ib];
-        f.R[3 * i + ia] = dadd(dmul(a, c), dmul(b, s));
-        f.R[3 * i + ib] = dadd(dmul(b, c), -dmul(a, s));
+    switch (rb.axis[k]) {   // columns (a, b) <- (a c + b s, b c - a s)
+        case 0: rot_cols_d<1, 2>(f.R, c, s); break;
+        case 1: rot_cols_d<2, 0>(f.R, c, s); break;
+        default: rot_cols_d<0, 1>(f.R, c, s); break;
     }
 }
 
@@ -219,14 +234,10 @@ RPM_HD void fk_step_f(Fk<float> &f, const DevRobot &rb, int k, float q) {
     }
     float s, c;
     sincosf(q, &s, &c);
-    const int ax = rb.axis[k];
-    const int ia = (ax == 0) ? 1 : (ax == 1 ? 2 : 0);
-    const int ib = (ax == 0) ? 2 : (ax == 1 ? 0 : 1);
-#pragma unroll
-    for (int i = 0; i < 3; ++i) {
-        float a = f.R[3 * i + ia], b = f.R[3 * i + ib];
-        f.R[3 * i + ia] = a * c + b * s;
-        f.R[3 * i + ib] = b * c - a * s;
+    switch (rb.axis[k]) {
+        case 0: rot_cols_f<1, 2>(f.R, c, s); break;
+        case 1: rot_cols_f<2, 0>(f.R, c, s); break;
+        default: rot_cols_f<0, 1>(f.R, c, s); break;
     }
 }
 

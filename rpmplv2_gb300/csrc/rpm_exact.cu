@@ -49,6 +49,7 @@ __global__ void __launch_bounds__(kThreads) k_check_exact(const __grid_constant_
     typedef typename std::conditional<MODE == 0, double, float>::type T;
     extern __shared__ __align__(128) unsigned char smem[];
     __shared__ uint64_t bar;
+    __shared__ WarpShared<T> wsh[kThreads / 32];
     const int s = find_seg(P);
     const Seg &sg = P.segs[s];
     bulk_init(&bar);
@@ -58,22 +59,27 @@ __global__ void __launch_bounds__(kThreads) k_check_exact(const __grid_constant_
     const float *ground = (MODE == 0) ? reinterpret_cast<const float *>(smem + sizeof(DevRobot) + kDRows * sg.n_pad * sizeof(double))
                                       : reinterpret_cast<const float *>(rows) + (size_t)kRowGround * sg.n_pad;
     const int64_t c = (int64_t)(blockIdx.x - sg.first_block) * kThreads + threadIdx.x;
-    if (c >= sg.count) return;
+    const int64_t warp0 = c - (threadIdx.x & 31);
+    if (warp0 >= sg.count) return;   // whole warp idle
+    const bool active = c < sg.count;
     ObsView<T> ob{rows, ground, sg.n, sg.n_pad};
     const Want w{sg.valid != nullptr, sg.dist != nullptr, sg.profile != nullptr};
     const int D = rb.D;
     Num<T> nm;
     if (MODE == 0) { nm.eq = (T)P.nmd.eq; nm.maxd = (T)P.nmd.maxd; }
     else { nm.eq = (T)P.nmf.eq; nm.maxd = (T)P.nmf.maxd; }
-    config_exact<MODE, T>(rb, ob, sg.q + c * D, nm, w, w.valid ? sg.valid + c : nullptr, w.dist ? sg.dist + c : nullptr,
-                          w.profile ? sg.profile + c * D : nullptr);
+    warp_check<MODE, T>(wsh[threadIdx.x >> 5], rb, ob, sg.q + c * D, active, nm, w,
+                        (w.valid && active) ? sg.valid + c : nullptr, (w.dist && active) ? sg.dist + c : nullptr,
+                        (w.profile && active) ? sg.profile + c * D : nullptr);
 }
 
-// FP64 recomputation of the configurations listed by the FP32 pass.  Reads
-// robot and obstacles from global memory (the list mixes segments).
+// FP64 recomputation of the configurations listed by the FP32 pass, one warp
+// per configuration.  Reads robot and obstacles from global memory (the list
+// mixes segments).
 __global__ void __launch_bounds__(kThreads) k_recheck(const __grid_constant__ KParams P) {
     const uint32_t n = *P.recheck_count;
-    for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+    const uint32_t warps = gridDim.x * (blockDim.x / 32);
+    for (uint32_t k = blockIdx.x * (blockDim.x / 32) + (threadIdx.x >> 5); k < n; k += warps) {
         const uint64_t e = P.recheck[k];
         const int s = (int)(e >> 40);
         const int64_t c = (int64_t)(e & ((1ull << 40) - 1));
@@ -83,8 +89,8 @@ __global__ void __launch_bounds__(kThreads) k_recheck(const __grid_constant__ KP
         ObsView<double> ob{sg.obs_d, sg.obs_f + (size_t)kRowGround * sg.n_pad, sg.n, sg.n_pad};
         const Want w{sg.valid != nullptr, sg.dist != nullptr, sg.profile != nullptr};
         const int D = sg.robot->D;
-        config_exact<0, double>(*sg.robot, ob, sg.q + c * D, P.nmd, w, w.valid ? sg.valid + c : nullptr,
-                                w.dist ? sg.dist + c : nullptr, w.profile ? sg.profile + c * D : nullptr);
+        config_exact_warp<0, double>(*sg.robot, ob, sg.q + c * D, P.nmd, w, w.valid ? sg.valid + c : nullptr,
+                                     w.dist ? sg.dist + c : nullptr, w.profile ? sg.profile + c * D : nullptr);
     }
 }
 

@@ -10,6 +10,7 @@ namespace rpm {
 __global__ void __launch_bounds__(kThreads) k_check_fp32(const __grid_constant__ KParams P) {
     extern __shared__ __align__(128) unsigned char smem[];
     __shared__ uint64_t bar;
+    __shared__ WarpShared<float> wsh[kThreads / 32];
     int s = 0;
     while (s + 1 < P.nseg && P.segs[s + 1].first_block <= (int64_t)blockIdx.x) ++s;
     const Seg &sg = P.segs[s];
@@ -25,16 +26,41 @@ __global__ void __launch_bounds__(kThreads) k_check_fp32(const __grid_constant__
     const DevRobot &rb = *reinterpret_cast<const DevRobot *>(smem);
     const float *rows = reinterpret_cast<const float *>(smem + sizeof(DevRobot));
     const int64_t c = (int64_t)(blockIdx.x - sg.first_block) * kThreads + threadIdx.x;
-    if (c >= sg.count) return;
+    const int64_t warp0 = c - (threadIdx.x & 31);
+    if (warp0 >= sg.count) return;   // whole warp idle
+    const bool active = c < sg.count;
     ObsView<float> ob{rows, rows + (size_t)kRowGround * sg.n_pad, sg.n, sg.n_pad};
     const Want w{sg.valid != nullptr, sg.dist != nullptr, sg.profile != nullptr};
     const int D = rb.D;
-    const bool ok = config_fp32(rb, ob, sg.q + c * D, P.nmf, w, w.valid ? sg.valid + c : nullptr,
-                                w.dist ? sg.dist + c : nullptr, w.profile ? sg.profile + c * D : nullptr);
-    if (!ok) {
+    const bool ok = warp_check<2, float>(wsh[threadIdx.x >> 5], rb, ob, sg.q + c * D, active, P.nmf, w,
+                                         (w.valid && active) ? sg.valid + c : nullptr,
+                                         (w.dist && active) ? sg.dist + c : nullptr,
+                                         (w.profile && active) ? sg.profile + c * D : nullptr);
+    if (active && !ok) {
         const uint32_t slot = atomicAdd(P.recheck_count, 1u);
         P.recheck[slot] = ((uint64_t)s << 40) | (uint64_t)c;
     }
+}
+
+// Peak FP32 issue rate of this GPU: independent FMA chains, no memory traffic.
+__global__ void k_ffma_probe(float *out, int iters) {
+    float a[kProbeChains];
+#pragma unroll
+    for (int k = 0; k < kProbeChains; ++k) a[k] = (float)(threadIdx.x + k);
+    const float m = 0.999999f, c = 1e-7f;
+    for (int i = 0; i < iters; ++i) {
+#pragma unroll
+        for (int k = 0; k < kProbeChains; ++k) a[k] = fmaf(a[k], m, c);
+    }
+    float s = 0.f;
+#pragma unroll
+    for (int k = 0; k < kProbeChains; ++k) s += a[k];
+    out[blockIdx.x * blockDim.x + threadIdx.x] = s;
+}
+
+cudaError_t launch_ffma_probe(float *out, int blocks, int threads, int iters, cudaStream_t st) {
+    k_ffma_probe<<<blocks, threads, 0, st>>>(out, iters);
+    return cudaGetLastError();
 }
 
 cudaError_t launch_check_fp32(const KParams &p, int64_t blocks, size_t smem, cudaStream_t st) {

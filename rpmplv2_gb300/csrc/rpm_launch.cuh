@@ -28,6 +28,9 @@ size_t smem_bytes(int mode, int n_pad);
 cudaError_t launch_check_exact(int mode, const KParams &p, int64_t blocks, size_t smem, cudaStream_t st);
 cudaError_t launch_check_fp32(const KParams &p, int64_t blocks, size_t smem, cudaStream_t st);
 cudaError_t launch_recheck(const KParams &p, int grid, cudaStream_t st);
+// FP32 FFMA throughput probe: kProbeChains independent FMA chains per thread.
+constexpr int kProbeChains = 8;
+cudaError_t launch_ffma_probe(float *out, int blocks, int threads, int iters, cudaStream_t st);
 cudaError_t launch_skeleton(int mode, const DevRobot *rb, int D, const float *q, int64_t C, double *out, cudaStream_t st);
 
 }  // namespace rpm

@@ -45,6 +45,7 @@ struct RB {
 
 struct ExactPol {
     static constexpr bool robust = false;
+    static constexpr float m = FLT_MAX;   // every decision is exact
     typedef bool C;
     template <typename T> RPM_HD static bool lt(T a, T b, float = 1.f) { return a < b; }
     template <typename T> RPM_HD static bool gt(T a, T b, float = 1.f) { return a > b; }
@@ -266,45 +267,64 @@ RPM_HD T seg_point(P &pol, const Num<T> &nm, const T *A, const T *B, const T *C)
     return d;
 }
 
-// checkCases (:113-148)
+// Selects in place of dynamic indexing (dynamic indices into register arrays
+// would spill them to local memory).
+template <typename T> RPM_HD T sel3(const T *v, int k) { return k == 0 ? v[0] : (k == 1 ? v[1] : v[2]); }
+template <typename T> RPM_HD T sel6(const T *v, int k) {
+    return k < 3 ? (k == 0 ? v[0] : (k == 1 ? v[1] : v[2])) : (k == 3 ? v[3] : (k == 4 ? v[4] : v[5]));
+}
+RPM_HD int gray2(int q) { return q ^ (q >> 1); }   // 0, 1, 3, 2: a loop around a square
+
+// checkCases (:113-148): at most two rectangle edges, the second only while
+// the first distance is positive.
 template <typename T, typename P>
-__host__ __device__ Val<T> check_cases(P &pol, const Num<T> &nm, const T *A, const T *B, const T *rec, T pu, T pv, T obs_coord,
-                              int coord) {
-    Val<T> d1{nm.maxd, 1.f}, d2{nm.maxd, 1.f};
-    T C[3], D[3];
-    if (RPM_TAKE(pol, P::lt(pu, rec[0]))) {
-        pt3(rec[0], rec[1], obs_coord, coord, C); pt3(rec[0], rec[3], obs_coord, coord, D);
-        d1 = seg_seg(pol, nm, A, B, C, D);
-    } else if (RPM_TAKE(pol, P::gt(pu, rec[2]))) {
-        pt3(rec[2], rec[1], obs_coord, coord, C); pt3(rec[2], rec[3], obs_coord, coord, D);
-        d1 = seg_seg(pol, nm, A, B, C, D);
+RPM_HD Val<T> check_cases(P &pol, const Num<T> &nm, const T *A, const T *B, const T *rec, T pu, T pv, T obs_coord,
+                          int coord) {
+    T d[2] = {nm.maxd, nm.maxd};
+#pragma unroll 1
+    for (int k = 0; k < 2; ++k) {
+        // k = 0: edge u = rec0 or u = rec2 (v from rec1 to rec3); k = 1: edge v = rec1 or v = rec3
+        int side = -1;
+        if (k == 0) {
+            if (RPM_TAKE(pol, P::lt(pu, rec[0]))) side = 0;
+            else if (RPM_TAKE(pol, P::gt(pu, rec[2]))) side = 1;
+        } else {
+            // d_c1 is MAX_DISTANCE, an exact 0 from the snap, or a distance of at
+            // least EQUALITY_THRESHOLD (the snap margin is recorded in seg_seg)
+            auto d1pos = P::settled(d[0] > T(0));
+            if (RPM_TAKE(pol, P::all(d1pos, P::lt(pv, rec[1])))) side = 0;
+            else if (RPM_TAKE(pol, P::all(d1pos, P::gt(pv, rec[3])))) side = 1;
+        }
+        if (side < 0) continue;
+        T C[3], D[3];
+        if (k == 0) {
+            const T u = side ? rec[2] : rec[0];
+            pt3(u, rec[1], obs_coord, coord, C);
+            pt3(u, rec[3], obs_coord, coord, D);
+        } else {
+            const T v = side ? rec[3] : rec[1];
+            pt3(rec[0], v, obs_coord, coord, C);
+            pt3(rec[2], v, obs_coord, coord, D);
+        }
+        d[k] = seg_seg(pol, nm, A, B, C, D).v;
     }
-    // d1 is MAX_DISTANCE, an exact 0 from the snap, or a distance at least
-    // EQUALITY_THRESHOLD (the snap margin is recorded inside seg_seg)
-    auto d1pos = P::settled(d1.v > T(0));
-    if (RPM_TAKE(pol, P::all(d1pos, P::lt(pv, rec[1])))) {
-        pt3(rec[0], rec[1], obs_coord, coord, C); pt3(rec[2], rec[1], obs_coord, coord, D);
-        d2 = seg_seg(pol, nm, A, B, C, D);
-    } else if (RPM_TAKE(pol, P::all(d1pos, P::gt(pv, rec[3])))) {
-        pt3(rec[0], rec[3], obs_coord, coord, C); pt3(rec[2], rec[3], obs_coord, coord, D);
-        d2 = seg_seg(pol, nm, A, B, C, D);
-    }
-    return Val<T>{smin(d1.v, d2.v), fminf(d1.ia, d2.ia)};
+    return Val<T>{smin(d[0], d[1]), 1.f};
 }
 
 // collisionCapsuleToRectangle (:46-111).  'face' in 0..5 = x_min..z_max.
 template <typename T, typename P>
-__host__ __device__ bool coll_rect(P &pol, const Num<T> &nm, const T *A, const T *B, T radius, const T *obs, int face) {
-    const T obs_coord = obs[face];
+RPM_HD bool coll_rect(P &pol, const Num<T> &nm, const T *A, const T *B, T radius, const T *obs, int face) {
     const int c = face > 2 ? face - 3 : face;
     const int a = (c == 0) ? 1 : 0, b = (c == 2) ? 1 : 2;
-    const T rec[4] = {obs[a], obs[b], obs[3 + a], obs[3 + b]};
-    const T Au = A[a], Av = A[b], Bu = B[a], Bv = B[b];
-    const T num = obs_coord - A[c], den = B[c] - A[c];
+    const T obs_coord = sel6(obs, face);
+    const T rec[4] = {sel6(obs, a), sel6(obs, b), sel6(obs, 3 + a), sel6(obs, 3 + b)};
+    const T Ac = sel3(A, c), Bc = sel3(B, c);
+    const T Au = sel3(A, a), Av = sel3(A, b), Bu = sel3(B, a), Bv = sel3(B, b);
+    const T num = obs_coord - Ac, den = Bc - Ac;
     T t = RPM_TAKE(pol, P::nonzero(den)) ? num / den : nm.maxd;
     const T Mu = Au + t * (Bu - Au), Mv = Av + t * (Bv - Av);
-    // |A - A_proj| and |B - B_proj|: two coordinates cancel exactly
-    const T xa = A[c] - obs_coord, xb = B[c] - obs_coord;
+    // |A - A_proj| and |B - B_proj|: the other two coordinates cancel exactly
+    const T xa = Ac - obs_coord, xb = Bc - obs_coord;
     const T dA = sqrtT(xa * xa), dB = sqrtT(xb * xb);
     if (RPM_TAKE(pol, P::t_inside(t, num, den))) {
         float iaM = 1.f;
@@ -335,30 +355,43 @@ __host__ __device__ bool coll_rect(P &pol, const Num<T> &nm, const T *A, const T
     if (radius > T(0)) {
         auto a_in = P::all(P::gt(Au, rec[0]), P::lt(Au, rec[2]), P::gt(Av, rec[1]), P::lt(Av, rec[3]));
         auto b_in = P::all(P::gt(Bu, rec[0]), P::lt(Bu, rec[2]), P::gt(Bv, rec[1]), P::lt(Bv, rec[3]));
-        if (RPM_TAKE(pol, a_in)) {
-            if (RPM_TAKE(pol, b_in)) {
-                if (RPM_TAKE(pol, P::lt(smin(dA, dB), radius))) return true;
-            } else {
-                Val<T> cc = check_cases(pol, nm, A, B, rec, Bu, Bv, obs_coord, c);
-                if (RPM_TAKE(pol, P::lt(smin(cc.v, dA), radius, cc.ia))) return true;
-            }
-        } else if (RPM_TAKE(pol, b_in)) {
-            Val<T> cc = check_cases(pol, nm, A, B, rec, Au, Av, obs_coord, c);
-            if (RPM_TAKE(pol, P::lt(smin(cc.v, dB), radius, cc.ia))) return true;
+        const bool ain = RPM_TAKE(pol, a_in);
+        const bool bin = RPM_TAKE(pol, b_in);
+        if (ain && bin) {                                                    // both projections
+            if (RPM_TAKE(pol, P::lt(smin(dA, dB), radius))) return true;
         } else {
-            Val<T> cc = check_cases(pol, nm, A, B, rec, Au, Av, obs_coord, c);
-            if (RPM_TAKE(pol, P::lt(cc.v, radius, cc.ia))) return true;
-            cc = check_cases(pol, nm, A, B, rec, Bu, Bv, obs_coord, c);
-            if (RPM_TAKE(pol, P::lt(cc.v, radius, cc.ia))) return true;
+            // only A: min(checkCases(B_rec), |A - A_proj|); only B: min(checkCases(A_rec),
+            // |B - B_proj|); neither: checkCases(A_rec), then checkCases(B_rec)
+            const int n = (ain || bin) ? 1 : 2;
+#pragma unroll 1
+            for (int k = 0; k < n; ++k) {
+                const bool use_b = ain || k == 1;
+                const T pu = use_b ? Bu : Au, pv = use_b ? Bv : Av;
+                Val<T> cc = check_cases(pol, nm, A, B, rec, pu, pv, obs_coord, c);
+                const T v = ain ? smin(cc.v, dA) : (bin ? smin(cc.v, dB) : cc.v);
+                if (RPM_TAKE(pol, P::lt(v, radius, cc.ia))) return true;
+            }
         }
     }
     return false;
 }
+// One out-of-line instance of coll_rect per (T, policy): both trees call it,
+// so sharing it halves the code the instruction cache has to hold.  The
+// policy state travels by value (decision, smallest margin).
+template <typename T, typename P>
+__host__ __device__ __noinline__ RB coll_rect_call(const Num<T> nm, const T *A, const T *B, T radius, const T *obs,
+                                                   int face) {
+    P pol;
+    const bool v = coll_rect(pol, nm, A, B, radius, obs, face);
+    return RB{v, pol.m};
+}
 
 // collisionCapsuleToBox (:4-42).  r_new = radius * sqrt(3) / 3 comes
-// precomputed per link with the reference's rounding.
+// precomputed per link with the reference's rounding.  The face tests of
+// :19-40 run as one loop over the axes (x, then y, then z), stopping at the
+// first collision.
 template <typename T, typename P>
-__host__ __device__ bool coll_box(P &pol, const Num<T> &nm, const T *A, const T *B, T radius, T r_new, const T *o) {
+RPM_HD bool coll_box(P &pol, const Num<T> &nm, const T *A, const T *B, T radius, T r_new, const T *o) {
     auto inA = P::all6(P::gt(A[0], o[0] - r_new), P::gt(A[1], o[1] - r_new), P::gt(A[2], o[2] - r_new),
                        P::lt(A[0], o[3] + r_new), P::lt(A[1], o[4] + r_new), P::lt(A[2], o[5] + r_new));
     auto inB = P::all6(P::gt(B[0], o[0] - r_new), P::gt(B[1], o[1] - r_new), P::gt(B[2], o[2] - r_new),
@@ -371,53 +404,59 @@ __host__ __device__ bool coll_box(P &pol, const Num<T> &nm, const T *A, const T 
                         P::all(P::lt(A[2], o[2] - radius), P::lt(B[2], o[2] - radius)),
                         P::all(P::gt(A[2], o[5] + radius), P::gt(B[2], o[5] + radius)));
     if (RPM_TAKE(pol, slab)) return false;
-    bool collision = false;
-    if (RPM_TAKE(pol, P::lt(A[0], o[0]))) collision = coll_rect(pol, nm, A, B, radius, o, 0);
-    else if (RPM_TAKE(pol, P::gt(A[0], o[3]))) collision = coll_rect(pol, nm, A, B, radius, o, 3);
-    if (!collision) {
-        if (RPM_TAKE(pol, P::lt(A[1], o[1]))) collision = coll_rect(pol, nm, A, B, radius, o, 1);
-        else if (RPM_TAKE(pol, P::gt(A[1], o[4]))) collision = coll_rect(pol, nm, A, B, radius, o, 4);
-        if (!collision) {
-            if (RPM_TAKE(pol, P::lt(A[2], o[2]))) collision = coll_rect(pol, nm, A, B, radius, o, 2);
-            else if (RPM_TAKE(pol, P::gt(A[2], o[5]))) collision = coll_rect(pol, nm, A, B, radius, o, 5);
+#pragma unroll 1
+    for (int ax = 0; ax < 3; ++ax) {
+        const T a = sel3(A, ax);
+        int face = -1;
+        if (RPM_TAKE(pol, P::lt(a, sel6(o, ax)))) face = ax;
+        else if (RPM_TAKE(pol, P::gt(a, sel6(o, ax + 3)))) face = ax + 3;
+        if (face >= 0) {
+            const RB rr = coll_rect_call<T, P>(nm, A, B, radius, o, face);
+            RPM_NOTE(pol, rr.m);
+            if (rr.v) return true;
         }
     }
-    return collision;
+    return false;
 }
 
-// distanceToMoreLineSegments (:576-595) over box edges given as corner pairs.
-template <typename T, typename P>
-RPM_HD void more_edges(P &pol, const Num<T> &nm, const T *A, const T *B, const T *o,
-                                           const uint8_t *edges, int ne, Val<T> &d) {
-    for (int k = 0; k < ne; ++k) {
-        T Cc[3], Dd[3];
-        corner(o, edges[2 * k], Cc);
-        corner(o, edges[2 * k + 1], Dd);
-        Val<T> dt = seg_seg(pol, nm, A, B, Cc, Dd);
-        if (dt.v <= T(0)) { d.v = T(0); d.ia = fminf(d.ia, dt.ia); return; }
-        if (dt.v < d.v) d.v = dt.v;
-        d.ia = fminf(d.ia, dt.ia);
-    }
-}
+// Edge sources of CapsuleToBox's distance phase, all as box-corner pairs
+// (corner bit 0 = x max, bit 1 = y max, bit 2 = z max).
+enum EdgeKind { kEdgesNone = 0, kEdgesList = 1, kEdgesFaceLoop = 2, kEdgesAll12 = 3 };
 
-// The 12 box edges as corner pairs: bottom loop, top loop, verticals (:747-750).
-RPM_HD uint8_t edge12(int k) {
-    switch (k) {
-        case 0: return 0; case 1: return 1; case 2: return 1; case 3: return 3; case 4: return 3; case 5: return 2;
-        case 6: return 2; case 7: return 0; case 8: return 4; case 9: return 5; case 10: return 5; case 11: return 7;
-        case 12: return 7; case 13: return 6; case 14: return 6; case 15: return 4; case 16: return 0; case 17: return 4;
-        case 18: return 1; case 19: return 5; case 20: return 3; case 21: return 7; case 22: return 2; default: return 6;
+// The k-th edge of a source.  List: up to 4 packed (c0 | c1 << 3) entries.
+// Face loop (checkOtherCases, one axis outside): the face's corners in the
+// reference's order (u, v) = (0,0), (1,0), (1,1), (0,1).  All 12 (:747-750):
+// bottom loop, top loop, then the four vertical edges.
+RPM_HD void edge_of(int kind, uint32_t list, int base, int u, int v, int k, int &c0, int &c1) {
+    if (kind == kEdgesList) {
+        const uint32_t e = (list >> (6 * k)) & 63u;
+        c0 = (int)(e & 7u);
+        c1 = (int)(e >> 3);
+    } else if (kind == kEdgesFaceLoop) {
+        const int g0 = gray2(k), g1 = gray2((k + 1) & 3);
+        c0 = base | ((g0 & 1) << u) | ((g0 >> 1) << v);
+        c1 = base | ((g1 & 1) << u) | ((g1 >> 1) << v);
+    } else {
+        if (k < 8) {
+            const int b = k & 4, kk = k & 3;
+            c0 = b | gray2(kk);
+            c1 = b | gray2((kk + 1) & 3);
+        } else {
+            c0 = gray2(k - 8);
+            c1 = c0 | 4;
+        }
     }
 }
 
 // CapsuleToBox::compute (:409-448) with projectionLineSegOnSide (:450-474),
-// checkEdges/getLineSegments (:476-574), checkOtherCases (:597-755).
-// Returns d_c after the radius is subtracted (or 0 when a point is inside).
+// checkEdges/getLineSegments (:476-574), distanceToMoreLineSegments (:576-595)
+// and checkOtherCases (:597-755).  Returns d_c after the radius is subtracted
+// (or 0 when an endpoint is inside the box).
 template <typename T, typename P>
-__host__ __device__ Val<T> capsule_box(P &pol, const Num<T> &nm, const T *A, const T *B, T radius, const T *o) {
+RPM_HD Val<T> capsule_box(P &pol, const Num<T> &nm, const T *A, const T *B, T radius, const T *o) {
     // ---- projections of A and B on the six faces
-    unsigned proj[2] = {0u, 0u};
-    T dist[2] = {nm.maxd, nm.maxd};
+    unsigned projA = 0u, projB = 0u;
+    T distA = nm.maxd, distB = nm.maxd;
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
         const int u = (c == 0) ? 1 : 0, v = (c == 2) ? 1 : 2;
@@ -427,51 +466,28 @@ __host__ __device__ Val<T> capsule_box(P &pol, const Num<T> &nm, const T *A, con
             auto inr = P::all(P::ge(X[u], o[u]), P::le(X[u], o[3 + u]), P::ge(X[v], o[v]), P::le(X[v], o[3 + v]));
             if (RPM_TAKE(pol, inr)) {
                 if (RPM_TAKE(pol, P::all(P::gt(X[c], o[c]), P::lt(X[c], o[3 + c])))) return Val<T>{T(0), 1.f};
-                if (RPM_TAKE(pol, P::le(X[c], o[c]))) { proj[i] |= 1u << c; dist[i] = o[c] - X[c]; }
-                else if (RPM_TAKE(pol, P::ge(X[c], o[3 + c]))) { proj[i] |= 1u << (3 + c); dist[i] = X[c] - o[3 + c]; }
+                unsigned &pj = i ? projB : projA;
+                T &dj = i ? distB : distA;
+                if (RPM_TAKE(pol, P::le(X[c], o[c]))) { pj |= 1u << c; dj = o[c] - X[c]; }
+                else if (RPM_TAKE(pol, P::ge(X[c], o[3 + c]))) { pj |= 1u << (3 + c); dj = X[c] - o[3 + c]; }
             }
         }
     }
-    Val<T> d{nm.maxd, 1.f};
-    const unsigned any = proj[0] | proj[1];
-    if (any) {
-        const int ip = RPM_TAKE(pol, P::lt(dist[0], dist[1])) ? 0 : 1;
-        d.v = (dist[1] < dist[0]) ? dist[1] : dist[0];
-        if ((proj[0] & proj[1]) == 0u) {   // num_proj == 1: checkEdges with the other point
-            const unsigned pm = proj[ip];
-            int face = -1;
-            if (pm & 1u) face = 0;
-            else if (pm & 8u) face = 3;
-            else if (pm & 2u) face = 1;
-            else if (pm & 16u) face = 4;
-            else if (pm & 4u) face = 2;
-            else if (pm & 32u) face = 5;
-            if (face >= 0) {
-                if (coll_rect(pol, nm, A, B, T(0), o, face)) {
-                    d.v = T(0);
-                } else {
-                    const T *Q = ip ? A : B;
-                    const int c = face > 2 ? face - 3 : face;
-                    const int u = (c == 0) ? 1 : 0, v = (c == 2) ? 1 : 2;
-                    const T p0 = Q[u], p1 = Q[v];
-                    const T min1 = o[u], min2 = o[v], max1 = o[3 + u], max2 = o[3 + v], cv = o[face];
-                    T S[4][3];
-                    int n = 0;
-                    if (RPM_TAKE(pol, P::lt(p0, min1))) { pt3(min1, min2, cv, c, S[0]); pt3(min1, max2, cv, c, S[1]); n = 2; }
-                    else if (RPM_TAKE(pol, P::gt(p0, max1))) { pt3(max1, min2, cv, c, S[0]); pt3(max1, max2, cv, c, S[1]); n = 2; }
-                    if (RPM_TAKE(pol, P::lt(p1, min2))) { pt3(min1, min2, cv, c, S[n]); pt3(max1, min2, cv, c, S[n + 1]); n += 2; }
-                    else if (RPM_TAKE(pol, P::gt(p1, max2))) { pt3(min1, max2, cv, c, S[n]); pt3(max1, max2, cv, c, S[n + 1]); n += 2; }
-                    for (int k = 0; k < n; k += 2) {
-                        Val<T> dt = seg_seg(pol, nm, A, B, S[k], S[k + 1]);
-                        d.ia = fminf(d.ia, dt.ia);
-                        if (dt.v <= T(0)) { d.v = T(0); break; }
-                        if (dt.v < d.v) d.v = dt.v;
-                    }
-                }
-            }
+    // ---- what to evaluate
+    T d = nm.maxd;
+    int rect_face = -1;      // 0..5: checkEdges' rectangle test; 6: all six faces (checkOtherCases)
+    int kind = kEdgesNone, ne = 0, base = 0, fu = 0, fv = 0, point = -1;
+    bool direct = false;     // a single edge whose distance replaces d_c (tie(...) in checkOtherCases)
+    int ip = 0, ce_face = -1;
+    if (projA | projB) {
+        ip = RPM_TAKE(pol, P::lt(distA, distB)) ? 0 : 1;
+        d = (distB < distA) ? distB : distA;
+        if ((projA & projB) == 0u) {   // num_proj == 1: checkEdges with the other point
+            const unsigned pm = ip ? projB : projA;
+            ce_face = (pm & 1u) ? 0 : (pm & 8u) ? 3 : (pm & 2u) ? 1 : (pm & 16u) ? 4 : (pm & 4u) ? 2 : (pm & 32u) ? 5 : -1;
+            rect_face = ce_face;
         }
     } else {
-        // ---- checkOtherCases: classify each axis as below / above / overlapping
         int rg[3];
 #pragma unroll
         for (int c = 0; c < 3; ++c) {
@@ -480,43 +496,85 @@ __host__ __device__ Val<T> capsule_box(P &pol, const Num<T> &nm, const T *A, con
             else rg[c] = 1;
         }
         const int mids = (rg[0] == 1) + (rg[1] == 1) + (rg[2] == 1);
-        int base = 0;
-#pragma unroll
-        for (int c = 0; c < 3; ++c) if (rg[c] == 2) base |= 1 << c;
+        base = (rg[0] == 2 ? 1 : 0) | (rg[1] == 2 ? 2 : 0) | (rg[2] == 2 ? 4 : 0);
         if (mids == 0) {
-            T Cc[3];
-            corner(o, base, Cc);
-            d.v = seg_point(pol, nm, A, B, Cc);
+            point = base;
         } else if (mids == 1) {
             const int k = (rg[0] == 1) ? 0 : (rg[1] == 1 ? 1 : 2);
-            T Cc[3], Dd[3];
-            corner(o, base, Cc);
-            corner(o, base | (1 << k), Dd);
-            d = seg_seg(pol, nm, A, B, Cc, Dd);
+            kind = kEdgesList; ne = 1; direct = true;
+            const uint32_t c0 = (uint32_t)base, c1 = (uint32_t)(base | (1 << k));
+            fu = (int)(c0 | (c1 << 3));
         } else if (mids == 2) {
             const int f = (rg[0] != 1) ? 0 : (rg[1] != 1 ? 1 : 2);
-            const int u = (f == 0) ? 1 : 0, v = (f == 2) ? 1 : 2;
-            const int s = base & (1 << f);
-            uint8_t e[8];
-            const int cu[4] = {0, 1, 1, 0}, cv[4] = {0, 0, 1, 1};
-#pragma unroll
-            for (int q = 0; q < 4; ++q) {
-                e[2 * q] = (uint8_t)(s | (cu[q] << u) | (cv[q] << v));
-                e[2 * q + 1] = (uint8_t)(s | (cu[(q + 1) & 3] << u) | (cv[(q + 1) & 3] << v));
-            }
-            more_edges(pol, nm, A, B, o, e, 4, d);
+            kind = kEdgesFaceLoop; ne = 4;
+            fu = (f == 0) ? 1 : 0;
+            fv = (f == 2) ? 1 : 2;
         } else {
-            for (int kk = 0; kk < 6; ++kk)
-                if (coll_rect(pol, nm, A, B, T(0), o, kk)) { d.v = T(0); return Val<T>{T(0) - radius, d.ia}; }
-            {
-                uint8_t e[24];
-                for (int k = 0; k < 24; ++k) e[k] = edge12(k);
-                more_edges(pol, nm, A, B, o, e, 12, d);
-            }
+            rect_face = 6;
+            kind = kEdgesAll12; ne = 12;
         }
     }
-    d.v = d.v - radius;
-    return d;
+    uint32_t list = (kind == kEdgesList) ? (uint32_t)fu : 0u;
+    // ---- rectangle tests (radius 0)
+    bool crossed = false;
+    if (rect_face >= 0) {
+        const int f0 = rect_face == 6 ? 0 : rect_face, f1 = rect_face == 6 ? 6 : rect_face + 1;
+#pragma unroll 1
+        for (int f = f0; f < f1; ++f) {
+            const RB rr = coll_rect_call<T, P>(nm, A, B, T(0), o, f);
+            RPM_NOTE(pol, rr.m);
+            if (rr.v) { crossed = true; break; }
+        }
+        if (crossed) {
+            d = T(0);
+            kind = kEdgesNone; ne = 0;
+        } else if (ce_face >= 0) {
+            // getLineSegments (:542-574): edges of the projected face facing the other point
+            const T *Q = ip ? A : B;
+            const int c = ce_face > 2 ? ce_face - 3 : ce_face;
+            const int u = (c == 0) ? 1 : 0, v = (c == 2) ? 1 : 2;
+            const int fb = (ce_face > 2 ? 1 : 0) << c;
+            const T qu = sel3(Q, u), qv = sel3(Q, v);
+            kind = kEdgesList; ne = 0; list = 0u;
+            int us = -1, vs = -1;
+            if (RPM_TAKE(pol, P::lt(qu, sel6(o, u)))) us = 0;
+            else if (RPM_TAKE(pol, P::gt(qu, sel6(o, u + 3)))) us = 1;
+            if (RPM_TAKE(pol, P::lt(qv, sel6(o, v)))) vs = 0;
+            else if (RPM_TAKE(pol, P::gt(qv, sel6(o, v + 3)))) vs = 1;
+            if (us >= 0) {   // u fixed, v from min to max
+                const uint32_t c0 = (uint32_t)(fb | (us << u)), c1 = c0 | (1u << v);
+                list |= (c0 | (c1 << 3)) << (6 * ne);
+                ++ne;
+            }
+            if (vs >= 0) {   // v fixed, u from min to max
+                const uint32_t c0 = (uint32_t)(fb | (vs << v)), c1 = c0 | (1u << u);
+                list |= (c0 | (c1 << 3)) << (6 * ne);
+                ++ne;
+            }
+            // no edge leaves the reference's 3x2 matrix uninitialised (undefined);
+            // that needs the segment to meet the face exactly on its border
+        }
+    }
+    // ---- point (one axis class per coordinate, no overlap): distanceLineSegToPoint
+    if (point >= 0) {
+        T Cc[3];
+        corner(o, point, Cc);
+        d = seg_point(pol, nm, A, B, Cc);
+    }
+    // ---- box edges
+#pragma unroll 1
+    for (int k = 0; k < ne; ++k) {
+        int c0, c1;
+        edge_of(kind, list, base, fu, fv, k, c0, c1);
+        T Cc[3], Dd[3];
+        corner(o, c0, Cc);
+        corner(o, c1, Dd);
+        const T dt = seg_seg(pol, nm, A, B, Cc, Dd).v;
+        if (direct) { d = dt; break; }
+        if (dt <= T(0)) { d = T(0); break; }
+        if (dt < d) d = dt;
+    }
+    return Val<T>{d - radius, 1.f};
 }
 
 // Lower bound of the segment-box distance: the gap between the box and the

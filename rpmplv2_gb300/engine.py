@@ -57,6 +57,9 @@ def load(build_if_missing=False):
     L.rpm_skeleton.argtypes = [_vp, _i32, _i32, _vp, _i64, _vp, _vp]
     L.rpm_last_stats.argtypes = [_vp, _vp, ctypes.POINTER(CheckStats)]
     L.rpm_sync.argtypes = [_vp, _vp]
+    L.rpm_ctx_set_timing.argtypes = [_vp, ctypes.c_int]
+    L.rpm_last_timing.argtypes = [_vp, _vp, ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_float)]
+    L.rpm_probe_fp32_peak.argtypes = [_vp, ctypes.POINTER(ctypes.c_double)]
     _LIB = L
     return L
 
@@ -146,6 +149,19 @@ class Engine:
         return {"configs": s.configs, "rechecked": s.rechecked, "overflow": s.overflow,
                 "device_status": s.device_status}
 
+    def set_timing(self, enable=True):
+        _check(self.lib.rpm_ctx_set_timing(self.ctx, 1 if enable else 0))
+
+    def last_timing(self, stream=None):
+        a, b = ctypes.c_float(), ctypes.c_float()
+        _check(self.lib.rpm_last_timing(self.ctx, stream, ctypes.byref(a), ctypes.byref(b)))
+        return a.value, b.value
+
+    def fp32_peak_tflops(self):
+        t = ctypes.c_double()
+        _check(self.lib.rpm_probe_fp32_peak(self.ctx, ctypes.byref(t)))
+        return t.value
+
     def sync(self, stream=None):
         _check(self.lib.rpm_sync(self.ctx, stream))
 
@@ -175,4 +191,5 @@ ABI_SYMBOLS = [
     "rpm_last_error_string", "rpm_version", "rpm_ctx_create", "rpm_ctx_destroy", "rpm_ctx_set_params",
     "rpm_robot_upload", "rpm_scene_create", "rpm_scene_update", "rpm_scene_destroy", "rpm_scene_info",
     "rpm_box_aabb", "rpm_check_configs", "rpm_check_configs_host", "rpm_skeleton", "rpm_last_stats", "rpm_sync",
+    "rpm_ctx_set_timing", "rpm_last_timing", "rpm_probe_fp32_peak",
 ]
