@@ -171,6 +171,25 @@ int rpm_last_timing(rpm_ctx *ctx, void *stream, float *bulk_ms, float *recheck_m
  * chains: the denominator of the FP32 roofline. */
 int rpm_probe_fp32_peak(rpm_ctx *ctx, double *tflops);
 
+/* The FP32 + FP64-recheck check of rpm_check_configs for callers that cannot
+ * allocate device memory (a CUDA graph being captured by someone else, a
+ * real-time loop that forbids allocator calls after start-up, a framework that
+ * owns all device memory).  No counterpart in the reference: it adds a calling
+ * convention, not a reference operation.  Everything is passed in: the robot
+ * as a host descriptor, obstacles as the caller's device arrays (aabb_dev n x 6
+ * floats as in rpm_scene_create, min_dist_tol_dev and flags_dev nullable),
+ * configurations and outputs as device pointers.  It calls no cudaMalloc,
+ * cudaFree or allocating library routine; its scratch (the recheck list) is a
+ * static device array of 65,536 entries (~512 KB held on every GPU that loads
+ * the library), so num_configs above 65,536 returns RPM_ERR_RANGE.  The first
+ * call on each device looks up the array's address and should come before any
+ * stream capture.  All calls share the array: calls that overlap on the GPU
+ * race and must be serialised by the caller. */
+int rpm_check_configs_noalloc(const rpm_robot_desc *robot, const float *aabb_dev, const float *min_dist_tol_dev,
+                              const uint8_t *flags_dev, int32_t n, const rpm_params *params, const float *q_dev,
+                              int64_t num_configs, uint8_t *valid_dev, double *dist_dev, float *profile_dev,
+                              void *stream);
+
 /* Synchronise a stream and report any device-side error status. */
 int rpm_sync(rpm_ctx *ctx, void *stream);
 

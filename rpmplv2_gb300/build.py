@@ -1,7 +1,7 @@
 """Builds the CUDA library librpm_gb300.so in-tree for sm_103a.
 
-rpm_exact.cu is compiled with --fmad=false (no contracted multiply-add, so the
-exact forms round like the CPU restatement); rpm_fast.cu and rpm_api.cu with
+rpm_exact.cu and rpm_noalloc.cu are compiled with --fmad=false (no contracted
+multiply-add, so the exact forms round like the CPU restatement); rpm_fast.cu and rpm_api.cu with
 the default contraction.  Translation units compile in parallel.
 """
 import concurrent.futures as cf
@@ -14,7 +14,8 @@ OUT_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT_DIR, "librpm_gb300.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off"]
-UNITS = {"rpm_exact.cu": ["--fmad=false"], "rpm_fast.cu": ["--fmad=true"], "rpm_api.cu": []}
+UNITS = {"rpm_exact.cu": ["--fmad=false"], "rpm_fast.cu": ["--fmad=true"], "rpm_api.cu": [],
+         "rpm_noalloc.cu": ["--fmad=false"]}
 
 
 def _deps():

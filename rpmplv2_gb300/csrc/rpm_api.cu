@@ -177,6 +177,10 @@ int get_scratch(rpm_ctx *ctx, cudaStream_t st, int64_t need, Scratch **out) {
     return RPM_OK;
 }
 
+}  // namespace
+
+namespace rpm {
+int set_error(int code, const char *msg) { return fail(code, "%s", msg); }
 int build_dev_robot(const rpm_robot_desc &d, DevRobot &r) {
     if (d.kind != RPM_ROBOT_CHAIN && d.kind != RPM_ROBOT_XARM6) return fail(RPM_ERR_INVALID, "unknown robot kind %d", d.kind);
     if (d.num_dofs < 1 || d.num_dofs > RPM_MAX_DOF) return fail(RPM_ERR_INVALID, "num_dofs %d out of range", d.num_dofs);
@@ -214,6 +218,9 @@ int build_dev_robot(const rpm_robot_desc &d, DevRobot &r) {
     r.grip03_f = (float)(0.3 * (double)d.gripper_length);
     return RPM_OK;
 }
+}  // namespace rpm
+
+namespace {
 
 SceneRec *find_scene(rpm_ctx *ctx, int id) {
     auto it = ctx->scenes.find(id);

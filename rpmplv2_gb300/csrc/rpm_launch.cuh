@@ -22,6 +22,10 @@ struct KParams {
     int32_t *status;
 };
 
+// Host helpers shared by the C ABI translation units (rpm_api.cu).
+int build_dev_robot(const rpm_robot_desc &d, DevRobot &r);   // RPM_OK or an error code (message set)
+int set_error(int code, const char *msg);                     // records the thread's error string
+
 // Dynamic shared memory of one CTA: robot + obstacle rows of its scene.
 size_t smem_bytes(int mode, int n_pad);
 

@@ -60,6 +60,8 @@ def load(build_if_missing=False):
     L.rpm_ctx_set_timing.argtypes = [_vp, ctypes.c_int]
     L.rpm_last_timing.argtypes = [_vp, _vp, ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_float)]
     L.rpm_probe_fp32_peak.argtypes = [_vp, ctypes.POINTER(ctypes.c_double)]
+    L.rpm_check_configs_noalloc.argtypes = [_vp, _vp, _vp, _vp, _i32, ctypes.POINTER(Params), _vp, _i64, _vp, _vp,
+                                            _vp, _vp]
     _LIB = L
     return L
 
@@ -191,5 +193,5 @@ ABI_SYMBOLS = [
     "rpm_last_error_string", "rpm_version", "rpm_ctx_create", "rpm_ctx_destroy", "rpm_ctx_set_params",
     "rpm_robot_upload", "rpm_scene_create", "rpm_scene_update", "rpm_scene_destroy", "rpm_scene_info",
     "rpm_box_aabb", "rpm_check_configs", "rpm_check_configs_host", "rpm_skeleton", "rpm_last_stats", "rpm_sync",
-    "rpm_ctx_set_timing", "rpm_last_timing", "rpm_probe_fp32_peak",
+    "rpm_ctx_set_timing", "rpm_last_timing", "rpm_probe_fp32_peak", "rpm_check_configs_noalloc",
 ]

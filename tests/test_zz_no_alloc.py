@@ -1,0 +1,70 @@
+"""rpm_check_configs_noalloc against rpm_check_configs.
+
+The no-allocation entry point serves callers that cannot call cudaMalloc (for
+example code running under someone else's CUDA-graph capture, or a real-time
+loop that forbids allocator calls after start-up).  It keeps its recheck list
+in a static device array shared by every call, so this test makes two calls in
+a row on different inputs and checks each against the allocating entry point
+with the FP32 + FP64-recheck tolerance of the parity tests: isValid identical,
+distances within 1e-5 m.  The file name makes pytest collect it last.
+"""
+import ctypes
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def _noalloc(lib, robot, scene_dev, q, valid, dist, prof):
+    import torch
+    from rpmplv2_gb300._abi import Params
+    aabb, tol, flags, n = scene_dev
+    params = Params(1e-4, 1000.0)
+    rc = lib.rpm_check_configs_noalloc(ctypes.addressof(robot.desc), aabb.data_ptr(), tol.data_ptr(), flags.data_ptr(),
+                                       n, ctypes.byref(params), q.data_ptr(), q.shape[0], valid.data_ptr(),
+                                       dist.data_ptr(), prof.data_ptr(), None)
+    assert rc == 0, lib.rpm_last_error_string().decode()
+    torch.cuda.synchronize()
+
+
+def test_noalloc_matches_allocating_entry_point():
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    from rpmplv2_gb300 import scenes
+    from rpmplv2_gb300.engine import Engine
+
+    eng = Engine(0)
+    lib = eng.lib
+    for seed in (21, 22):   # two calls in a row share the static scratch array
+        robot, scene, q = scenes.xarm6_workload(40000, seed=seed)
+        C, L = q.shape[0], robot.num_links
+        rid = eng.upload_robot(robot)
+        sid = eng.create_scene(rid, scene)
+        qd = torch.from_numpy(q).cuda()
+        v_ref = torch.zeros(C, dtype=torch.uint8, device="cuda")
+        d_ref = torch.zeros(C, dtype=torch.float64, device="cuda")
+        p_ref = torch.zeros((C, L), dtype=torch.float32, device="cuda")
+        eng.check_configs(sid, qd, "fp32_recheck", v_ref, d_ref, p_ref)
+        eng.sync()
+        scene_dev = (torch.from_numpy(scene.aabb).cuda(), torch.from_numpy(scene.tol).cuda(),
+                     torch.from_numpy(scene.flags).cuda(), scene.n)
+        v = torch.full((C,), 7, dtype=torch.uint8, device="cuda")
+        d = torch.full((C,), -1.0, dtype=torch.float64, device="cuda")
+        p = torch.full((C, L), -1.0, dtype=torch.float32, device="cuda")
+        _noalloc(lib, robot, scene_dev, qd, v, d, p)
+        assert torch.equal(v, v_ref), "isValid differs in %d configurations" % int((v != v_ref).sum())
+        assert float((d - d_ref).abs().max()) <= 1e-5
+        assert float((p - p_ref).abs().max()) <= 1e-5
+        eng.destroy_scene(sid)
+    # sizes beyond the static array's capacity are rejected, not truncated
+    big = torch.zeros((65537, 6), dtype=torch.float32, device="cuda")
+    out_v = torch.zeros(65537, dtype=torch.uint8, device="cuda")
+    from rpmplv2_gb300._abi import Params, RPM_ERR_RANGE
+    rc = lib.rpm_check_configs_noalloc(ctypes.addressof(robot.desc), scene_dev[0].data_ptr(), None, None, scene.n,
+                                       ctypes.byref(Params(1e-4, 1000.0)), big.data_ptr(), 65537, out_v.data_ptr(),
+                                       None, None, None)
+    assert rc == RPM_ERR_RANGE
+    assert b"65536" in lib.rpm_last_error_string()
+    eng.close()
