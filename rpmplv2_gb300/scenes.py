@@ -11,10 +11,13 @@ generators produce the same kinds of scenes with fixed seeds:
                              (0, 0, 0.267) rejected if they touch q = 0,
                              1,048,576 configs in [-pi, pi]^6
 * ``spatial10_edge_workload`` spatial_10dof (r 0.03), 200 rotated boxes turned
-                             into fcl world AABBs, 262,144 edges discretised
-                             at 0.05 rad
+                             into fcl world AABBs in a 1.2 m ball around the
+                             spatial scenarios' WS_center (0, 0, 0.1), rejected
+                             if they touch q = 0; 262,144 edges discretised at
+                             0.05 rad
 * ``mixed_dof_workload``     spatial 14/18/22 (r 0.03), 500 AABBs in a 1.5 m
-                             ball, 32,768/49,152/49,152 configs
+                             ball around WS_center, rejected if they touch
+                             q = 0; 32,768/49,152/49,152 configs
 
 Every array is float32 (the reference's State coordinates are
 Eigen::VectorXf, include/state_spaces/State.h:27).
@@ -131,9 +134,17 @@ def xarm6_workload(num_configs=1 << 20, num_obstacles=50, seed=1, gripper_length
     return robot, scene, q
 
 
-def random_obb_scene(rng, n, dim_lo, dim_hi, center, radius, rotated=True):
+SPATIAL_WS_CENTER = (0.0, 0.0, 0.1)   # WS_center of the spatial scenarios (data/spatial_10dof/*/*.yaml)
+
+
+def random_obb_scene(rng, n, dim_lo, dim_hi, center, radius, rotated=True, reject_robot=None):
+    """n boxes with dims U[dim_lo, dim_hi], centres uniform in a ball, as fcl
+    world AABBs.  Like the reference's generator (which drops obstacles that
+    make the start configuration invalid), boxes touching reject_robot at
+    q = 0 are redrawn."""
     boxes = []
-    for _ in range(n):
+    q0 = None if reject_robot is None else np.zeros(reject_robot.num_dofs)
+    while len(boxes) < n:
         dim = rng.uniform(dim_lo, dim_hi, 3)
         c = _ball(rng, 1, center, radius)[0]
         if rotated:
@@ -141,14 +152,17 @@ def random_obb_scene(rng, n, dim_lo, dim_hi, center, radius, rotated=True):
             qv = qv / np.linalg.norm(qv)
         else:
             qv = np.array([0.0, 0.0, 0.0, 1.0])
-        boxes.append(box_aabb(dim, c, qv))
+        box = box_aabb(dim, c, qv)
+        if q0 is not None and touches(reject_robot, q0, box):
+            continue
+        boxes.append(box)
     return Scene(np.array(boxes))
 
 
 def spatial10_edge_workload(num_edges=1 << 18, seed=2, step=0.05):
     rng = np.random.default_rng(seed)
     robot = _robots.spatial(10, radius=0.03)
-    scene = random_obb_scene(rng, 200, 0.02, 0.1, (0.0, 0.0, 0.0), 1.2, rotated=True)
+    scene = random_obb_scene(rng, 200, 0.02, 0.1, SPATIAL_WS_CENTER, 1.2, rotated=True, reject_robot=robot)
     q1 = uniform_configs(rng, num_edges, 10)
     u = rng.normal(size=(num_edges, 10))
     u /= np.linalg.norm(u, axis=1, keepdims=True)
@@ -159,7 +173,8 @@ def spatial10_edge_workload(num_edges=1 << 18, seed=2, step=0.05):
 
 def mixed_dof_workload(counts=(32768, 49152, 49152), seed=3):
     rng = np.random.default_rng(seed)
-    scene = random_obb_scene(rng, 500, 0.02, 0.15, (0.0, 0.0, 0.0), 1.5, rotated=False)
+    scene = random_obb_scene(rng, 500, 0.02, 0.15, SPATIAL_WS_CENTER, 1.5, rotated=False,
+                             reject_robot=_robots.spatial(22, radius=0.03))
     parts = []
     for dofs, n in zip((14, 18, 22), counts):
         robot = _robots.spatial(dofs, radius=0.03)
