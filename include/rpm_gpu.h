@@ -145,11 +145,45 @@ int rpm_box_aabb(const float dim[3], const float pos[3], const float quat_xyzw[4
 int rpm_check_configs(rpm_ctx *ctx, int32_t scene_id, int32_t precision, const float *q_dev, int64_t num_configs,
                       uint8_t *valid_dev, double *dist_dev, float *profile_dev, void *stream);
 
+/* Several scenes (and robots of different DOF) in one launch: item k checks
+ * num_configs configurations of its own scene (BASELINE-style mixed-DOF
+ * batches, serving batches).  Same outputs as rpm_check_configs per item. */
+typedef struct rpm_batch_item {
+    int32_t scene_id;
+    int32_t reserved;
+    const float *q_dev;       /* num_configs x D of the scene's robot */
+    int64_t num_configs;
+    uint8_t *valid_dev;       /* nullable */
+    double *dist_dev;         /* nullable */
+    float *profile_dev;       /* nullable, num_configs x L */
+} rpm_batch_item;
+int rpm_check_batch(rpm_ctx *ctx, int32_t precision, const rpm_batch_item *items, int32_t n_items, void *stream);
+
 /* Same as rpm_check_configs with host buffers: stages through context-owned
  * pinned memory, overlaps copies with compute and returns after the results
  * are in the host buffers. */
 int rpm_check_configs_host(rpm_ctx *ctx, int32_t scene_id, int32_t precision, const float *q_host, int64_t num_configs,
                            uint8_t *valid_host, double *dist_host, float *profile_host);
+
+/* RealVectorSpace::isValid(q1, q2) (RealVectorSpace.cpp:261-275) for a batch
+ * of edges (q1_dev, q2_dev: E x D).  With step > 0 edge e is checked at
+ * n_e = max(1, ceil(|q1 - q2| / step)) points, otherwise at num_checks points
+ * (NUM_INTERPOLATION_VALIDITY_CHECKS); points run from q2 towards q1 as in the
+ * reference and q1 itself is not checked.  valid_dev[e] = isValid(q1, q2);
+ * checks_dev[e] (nullable) = the number of checks the reference evaluates
+ * before its early exit.  Runs as a persistent work-queue kernel; with
+ * rpm_ctx_set_graphs enabled, repeated calls with the same arguments replay
+ * a captured CUDA graph of the whole pipeline. */
+int rpm_check_edges(rpm_ctx *ctx, int32_t scene_id, int32_t precision, const float *q1_dev, const float *q2_dev,
+                    int64_t num_edges, float step, int32_t num_checks, uint8_t *valid_dev, int32_t *checks_dev,
+                    void *stream);
+int rpm_ctx_set_graphs(rpm_ctx *ctx, int enable);
+/* Times the edge pipeline on the given batch for several persistent-grid
+ * sizes (CTAs per SM) and keeps the fastest for this scene's robot and
+ * precision; *ctas_out receives it.  rpm_set_edge_ctas sets it directly. */
+int rpm_autotune_edges(rpm_ctx *ctx, int32_t scene_id, int32_t precision, const float *q1_dev, const float *q2_dev,
+                       int64_t num_edges, float step, int32_t num_checks, uint8_t *valid_dev, int32_t *ctas_out);
+int rpm_set_edge_ctas(rpm_ctx *ctx, int32_t scene_id, int32_t precision, int32_t ctas_per_sm);
 
 /* Skeleton points (L+1 points x 3) per configuration, widened to double
  * (computeSkeleton; xArm6.cpp:209-235, Planar2DOF.cpp:117-130): RPM_PREC_FP64

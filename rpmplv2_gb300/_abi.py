@@ -50,3 +50,15 @@ class CheckStats(ctypes.Structure):
         ("device_status", ctypes.c_int32),
         ("pad", ctypes.c_int32),
     ]
+
+
+class BatchItem(ctypes.Structure):
+    _fields_ = [
+        ("scene_id", ctypes.c_int32),
+        ("reserved", ctypes.c_int32),
+        ("q_dev", ctypes.c_void_p),
+        ("num_configs", ctypes.c_int64),
+        ("valid_dev", ctypes.c_void_p),
+        ("dist_dev", ctypes.c_void_p),
+        ("profile_dev", ctypes.c_void_p),
+    ]

@@ -14,6 +14,7 @@
 #include <string>
 #include <vector>
 
+#include "rpm_edges.cuh"
 #include "rpm_launch.cuh"
 
 using namespace rpm;
@@ -70,6 +71,17 @@ struct Scratch {
     int64_t last_configs = 0;
     cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};   // bulk start, bulk end / recheck start, recheck end
     bool timed = false, had_recheck = false;
+    // edge checks
+    size_t ecap = 0;
+    int32_t *n_e = nullptr, *local = nullptr, *kmax = nullptr;
+    int64_t *bprefix = nullptr;
+    uint8_t *full = nullptr;
+    unsigned long long *work = nullptr;
+    uint64_t *erecheck = nullptr;
+    size_t erecheck_cap = 0;
+    // cached CUDA graphs of edge calls, keyed by their arguments
+    struct Graph { std::vector<uint64_t> key; cudaGraphExec_t exec; };
+    std::vector<Graph> graphs;
 };
 
 }  // namespace
@@ -92,6 +104,8 @@ struct rpm_ctx {
     float *hp[2] = {nullptr, nullptr};
     size_t hcap_cfg = 0, hcap_prof = 0;
     bool timing = false;
+    bool use_graphs = false;
+    std::map<std::pair<int, int>, int> edge_ctas;   // (robot, precision) -> CTAs per SM of the edge kernel
 };
 
 namespace {
@@ -227,60 +241,138 @@ SceneRec *find_scene(rpm_ctx *ctx, int id) {
     return it == ctx->scenes.end() ? nullptr : it->second;
 }
 
-// Queue one check of C configurations on 'st'; the caller holds ctx->mu.
-int enqueue_check(rpm_ctx *ctx, SceneRec *s, int prec, const float *q, int64_t C, uint8_t *valid, double *dist,
-                  float *profile, cudaStream_t st) {
-    const RobotRec &rb = ctx->robots[s->robot];
-    SceneBuf &buf = s->bufs[s->cur];
-    KParams p;
-    std::memset(&p, 0, sizeof p);
-    p.nseg = 1;
-    Seg &g = p.segs[0];
-    g.robot = rb.dev;
-    g.obs_f = buf.f;
-    g.obs_d = buf.d;
-    g.q = q;
-    g.valid = valid;
-    g.dist = dist;
-    g.profile = profile;
-    g.count = C;
-    g.first_block = 0;
-    g.n = s->n;
-    g.n_pad = s->n_pad;
-    p.nmd.eq = ctx->params.equality_threshold;
-    p.nmd.maxd = ctx->params.max_distance;
-    p.nmf.eq = (float)ctx->params.equality_threshold;
-    p.nmf.maxd = (float)ctx->params.max_distance;
+// One segment of a launch: a scene and its configurations / outputs.
+struct SegReq {
+    SceneRec *scene;
+    const float *q;
+    int64_t count;
+    uint8_t *valid;
+    double *dist;
+    float *profile;
+};
+
+// Queue checks of up to kMaxSegs segments as one launch on 'st' (more
+// segments become several launches).  The caller holds ctx->mu.
+int enqueue_segments(rpm_ctx *ctx, int prec, const std::vector<SegReq> &reqs, cudaStream_t st) {
+    int64_t total = 0;
+    for (const SegReq &r : reqs) total += r.count;
     Scratch *sc = nullptr;
-    int rc = get_scratch(ctx, st, prec == RPM_PREC_FP32_RECHECK ? C : 0, &sc);
+    int rc = get_scratch(ctx, st, prec == RPM_PREC_FP32_RECHECK ? total : 0, &sc);
     if (rc) return rc;
-    p.recheck = sc->recheck;
-    p.recheck_count = sc->counters;
-    p.status = sc->status;
-    sc->last_configs = C;
-    const int64_t blocks = (C + kThreads - 1) / kThreads;
+    sc->last_configs = total;
     CK(cudaMemsetAsync(sc->counters, 0, sizeof(uint32_t), st));
-    sc->timed = ctx->timing && blocks > 0;
+    sc->timed = ctx->timing && total > 0;
     sc->had_recheck = prec == RPM_PREC_FP32_RECHECK;
     if (sc->timed && !sc->ev[0])
         for (int i = 0; i < 3; ++i) CK(cudaEventCreate(&sc->ev[i]));
-    if (blocks > 0) {
-        if (sc->timed) CK(cudaEventRecord(sc->ev[0], st));
-        if (prec == RPM_PREC_FP32_RECHECK) {
-            CK(launch_check_fp32(p, blocks, smem_bytes(RPM_PREC_FP32_REF, s->n_pad), st));
-            if (sc->timed) CK(cudaEventRecord(sc->ev[1], st));
-            CK(launch_recheck(p, ctx->num_sms * 4, st));
-        } else {
-            CK(launch_check_exact(prec, p, blocks, smem_bytes(prec, s->n_pad), st));
-            if (sc->timed) CK(cudaEventRecord(sc->ev[1], st));
+    if (sc->timed) CK(cudaEventRecord(sc->ev[0], st));
+    std::vector<SceneBuf *> used;
+    for (size_t off = 0; off < reqs.size(); off += kMaxSegs) {
+        KParams p;
+        std::memset(&p, 0, sizeof p);
+        int64_t blocks = 0;
+        int max_pad = 16;
+        for (size_t k = off; k < reqs.size() && k < off + kMaxSegs; ++k) {
+            const SegReq &r = reqs[k];
+            SceneBuf &buf = r.scene->bufs[r.scene->cur];
+            used.push_back(&buf);
+            Seg &g = p.segs[p.nseg++];
+            g.robot = ctx->robots[r.scene->robot].dev;
+            g.obs_f = buf.f;
+            g.obs_d = buf.d;
+            g.q = r.q;
+            g.valid = r.valid;
+            g.dist = r.dist;
+            g.profile = r.profile;
+            g.count = r.count;
+            g.first_block = blocks;
+            g.n = r.scene->n;
+            g.n_pad = r.scene->n_pad;
+            blocks += (r.count + kThreads - 1) / kThreads;
+            max_pad = std::max(max_pad, r.scene->n_pad);
         }
-        if (sc->timed) CK(cudaEventRecord(sc->ev[2], st));
+        p.nmd.eq = ctx->params.equality_threshold;
+        p.nmd.maxd = ctx->params.max_distance;
+        p.nmf.eq = (float)ctx->params.equality_threshold;
+        p.nmf.maxd = (float)ctx->params.max_distance;
+        p.recheck = sc->recheck;
+        p.recheck_count = sc->counters;
+        p.status = sc->status;
+        if (blocks == 0) continue;
+        if (prec == RPM_PREC_FP32_RECHECK) {
+            CK(launch_check_fp32(p, blocks, smem_bytes(RPM_PREC_FP32_REF, max_pad), st));
+            if (sc->timed && off + kMaxSegs >= reqs.size()) CK(cudaEventRecord(sc->ev[1], st));
+            CK(launch_recheck(p, ctx->num_sms * 4, st));
+            // the recheck list is consumed per launch
+            if (off + kMaxSegs < reqs.size()) CK(cudaMemsetAsync(sc->counters, 0, sizeof(uint32_t), st));
+        } else {
+            CK(launch_check_exact(prec, p, blocks, smem_bytes(prec, max_pad), st));
+            if (sc->timed && off + kMaxSegs >= reqs.size()) CK(cudaEventRecord(sc->ev[1], st));
+        }
     }
-    prune_users(ctx, buf);
-    cudaEvent_t e = get_event(ctx);
-    CK(cudaEventRecord(e, st));
-    buf.users.push_back(e);
+    if (sc->timed) CK(cudaEventRecord(sc->ev[2], st));
+    for (SceneBuf *b : used) {
+        prune_users(ctx, *b);
+        cudaEvent_t e = get_event(ctx);
+        CK(cudaEventRecord(e, st));
+        b->users.push_back(e);
+    }
     return RPM_OK;
+}
+
+int edge_scratch(rpm_ctx *ctx, Scratch *sc, int64_t E, cudaStream_t st) {
+    if ((int64_t)sc->ecap >= E && sc->work) return RPM_OK;
+    CK(cudaStreamSynchronize(st));
+    for (auto &g : sc->graphs) cudaGraphExecDestroy(g.exec);
+    sc->graphs.clear();
+    cudaFree(sc->n_e); cudaFree(sc->local); cudaFree(sc->kmax); cudaFree(sc->bprefix); cudaFree(sc->full);
+    cudaFree(sc->work); cudaFree(sc->erecheck);
+    const size_t cap = std::max<size_t>((size_t)E, 1u << 12);
+    const size_t nb = cap / kEdgeScanBlock + 2;
+    sc->erecheck_cap = 4 * cap + (1u << 16);
+    if (cudaMalloc(&sc->n_e, cap * 4) || cudaMalloc(&sc->local, cap * 4) || cudaMalloc(&sc->kmax, cap * 4) ||
+        cudaMalloc(&sc->bprefix, nb * 8) || cudaMalloc(&sc->full, cap) || cudaMalloc(&sc->work, 64) ||
+        cudaMalloc(&sc->erecheck, sc->erecheck_cap * 8))
+        return fail(RPM_ERR_NOMEM, "edge scratch allocation failed");
+    sc->ecap = cap;
+    (void)ctx;
+    return RPM_OK;
+}
+
+// Queue the edge pipeline (counts + scan, persistent checks, recheck, final).
+int enqueue_edges(rpm_ctx *ctx, Scratch *sc, SceneRec *s, int prec, const float *q1, const float *q2, int64_t E,
+                  float step, int32_t num_checks, uint8_t *valid, int32_t *checks, int ctas_per_sm, cudaStream_t st) {
+    SceneBuf &buf = s->bufs[s->cur];
+    EdgeParams p;
+    std::memset(&p, 0, sizeof p);
+    p.seg.robot = ctx->robots[s->robot].dev;
+    p.seg.obs_f = buf.f;
+    p.seg.obs_d = buf.d;
+    p.seg.n = s->n;
+    p.seg.n_pad = s->n_pad;
+    p.q1 = q1; p.q2 = q2; p.E = E; p.step = step; p.num_checks = num_checks;
+    p.n_e = sc->n_e; p.local = sc->local; p.bprefix = sc->bprefix; p.kmax = sc->kmax; p.work = sc->work;
+    p.full = sc->full;
+    p.recheck = sc->erecheck;
+    p.recheck_cap = (uint32_t)std::min<size_t>(sc->erecheck_cap, 0xffffffffu);
+    p.recheck_count = sc->counters;
+    p.overflow = sc->counters + 1;
+    p.valid = valid; p.checks_out = checks; p.status = sc->status;
+    p.nmd.eq = ctx->params.equality_threshold; p.nmd.maxd = ctx->params.max_distance;
+    p.nmf.eq = (float)ctx->params.equality_threshold; p.nmf.maxd = (float)ctx->params.max_distance;
+    CK(cudaMemsetAsync(sc->counters, 0, 2 * sizeof(uint32_t), st));
+    if (E == 0) return RPM_OK;
+    CK(launch_edge_prep(p, st));
+    const int grid = ctx->num_sms * std::max(1, ctas_per_sm);
+    if (prec == RPM_PREC_FP32_RECHECK) CK(launch_edges_fp32(p, grid, smem_bytes(RPM_PREC_FP32_REF, s->n_pad), st));
+    else CK(launch_edges(prec, p, grid, smem_bytes(prec, s->n_pad), st));
+    CK(launch_edge_recheck_final(p, ctx->num_sms * 4, st));
+    return RPM_OK;
+}
+
+int enqueue_check(rpm_ctx *ctx, SceneRec *s, int prec, const float *q, int64_t C, uint8_t *valid, double *dist,
+                  float *profile, cudaStream_t st) {
+    return enqueue_segments(ctx, prec, {SegReq{s, q, C, valid, dist, profile}}, st);
 }
 
 }  // namespace
@@ -316,6 +408,10 @@ int rpm_ctx_destroy(rpm_ctx *ctx) {
     }
     for (auto &r : ctx->robots) cudaFree(r.dev);
     for (auto &kv : ctx->scratch) {
+        for (auto &g : kv.second->graphs) cudaGraphExecDestroy(g.exec);
+        cudaFree(kv.second->n_e); cudaFree(kv.second->local); cudaFree(kv.second->kmax);
+        cudaFree(kv.second->bprefix); cudaFree(kv.second->full); cudaFree(kv.second->work);
+        cudaFree(kv.second->erecheck);
         cudaFree(kv.second->recheck);
         cudaFree(kv.second->counters);
         cudaFree(kv.second->status);
@@ -457,6 +553,142 @@ int rpm_check_configs(rpm_ctx *ctx, int32_t scene_id, int32_t precision, const f
     return enqueue_check(ctx, s, precision, q_dev, num_configs, valid_dev, dist_dev, profile_dev, (cudaStream_t)stream);
 }
 
+int rpm_check_batch(rpm_ctx *ctx, int32_t precision, const rpm_batch_item *items, int32_t n_items, void *stream) {
+    if (!ctx || (n_items > 0 && !items) || n_items < 0) return fail(RPM_ERR_INVALID, "bad batch");
+    if (precision < RPM_PREC_FP64 || precision > RPM_PREC_FP32_REF) return fail(RPM_ERR_INVALID, "unknown precision %d", precision);
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    if (set_device(ctx)) return RPM_ERR_CUDA;
+    std::vector<SegReq> reqs;
+    int64_t total = 0;
+    for (int k = 0; k < n_items; ++k) {
+        const rpm_batch_item &it = items[k];
+        SceneRec *s = find_scene(ctx, it.scene_id);
+        if (!s) return fail(RPM_ERR_INVALID, "batch item %d: unknown scene %d", k, it.scene_id);
+        if (it.num_configs < 0 || (it.num_configs > 0 && !it.q_dev)) return fail(RPM_ERR_INVALID, "batch item %d: bad configurations", k);
+        total += it.num_configs;
+        reqs.push_back(SegReq{s, it.q_dev, it.num_configs, it.valid_dev, it.dist_dev, it.profile_dev});
+    }
+    if (total >= (int64_t)1 << 40) return fail(RPM_ERR_RANGE, "too many configurations in one batch");
+    return enqueue_segments(ctx, precision, reqs, (cudaStream_t)stream);
+}
+
+int rpm_check_edges(rpm_ctx *ctx, int32_t scene_id, int32_t precision, const float *q1_dev, const float *q2_dev,
+                    int64_t num_edges, float step, int32_t num_checks, uint8_t *valid_dev, int32_t *checks_dev,
+                    void *stream) {
+    if (!ctx) return fail(RPM_ERR_INVALID, "NULL context");
+    if (num_edges < 0 || (num_edges > 0 && (!q1_dev || !q2_dev || !valid_dev))) return fail(RPM_ERR_INVALID, "bad edge buffers");
+    if (precision < RPM_PREC_FP64 || precision > RPM_PREC_FP32_REF) return fail(RPM_ERR_INVALID, "unknown precision %d", precision);
+    if (!(step > 0.f) && num_checks < 1) return fail(RPM_ERR_INVALID, "need step > 0 or num_checks >= 1");
+    if (num_edges >= (int64_t)1 << 40) return fail(RPM_ERR_RANGE, "too many edges in one call");
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    SceneRec *s = find_scene(ctx, scene_id);
+    if (!s) return fail(RPM_ERR_INVALID, "unknown scene %d", scene_id);
+    if (set_device(ctx)) return RPM_ERR_CUDA;
+    cudaStream_t st = (cudaStream_t)stream;
+    Scratch *sc = nullptr;
+    int rc = get_scratch(ctx, st, 0, &sc);
+    if (rc) return rc;
+    rc = edge_scratch(ctx, sc, num_edges, st);
+    if (rc) return rc;
+    sc->last_configs = num_edges;
+    sc->timed = false;
+    auto it = ctx->edge_ctas.find({s->robot, precision});
+    const int ctas = it == ctx->edge_ctas.end() ? 4 : it->second;
+    SceneBuf &buf = s->bufs[s->cur];
+    if (ctx->use_graphs) {
+        // replay a captured graph of the whole pipeline when the arguments repeat
+        uint32_t step_bits;
+        std::memcpy(&step_bits, &step, sizeof step_bits);
+        std::vector<uint64_t> key = {(uint64_t)(uintptr_t)&buf, (uint64_t)(uintptr_t)buf.f, (uint64_t)precision,
+                                     (uint64_t)(uintptr_t)q1_dev, (uint64_t)(uintptr_t)q2_dev, (uint64_t)num_edges,
+                                     (uint64_t)step_bits, (uint64_t)num_checks, (uint64_t)(uintptr_t)valid_dev,
+                                     (uint64_t)(uintptr_t)checks_dev, (uint64_t)ctas};
+        cudaGraphExec_t exec = nullptr;
+        for (auto &g : sc->graphs) if (g.key == key) { exec = g.exec; break; }
+        if (!exec) {
+            cudaStream_t cap;
+            CK(cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking));
+            CK(cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal));
+            rc = enqueue_edges(ctx, sc, s, precision, q1_dev, q2_dev, num_edges, step, num_checks, valid_dev, checks_dev,
+                               ctas, cap);
+            cudaGraph_t graph = nullptr;
+            const cudaError_t ce = cudaStreamEndCapture(cap, &graph);
+            cudaStreamDestroy(cap);
+            if (rc) { if (graph) cudaGraphDestroy(graph); return rc; }
+            CK(ce);
+            CK(cudaGraphInstantiate(&exec, graph, 0));
+            cudaGraphDestroy(graph);
+            if (sc->graphs.size() >= 16) { cudaGraphExecDestroy(sc->graphs.front().exec); sc->graphs.erase(sc->graphs.begin()); }
+            sc->graphs.push_back({key, exec});
+        }
+        CK(cudaGraphLaunch(exec, st));
+    } else {
+        rc = enqueue_edges(ctx, sc, s, precision, q1_dev, q2_dev, num_edges, step, num_checks, valid_dev, checks_dev, ctas, st);
+        if (rc) return rc;
+    }
+    prune_users(ctx, buf);
+    cudaEvent_t e = get_event(ctx);
+    CK(cudaEventRecord(e, st));
+    buf.users.push_back(e);
+    return RPM_OK;
+}
+
+int rpm_ctx_set_graphs(rpm_ctx *ctx, int enable) {
+    if (!ctx) return fail(RPM_ERR_INVALID, "NULL context");
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    ctx->use_graphs = enable != 0;
+    return RPM_OK;
+}
+
+int rpm_autotune_edges(rpm_ctx *ctx, int32_t scene_id, int32_t precision, const float *q1_dev, const float *q2_dev,
+                       int64_t num_edges, float step, int32_t num_checks, uint8_t *valid_dev, int32_t *ctas_out) {
+    if (!ctx || !ctas_out) return fail(RPM_ERR_INVALID, "NULL argument");
+    static const int cands[] = {1, 2, 3, 4, 6, 8};
+    float best_ms = 1e30f;
+    int best = 4;
+    int32_t robot = 0;
+    {
+        std::lock_guard<std::mutex> lk(ctx->mu);
+        SceneRec *s = find_scene(ctx, scene_id);
+        if (!s) return fail(RPM_ERR_INVALID, "unknown scene %d", scene_id);
+        robot = s->robot;
+    }
+    cudaEvent_t a, b;
+    CK(cudaEventCreate(&a));
+    CK(cudaEventCreate(&b));
+    for (int c : cands) {
+        {
+            std::lock_guard<std::mutex> lk(ctx->mu);
+            ctx->edge_ctas[{robot, precision}] = c;
+        }
+        int rc = rpm_check_edges(ctx, scene_id, precision, q1_dev, q2_dev, num_edges, step, num_checks, valid_dev, nullptr, 0);
+        if (rc) { cudaEventDestroy(a); cudaEventDestroy(b); return rc; }
+        CK(cudaEventRecord(a, 0));
+        rc = rpm_check_edges(ctx, scene_id, precision, q1_dev, q2_dev, num_edges, step, num_checks, valid_dev, nullptr, 0);
+        if (rc) { cudaEventDestroy(a); cudaEventDestroy(b); return rc; }
+        CK(cudaEventRecord(b, 0));
+        CK(cudaEventSynchronize(b));
+        float ms = 0.f;
+        CK(cudaEventElapsedTime(&ms, a, b));
+        if (ms < best_ms) { best_ms = ms; best = c; }
+    }
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    ctx->edge_ctas[{robot, precision}] = best;
+    *ctas_out = best;
+    return RPM_OK;
+}
+
+int rpm_set_edge_ctas(rpm_ctx *ctx, int32_t scene_id, int32_t precision, int32_t ctas_per_sm) {
+    if (!ctx || ctas_per_sm < 1 || ctas_per_sm > 32) return fail(RPM_ERR_INVALID, "bad arguments");
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    SceneRec *s = find_scene(ctx, scene_id);
+    if (!s) return fail(RPM_ERR_INVALID, "unknown scene %d", scene_id);
+    ctx->edge_ctas[{s->robot, precision}] = ctas_per_sm;
+    return RPM_OK;
+}
+
 int rpm_check_configs_host(rpm_ctx *ctx, int32_t scene_id, int32_t precision, const float *q_host, int64_t num_configs,
                            uint8_t *valid_host, double *dist_host, float *profile_host) {
     if (!ctx) return fail(RPM_ERR_INVALID, "NULL context");
@@ -536,13 +768,13 @@ int rpm_last_stats(rpm_ctx *ctx, void *stream, rpm_check_stats *out) {
     auto it = ctx->scratch.find(st);
     if (it == ctx->scratch.end()) return RPM_OK;
     CK(cudaStreamSynchronize(st));
-    uint32_t cnt = 0;
+    uint32_t cnt[2] = {0, 0};
     int32_t status = 0;
-    CK(cudaMemcpy(&cnt, it->second->counters, sizeof cnt, cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(cnt, it->second->counters, sizeof cnt, cudaMemcpyDeviceToHost));
     CK(cudaMemcpy(&status, it->second->status, sizeof status, cudaMemcpyDeviceToHost));
     out->configs = it->second->last_configs;
-    out->rechecked = cnt;
-    out->overflow = 0;
+    out->rechecked = cnt[0];
+    out->overflow = cnt[1];
     out->device_status = status;
     return RPM_OK;
 }

@@ -5,6 +5,7 @@
 #include <type_traits>
 
 #include "rpm_check.cuh"
+#include "rpm_edges.cuh"
 #include "rpm_launch.cuh"
 
 namespace rpm {
@@ -116,6 +117,175 @@ __global__ void k_skeleton(const DevRobot *rbp, const float *q, int64_t C, doubl
             for (int i = 0; i < 3; ++i) out[(c * (D + 1) + k) * 3 + i] = (double)p[i];
         }
     }
+}
+
+// ---------------------------------------------------------------- edges --
+// Checks per edge and their exclusive offsets within blocks of kEdgeScanBlock
+// edges; block totals go to bprefix[b + 1] for the block scan.
+__global__ void __launch_bounds__(kEdgeScanBlock) k_edge_prep(const __grid_constant__ EdgeParams P) {
+    __shared__ int32_t warp_sum[kEdgeScanBlock / 32];
+    const int64_t e = (int64_t)blockIdx.x * kEdgeScanBlock + threadIdx.x;
+    const int D = P.seg.robot->D;
+    int n = 0;
+    if (e < P.E) {
+        float dist;
+        n = edge_count(P.q1 + e * D, P.q2 + e * D, D, P.step, P.num_checks, dist);
+        P.n_e[e] = n;
+        P.kmax[e] = 0;
+        P.full[e] = 0;
+    }
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    int x = n;
+#pragma unroll
+    for (int off = 1; off < 32; off <<= 1) {
+        const int y = __shfl_up_sync(0xffffffffu, x, off);
+        if (lane >= off) x += y;
+    }
+    if (lane == 31) warp_sum[wid] = x;
+    __syncthreads();
+    if (wid == 0) {
+        int t = warp_sum[lane];
+#pragma unroll
+        for (int off = 1; off < 32; off <<= 1) {
+            const int y = __shfl_up_sync(0xffffffffu, t, off);
+            if (lane >= off) t += y;
+        }
+        warp_sum[lane] = t;   // inclusive over warps
+    }
+    __syncthreads();
+    const int excl = x - n + (wid > 0 ? warp_sum[wid - 1] : 0);
+    if (e < P.E) P.local[e] = excl;
+    if (threadIdx.x == kEdgeScanBlock - 1) P.bprefix[blockIdx.x + 1] = warp_sum[31];
+}
+
+// Exclusive scan of the block totals (one CTA; bprefix[0] = 0).
+__global__ void k_edge_scan(const __grid_constant__ EdgeParams P, int nblocks) {
+    if (threadIdx.x == 0) {
+        int64_t acc = 0;
+        P.bprefix[0] = 0;
+        for (int b = 1; b <= nblocks; ++b) {
+            acc += P.bprefix[b];
+            P.bprefix[b] = acc;
+        }
+        *P.work = 0ull;
+    }
+}
+
+template <int MODE>
+__global__ void __launch_bounds__(kThreads) k_edges_exact(const __grid_constant__ EdgeParams P) {
+    typedef typename std::conditional<MODE == 0, double, float>::type T;
+    extern __shared__ __align__(128) unsigned char smem[];
+    __shared__ uint64_t bar;
+    __shared__ WarpShared<T> wsh[kThreads / 32];
+    __shared__ float qbuf[kThreads / 32][32 * kMaxDof];
+    bulk_init(&bar);
+    if (!stage<MODE>(P.seg, smem, &bar, P.status)) return;
+    const DevRobot &rb = *reinterpret_cast<const DevRobot *>(smem);
+    const T *rows = reinterpret_cast<const T *>(smem + sizeof(DevRobot));
+    const float *ground = (MODE == 0) ? reinterpret_cast<const float *>(smem + sizeof(DevRobot) + kDRows * P.seg.n_pad * sizeof(double))
+                                      : reinterpret_cast<const float *>(rows) + (size_t)kRowGround * P.seg.n_pad;
+    ObsView<T> ob{rows, ground, P.seg.n, P.seg.n_pad};
+    Num<T> nm;
+    if (MODE == 0) { nm.eq = (T)P.nmd.eq; nm.maxd = (T)P.nmd.maxd; }
+    else { nm.eq = (T)P.nmf.eq; nm.maxd = (T)P.nmf.maxd; }
+    edge_warps<MODE, T>(P, rb, ob, nm, wsh[threadIdx.x >> 5], qbuf[threadIdx.x >> 5]);
+}
+
+// FP64 recheck of the checks the FP32 edge pass left unsettled (one warp each).
+__global__ void __launch_bounds__(kThreads) k_edge_recheck(const __grid_constant__ EdgeParams P) {
+    __shared__ float qbuf[kThreads / 32][kMaxDof];
+    const uint32_t n = min(*P.recheck_count, P.recheck_cap);
+    const uint32_t warps = gridDim.x * (blockDim.x / 32);
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const DevRobot &rb = *P.seg.robot;
+    const int D = rb.D;
+    ObsView<double> ob{P.seg.obs_d, P.seg.obs_f + (size_t)kRowGround * P.seg.n_pad, P.seg.n, P.seg.n_pad};
+    for (uint32_t it = blockIdx.x * (blockDim.x / 32) + wid; it < n; it += warps) {
+        const uint64_t ent = P.recheck[it];
+        const int64_t e = (int64_t)(ent >> 20);
+        const int k = (int)(ent & 0xfffff);
+        if (k <= *(volatile int32_t *)&P.kmax[e]) continue;
+        if (lane == 0) {
+            float dist;
+            const int N = edge_count(P.q1 + e * D, P.q2 + e * D, D, P.step, P.num_checks, dist);
+            edge_config(P.q1 + e * D, P.q2 + e * D, D, N, k, dist, qbuf[wid]);
+        }
+        __syncwarp();
+        uint8_t v = 1;
+        config_exact_warp<0, double>(rb, ob, qbuf[wid], P.nmd, Want{true, false, false}, &v, nullptr, nullptr);
+        v = (uint8_t)__shfl_sync(0xffffffffu, (int)v, 0);
+        if (lane == 0 && v == 0) atomicMax(&P.kmax[e], k);
+        __syncwarp();
+    }
+}
+
+// Edges whose unsettled checks overflowed the list: every remaining check in
+// FP64, nearest q2 first (one warp per edge).
+__global__ void __launch_bounds__(kThreads) k_edge_full(const __grid_constant__ EdgeParams P) {
+    __shared__ float qbuf[kThreads / 32][kMaxDof];
+    if (*P.overflow == 0) return;
+    const int64_t warps = (int64_t)gridDim.x * (blockDim.x / 32);
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const DevRobot &rb = *P.seg.robot;
+    const int D = rb.D;
+    ObsView<double> ob{P.seg.obs_d, P.seg.obs_f + (size_t)kRowGround * P.seg.n_pad, P.seg.n, P.seg.n_pad};
+    for (int64_t e = (int64_t)blockIdx.x * (blockDim.x / 32) + wid; e < P.E; e += warps) {
+        if (!P.full[e]) continue;
+        const int N = P.n_e[e];
+        for (int k = N; k > P.kmax[e]; --k) {
+            if (lane == 0) {
+                float dist;
+                edge_count(P.q1 + e * D, P.q2 + e * D, D, P.step, P.num_checks, dist);
+                edge_config(P.q1 + e * D, P.q2 + e * D, D, N, k, dist, qbuf[wid]);
+            }
+            __syncwarp();
+            uint8_t v = 1;
+            config_exact_warp<0, double>(rb, ob, qbuf[wid], P.nmd, Want{true, false, false}, &v, nullptr, nullptr);
+            v = (uint8_t)__shfl_sync(0xffffffffu, (int)v, 0);
+            __syncwarp();
+            if (v == 0) {
+                if (lane == 0) atomicMax(&P.kmax[e], k);
+                break;
+            }
+        }
+    }
+}
+
+__global__ void k_edge_final(const __grid_constant__ EdgeParams P) {
+    const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= P.E) return;
+    const int km = P.kmax[e];
+    P.valid[e] = km == 0 ? 1 : 0;
+    if (P.checks_out) P.checks_out[e] = km == 0 ? P.n_e[e] : P.n_e[e] - km + 1;
+}
+
+cudaError_t launch_edge_prep(const EdgeParams &p, cudaStream_t st) {
+    const int nb = (int)((p.E + kEdgeScanBlock - 1) / kEdgeScanBlock);
+    if (nb == 0) return cudaSuccess;
+    k_edge_prep<<<nb, kEdgeScanBlock, 0, st>>>(p);
+    k_edge_scan<<<1, 32, 0, st>>>(p, nb);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_edges(int mode, const EdgeParams &p, int grid, size_t smem, cudaStream_t st) {
+    if (mode == RPM_PREC_FP64) {
+        static bool attr = false;
+        if (!attr) { cudaFuncSetAttribute(k_edges_exact<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, 160 * 1024); attr = true; }
+        k_edges_exact<0><<<grid, kThreads, smem, st>>>(p);
+    } else {
+        static bool attr = false;
+        if (!attr) { cudaFuncSetAttribute(k_edges_exact<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, 160 * 1024); attr = true; }
+        k_edges_exact<1><<<grid, kThreads, smem, st>>>(p);
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_edge_recheck_final(const EdgeParams &p, int grid, cudaStream_t st) {
+    k_edge_recheck<<<grid, kThreads, 0, st>>>(p);
+    k_edge_full<<<grid, kThreads, 0, st>>>(p);
+    const unsigned fb = (unsigned)((p.E + 255) / 256);
+    if (fb) k_edge_final<<<fb, 256, 0, st>>>(p);
+    return cudaGetLastError();
 }
 
 cudaError_t launch_check_exact(int mode, const KParams &p, int64_t blocks, size_t smem, cudaStream_t st) {

@@ -3,6 +3,7 @@
 // depended on a decision within kBand of its boundary are appended to the
 // recheck list and recomputed in FP64 by k_recheck (rpm_exact.cu).
 #include "rpm_check.cuh"
+#include "rpm_edges.cuh"
 #include "rpm_launch.cuh"
 
 namespace rpm {
@@ -40,6 +41,34 @@ __global__ void __launch_bounds__(kThreads) k_check_fp32(const __grid_constant__
         const uint32_t slot = atomicAdd(P.recheck_count, 1u);
         P.recheck[slot] = ((uint64_t)s << 40) | (uint64_t)c;
     }
+}
+
+// FP32 pass of the edge checks (unsettled checks go to k_edge_recheck).
+__global__ void __launch_bounds__(kThreads) k_edges_fp32(const __grid_constant__ EdgeParams P) {
+    extern __shared__ __align__(128) unsigned char smem[];
+    __shared__ uint64_t bar;
+    __shared__ WarpShared<float> wsh[kThreads / 32];
+    __shared__ float qbuf[kThreads / 32][32 * kMaxDof];
+    bulk_init(&bar);
+    if (threadIdx.x == 0) {
+        const uint32_t rb = (uint32_t)sizeof(DevRobot);
+        const uint32_t rows = (uint32_t)(kFRows * P.seg.n_pad * sizeof(float));
+        bulk_expect(&bar, rb + rows);
+        bulk_copy(&bar, smem, P.seg.robot, rb);
+        bulk_copy(&bar, smem + rb, P.seg.obs_f, rows);
+    }
+    if (!bulk_wait(&bar, 0, P.status)) return;
+    const DevRobot &rb = *reinterpret_cast<const DevRobot *>(smem);
+    const float *rows = reinterpret_cast<const float *>(smem + sizeof(DevRobot));
+    ObsView<float> ob{rows, rows + (size_t)kRowGround * P.seg.n_pad, P.seg.n, P.seg.n_pad};
+    edge_warps<2, float>(P, rb, ob, P.nmf, wsh[threadIdx.x >> 5], qbuf[threadIdx.x >> 5]);
+}
+
+cudaError_t launch_edges_fp32(const EdgeParams &p, int grid, size_t smem, cudaStream_t st) {
+    static bool attr = false;
+    if (!attr) { cudaFuncSetAttribute(k_edges_fp32, cudaFuncAttributeMaxDynamicSharedMemorySize, 160 * 1024); attr = true; }
+    k_edges_fp32<<<grid, kThreads, smem, st>>>(p);
+    return cudaGetLastError();
 }
 
 // Peak FP32 issue rate of this GPU: independent FMA chains, no memory traffic.

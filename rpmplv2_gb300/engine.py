@@ -9,7 +9,7 @@ import os
 import numpy as np
 
 from . import _abi
-from ._abi import CheckStats, Params, PRECISIONS
+from ._abi import BatchItem, CheckStats, Params, PRECISIONS
 
 _LIB = None
 
@@ -53,6 +53,11 @@ def load(build_if_missing=False):
     L.rpm_scene_info.argtypes = [_vp, _i32, _pi32, _pi32, ctypes.POINTER(ctypes.c_uint64)]
     L.rpm_box_aabb.argtypes = [_vp, _vp, _vp, _vp]
     L.rpm_check_configs.argtypes = [_vp, _i32, _i32, _vp, _i64, _vp, _vp, _vp, _vp]
+    L.rpm_check_batch.argtypes = [_vp, _i32, _vp, _i32, _vp]
+    L.rpm_check_edges.argtypes = [_vp, _i32, _i32, _vp, _vp, _i64, ctypes.c_float, _i32, _vp, _vp, _vp]
+    L.rpm_ctx_set_graphs.argtypes = [_vp, ctypes.c_int]
+    L.rpm_autotune_edges.argtypes = [_vp, _i32, _i32, _vp, _vp, _i64, ctypes.c_float, _i32, _vp, _pi32]
+    L.rpm_set_edge_ctas.argtypes = [_vp, _i32, _i32, _i32]
     L.rpm_check_configs_host.argtypes = [_vp, _i32, _i32, _vp, _i64, _vp, _vp, _vp]
     L.rpm_skeleton.argtypes = [_vp, _i32, _i32, _vp, _i64, _vp, _vp]
     L.rpm_last_stats.argtypes = [_vp, _vp, ctypes.POINTER(CheckStats)]
@@ -141,6 +146,34 @@ class Engine:
         _check(self.lib.rpm_check_configs(self.ctx, scene_id, prec, _ptr(q), n, _ptr(valid), _ptr(dist),
                                           _ptr(profile), stream))
 
+    def check_batch(self, items, precision="fp64", stream=None):
+        """items: list of (scene_id, q, valid, dist, profile) with torch CUDA tensors (outputs nullable)."""
+        prec = PRECISIONS[precision] if isinstance(precision, str) else int(precision)
+        arr = (BatchItem * len(items))()
+        for k, (sid, q, valid, dist, profile) in enumerate(items):
+            arr[k] = BatchItem(sid, 0, _ptr(q), int(q.shape[0]), _ptr(valid), _ptr(dist), _ptr(profile))
+        _check(self.lib.rpm_check_batch(self.ctx, prec, ctypes.addressof(arr), len(items), stream))
+
+    def check_edges(self, scene_id, q1, q2, valid, checks=None, step=0.0, num_checks=10, precision="fp64",
+                    stream=None):
+        prec = PRECISIONS[precision] if isinstance(precision, str) else int(precision)
+        _check(self.lib.rpm_check_edges(self.ctx, scene_id, prec, _ptr(q1), _ptr(q2), int(q1.shape[0]), float(step),
+                                        int(num_checks), _ptr(valid), _ptr(checks), stream))
+
+    def set_graphs(self, enable=True):
+        _check(self.lib.rpm_ctx_set_graphs(self.ctx, 1 if enable else 0))
+
+    def autotune_edges(self, scene_id, q1, q2, valid, step=0.0, num_checks=10, precision="fp32_recheck"):
+        prec = PRECISIONS[precision] if isinstance(precision, str) else int(precision)
+        out = _i32()
+        _check(self.lib.rpm_autotune_edges(self.ctx, scene_id, prec, _ptr(q1), _ptr(q2), int(q1.shape[0]),
+                                           float(step), int(num_checks), _ptr(valid), ctypes.byref(out)))
+        return out.value
+
+    def set_edge_ctas(self, scene_id, precision, ctas_per_sm):
+        prec = PRECISIONS[precision] if isinstance(precision, str) else int(precision)
+        _check(self.lib.rpm_set_edge_ctas(self.ctx, scene_id, prec, int(ctas_per_sm)))
+
     def skeleton(self, robot_id, q, points, precision="fp64", stream=None):
         prec = PRECISIONS[precision] if isinstance(precision, str) else int(precision)
         _check(self.lib.rpm_skeleton(self.ctx, robot_id, prec, _ptr(q), int(q.shape[0]), _ptr(points), stream))
@@ -193,5 +226,6 @@ ABI_SYMBOLS = [
     "rpm_last_error_string", "rpm_version", "rpm_ctx_create", "rpm_ctx_destroy", "rpm_ctx_set_params",
     "rpm_robot_upload", "rpm_scene_create", "rpm_scene_update", "rpm_scene_destroy", "rpm_scene_info",
     "rpm_box_aabb", "rpm_check_configs", "rpm_check_configs_host", "rpm_skeleton", "rpm_last_stats", "rpm_sync",
-    "rpm_ctx_set_timing", "rpm_last_timing", "rpm_probe_fp32_peak", "rpm_check_configs_noalloc",
+    "rpm_ctx_set_timing", "rpm_last_timing", "rpm_probe_fp32_peak", "rpm_check_configs_noalloc", "rpm_check_batch",
+    "rpm_check_edges", "rpm_ctx_set_graphs", "rpm_autotune_edges", "rpm_set_edge_ctas",
 ]
