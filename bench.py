@@ -45,6 +45,7 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--configs", type=int, default=NUM_CONFIGS)
+    ap.add_argument("--no-extra", action="store_true", help="skip the edge, mixed-DOF and serving measurements")
     return ap.parse_args()
 
 
@@ -130,6 +131,77 @@ def traffic_per_launch():
             return json.load(f).get("dram_bytes_per_launch_full")
     except Exception:
         return None
+
+
+def extra_workloads(eng, args):
+    """The other configurations of the path, measured the same way (device
+    events around whole steps, FP32 + FP64 recheck): edge checks (262,144
+    spatial_10dof edges, 0.05 rad steps), the mixed-DOF profile launch
+    (spatial 14/18/22, 500 AABBs) and the serving replay."""
+    import torch
+    from rpmplv2_gb300 import scenes, serve
+    out = {}
+
+    def timed(fn, steps=3, warmup=1):
+        for _ in range(warmup):
+            fn()
+        torch.cuda.synchronize()
+        ms = []
+        for _ in range(steps):
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record()
+            fn()
+            b.record()
+            b.synchronize()
+            ms.append(a.elapsed_time(b))
+        return statistics.median(ms)
+
+    # ---- edges (BASELINE config 2)
+    robot, scene, q1, q2, step = scenes.spatial10_edge_workload(1 << 18, seed=2)
+    sid = eng.create_scene(eng.upload_robot(robot), scene)
+    q1d, q2d = torch.from_numpy(q1).cuda(), torch.from_numpy(q2).cuda()
+    v = torch.zeros(q1.shape[0], dtype=torch.uint8, device="cuda")
+    k = torch.zeros(q1.shape[0], dtype=torch.int32, device="cuda")
+    ctas = eng.autotune_edges(sid, q1d[:32768], q2d[:32768], v[:32768], step=float(step), precision="fp32_recheck")
+    eng.set_graphs(True)
+    ms = timed(lambda: eng.check_edges(sid, q1d, q2d, v, k, step=float(step), precision="fp32_recheck"))
+    eng.set_graphs(False)
+    checks = int(k.sum().item())
+    out["edges"] = {"workload": "spatial_10dof (r 0.03) vs 200 rotated boxes as fcl AABBs, 262,144 edges, 0.05 rad",
+                    "edges_per_s": q1.shape[0] / (ms / 1e3), "checks_per_s": checks / (ms / 1e3),
+                    "ms_per_step": ms, "checks_reference_order": checks, "valid_fraction": float(v.float().mean()),
+                    "ctas_per_sm": ctas, "cuda_graph": True, "precision": "fp32_recheck"}
+    eng.destroy_scene(sid)
+    # ---- mixed-DOF profile launch (BASELINE config 3)
+    scene, parts = scenes.mixed_dof_workload(seed=3)
+    items = []
+    for robot, q in parts:
+        sid = eng.create_scene(eng.upload_robot(robot), scene)
+        C, L = q.shape[0], robot.num_links
+        items.append((sid, torch.from_numpy(q).cuda(), None, torch.zeros(C, dtype=torch.float64, device="cuda"),
+                      torch.zeros((C, L), device="cuda")))
+    total = sum(it[1].shape[0] for it in items)
+    ms = timed(lambda: eng.check_batch(items, "fp32_recheck"))
+    out["mixed_dof"] = {"workload": "spatial 14/18/22 DOF (r 0.03), 32,768/49,152/49,152 configs, 500 AABBs, "
+                        "per-link distance + global min in one launch",
+                        "configs_per_s": total / (ms / 1e3), "ms_per_step": ms, "precision": "fp32_recheck"}
+    for it in items:
+        eng.destroy_scene(it[0])
+    # ---- serving replay (BASELINE config 4)
+    wl = serve.serving_workload(eng, seed=4, rate=20000.0, duration=0.5)
+    srv = serve.Server(eng, num_slots=6)
+    srv.replay(wl["requests"][:200], [0.0] * 200)
+    tim = srv.replay(wl["requests"], wl["arrivals"], wl["motions"], period=0.001)
+    summ = serve.latency_summary(tim, wl["meta"])
+    summ.update({"workload": "64 resident scenes (robots of configs 0-3, 10-1000 boxes log-uniform, 20% with 5 "
+                             "boxes moving up to 1.6 m/s updated every 1 ms), Poisson 20,000 req/s for 0.5 s, "
+                             "sizes log-uniform 1-65,536, isValid / distance / edge in equal shares",
+                 "memory_budget_bytes": 8 << 30, "slots": 6})
+    out["serve"] = summ
+    srv.close()
+    for sid in wl["scene_ids"]:
+        eng.destroy_scene(sid)
+    return out
 
 
 def run_reference(args, ws, rank):
@@ -259,6 +331,8 @@ def run_ours(args, ws, rank, local):
     hbm_peak = peaks.get("hbm_gbs")
     hbm_achieved = BYTES_PER_CONFIG * C / bulk_s / 1e9
 
+    extra = {} if args.no_extra else extra_workloads(eng, args)
+
     if rank != 0:
         return
     line = {
@@ -285,6 +359,7 @@ def run_ours(args, ws, rank, local):
                              "frac": (hbm_achieved / hbm_peak) if hbm_peak else None,
                              "bytes_per_config": BYTES_PER_CONFIG, "peak_source": "MEASURED_PEAKS.json hbm_gbs"}},
     }
+    line.update(extra)
     if ws == 1 or rank == 0:
         line["cpu_baseline"] = cpu_baseline(robot, scene, q, min(C, 1 << 20))
     print(json.dumps(line), flush=True)

@@ -122,9 +122,10 @@ int rpm_robot_upload(rpm_ctx *ctx, const rpm_robot_desc *desc, int32_t *robot_id
 int rpm_scene_create(rpm_ctx *ctx, int32_t robot_id, const float *aabb_host, const float *min_dist_tol_host,
                      const uint8_t *flags_host, int32_t n, int32_t *scene_id);
 /* Replace the AABBs of obstacles idx[0..m) (Object::setPosition, Object.cpp:21-26;
- * Environment::updateEnvironment moves).  The new version is visible to every
- * check issued on any stream after this call returns; checks already issued
- * keep the version they started with. */
+ * Environment::updateEnvironment moves).  Incremental and asynchronous: the
+ * next version is the current one copied on the device with the m rows
+ * scattered in.  It is visible to every check issued on any stream after this
+ * call returns; checks already issued keep the version they started with. */
 int rpm_scene_update(rpm_ctx *ctx, int32_t scene_id, const int32_t *idx_host, const float *aabb_host, int32_t m,
                      uint64_t *version_out);
 int rpm_scene_destroy(rpm_ctx *ctx, int32_t scene_id);
@@ -191,6 +192,70 @@ int rpm_set_edge_ctas(rpm_ctx *ctx, int32_t scene_id, int32_t precision, int32_t
  * RPM_PREC_FP32_RECHECK the FP32 FK of the bulk pass. */
 int rpm_skeleton(rpm_ctx *ctx, int32_t robot_id, int32_t precision, const float *q_dev, int64_t num_configs,
                  double *points_dev, void *stream);
+
+/* ---- serving loop (continuous batching) -----------------------------------
+ * Planners submit isValid / distance batches and edge batches of any size
+ * against resident scenes while obstacles move (the DRGBT replanning shape,
+ * DRGBT.cpp:79-176 with MotionValidity.cpp:30-53).  A worker thread admits
+ * requests as device memory of the budget frees up, packs waiting
+ * configuration requests from any scenes into one launch per free slot
+ * (stream), so batches overlap on the device, and time-stamps each request.
+ * Smaller requests are served first (requests waiting over 50 ms are served
+ * as small); half of the slots are high-priority streams reserved for batches
+ * of small requests, so a replanning query is not held behind a bulk batch.
+ * Host buffers should be pinned for copies to overlap. */
+typedef struct rpm_server rpm_server;
+typedef struct rpm_server_config {
+    int32_t num_slots;           /* concurrent batches (streams), default 4 */
+    int32_t precision;           /* RPM_PREC_* of every request */
+    int64_t memory_budget;       /* device bytes for request buffers (admission), default 8 GiB */
+    int32_t max_batch_segments;  /* requests per launch, <= 32 */
+    int32_t max_batch_configs;   /* configurations per launch */
+} rpm_server_config;
+
+enum rpm_request_kind { RPM_REQ_CONFIGS = 0, RPM_REQ_EDGES = 1 };
+
+typedef struct rpm_request {
+    int32_t kind;                /* enum rpm_request_kind */
+    int32_t scene_id;
+    int64_t count;               /* configurations or edges */
+    const float *q_host;         /* CONFIGS: count x D */
+    const float *q1_host;        /* EDGES: count x D each */
+    const float *q2_host;
+    float step;                  /* EDGES: as rpm_check_edges */
+    int32_t num_checks;
+    uint8_t *valid_host;         /* isValid (required for EDGES) */
+    double *dist_host;           /* CONFIGS, nullable */
+    float *profile_host;         /* CONFIGS, nullable */
+    int32_t *checks_host;        /* EDGES, nullable */
+} rpm_request;
+
+typedef struct rpm_request_timing {
+    int32_t status;              /* 0 done, 1 pending, < 0 error (RPM_ERR_ADMISSION: larger than the budget) */
+    int32_t batch_size;          /* requests in the launch it ran in */
+    double t_submit, t_admit, t_launch, t_done;   /* seconds (monotonic; relative to the start in a replay) */
+} rpm_request_timing;
+
+/* A moving obstacle of a replay: AABB(t) = AABB(0) + velocity * t. */
+typedef struct rpm_motion {
+    int32_t scene_id;
+    int32_t index;
+    float velocity[3];
+} rpm_motion;
+
+int rpm_server_create(rpm_ctx *ctx, const rpm_server_config *cfg, rpm_server **out);
+int rpm_server_submit(rpm_server *srv, const rpm_request *req, uint64_t *ticket);
+int rpm_server_poll(rpm_server *srv, uint64_t ticket, rpm_request_timing *out);
+int rpm_server_wait(rpm_server *srv, uint64_t ticket, double timeout_s, rpm_request_timing *out);
+int rpm_server_release(rpm_server *srv, uint64_t ticket);
+/* Submits reqs[i] at arrival_s[i] seconds after the start from a native
+ * thread while a second thread moves the given obstacles every period_s
+ * (incremental scene updates), waits for every request and returns their
+ * timings relative to the start. */
+int rpm_server_replay(rpm_server *srv, const rpm_request *reqs, const double *arrival_s, int64_t n,
+                      const rpm_motion *motions, int32_t n_motions, double period_s, rpm_request_timing *out);
+int rpm_server_stats(rpm_server *srv, int64_t *batches, int64_t *pending);
+int rpm_server_destroy(rpm_server *srv);
 
 /* Statistics of the last check on this context; synchronises 'stream'. */
 int rpm_last_stats(rpm_ctx *ctx, void *stream, rpm_check_stats *out);

@@ -14,101 +14,14 @@
 #include <string>
 #include <vector>
 
-#include "rpm_edges.cuh"
-#include "rpm_launch.cuh"
+#include "rpm_ctx_impl.cuh"
 
 using namespace rpm;
 
-namespace {
+namespace rpm {
+namespace impl {
 
 thread_local std::string g_err;
-
-int fail(int code, const char *fmt, ...) {
-    char buf[512];
-    va_list ap;
-    va_start(ap, fmt);
-    vsnprintf(buf, sizeof buf, fmt, ap);
-    va_end(ap);
-    g_err = buf;
-    return code;
-}
-
-#define CK(x)                                                                                   \
-    do {                                                                                        \
-        cudaError_t e_ = (x);                                                                   \
-        if (e_ != cudaSuccess) return fail(RPM_ERR_CUDA, "%s: %s", #x, cudaGetErrorString(e_)); \
-    } while (0)
-
-constexpr int kRing = 4;   // versions kept per scene
-
-struct RobotRec {
-    rpm_robot_desc desc;
-    DevRobot *dev = nullptr;
-};
-
-struct SceneBuf {
-    void *mem = nullptr;
-    float *f = nullptr;
-    double *d = nullptr;
-    std::vector<cudaEvent_t> users;   // checks that may still read this buffer
-};
-
-struct SceneRec {
-    int robot = 0;
-    int n = 0, n_pad = 16;
-    std::vector<float> aabb, tol;
-    std::vector<uint8_t> flags;
-    int cur = 0;
-    SceneBuf bufs[kRing];
-    uint64_t version = 0;
-};
-
-struct Scratch {
-    uint64_t *recheck = nullptr;
-    size_t cap = 0;
-    uint32_t *counters = nullptr;   // [0] recheck count
-    int32_t *status = nullptr;
-    int64_t last_configs = 0;
-    cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};   // bulk start, bulk end / recheck start, recheck end
-    bool timed = false, had_recheck = false;
-    // edge checks
-    size_t ecap = 0;
-    int32_t *n_e = nullptr, *local = nullptr, *kmax = nullptr;
-    int64_t *bprefix = nullptr;
-    uint8_t *full = nullptr;
-    unsigned long long *work = nullptr;
-    uint64_t *erecheck = nullptr;
-    size_t erecheck_cap = 0;
-    // cached CUDA graphs of edge calls, keyed by their arguments
-    struct Graph { std::vector<uint64_t> key; cudaGraphExec_t exec; };
-    std::vector<Graph> graphs;
-};
-
-}  // namespace
-
-struct rpm_ctx {
-    int device = 0;
-    int num_sms = 0;
-    rpm_params params{1e-4, 1000.0};
-    std::mutex mu;
-    std::vector<RobotRec> robots;
-    std::map<int, SceneRec *> scenes;
-    int next_scene = 0;
-    std::map<cudaStream_t, Scratch *> scratch;
-    std::vector<cudaEvent_t> event_pool;
-    // host-buffer pipeline
-    cudaStream_t hs[2] = {nullptr, nullptr};
-    float *hq[2] = {nullptr, nullptr};
-    uint8_t *hv[2] = {nullptr, nullptr};
-    double *hd[2] = {nullptr, nullptr};
-    float *hp[2] = {nullptr, nullptr};
-    size_t hcap_cfg = 0, hcap_prof = 0;
-    bool timing = false;
-    bool use_graphs = false;
-    std::map<std::pair<int, int>, int> edge_ctas;   // (robot, precision) -> CTAs per SM of the edge kernel
-};
-
-namespace {
 
 int set_device(rpm_ctx *ctx) {
     CK(cudaSetDevice(ctx->device));
@@ -191,9 +104,10 @@ int get_scratch(rpm_ctx *ctx, cudaStream_t st, int64_t need, Scratch **out) {
     return RPM_OK;
 }
 
-}  // namespace
+}  // namespace impl
 
-namespace rpm {
+using impl::fail;
+
 int set_error(int code, const char *msg) { return fail(code, "%s", msg); }
 int build_dev_robot(const rpm_robot_desc &d, DevRobot &r) {
     if (d.kind != RPM_ROBOT_CHAIN && d.kind != RPM_ROBOT_XARM6) return fail(RPM_ERR_INVALID, "unknown robot kind %d", d.kind);
@@ -234,22 +148,13 @@ int build_dev_robot(const rpm_robot_desc &d, DevRobot &r) {
 }
 }  // namespace rpm
 
-namespace {
+namespace rpm {
+namespace impl {
 
 SceneRec *find_scene(rpm_ctx *ctx, int id) {
     auto it = ctx->scenes.find(id);
     return it == ctx->scenes.end() ? nullptr : it->second;
 }
-
-// One segment of a launch: a scene and its configurations / outputs.
-struct SegReq {
-    SceneRec *scene;
-    const float *q;
-    int64_t count;
-    uint8_t *valid;
-    double *dist;
-    float *profile;
-};
 
 // Queue checks of up to kMaxSegs segments as one launch on 'st' (more
 // segments become several launches).  The caller holds ctx->mu.
@@ -275,6 +180,10 @@ int enqueue_segments(rpm_ctx *ctx, int prec, const std::vector<SegReq> &reqs, cu
         for (size_t k = off; k < reqs.size() && k < off + kMaxSegs; ++k) {
             const SegReq &r = reqs[k];
             SceneBuf &buf = r.scene->bufs[r.scene->cur];
+            if (buf.pending) {   // an incremental update still writing this version
+                if (cudaEventQuery(buf.ready) == cudaSuccess) buf.pending = false;
+                else CK(cudaStreamWaitEvent(st, buf.ready, 0));
+            }
             used.push_back(&buf);
             Seg &g = p.segs[p.nseg++];
             g.robot = ctx->robots[r.scene->robot].dev;
@@ -343,6 +252,10 @@ int edge_scratch(rpm_ctx *ctx, Scratch *sc, int64_t E, cudaStream_t st) {
 int enqueue_edges(rpm_ctx *ctx, Scratch *sc, SceneRec *s, int prec, const float *q1, const float *q2, int64_t E,
                   float step, int32_t num_checks, uint8_t *valid, int32_t *checks, int ctas_per_sm, cudaStream_t st) {
     SceneBuf &buf = s->bufs[s->cur];
+    if (buf.pending) {
+        if (cudaEventQuery(buf.ready) == cudaSuccess) buf.pending = false;
+        else CK(cudaStreamWaitEvent(st, buf.ready, 0));
+    }
     EdgeParams p;
     std::memset(&p, 0, sizeof p);
     p.seg.robot = ctx->robots[s->robot].dev;
@@ -375,7 +288,10 @@ int enqueue_check(rpm_ctx *ctx, SceneRec *s, int prec, const float *q, int64_t C
     return enqueue_segments(ctx, prec, {SegReq{s, q, C, valid, dist, profile}}, st);
 }
 
-}  // namespace
+}  // namespace impl
+}  // namespace rpm
+
+using namespace rpm::impl;
 
 extern "C" {
 
@@ -481,21 +397,15 @@ int rpm_scene_create(rpm_ctx *ctx, int32_t robot_id, const float *aabb_host, con
 
 int rpm_scene_update(rpm_ctx *ctx, int32_t scene_id, const int32_t *idx_host, const float *aabb_host, int32_t m,
                      uint64_t *version_out) {
-    if (!ctx || (m > 0 && (!idx_host || !aabb_host))) return fail(RPM_ERR_INVALID, "NULL argument");
+    if (!ctx || m < 0 || (m > 0 && (!idx_host || !aabb_host))) return fail(RPM_ERR_INVALID, "bad update arguments");
     std::lock_guard<std::mutex> lk(ctx->mu);
     SceneRec *s = find_scene(ctx, scene_id);
     if (!s) return fail(RPM_ERR_INVALID, "unknown scene %d", scene_id);
     for (int k = 0; k < m; ++k)
         if (idx_host[k] < 0 || idx_host[k] >= s->n) return fail(RPM_ERR_INVALID, "obstacle index %d out of range", idx_host[k]);
     if (set_device(ctx)) return RPM_ERR_CUDA;
-    for (int k = 0; k < m; ++k)
-        for (int c = 0; c < 6; ++c) s->aabb[6 * (size_t)idx_host[k] + c] = aabb_host[6 * (size_t)k + c];
-    const int nxt = (s->cur + 1) % kRing;
-    wait_users(ctx, s->bufs[nxt]);
-    int rc = upload_scene(ctx, *s, s->bufs[nxt]);
+    const int rc = scene_update(ctx, s, idx_host, aabb_host, m);
     if (rc) return rc;
-    s->cur = nxt;
-    s->version++;
     if (version_out) *version_out = s->version;
     return RPM_OK;
 }
@@ -507,7 +417,10 @@ int rpm_scene_destroy(rpm_ctx *ctx, int32_t scene_id) {
     if (!s) return fail(RPM_ERR_INVALID, "unknown scene %d", scene_id);
     for (auto &b : s->bufs) {
         wait_users(ctx, b);
+        if (b.ready) { cudaEventSynchronize(b.ready); cudaEventDestroy(b.ready); }
         if (b.mem) cudaFree(b.mem);
+        if (b.upd_host) cudaFreeHost(b.upd_host);
+        if (b.upd_dev) cudaFree(b.upd_dev);
     }
     ctx->scenes.erase(scene_id);
     delete s;

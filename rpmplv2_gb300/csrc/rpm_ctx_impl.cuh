@@ -1,0 +1,139 @@
+// rpm_ctx_impl.cuh -- internal state of a context (robots, versioned scenes,
+// per-stream scratch) shared by the C ABI translation units.  Not part of the
+// public interface.
+#pragma once
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "rpm_edges.cuh"
+#include "rpm_launch.cuh"
+
+namespace rpm {
+namespace impl {
+
+extern thread_local std::string g_err;
+
+inline int fail(int code, const char *fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    g_err = buf;
+    return code;
+}
+
+#define CK(x)                                                                                                \
+    do {                                                                                                     \
+        cudaError_t e_ = (x);                                                                                \
+        if (e_ != cudaSuccess) return ::rpm::impl::fail(RPM_ERR_CUDA, "%s: %s", #x, cudaGetErrorString(e_)); \
+    } while (0)
+
+constexpr int kRing = 8;   // versions kept per scene
+
+struct RobotRec {
+    rpm_robot_desc desc;
+    DevRobot *dev = nullptr;
+};
+
+struct SceneBuf {
+    void *mem = nullptr;
+    float *f = nullptr;
+    double *d = nullptr;
+    std::vector<cudaEvent_t> users;   // checks that may still read this buffer
+    cudaEvent_t ready = nullptr;      // end of the incremental update that wrote this version
+    bool pending = false;             // 'ready' must be waited on before reading
+    // staging of the incremental update list that produced this version
+    float *upd_host = nullptr;        // pinned, [m][7]: index (as bits) + six AABB values
+    float *upd_dev = nullptr;
+    int32_t upd_cap = 0;
+};
+
+struct SceneRec {
+    int robot = 0;
+    int n = 0, n_pad = 16;
+    std::vector<float> aabb, tol;
+    std::vector<uint8_t> flags;
+    int cur = 0;
+    SceneBuf bufs[kRing];
+    uint64_t version = 0;
+};
+
+struct Scratch {
+    uint64_t *recheck = nullptr;
+    size_t cap = 0;
+    uint32_t *counters = nullptr;   // [0] recheck count, [1] overflow
+    int32_t *status = nullptr;
+    int64_t last_configs = 0;
+    cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};   // bulk start, bulk end / recheck start, recheck end
+    bool timed = false, had_recheck = false;
+    // edge checks
+    size_t ecap = 0;
+    int32_t *n_e = nullptr, *local = nullptr, *kmax = nullptr;
+    int64_t *bprefix = nullptr;
+    uint8_t *full = nullptr;
+    unsigned long long *work = nullptr;
+    uint64_t *erecheck = nullptr;
+    size_t erecheck_cap = 0;
+    // cached CUDA graphs of edge calls, keyed by their arguments
+    struct Graph { std::vector<uint64_t> key; cudaGraphExec_t exec; };
+    std::vector<Graph> graphs;
+};
+
+// One segment of a launch: a scene and its configurations / outputs.
+struct SegReq {
+    SceneRec *scene;
+    const float *q;
+    int64_t count;
+    uint8_t *valid;
+    double *dist;
+    float *profile;
+};
+
+}  // namespace impl
+}  // namespace rpm
+
+struct rpm_ctx {
+    int device = 0;
+    int num_sms = 0;
+    rpm_params params{1e-4, 1000.0};
+    std::mutex mu;
+    std::vector<rpm::impl::RobotRec> robots;
+    std::map<int, rpm::impl::SceneRec *> scenes;
+    int next_scene = 0;
+    std::map<cudaStream_t, rpm::impl::Scratch *> scratch;
+    std::vector<cudaEvent_t> event_pool;
+    cudaStream_t upd_stream = nullptr;    // incremental scene updates
+    // host-buffer pipeline
+    cudaStream_t hs[2] = {nullptr, nullptr};
+    float *hq[2] = {nullptr, nullptr};
+    uint8_t *hv[2] = {nullptr, nullptr};
+    double *hd[2] = {nullptr, nullptr};
+    float *hp[2] = {nullptr, nullptr};
+    size_t hcap_cfg = 0, hcap_prof = 0;
+    bool timing = false;
+    bool use_graphs = false;
+    std::map<std::pair<int, int>, int> edge_ctas;   // (robot, precision) -> CTAs per SM of the edge kernel
+};
+
+namespace rpm {
+namespace impl {
+// helpers defined in rpm_api.cu; callers hold ctx->mu
+int set_device(rpm_ctx *ctx);
+cudaEvent_t get_event(rpm_ctx *ctx);
+void prune_users(rpm_ctx *ctx, SceneBuf &b);
+void wait_users(rpm_ctx *ctx, SceneBuf &b);
+int get_scratch(rpm_ctx *ctx, cudaStream_t st, int64_t need, Scratch **out);
+SceneRec *find_scene(rpm_ctx *ctx, int id);
+int enqueue_segments(rpm_ctx *ctx, int prec, const std::vector<SegReq> &reqs, cudaStream_t st);
+int edge_scratch(rpm_ctx *ctx, Scratch *sc, int64_t E, cudaStream_t st);
+int enqueue_edges(rpm_ctx *ctx, Scratch *sc, SceneRec *s, int prec, const float *q1, const float *q2, int64_t E,
+                  float step, int32_t num_checks, uint8_t *valid, int32_t *checks, int ctas_per_sm, cudaStream_t st);
+int scene_update(rpm_ctx *ctx, SceneRec *s, const int32_t *idx, const float *aabb, int32_t m);
+}  // namespace impl
+}  // namespace rpm

@@ -228,4 +228,6 @@ ABI_SYMBOLS = [
     "rpm_box_aabb", "rpm_check_configs", "rpm_check_configs_host", "rpm_skeleton", "rpm_last_stats", "rpm_sync",
     "rpm_ctx_set_timing", "rpm_last_timing", "rpm_probe_fp32_peak", "rpm_check_configs_noalloc", "rpm_check_batch",
     "rpm_check_edges", "rpm_ctx_set_graphs", "rpm_autotune_edges", "rpm_set_edge_ctas",
+    "rpm_server_create", "rpm_server_submit", "rpm_server_poll", "rpm_server_wait", "rpm_server_release",
+    "rpm_server_replay", "rpm_server_stats", "rpm_server_destroy",
 ]

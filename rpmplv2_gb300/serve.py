@@ -1,0 +1,268 @@
+"""Python front end of the serving loop (rpm_server_* in include/rpm_gpu.h) and
+the serving workload: resident scenes from the reference's robots, moving
+obstacles, and a Poisson trace of mixed-size isValid / distance / edge
+requests (DRGBT-style replanning traffic from many planners)."""
+import ctypes
+import math
+
+import numpy as np
+
+from . import robots as _robots
+from . import scenes as _scenes
+from .engine import _check, _i32, _i64, _vp, load
+
+RPM_REQ_CONFIGS = 0
+RPM_REQ_EDGES = 1
+
+
+class ServerConfig(ctypes.Structure):
+    _fields_ = [("num_slots", ctypes.c_int32), ("precision", ctypes.c_int32), ("memory_budget", ctypes.c_int64),
+                ("max_batch_segments", ctypes.c_int32), ("max_batch_configs", ctypes.c_int32)]
+
+
+class Request(ctypes.Structure):
+    _fields_ = [("kind", ctypes.c_int32), ("scene_id", ctypes.c_int32), ("count", ctypes.c_int64),
+                ("q_host", ctypes.c_void_p), ("q1_host", ctypes.c_void_p), ("q2_host", ctypes.c_void_p),
+                ("step", ctypes.c_float), ("num_checks", ctypes.c_int32), ("valid_host", ctypes.c_void_p),
+                ("dist_host", ctypes.c_void_p), ("profile_host", ctypes.c_void_p), ("checks_host", ctypes.c_void_p)]
+
+
+class Timing(ctypes.Structure):
+    _fields_ = [("status", ctypes.c_int32), ("batch_size", ctypes.c_int32), ("t_submit", ctypes.c_double),
+                ("t_admit", ctypes.c_double), ("t_launch", ctypes.c_double), ("t_done", ctypes.c_double)]
+
+
+class Motion(ctypes.Structure):
+    _fields_ = [("scene_id", ctypes.c_int32), ("index", ctypes.c_int32), ("velocity", ctypes.c_float * 3)]
+
+
+def _bind(L):
+    if getattr(L, "_rpm_server_bound", False):
+        return
+    L.rpm_server_create.argtypes = [_vp, ctypes.POINTER(ServerConfig), ctypes.POINTER(_vp)]
+    L.rpm_server_submit.argtypes = [_vp, ctypes.POINTER(Request), ctypes.POINTER(ctypes.c_uint64)]
+    L.rpm_server_poll.argtypes = [_vp, ctypes.c_uint64, ctypes.POINTER(Timing)]
+    L.rpm_server_wait.argtypes = [_vp, ctypes.c_uint64, ctypes.c_double, ctypes.POINTER(Timing)]
+    L.rpm_server_release.argtypes = [_vp, ctypes.c_uint64]
+    L.rpm_server_replay.argtypes = [_vp, _vp, _vp, _i64, _vp, _i32, ctypes.c_double, _vp]
+    L.rpm_server_stats.argtypes = [_vp, ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(ctypes.c_int64)]
+    L.rpm_server_destroy.argtypes = [_vp]
+    L._rpm_server_bound = True
+
+
+def _addr(a):
+    return None if a is None else a.ctypes.data
+
+
+def pinned(shape, dtype):
+    """A numpy array in page-locked host memory (copies to and from it
+    overlap); plain host memory where no CUDA driver is present.  The array's
+    base is the pinned torch tensor, which keeps the storage alive."""
+    import torch
+    dt = {np.float32: torch.float32, np.float64: torch.float64, np.uint8: torch.uint8,
+          np.int32: torch.int32}[np.dtype(dtype).type]
+    t = torch.empty(shape, dtype=dt)
+    if torch.cuda.is_available():
+        t = t.pin_memory()
+    return t.numpy()
+
+
+class Server:
+    def __init__(self, engine, num_slots=4, precision="fp32_recheck", memory_budget=8 << 30, max_batch_segments=32,
+                 max_batch_configs=1 << 18):
+        from ._abi import PRECISIONS
+        self.engine = engine
+        self.lib = load()
+        _bind(self.lib)
+        cfg = ServerConfig(num_slots, PRECISIONS[precision], memory_budget, max_batch_segments, max_batch_configs)
+        self.srv = _vp()
+        _check(self.lib.rpm_server_create(engine.ctx, ctypes.byref(cfg), ctypes.byref(self.srv)))
+
+    def close(self):
+        if self.srv:
+            self.lib.rpm_server_destroy(self.srv)
+            self.srv = _vp()
+
+    def submit(self, req):
+        t = ctypes.c_uint64()
+        _check(self.lib.rpm_server_submit(self.srv, ctypes.byref(req), ctypes.byref(t)))
+        return t.value
+
+    def wait(self, ticket, timeout=120.0):
+        tm = Timing()
+        rc = self.lib.rpm_server_wait(self.srv, ticket, timeout, ctypes.byref(tm))
+        self.lib.rpm_server_release(self.srv, ticket)
+        _check(rc)
+        return tm
+
+    def replay(self, reqs, arrivals, motions=(), period=0.0):
+        n = len(reqs)
+        arr = (Request * n)(*reqs)
+        ts = np.ascontiguousarray(arrivals, np.float64)
+        mot = (Motion * max(1, len(motions)))(*motions) if motions else None
+        out = (Timing * n)()
+        _check(self.lib.rpm_server_replay(self.srv, ctypes.addressof(arr), ts.ctypes.data, n,
+                                          ctypes.addressof(mot) if mot is not None else None, len(motions),
+                                          float(period), ctypes.addressof(out)))
+        return [out[i] for i in range(n)]
+
+    def stats(self):
+        b, p = ctypes.c_int64(), ctypes.c_int64()
+        _check(self.lib.rpm_server_stats(self.srv, ctypes.byref(b), ctypes.byref(p)))
+        return {"batches": b.value, "pending": p.value}
+
+
+def configs_request(scene_id, q, valid=None, dist=None, profile=None):
+    return Request(RPM_REQ_CONFIGS, scene_id, q.shape[0], _addr(q), None, None, 0.0, 0, _addr(valid), _addr(dist),
+                   _addr(profile), None)
+
+
+def edges_request(scene_id, q1, q2, valid, checks=None, step=0.05, num_checks=10):
+    return Request(RPM_REQ_EDGES, scene_id, q1.shape[0], None, _addr(q1), _addr(q2), step, num_checks, _addr(valid),
+                   None, None, _addr(checks))
+
+
+# ----------------------------------------------------------------- workload --
+def reject_touching(robot, aabbs, margin=0.01, samples=33):
+    """Mask of boxes that stay clear of the capsule skeleton at q = 0 (the
+    reference's generator drops obstacles that invalidate the start)."""
+    sk = robot.skeleton_np(np.zeros(robot.num_dofs))
+    t = np.linspace(0.0, 1.0, samples)
+    pts = sk[:-1, None, :] + t[None, :, None] * (sk[1:] - sk[:-1])[:, None, :]        # (L, S, 3)
+    seg_len = np.linalg.norm(sk[1:] - sk[:-1], axis=1) / (samples - 1)
+    lo, hi = aabbs[:, None, None, :3], aabbs[:, None, None, 3:]
+    d = np.maximum(np.maximum(lo - pts[None], pts[None] - hi), 0.0)
+    dist = np.sqrt((d * d).sum(-1)).min(-1)                                              # (n, L)
+    need = robot.capsule_radius[None, :] + margin + seg_len[None, :]
+    return (dist > need).all(1)
+
+
+def _scene_for(robot, rng, n):
+    if robot.name == "planar_2dof":
+        dims = rng.uniform(0.1, 0.5, (n, 2))
+        rr, th = 2.0 * np.sqrt(rng.uniform(size=n)), rng.uniform(0, 2 * math.pi, n)
+        c = np.stack([rr * np.cos(th), rr * np.sin(th), np.zeros(n)], 1)
+        h = np.concatenate([dims / 2, np.full((n, 1), 0.05)], 1)
+        return _scenes.Scene(np.concatenate([c - h, c + h], 1).astype(np.float32))
+    if robot.name == "xarm6":
+        boxes, g_aabb, g_tol = [], *_scenes.ground_box()
+        center, radius, half = np.array([0.0, 0.0, 0.267]), 1.0, 0.025
+    else:
+        boxes, center, radius = [], np.array(_scenes.SPATIAL_WS_CENTER), 1.2
+    out = np.zeros((0, 6), np.float32)
+    while out.shape[0] < n:
+        m = 2 * (n - out.shape[0]) + 8
+        p = rng.uniform(-1, 1, (m, 3))
+        c = center + radius * p[(p * p).sum(1) <= 1.0]
+        hh = np.full((c.shape[0], 3), half) if robot.name == "xarm6" else rng.uniform(0.01, 0.05, (c.shape[0], 3))
+        cand = np.concatenate([c - hh, c + hh], 1).astype(np.float32)
+        out = np.concatenate([out, cand[reject_touching(robot, cand)]])[:n]
+    if robot.name == "xarm6":
+        aabb = np.concatenate([g_aabb[None, :], out])
+        tol = np.full(n + 1, _scenes.MAX_DISTANCE, np.float32)
+        tol[0] = g_tol
+        flags = np.zeros(n + 1, np.uint8)
+        flags[0] = 1
+        return _scenes.Scene(aabb, tol, flags)
+    return _scenes.Scene(out)
+
+
+SERVE_ROBOTS = ("planar_2dof", "xarm6", "spatial_10dof", "spatial_14dof", "spatial_18dof", "spatial_22dof")
+
+
+def make_robot(name):
+    if name == "planar_2dof":
+        return _robots.planar_2dof(radius=0.0)
+    if name == "xarm6":
+        return _robots.xarm6(radius=0.05, gripper_length=0.1, ground_included=2)
+    return _robots.by_name(name, radius=0.03)
+
+
+def serving_workload(engine, seed=4, n_scenes=64, rate=20000.0, duration=0.5, max_size=65536, dynamic_frac=0.2,
+                     n_dynamic=5, max_speed=1.6, edge_divisor=16, pool=65536, distinct_outputs=False):
+    """Scenes on the device, a Poisson request trace and the moving obstacles.
+
+    Request sizes are log-uniform in [1, max_size]; kinds are isValid,
+    isValid + computeDistance and edge checks in equal shares.  An edge
+    request of size s carries max(1, s // edge_divisor) edges at 0.05 rad
+    steps (about 12 checks each), so its work is near a configuration
+    request of the same size.  Inputs are slices of per-DOF pinned pools;
+    outputs alias shared pinned pools unless distinct_outputs is set."""
+    rng = np.random.default_rng(seed)
+    robots = {name: make_robot(name) for name in SERVE_ROBOTS}
+    rids = {name: engine.upload_robot(r) for name, r in robots.items()}
+    scene_ids, scene_robot, motions = [], [], []
+    for s in range(n_scenes):
+        name = SERVE_ROBOTS[rng.integers(len(SERVE_ROBOTS))]
+        n = int(round(math.exp(rng.uniform(math.log(10), math.log(1000)))))
+        sc = _scene_for(robots[name], rng, n)
+        sid = engine.create_scene(rids[name], sc)
+        scene_ids.append(sid)
+        scene_robot.append(name)
+        if rng.uniform() < dynamic_frac:
+            first = 1 if name == "xarm6" else 0
+            for j in rng.choice(np.arange(first, sc.n), size=min(n_dynamic, sc.n - first), replace=False):
+                u = rng.normal(size=3)
+                u = u / np.linalg.norm(u) * rng.uniform(0, max_speed)
+                motions.append(Motion(sid, int(j), (ctypes.c_float * 3)(*u)))
+    dofs = sorted({robots[n].num_dofs for n in SERVE_ROBOTS})
+    qpool = {d: pinned((pool, d), np.float32) for d in dofs}
+    q2pool = {}
+    for d in dofs:
+        qpool[d][:] = rng.uniform(-math.pi, math.pi, (pool, d))
+        u = rng.normal(size=(pool, d))
+        u /= np.linalg.norm(u, axis=1, keepdims=True)
+        q2pool[d] = pinned((pool, d), np.float32)
+        q2pool[d][:] = qpool[d] + u * rng.uniform(0.01, 2.0, (pool, 1))
+    shared = {"valid": pinned(pool, np.uint8), "dist": pinned(pool, np.float64), "checks": pinned(pool, np.int32)}
+    n_req = rng.poisson(rate * duration)
+    arrivals = np.sort(rng.uniform(0, duration, n_req))
+    reqs, meta, keep = [], [], []
+    for i in range(n_req):
+        s = int(rng.integers(n_scenes))
+        name = scene_robot[s]
+        d = robots[name].num_dofs
+        size = int(min(max_size, round(math.exp(rng.uniform(0, math.log(max_size))))))
+        kind = int(rng.integers(3))
+        off = int(rng.integers(0, pool - size + 1))
+        if kind == 2:
+            ne = max(1, size // edge_divisor)
+            off = int(rng.integers(0, pool - ne + 1))
+            v = pinned(ne, np.uint8) if distinct_outputs else shared["valid"][:ne]
+            k = pinned(ne, np.int32) if distinct_outputs else shared["checks"][:ne]
+            q1, q2 = qpool[d][off:off + ne], q2pool[d][off:off + ne]
+            reqs.append(edges_request(scene_ids[s], q1, q2, v, k, step=0.05))
+            keep += [v, k]
+            meta.append(("edges", size, ne, s, q1, q2, v, k))
+        else:
+            q = qpool[d][off:off + size]
+            v = pinned(size, np.uint8) if distinct_outputs else shared["valid"][:size]
+            dd = None
+            if kind == 1:
+                dd = pinned(size, np.float64) if distinct_outputs else shared["dist"][:size]
+            reqs.append(configs_request(scene_ids[s], q, v, dd))
+            keep += [v, dd]
+            meta.append(("valid" if kind == 0 else "distance", size, size, s, q, None, v, dd))
+    return {"scene_ids": scene_ids, "scene_robot": scene_robot, "robots": robots, "requests": reqs,
+            "arrivals": arrivals, "meta": meta, "motions": motions, "pools": (qpool, q2pool, shared), "keep": keep}
+
+
+def latency_summary(timings, meta, bucket=(2048, 8192)):
+    lat = np.array([t.t_done - t.t_submit for t in timings])
+    ok = np.array([t.status == 0 for t in timings])
+    sizes = np.array([m[1] for m in meta])
+    sel = ok & (sizes >= bucket[0]) & (sizes <= bucket[1])
+    small = ok & (sizes <= 4096)
+    pct = lambda a, p: float(np.percentile(a, p)) * 1e3 if a.size else None
+    work = sum(m[2] for m, o in zip(meta, ok) if o)
+    span = max(t.t_done for t in timings) - min(t.t_submit for t in timings) if timings else 0.0
+    return {"requests": int(len(timings)), "completed": int(ok.sum()),
+            "rejected": int(sum(t.status == -5 for t in timings)),
+            "p50_ms": pct(lat[ok], 50), "p99_ms": pct(lat[ok], 99),
+            "p50_ms_4096": pct(lat[sel], 50), "p99_ms_4096": pct(lat[sel], 99),
+            "bucket_4096": list(bucket), "p99_ms_le4096": pct(lat[small], 99),
+            "queries_per_s": float(ok.sum() / span) if span > 0 else None,
+            "configs_or_edges_per_s": float(work / span) if span > 0 else None,
+            "mean_batch": float(np.mean([t.batch_size for t in timings])) if timings else None,
+            "median_queue_ms": pct(np.array([t.t_launch - t.t_submit for t in timings])[ok], 50),
+            "median_run_ms": pct(np.array([t.t_done - t.t_launch for t in timings])[ok], 50)}
