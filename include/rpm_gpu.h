@@ -85,6 +85,13 @@ enum rpm_precision {
     RPM_PREC_FP32_REF = 2       /* the reference's own numerics: FP64 FK rounded to FP32, FP32 narrow phase */
 };
 
+/* How configuration checks are spread over the GPU.  Results are identical. */
+enum rpm_layout {
+    RPM_LAYOUT_AUTO = 0,        /* chosen per segment from the scene size, link count and batch size */
+    RPM_LAYOUT_LANE = 1,        /* one lane per configuration, obstacles walked in order */
+    RPM_LAYOUT_WARP = 2         /* one warp per configuration over the spatially sorted obstacles */
+};
+
 typedef struct rpm_ctx rpm_ctx;
 
 /* Statistics of the last check issued on a context (read after a sync). */
@@ -185,6 +192,10 @@ int rpm_ctx_set_graphs(rpm_ctx *ctx, int enable);
 int rpm_autotune_edges(rpm_ctx *ctx, int32_t scene_id, int32_t precision, const float *q1_dev, const float *q2_dev,
                        int64_t num_edges, float step, int32_t num_checks, uint8_t *valid_dev, int32_t *ctas_out);
 int rpm_set_edge_ctas(rpm_ctx *ctx, int32_t scene_id, int32_t precision, int32_t ctas_per_sm);
+/* Layout of the configuration checks (rpm_check_configs, rpm_check_batch,
+ * rpm_check_configs_host and the server): one of enum rpm_layout.  A GB300
+ * addition with no reference counterpart; outputs do not depend on it. */
+int rpm_ctx_set_layout(rpm_ctx *ctx, int32_t layout);
 
 /* Skeleton points (L+1 points x 3) per configuration, widened to double
  * (computeSkeleton; xArm6.cpp:209-235, Planar2DOF.cpp:117-130): RPM_PREC_FP64

@@ -23,6 +23,12 @@ RPM_PREC_FP32_REF = 2
 
 PRECISIONS = {"fp64": RPM_PREC_FP64, "fp32_recheck": RPM_PREC_FP32_RECHECK, "fp32_ref": RPM_PREC_FP32_REF}
 
+RPM_LAYOUT_AUTO = 0
+RPM_LAYOUT_LANE = 1
+RPM_LAYOUT_WARP = 2
+
+LAYOUTS = {"auto": RPM_LAYOUT_AUTO, "lane": RPM_LAYOUT_LANE, "warp": RPM_LAYOUT_WARP}
+
 
 class RobotDesc(ctypes.Structure):
     _fields_ = [

@@ -9,6 +9,7 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <limits>
 #include <map>
 #include <mutex>
 #include <string>
@@ -57,13 +58,146 @@ void wait_users(rpm_ctx *ctx, SceneBuf &b) {
     b.users.clear();
 }
 
+// Spread the low 10 bits of v to every third bit (Morton interleave).
+static uint32_t spread10(uint32_t v) {
+    v &= 1023u;
+    v = (v | (v << 16)) & 0x030000FFu;
+    v = (v | (v << 8)) & 0x0300F00Fu;
+    v = (v | (v << 4)) & 0x030C30C3u;
+    v = (v | (v << 2)) & 0x09249249u;
+    return v;
+}
+
+void sorted_layout(SceneRec &s) {
+    std::vector<int> ground, other;
+    for (int j = 0; j < s.n; ++j) ((s.flags[j] & RPM_OBS_GROUND) ? ground : other).push_back(j);
+    const float big = std::numeric_limits<float>::infinity();
+    float lo[3] = {big, big, big}, hi[3] = {-big, -big, -big};
+    auto centre = [&](int j, int k) { return 0.5f * (s.aabb[6 * (size_t)j + k] + s.aabb[6 * (size_t)j + 3 + k]); };
+    for (int j : other)
+        for (int k = 0; k < 3; ++k) {
+            const float c = centre(j, k);
+            if (!std::isfinite(c)) continue;   // NaN and infinite centres do not shape the frame
+            lo[k] = std::min(lo[k], c);
+            hi[k] = std::max(hi[k], c);
+        }
+    std::vector<std::pair<uint32_t, int>> key;
+    key.reserve(other.size());
+    for (int j : other) {
+        uint32_t code = 0;
+        for (int k = 0; k < 3; ++k) {
+            const float c = centre(j, k);
+            const float span = hi[k] - lo[k];
+            float t = (span > 0.f && span < big && c == c) ? (c - lo[k]) / span : 0.f;
+            t = t < 0.f ? 0.f : (t > 1.f ? 1.f : t);
+            code |= spread10((uint32_t)(t * 1023.f)) << k;
+        }
+        key.push_back({code, j});
+    }
+    std::sort(key.begin(), key.end());
+    const int m = (int)other.size(), g = (int)ground.size();
+    const int mr = (m + 31) / 32 * 32, gr = (g + 31) / 32 * 32;
+    s.ns = std::max(32, mr + gr);
+    s.nb = s.ns / 32;
+    s.perm.assign(s.ns, -1);
+    for (int k = 0; k < m; ++k) s.perm[k] = key[k].second;
+    for (int k = 0; k < g; ++k) s.perm[mr + k] = ground[k];
+}
+
+size_t scene_bytes(const SceneRec &s) {
+    const size_t np = (size_t)s.n_pad, ns = (size_t)s.ns;
+    return kFRows * np * sizeof(float) + kDRows * np * sizeof(double) + 8 * ns * sizeof(float) +
+           7 * ns * sizeof(double) + (size_t)s.nb * kBlkRec * sizeof(float) + ns * sizeof(int32_t);
+}
+
+void bind_scene_buf(const SceneRec &s, SceneBuf &b) {
+    const size_t np = (size_t)s.n_pad, ns = (size_t)s.ns;
+    char *p = reinterpret_cast<char *>(b.mem);
+    b.f = reinterpret_cast<float *>(p);
+    p += kFRows * np * sizeof(float);
+    b.d = reinterpret_cast<double *>(p);
+    p += kDRows * np * sizeof(double);
+    b.sf = reinterpret_cast<float *>(p);
+    p += 8 * ns * sizeof(float);
+    b.sd = reinterpret_cast<double *>(p);
+    p += 7 * ns * sizeof(double);
+    b.blk = reinterpret_cast<float *>(p);
+    p += (size_t)s.nb * kBlkRec * sizeof(float);
+    b.perm = reinterpret_cast<int32_t *>(p);
+}
+
+// Gather the sorted copy of a version from its rows and bound each block of
+// 32 slots (one warp per block).  Padding slots get bounds +inf / -inf so no
+// gap test passes them; a block holding a NaN coordinate gets infinite bounds
+// so it is never skipped.
+__global__ void k_scene_sort(const float *f, const double *d, int n_pad, const int32_t *perm, int ns, float *sf,
+                             double *sd, float *blk) {
+    const int s = blockIdx.x * 32 + threadIdx.x;
+    const int j = perm[s];
+    const float inf = __int_as_float(0x7f800000);
+    float lo[3], hi[3], tmax = -inf, tmin = inf;
+    bool nan = false;
+    uint32_t id = kPadIdx;
+    if (j >= 0) {
+        for (int c = 0; c < kDRows; ++c) {
+            sf[c * ns + s] = f[c * n_pad + j];
+            sd[c * ns + s] = d[c * n_pad + j];
+        }
+        for (int c = 0; c < 3; ++c) {
+            lo[c] = f[c * n_pad + j];
+            hi[c] = f[(3 + c) * n_pad + j];
+            nan = nan || !(lo[c] == lo[c]) || !(hi[c] == hi[c]);
+        }
+        const float tol = f[kRowTol * n_pad + j];
+        tmax = (tol == tol) ? tol : inf;
+        tmin = (tol == tol) ? tol : inf;
+        id = (uint32_t)j | (f[kRowGround * n_pad + j] != 0.f ? kGroundBit : 0u);
+    } else {
+        for (int c = 0; c < 3; ++c) {
+            lo[c] = inf;
+            hi[c] = -inf;
+            sf[c * ns + s] = inf;
+            sf[(3 + c) * ns + s] = -inf;
+            sd[c * ns + s] = (double)inf;
+            sd[(3 + c) * ns + s] = -(double)inf;
+        }
+        sf[kRowTol * ns + s] = 0.f;
+        sd[kRowTol * ns + s] = 0.0;
+    }
+    sf[7 * ns + s] = __uint_as_float(id);
+    const unsigned full = 0xffffffffu;
+    nan = __any_sync(full, nan);
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+        for (int c = 0; c < 3; ++c) {
+            lo[c] = fminf(lo[c], __shfl_xor_sync(full, lo[c], off));
+            hi[c] = fmaxf(hi[c], __shfl_xor_sync(full, hi[c], off));
+        }
+        tmax = fmaxf(tmax, __shfl_xor_sync(full, tmax, off));
+        tmin = fminf(tmin, __shfl_xor_sync(full, tmin, off));
+    }
+    if (threadIdx.x == 0) {
+        float *r = blk + (size_t)blockIdx.x * kBlkRec;
+        for (int c = 0; c < 3; ++c) {
+            r[c] = nan ? -inf : lo[c];
+            r[3 + c] = nan ? inf : hi[c];
+        }
+        r[6] = (tmax == -inf) ? 0.f : tmax;   // an all-padding block
+        r[7] = (tmin == inf) ? 0.f : tmin;
+    }
+}
+
+cudaError_t launch_scene_sort(const SceneRec &s, const SceneBuf &b, cudaStream_t st) {
+    k_scene_sort<<<s.nb, 32, 0, st>>>(b.f, b.d, s.n_pad, b.perm, s.ns, b.sf, b.sd, b.blk);
+    return cudaGetLastError();
+}
+
 int upload_scene(rpm_ctx *ctx, SceneRec &s, SceneBuf &b) {
     const int np = s.n_pad;
     if (!b.mem) {
-        const size_t bytes = (size_t)kFRows * np * sizeof(float) + (size_t)kDRows * np * sizeof(double);
+        const size_t bytes = scene_bytes(s);
         if (cudaMalloc(&b.mem, bytes) != cudaSuccess) return fail(RPM_ERR_NOMEM, "scene allocation of %zu bytes failed", bytes);
-        b.f = reinterpret_cast<float *>(b.mem);
-        b.d = reinterpret_cast<double *>(reinterpret_cast<char *>(b.mem) + (size_t)kFRows * np * sizeof(float));
+        bind_scene_buf(s, b);
     }
     std::vector<float> f((size_t)kFRows * np, 0.f);
     std::vector<double> d((size_t)kDRows * np, 0.0);
@@ -76,6 +210,9 @@ int upload_scene(rpm_ctx *ctx, SceneRec &s, SceneBuf &b) {
     (void)ctx;
     CK(cudaMemcpy(b.f, f.data(), f.size() * sizeof(float), cudaMemcpyHostToDevice));
     CK(cudaMemcpy(b.d, d.data(), d.size() * sizeof(double), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(b.perm, s.perm.data(), s.perm.size() * sizeof(int32_t), cudaMemcpyHostToDevice));
+    CK(launch_scene_sort(s, b, 0));
+    CK(cudaStreamSynchronize(0));
     return RPM_OK;
 }
 
@@ -156,8 +293,23 @@ SceneRec *find_scene(rpm_ctx *ctx, int id) {
     return it == ctx->scenes.end() ? nullptr : it->second;
 }
 
+// Layout of one segment.  Lane-per-configuration walks a scene's obstacles in
+// series per lane, which suits small scenes and large batches; warp-per-
+// configuration culls whole blocks of the sorted copy and spreads the
+// survivors over a warp, which suits large scenes and batches too small to
+// fill the GPU with lanes.
+static bool use_warp_layout(const rpm_ctx *ctx, const SegReq &r, int64_t total) {
+    if (ctx->layout == RPM_LAYOUT_LANE) return false;
+    if (ctx->layout == RPM_LAYOUT_WARP) return true;
+    const int L = ctx->robots[r.scene->robot].desc.num_dofs;
+    const int64_t lane_warps = (total + 31) / 32;
+    if (r.scene->n >= kWideMinObstacles) return true;
+    return lane_warps < (int64_t)ctx->num_sms * 4 && (int64_t)r.scene->n * L >= kWideMinPairs;
+}
+
 // Queue checks of up to kMaxSegs segments as one launch on 'st' (more
-// segments become several launches).  The caller holds ctx->mu.
+// segments, or segments of both layouts, become several launches).  The
+// caller holds ctx->mu.
 int enqueue_segments(rpm_ctx *ctx, int prec, const std::vector<SegReq> &reqs, cudaStream_t st) {
     int64_t total = 0;
     for (const SegReq &r : reqs) total += r.count;
@@ -171,14 +323,40 @@ int enqueue_segments(rpm_ctx *ctx, int prec, const std::vector<SegReq> &reqs, cu
     if (sc->timed && !sc->ev[0])
         for (int i = 0; i < 3; ++i) CK(cudaEventCreate(&sc->ev[i]));
     if (sc->timed) CK(cudaEventRecord(sc->ev[0], st));
+    // chunks of at most kMaxSegs segments of one layout
+    std::vector<std::pair<bool, std::vector<const SegReq *>>> chunks;
+    for (int wide = 0; wide < 2; ++wide) {
+        std::vector<const SegReq *> cur;
+        for (const SegReq &r : reqs) {
+            if (r.count <= 0 || use_warp_layout(ctx, r, total) != (wide == 1)) continue;
+            cur.push_back(&r);
+            if ((int)cur.size() == kMaxSegs) { chunks.push_back({wide == 1, cur}); cur.clear(); }
+        }
+        if (!cur.empty()) chunks.push_back({wide == 1, cur});
+    }
+    const size_t tsz = prec == RPM_PREC_FP64 ? sizeof(double) : sizeof(float);
     std::vector<SceneBuf *> used;
-    for (size_t off = 0; off < reqs.size(); off += kMaxSegs) {
+    for (size_t ci = 0; ci < chunks.size(); ++ci) {
+        const bool wide = chunks[ci].first;
+        const std::vector<const SegReq *> &segs = chunks[ci].second;
+        const bool last = ci + 1 == chunks.size();
         KParams p;
         std::memset(&p, 0, sizeof p);
+        int64_t chunk_total = 0;
+        int gmax = 32;
+        for (const SegReq *r : segs) {
+            chunk_total += r->count;
+            const int D = ctx->robots[r->scene->robot].desc.num_dofs;
+            gmax = std::min(gmax, kWidePtsBytes / ((D + 1) * 3 * (int)tsz));
+        }
+        // configurations per warp: enough warps for two waves of two CTAs per SM
+        const int64_t want = (chunk_total + (int64_t)ctx->num_sms * 32 - 1) / ((int64_t)ctx->num_sms * 32);
+        p.wide_g = (int32_t)std::max<int64_t>(1, std::min<int64_t>(gmax, want));
+        const int64_t per_cta = wide ? (int64_t)kWideWarps * p.wide_g : kThreads;
         int64_t blocks = 0;
-        int max_pad = 16;
-        for (size_t k = off; k < reqs.size() && k < off + kMaxSegs; ++k) {
-            const SegReq &r = reqs[k];
+        size_t smem = 0;
+        for (const SegReq *rp : segs) {
+            const SegReq &r = *rp;
             SceneBuf &buf = r.scene->bufs[r.scene->cur];
             if (buf.pending) {   // an incremental update still writing this version
                 if (cudaEventQuery(buf.ready) == cudaSuccess) buf.pending = false;
@@ -197,8 +375,14 @@ int enqueue_segments(rpm_ctx *ctx, int prec, const std::vector<SegReq> &reqs, cu
             g.first_block = blocks;
             g.n = r.scene->n;
             g.n_pad = r.scene->n_pad;
-            blocks += (r.count + kThreads - 1) / kThreads;
-            max_pad = std::max(max_pad, r.scene->n_pad);
+            g.srt_f = buf.sf;
+            g.srt_d = buf.sd;
+            g.blk = buf.blk;
+            g.ns = r.scene->ns;
+            g.nb = r.scene->nb;
+            blocks += (r.count + per_cta - 1) / per_cta;
+            smem = std::max(smem, wide ? wide_smem_bytes(prec, r.scene->ns, r.scene->nb)
+                                       : smem_bytes(prec == RPM_PREC_FP32_RECHECK ? RPM_PREC_FP32_REF : prec, r.scene->n_pad));
         }
         p.nmd.eq = ctx->params.equality_threshold;
         p.nmd.maxd = ctx->params.max_distance;
@@ -207,19 +391,17 @@ int enqueue_segments(rpm_ctx *ctx, int prec, const std::vector<SegReq> &reqs, cu
         p.recheck = sc->recheck;
         p.recheck_count = sc->counters;
         p.status = sc->status;
-        if (blocks == 0) continue;
-        if (prec == RPM_PREC_FP32_RECHECK) {
-            CK(launch_check_fp32(p, blocks, smem_bytes(RPM_PREC_FP32_REF, max_pad), st));
-            if (sc->timed && off + kMaxSegs >= reqs.size()) CK(cudaEventRecord(sc->ev[1], st));
-            CK(launch_recheck(p, ctx->num_sms * 4, st));
-            // the recheck list is consumed per launch
-            if (off + kMaxSegs < reqs.size()) CK(cudaMemsetAsync(sc->counters, 0, sizeof(uint32_t), st));
-        } else {
-            CK(launch_check_exact(prec, p, blocks, smem_bytes(prec, max_pad), st));
-            if (sc->timed && off + kMaxSegs >= reqs.size()) CK(cudaEventRecord(sc->ev[1], st));
-        }
+        if (ci > 0) CK(cudaMemsetAsync(sc->counters, 0, sizeof(uint32_t), st));   // the recheck list is per launch
+        if (wide) CK(launch_check_wide(prec, p, blocks, smem, st));
+        else if (prec == RPM_PREC_FP32_RECHECK) CK(launch_check_fp32(p, blocks, smem, st));
+        else CK(launch_check_exact(prec, p, blocks, smem, st));
+        if (sc->timed && last) CK(cudaEventRecord(sc->ev[1], st));
+        if (prec == RPM_PREC_FP32_RECHECK) CK(launch_recheck(p, ctx->num_sms * 4, st));
     }
-    if (sc->timed) CK(cudaEventRecord(sc->ev[2], st));
+    if (sc->timed) {
+        if (chunks.empty()) CK(cudaEventRecord(sc->ev[1], st));
+        CK(cudaEventRecord(sc->ev[2], st));
+    }
     for (SceneBuf *b : used) {
         prune_users(ctx, *b);
         cudaEvent_t e = get_event(ctx);
@@ -386,6 +568,7 @@ int rpm_scene_create(rpm_ctx *ctx, int32_t robot_id, const float *aabb_host, con
         s->tol[j] = min_dist_tol_host ? min_dist_tol_host[j] : (float)ctx->params.max_distance;
         s->flags[j] = flags_host ? flags_host[j] : 0;
     }
+    sorted_layout(*s);
     int rc = upload_scene(ctx, *s, s->bufs[0]);
     if (rc) { delete s; return rc; }
     s->cur = 0;
@@ -543,6 +726,14 @@ int rpm_check_edges(rpm_ctx *ctx, int32_t scene_id, int32_t precision, const flo
     cudaEvent_t e = get_event(ctx);
     CK(cudaEventRecord(e, st));
     buf.users.push_back(e);
+    return RPM_OK;
+}
+
+int rpm_ctx_set_layout(rpm_ctx *ctx, int32_t layout) {
+    if (!ctx) return fail(RPM_ERR_INVALID, "NULL context");
+    if (layout < RPM_LAYOUT_AUTO || layout > RPM_LAYOUT_WARP) return fail(RPM_ERR_INVALID, "unknown layout %d", layout);
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    ctx->layout = layout;
     return RPM_OK;
 }
 

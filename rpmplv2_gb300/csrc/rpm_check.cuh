@@ -209,8 +209,8 @@ __device__ __forceinline__ void drain_bool(WarpShared<T> &sh, const DevRobot &rb
     }
 }
 
-template <int MODE, typename T>
-__device__ __forceinline__ T pair_distance(const DevRobot &rb, const ObsView<T> &ob, const Num<T> &nm, const T *A,
+template <int MODE, typename T, typename V>
+__device__ __forceinline__ T pair_distance(const DevRobot &rb, const V &ob, const Num<T> &nm, const T *A,
                                            const T *B, int i, int j, bool &settled) {
     typedef typename PolOf<MODE>::type P;
     T o[6];

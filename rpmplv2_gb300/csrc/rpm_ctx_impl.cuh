@@ -12,6 +12,7 @@
 
 #include "rpm_edges.cuh"
 #include "rpm_launch.cuh"
+#include "rpm_wide.cuh"
 
 namespace rpm {
 namespace impl {
@@ -41,10 +42,19 @@ struct RobotRec {
     DevRobot *dev = nullptr;
 };
 
+// One version of a scene's obstacles in device memory (one allocation):
+//   f [8][n_pad], d [7][n_pad]  rows in the caller's order
+//   sf [8][ns], sd [7][ns]      spatially sorted copy (row 7 of sf: original index | ground bit)
+//   blk [nb][8]                 bounds and tolerance range of each block of 32 sorted slots
+//   perm [ns]                   original index of each sorted slot (-1 = padding)
 struct SceneBuf {
     void *mem = nullptr;
     float *f = nullptr;
     double *d = nullptr;
+    float *sf = nullptr;
+    double *sd = nullptr;
+    float *blk = nullptr;
+    int32_t *perm = nullptr;
     std::vector<cudaEvent_t> users;   // checks that may still read this buffer
     cudaEvent_t ready = nullptr;      // end of the incremental update that wrote this version
     bool pending = false;             // 'ready' must be waited on before reading
@@ -57,6 +67,8 @@ struct SceneBuf {
 struct SceneRec {
     int robot = 0;
     int n = 0, n_pad = 16;
+    int ns = 32, nb = 1;            // sorted slots and blocks
+    std::vector<int32_t> perm;      // [ns] original index per sorted slot, -1 = padding
     std::vector<float> aabb, tol;
     std::vector<uint8_t> flags;
     int cur = 0;
@@ -118,6 +130,7 @@ struct rpm_ctx {
     size_t hcap_cfg = 0, hcap_prof = 0;
     bool timing = false;
     bool use_graphs = false;
+    int layout = RPM_LAYOUT_AUTO;    // lane- or warp-per-configuration checks
     std::map<std::pair<int, int>, int> edge_ctas;   // (robot, precision) -> CTAs per SM of the edge kernel
 };
 
@@ -135,5 +148,11 @@ int edge_scratch(rpm_ctx *ctx, Scratch *sc, int64_t E, cudaStream_t st);
 int enqueue_edges(rpm_ctx *ctx, Scratch *sc, SceneRec *s, int prec, const float *q1, const float *q2, int64_t E,
                   float step, int32_t num_checks, uint8_t *valid, int32_t *checks, int ctas_per_sm, cudaStream_t st);
 int scene_update(rpm_ctx *ctx, SceneRec *s, const int32_t *idx, const float *aabb, int32_t m);
+// Spatially sorted copy: Morton order of the obstacle centres (fixed for the
+// scene's lifetime), its size, and the kernel that rebuilds it in a version.
+void sorted_layout(SceneRec &s);
+size_t scene_bytes(const SceneRec &s);
+void bind_scene_buf(const SceneRec &s, SceneBuf &b);
+cudaError_t launch_scene_sort(const SceneRec &s, const SceneBuf &b, cudaStream_t st);
 }  // namespace impl
 }  // namespace rpm

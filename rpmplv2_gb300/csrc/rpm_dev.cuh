@@ -98,6 +98,11 @@ struct Seg {
     int64_t count;
     int64_t first_block;     // first CTA of this segment in the launch
     int32_t n, n_pad;
+    // spatially sorted copy (warp-per-configuration kernels)
+    const float *srt_f;      // [8][ns]: AABB, tol, original index | ground bit (as bits)
+    const double *srt_d;     // [7][ns]
+    const float *blk;        // [nb][8]: union bounds, max tol, min tol of each block of 32 slots
+    int32_t ns, nb;
 };
 
 struct LaunchCtl {

@@ -7,6 +7,7 @@
 #include "rpm_check.cuh"
 #include "rpm_edges.cuh"
 #include "rpm_launch.cuh"
+#include "rpm_wide.cuh"
 
 namespace rpm {
 
@@ -72,6 +73,17 @@ __global__ void __launch_bounds__(kThreads) k_check_exact(const __grid_constant_
     warp_check<MODE, T>(wsh[threadIdx.x >> 5], rb, ob, sg.q + c * D, active, nm, w,
                         (w.valid && active) ? sg.valid + c : nullptr, (w.dist && active) ? sg.dist + c : nullptr,
                         (w.profile && active) ? sg.profile + c * D : nullptr);
+}
+
+// Warp-per-configuration form (rpm_wide.cuh): G configurations per warp.
+template <int MODE>
+__global__ void __launch_bounds__(kWideThreads, MODE == 0 ? 1 : 2) k_check_wide(const __grid_constant__ KParams P) {
+    extern __shared__ __align__(128) unsigned char smem[];
+    __shared__ uint64_t bar;
+    __shared__ uint32_t wq[kWideWarps][64];
+    const int s = find_seg(P);
+    bulk_init(&bar);
+    wide_kernel_body<MODE>(P, smem, &bar, wq, s);
 }
 
 // FP64 recomputation of the configurations listed by the FP32 pass, one warp
@@ -297,6 +309,22 @@ cudaError_t launch_check_exact(int mode, const KParams &p, int64_t blocks, size_
         static bool attr = false;
         if (!attr) { cudaFuncSetAttribute(k_check_exact<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024); attr = true; }
         k_check_exact<1><<<(unsigned)blocks, kThreads, smem, st>>>(p);
+    }
+    return cudaGetLastError();
+}
+
+size_t wide_smem_bytes(int mode, int ns, int nb) { return WideLayout::of(mode, ns, nb).total; }
+
+cudaError_t launch_check_wide(int mode, const KParams &p, int64_t blocks, size_t smem, cudaStream_t st) {
+    if (mode == RPM_PREC_FP32_RECHECK) return launch_check_wide_fp32(p, blocks, smem, st);
+    if (mode == RPM_PREC_FP64) {
+        static bool attr = false;
+        if (!attr) { cudaFuncSetAttribute(k_check_wide<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024); attr = true; }
+        k_check_wide<0><<<(unsigned)blocks, kWideThreads, smem, st>>>(p);
+    } else {
+        static bool attr = false;
+        if (!attr) { cudaFuncSetAttribute(k_check_wide<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024); attr = true; }
+        k_check_wide<1><<<(unsigned)blocks, kWideThreads, smem, st>>>(p);
     }
     return cudaGetLastError();
 }

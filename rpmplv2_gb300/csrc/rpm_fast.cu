@@ -5,6 +5,7 @@
 #include "rpm_check.cuh"
 #include "rpm_edges.cuh"
 #include "rpm_launch.cuh"
+#include "rpm_wide.cuh"
 
 namespace rpm {
 
@@ -41,6 +42,25 @@ __global__ void __launch_bounds__(kThreads) k_check_fp32(const __grid_constant__
         const uint32_t slot = atomicAdd(P.recheck_count, 1u);
         P.recheck[slot] = ((uint64_t)s << 40) | (uint64_t)c;
     }
+}
+
+// FP32 pass of the warp-per-configuration form; unsettled configurations go
+// to the same recheck list as k_check_fp32's.
+__global__ void __launch_bounds__(kWideThreads, 2) k_check_wide_fp32(const __grid_constant__ KParams P) {
+    extern __shared__ __align__(128) unsigned char smem[];
+    __shared__ uint64_t bar;
+    __shared__ uint32_t wq[kWideWarps][64];
+    int s = 0;
+    while (s + 1 < P.nseg && P.segs[s + 1].first_block <= (int64_t)blockIdx.x) ++s;
+    bulk_init(&bar);
+    wide_kernel_body<2>(P, smem, &bar, wq, s);
+}
+
+cudaError_t launch_check_wide_fp32(const KParams &p, int64_t blocks, size_t smem, cudaStream_t st) {
+    static bool attr = false;
+    if (!attr) { cudaFuncSetAttribute(k_check_wide_fp32, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024); attr = true; }
+    k_check_wide_fp32<<<(unsigned)blocks, kWideThreads, smem, st>>>(p);
+    return cudaGetLastError();
 }
 
 // FP32 pass of the edge checks (unsettled checks go to k_edge_recheck).

@@ -14,7 +14,7 @@ constexpr int kMaxSegs = 32;      // segments per launch (passed by value)
 struct KParams {
     Seg segs[kMaxSegs];
     int32_t nseg;
-    int32_t pad;
+    int32_t wide_g;             // warp-per-configuration kernels: configurations per warp
     Num<double> nmd;
     Num<float> nmf;
     uint64_t *recheck;          // FP32 pass -> FP64 recheck list: (segment << 40) | config
@@ -32,6 +32,10 @@ size_t smem_bytes(int mode, int n_pad);
 cudaError_t launch_check_exact(int mode, const KParams &p, int64_t blocks, size_t smem, cudaStream_t st);
 cudaError_t launch_check_fp32(const KParams &p, int64_t blocks, size_t smem, cudaStream_t st);
 cudaError_t launch_recheck(const KParams &p, int grid, cudaStream_t st);
+// Warp-per-configuration form over the sorted scene copy (rpm_wide.cuh).
+size_t wide_smem_bytes(int mode, int ns, int nb);
+cudaError_t launch_check_wide(int mode, const KParams &p, int64_t blocks, size_t smem, cudaStream_t st);
+cudaError_t launch_check_wide_fp32(const KParams &p, int64_t blocks, size_t smem, cudaStream_t st);
 // FP32 FFMA throughput probe: kProbeChains independent FMA chains per thread.
 constexpr int kProbeChains = 8;
 cudaError_t launch_ffma_probe(float *out, int blocks, int threads, int iters, cudaStream_t st);

@@ -47,7 +47,7 @@ __global__ void k_obstacle_update(float *rows_f, double *rows_d, int n_pad, cons
 }
 
 // The next version of a scene: copy the current version device-to-device,
-// scatter the m updated AABBs, record 'ready'.  Checks issued afterwards wait
+// scatter the m updated AABBs, rebuild the sorted copy, record 'ready'.  Checks issued afterwards wait
 // on 'ready'; checks already issued keep reading the version they started on.
 // Caller holds ctx->mu.
 int scene_update(rpm_ctx *ctx, SceneRec *s, const int32_t *idx, const float *aabb, int32_t m) {
@@ -59,11 +59,10 @@ int scene_update(rpm_ctx *ctx, SceneRec *s, const int32_t *idx, const float *aab
     SceneBuf &b = s->bufs[nxt];
     wait_users(ctx, b);
     if (b.ready) CK(cudaEventSynchronize(b.ready));   // its staging may be reused now
-    const size_t bytes = (size_t)kFRows * s->n_pad * sizeof(float) + (size_t)kDRows * s->n_pad * sizeof(double);
+    const size_t bytes = scene_bytes(*s);
     if (!b.mem) {
         if (cudaMalloc(&b.mem, bytes) != cudaSuccess) return fail(RPM_ERR_NOMEM, "scene version allocation failed");
-        b.f = reinterpret_cast<float *>(b.mem);
-        b.d = reinterpret_cast<double *>(reinterpret_cast<char *>(b.mem) + (size_t)kFRows * s->n_pad * sizeof(float));
+        bind_scene_buf(*s, b);
     }
     if (!b.ready) CK(cudaEventCreateWithFlags(&b.ready, cudaEventDisableTiming));
     if (b.upd_cap < m) {
@@ -84,6 +83,7 @@ int scene_update(rpm_ctx *ctx, SceneRec *s, const int32_t *idx, const float *aab
         CK(cudaMemcpyAsync(b.upd_dev, b.upd_host, (size_t)m * 7 * sizeof(float), cudaMemcpyHostToDevice, ctx->upd_stream));
         k_obstacle_update<<<(m + 127) / 128, 128, 0, ctx->upd_stream>>>(b.f, b.d, s->n_pad, b.upd_dev, m);
         CK(cudaGetLastError());
+        CK(launch_scene_sort(*s, b, ctx->upd_stream));   // same order, new contents and block bounds
     }
     CK(cudaEventRecord(b.ready, ctx->upd_stream));
     b.pending = true;

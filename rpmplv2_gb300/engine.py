@@ -9,7 +9,7 @@ import os
 import numpy as np
 
 from . import _abi
-from ._abi import BatchItem, CheckStats, Params, PRECISIONS
+from ._abi import BatchItem, CheckStats, LAYOUTS, Params, PRECISIONS
 
 _LIB = None
 
@@ -56,6 +56,7 @@ def load(build_if_missing=False):
     L.rpm_check_batch.argtypes = [_vp, _i32, _vp, _i32, _vp]
     L.rpm_check_edges.argtypes = [_vp, _i32, _i32, _vp, _vp, _i64, ctypes.c_float, _i32, _vp, _vp, _vp]
     L.rpm_ctx_set_graphs.argtypes = [_vp, ctypes.c_int]
+    L.rpm_ctx_set_layout.argtypes = [_vp, ctypes.c_int32]
     L.rpm_autotune_edges.argtypes = [_vp, _i32, _i32, _vp, _vp, _i64, ctypes.c_float, _i32, _vp, _pi32]
     L.rpm_set_edge_ctas.argtypes = [_vp, _i32, _i32, _i32]
     L.rpm_check_configs_host.argtypes = [_vp, _i32, _i32, _vp, _i64, _vp, _vp, _vp]
@@ -163,6 +164,13 @@ class Engine:
     def set_graphs(self, enable=True):
         _check(self.lib.rpm_ctx_set_graphs(self.ctx, 1 if enable else 0))
 
+    def set_layout(self, layout="auto"):
+        """Spread configuration checks one lane ('lane') or one warp ('warp')
+        per configuration, or choose per segment ('auto').  Outputs do not
+        depend on it."""
+        code = LAYOUTS[layout] if isinstance(layout, str) else int(layout)
+        _check(self.lib.rpm_ctx_set_layout(self.ctx, code))
+
     def autotune_edges(self, scene_id, q1, q2, valid, step=0.0, num_checks=10, precision="fp32_recheck"):
         prec = PRECISIONS[precision] if isinstance(precision, str) else int(precision)
         out = _i32()
@@ -227,7 +235,7 @@ ABI_SYMBOLS = [
     "rpm_robot_upload", "rpm_scene_create", "rpm_scene_update", "rpm_scene_destroy", "rpm_scene_info",
     "rpm_box_aabb", "rpm_check_configs", "rpm_check_configs_host", "rpm_skeleton", "rpm_last_stats", "rpm_sync",
     "rpm_ctx_set_timing", "rpm_last_timing", "rpm_probe_fp32_peak", "rpm_check_configs_noalloc", "rpm_check_batch",
-    "rpm_check_edges", "rpm_ctx_set_graphs", "rpm_autotune_edges", "rpm_set_edge_ctas",
+    "rpm_check_edges", "rpm_ctx_set_graphs", "rpm_autotune_edges", "rpm_set_edge_ctas", "rpm_ctx_set_layout",
     "rpm_server_create", "rpm_server_submit", "rpm_server_poll", "rpm_server_wait", "rpm_server_release",
     "rpm_server_replay", "rpm_server_stats", "rpm_server_destroy",
 ]
