@@ -58,50 +58,53 @@ void wait_users(rpm_ctx *ctx, SceneBuf &b) {
     b.users.clear();
 }
 
-// Spread the low 10 bits of v to every third bit (Morton interleave).
-static uint32_t spread10(uint32_t v) {
-    v &= 1023u;
-    v = (v | (v << 16)) & 0x030000FFu;
-    v = (v | (v << 8)) & 0x0300F00Fu;
-    v = (v | (v << 4)) & 0x030C30C3u;
-    v = (v | (v << 2)) & 0x09249249u;
-    return v;
+// Top-down median split of the obstacles in 'idx' (by centre, along the
+// longest axis of their centres), left parts a multiple of kLeaf, appended to
+// 'out' in depth-first order: every run of kLeaf consecutive entries is a
+// compact leaf, and consecutive leaves are spatial neighbours.
+static void kd_order(const SceneRec &s, std::vector<int> idx, std::vector<int> &out) {
+    if ((int)idx.size() <= kLeaf) {
+        out.insert(out.end(), idx.begin(), idx.end());
+        return;
+    }
+    auto centre = [&](int j, int k) {
+        const float c = 0.5f * (s.aabb[6 * (size_t)j + k] + s.aabb[6 * (size_t)j + 3 + k]);
+        return std::isfinite(c) ? c : 0.f;
+    };
+    float lo[3], hi[3];
+    for (int k = 0; k < 3; ++k) lo[k] = hi[k] = centre(idx[0], k);
+    for (int j : idx)
+        for (int k = 0; k < 3; ++k) {
+            lo[k] = std::min(lo[k], centre(j, k));
+            hi[k] = std::max(hi[k], centre(j, k));
+        }
+    int ax = 0;
+    for (int k = 1; k < 3; ++k)
+        if (hi[k] - lo[k] > hi[ax] - lo[ax]) ax = k;
+    std::stable_sort(idx.begin(), idx.end(), [&](int a, int b) { return centre(a, ax) < centre(b, ax); });
+    const int n = (int)idx.size();
+    int h = std::max(kLeaf, (int)std::lround((double)n / 2 / kLeaf) * kLeaf);
+    h = std::min(h, n - 1);
+    kd_order(s, std::vector<int>(idx.begin(), idx.begin() + h), out);
+    kd_order(s, std::vector<int>(idx.begin() + h, idx.end()), out);
 }
 
 void sorted_layout(SceneRec &s) {
-    std::vector<int> ground, other;
-    for (int j = 0; j < s.n; ++j) ((s.flags[j] & RPM_OBS_GROUND) ? ground : other).push_back(j);
-    const float big = std::numeric_limits<float>::infinity();
-    float lo[3] = {big, big, big}, hi[3] = {-big, -big, -big};
-    auto centre = [&](int j, int k) { return 0.5f * (s.aabb[6 * (size_t)j + k] + s.aabb[6 * (size_t)j + 3 + k]); };
-    for (int j : other)
-        for (int k = 0; k < 3; ++k) {
-            const float c = centre(j, k);
-            if (!std::isfinite(c)) continue;   // NaN and infinite centres do not shape the frame
-            lo[k] = std::min(lo[k], c);
-            hi[k] = std::max(hi[k], c);
-        }
-    std::vector<std::pair<uint32_t, int>> key;
-    key.reserve(other.size());
-    for (int j : other) {
-        uint32_t code = 0;
-        for (int k = 0; k < 3; ++k) {
-            const float c = centre(j, k);
-            const float span = hi[k] - lo[k];
-            float t = (span > 0.f && span < big && c == c) ? (c - lo[k]) / span : 0.f;
-            t = t < 0.f ? 0.f : (t > 1.f ? 1.f : t);
-            code |= spread10((uint32_t)(t * 1023.f)) << k;
-        }
-        key.push_back({code, j});
+    // static, moving and ground obstacles in separate leaves, so moving ones
+    // never widen a static leaf and ground leaves can be skipped whole
+    std::vector<int> group[3];
+    for (int j = 0; j < s.n; ++j)
+        group[(s.flags[j] & RPM_OBS_GROUND) ? 2 : ((s.flags[j] & RPM_OBS_DYNAMIC) ? 1 : 0)].push_back(j);
+    s.perm.clear();
+    for (int g = 0; g < 3; ++g) {
+        std::vector<int> ord;
+        if (!group[g].empty()) kd_order(s, group[g], ord);
+        for (int j : ord) s.perm.push_back(j);
+        while (s.perm.size() % kLeaf) s.perm.push_back(-1);
     }
-    std::sort(key.begin(), key.end());
-    const int m = (int)other.size(), g = (int)ground.size();
-    const int mr = (m + 31) / 32 * 32, gr = (g + 31) / 32 * 32;
-    s.ns = std::max(32, mr + gr);
-    s.nb = s.ns / 32;
-    s.perm.assign(s.ns, -1);
-    for (int k = 0; k < m; ++k) s.perm[k] = key[k].second;
-    for (int k = 0; k < g; ++k) s.perm[mr + k] = ground[k];
+    if (s.perm.empty()) s.perm.assign(kLeaf, -1);
+    s.ns = (int)s.perm.size();
+    s.nb = s.ns / kLeaf;
 }
 
 size_t scene_bytes(const SceneRec &s) {
@@ -126,14 +129,15 @@ void bind_scene_buf(const SceneRec &s, SceneBuf &b) {
     b.perm = reinterpret_cast<int32_t *>(p);
 }
 
-// Gather the sorted copy of a version from its rows and bound each block of
-// 32 slots (one warp per block).  Padding slots get bounds +inf / -inf so no
-// gap test passes them; a block holding a NaN coordinate gets infinite bounds
-// so it is never skipped.
+// Gather the sorted copy of a version from its rows and bound each leaf of
+// kLeaf slots (four leaves per warp).  Padding slots get bounds +inf / -inf so
+// no gap test passes them; a leaf holding a NaN coordinate gets infinite
+// bounds so it is never skipped.
 __global__ void k_scene_sort(const float *f, const double *d, int n_pad, const int32_t *perm, int ns, float *sf,
                              double *sd, float *blk) {
     const int s = blockIdx.x * 32 + threadIdx.x;
-    const int j = perm[s];
+    const bool in = s < ns;
+    const int j = in ? perm[s] : -1;
     const float inf = __int_as_float(0x7f800000);
     float lo[3], hi[3], tmax = -inf, tmin = inf;
     bool nan = false;
@@ -156,39 +160,45 @@ __global__ void k_scene_sort(const float *f, const double *d, int n_pad, const i
         for (int c = 0; c < 3; ++c) {
             lo[c] = inf;
             hi[c] = -inf;
-            sf[c * ns + s] = inf;
-            sf[(3 + c) * ns + s] = -inf;
-            sd[c * ns + s] = (double)inf;
-            sd[(3 + c) * ns + s] = -(double)inf;
+            if (in) {
+                sf[c * ns + s] = inf;
+                sf[(3 + c) * ns + s] = -inf;
+                sd[c * ns + s] = (double)inf;
+                sd[(3 + c) * ns + s] = -(double)inf;
+            }
         }
-        sf[kRowTol * ns + s] = 0.f;
-        sd[kRowTol * ns + s] = 0.0;
+        if (in) {
+            sf[kRowTol * ns + s] = 0.f;
+            sd[kRowTol * ns + s] = 0.0;
+        }
     }
-    sf[7 * ns + s] = __uint_as_float(id);
+    if (in) sf[7 * ns + s] = __uint_as_float(id);
     const unsigned full = 0xffffffffu;
-    nan = __any_sync(full, nan);
+    // reductions within each group of kLeaf lanes
 #pragma unroll
-    for (int off = 16; off > 0; off >>= 1) {
+    for (int off = kLeaf / 2; off > 0; off >>= 1) {
         for (int c = 0; c < 3; ++c) {
             lo[c] = fminf(lo[c], __shfl_xor_sync(full, lo[c], off));
             hi[c] = fmaxf(hi[c], __shfl_xor_sync(full, hi[c], off));
         }
         tmax = fmaxf(tmax, __shfl_xor_sync(full, tmax, off));
         tmin = fminf(tmin, __shfl_xor_sync(full, tmin, off));
+        nan = nan || __shfl_xor_sync(full, (int)nan, off);
     }
-    if (threadIdx.x == 0) {
-        float *r = blk + (size_t)blockIdx.x * kBlkRec;
+    const int leaf = s / kLeaf;
+    if ((threadIdx.x % kLeaf) == 0 && in) {
+        float *r = blk + (size_t)leaf * kBlkRec;
         for (int c = 0; c < 3; ++c) {
             r[c] = nan ? -inf : lo[c];
             r[3 + c] = nan ? inf : hi[c];
         }
-        r[6] = (tmax == -inf) ? 0.f : tmax;   // an all-padding block
+        r[6] = (tmax == -inf) ? 0.f : tmax;   // an all-padding leaf
         r[7] = (tmin == inf) ? 0.f : tmin;
     }
 }
 
 cudaError_t launch_scene_sort(const SceneRec &s, const SceneBuf &b, cudaStream_t st) {
-    k_scene_sort<<<s.nb, 32, 0, st>>>(b.f, b.d, s.n_pad, b.perm, s.ns, b.sf, b.sd, b.blk);
+    k_scene_sort<<<(s.ns + 31) / 32, 32, 0, st>>>(b.f, b.d, s.n_pad, b.perm, s.ns, b.sf, b.sd, b.blk);
     return cudaGetLastError();
 }
 
@@ -216,6 +226,15 @@ int upload_scene(rpm_ctx *ctx, SceneRec &s, SceneBuf &b) {
     return RPM_OK;
 }
 
+void free_scratch(Scratch *sc) {
+    for (auto &g : sc->graphs) cudaGraphExecDestroy(g.exec);
+    cudaFree(sc->n_e); cudaFree(sc->local); cudaFree(sc->kmax); cudaFree(sc->bprefix); cudaFree(sc->full);
+    cudaFree(sc->work); cudaFree(sc->erecheck); cudaFree(sc->recheck); cudaFree(sc->counters); cudaFree(sc->status);
+    cudaFree(sc->pairs); cudaFree(sc->pcfgs); cudaFree(sc->slot_of); cudaFree(sc->pskel); cudaFree(sc->pacc);
+    for (int i = 0; i < 3; ++i) if (sc->ev[i]) cudaEventDestroy(sc->ev[i]);
+    delete sc;
+}
+
 int get_scratch(rpm_ctx *ctx, cudaStream_t st, int64_t need, Scratch **out) {
     Scratch *s = ctx->scratch[st];
     if (!s) {
@@ -230,12 +249,24 @@ int get_scratch(rpm_ctx *ctx, cudaStream_t st, int64_t need, Scratch **out) {
         if (s->recheck) {
             CK(cudaStreamSynchronize(st));
             cudaFree(s->recheck);
+            cudaFree(s->pairs); cudaFree(s->pcfgs); cudaFree(s->slot_of); cudaFree(s->pskel); cudaFree(s->pacc);
             s->recheck = nullptr;
         }
-        size_t cap = std::max<size_t>((size_t)need, 1u << 16);
-        if (cudaMalloc(&s->recheck, cap * sizeof(uint64_t)) != cudaSuccess)
+        const size_t cap = std::max<size_t>((size_t)need, 1u << 16);
+        // records for 1/8 of the configurations (at least 4096, at most 65536),
+        // 16 listed pairs per record; what does not fit is rechecked whole
+        const size_t pcfg = std::min<size_t>(cap, std::max<size_t>(4096, std::min<size_t>(cap / 8, 1u << 16)));
+        const size_t ppair = 16 * pcfg;
+        if (cudaMalloc(&s->recheck, cap * sizeof(uint64_t)) != cudaSuccess ||
+            cudaMalloc(&s->slot_of, cap * sizeof(uint32_t)) != cudaSuccess ||
+            cudaMalloc(&s->pairs, ppair * sizeof(uint64_t)) != cudaSuccess ||
+            cudaMalloc(&s->pcfgs, pcfg * sizeof(PairCfg)) != cudaSuccess ||
+            cudaMalloc(&s->pskel, pcfg * (kMaxDof + 1) * 3 * sizeof(double)) != cudaSuccess ||
+            cudaMalloc(&s->pacc, pcfg * sizeof(PairAcc)) != cudaSuccess)
             return fail(RPM_ERR_NOMEM, "recheck list allocation failed");
         s->cap = cap;
+        s->pcfg_cap = pcfg;
+        s->ppair_cap = ppair;
     }
     *out = s;
     return RPM_OK;
@@ -295,16 +326,19 @@ SceneRec *find_scene(rpm_ctx *ctx, int id) {
 
 // Layout of one segment.  Lane-per-configuration walks a scene's obstacles in
 // series per lane, which suits small scenes and large batches; warp-per-
-// configuration culls whole blocks of the sorted copy and spreads the
+// configuration culls whole leaves of the sorted copy and spreads the
 // survivors over a warp, which suits large scenes and batches too small to
-// fill the GPU with lanes.
+// fill the GPU with lanes.  Per-link distance profiles of large batches stay
+// lane-per-configuration: every link needs its own nearest-first search
+// there, which keeps the warp's drains half empty.  (Thresholds measured on
+// GB300 over 10-22 links, 10-1000 obstacles and 256-65,536 configurations.)
 static bool use_warp_layout(const rpm_ctx *ctx, const SegReq &r, int64_t total) {
     if (ctx->layout == RPM_LAYOUT_LANE) return false;
     if (ctx->layout == RPM_LAYOUT_WARP) return true;
-    const int L = ctx->robots[r.scene->robot].desc.num_dofs;
-    const int64_t lane_warps = (total + 31) / 32;
-    if (r.scene->n >= kWideMinObstacles) return true;
-    return lane_warps < (int64_t)ctx->num_sms * 4 && (int64_t)r.scene->n * L >= kWideMinPairs;
+    const int n = r.scene->n;
+    if (n >= kWideMinObstacles) return !(r.profile != nullptr && total > kWideMaxProfileBatch);
+    if (n >= kWideMidObstacles) return total <= kWideMidBatch;
+    return n >= kWideSmallObstacles && total <= kWideSmallBatch;
 }
 
 // Queue checks of up to kMaxSegs segments as one launch on 'st' (more
@@ -317,7 +351,7 @@ int enqueue_segments(rpm_ctx *ctx, int prec, const std::vector<SegReq> &reqs, cu
     int rc = get_scratch(ctx, st, prec == RPM_PREC_FP32_RECHECK ? total : 0, &sc);
     if (rc) return rc;
     sc->last_configs = total;
-    CK(cudaMemsetAsync(sc->counters, 0, sizeof(uint32_t), st));
+    CK(cudaMemsetAsync(sc->counters, 0, 4 * sizeof(uint32_t), st));
     sc->timed = ctx->timing && total > 0;
     sc->had_recheck = prec == RPM_PREC_FP32_RECHECK;
     if (sc->timed && !sc->ev[0])
@@ -353,7 +387,7 @@ int enqueue_segments(rpm_ctx *ctx, int prec, const std::vector<SegReq> &reqs, cu
         const int64_t want = (chunk_total + (int64_t)ctx->num_sms * 32 - 1) / ((int64_t)ctx->num_sms * 32);
         p.wide_g = (int32_t)std::max<int64_t>(1, std::min<int64_t>(gmax, want));
         const int64_t per_cta = wide ? (int64_t)kWideWarps * p.wide_g : kThreads;
-        int64_t blocks = 0;
+        int64_t blocks = 0, flat = 0;
         size_t smem = 0;
         for (const SegReq *rp : segs) {
             const SegReq &r = *rp;
@@ -373,6 +407,8 @@ int enqueue_segments(rpm_ctx *ctx, int prec, const std::vector<SegReq> &reqs, cu
             g.profile = r.profile;
             g.count = r.count;
             g.first_block = blocks;
+            g.flat0 = flat;
+            flat += r.count;
             g.n = r.scene->n;
             g.n_pad = r.scene->n_pad;
             g.srt_f = buf.sf;
@@ -391,12 +427,24 @@ int enqueue_segments(rpm_ctx *ctx, int prec, const std::vector<SegReq> &reqs, cu
         p.recheck = sc->recheck;
         p.recheck_count = sc->counters;
         p.status = sc->status;
-        if (ci > 0) CK(cudaMemsetAsync(sc->counters, 0, sizeof(uint32_t), st));   // the recheck list is per launch
+        p.ps.pairs = sc->pairs;
+        p.ps.pair_count = sc->counters + 3;
+        p.ps.pair_cap = (uint32_t)sc->ppair_cap;
+        p.ps.cfg_cap = (uint32_t)sc->pcfg_cap;
+        p.ps.cfgs = sc->pcfgs;
+        p.ps.cfg_count = sc->counters + 2;
+        p.ps.slot_of = sc->slot_of;
+        p.ps.skel = sc->pskel;
+        p.ps.acc = sc->pacc;
+        if (ci > 0) CK(cudaMemsetAsync(sc->counters, 0, 4 * sizeof(uint32_t), st));   // the recheck lists are per launch
         if (wide) CK(launch_check_wide(prec, p, blocks, smem, st));
         else if (prec == RPM_PREC_FP32_RECHECK) CK(launch_check_fp32(p, blocks, smem, st));
         else CK(launch_check_exact(prec, p, blocks, smem, st));
         if (sc->timed && last) CK(cudaEventRecord(sc->ev[1], st));
-        if (prec == RPM_PREC_FP32_RECHECK) CK(launch_recheck(p, ctx->num_sms * 4, st));
+        if (prec == RPM_PREC_FP32_RECHECK) {
+            CK(launch_pair_recheck(p, ctx->num_sms * 2, st));
+            CK(launch_recheck(p, ctx->num_sms * 4, st));
+        }
     }
     if (sc->timed) {
         if (chunks.empty()) CK(cudaEventRecord(sc->ev[1], st));
@@ -455,7 +503,7 @@ int enqueue_edges(rpm_ctx *ctx, Scratch *sc, SceneRec *s, int prec, const float 
     p.valid = valid; p.checks_out = checks; p.status = sc->status;
     p.nmd.eq = ctx->params.equality_threshold; p.nmd.maxd = ctx->params.max_distance;
     p.nmf.eq = (float)ctx->params.equality_threshold; p.nmf.maxd = (float)ctx->params.max_distance;
-    CK(cudaMemsetAsync(sc->counters, 0, 2 * sizeof(uint32_t), st));
+    CK(cudaMemsetAsync(sc->counters, 0, 4 * sizeof(uint32_t), st));
     if (E == 0) return RPM_OK;
     CK(launch_edge_prep(p, st));
     const int grid = ctx->num_sms * std::max(1, ctas_per_sm);
@@ -506,14 +554,7 @@ int rpm_ctx_destroy(rpm_ctx *ctx) {
     }
     for (auto &r : ctx->robots) cudaFree(r.dev);
     for (auto &kv : ctx->scratch) {
-        for (auto &g : kv.second->graphs) cudaGraphExecDestroy(g.exec);
-        cudaFree(kv.second->n_e); cudaFree(kv.second->local); cudaFree(kv.second->kmax);
-        cudaFree(kv.second->bprefix); cudaFree(kv.second->full); cudaFree(kv.second->work);
-        cudaFree(kv.second->erecheck);
-        cudaFree(kv.second->recheck);
-        cudaFree(kv.second->counters);
-        cudaFree(kv.second->status);
-        delete kv.second;
+        free_scratch(kv.second);
     }
     for (int i = 0; i < 2; ++i) {
         if (ctx->hs[i]) cudaStreamDestroy(ctx->hs[i]);
@@ -872,12 +913,13 @@ int rpm_last_stats(rpm_ctx *ctx, void *stream, rpm_check_stats *out) {
     auto it = ctx->scratch.find(st);
     if (it == ctx->scratch.end()) return RPM_OK;
     CK(cudaStreamSynchronize(st));
-    uint32_t cnt[2] = {0, 0};
+    uint32_t cnt[4] = {0, 0, 0, 0};
     int32_t status = 0;
     CK(cudaMemcpy(cnt, it->second->counters, sizeof cnt, cudaMemcpyDeviceToHost));
     CK(cudaMemcpy(&status, it->second->status, sizeof status, cudaMemcpyDeviceToHost));
     out->configs = it->second->last_configs;
-    out->rechecked = cnt[0];
+    // configurations that used FP64: whole, or through their listed pairs
+    out->rechecked = (int64_t)cnt[0] + std::min<int64_t>(cnt[2], (int64_t)it->second->pcfg_cap);
     out->overflow = cnt[1];
     out->device_status = status;
     return RPM_OK;

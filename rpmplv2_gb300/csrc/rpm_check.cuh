@@ -43,6 +43,75 @@ struct Want {
     bool valid, dist, profile;
 };
 
+// ---------------------------------------------------------------------------
+// Pair-level FP64 recheck of the FP32 pass.  The FP32 pass folds only settled
+// pairs into its outputs and running minima (a settled value is within the
+// contact band of its FP64 value, so pruning on settled values stays exact)
+// and lists every unsettled (configuration, link, obstacle, kind) pair.  A
+// configuration whose outputs depend on a listed pair gets a record; the FP64
+// kernels then run the forward kinematics of each recorded configuration,
+// evaluate its listed pairs and fold their results into the outputs in the
+// reference's link order.  Configurations whose pairs do not fit the lists
+// are recomputed whole by the configuration-level recheck.
+constexpr int kSettled = 0;      // outputs final
+constexpr int kPairs = 1;        // outputs final after the pair recheck
+constexpr int kFull = 2;         // recompute the whole configuration in FP64
+
+struct PairCfg {
+    uint32_t flat;               // configuration index within the launch
+    int32_t seg;
+    int64_t config;              // index within its segment
+    int32_t hit_link;            // link of the first settled hit (-1: none)
+    int32_t hit_j;               // lowest obstacle index of a settled hit in that link
+};
+
+struct PairAcc {
+    int lkey[kMaxDof];                    // ordered key of (float) FP64 link minimum
+    unsigned long long hkey[kMaxDof];     // obstacle index << 32 | float bits, lowest-index FP64 hit per link
+    long long dkey;                       // ordered key of the FP64 minimum over all links
+    int coll;                             // an FP64 collision
+    int pad;
+};
+
+struct PairSink {
+    uint64_t *pairs;             // flat << 17 | link << 12 | obstacle << 1 | kind (0 isValid, 1 distance)
+    uint32_t *pair_count;
+    uint32_t pair_cap;
+    uint32_t cfg_cap;
+    PairCfg *cfgs;
+    uint32_t *cfg_count;
+    uint32_t *slot_of;           // [configurations of the launch] -> record
+    double *skel;                // [cfg_cap][kMaxDof + 1][3]
+    PairAcc *acc;                // [cfg_cap]
+};
+
+#ifdef __CUDACC__
+// Append an unsettled pair; false when the list is full.
+__device__ __forceinline__ bool push_pair(const PairSink *ps, uint32_t flat, int link, int j, int kind) {
+    const uint32_t s = atomicAdd(ps->pair_count, 1u);
+    if (s >= ps->pair_cap) return false;
+    ps->pairs[s] = ((uint64_t)flat << 17) | ((uint64_t)link << 12) | ((uint64_t)j << 1) | (uint64_t)kind;
+    return true;
+}
+
+// Route a configuration the FP32 pass did not settle: a pair-recheck record,
+// or (no sink, list overflow) the whole-configuration recheck list.
+__device__ __forceinline__ void finish_config(const PairSink *ps, int status, uint32_t flat, int seg, int64_t c,
+                                              int hit_link, int hit_j, uint64_t *recheck, uint32_t *recheck_count) {
+    if (status == kSettled) return;
+    if (status == kPairs && ps) {
+        const uint32_t slot = atomicAdd(ps->cfg_count, 1u);
+        if (slot < ps->cfg_cap) {
+            ps->cfgs[slot] = PairCfg{flat, seg, c, hit_link, hit_j};
+            ps->slot_of[flat] = slot;
+            return;
+        }
+    }
+    const uint32_t r = atomicAdd(recheck_count, 1u);
+    recheck[r] = ((uint64_t)seg << 40) | (uint64_t)c;
+}
+#endif
+
 #if defined(RPM_MARGIN_DEBUG)
 inline int g_dbg_site_b = 0, g_dbg_site_d = 0;   // host debugging only
 #endif
@@ -192,9 +261,11 @@ template <int MODE, typename T> struct BoolMargin;
 template <int MODE> struct BoolMargin<MODE, double> { __device__ static double m() { return 1e-9; } };
 template <int MODE> struct BoolMargin<MODE, float> { __device__ static float m() { return MODE == 2 ? kDecide : 1e-5f; } };
 
+// flags bits: 1 settled collision, 2 unsettled isValid pair, 4 unsettled
+// distance pair (bits 1-4 per link), 8 pair list full (per configuration).
 template <int MODE, typename T>
 __device__ __forceinline__ void drain_bool(WarpShared<T> &sh, const DevRobot &rb, const ObsView<T> &ob, const Num<T> &nm,
-                                           int i, int nitems) {
+                                           int i, int nitems, const PairSink *ps, uint32_t flat_base) {
     typedef typename PolOf<MODE>::type P;
     const int lane = threadIdx.x & 31;
     if (lane < nitems) {
@@ -204,8 +275,12 @@ __device__ __forceinline__ void drain_bool(WarpShared<T> &sh, const DevRobot &rb
         ob.box(j, o);
         P pol;
         const bool c = coll_box(pol, nm, sh.a[owner], sh.b[owner], LinkConst<T>::r(rb, i), LinkConst<T>::rn(rb, i), o);
-        if (P::robust && pol.m < kDecide) atomicOr(&sh.flags[owner], 2);
-        else if (c) atomicOr(&sh.flags[owner], 1);
+        if (P::robust && pol.m < kDecide) {
+            atomicOr(&sh.flags[owner], 2);
+            if (ps && !push_pair(ps, flat_base + (uint32_t)owner, i, j, 0)) atomicOr(&sh.flags[owner], 8);
+        } else if (c) {
+            atomicOr(&sh.flags[owner], 1);
+        }
     }
 }
 
@@ -231,17 +306,19 @@ __device__ __forceinline__ T pair_distance(const DevRobot &rb, const V &ob, cons
 
 template <int MODE, typename T>
 __device__ __forceinline__ void drain_dist(WarpShared<T> &sh, const DevRobot &rb, const ObsView<T> &ob, const Num<T> &nm,
-                                           int i, int nitems) {
+                                           int i, int nitems, const PairSink *ps, uint32_t flat_base) {
     const int lane = threadIdx.x & 31;
     if (lane < nitems) {
         const uint32_t e = sh.qd[lane];
         const int owner = (int)(e & 31u), j = (int)(e >> 5);
         bool settled;
         const T d = pair_distance<MODE, T>(rb, ob, nm, sh.a[owner], sh.b[owner], i, j, settled);
-        if (!settled) atomicOr(&sh.flags[owner], 4);
-        if (d == d) {   // the reference's std::min ignores NaN
+        if (!settled) {
+            atomicOr(&sh.flags[owner], 4);
+            if (ps && !push_pair(ps, flat_base + (uint32_t)owner, i, j, 1)) atomicOr(&sh.flags[owner], 8);
+        } else if (d == d) {   // the reference's std::min ignores NaN
             atomicMin(&sh.lmin[owner], Key<T>::of(d));
-            if (d <= T(0) && settled) atomicMin(&sh.hitj[owner], j);
+            if (d <= T(0)) atomicMin(&sh.hitj[owner], j);
         }
         __syncwarp(__activemask());
         if (d <= T(0) && settled && sh.hitj[owner] == j) sh.hitv[owner] = d;   // one entry per (owner, j)
@@ -272,7 +349,7 @@ template <typename T> __device__ __forceinline__ T gap2_bb(const T *lo, const T 
         (N) += __popc(m_);                                                             \
         __syncwarp();                                                                  \
         if ((N) >= 32) {                                                               \
-            DRAIN<MODE, T>(sh, rb, ob, nm, i, 32);                                     \
+            DRAIN<MODE, T>(sh, rb, ob, nm, i, 32, ps, flat_base);                      \
             __syncwarp();                                                              \
             if (lane < (N) - 32) sh.Q[lane] = sh.Q[32 + lane];                         \
             (N) -= 32;                                                                 \
@@ -280,13 +357,17 @@ template <typename T> __device__ __forceinline__ T gap2_bb(const T *lo, const T 
         }                                                                              \
     } while (0)
 
-// Returns, per lane, whether the configuration is settled (always true for
-// the exact forms).  Outputs of unsettled configurations are provisional.
-// Once a lane has a settled hit it only looks for an earlier hit (lower
-// obstacle index), which is all the profile's first-hit semantics need.
+// Returns, per lane, kSettled, kPairs or kFull (always kSettled for the exact
+// forms); outputs of unsettled configurations are provisional.  With a pair
+// sink, lane k's configuration is number flat_base + k of the launch, and its
+// first settled hit (link, obstacle) goes to *hit_link / *hit_j.  Once a lane
+// has a settled hit it only looks for an earlier hit (lower obstacle index),
+// which is all the profile's first-hit semantics need.
 template <int MODE, typename T>
-__device__ bool warp_check(WarpShared<T> &sh, const DevRobot &rb, const ObsView<T> &ob, const float *q, bool active,
-                           const Num<T> &nm, Want w, uint8_t *valid_out, double *dist_out, float *prof_out) {
+__device__ int warp_check(WarpShared<T> &sh, const DevRobot &rb, const ObsView<T> &ob, const float *q, bool active,
+                          const Num<T> &nm, Want w, uint8_t *valid_out, double *dist_out, float *prof_out,
+                          const PairSink *ps = nullptr, uint32_t flat_base = 0, int *hit_link = nullptr,
+                          int *hit_j = nullptr) {
     const unsigned full = 0xffffffffu;
     const int lane = threadIdx.x & 31;
     const unsigned lt_mask = (1u << lane) - 1u;
@@ -297,7 +378,7 @@ __device__ bool warp_check(WarpShared<T> &sh, const DevRobot &rb, const ObsView<
     bool need_b = active && w.valid, need_d = active && (w.dist || w.profile);
     bool collided = false, unc_b = false, unc_d = false;
     T best = nm.maxd;
-    int hit = -1;
+    int hit = -1, hit_obs = 0x7fffffff;
     const int L = rb.D;
     const T dmargin = (MODE == 2) ? T(kBand) : LinkConst<T>::margin();
     sh.flags[lane] = 0;
@@ -349,8 +430,8 @@ __device__ bool warp_check(WarpShared<T> &sh, const DevRobot &rb, const ObsView<
             RPM_PUSH_AND_DRAIN(qb, nb, qb, item, drain_bool);
             RPM_PUSH_AND_DRAIN(qd, nd, qd, item, drain_dist);
         }
-        if (nb > 0) drain_bool<MODE, T>(sh, rb, ob, nm, i, nb);
-        if (nd > 0) drain_dist<MODE, T>(sh, rb, ob, nm, i, nd);
+        if (nb > 0) drain_bool<MODE, T>(sh, rb, ob, nm, i, nb, ps, flat_base);
+        if (nd > 0) drain_dist<MODE, T>(sh, rb, ob, nm, i, nd, ps, flat_base);
         __syncwarp();
         // ---- fold this link's results into the lane's configuration
         const int fl = sh.flags[lane];
@@ -365,6 +446,7 @@ __device__ bool warp_check(WarpShared<T> &sh, const DevRobot &rb, const ObsView<
             if (hj != 0x7fffffff) {
                 // the partial minimum at the first hit is the hit's own value
                 hit = i;
+                hit_obs = hj;
                 need_d = false;
                 if (w.profile) prof_out[i] = (float)sh.hitv[lane];
             } else {
@@ -376,14 +458,17 @@ __device__ bool warp_check(WarpShared<T> &sh, const DevRobot &rb, const ObsView<
         __syncwarp();
         A[0] = B[0]; A[1] = B[1]; A[2] = B[2];
     }
-    if (!active) return true;
+    if (!active) return kSettled;
     if (w.profile && hit >= 0)
         for (int k = hit + 1; k < L; ++k) prof_out[k] = 0.f;
     if (w.valid) *valid_out = collided ? 0 : 1;
     if (w.dist) *dist_out = (hit >= 0) ? 0.0 : (double)best;
+    if (hit_link) *hit_link = hit;
+    if (hit_j) *hit_j = hit_obs;
     const bool bad_b = w.valid && !collided && unc_b;
     const bool bad_d = (w.dist || w.profile) && unc_d && (w.profile || hit < 0);
-    return !(bad_b || bad_d);
+    if (!(bad_b || bad_d)) return kSettled;
+    return (ps && !(sh.flags[lane] & 8)) ? kPairs : kFull;
 }
 #endif
 

@@ -79,7 +79,16 @@ struct SceneRec {
 struct Scratch {
     uint64_t *recheck = nullptr;
     size_t cap = 0;
-    uint32_t *counters = nullptr;   // [0] recheck count, [1] overflow
+    // pair-level recheck lists (see PairSink)
+    size_t pcfg_cap = 0, ppair_cap = 0;
+    uint64_t *pairs = nullptr;
+    PairCfg *pcfgs = nullptr;
+    uint32_t *slot_of = nullptr;
+    double *pskel = nullptr;
+    PairAcc *pacc = nullptr;
+    // [0] whole-configuration recheck count, [1] edge recheck overflow,
+    // [2] pair-recheck records, [3] listed pairs
+    uint32_t *counters = nullptr;
     int32_t *status = nullptr;
     int64_t last_configs = 0;
     cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};   // bulk start, bulk end / recheck start, recheck end
@@ -142,6 +151,7 @@ cudaEvent_t get_event(rpm_ctx *ctx);
 void prune_users(rpm_ctx *ctx, SceneBuf &b);
 void wait_users(rpm_ctx *ctx, SceneBuf &b);
 int get_scratch(rpm_ctx *ctx, cudaStream_t st, int64_t need, Scratch **out);
+void free_scratch(Scratch *sc);   // stream work using it must be complete
 SceneRec *find_scene(rpm_ctx *ctx, int id);
 int enqueue_segments(rpm_ctx *ctx, int prec, const std::vector<SegReq> &reqs, cudaStream_t st);
 int edge_scratch(rpm_ctx *ctx, Scratch *sc, int64_t E, cudaStream_t st);

@@ -119,7 +119,7 @@ __device__ void edge_warps(const EdgeParams &P, const DevRobot &rb, const ObsVie
         __syncwarp();
         const Want w{true, false, false};
         uint8_t v = 1;
-        const bool settled = warp_check<MODE, T>(sh, rb, ob, qbuf + lane * kMaxDof, active, nm, w, &v, nullptr, nullptr);
+        const bool settled = warp_check<MODE, T>(sh, rb, ob, qbuf + lane * kMaxDof, active, nm, w, &v, nullptr, nullptr) == kSettled;
         if (active) {
             if (!settled) {
                 const uint32_t slot = atomicAdd(P.recheck_count, 1u);

@@ -107,6 +107,107 @@ __global__ void __launch_bounds__(kThreads) k_recheck(const __grid_constant__ KP
     }
 }
 
+// ---------------------------------------------------------- pair recheck --
+// 1. FP64 skeleton of each recorded configuration; its accumulators reset.
+__global__ void k_pair_skel(const __grid_constant__ KParams P) {
+    const uint32_t n = min(*P.ps.cfg_count, P.ps.cfg_cap);
+    for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+        const PairCfg c = P.ps.cfgs[k];
+        const Seg &sg = P.segs[c.seg];
+        const DevRobot &rb = *sg.robot;
+        SkelWalker<0> sw;
+        sw.begin();
+        double *out = P.ps.skel + (size_t)k * (kMaxDof + 1) * 3;
+        const float *q = sg.q + c.config * rb.D;
+        for (int i = 0; i <= rb.D; ++i) sw.point(rb, q, i, out + 3 * i);
+        PairAcc &a = P.ps.acc[k];
+        for (int i = 0; i < kMaxDof; ++i) {
+            a.lkey[i] = 0x7fffffff;
+            a.hkey[i] = ~0ull;
+        }
+        a.dkey = 0x7fffffffffffffffLL;
+        a.coll = 0;
+    }
+}
+
+// 2. One thread per listed pair: the reference's FP64 tree on the FP64
+// skeleton (pairs of configurations that ended settled, or that were routed
+// to the whole-configuration recheck, have no record and are skipped).
+__global__ void k_pair_eval(const __grid_constant__ KParams P) {
+    const uint32_t n = min(*P.ps.pair_count, P.ps.pair_cap);
+    const uint32_t ncfg = min(*P.ps.cfg_count, P.ps.cfg_cap);
+    for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+        const uint64_t e = P.ps.pairs[k];
+        const uint32_t flat = (uint32_t)(e >> 17);
+        const int link = (int)((e >> 12) & 31u), j = (int)((e >> 1) & 2047u), kind = (int)(e & 1u);
+        const uint32_t slot = P.ps.slot_of[flat];
+        if (slot >= ncfg || P.ps.cfgs[slot].flat != flat) continue;
+        const Seg &sg = P.segs[P.ps.cfgs[slot].seg];
+        const DevRobot &rb = *sg.robot;
+        const double *A = P.ps.skel + (size_t)slot * (kMaxDof + 1) * 3 + 3 * link;
+        const double *B = A + 3;
+        ObsView<double> ob{sg.obs_d, sg.obs_f + (size_t)kRowGround * sg.n_pad, sg.n, sg.n_pad};
+        double o[6];
+        ob.box(j, o);
+        ExactPol pol;
+        PairAcc &a = P.ps.acc[slot];
+        if (kind == 0) {
+            if (coll_box(pol, P.nmd, A, B, rb.radius_d[link], rb.rnew_d[link], o)) atomicOr(&a.coll, 1);
+        } else {
+            double d = capsule_box(pol, P.nmd, A, B, rb.radius_d[link], o).v;
+            if (d > ob.tol(j)) d = P.nmd.maxd;   // :367-368
+            if (d == d) {
+                const float f = (float)d;
+                atomicMin(&a.lkey[link], Key<float>::of(f));
+                atomicMin(&a.dkey, Key<double>::of(d));
+                if (d <= 0.0) atomicMin(&a.hkey[link], ((unsigned long long)j << 32) | __float_as_uint(f));
+            }
+        }
+    }
+}
+
+// 3. Fold per recorded configuration in the reference's link order: the
+// first link holding a hit (settled FP32 or FP64) ends the scan; its profile
+// entry is the hit with the lowest obstacle index; earlier links take the
+// smaller of the settled FP32 minimum and the FP64 minimum.
+__global__ void k_pair_fold(const __grid_constant__ KParams P) {
+    const uint32_t n = min(*P.ps.cfg_count, P.ps.cfg_cap);
+    for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+        const PairCfg c = P.ps.cfgs[k];
+        const Seg &sg = P.segs[c.seg];
+        const PairAcc &a = P.ps.acc[k];
+        const int L = sg.robot->D;
+        const int64_t q = c.config;
+        if (sg.valid && a.coll) sg.valid[q] = 0;
+        if (!sg.dist && !sg.profile) continue;
+        float *prof = sg.profile ? sg.profile + q * L : nullptr;
+        int first = -1;
+        for (int i = 0; i < L; ++i) {
+            const unsigned long long h = a.hkey[i];
+            if (i == c.hit_link) {
+                if (prof && h != ~0ull && (int)(h >> 32) < c.hit_j) prof[i] = __uint_as_float((uint32_t)h);
+                first = i;
+                break;
+            }
+            if (h != ~0ull) {
+                if (prof) prof[i] = __uint_as_float((uint32_t)h);
+                first = i;
+                break;
+            }
+            if (prof && a.lkey[i] != 0x7fffffff) {
+                const float v = Key<float>::value(a.lkey[i]);
+                prof[i] = smin(prof[i], v);
+            }
+        }
+        if (prof && first >= 0)
+            for (int i = first + 1; i < L; ++i) prof[i] = 0.f;
+        if (sg.dist) {
+            if (first >= 0) sg.dist[q] = 0.0;
+            else if (a.dkey != 0x7fffffffffffffffLL) sg.dist[q] = smin(sg.dist[q], Key<double>::value(a.dkey));
+        }
+    }
+}
+
 // Skeleton points of each configuration (computeSkeleton), widened to double:
 // MODE 0 FP64, MODE 1 the reference's float skeleton, MODE 2 the FP32 FK of
 // the FP32 bulk pass.
@@ -326,6 +427,13 @@ cudaError_t launch_check_wide(int mode, const KParams &p, int64_t blocks, size_t
         if (!attr) { cudaFuncSetAttribute(k_check_wide<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024); attr = true; }
         k_check_wide<1><<<(unsigned)blocks, kWideThreads, smem, st>>>(p);
     }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_pair_recheck(const KParams &p, int grid, cudaStream_t st) {
+    k_pair_skel<<<grid, kThreads, 0, st>>>(p);
+    k_pair_eval<<<grid * 2, kThreads, 0, st>>>(p);
+    k_pair_fold<<<grid, kThreads, 0, st>>>(p);
     return cudaGetLastError();
 }
 

@@ -1,7 +1,8 @@
 // rpm_fast.cu -- the FP32 bulk pass of the FP32 + FP64-recheck form.  Every
-// decision of both trees carries a margin; configurations whose outputs
-// depended on a decision within kBand of its boundary are appended to the
-// recheck list and recomputed in FP64 by k_recheck (rpm_exact.cu).
+// decision of both trees carries a margin; pairs whose decisions fell within
+// kBand of a boundary are listed and re-evaluated in FP64 by the pair recheck
+// (rpm_exact.cu), or, when the lists are full, their configurations are
+// recomputed whole by k_recheck.
 #include "rpm_check.cuh"
 #include "rpm_edges.cuh"
 #include "rpm_launch.cuh"
@@ -34,14 +35,13 @@ __global__ void __launch_bounds__(kThreads) k_check_fp32(const __grid_constant__
     ObsView<float> ob{rows, rows + (size_t)kRowGround * sg.n_pad, sg.n, sg.n_pad};
     const Want w{sg.valid != nullptr, sg.dist != nullptr, sg.profile != nullptr};
     const int D = rb.D;
-    const bool ok = warp_check<2, float>(wsh[threadIdx.x >> 5], rb, ob, sg.q + c * D, active, P.nmf, w,
-                                         (w.valid && active) ? sg.valid + c : nullptr,
-                                         (w.dist && active) ? sg.dist + c : nullptr,
-                                         (w.profile && active) ? sg.profile + c * D : nullptr);
-    if (active && !ok) {
-        const uint32_t slot = atomicAdd(P.recheck_count, 1u);
-        P.recheck[slot] = ((uint64_t)s << 40) | (uint64_t)c;
-    }
+    int hl = -1, hj = 0x7fffffff;
+    const int st = warp_check<2, float>(wsh[threadIdx.x >> 5], rb, ob, sg.q + c * D, active, P.nmf, w,
+                                        (w.valid && active) ? sg.valid + c : nullptr,
+                                        (w.dist && active) ? sg.dist + c : nullptr,
+                                        (w.profile && active) ? sg.profile + c * D : nullptr, &P.ps,
+                                        (uint32_t)(sg.flat0 + warp0), &hl, &hj);
+    if (active) finish_config(&P.ps, st, (uint32_t)(sg.flat0 + c), s, c, hl, hj, P.recheck, P.recheck_count);
 }
 
 // FP32 pass of the warp-per-configuration form; unsettled configurations go

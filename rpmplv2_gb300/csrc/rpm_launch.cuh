@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 
 #include "rpm_dev.cuh"
+#include "rpm_check.cuh"
 #include "rpm_tree.cuh"
 
 namespace rpm {
@@ -17,9 +18,10 @@ struct KParams {
     int32_t wide_g;             // warp-per-configuration kernels: configurations per warp
     Num<double> nmd;
     Num<float> nmf;
-    uint64_t *recheck;          // FP32 pass -> FP64 recheck list: (segment << 40) | config
+    uint64_t *recheck;          // FP32 pass -> whole-configuration FP64 recheck: (segment << 40) | config
     uint32_t *recheck_count;
     int32_t *status;
+    PairSink ps;                // FP32 pass -> pair-level FP64 recheck
 };
 
 // Host helpers shared by the C ABI translation units (rpm_api.cu).
@@ -32,6 +34,9 @@ size_t smem_bytes(int mode, int n_pad);
 cudaError_t launch_check_exact(int mode, const KParams &p, int64_t blocks, size_t smem, cudaStream_t st);
 cudaError_t launch_check_fp32(const KParams &p, int64_t blocks, size_t smem, cudaStream_t st);
 cudaError_t launch_recheck(const KParams &p, int grid, cudaStream_t st);
+// Pair-level FP64 recheck: FK of the recorded configurations, their listed
+// pairs, and the fold into the outputs.
+cudaError_t launch_pair_recheck(const KParams &p, int grid, cudaStream_t st);
 // Warp-per-configuration form over the sorted scene copy (rpm_wide.cuh).
 size_t wide_smem_bytes(int mode, int ns, int nb);
 cudaError_t launch_check_wide(int mode, const KParams &p, int64_t blocks, size_t smem, cudaStream_t st);

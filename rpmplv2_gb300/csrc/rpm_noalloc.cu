@@ -79,7 +79,7 @@ __global__ void __launch_bounds__(kThreads) k_noalloc_fp32(const __grid_constant
     const bool ok = warp_check<2, float>(wsh[threadIdx.x >> 5], P.rb, ob, P.q + c * D, active, P.nmf, w,
                                          (w.valid && active) ? P.valid + c : nullptr,
                                          (w.dist && active) ? P.dist + c : nullptr,
-                                         (w.profile && active) ? P.profile + c * D : nullptr);
+                                         (w.profile && active) ? P.profile + c * D : nullptr) == kSettled;
     if (active && !ok) {
         unsigned long long *cnt = reinterpret_cast<unsigned long long *>(&P.scratch[kNoAllocMaxConfigs]);
         const unsigned long long slot = atomicAdd(cnt, 1ull);

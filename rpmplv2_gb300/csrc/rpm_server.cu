@@ -579,12 +579,7 @@ int rpm_server_destroy(rpm_server *srv) {
         for (Slot &sl : srv->slots) {
             auto it = srv->ctx->scratch.find(sl.st);
             if (it != srv->ctx->scratch.end()) {
-                Scratch *sc = it->second;
-                for (auto &g : sc->graphs) cudaGraphExecDestroy(g.exec);
-                cudaFree(sc->n_e); cudaFree(sc->local); cudaFree(sc->kmax); cudaFree(sc->bprefix); cudaFree(sc->full);
-                cudaFree(sc->work); cudaFree(sc->erecheck); cudaFree(sc->recheck); cudaFree(sc->counters); cudaFree(sc->status);
-                for (int i = 0; i < 3; ++i) if (sc->ev[i]) cudaEventDestroy(sc->ev[i]);
-                delete sc;
+                free_scratch(it->second);
                 srv->ctx->scratch.erase(it);
             }
             cudaStreamDestroy(sl.st);

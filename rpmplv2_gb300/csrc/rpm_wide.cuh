@@ -1,20 +1,22 @@
 // rpm_wide.cuh -- warp-per-configuration drivers of RealVectorSpace::isValid(q)
 // (RealVectorSpace.cpp:277-309) and computeDistance(q) (:318-392) over a
-// spatially sorted, block-bounded copy of the obstacles.
+// spatially sorted, leaf-bounded copy of the obstacles.
 //
 // Used for large scenes and small requests, where lane-per-configuration
 // leaves the GPU mostly idle and each lane walks hundreds of obstacles in
 // series.  Here a warp first runs the forward kinematics of G configurations
 // (lane = configuration, skeleton points kept in shared memory), then checks
 // them one at a time with the lanes spread over the obstacles:
-//   * blocks of 32 obstacles (Morton order of their centres) carry their union
-//     bounds and their largest / smallest min_dist_tol, so one gap test rejects
-//     a whole block;
-//   * isValid scans the blocks whose gap is within r*sqrt(2) of the link's
-//     bounding box (the reach of the reference's capsule-box tree);
-//   * distance visits blocks nearest-first and drains candidate pairs as they
-//     fill a 32-entry queue, so the running minimum tightens the threshold for
-//     the blocks still to visit.
+//   * leaves of 8 obstacles (a top-down median split of their centres) carry
+//     their union bounds and their largest / smallest min_dist_tol, so one gap
+//     test rejects a whole leaf; lanes cull 32 leaves at a time and then test
+//     the obstacles of up to four surviving leaves at a time (4 x 8 lanes);
+//   * isValid keeps the leaves within r*sqrt(2) of the link's bounding box
+//     (the reach of the reference's capsule-box tree);
+//   * distance visits the leaves in nearest-first bands (gap at most twice
+//     the nearest live gap plus 2 (r + EQUALITY_THRESHOLD + margin)) and
+//     re-prunes after each band, so the running minimum tightens the
+//     threshold for the leaves still to visit.
 // Every pair the lane-per-configuration driver would evaluate with a tree and
 // that can change an output is evaluated here too, with the same arithmetic;
 // results combine by the same rules (OR; minimum of ordered keys; first hit =
@@ -30,39 +32,57 @@ namespace rpm {
 constexpr int kWideWarps = 8;                       // warps per CTA
 constexpr int kWideThreads = kWideWarps * 32;
 constexpr int kWidePtsBytes = 2048;                 // skeleton buffer per warp
-constexpr int kBlk = 32;                            // obstacles per block
+constexpr int kLeaf = 8;                            // obstacles per leaf
 constexpr int kBlkRec = 8;                          // lo[3] hi[3] max tol, min tol (float)
-constexpr int kBlkPerLane = 3;                      // blocks per lane in the distance search
-constexpr int kMaxSorted = kBlk * 32 * kBlkPerLane; // sorted slots per scene (>= kMaxObstacles + 2 * kBlk)
+constexpr int kLeafPerLane = 9;                     // leaves per lane in the distance search
+constexpr int kMaxLeaves = 32 * kLeafPerLane;
 constexpr uint32_t kGroundBit = 0x80000000u;        // idx row: ground obstacle
 constexpr uint32_t kPadIdx = 0x7fffffffu;           // idx row: padding slot (bounds +inf / -inf)
-static_assert(kMaxSorted >= kMaxObstacles + 2 * kBlk, "sorted layout too small");
-// Automatic layout: warp-per-configuration for scenes of at least
-// kWideMinObstacles obstacles, or for batches too small to give each SM four
-// lane-per-configuration warps when links x obstacles reaches kWideMinPairs.
-constexpr int kWideMinObstacles = 128;
-constexpr int kWideMinPairs = 512;
+// static, moving and ground obstacles each pad to whole leaves
+static_assert(kMaxLeaves * kLeaf >= kMaxObstacles + 3 * (kLeaf - 1), "sorted layout too small");
+// Automatic layout (rpm_api.cu): warp-per-configuration for scenes of at
+// least kWideMinObstacles obstacles (profiles: batches up to
+// kWideMaxProfileBatch), of kWideMidObstacles with batches up to
+// kWideMidBatch, and of kWideSmallObstacles with batches up to kWideSmallBatch.
+constexpr int kWideMinObstacles = 150;
+constexpr int64_t kWideMaxProfileBatch = 16384;
+constexpr int kWideMidObstacles = 40;
+constexpr int64_t kWideMidBatch = 8192;
+constexpr int kWideSmallObstacles = 8;
+constexpr int64_t kWideSmallBatch = 512;
 
 // Sorted copy of one scene version: slot s holds original obstacle idx[s].
-// Non-ground obstacles come first in Morton order, ground obstacles start on a
-// block boundary after them, so a block is ground-only iff its first slot is.
+// Static obstacles come first, then moving ones, then ground ones, each group
+// in whole leaves, so a leaf is ground-only iff its first slot is ground.
 template <typename T> struct SortedView {
     const T *rows;          // [7][ns]: AABB, min_dist_tol
     const uint32_t *idx;    // [ns]
-    const float *blk;       // [nb][kBlkRec]
+    const float *blk;       // [nb][kBlkRec] leaf records
     int ns, nb;
     RPM_HD void box(int s, T *o) const {
 #pragma unroll
         for (int k = 0; k < 6; ++k) o[k] = rows[k * ns + s];
     }
     RPM_HD T tol(int s) const { return rows[kRowTol * ns + s]; }
-    RPM_HD bool ground_block(int b) const { return (idx[b * kBlk] & kGroundBit) != 0u; }
+    RPM_HD bool ground_leaf(int l) const { return (idx[l * kLeaf] & kGroundBit) != 0u; }
+    RPM_HD void leaf(int l, T *o) const {
+#pragma unroll
+        for (int k = 0; k < 6; ++k) o[k] = (T)blk[l * kBlkRec + k];
+    }
 };
 
 #ifdef __CUDACC__
-// Skeleton points per warp that fit the per-warp buffer.
-template <typename T> __host__ __device__ constexpr int wide_g_max(int D) {
-    return kWidePtsBytes / ((D + 1) * 3 * (int)sizeof(T));
+// Position of the (n+1)-th set bit of m (-1 if m has fewer).
+__device__ __forceinline__ int nth_bit(unsigned m, int n) {
+    for (int k = 0; k < n; ++k) m &= m - 1u;
+    return m ? __ffs(m) - 1 : -1;
+}
+
+// Drop the lowest four set bits of m (the leaves of one round).
+__device__ __forceinline__ unsigned drop4(unsigned m) {
+#pragma unroll
+    for (int k = 0; k < 4; ++k) m &= m - 1u;
+    return m;
 }
 
 template <int MODE, typename T>
@@ -83,27 +103,42 @@ __device__ __forceinline__ void wide_pop32(uint32_t *q, int &nq) {
     __syncwarp();
 }
 
+// Where unsettled pairs go: the sink (may be null), this configuration's
+// index in the launch, and the sticky list-full flag.
+struct WideSink {
+    const PairSink *ps;
+    uint32_t flat;
+    bool full;
+};
+
 template <int MODE, typename T>
 __device__ __forceinline__ void wide_drain_bool(const uint32_t *q, int nitems, const SortedView<T> &ob, const Num<T> &nm,
-                                                const T *A, const T *B, T r, T rn, bool &hit, bool &unc) {
+                                                const T *A, const T *B, T r, T rn, int i, WideSink &sk, bool &hit,
+                                                bool &unc) {
     typedef typename PolOf<MODE>::type P;
     const int lane = threadIdx.x & 31;
-    bool c = false, u = false;
+    bool c = false, u = false, f = false;
     if (lane < nitems) {
+        const int s = (int)q[lane];
         T o[6];
-        ob.box((int)q[lane], o);
+        ob.box(s, o);
         P pol;
         const bool cc = coll_box(pol, nm, A, B, r, rn, o);
-        if (P::robust && pol.m < kDecide) u = true;
-        else c = cc;
+        if (P::robust && pol.m < kDecide) {
+            u = true;
+            if (sk.ps) f = !push_pair(sk.ps, sk.flat, i, (int)(ob.idx[s] & ~kGroundBit), 0);
+        } else {
+            c = cc;
+        }
     }
     hit = hit || __any_sync(0xffffffffu, c);
     unc = unc || __any_sync(0xffffffffu, u);
+    sk.full = sk.full || __any_sync(0xffffffffu, f);
 }
 
 template <int MODE, typename T>
 __device__ __forceinline__ void wide_drain_dist(const uint32_t *q, int nitems, const DevRobot &rb, const SortedView<T> &ob,
-                                                const Num<T> &nm, const T *A, const T *B, int i,
+                                                const Num<T> &nm, const T *A, const T *B, int i, WideSink &sk,
                                                 typename Key<T>::type &lkey, int &hj, T &hv, bool &unc) {
     typedef typename Key<T>::type K;
     const unsigned full = 0xffffffffu;
@@ -111,17 +146,21 @@ __device__ __forceinline__ void wide_drain_dist(const uint32_t *q, int nitems, c
     K kk = Key<T>::of(nm.maxd);
     int jj = 0x7fffffff;
     T vv = T(0);
-    bool u = false;
+    bool u = false, f = false;
     if (lane < nitems) {
         const int s = (int)q[lane];
         bool settled;
         const T d = pair_distance<MODE, T>(rb, ob, nm, A, B, i, s, settled);
-        u = !settled;
-        if (d == d) {   // the reference's std::min ignores NaN
+        const int j = (int)(ob.idx[s] & ~kGroundBit);
+        if (!settled) {
+            u = true;
+            if (sk.ps) f = !push_pair(sk.ps, sk.flat, i, j, 1);
+        } else if (d == d) {   // the reference's std::min ignores NaN
             kk = Key<T>::of(d);
-            if (d <= T(0) && settled) { jj = (int)(ob.idx[s] & ~kGroundBit); vv = d; }
+            if (d <= T(0)) { jj = j; vv = d; }
         }
     }
+    sk.full = sk.full || __any_sync(full, f);
 #pragma unroll
     for (int off = 16; off > 0; off >>= 1) {
         const K ok = __shfl_xor_sync(full, kk, off);
@@ -135,12 +174,14 @@ __device__ __forceinline__ void wide_drain_dist(const uint32_t *q, int nitems, c
     unc = unc || __any_sync(full, u);
 }
 
-// One configuration, the whole warp.  pts = skeleton points [(D+1)][3].
-// Returns whether the outputs are settled (always true for the exact forms);
-// lane 0 writes the outputs.
+// One configuration, the whole warp.  pts = skeleton points [(D+1)][3];
+// gl = per-warp scratch of nb leaf gaps.  Returns kSettled, kPairs or kFull
+// (always kSettled for the exact forms) and the first settled hit (link,
+// original obstacle index); lane 0 writes the outputs.
 template <int MODE, typename T>
-__device__ bool wide_config(uint32_t *q, const DevRobot &rb, const SortedView<T> &ob, const T *pts, const Num<T> &nm,
-                            Want w, uint8_t *valid_out, double *dist_out, float *prof_out) {
+__device__ int wide_config(uint32_t *q, T *gl, const DevRobot &rb, const SortedView<T> &ob, const T *pts,
+                           const Num<T> &nm, Want w, uint8_t *valid_out, double *dist_out, float *prof_out,
+                           WideSink &sk, int &hit_link, int &hit_j) {
     typedef typename Key<T>::type K;
     const unsigned full = 0xffffffffu;
     const int lane = threadIdx.x & 31;
@@ -149,7 +190,9 @@ __device__ bool wide_config(uint32_t *q, const DevRobot &rb, const SortedView<T>
     bool collided = false, unc_b = false, unc_d = false;
     T best = nm.maxd;
     int hit = -1;
+    hit_j = 0x7fffffff;
     const int L = rb.D;
+    const int kspan = (ob.nb + 31) / 32;   // leaf slices of 32
     const T dmargin = (MODE == 2) ? T(kBand) : LinkConst<T>::margin();
     for (int i = 0; i < L && (need_b || need_d); ++i) {
         T A[3], B[3], lo[3], hi[3];
@@ -169,36 +212,37 @@ __device__ bool wide_config(uint32_t *q, const DevRobot &rb, const SortedView<T>
             const T rn = LinkConst<T>::rn(rb, i);
             bool hb = false, ub = false;
             int nq = 0;
-            for (int b0 = 0; b0 < ob.nb && !hb; b0 += 32) {
-                const int b = b0 + lane;
-                bool cb = false;
-                if (b < ob.nb && !(gskip && ob.ground_block(b))) {
-                    const float *bk = ob.blk + b * kBlkRec;
+            for (int l0 = 0; l0 < ob.nb && !hb; l0 += 32) {
+                const int l = l0 + lane;
+                bool cl = false;
+                if (l < ob.nb && !(gskip && ob.ground_leaf(l))) {
                     T o[6];
-#pragma unroll
-                    for (int k = 0; k < 6; ++k) o[k] = (T)bk[k];
-                    cb = !(gap2_bb(lo, hi, o) > tb2);
+                    ob.leaf(l, o);
+                    cl = !(gap2_bb(lo, hi, o) > tb2);
                 }
-                unsigned mb = __ballot_sync(full, cb);
-                while (mb != 0u && !hb) {
-                    const int bb = __ffs(mb) - 1;
-                    mb &= mb - 1u;
-                    const int s = (b0 + bb) * kBlk + lane;
-                    const uint32_t id = ob.idx[s];
+                unsigned ml = __ballot_sync(full, cl);
+                while (ml != 0u && !hb) {
+                    const int bit = nth_bit(ml, lane >> 3);
+                    ml = drop4(ml);
                     bool c = false;
-                    if (id != kPadIdx && !(gskip && (id & kGroundBit))) {
-                        T o[6];
-                        ob.box(s, o);
-                        c = !(gap2_bb(lo, hi, o) > tb2);
+                    int s = 0;
+                    if (bit >= 0) {
+                        s = (l0 + bit) * kLeaf + (lane & (kLeaf - 1));
+                        const uint32_t id = ob.idx[s];
+                        if (id != kPadIdx && !(gskip && (id & kGroundBit))) {
+                            T o[6];
+                            ob.box(s, o);
+                            c = !(gap2_bb(lo, hi, o) > tb2);
+                        }
                     }
                     wide_push<MODE, T>(q, nq, c, (uint32_t)s);
                     if (nq >= 32) {
-                        wide_drain_bool<MODE, T>(q, 32, ob, nm, A, B, r, rn, hb, ub);
+                        wide_drain_bool<MODE, T>(q, 32, ob, nm, A, B, r, rn, i, sk, hb, ub);
                         wide_pop32(q, nq);
                     }
                 }
             }
-            if (nq > 0 && !hb) wide_drain_bool<MODE, T>(q, nq, ob, nm, A, B, r, rn, hb, ub);
+            if (nq > 0 && !hb) wide_drain_bool<MODE, T>(q, nq, ob, nm, A, B, r, rn, i, sk, hb, ub);
             __syncwarp();
             if (hb) { collided = true; need_b = false; }
             else if (ub) unc_b = true;
@@ -210,84 +254,97 @@ __device__ bool wide_config(uint32_t *q, const DevRobot &rb, const SortedView<T>
             int hj = 0x7fffffff;
             T hv = T(0);
             bool ud = false;
-            T g2b[kBlkPerLane], tmax[kBlkPerLane], tmin[kBlkPerLane];
             unsigned todo = 0u;
-#pragma unroll
-            for (int k = 0; k < kBlkPerLane; ++k) {
-                const int b = lane + 32 * k;
-                g2b[k] = inf; tmax[k] = T(0); tmin[k] = T(0);
-                if (b < ob.nb && !(gskip && ob.ground_block(b))) {
-                    const float *bk = ob.blk + b * kBlkRec;
-                    T o[6];
-#pragma unroll
-                    for (int c = 0; c < 6; ++c) o[c] = (T)bk[c];
-                    g2b[k] = gap2_bb(lo, hi, o);
-                    tmax[k] = (T)bk[6];
-                    tmin[k] = (T)bk[7];
-                    todo |= 1u << k;
+            for (int k = 0; k < kspan; ++k) {
+                const int l = lane + 32 * k;
+                if (l < ob.nb) {
+                    T g = inf;
+                    if (!(gskip && ob.ground_leaf(l))) {
+                        T o[6];
+                        ob.leaf(l, o);
+                        g = gap2_bb(lo, hi, o);
+                        todo |= 1u << k;
+                    }
+                    gl[l] = g;
                 }
             }
+            __syncwarp();
             int nq = 0;
-            bool seeded = false;
-            for (;;) {
+            bool stop = false;
+            while (!stop) {
                 const bool hunting = hj != 0x7fffffff;
                 const T thr0 = w.profile ? Key<T>::value(lkey) : smin(best, Key<T>::value(lkey));
-                // nearest block still alive (thresholds only shrink, so a pruned block stays pruned)
-                T bg = inf;
-                int sel = 0x7fffffff;
-#pragma unroll
-                for (int k = 0; k < kBlkPerLane; ++k) {
+                // prune (thresholds only shrink, so a pruned leaf stays pruned) and find the nearest live leaf
+                T gmin = inf;
+                for (int k = 0; k < kspan; ++k) {
                     if (!((todo >> k) & 1u)) continue;
+                    const int l = lane + 32 * k;
+                    const T g = gl[l];
                     bool alive;
                     if (hunting) {
-                        alive = !(g2b[k] > hunt * hunt);
+                        alive = !(g > hunt * hunt);
                     } else {
-                        const T smax = smin(thr0, tmax[k]) + r + nm.eq + dmargin;
-                        const T slo = smin(thr0, tmin[k]) + r + nm.eq + dmargin;
-                        alive = !(slo > T(0) && g2b[k] > smax * smax);
+                        const T smax = smin(thr0, (T)ob.blk[l * kBlkRec + 6]) + r + nm.eq + dmargin;
+                        const T slo = smin(thr0, (T)ob.blk[l * kBlkRec + 7]) + r + nm.eq + dmargin;
+                        alive = !(slo > T(0) && g > smax * smax);
                     }
                     if (!alive) todo &= ~(1u << k);
-                    else if (g2b[k] < bg || sel == 0x7fffffff) { bg = g2b[k]; sel = lane + 32 * k; }
+                    else if (g < gmin) gmin = g;
                 }
+                if (!__any_sync(full, todo != 0u)) break;
 #pragma unroll
                 for (int off = 16; off > 0; off >>= 1) {
-                    const T og = __shfl_xor_sync(full, bg, off);
-                    const int ob_ = __shfl_xor_sync(full, sel, off);
-                    if (og < bg || (!(bg < og) && ob_ < sel)) { bg = og; sel = ob_; }
+                    const T o = __shfl_xor_sync(full, gmin, off);
+                    gmin = o < gmin ? o : gmin;
                 }
-                if (sel == 0x7fffffff) break;
-                if ((sel & 31) == lane) todo &= ~(1u << (sel >> 5));
-                const int s = sel * kBlk + lane;
-                const uint32_t id = ob.idx[s];
-                bool c = false;
-                if (id != kPadIdx && !(gskip && (id & kGroundBit))) {
-                    T o[6];
-                    ob.box(s, o);
-                    const T g2 = gap2_bb(lo, hi, o);
-                    if (hunting) {
-                        c = w.profile && (int)(id & ~kGroundBit) < hj && !(g2 > hunt * hunt);
-                    } else {
-                        const T sv = smin(thr0, ob.tol(s)) + r + nm.eq + dmargin;
-                        c = !(sv > T(0) && g2 > sv * sv);
+                // this band: live leaves with gap <= 2 * nearest gap + 2 (r + eq + margin)
+                const T gb = hunting ? inf : T(2) * sqrt(gmin) + T(2) * (r + nm.eq + dmargin);
+                const T gb2 = gb * gb;
+                unsigned band = 0u;
+                for (int k = 0; k < kspan; ++k)
+                    if (((todo >> k) & 1u) && !(gl[lane + 32 * k] > gb2)) band |= 1u << k;
+                todo &= ~band;
+                for (int k = 0; k < kspan && !stop; ++k) {
+                    unsigned ml = __ballot_sync(full, (band >> k) & 1u);
+                    while (ml != 0u && !stop) {
+                        const int bit = nth_bit(ml, lane >> 3);
+                        ml = drop4(ml);
+                        bool c = false;
+                        int s = 0;
+                        if (bit >= 0) {
+                            s = (bit + 32 * k) * kLeaf + (lane & (kLeaf - 1));
+                            const uint32_t id = ob.idx[s];
+                            if (id != kPadIdx && !(gskip && (id & kGroundBit))) {
+                                T o[6];
+                                ob.box(s, o);
+                                const T g2 = gap2_bb(lo, hi, o);
+                                if (hunting) {
+                                    c = w.profile && (int)(id & ~kGroundBit) < hj && !(g2 > hunt * hunt);
+                                } else {
+                                    const T sv = smin(thr0, ob.tol(s)) + r + nm.eq + dmargin;
+                                    c = !(sv > T(0) && g2 > sv * sv);
+                                }
+                            }
+                        }
+                        wide_push<MODE, T>(q, nq, c, (uint32_t)s);
+                        if (nq >= 32) {
+                            wide_drain_dist<MODE, T>(q, 32, rb, ob, nm, A, B, i, sk, lkey, hj, hv, ud);
+                            wide_pop32(q, nq);
+                            stop = hj != 0x7fffffff && !w.profile;   // the distance is 0 whatever else is found
+                        }
                     }
                 }
-                wide_push<MODE, T>(q, nq, c, (uint32_t)s);
-                if (nq >= 32 || (nq > 0 && !seeded)) {
-                    const int take = nq < 32 ? nq : 32;
-                    wide_drain_dist<MODE, T>(q, take, rb, ob, nm, A, B, i, lkey, hj, hv, ud);
-                    if (take == 32) wide_pop32(q, nq);
-                    else nq = 0;
-                    seeded = true;
-                    if (hj != 0x7fffffff && !w.profile) break;   // the distance is 0 whatever else is found
-                }
+                if (nq > 0 && !stop) wide_drain_dist<MODE, T>(q, nq, rb, ob, nm, A, B, i, sk, lkey, hj, hv, ud);
+                nq = 0;
+                __syncwarp();
+                if (hj != 0x7fffffff && !w.profile) stop = true;
             }
-            if (nq > 0 && !(hj != 0x7fffffff && !w.profile))
-                wide_drain_dist<MODE, T>(q, nq, rb, ob, nm, A, B, i, lkey, hj, hv, ud);
             __syncwarp();
             if (ud) unc_d = true;
             if (hj != 0x7fffffff) {
                 // the partial minimum at the first hit is the hit's own value
                 hit = i;
+                hit_j = hj;
                 need_d = false;
                 if (w.profile && lane == 0) prof_out[i] = (float)hv;
             } else {
@@ -303,16 +360,18 @@ __device__ bool wide_config(uint32_t *q, const DevRobot &rb, const SortedView<T>
         if (w.valid) *valid_out = collided ? 0 : 1;
         if (w.dist) *dist_out = (hit >= 0) ? 0.0 : (double)best;
     }
+    hit_link = hit;
     const bool bad_b = w.valid && !collided && unc_b;
     const bool bad_d = (w.dist || w.profile) && unc_d && (w.profile || hit < 0);
-    return !(bad_b || bad_d);
+    if (!(bad_b || bad_d)) return kSettled;
+    return (sk.ps && !sk.full) ? kPairs : kFull;
 }
 
 // Shared-memory layout of the wide kernels: robot, sorted rows, index row,
 // block records, per-warp skeleton buffers.  Every piece is a multiple of 16
 // bytes (ns is a multiple of 32).
 struct WideLayout {
-    uint32_t rows, idx, blk, pts, total;
+    uint32_t rows, idx, blk, pts, gl, gl_warp, total;
     RPM_HD static WideLayout of(int mode, int ns, int nb) {
         WideLayout l;
         const uint32_t tsz = mode == RPM_PREC_FP64 ? 8u : 4u;
@@ -320,7 +379,9 @@ struct WideLayout {
         l.idx = l.rows + 7u * (uint32_t)ns * tsz;
         l.blk = l.idx + 4u * (uint32_t)ns;
         l.pts = l.blk + 4u * kBlkRec * (uint32_t)nb;
-        l.total = l.pts + kWideWarps * kWidePtsBytes;
+        l.gl = l.pts + kWideWarps * kWidePtsBytes;
+        l.gl_warp = ((uint32_t)nb * tsz + 15u) & ~15u;
+        l.total = l.gl + kWideWarps * l.gl_warp;
         return l;
     }
 };
@@ -353,6 +414,7 @@ __device__ __forceinline__ void wide_kernel_body(const KParams &P, unsigned char
     const int64_t c0 = (int64_t)(blockIdx.x - sg.first_block) * (kWideWarps * G) + (int64_t)warp * G;
     if (c0 >= sg.count) return;   // whole warp idle
     T *pts = reinterpret_cast<T *>(smem + L.pts + warp * kWidePtsBytes);
+    T *gl = reinterpret_cast<T *>(smem + L.gl + warp * L.gl_warp);
     // forward kinematics, lane = configuration
     if (lane < G && c0 + lane < sg.count) {
         SkelWalker<MODE> sw;
@@ -369,13 +431,12 @@ __device__ __forceinline__ void wide_kernel_body(const KParams &P, unsigned char
     for (int g = 0; g < G; ++g) {
         const int64_t c = c0 + g;
         if (c >= sg.count) break;
-        const bool ok = wide_config<MODE, T>(wq[warp], rb, ob, pts + g * (D + 1) * 3, nm, w,
-                                             w.valid ? sg.valid + c : nullptr, w.dist ? sg.dist + c : nullptr,
-                                             w.profile ? sg.profile + c * D : nullptr);
-        if (MODE == 2 && !ok && lane == 0) {
-            const uint32_t slot = atomicAdd(P.recheck_count, 1u);
-            P.recheck[slot] = ((uint64_t)s << 40) | (uint64_t)c;
-        }
+        WideSink sk{MODE == 2 ? &P.ps : nullptr, (uint32_t)(sg.flat0 + c), false};
+        int hl, hj;
+        const int st = wide_config<MODE, T>(wq[warp], gl, rb, ob, pts + g * (D + 1) * 3, nm, w,
+                                            w.valid ? sg.valid + c : nullptr, w.dist ? sg.dist + c : nullptr,
+                                            w.profile ? sg.profile + c * D : nullptr, sk, hl, hj);
+        if (MODE == 2 && lane == 0) finish_config(&P.ps, st, sk.flat, s, c, hl, hj, P.recheck, P.recheck_count);
     }
 }
 #endif
