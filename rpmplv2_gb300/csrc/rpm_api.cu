@@ -230,7 +230,7 @@ void free_scratch(Scratch *sc) {
     for (auto &g : sc->graphs) cudaGraphExecDestroy(g.exec);
     cudaFree(sc->n_e); cudaFree(sc->local); cudaFree(sc->kmax); cudaFree(sc->bprefix); cudaFree(sc->full);
     cudaFree(sc->work); cudaFree(sc->erecheck); cudaFree(sc->recheck); cudaFree(sc->counters); cudaFree(sc->status);
-    cudaFree(sc->pairs); cudaFree(sc->pcfgs); cudaFree(sc->slot_of); cudaFree(sc->pskel); cudaFree(sc->pacc);
+    cudaFree(sc->pairs); cudaFree(sc->pcfgs); cudaFree(sc->pskel); cudaFree(sc->pacc);
     for (int i = 0; i < 3; ++i) if (sc->ev[i]) cudaEventDestroy(sc->ev[i]);
     delete sc;
 }
@@ -249,7 +249,7 @@ int get_scratch(rpm_ctx *ctx, cudaStream_t st, int64_t need, Scratch **out) {
         if (s->recheck) {
             CK(cudaStreamSynchronize(st));
             cudaFree(s->recheck);
-            cudaFree(s->pairs); cudaFree(s->pcfgs); cudaFree(s->slot_of); cudaFree(s->pskel); cudaFree(s->pacc);
+            cudaFree(s->pairs); cudaFree(s->pcfgs); cudaFree(s->pskel); cudaFree(s->pacc);
             s->recheck = nullptr;
         }
         const size_t cap = std::max<size_t>((size_t)need, 1u << 16);
@@ -258,7 +258,6 @@ int get_scratch(rpm_ctx *ctx, cudaStream_t st, int64_t need, Scratch **out) {
         const size_t pcfg = std::min<size_t>(cap, std::max<size_t>(4096, std::min<size_t>(cap / 8, 1u << 16)));
         const size_t ppair = 16 * pcfg;
         if (cudaMalloc(&s->recheck, cap * sizeof(uint64_t)) != cudaSuccess ||
-            cudaMalloc(&s->slot_of, cap * sizeof(uint32_t)) != cudaSuccess ||
             cudaMalloc(&s->pairs, ppair * sizeof(uint64_t)) != cudaSuccess ||
             cudaMalloc(&s->pcfgs, pcfg * sizeof(PairCfg)) != cudaSuccess ||
             cudaMalloc(&s->pskel, pcfg * (kMaxDof + 1) * 3 * sizeof(double)) != cudaSuccess ||
@@ -387,7 +386,7 @@ int enqueue_segments(rpm_ctx *ctx, int prec, const std::vector<SegReq> &reqs, cu
         const int64_t want = (chunk_total + (int64_t)ctx->num_sms * 32 - 1) / ((int64_t)ctx->num_sms * 32);
         p.wide_g = (int32_t)std::max<int64_t>(1, std::min<int64_t>(gmax, want));
         const int64_t per_cta = wide ? (int64_t)kWideWarps * p.wide_g : kThreads;
-        int64_t blocks = 0, flat = 0;
+        int64_t blocks = 0;
         size_t smem = 0;
         for (const SegReq *rp : segs) {
             const SegReq &r = *rp;
@@ -407,8 +406,6 @@ int enqueue_segments(rpm_ctx *ctx, int prec, const std::vector<SegReq> &reqs, cu
             g.profile = r.profile;
             g.count = r.count;
             g.first_block = blocks;
-            g.flat0 = flat;
-            flat += r.count;
             g.n = r.scene->n;
             g.n_pad = r.scene->n_pad;
             g.srt_f = buf.sf;
@@ -433,7 +430,6 @@ int enqueue_segments(rpm_ctx *ctx, int prec, const std::vector<SegReq> &reqs, cu
         p.ps.cfg_cap = (uint32_t)sc->pcfg_cap;
         p.ps.cfgs = sc->pcfgs;
         p.ps.cfg_count = sc->counters + 2;
-        p.ps.slot_of = sc->slot_of;
         p.ps.skel = sc->pskel;
         p.ps.acc = sc->pacc;
         if (ci > 0) CK(cudaMemsetAsync(sc->counters, 0, 4 * sizeof(uint32_t), st));   // the recheck lists are per launch
@@ -457,6 +453,16 @@ int enqueue_segments(rpm_ctx *ctx, int prec, const std::vector<SegReq> &reqs, cu
         b->users.push_back(e);
     }
     return RPM_OK;
+}
+
+// Layout of an edge batch: the checks of one edge are neighbours in space,
+// so the lane-per-check warps of the lane layout already share most of their
+// obstacle walk; the warp layout pays off once culling whole leaves beats
+// walking every obstacle.
+static bool edge_warp_layout(const rpm_ctx *ctx, const SceneRec *s) {
+    if (ctx->layout == RPM_LAYOUT_LANE) return false;
+    if (ctx->layout == RPM_LAYOUT_WARP) return true;
+    return s->n >= kWideEdgeObstacles;
 }
 
 int edge_scratch(rpm_ctx *ctx, Scratch *sc, int64_t E, cudaStream_t st) {
@@ -493,6 +499,11 @@ int enqueue_edges(rpm_ctx *ctx, Scratch *sc, SceneRec *s, int prec, const float 
     p.seg.obs_d = buf.d;
     p.seg.n = s->n;
     p.seg.n_pad = s->n_pad;
+    p.seg.srt_f = buf.sf;
+    p.seg.srt_d = buf.sd;
+    p.seg.blk = buf.blk;
+    p.seg.ns = s->ns;
+    p.seg.nb = s->nb;
     p.q1 = q1; p.q2 = q2; p.E = E; p.step = step; p.num_checks = num_checks;
     p.n_e = sc->n_e; p.local = sc->local; p.bprefix = sc->bprefix; p.kmax = sc->kmax; p.work = sc->work;
     p.full = sc->full;
@@ -503,13 +514,31 @@ int enqueue_edges(rpm_ctx *ctx, Scratch *sc, SceneRec *s, int prec, const float 
     p.valid = valid; p.checks_out = checks; p.status = sc->status;
     p.nmd.eq = ctx->params.equality_threshold; p.nmd.maxd = ctx->params.max_distance;
     p.nmf.eq = (float)ctx->params.equality_threshold; p.nmf.maxd = (float)ctx->params.max_distance;
+    p.ps.pairs = sc->pairs;
+    p.ps.pair_count = sc->counters + 3;
+    p.ps.pair_cap = (uint32_t)sc->ppair_cap;
+    p.ps.cfg_cap = (uint32_t)sc->pcfg_cap;
+    p.ps.cfgs = sc->pcfgs;
+    p.ps.cfg_count = sc->counters + 2;
+    p.ps.skel = sc->pskel;
+    p.ps.acc = sc->pacc;
+    const int D = ctx->robots[s->robot].desc.num_dofs;
+    const size_t tsz = prec == RPM_PREC_FP64 ? sizeof(double) : sizeof(float);
+    p.wide_g = std::max(1, std::min(32, kWidePtsBytes / ((D + 1) * 3 * (int)tsz)));
     CK(cudaMemsetAsync(sc->counters, 0, 4 * sizeof(uint32_t), st));
     if (E == 0) return RPM_OK;
     CK(launch_edge_prep(p, st));
-    const int grid = ctx->num_sms * std::max(1, ctas_per_sm);
-    if (prec == RPM_PREC_FP32_RECHECK) CK(launch_edges_fp32(p, grid, smem_bytes(RPM_PREC_FP32_REF, s->n_pad), st));
-    else CK(launch_edges(prec, p, grid, smem_bytes(prec, s->n_pad), st));
-    CK(launch_edge_recheck_final(p, ctx->num_sms * 4, st));
+    const bool wide = edge_warp_layout(ctx, s);
+    if (wide) {
+        // persistent: as many CTAs as fit (two per SM for the FP32 forms)
+        const int grid = ctx->num_sms * (prec == RPM_PREC_FP64 ? 1 : 2);
+        CK(launch_edges_wide(prec, p, grid, wide_smem_bytes(prec, s->ns, s->nb), st));
+    } else {
+        const int grid = ctx->num_sms * std::max(1, ctas_per_sm);
+        if (prec == RPM_PREC_FP32_RECHECK) CK(launch_edges_fp32(p, grid, smem_bytes(RPM_PREC_FP32_REF, s->n_pad), st));
+        else CK(launch_edges(prec, p, grid, smem_bytes(prec, s->n_pad), st));
+    }
+    CK(launch_edge_recheck_final(p, ctx->num_sms * 4, prec == RPM_PREC_FP32_RECHECK, st));
     return RPM_OK;
 }
 
@@ -723,7 +752,7 @@ int rpm_check_edges(rpm_ctx *ctx, int32_t scene_id, int32_t precision, const flo
     if (set_device(ctx)) return RPM_ERR_CUDA;
     cudaStream_t st = (cudaStream_t)stream;
     Scratch *sc = nullptr;
-    int rc = get_scratch(ctx, st, 0, &sc);
+    int rc = get_scratch(ctx, st, std::max<int64_t>(1, num_edges), &sc);   // pair-recheck lists sized by the batch
     if (rc) return rc;
     rc = edge_scratch(ctx, sc, num_edges, st);
     if (rc) return rc;
@@ -739,7 +768,7 @@ int rpm_check_edges(rpm_ctx *ctx, int32_t scene_id, int32_t precision, const flo
         std::vector<uint64_t> key = {(uint64_t)(uintptr_t)&buf, (uint64_t)(uintptr_t)buf.f, (uint64_t)precision,
                                      (uint64_t)(uintptr_t)q1_dev, (uint64_t)(uintptr_t)q2_dev, (uint64_t)num_edges,
                                      (uint64_t)step_bits, (uint64_t)num_checks, (uint64_t)(uintptr_t)valid_dev,
-                                     (uint64_t)(uintptr_t)checks_dev, (uint64_t)ctas};
+                                     (uint64_t)(uintptr_t)checks_dev, (uint64_t)ctas, (uint64_t)ctx->layout};
         cudaGraphExec_t exec = nullptr;
         for (auto &g : sc->graphs) if (g.key == key) { exec = g.exec; break; }
         if (!exec) {

@@ -47,20 +47,21 @@ struct Want {
 // Pair-level FP64 recheck of the FP32 pass.  The FP32 pass folds only settled
 // pairs into its outputs and running minima (a settled value is within the
 // contact band of its FP64 value, so pruning on settled values stays exact)
-// and lists every unsettled (configuration, link, obstacle, kind) pair.  A
-// configuration whose outputs depend on a listed pair gets a record; the FP64
-// kernels then run the forward kinematics of each recorded configuration,
+// and lists every unsettled (record, link, obstacle, kind) pair.  A record is
+// allocated at a configuration's first unsettled pair and completed when the
+// configuration ends; only records completed with status kPairs are used.
+// The FP64 kernels then run the forward kinematics of each such configuration,
 // evaluate its listed pairs and fold their results into the outputs in the
-// reference's link order.  Configurations whose pairs do not fit the lists
-// are recomputed whole by the configuration-level recheck.
+// reference's link order.  Configurations whose pairs do not fit the lists are
+// recomputed whole by the configuration-level recheck.
 constexpr int kSettled = 0;      // outputs final
 constexpr int kPairs = 1;        // outputs final after the pair recheck
 constexpr int kFull = 2;         // recompute the whole configuration in FP64
 
 struct PairCfg {
-    uint32_t flat;               // configuration index within the launch
-    int32_t seg;
-    int64_t config;              // index within its segment
+    int32_t status;              // kPairs when the pair recheck applies
+    int32_t seg;                 // segment (edge checks: the check number k)
+    int64_t config;              // index within its segment (edge checks: the edge)
     int32_t hit_link;            // link of the first settled hit (-1: none)
     int32_t hit_j;               // lowest obstacle index of a settled hit in that link
 };
@@ -74,44 +75,44 @@ struct PairAcc {
 };
 
 struct PairSink {
-    uint64_t *pairs;             // flat << 17 | link << 12 | obstacle << 1 | kind (0 isValid, 1 distance)
+    uint64_t *pairs;             // record << 17 | link << 12 | obstacle << 1 | kind (0 isValid, 1 distance)
     uint32_t *pair_count;
     uint32_t pair_cap;
     uint32_t cfg_cap;
     PairCfg *cfgs;
     uint32_t *cfg_count;
-    uint32_t *slot_of;           // [configurations of the launch] -> record
     double *skel;                // [cfg_cap][kMaxDof + 1][3]
     PairAcc *acc;                // [cfg_cap]
 };
 
 #ifdef __CUDACC__
-// Append an unsettled pair; false when the list is full.
-__device__ __forceinline__ bool push_pair(const PairSink *ps, uint32_t flat, int link, int j, int kind) {
+// A new record (status kSettled until completed), or -1 when the list is full.
+__device__ __forceinline__ int alloc_record(const PairSink *ps) {
+    const uint32_t s = atomicAdd(ps->cfg_count, 1u);
+    if (s >= ps->cfg_cap) return -1;
+    ps->cfgs[s].status = kSettled;
+    return (int)s;
+}
+
+// Append an unsettled pair of record 'slot'; false when the list is full.
+__device__ __forceinline__ bool push_pair(const PairSink *ps, int slot, int link, int j, int kind) {
     const uint32_t s = atomicAdd(ps->pair_count, 1u);
     if (s >= ps->pair_cap) return false;
-    ps->pairs[s] = ((uint64_t)flat << 17) | ((uint64_t)link << 12) | ((uint64_t)j << 1) | (uint64_t)kind;
+    ps->pairs[s] = ((uint64_t)(uint32_t)slot << 17) | ((uint64_t)link << 12) | ((uint64_t)j << 1) | (uint64_t)kind;
     return true;
 }
 
-// Route a configuration the FP32 pass did not settle: a pair-recheck record,
-// or (no sink, list overflow) the whole-configuration recheck list.
-__device__ __forceinline__ void finish_config(const PairSink *ps, int status, uint32_t flat, int seg, int64_t c,
-                                              int hit_link, int hit_j, uint64_t *recheck, uint32_t *recheck_count) {
-    if (status == kSettled) return;
-    if (status == kPairs && ps) {
-        const uint32_t slot = atomicAdd(ps->cfg_count, 1u);
-        if (slot < ps->cfg_cap) {
-            ps->cfgs[slot] = PairCfg{flat, seg, c, hit_link, hit_j};
-            ps->slot_of[flat] = slot;
-            return;
-        }
-    }
-    const uint32_t r = atomicAdd(recheck_count, 1u);
-    recheck[r] = ((uint64_t)seg << 40) | (uint64_t)c;
+__device__ __forceinline__ void complete_record(const PairSink *ps, int slot, int status, int seg, int64_t config,
+                                                int hit_link, int hit_j) {
+    if (slot >= 0) ps->cfgs[slot] = PairCfg{status == kPairs ? kPairs : kSettled, seg, config, hit_link, hit_j};
 }
-#endif
 
+// An unsettled pair found by a drain lane, waiting for its owner's record.
+struct Pend {
+    bool on;
+    int owner, j, kind;
+};
+#endif
 #if defined(RPM_MARGIN_DEBUG)
 inline int g_dbg_site_b = 0, g_dbg_site_d = 0;   // host debugging only
 #endif
@@ -251,8 +252,37 @@ template <typename T> struct WarpShared {
     int hitj[32];                        // lowest obstacle index with a settled d' <= 0
     T hitv[32];                          // d' at that index
     int flags[32];                       // bit0 collision, bit1 isValid unsettled, bit2 distance unsettled
+    int slot[32];                        // pair-recheck record per owner (-1: none yet)
+    int need[32];                        // owner has pairs waiting for a record
+    uint32_t pend[32];                   // drain lane's unsettled pair: 1 << 31 | kind << 16 | j << 5 | owner
     uint32_t qb[64], qd[64];             // queues: owner | j << 5
 };
+
+// After a drain: give every owner with waiting pairs a record, then list the
+// pairs (an owner without a record, or a full pair list, marks bit 8).
+template <typename T>
+__device__ __forceinline__ void flush_pending(WarpShared<T> &sh, const PairSink *ps, int link) {
+    const unsigned full = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    const uint32_t pe = sh.pend[lane];
+    const Pend pp{pe != 0u, (int)(pe & 31u), (int)((pe >> 5) & 2047u), (int)((pe >> 16) & 1u)};
+    if (pp.on) sh.need[pp.owner] = 1;
+    __syncwarp();
+    if (sh.need[lane]) {
+        sh.need[lane] = 0;
+        if (sh.slot[lane] < 0 && !(sh.flags[lane] & 8)) {
+            const int s = alloc_record(ps);
+            if (s >= 0) sh.slot[lane] = s;
+            else atomicOr(&sh.flags[lane], 8);
+        }
+    }
+    __syncwarp();
+    if (pp.on) {
+        const int s = sh.slot[pp.owner];
+        if (s < 0 || !push_pair(ps, s, link, pp.j, pp.kind)) atomicOr(&sh.flags[pp.owner], 8);
+    }
+    __syncwarp();
+}
 
 template <int MODE> struct PolOf { typedef ExactPol type; };
 template <> struct PolOf<2> { typedef RobustPol type; };
@@ -265,9 +295,10 @@ template <int MODE> struct BoolMargin<MODE, float> { __device__ static float m()
 // distance pair (bits 1-4 per link), 8 pair list full (per configuration).
 template <int MODE, typename T>
 __device__ __forceinline__ void drain_bool(WarpShared<T> &sh, const DevRobot &rb, const ObsView<T> &ob, const Num<T> &nm,
-                                           int i, int nitems, const PairSink *ps, uint32_t flat_base) {
+                                           int i, int nitems, const PairSink *ps) {
     typedef typename PolOf<MODE>::type P;
     const int lane = threadIdx.x & 31;
+    uint32_t pe = 0u;
     if (lane < nitems) {
         const uint32_t e = sh.qb[lane];
         const int owner = (int)(e & 31u), j = (int)(e >> 5);
@@ -277,10 +308,14 @@ __device__ __forceinline__ void drain_bool(WarpShared<T> &sh, const DevRobot &rb
         const bool c = coll_box(pol, nm, sh.a[owner], sh.b[owner], LinkConst<T>::r(rb, i), LinkConst<T>::rn(rb, i), o);
         if (P::robust && pol.m < kDecide) {
             atomicOr(&sh.flags[owner], 2);
-            if (ps && !push_pair(ps, flat_base + (uint32_t)owner, i, j, 0)) atomicOr(&sh.flags[owner], 8);
+            pe = 0x80000000u | e;
         } else if (c) {
             atomicOr(&sh.flags[owner], 1);
         }
+    }
+    if (ps) {
+        sh.pend[lane] = pe;
+        if (__any_sync(0xffffffffu, pe != 0u)) flush_pending(sh, ps, i);
     }
 }
 
@@ -306,8 +341,9 @@ __device__ __forceinline__ T pair_distance(const DevRobot &rb, const V &ob, cons
 
 template <int MODE, typename T>
 __device__ __forceinline__ void drain_dist(WarpShared<T> &sh, const DevRobot &rb, const ObsView<T> &ob, const Num<T> &nm,
-                                           int i, int nitems, const PairSink *ps, uint32_t flat_base) {
+                                           int i, int nitems, const PairSink *ps) {
     const int lane = threadIdx.x & 31;
+    uint32_t pe = 0u;
     if (lane < nitems) {
         const uint32_t e = sh.qd[lane];
         const int owner = (int)(e & 31u), j = (int)(e >> 5);
@@ -315,13 +351,17 @@ __device__ __forceinline__ void drain_dist(WarpShared<T> &sh, const DevRobot &rb
         const T d = pair_distance<MODE, T>(rb, ob, nm, sh.a[owner], sh.b[owner], i, j, settled);
         if (!settled) {
             atomicOr(&sh.flags[owner], 4);
-            if (ps && !push_pair(ps, flat_base + (uint32_t)owner, i, j, 1)) atomicOr(&sh.flags[owner], 8);
+            pe = 0x80000000u | (1u << 16) | e;
         } else if (d == d) {   // the reference's std::min ignores NaN
             atomicMin(&sh.lmin[owner], Key<T>::of(d));
             if (d <= T(0)) atomicMin(&sh.hitj[owner], j);
         }
         __syncwarp(__activemask());
         if (d <= T(0) && settled && sh.hitj[owner] == j) sh.hitv[owner] = d;   // one entry per (owner, j)
+    }
+    if (ps) {
+        sh.pend[lane] = pe;
+        if (__any_sync(0xffffffffu, pe != 0u)) flush_pending(sh, ps, i);
     }
 }
 
@@ -349,7 +389,7 @@ template <typename T> __device__ __forceinline__ T gap2_bb(const T *lo, const T 
         (N) += __popc(m_);                                                             \
         __syncwarp();                                                                  \
         if ((N) >= 32) {                                                               \
-            DRAIN<MODE, T>(sh, rb, ob, nm, i, 32, ps, flat_base);                      \
+            DRAIN<MODE, T>(sh, rb, ob, nm, i, 32, ps);                                 \
             __syncwarp();                                                              \
             if (lane < (N) - 32) sh.Q[lane] = sh.Q[32 + lane];                         \
             (N) -= 32;                                                                 \
@@ -359,14 +399,14 @@ template <typename T> __device__ __forceinline__ T gap2_bb(const T *lo, const T 
 
 // Returns, per lane, kSettled, kPairs or kFull (always kSettled for the exact
 // forms); outputs of unsettled configurations are provisional.  With a pair
-// sink, lane k's configuration is number flat_base + k of the launch, and its
-// first settled hit (link, obstacle) goes to *hit_link / *hit_j.  Once a lane
-// has a settled hit it only looks for an earlier hit (lower obstacle index),
-// which is all the profile's first-hit semantics need.
+// sink, *slot receives the lane's record (-1: none) and *hit_link / *hit_j its
+// first settled hit (link, obstacle); the caller completes the record.  Once a
+// lane has a settled hit it only looks for an earlier hit (lower obstacle
+// index), which is all the profile's first-hit semantics need.
 template <int MODE, typename T>
 __device__ int warp_check(WarpShared<T> &sh, const DevRobot &rb, const ObsView<T> &ob, const float *q, bool active,
                           const Num<T> &nm, Want w, uint8_t *valid_out, double *dist_out, float *prof_out,
-                          const PairSink *ps = nullptr, uint32_t flat_base = 0, int *hit_link = nullptr,
+                          const PairSink *ps = nullptr, int *slot = nullptr, int *hit_link = nullptr,
                           int *hit_j = nullptr) {
     const unsigned full = 0xffffffffu;
     const int lane = threadIdx.x & 31;
@@ -382,6 +422,8 @@ __device__ int warp_check(WarpShared<T> &sh, const DevRobot &rb, const ObsView<T
     const int L = rb.D;
     const T dmargin = (MODE == 2) ? T(kBand) : LinkConst<T>::margin();
     sh.flags[lane] = 0;
+    sh.slot[lane] = -1;
+    sh.need[lane] = 0;
     for (int i = 0; i < L; ++i) {
         if (!__any_sync(full, need_b || need_d)) break;
         if (active) sw.point(rb, q, i + 1, B);
@@ -430,8 +472,8 @@ __device__ int warp_check(WarpShared<T> &sh, const DevRobot &rb, const ObsView<T
             RPM_PUSH_AND_DRAIN(qb, nb, qb, item, drain_bool);
             RPM_PUSH_AND_DRAIN(qd, nd, qd, item, drain_dist);
         }
-        if (nb > 0) drain_bool<MODE, T>(sh, rb, ob, nm, i, nb, ps, flat_base);
-        if (nd > 0) drain_dist<MODE, T>(sh, rb, ob, nm, i, nd, ps, flat_base);
+        if (nb > 0) drain_bool<MODE, T>(sh, rb, ob, nm, i, nb, ps);
+        if (nd > 0) drain_dist<MODE, T>(sh, rb, ob, nm, i, nd, ps);
         __syncwarp();
         // ---- fold this link's results into the lane's configuration
         const int fl = sh.flags[lane];
@@ -458,6 +500,7 @@ __device__ int warp_check(WarpShared<T> &sh, const DevRobot &rb, const ObsView<T
         __syncwarp();
         A[0] = B[0]; A[1] = B[1]; A[2] = B[2];
     }
+    if (slot) *slot = sh.slot[lane];
     if (!active) return kSettled;
     if (w.profile && hit >= 0)
         for (int k = hit + 1; k < L; ++k) prof_out[k] = 0.f;
@@ -468,7 +511,7 @@ __device__ int warp_check(WarpShared<T> &sh, const DevRobot &rb, const ObsView<T
     const bool bad_b = w.valid && !collided && unc_b;
     const bool bad_d = (w.dist || w.profile) && unc_d && (w.profile || hit < 0);
     if (!(bad_b || bad_d)) return kSettled;
-    return (ps && !(sh.flags[lane] & 8)) ? kPairs : kFull;
+    return (ps && sh.slot[lane] >= 0 && !(sh.flags[lane] & 8)) ? kPairs : kFull;
 }
 #endif
 

@@ -83,7 +83,6 @@ struct Scratch {
     size_t pcfg_cap = 0, ppair_cap = 0;
     uint64_t *pairs = nullptr;
     PairCfg *pcfgs = nullptr;
-    uint32_t *slot_of = nullptr;
     double *pskel = nullptr;
     PairAcc *pacc = nullptr;
     // [0] whole-configuration recheck count, [1] edge recheck overflow,

@@ -97,7 +97,6 @@ struct Seg {
     float *profile;          // nullable, [count][L]
     int64_t count;
     int64_t first_block;     // first CTA of this segment in the launch
-    int64_t flat0;           // index of its first configuration within the launch
     int32_t n, n_pad;
     // spatially sorted copy (warp-per-configuration kernels)
     const float *srt_f;      // [8][ns]: AABB, tol, original index | ground bit (as bits)

@@ -42,6 +42,8 @@ struct EdgeParams {
     int32_t *status;
     Num<double> nmd;
     Num<float> nmf;
+    PairSink ps;             // FP32 pass -> pair-level FP64 recheck (records: seg = k, config = edge)
+    int32_t wide_g;          // warp-per-check kernels: checks taken per warp
 };
 
 RPM_HD void edge_point(const float *a, const float *b, int D, float ratio, float *out) {
@@ -76,6 +78,22 @@ RPM_HD void edge_config(const float *a, const float *b, int D, int N, int k, flo
 }
 
 #ifdef __CUDACC__
+// A check the FP32 pass could not settle through the pair recheck: recheck it
+// whole in FP64, or, when that list is full, every check of its edge.
+__device__ __forceinline__ void edge_recheck_whole(const EdgeParams &P, int64_t e, int k) {
+    const uint32_t slot = atomicAdd(P.recheck_count, 1u);
+    if (slot < P.recheck_cap) P.recheck[slot] = ((uint64_t)e << 20) | (uint64_t)k;
+    else { atomicAdd(P.overflow, 1u); P.full[e] = 1; }
+}
+
+// Record the outcome of check k of edge e.
+template <int MODE>
+__device__ __forceinline__ void edge_outcome(const EdgeParams &P, int64_t e, int k, int st, int slot, uint8_t v) {
+    if (MODE == 2) complete_record(&P.ps, slot, st, k, e, -1, 0x7fffffff);
+    if (st == kFull) edge_recheck_whole(P, e, k);
+    else if (st == kSettled && v == 0) atomicMax(&P.kmax[e], k);
+}
+
 // Edge index of flat check 'idx': the last edge whose global offset <= idx.
 __device__ __forceinline__ int64_t edge_of_flat(const EdgeParams &P, int64_t idx) {
     int64_t lo = 0, hi = P.E - 1;
@@ -119,16 +137,10 @@ __device__ void edge_warps(const EdgeParams &P, const DevRobot &rb, const ObsVie
         __syncwarp();
         const Want w{true, false, false};
         uint8_t v = 1;
-        const bool settled = warp_check<MODE, T>(sh, rb, ob, qbuf + lane * kMaxDof, active, nm, w, &v, nullptr, nullptr) == kSettled;
-        if (active) {
-            if (!settled) {
-                const uint32_t slot = atomicAdd(P.recheck_count, 1u);
-                if (slot < P.recheck_cap) P.recheck[slot] = ((uint64_t)e << 20) | (uint64_t)k;
-                else { atomicAdd(P.overflow, 1u); P.full[e] = 1; }
-            } else if (v == 0) {
-                atomicMax(&P.kmax[e], k);
-            }
-        }
+        int slot = -1;
+        const int st = warp_check<MODE, T>(sh, rb, ob, qbuf + lane * kMaxDof, active, nm, w, &v, nullptr, nullptr,
+                                           MODE == 2 ? &P.ps : nullptr, &slot);
+        if (active) edge_outcome<MODE>(P, e, k, st, slot, v);
         __syncwarp();
     }
 }
@@ -138,6 +150,8 @@ __device__ void edge_warps(const EdgeParams &P, const DevRobot &rb, const ObsVie
 cudaError_t launch_edge_prep(const EdgeParams &p, cudaStream_t st);
 cudaError_t launch_edges(int mode, const EdgeParams &p, int grid, size_t smem, cudaStream_t st);
 cudaError_t launch_edges_fp32(const EdgeParams &p, int grid, size_t smem, cudaStream_t st);
-cudaError_t launch_edge_recheck_final(const EdgeParams &p, int grid, cudaStream_t st);
+cudaError_t launch_edge_recheck_final(const EdgeParams &p, int grid, bool pairs, cudaStream_t st);
+cudaError_t launch_edges_wide(int mode, const EdgeParams &p, int grid, size_t smem, cudaStream_t st);
+cudaError_t launch_edges_wide_fp32(const EdgeParams &p, int grid, size_t smem, cudaStream_t st);
 
 }  // namespace rpm

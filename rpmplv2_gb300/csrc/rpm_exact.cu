@@ -108,62 +108,127 @@ __global__ void __launch_bounds__(kThreads) k_recheck(const __grid_constant__ KP
 }
 
 // ---------------------------------------------------------- pair recheck --
-// 1. FP64 skeleton of each recorded configuration; its accumulators reset.
+// FP64 skeleton of one configuration; its accumulators reset.
+__device__ __forceinline__ void pair_skel_one(const DevRobot &rb, const float *q, double *out, PairAcc &a) {
+    SkelWalker<0> sw;
+    sw.begin();
+    for (int i = 0; i <= rb.D; ++i) sw.point(rb, q, i, out + 3 * i);
+    for (int i = 0; i < kMaxDof; ++i) {
+        a.lkey[i] = 0x7fffffff;
+        a.hkey[i] = ~0ull;
+    }
+    a.dkey = 0x7fffffffffffffffLL;
+    a.coll = 0;
+}
+
+// The reference's FP64 tree for one listed pair, folded into the record's
+// accumulators.
+__device__ __forceinline__ void pair_eval_one(const DevRobot &rb, const ObsView<double> &ob, const Num<double> &nmd,
+                                              const double *skel, int link, int j, int kind, PairAcc &a) {
+    const double *A = skel + 3 * link;
+    const double *B = A + 3;
+    double o[6];
+    ob.box(j, o);
+    ExactPol pol;
+    if (kind == 0) {
+        if (coll_box(pol, nmd, A, B, rb.radius_d[link], rb.rnew_d[link], o)) atomicOr(&a.coll, 1);
+    } else {
+        double d = capsule_box(pol, nmd, A, B, rb.radius_d[link], o).v;
+        if (d > ob.tol(j)) d = nmd.maxd;   // :367-368
+        if (d == d) {
+            const float f = (float)d;
+            atomicMin(&a.lkey[link], Key<float>::of(f));
+            atomicMin(&a.dkey, Key<double>::of(d));
+            if (d <= 0.0) atomicMin(&a.hkey[link], ((unsigned long long)j << 32) | __float_as_uint(f));
+        }
+    }
+}
+
+__device__ __forceinline__ bool decode_pair(const PairSink &ps, uint32_t k, uint32_t ncfg, uint32_t &slot, int &link,
+                                            int &j, int &kind) {
+    const uint64_t e = ps.pairs[k];
+    slot = (uint32_t)(e >> 17);
+    link = (int)((e >> 12) & 31u);
+    j = (int)((e >> 1) & 2047u);
+    kind = (int)(e & 1u);
+    return slot < ncfg && ps.cfgs[slot].status == kPairs;
+}
+
+// 1. FP64 skeleton of each recorded configuration.
 __global__ void k_pair_skel(const __grid_constant__ KParams P) {
     const uint32_t n = min(*P.ps.cfg_count, P.ps.cfg_cap);
     for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
         const PairCfg c = P.ps.cfgs[k];
+        if (c.status != kPairs) continue;
         const Seg &sg = P.segs[c.seg];
         const DevRobot &rb = *sg.robot;
-        SkelWalker<0> sw;
-        sw.begin();
-        double *out = P.ps.skel + (size_t)k * (kMaxDof + 1) * 3;
-        const float *q = sg.q + c.config * rb.D;
-        for (int i = 0; i <= rb.D; ++i) sw.point(rb, q, i, out + 3 * i);
-        PairAcc &a = P.ps.acc[k];
-        for (int i = 0; i < kMaxDof; ++i) {
-            a.lkey[i] = 0x7fffffff;
-            a.hkey[i] = ~0ull;
-        }
-        a.dkey = 0x7fffffffffffffffLL;
-        a.coll = 0;
+        pair_skel_one(rb, sg.q + c.config * rb.D, P.ps.skel + (size_t)k * (kMaxDof + 1) * 3, P.ps.acc[k]);
     }
 }
 
 // 2. One thread per listed pair: the reference's FP64 tree on the FP64
 // skeleton (pairs of configurations that ended settled, or that were routed
-// to the whole-configuration recheck, have no record and are skipped).
+// to the whole-configuration recheck, belong to records not completed with
+// kPairs and are skipped).
 __global__ void k_pair_eval(const __grid_constant__ KParams P) {
     const uint32_t n = min(*P.ps.pair_count, P.ps.pair_cap);
     const uint32_t ncfg = min(*P.ps.cfg_count, P.ps.cfg_cap);
     for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
-        const uint64_t e = P.ps.pairs[k];
-        const uint32_t flat = (uint32_t)(e >> 17);
-        const int link = (int)((e >> 12) & 31u), j = (int)((e >> 1) & 2047u), kind = (int)(e & 1u);
-        const uint32_t slot = P.ps.slot_of[flat];
-        if (slot >= ncfg || P.ps.cfgs[slot].flat != flat) continue;
+        uint32_t slot;
+        int link, j, kind;
+        if (!decode_pair(P.ps, k, ncfg, slot, link, j, kind)) continue;
         const Seg &sg = P.segs[P.ps.cfgs[slot].seg];
-        const DevRobot &rb = *sg.robot;
-        const double *A = P.ps.skel + (size_t)slot * (kMaxDof + 1) * 3 + 3 * link;
-        const double *B = A + 3;
         ObsView<double> ob{sg.obs_d, sg.obs_f + (size_t)kRowGround * sg.n_pad, sg.n, sg.n_pad};
-        double o[6];
-        ob.box(j, o);
-        ExactPol pol;
-        PairAcc &a = P.ps.acc[slot];
-        if (kind == 0) {
-            if (coll_box(pol, P.nmd, A, B, rb.radius_d[link], rb.rnew_d[link], o)) atomicOr(&a.coll, 1);
-        } else {
-            double d = capsule_box(pol, P.nmd, A, B, rb.radius_d[link], o).v;
-            if (d > ob.tol(j)) d = P.nmd.maxd;   // :367-368
-            if (d == d) {
-                const float f = (float)d;
-                atomicMin(&a.lkey[link], Key<float>::of(f));
-                atomicMin(&a.dkey, Key<double>::of(d));
-                if (d <= 0.0) atomicMin(&a.hkey[link], ((unsigned long long)j << 32) | __float_as_uint(f));
-            }
-        }
+        pair_eval_one(*sg.robot, ob, P.nmd, P.ps.skel + (size_t)slot * (kMaxDof + 1) * 3, link, j, kind, P.ps.acc[slot]);
     }
+}
+
+// Edge checks: the same three steps; a record is check k (seg) of an edge
+// (config), and an FP64 collision raises the edge's largest colliding k.
+__global__ void k_edge_pair_skel(const __grid_constant__ EdgeParams P) {
+    const uint32_t n = min(*P.ps.cfg_count, P.ps.cfg_cap);
+    const DevRobot &rb = *P.seg.robot;
+    const int D = rb.D;
+    for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+        const PairCfg c = P.ps.cfgs[k];
+        if (c.status != kPairs) continue;
+        const int64_t e = c.config;
+        float dist, q[kMaxDof];
+        const int N = edge_count(P.q1 + e * D, P.q2 + e * D, D, P.step, P.num_checks, dist);
+        edge_config(P.q1 + e * D, P.q2 + e * D, D, N, c.seg, dist, q);
+        pair_skel_one(rb, q, P.ps.skel + (size_t)k * (kMaxDof + 1) * 3, P.ps.acc[k]);
+    }
+}
+
+__global__ void k_edge_pair_eval(const __grid_constant__ EdgeParams P) {
+    const uint32_t n = min(*P.ps.pair_count, P.ps.pair_cap);
+    const uint32_t ncfg = min(*P.ps.cfg_count, P.ps.cfg_cap);
+    ObsView<double> ob{P.seg.obs_d, P.seg.obs_f + (size_t)kRowGround * P.seg.n_pad, P.seg.n, P.seg.n_pad};
+    for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+        uint32_t slot;
+        int link, j, kind;
+        if (!decode_pair(P.ps, k, ncfg, slot, link, j, kind)) continue;
+        pair_eval_one(*P.seg.robot, ob, P.nmd, P.ps.skel + (size_t)slot * (kMaxDof + 1) * 3, link, j, kind,
+                      P.ps.acc[slot]);
+    }
+}
+
+__global__ void k_edge_pair_fold(const __grid_constant__ EdgeParams P) {
+    const uint32_t n = min(*P.ps.cfg_count, P.ps.cfg_cap);
+    for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+        const PairCfg c = P.ps.cfgs[k];
+        if (c.status == kPairs && P.ps.acc[k].coll) atomicMax(&P.kmax[c.config], c.seg);
+    }
+}
+
+// Warp-per-check edge pass (rpm_wide.cuh).
+template <int MODE>
+__global__ void __launch_bounds__(kWideThreads, MODE == 0 ? 1 : 2) k_edges_wide(const __grid_constant__ EdgeParams P) {
+    extern __shared__ __align__(128) unsigned char smem[];
+    __shared__ uint64_t bar;
+    __shared__ uint32_t wq[kWideWarps][64];
+    bulk_init(&bar);
+    edge_wide_body<MODE>(P, smem, &bar, wq);
 }
 
 // 3. Fold per recorded configuration in the reference's link order: the
@@ -174,6 +239,7 @@ __global__ void k_pair_fold(const __grid_constant__ KParams P) {
     const uint32_t n = min(*P.ps.cfg_count, P.ps.cfg_cap);
     for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
         const PairCfg c = P.ps.cfgs[k];
+        if (c.status != kPairs) continue;
         const Seg &sg = P.segs[c.seg];
         const PairAcc &a = P.ps.acc[k];
         const int L = sg.robot->D;
@@ -393,7 +459,26 @@ cudaError_t launch_edges(int mode, const EdgeParams &p, int grid, size_t smem, c
     return cudaGetLastError();
 }
 
-cudaError_t launch_edge_recheck_final(const EdgeParams &p, int grid, cudaStream_t st) {
+cudaError_t launch_edges_wide(int mode, const EdgeParams &p, int grid, size_t smem, cudaStream_t st) {
+    if (mode == RPM_PREC_FP32_RECHECK) return launch_edges_wide_fp32(p, grid, smem, st);
+    if (mode == RPM_PREC_FP64) {
+        static bool attr = false;
+        if (!attr) { cudaFuncSetAttribute(k_edges_wide<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024); attr = true; }
+        k_edges_wide<0><<<grid, kWideThreads, smem, st>>>(p);
+    } else {
+        static bool attr = false;
+        if (!attr) { cudaFuncSetAttribute(k_edges_wide<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024); attr = true; }
+        k_edges_wide<1><<<grid, kWideThreads, smem, st>>>(p);
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_edge_recheck_final(const EdgeParams &p, int grid, bool pairs, cudaStream_t st) {
+    if (pairs) {
+        k_edge_pair_skel<<<grid, kThreads, 0, st>>>(p);
+        k_edge_pair_eval<<<grid * 2, kThreads, 0, st>>>(p);
+        k_edge_pair_fold<<<grid, kThreads, 0, st>>>(p);
+    }
     k_edge_recheck<<<grid, kThreads, 0, st>>>(p);
     k_edge_full<<<grid, kThreads, 0, st>>>(p);
     const unsigned fb = (unsigned)((p.E + 255) / 256);

@@ -35,13 +35,15 @@ __global__ void __launch_bounds__(kThreads) k_check_fp32(const __grid_constant__
     ObsView<float> ob{rows, rows + (size_t)kRowGround * sg.n_pad, sg.n, sg.n_pad};
     const Want w{sg.valid != nullptr, sg.dist != nullptr, sg.profile != nullptr};
     const int D = rb.D;
-    int hl = -1, hj = 0x7fffffff;
+    int hl = -1, hj = 0x7fffffff, slot = -1;
     const int st = warp_check<2, float>(wsh[threadIdx.x >> 5], rb, ob, sg.q + c * D, active, P.nmf, w,
                                         (w.valid && active) ? sg.valid + c : nullptr,
                                         (w.dist && active) ? sg.dist + c : nullptr,
-                                        (w.profile && active) ? sg.profile + c * D : nullptr, &P.ps,
-                                        (uint32_t)(sg.flat0 + warp0), &hl, &hj);
-    if (active) finish_config(&P.ps, st, (uint32_t)(sg.flat0 + c), s, c, hl, hj, P.recheck, P.recheck_count);
+                                        (w.profile && active) ? sg.profile + c * D : nullptr, &P.ps, &slot, &hl, &hj);
+    if (active) {
+        complete_record(&P.ps, slot, st, s, c, hl, hj);
+        if (st == kFull) recheck_whole(P, s, c);
+    }
 }
 
 // FP32 pass of the warp-per-configuration form; unsettled configurations go
@@ -63,7 +65,23 @@ cudaError_t launch_check_wide_fp32(const KParams &p, int64_t blocks, size_t smem
     return cudaGetLastError();
 }
 
-// FP32 pass of the edge checks (unsettled checks go to k_edge_recheck).
+// FP32 pass of the warp-per-check edge form.
+__global__ void __launch_bounds__(kWideThreads, 2) k_edges_wide_fp32(const __grid_constant__ EdgeParams P) {
+    extern __shared__ __align__(128) unsigned char smem[];
+    __shared__ uint64_t bar;
+    __shared__ uint32_t wq[kWideWarps][64];
+    bulk_init(&bar);
+    edge_wide_body<2>(P, smem, &bar, wq);
+}
+
+cudaError_t launch_edges_wide_fp32(const EdgeParams &p, int grid, size_t smem, cudaStream_t st) {
+    static bool attr = false;
+    if (!attr) { cudaFuncSetAttribute(k_edges_wide_fp32, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024); attr = true; }
+    k_edges_wide_fp32<<<grid, kWideThreads, smem, st>>>(p);
+    return cudaGetLastError();
+}
+
+// FP32 pass of the edge checks (unsettled checks go to the pair recheck or k_edge_recheck).
 __global__ void __launch_bounds__(kThreads) k_edges_fp32(const __grid_constant__ EdgeParams P) {
     extern __shared__ __align__(128) unsigned char smem[];
     __shared__ uint64_t bar;

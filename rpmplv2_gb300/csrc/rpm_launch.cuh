@@ -24,6 +24,15 @@ struct KParams {
     PairSink ps;                // FP32 pass -> pair-level FP64 recheck
 };
 
+#ifdef __CUDACC__
+// A configuration the FP32 pass could not settle through the pair recheck:
+// recompute it whole in FP64 (the list holds every configuration of a launch).
+__device__ __forceinline__ void recheck_whole(const KParams &P, int seg, int64_t c) {
+    const uint32_t r = atomicAdd(P.recheck_count, 1u);
+    P.recheck[r] = ((uint64_t)seg << 40) | (uint64_t)c;
+}
+#endif
+
 // Host helpers shared by the C ABI translation units (rpm_api.cu).
 int build_dev_robot(const rpm_robot_desc &d, DevRobot &r);   // RPM_OK or an error code (message set)
 int set_error(int code, const char *msg);                     // records the thread's error string

@@ -25,6 +25,7 @@
 #include <type_traits>
 
 #include "rpm_check.cuh"
+#include "rpm_edges.cuh"
 #include "rpm_launch.cuh"
 
 namespace rpm {
@@ -50,6 +51,8 @@ constexpr int kWideMidObstacles = 40;
 constexpr int64_t kWideMidBatch = 8192;
 constexpr int kWideSmallObstacles = 8;
 constexpr int64_t kWideSmallBatch = 512;
+// Edge batches (rpm_api.cu): warp-per-check for scenes of at least this many obstacles.
+constexpr int kWideEdgeObstacles = 100;
 
 // Sorted copy of one scene version: slot s holds original obstacle idx[s].
 // Static obstacles come first, then moving ones, then ground ones, each group
@@ -104,12 +107,28 @@ __device__ __forceinline__ void wide_pop32(uint32_t *q, int &nq) {
 }
 
 // Where unsettled pairs go: the sink (may be null), this configuration's
-// index in the launch, and the sticky list-full flag.
+// record (-1 until its first unsettled pair) and the sticky list-full flag.
 struct WideSink {
     const PairSink *ps;
-    uint32_t flat;
+    int slot;
     bool full;
 };
+
+// After a drain (all lanes): list this configuration's unsettled pairs,
+// allocating its record on the first one.
+__device__ __forceinline__ void wide_flush(WideSink &sk, bool pend, int link, int j, int kind) {
+    const unsigned full = 0xffffffffu;
+    if (!sk.ps || !__any_sync(full, pend)) return;
+    if (sk.slot < 0 && !sk.full) {
+        int s = -1;
+        if ((threadIdx.x & 31) == 0) s = alloc_record(sk.ps);
+        sk.slot = __shfl_sync(full, s, 0);
+        sk.full = sk.slot < 0;
+    }
+    bool f = false;
+    if (pend) f = sk.slot < 0 || !push_pair(sk.ps, sk.slot, link, j, kind);
+    sk.full = sk.full || __any_sync(full, f);
+}
 
 template <int MODE, typename T>
 __device__ __forceinline__ void wide_drain_bool(const uint32_t *q, int nitems, const SortedView<T> &ob, const Num<T> &nm,
@@ -117,23 +136,21 @@ __device__ __forceinline__ void wide_drain_bool(const uint32_t *q, int nitems, c
                                                 bool &unc) {
     typedef typename PolOf<MODE>::type P;
     const int lane = threadIdx.x & 31;
-    bool c = false, u = false, f = false;
+    bool c = false, u = false;
+    int j = 0;
     if (lane < nitems) {
         const int s = (int)q[lane];
         T o[6];
         ob.box(s, o);
         P pol;
         const bool cc = coll_box(pol, nm, A, B, r, rn, o);
-        if (P::robust && pol.m < kDecide) {
-            u = true;
-            if (sk.ps) f = !push_pair(sk.ps, sk.flat, i, (int)(ob.idx[s] & ~kGroundBit), 0);
-        } else {
-            c = cc;
-        }
+        j = (int)(ob.idx[s] & ~kGroundBit);
+        if (P::robust && pol.m < kDecide) u = true;
+        else c = cc;
     }
     hit = hit || __any_sync(0xffffffffu, c);
     unc = unc || __any_sync(0xffffffffu, u);
-    sk.full = sk.full || __any_sync(0xffffffffu, f);
+    wide_flush(sk, u, i, j, 0);
 }
 
 template <int MODE, typename T>
@@ -146,21 +163,21 @@ __device__ __forceinline__ void wide_drain_dist(const uint32_t *q, int nitems, c
     K kk = Key<T>::of(nm.maxd);
     int jj = 0x7fffffff;
     T vv = T(0);
-    bool u = false, f = false;
+    bool u = false;
+    int j = 0;
     if (lane < nitems) {
         const int s = (int)q[lane];
         bool settled;
         const T d = pair_distance<MODE, T>(rb, ob, nm, A, B, i, s, settled);
-        const int j = (int)(ob.idx[s] & ~kGroundBit);
+        j = (int)(ob.idx[s] & ~kGroundBit);
         if (!settled) {
             u = true;
-            if (sk.ps) f = !push_pair(sk.ps, sk.flat, i, j, 1);
         } else if (d == d) {   // the reference's std::min ignores NaN
             kk = Key<T>::of(d);
             if (d <= T(0)) { jj = j; vv = d; }
         }
     }
-    sk.full = sk.full || __any_sync(full, f);
+    wide_flush(sk, u, i, j, 1);
 #pragma unroll
     for (int off = 16; off > 0; off >>= 1) {
         const K ok = __shfl_xor_sync(full, kk, off);
@@ -364,7 +381,7 @@ __device__ int wide_config(uint32_t *q, T *gl, const DevRobot &rb, const SortedV
     const bool bad_b = w.valid && !collided && unc_b;
     const bool bad_d = (w.dist || w.profile) && unc_d && (w.profile || hit < 0);
     if (!(bad_b || bad_d)) return kSettled;
-    return (sk.ps && !sk.full) ? kPairs : kFull;
+    return (sk.ps && sk.slot >= 0 && !sk.full) ? kPairs : kFull;
 }
 
 // Shared-memory layout of the wide kernels: robot, sorted rows, index row,
@@ -386,14 +403,10 @@ struct WideLayout {
     }
 };
 
-// Body of k_check_wide<MODE>: CTA = kWideWarps warps, each owning G = P.wide_g
-// consecutive configurations of one segment.
+// Stage the robot and the sorted scene of 'sg' (all threads wait).
 template <int MODE>
-__device__ __forceinline__ void wide_kernel_body(const KParams &P, unsigned char *smem, uint64_t *bar,
-                                                 uint32_t (*wq)[64], int s) {
-    typedef typename std::conditional<MODE == 0, double, float>::type T;
-    const Seg &sg = P.segs[s];
-    const WideLayout L = WideLayout::of(MODE == 0 ? RPM_PREC_FP64 : RPM_PREC_FP32_REF, sg.ns, sg.nb);
+__device__ __forceinline__ bool wide_stage(const Seg &sg, const WideLayout &L, unsigned char *smem, uint64_t *bar,
+                                           int32_t *status) {
     if (threadIdx.x == 0) {
         const uint32_t rb = (uint32_t)sizeof(DevRobot);
         const uint32_t rows = L.idx - L.rows, idx = L.blk - L.idx, blk = L.pts - L.blk;
@@ -404,7 +417,18 @@ __device__ __forceinline__ void wide_kernel_body(const KParams &P, unsigned char
         bulk_copy(bar, smem + L.idx, sg.srt_f + (size_t)7 * sg.ns, idx);
         bulk_copy(bar, smem + L.blk, sg.blk, blk);
     }
-    if (!bulk_wait(bar, 0, P.status)) return;
+    return bulk_wait(bar, 0, status);
+}
+
+// Body of k_check_wide<MODE>: CTA = kWideWarps warps, each owning G = P.wide_g
+// consecutive configurations of one segment.
+template <int MODE>
+__device__ __forceinline__ void wide_kernel_body(const KParams &P, unsigned char *smem, uint64_t *bar,
+                                                 uint32_t (*wq)[64], int s) {
+    typedef typename std::conditional<MODE == 0, double, float>::type T;
+    const Seg &sg = P.segs[s];
+    const WideLayout L = WideLayout::of(MODE == 0 ? RPM_PREC_FP64 : RPM_PREC_FP32_REF, sg.ns, sg.nb);
+    if (!wide_stage<MODE>(sg, L, smem, bar, P.status)) return;
     const DevRobot &rb = *reinterpret_cast<const DevRobot *>(smem);
     SortedView<T> ob{reinterpret_cast<const T *>(smem + L.rows), reinterpret_cast<const uint32_t *>(smem + L.idx),
                      reinterpret_cast<const float *>(smem + L.blk), sg.ns, sg.nb};
@@ -431,12 +455,84 @@ __device__ __forceinline__ void wide_kernel_body(const KParams &P, unsigned char
     for (int g = 0; g < G; ++g) {
         const int64_t c = c0 + g;
         if (c >= sg.count) break;
-        WideSink sk{MODE == 2 ? &P.ps : nullptr, (uint32_t)(sg.flat0 + c), false};
+        WideSink sk{MODE == 2 ? &P.ps : nullptr, -1, false};
         int hl, hj;
         const int st = wide_config<MODE, T>(wq[warp], gl, rb, ob, pts + g * (D + 1) * 3, nm, w,
                                             w.valid ? sg.valid + c : nullptr, w.dist ? sg.dist + c : nullptr,
                                             w.profile ? sg.profile + c * D : nullptr, sk, hl, hj);
-        if (MODE == 2 && lane == 0) finish_config(&P.ps, st, sk.flat, s, c, hl, hj, P.recheck, P.recheck_count);
+        if (MODE == 2 && lane == 0) {
+            complete_record(&P.ps, sk.slot, st, s, c, hl, hj);
+            if (st == kFull) recheck_whole(P, s, c);
+        }
+    }
+}
+
+// Body of k_edges_wide<MODE>: persistent warps take G consecutive flat checks
+// at a time (edge-major, k descending), run their forward kinematics lane =
+// check, then check them one at a time with the whole warp, skipping every
+// check at or below its edge's largest colliding k.
+template <int MODE>
+__device__ __forceinline__ void edge_wide_body(const EdgeParams &P, unsigned char *smem, uint64_t *bar,
+                                               uint32_t (*wq)[64]) {
+    typedef typename std::conditional<MODE == 0, double, float>::type T;
+    const Seg &sg = P.seg;
+    const WideLayout L = WideLayout::of(MODE == 0 ? RPM_PREC_FP64 : RPM_PREC_FP32_REF, sg.ns, sg.nb);
+    if (!wide_stage<MODE>(sg, L, smem, bar, P.status)) return;
+    const DevRobot &rb = *reinterpret_cast<const DevRobot *>(smem);
+    SortedView<T> ob{reinterpret_cast<const T *>(smem + L.rows), reinterpret_cast<const uint32_t *>(smem + L.idx),
+                     reinterpret_cast<const float *>(smem + L.blk), sg.ns, sg.nb};
+    const unsigned full = 0xffffffffu;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int G = P.wide_g;
+    const int D = rb.D;
+    T *pts = reinterpret_cast<T *>(smem + L.pts + warp * kWidePtsBytes);
+    T *gl = reinterpret_cast<T *>(smem + L.gl + warp * L.gl_warp);
+    Num<T> nm;
+    if (MODE == 0) { nm.eq = (T)P.nmd.eq; nm.maxd = (T)P.nmd.maxd; }
+    else { nm.eq = (T)P.nmf.eq; nm.maxd = (T)P.nmf.maxd; }
+    const int64_t total = P.bprefix[(P.E + kEdgeScanBlock - 1) / kEdgeScanBlock];
+    for (;;) {
+        unsigned long long base = 0;
+        if (lane == 0) base = atomicAdd(P.work, (unsigned long long)G);
+        base = __shfl_sync(full, base, 0);
+        if ((int64_t)base >= total) break;
+        int64_t e = 0;
+        int k = 0;
+        bool act = false;
+        if (lane < G && (int64_t)base + lane < total) {
+            const int64_t idx = (int64_t)base + lane;
+            e = edge_of_flat(P, idx);
+            const int64_t first = P.bprefix[e / kEdgeScanBlock] + P.local[e];
+            const int n = P.n_e[e];
+            k = n - (int)(idx - first);
+            act = k > *(volatile int32_t *)&P.kmax[e];
+            if (act) {
+                float dist, q[kMaxDof];
+                edge_count(P.q1 + e * D, P.q2 + e * D, D, P.step, P.num_checks, dist);
+                edge_config(P.q1 + e * D, P.q2 + e * D, D, n, k, dist, q);
+                SkelWalker<MODE> sw;
+                sw.begin();
+                T *p = pts + lane * (D + 1) * 3;
+                for (int t = 0; t <= D; ++t) sw.point(rb, q, t, p + 3 * t);
+            }
+        }
+        __syncwarp();
+        const unsigned am = __ballot_sync(full, act);
+        for (int g = 0; g < G; ++g) {
+            if (!((am >> g) & 1u)) continue;
+            const int64_t eg = __shfl_sync(full, e, g);
+            const int kg = __shfl_sync(full, k, g);
+            int km = 0;
+            if (lane == 0) km = *(volatile int32_t *)&P.kmax[eg];
+            if (kg <= __shfl_sync(full, km, 0)) continue;   // a check nearer q2 already collides
+            WideSink sk{MODE == 2 ? &P.ps : nullptr, -1, false};
+            uint8_t v = 1;
+            int hl, hj;
+            const int st = wide_config<MODE, T>(wq[warp], gl, rb, ob, pts + g * (D + 1) * 3, nm, Want{true, false, false},
+                                                &v, nullptr, nullptr, sk, hl, hj);
+            if (lane == 0) edge_outcome<MODE>(P, eg, kg, st, sk.slot, v);
+            __syncwarp();
+        }
     }
 }
 #endif

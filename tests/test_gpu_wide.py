@@ -1,6 +1,7 @@
-"""GPU parity of the warp-per-configuration layout (spatially sorted obstacles,
-block culling, nearest-first distance search) against the oracle, and its
-equality with the lane-per-configuration layout.
+"""GPU parity of the warp-per-configuration layout (obstacles in spatially
+sorted leaves, leaf culling, nearest-first distance bands, pair-level FP64
+recheck) against the oracle, and its equality with the lane-per-configuration
+layout.
 
 Bars as in test_gpu_parity: fp64 and fp32_ref bit-equal to ref64 / ref32,
 fp32_recheck with 0 isValid flips and distances within 1e-5 m of ref64.
@@ -193,3 +194,49 @@ def test_auto_batch_mixes_layouts(engine, layout, prec, oprec):
         _assert_oracle(robot, scene, q, (v.cpu().numpy(), d.cpu().numpy(), p.cpu().numpy()), prec, oprec)
     for it in items:
         engine.destroy_scene(it[0])
+
+
+@pytest.mark.parametrize("prec,oprec", FORMS)
+def test_warp_edges_match_oracle_and_lane(engine, layout, prec, oprec):
+    """isValid(q1, q2) batches with uneven discretisation: the warp-per-check
+    pass gives the reference's validity and check counts, as the lane pass does."""
+    robot, scene, q1, q2, step = scenes.spatial10_edge_workload(4000, seed=57)
+    sid = engine.create_scene(engine.upload_robot(robot), scene)
+    outs = {}
+    for lay in ("warp", "lane"):
+        layout(lay)
+        v = torch.zeros(q1.shape[0], dtype=torch.uint8, device="cuda")
+        k = torch.zeros(q1.shape[0], dtype=torch.int32, device="cuda")
+        engine.check_edges(sid, torch.from_numpy(q1).cuda(), torch.from_numpy(q2).cuda(), v, k, step=float(step),
+                           precision=prec)
+        engine.sync()
+        outs[lay] = (v.cpu().numpy(), k.cpu().numpy())
+    engine.destroy_scene(sid)
+    rv, rk = O.check_edges(robot, scene, q1, q2, step=step, prec=oprec)
+    assert np.array_equal(outs["warp"][0], rv) and np.array_equal(outs["warp"][1], rk)
+    assert np.array_equal(outs["lane"][0], rv) and np.array_equal(outs["lane"][1], rk)
+
+
+def test_warp_edges_big_scene_fixed_count(engine, layout):
+    """22 links against 1000 boxes with the fixed NUM_INTERPOLATION_VALIDITY_CHECKS
+    discretisation (step <= 0), FP32 + FP64 recheck, with CUDA-graph replay."""
+    robot = robots.spatial(22, radius=0.03)
+    scene = _big_scene(58, 1000, 0.01, 0.06, 2.0)
+    rng = np.random.default_rng(59)
+    q1 = scenes.uniform_configs(rng, 600, 22)
+    q2 = (q1 + rng.uniform(-0.3, 0.3, q1.shape)).astype(np.float32)
+    sid = engine.create_scene(engine.upload_robot(robot), scene)
+    layout("warp")
+    engine.set_graphs(True)
+    try:
+        for _ in range(2):   # capture, then replay
+            v = torch.zeros(600, dtype=torch.uint8, device="cuda")
+            k = torch.zeros(600, dtype=torch.int32, device="cuda")
+            engine.check_edges(sid, torch.from_numpy(q1).cuda(), torch.from_numpy(q2).cuda(), v, k, step=0.0,
+                               num_checks=10, precision="fp32_recheck")
+            engine.sync()
+            rv, rk = O.check_edges(robot, scene, q1, q2, step=0.0, num_checks=10, prec="ref64")
+            assert np.array_equal(v.cpu().numpy(), rv) and np.array_equal(k.cpu().numpy(), rk)
+    finally:
+        engine.set_graphs(False)
+        engine.destroy_scene(sid)
