@@ -331,13 +331,14 @@ SceneRec *find_scene(rpm_ctx *ctx, int id) {
 // lane-per-configuration: every link needs its own nearest-first search
 // there, which keeps the warp's drains half empty.  (Thresholds measured on
 // GB300 over 10-22 links, 10-1000 obstacles and 256-65,536 configurations.)
-static bool use_warp_layout(const rpm_ctx *ctx, const SegReq &r, int64_t total) {
+static bool use_warp_layout(const rpm_ctx *ctx, const SegReq &r, int64_t total, int prec) {
     if (ctx->layout == RPM_LAYOUT_LANE) return false;
     if (ctx->layout == RPM_LAYOUT_WARP) return true;
     const int n = r.scene->n;
     if (n >= kWideMinObstacles) return !(r.profile != nullptr && total > kWideMaxProfileBatch);
     if (n >= kWideMidObstacles) return total <= kWideMidBatch;
-    return n >= kWideSmallObstacles && total <= kWideSmallBatch;
+    const int64_t small = (prec == RPM_PREC_FP64) ? kWideSmallBatch : kWideSmallBatch32;
+    return n >= kWideSmallObstacles && r.profile == nullptr && total <= small;
 }
 
 // Queue checks of up to kMaxSegs segments as one launch on 'st' (more
@@ -361,7 +362,7 @@ int enqueue_segments(rpm_ctx *ctx, int prec, const std::vector<SegReq> &reqs, cu
     for (int wide = 0; wide < 2; ++wide) {
         std::vector<const SegReq *> cur;
         for (const SegReq &r : reqs) {
-            if (r.count <= 0 || use_warp_layout(ctx, r, total) != (wide == 1)) continue;
+            if (r.count <= 0 || use_warp_layout(ctx, r, total, prec) != (wide == 1)) continue;
             cur.push_back(&r);
             if ((int)cur.size() == kMaxSegs) { chunks.push_back({wide == 1, cur}); cur.clear(); }
         }

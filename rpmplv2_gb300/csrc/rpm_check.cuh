@@ -154,8 +154,7 @@ __device__ void config_exact_warp(const DevRobot &rb, const ObsView<T> &ob, cons
                 if (ground_skip && ob.is_ground(j)) continue;
                 T o[6];
                 ob.box(j, o);
-                ExactPol pol;
-                mine = coll_box(pol, nm, A, B, r, rn, o);
+                mine = coll_box_call<T, ExactPol>(nm, A, B, r, rn, o).v;
             }
             if (__any_sync(full, mine)) { collided = true; need_b = false; }
         }
@@ -171,8 +170,7 @@ __device__ void config_exact_warp(const DevRobot &rb, const ObsView<T> &ob, cons
                 thr = smin(thr, tol);
                 const T s = thr + r + nm.eq + LinkConst<T>::margin();
                 if (s > T(0) && gap2(A, B, o) > s * s) continue;
-                ExactPol pol;
-                T d = capsule_box(pol, nm, A, B, r, o).v;
+                T d = capsule_box_call<T, ExactPol>(nm, A, B, r, o).v;
                 if (d > tol) d = nm.maxd;
                 lb = smin(lb, d);
                 if (d <= T(0)) { hj = j; hv = d; break; }
@@ -304,9 +302,9 @@ __device__ __forceinline__ void drain_bool(WarpShared<T> &sh, const DevRobot &rb
         const int owner = (int)(e & 31u), j = (int)(e >> 5);
         T o[6];
         ob.box(j, o);
-        P pol;
-        const bool c = coll_box(pol, nm, sh.a[owner], sh.b[owner], LinkConst<T>::r(rb, i), LinkConst<T>::rn(rb, i), o);
-        if (P::robust && pol.m < kDecide) {
+        const RB rr = coll_box_call<T, P>(nm, sh.a[owner], sh.b[owner], LinkConst<T>::r(rb, i), LinkConst<T>::rn(rb, i), o);
+        const bool c = rr.v;
+        if (P::robust && rr.m < kDecide) {
             atomicOr(&sh.flags[owner], 2);
             pe = 0x80000000u | e;
         } else if (c) {
@@ -325,17 +323,18 @@ __device__ __forceinline__ T pair_distance(const DevRobot &rb, const V &ob, cons
     typedef typename PolOf<MODE>::type P;
     T o[6];
     ob.box(j, o);
-    P pol;
-    Val<T> dv = capsule_box(pol, nm, A, B, LinkConst<T>::r(rb, i), o);
+    const ValM<T> dv = capsule_box_call<T, P>(nm, A, B, LinkConst<T>::r(rb, i), o);
     const T tol = ob.tol(j);
     T d = dv.v;
+    float m = dv.m;
     if (P::robust) {
+        // the clamp to MAX_DISTANCE and the hit test are decisions on d too
         const float band = dv.ia * (kDecide / kBand);
-        RPM_NOTE(pol, fabsf((float)(d - tol)) * band);
-        if (d != T(0)) RPM_NOTE(pol, fabsf((float)(d > tol ? nm.maxd : d)) * band);
+        m = fminf(m, fabsf((float)(d - tol)) * band);
+        if (d != T(0)) m = fminf(m, fabsf((float)(d > tol ? nm.maxd : d)) * band);
     }
     if (d > tol) d = nm.maxd;   // :367-368
-    settled = !P::robust || pol.m >= kDecide;
+    settled = !P::robust || m >= kDecide;
     return d;
 }
 

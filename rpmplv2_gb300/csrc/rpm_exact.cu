@@ -80,7 +80,7 @@ template <int MODE>
 __global__ void __launch_bounds__(kWideThreads, MODE == 0 ? 1 : 2) k_check_wide(const __grid_constant__ KParams P) {
     extern __shared__ __align__(128) unsigned char smem[];
     __shared__ uint64_t bar;
-    __shared__ uint32_t wq[kWideWarps][64];
+    __shared__ uint32_t wq[kWideWarps][128];
     const int s = find_seg(P);
     bulk_init(&bar);
     wide_kernel_body<MODE>(P, smem, &bar, wq, s);
@@ -129,11 +129,10 @@ __device__ __forceinline__ void pair_eval_one(const DevRobot &rb, const ObsView<
     const double *B = A + 3;
     double o[6];
     ob.box(j, o);
-    ExactPol pol;
     if (kind == 0) {
-        if (coll_box(pol, nmd, A, B, rb.radius_d[link], rb.rnew_d[link], o)) atomicOr(&a.coll, 1);
+        if (coll_box_call<double, ExactPol>(nmd, A, B, rb.radius_d[link], rb.rnew_d[link], o).v) atomicOr(&a.coll, 1);
     } else {
-        double d = capsule_box(pol, nmd, A, B, rb.radius_d[link], o).v;
+        double d = capsule_box_call<double, ExactPol>(nmd, A, B, rb.radius_d[link], o).v;
         if (d > ob.tol(j)) d = nmd.maxd;   // :367-368
         if (d == d) {
             const float f = (float)d;
@@ -226,7 +225,7 @@ template <int MODE>
 __global__ void __launch_bounds__(kWideThreads, MODE == 0 ? 1 : 2) k_edges_wide(const __grid_constant__ EdgeParams P) {
     extern __shared__ __align__(128) unsigned char smem[];
     __shared__ uint64_t bar;
-    __shared__ uint32_t wq[kWideWarps][64];
+    __shared__ uint32_t wq[kWideWarps][128];
     bulk_init(&bar);
     edge_wide_body<MODE>(P, smem, &bar, wq);
 }

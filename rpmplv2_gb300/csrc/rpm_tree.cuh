@@ -577,6 +577,30 @@ RPM_HD Val<T> capsule_box(P &pol, const Num<T> &nm, const T *A, const T *B, T ra
     return Val<T>{d - radius, 1.f};
 }
 
+// Out-of-line instances of the two trees per (T, policy): every drain of a
+// kernel calls the same copy, so the instruction cache holds each tree once.
+// The policy's smallest margin travels back by value.
+template <typename T> struct ValM {
+    T v;
+    float ia, m;
+};
+
+template <typename T, typename P>
+__host__ __device__ __noinline__ RB coll_box_call(const Num<T> nm, const T *A, const T *B, T radius, T r_new,
+                                                  const T *o) {
+    P pol;
+    const bool v = coll_box(pol, nm, A, B, radius, r_new, o);
+    return RB{v, pol.m};
+}
+
+template <typename T, typename P>
+__host__ __device__ __noinline__ ValM<T> capsule_box_call(const Num<T> nm, const T *A, const T *B, T radius,
+                                                          const T *o) {
+    P pol;
+    const Val<T> r = capsule_box(pol, nm, A, B, radius, o);
+    return ValM<T>{r.v, r.ia, pol.m};
+}
+
 // Lower bound of the segment-box distance: the gap between the box and the
 // segment's own bounding box.  Any reference distance of the pair is at least
 // this bound minus EQUALITY_THRESHOLD (the snap of :237, :338).

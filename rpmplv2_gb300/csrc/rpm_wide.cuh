@@ -44,13 +44,15 @@ static_assert(kMaxLeaves * kLeaf >= kMaxObstacles + 3 * (kLeaf - 1), "sorted lay
 // Automatic layout (rpm_api.cu): warp-per-configuration for scenes of at
 // least kWideMinObstacles obstacles (profiles: batches up to
 // kWideMaxProfileBatch), of kWideMidObstacles with batches up to
-// kWideMidBatch, and of kWideSmallObstacles with batches up to kWideSmallBatch.
+// kWideMidBatch, and of kWideSmallObstacles with batches up to kWideSmallBatch
+// (FP64) or kWideSmallBatch32 (FP32 forms) without profiles.
 constexpr int kWideMinObstacles = 150;
 constexpr int64_t kWideMaxProfileBatch = 16384;
 constexpr int kWideMidObstacles = 40;
 constexpr int64_t kWideMidBatch = 8192;
 constexpr int kWideSmallObstacles = 8;
 constexpr int64_t kWideSmallBatch = 512;
+constexpr int64_t kWideSmallBatch32 = 4096;
 // Edge batches (rpm_api.cu): warp-per-check for scenes of at least this many obstacles.
 constexpr int kWideEdgeObstacles = 100;
 
@@ -114,8 +116,8 @@ struct WideSink {
     bool full;
 };
 
-// After a drain (all lanes): list this configuration's unsettled pairs,
-// allocating its record on the first one.
+// After a drain (all lanes): list this configuration's unsettled pairs
+// (each lane its own link and obstacle), allocating its record on the first.
 __device__ __forceinline__ void wide_flush(WideSink &sk, bool pend, int link, int j, int kind) {
     const unsigned full = 0xffffffffu;
     if (!sk.ps || !__any_sync(full, pend)) return;
@@ -142,11 +144,10 @@ __device__ __forceinline__ void wide_drain_bool(const uint32_t *q, int nitems, c
         const int s = (int)q[lane];
         T o[6];
         ob.box(s, o);
-        P pol;
-        const bool cc = coll_box(pol, nm, A, B, r, rn, o);
+        const RB rr = coll_box_call<T, P>(nm, A, B, r, rn, o);
         j = (int)(ob.idx[s] & ~kGroundBit);
-        if (P::robust && pol.m < kDecide) u = true;
-        else c = cc;
+        if (P::robust && rr.m < kDecide) u = true;
+        else c = rr.v;
     }
     hit = hit || __any_sync(0xffffffffu, c);
     unc = unc || __any_sync(0xffffffffu, u);
@@ -189,6 +190,238 @@ __device__ __forceinline__ void wide_drain_dist(const uint32_t *q, int nitems, c
     lkey = kk < lkey ? kk : lkey;
     if (jj < hj) { hj = jj; hv = vv; }
     unc = unc || __any_sync(full, u);
+}
+
+// ---------------------------------------------------------------------------
+// isValid and / or computeDistance without the per-link profile.  Neither
+// output depends on the order in which links are visited (isValid is an OR,
+// the distance a minimum over all pairs with any hit giving 0), so the pairs
+// of all links share two queues and every drain is full:
+//   seeds   : for each link, the obstacle with the smallest gap in its
+//             nearest leaf; the L seed pairs are one drain, and their settled
+//             minimum is the first threshold;
+//   main    : for each link, one leaf cull against both thresholds (r*sqrt(2)
+//             for isValid; best + r + EQUALITY_THRESHOLD + margin, bounded by
+//             the leaf's tolerances, for the distance), obstacle tests of up to
+//             four leaves at a time, and (link, slot) items pushed to the
+//             isValid and distance queues, each drained 32 at a time; best
+//             tightens with every drain.
+// Queue items: link << 16 | slot.
+template <int MODE, typename T>
+__device__ __forceinline__ void np_drain_bool(const uint32_t *q, int nitems, const DevRobot &rb,
+                                              const SortedView<T> &ob, const Num<T> &nm, const T *pts, WideSink &sk,
+                                              bool &hit, bool &unc) {
+    typedef typename PolOf<MODE>::type P;
+    const int lane = threadIdx.x & 31;
+    bool c = false, u = false;
+    int j = 0, link = 0;
+    if (lane < nitems) {
+        const uint32_t it = q[lane];
+        link = (int)(it >> 16);
+        const int s = (int)(it & 0xffffu);
+        T o[6];
+        ob.box(s, o);
+        const RB rr = coll_box_call<T, P>(nm, pts + 3 * link, pts + 3 * link + 3, LinkConst<T>::r(rb, link),
+                                          LinkConst<T>::rn(rb, link), o);
+        j = (int)(ob.idx[s] & ~kGroundBit);
+        if (P::robust && rr.m < kDecide) u = true;
+        else c = rr.v;
+    }
+    hit = hit || __any_sync(0xffffffffu, c);
+    unc = unc || __any_sync(0xffffffffu, u);
+    wide_flush(sk, u, link, j, 0);
+}
+
+template <int MODE, typename T>
+__device__ __forceinline__ void np_drain_dist(const uint32_t *q, int nitems, const DevRobot &rb,
+                                              const SortedView<T> &ob, const Num<T> &nm, const T *pts, WideSink &sk,
+                                              T &best, int &hit_link, int &hit_j, bool &unc) {
+    typedef typename Key<T>::type K;
+    const unsigned full = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    K kk = Key<T>::of(nm.maxd);
+    int hl = 0x7fffffff, j = 0, link = 0;
+    bool u = false;
+    if (lane < nitems) {
+        const uint32_t it = q[lane];
+        link = (int)(it >> 16);
+        const int s = (int)(it & 0xffffu);
+        bool settled;
+        const T d = pair_distance<MODE, T>(rb, ob, nm, pts + 3 * link, pts + 3 * link + 3, link, s, settled);
+        j = (int)(ob.idx[s] & ~kGroundBit);
+        if (!settled) u = true;
+        else if (d == d) {   // the reference's std::min ignores NaN
+            kk = Key<T>::of(d);
+            if (d <= T(0)) hl = link;
+        }
+    }
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+        const K ok = __shfl_xor_sync(full, kk, off);
+        kk = ok < kk ? ok : kk;
+    }
+    best = smin(best, Key<T>::value(kk));
+    const unsigned hm = __ballot_sync(full, hl != 0x7fffffff);
+    if (hm && hit_link < 0) {
+        const int src = __ffs(hm) - 1;
+        hit_link = __shfl_sync(full, hl, src);
+        hit_j = __shfl_sync(full, j, src);
+    }
+    unc = unc || __any_sync(full, u);
+    wide_flush(sk, u, link, j, 1);
+}
+
+template <int MODE, typename T>
+__device__ int wide_config_np(uint32_t *qb, uint32_t *qd, const DevRobot &rb, const SortedView<T> &ob, const T *pts,
+                              const Num<T> &nm, Want w, uint8_t *valid_out, double *dist_out, WideSink &sk,
+                              int &hit_link, int &hit_j) {
+    const unsigned full = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    const T inf = T(1) / T(0);
+    const int L = rb.D;
+    const T dmargin = (MODE == 2) ? T(kBand) : LinkConst<T>::margin();
+    bool need_b = w.valid, need_d = w.dist;
+    bool collided = false, unc_b = false, unc_d = false;
+    T best = nm.maxd;
+    hit_link = -1;
+    hit_j = 0x7fffffff;
+    // ------------------------------------------------------------- seeds
+    if (need_d) {
+        uint32_t seed = 0xffffffffu;   // lane i: the seed item of link i
+        for (int i = 0; i < L; ++i) {
+            T lo[3], hi[3];
+#pragma unroll
+            for (int k = 0; k < 3; ++k) {
+                const T a = pts[3 * i + k], b = pts[3 * i + 3 + k];
+                lo[k] = a < b ? a : b;
+                hi[k] = a < b ? b : a;
+            }
+            const bool gskip = i < rb.ground_included;
+            T gb = inf;
+            int lb = 0x7fffffff;
+            for (int l = lane; l < ob.nb; l += 32) {
+                if (gskip && ob.ground_leaf(l)) continue;
+                T o[6];
+                ob.leaf(l, o);
+                const T g = gap2_bb(lo, hi, o);
+                if (g < gb || lb == 0x7fffffff) { gb = g; lb = l; }
+            }
+#pragma unroll
+            for (int off = 16; off > 0; off >>= 1) {
+                const T og = __shfl_xor_sync(full, gb, off);
+                const int ol = __shfl_xor_sync(full, lb, off);
+                if (og < gb || (!(gb < og) && ol < lb)) { gb = og; lb = ol; }
+            }
+            if (lb == 0x7fffffff) continue;
+            // the obstacle of that leaf with the smallest gap (lanes 0-7 of each octet agree)
+            const int s = lb * kLeaf + (lane & (kLeaf - 1));
+            const uint32_t id = ob.idx[s];
+            T g = inf;
+            if (id != kPadIdx && !(gskip && (id & kGroundBit))) {
+                T o[6];
+                ob.box(s, o);
+                g = gap2_bb(lo, hi, o);
+            }
+            int sb = (g < inf) ? s : 0x7fffffff;
+#pragma unroll
+            for (int off = kLeaf / 2; off > 0; off >>= 1) {
+                const T og = __shfl_xor_sync(full, g, off);
+                const int os = __shfl_xor_sync(full, sb, off);
+                if (og < g || (!(g < og) && os < sb)) { g = og; sb = os; }
+            }
+            if (lane == i && sb != 0x7fffffff) seed = ((uint32_t)i << 16) | (uint32_t)sb;
+        }
+        const bool has = seed != 0xffffffffu;
+        const unsigned m = __ballot_sync(full, has);
+        if (has) qd[__popc(m & ((1u << lane) - 1u))] = seed;
+        __syncwarp();
+        if (m) np_drain_dist<MODE, T>(qd, __popc(m), rb, ob, nm, pts, sk, best, hit_link, hit_j, unc_d);
+        __syncwarp();
+        if (hit_link >= 0) need_d = false;   // a settled hit: the distance is 0
+    }
+    // -------------------------------------------------------------- main
+    int nqb = 0, nqd = 0;
+    for (int i = 0; i < L && (need_b || need_d); ++i) {
+        T lo[3], hi[3];
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            const T a = pts[3 * i + k], b = pts[3 * i + 3 + k];
+            lo[k] = a < b ? a : b;
+            hi[k] = a < b ? b : a;
+        }
+        const T r = LinkConst<T>::r(rb, i);
+        const bool gskip = i < rb.ground_included;
+        const T tb = r * T(1.41421356237309515) + BoolMargin<MODE, T>::m();
+        const T tb2 = tb * tb;
+        const T slack = r + nm.eq + dmargin;
+        for (int l0 = 0; l0 < ob.nb && (need_b || need_d); l0 += 32) {
+            const int l = l0 + lane;
+            bool cl = false;
+            if (l < ob.nb && !(gskip && ob.ground_leaf(l))) {
+                T o[6];
+                ob.leaf(l, o);
+                const T g = gap2_bb(lo, hi, o);
+                const bool cb = need_b && !(g > tb2);
+                bool cd = false;
+                if (need_d) {
+                    const T smax = smin(best, (T)ob.blk[l * kBlkRec + 6]) + slack;
+                    const T slo = smin(best, (T)ob.blk[l * kBlkRec + 7]) + slack;
+                    cd = !(slo > T(0) && g > smax * smax);
+                }
+                cl = cb || cd;
+            }
+            unsigned ml = __ballot_sync(full, cl);
+            while (ml != 0u && (need_b || need_d)) {
+                const int bit = nth_bit(ml, lane >> 3);
+                ml = drop4(ml);
+                bool pb = false, pd = false;
+                uint32_t item = 0u;
+                if (bit >= 0) {
+                    const int s = (l0 + bit) * kLeaf + (lane & (kLeaf - 1));
+                    const uint32_t id = ob.idx[s];
+                    item = ((uint32_t)i << 16) | (uint32_t)s;
+                    if (id != kPadIdx && !(gskip && (id & kGroundBit))) {
+                        T o[6];
+                        ob.box(s, o);
+                        const T g2 = gap2_bb(lo, hi, o);
+                        pb = need_b && !(g2 > tb2);
+                        if (need_d) {
+                            const T sv = smin(best, ob.tol(s)) + slack;
+                            pd = !(sv > T(0) && g2 > sv * sv);
+                        }
+                    }
+                }
+                if (need_b) {
+                    wide_push<MODE, T>(qb, nqb, pb, item);
+                    if (nqb >= 32) {
+                        np_drain_bool<MODE, T>(qb, 32, rb, ob, nm, pts, sk, collided, unc_b);
+                        wide_pop32(qb, nqb);
+                        if (collided) { need_b = false; nqb = 0; }
+                    }
+                }
+                if (need_d) {
+                    wide_push<MODE, T>(qd, nqd, pd, item);
+                    if (nqd >= 32) {
+                        np_drain_dist<MODE, T>(qd, 32, rb, ob, nm, pts, sk, best, hit_link, hit_j, unc_d);
+                        wide_pop32(qd, nqd);
+                        if (hit_link >= 0) { need_d = false; nqd = 0; }
+                    }
+                }
+            }
+        }
+    }
+    if (need_b && nqb > 0) np_drain_bool<MODE, T>(qb, nqb, rb, ob, nm, pts, sk, collided, unc_b);
+    if (need_d && nqd > 0) np_drain_dist<MODE, T>(qd, nqd, rb, ob, nm, pts, sk, best, hit_link, hit_j, unc_d);
+    __syncwarp();
+    const bool hit = hit_link >= 0;
+    if (lane == 0) {
+        if (w.valid) *valid_out = collided ? 0 : 1;
+        if (w.dist) *dist_out = hit ? 0.0 : (double)best;
+    }
+    const bool bad_b = w.valid && !collided && unc_b;
+    const bool bad_d = w.dist && unc_d && !hit;
+    if (!(bad_b || bad_d)) return kSettled;
+    return (sk.ps && sk.slot >= 0 && !sk.full) ? kPairs : kFull;
 }
 
 // One configuration, the whole warp.  pts = skeleton points [(D+1)][3];
@@ -424,7 +657,7 @@ __device__ __forceinline__ bool wide_stage(const Seg &sg, const WideLayout &L, u
 // consecutive configurations of one segment.
 template <int MODE>
 __device__ __forceinline__ void wide_kernel_body(const KParams &P, unsigned char *smem, uint64_t *bar,
-                                                 uint32_t (*wq)[64], int s) {
+                                                 uint32_t (*wq)[128], int s) {
     typedef typename std::conditional<MODE == 0, double, float>::type T;
     const Seg &sg = P.segs[s];
     const WideLayout L = WideLayout::of(MODE == 0 ? RPM_PREC_FP64 : RPM_PREC_FP32_REF, sg.ns, sg.nb);
@@ -457,9 +690,13 @@ __device__ __forceinline__ void wide_kernel_body(const KParams &P, unsigned char
         if (c >= sg.count) break;
         WideSink sk{MODE == 2 ? &P.ps : nullptr, -1, false};
         int hl, hj;
-        const int st = wide_config<MODE, T>(wq[warp], gl, rb, ob, pts + g * (D + 1) * 3, nm, w,
-                                            w.valid ? sg.valid + c : nullptr, w.dist ? sg.dist + c : nullptr,
-                                            w.profile ? sg.profile + c * D : nullptr, sk, hl, hj);
+        const T *pc = pts + g * (D + 1) * 3;
+        const int st = w.profile
+                           ? wide_config<MODE, T>(wq[warp], gl, rb, ob, pc, nm, w, w.valid ? sg.valid + c : nullptr,
+                                                  w.dist ? sg.dist + c : nullptr, sg.profile + c * D, sk, hl, hj)
+                           : wide_config_np<MODE, T>(wq[warp], wq[warp] + 64, rb, ob, pc, nm, w,
+                                                     w.valid ? sg.valid + c : nullptr, w.dist ? sg.dist + c : nullptr,
+                                                     sk, hl, hj);
         if (MODE == 2 && lane == 0) {
             complete_record(&P.ps, sk.slot, st, s, c, hl, hj);
             if (st == kFull) recheck_whole(P, s, c);
@@ -473,7 +710,7 @@ __device__ __forceinline__ void wide_kernel_body(const KParams &P, unsigned char
 // check at or below its edge's largest colliding k.
 template <int MODE>
 __device__ __forceinline__ void edge_wide_body(const EdgeParams &P, unsigned char *smem, uint64_t *bar,
-                                               uint32_t (*wq)[64]) {
+                                               uint32_t (*wq)[128]) {
     typedef typename std::conditional<MODE == 0, double, float>::type T;
     const Seg &sg = P.seg;
     const WideLayout L = WideLayout::of(MODE == 0 ? RPM_PREC_FP64 : RPM_PREC_FP32_REF, sg.ns, sg.nb);
@@ -486,7 +723,6 @@ __device__ __forceinline__ void edge_wide_body(const EdgeParams &P, unsigned cha
     const int G = P.wide_g;
     const int D = rb.D;
     T *pts = reinterpret_cast<T *>(smem + L.pts + warp * kWidePtsBytes);
-    T *gl = reinterpret_cast<T *>(smem + L.gl + warp * L.gl_warp);
     Num<T> nm;
     if (MODE == 0) { nm.eq = (T)P.nmd.eq; nm.maxd = (T)P.nmd.maxd; }
     else { nm.eq = (T)P.nmf.eq; nm.maxd = (T)P.nmf.maxd; }
@@ -528,8 +764,8 @@ __device__ __forceinline__ void edge_wide_body(const EdgeParams &P, unsigned cha
             WideSink sk{MODE == 2 ? &P.ps : nullptr, -1, false};
             uint8_t v = 1;
             int hl, hj;
-            const int st = wide_config<MODE, T>(wq[warp], gl, rb, ob, pts + g * (D + 1) * 3, nm, Want{true, false, false},
-                                                &v, nullptr, nullptr, sk, hl, hj);
+            const int st = wide_config_np<MODE, T>(wq[warp], wq[warp] + 64, rb, ob, pts + g * (D + 1) * 3, nm,
+                                                   Want{true, false, false}, &v, nullptr, sk, hl, hj);
             if (lane == 0) edge_outcome<MODE>(P, eg, kg, st, sk.slot, v);
             __syncwarp();
         }

@@ -191,20 +191,24 @@ def serving_workload(engine, seed=4, n_scenes=64, rate=20000.0, duration=0.5, ma
     rng = np.random.default_rng(seed)
     robots = {name: make_robot(name) for name in SERVE_ROBOTS}
     rids = {name: engine.upload_robot(r) for name, r in robots.items()}
-    scene_ids, scene_robot, motions = [], [], []
+    scene_ids, scene_robot, scene_n, motions = [], [], [], []
     for s in range(n_scenes):
         name = SERVE_ROBOTS[rng.integers(len(SERVE_ROBOTS))]
         n = int(round(math.exp(rng.uniform(math.log(10), math.log(1000)))))
         sc = _scene_for(robots[name], rng, n)
+        moving = []
+        if rng.uniform() < dynamic_frac:
+            first = 1 if name == "xarm6" else 0
+            moving = rng.choice(np.arange(first, sc.n), size=min(n_dynamic, sc.n - first), replace=False)
+            sc.flags[moving] |= _scenes.RPM_OBS_DYNAMIC   # label "dynamic_obstacle"
         sid = engine.create_scene(rids[name], sc)
         scene_ids.append(sid)
         scene_robot.append(name)
-        if rng.uniform() < dynamic_frac:
-            first = 1 if name == "xarm6" else 0
-            for j in rng.choice(np.arange(first, sc.n), size=min(n_dynamic, sc.n - first), replace=False):
-                u = rng.normal(size=3)
-                u = u / np.linalg.norm(u) * rng.uniform(0, max_speed)
-                motions.append(Motion(sid, int(j), (ctypes.c_float * 3)(*u)))
+        scene_n.append(sc.n)
+        for j in moving:
+            u = rng.normal(size=3)
+            u = u / np.linalg.norm(u) * rng.uniform(0, max_speed)
+            motions.append(Motion(sid, int(j), (ctypes.c_float * 3)(*u)))
     dofs = sorted({robots[n].num_dofs for n in SERVE_ROBOTS})
     qpool = {d: pinned((pool, d), np.float32) for d in dofs}
     q2pool = {}
@@ -243,7 +247,7 @@ def serving_workload(engine, seed=4, n_scenes=64, rate=20000.0, duration=0.5, ma
             reqs.append(configs_request(scene_ids[s], q, v, dd))
             keep += [v, dd]
             meta.append(("valid" if kind == 0 else "distance", size, size, s, q, None, v, dd))
-    return {"scene_ids": scene_ids, "scene_robot": scene_robot, "robots": robots, "requests": reqs,
+    return {"scene_ids": scene_ids, "scene_robot": scene_robot, "scene_n": scene_n, "robots": robots, "requests": reqs,
             "arrivals": arrivals, "meta": meta, "motions": motions, "pools": (qpool, q2pool, shared), "keep": keep}
 
 
