@@ -80,10 +80,10 @@ template <int MODE>
 __global__ void __launch_bounds__(kWideThreads, MODE == 0 ? 1 : 2) k_check_wide(const __grid_constant__ KParams P) {
     extern __shared__ __align__(128) unsigned char smem[];
     __shared__ uint64_t bar;
-    __shared__ uint32_t wq[kWideWarps][128];
+    __shared__ MultiState<typename std::conditional<MODE == 0, double, float>::type> ms[kWideWarps];
     const int s = find_seg(P);
     bulk_init(&bar);
-    wide_kernel_body<MODE>(P, smem, &bar, wq, s);
+    wide_kernel_body<MODE>(P, smem, &bar, ms, s);
 }
 
 // FP64 recomputation of the configurations listed by the FP32 pass, one warp
@@ -225,9 +225,9 @@ template <int MODE>
 __global__ void __launch_bounds__(kWideThreads, MODE == 0 ? 1 : 2) k_edges_wide(const __grid_constant__ EdgeParams P) {
     extern __shared__ __align__(128) unsigned char smem[];
     __shared__ uint64_t bar;
-    __shared__ uint32_t wq[kWideWarps][128];
+    __shared__ MultiState<typename std::conditional<MODE == 0, double, float>::type> ms[kWideWarps];
     bulk_init(&bar);
-    edge_wide_body<MODE>(P, smem, &bar, wq);
+    edge_wide_body<MODE>(P, smem, &bar, ms);
 }
 
 // 3. Fold per recorded configuration in the reference's link order: the

@@ -51,11 +51,11 @@ __global__ void __launch_bounds__(kThreads) k_check_fp32(const __grid_constant__
 __global__ void __launch_bounds__(kWideThreads, 2) k_check_wide_fp32(const __grid_constant__ KParams P) {
     extern __shared__ __align__(128) unsigned char smem[];
     __shared__ uint64_t bar;
-    __shared__ uint32_t wq[kWideWarps][128];
+    __shared__ MultiState<float> ms[kWideWarps];
     int s = 0;
     while (s + 1 < P.nseg && P.segs[s + 1].first_block <= (int64_t)blockIdx.x) ++s;
     bulk_init(&bar);
-    wide_kernel_body<2>(P, smem, &bar, wq, s);
+    wide_kernel_body<2>(P, smem, &bar, ms, s);
 }
 
 cudaError_t launch_check_wide_fp32(const KParams &p, int64_t blocks, size_t smem, cudaStream_t st) {
@@ -69,9 +69,9 @@ cudaError_t launch_check_wide_fp32(const KParams &p, int64_t blocks, size_t smem
 __global__ void __launch_bounds__(kWideThreads, 2) k_edges_wide_fp32(const __grid_constant__ EdgeParams P) {
     extern __shared__ __align__(128) unsigned char smem[];
     __shared__ uint64_t bar;
-    __shared__ uint32_t wq[kWideWarps][128];
+    __shared__ MultiState<float> ms[kWideWarps];
     bulk_init(&bar);
-    edge_wide_body<2>(P, smem, &bar, wq);
+    edge_wide_body<2>(P, smem, &bar, ms);
 }
 
 cudaError_t launch_edges_wide_fp32(const EdgeParams &p, int grid, size_t smem, cudaStream_t st) {

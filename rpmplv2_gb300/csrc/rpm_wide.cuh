@@ -193,235 +193,290 @@ __device__ __forceinline__ void wide_drain_dist(const uint32_t *q, int nitems, c
 }
 
 // ---------------------------------------------------------------------------
-// isValid and / or computeDistance without the per-link profile.  Neither
-// output depends on the order in which links are visited (isValid is an OR,
-// the distance a minimum over all pairs with any hit giving 0), so the pairs
-// of all links share two queues and every drain is full:
-//   seeds   : for each link, the obstacle with the smallest gap in its
-//             nearest leaf; the L seed pairs are one drain, and their settled
-//             minimum is the first threshold;
-//   main    : for each link, one leaf cull against both thresholds (r*sqrt(2)
-//             for isValid; best + r + EQUALITY_THRESHOLD + margin, bounded by
-//             the leaf's tolerances, for the distance), obstacle tests of up to
-//             four leaves at a time, and (link, slot) items pushed to the
-//             isValid and distance queues, each drained 32 at a time; best
-//             tightens with every drain.
-// Queue items: link << 16 | slot.
-template <int MODE, typename T>
-__device__ __forceinline__ void np_drain_bool(const uint32_t *q, int nitems, const DevRobot &rb,
-                                              const SortedView<T> &ob, const Num<T> &nm, const T *pts, WideSink &sk,
-                                              bool &hit, bool &unc) {
-    typedef typename PolOf<MODE>::type P;
-    const int lane = threadIdx.x & 31;
-    bool c = false, u = false;
-    int j = 0, link = 0;
-    if (lane < nitems) {
-        const uint32_t it = q[lane];
-        link = (int)(it >> 16);
-        const int s = (int)(it & 0xffffu);
-        T o[6];
-        ob.box(s, o);
-        const RB rr = coll_box_call<T, P>(nm, pts + 3 * link, pts + 3 * link + 3, LinkConst<T>::r(rb, link),
-                                          LinkConst<T>::rn(rb, link), o);
-        j = (int)(ob.idx[s] & ~kGroundBit);
-        if (P::robust && rr.m < kDecide) u = true;
-        else c = rr.v;
-    }
-    hit = hit || __any_sync(0xffffffffu, c);
-    unc = unc || __any_sync(0xffffffffu, u);
-    wide_flush(sk, u, link, j, 0);
-}
+// isValid and / or computeDistance without the per-link profile, for the G
+// configurations of a warp at once.  Neither output depends on the order in
+// which links and pairs are visited (isValid is an OR, the distance a minimum
+// over all pairs with any hit giving 0), so seeds and candidate pairs of all
+// G configurations share two queues, and drains stay full even when each
+// configuration has few candidates:
+//   seeds : for each (configuration, link), the obstacle with the smallest
+//           gap in the link's nearest leaf; their settled distances give each
+//           configuration its first threshold;
+//   main  : for each (configuration, link), one leaf cull against both
+//           thresholds (r*sqrt(2) for isValid; best + r + EQUALITY_THRESHOLD
+//           + margin, bounded by the leaf's tolerances, for the distance),
+//           obstacle tests of up to four leaves at a time, and items pushed to
+//           the isValid and distance queues, each drained 32 at a time;
+//           configurations already settled are skipped.  Per
+// configuration the warp keeps, in shared memory, its flags, the ordered key
+// of its settled minimum, a settled hit and its pair-recheck record; drains
+// update them with shared atomics.  Items: g << 21 | link << 16 | slot.
+template <typename T> struct MultiState {
+    int flags[32];                        // bit0 collision, bit1 / bit2 unsettled isValid / distance pair, bit3 list full
+    typename Key<T>::type best[32];       // ordered key of the settled minimum
+    int hit_link[32];                     // a link with a settled hit (-1: none)
+    int hit_j[32];
+    int slot[32];                         // pair-recheck record (-1: none yet)
+    int need[32];
+    uint32_t pend[32];                    // drain lane's unsettled pair: 1 << 31 | kind << 30 | j << 10 | link << 5 | g
+    uint32_t qb[64], qd[64];
+};
 
 template <int MODE, typename T>
-__device__ __forceinline__ void np_drain_dist(const uint32_t *q, int nitems, const DevRobot &rb,
-                                              const SortedView<T> &ob, const Num<T> &nm, const T *pts, WideSink &sk,
-                                              T &best, int &hit_link, int &hit_j, bool &unc) {
-    typedef typename Key<T>::type K;
+__device__ __forceinline__ void multi_flush(MultiState<T> &ms, const PairSink *ps) {
     const unsigned full = 0xffffffffu;
     const int lane = threadIdx.x & 31;
-    K kk = Key<T>::of(nm.maxd);
-    int hl = 0x7fffffff, j = 0, link = 0;
-    bool u = false;
-    if (lane < nitems) {
-        const uint32_t it = q[lane];
-        link = (int)(it >> 16);
-        const int s = (int)(it & 0xffffu);
-        bool settled;
-        const T d = pair_distance<MODE, T>(rb, ob, nm, pts + 3 * link, pts + 3 * link + 3, link, s, settled);
-        j = (int)(ob.idx[s] & ~kGroundBit);
-        if (!settled) u = true;
-        else if (d == d) {   // the reference's std::min ignores NaN
-            kk = Key<T>::of(d);
-            if (d <= T(0)) hl = link;
+    const uint32_t pe = ms.pend[lane];
+    if (!__any_sync(full, pe != 0u)) return;
+    const int g = (int)(pe & 31u);
+    if (pe) ms.need[g] = 1;
+    __syncwarp();
+    if (ms.need[lane]) {
+        ms.need[lane] = 0;
+        if (ms.slot[lane] < 0 && !(ms.flags[lane] & 8)) {
+            const int sl = alloc_record(ps);
+            if (sl >= 0) ms.slot[lane] = sl;
+            else atomicOr(&ms.flags[lane], 8);
         }
     }
-#pragma unroll
-    for (int off = 16; off > 0; off >>= 1) {
-        const K ok = __shfl_xor_sync(full, kk, off);
-        kk = ok < kk ? ok : kk;
+    __syncwarp();
+    if (pe) {
+        const int sl = ms.slot[g];
+        const int link = (int)((pe >> 5) & 31u), j = (int)((pe >> 10) & 2047u), kind = (int)((pe >> 30) & 1u);
+        if (sl < 0 || !push_pair(ps, sl, link, j, kind)) atomicOr(&ms.flags[g], 8);
     }
-    best = smin(best, Key<T>::value(kk));
-    const unsigned hm = __ballot_sync(full, hl != 0x7fffffff);
-    if (hm && hit_link < 0) {
-        const int src = __ffs(hm) - 1;
-        hit_link = __shfl_sync(full, hl, src);
-        hit_j = __shfl_sync(full, j, src);
-    }
-    unc = unc || __any_sync(full, u);
-    wide_flush(sk, u, link, j, 1);
+    __syncwarp();
 }
 
 template <int MODE, typename T>
-__device__ int wide_config_np(uint32_t *qb, uint32_t *qd, const DevRobot &rb, const SortedView<T> &ob, const T *pts,
-                              const Num<T> &nm, Want w, uint8_t *valid_out, double *dist_out, WideSink &sk,
-                              int &hit_link, int &hit_j) {
+__device__ __forceinline__ void multi_drain_bool(MultiState<T> &ms, int nitems, const DevRobot &rb,
+                                                 const SortedView<T> &ob, const Num<T> &nm, const T *pts, int stride,
+                                                 const PairSink *ps) {
+    typedef typename PolOf<MODE>::type P;
+    const int lane = threadIdx.x & 31;
+    uint32_t pe = 0u;
+    if (lane < nitems) {
+        const uint32_t it = ms.qb[lane];
+        const int g = (int)(it >> 21), link = (int)((it >> 16) & 31u), s = (int)(it & 0xffffu);
+        const T *A = pts + g * stride + 3 * link;
+        T o[6];
+        ob.box(s, o);
+        const RB rr = coll_box_call<T, P>(nm, A, A + 3, LinkConst<T>::r(rb, link), LinkConst<T>::rn(rb, link), o);
+        if (P::robust && rr.m < kDecide) {
+            atomicOr(&ms.flags[g], 2);
+            pe = 0x80000000u | ((ob.idx[s] & 2047u) << 10) | ((uint32_t)link << 5) | (uint32_t)g;
+        } else if (rr.v) {
+            atomicOr(&ms.flags[g], 1);
+        }
+    }
+    __syncwarp();
+    if (ps) {
+        ms.pend[lane] = pe;
+        __syncwarp();
+        multi_flush<MODE, T>(ms, ps);
+    }
+}
+
+template <int MODE, typename T>
+__device__ __forceinline__ void multi_drain_dist(MultiState<T> &ms, int nitems, const DevRobot &rb,
+                                                 const SortedView<T> &ob, const Num<T> &nm, const T *pts, int stride,
+                                                 const PairSink *ps) {
+    const int lane = threadIdx.x & 31;
+    uint32_t pe = 0u;
+    if (lane < nitems) {
+        const uint32_t it = ms.qd[lane];
+        const int g = (int)(it >> 21), link = (int)((it >> 16) & 31u), s = (int)(it & 0xffffu);
+        const T *A = pts + g * stride + 3 * link;
+        bool settled;
+        const T d = pair_distance<MODE, T>(rb, ob, nm, A, A + 3, link, s, settled);
+        const uint32_t j = ob.idx[s] & ~kGroundBit;
+        if (!settled) {
+            atomicOr(&ms.flags[g], 4);
+            pe = 0x80000000u | 0x40000000u | ((j & 2047u) << 10) | ((uint32_t)link << 5) | (uint32_t)g;
+        } else if (d == d) {   // the reference's std::min ignores NaN
+            atomicMin(&ms.best[g], Key<T>::of(d));
+            if (d <= T(0) && atomicCAS(&ms.hit_link[g], -1, link) == -1) ms.hit_j[g] = (int)j;
+        }
+    }
+    __syncwarp();
+    if (ps) {
+        ms.pend[lane] = pe;
+        __syncwarp();
+        multi_flush<MODE, T>(ms, ps);
+    }
+}
+
+// Checks configurations 0..G-1 (skeletons at pts + g * stride) for isValid
+// and / or the distance; 'live' marks the configurations to check.  On return
+// lane g < G holds configuration g's results: *valid (0 / 1), *dist, the
+// status (kSettled / kPairs / kFull), its record and first settled hit.
+template <int MODE, typename T>
+__device__ void wide_multi_np(MultiState<T> &ms, const DevRobot &rb, const SortedView<T> &ob, const T *pts,
+                              int stride, int G, unsigned live, const Num<T> &nm, Want w, const PairSink *ps,
+                              uint8_t &valid, double &dist, int &status, int &slot, int &hit_link, int &hit_j) {
+    typedef typename Key<T>::type K;
     const unsigned full = 0xffffffffu;
     const int lane = threadIdx.x & 31;
     const T inf = T(1) / T(0);
     const int L = rb.D;
     const T dmargin = (MODE == 2) ? T(kBand) : LinkConst<T>::margin();
-    bool need_b = w.valid, need_d = w.dist;
-    bool collided = false, unc_b = false, unc_d = false;
-    T best = nm.maxd;
-    hit_link = -1;
-    hit_j = 0x7fffffff;
+    ms.flags[lane] = 0;
+    ms.best[lane] = Key<T>::of(nm.maxd);
+    ms.hit_link[lane] = -1;
+    ms.hit_j[lane] = 0x7fffffff;
+    ms.slot[lane] = -1;
+    ms.need[lane] = 0;
+    ms.pend[lane] = 0u;
+    __syncwarp();
+    int nqb = 0, nqd = 0;
     // ------------------------------------------------------------- seeds
-    if (need_d) {
-        uint32_t seed = 0xffffffffu;   // lane i: the seed item of link i
+    if (w.dist) {
+        for (int g = 0; g < G; ++g) {
+            if (!((live >> g) & 1u)) continue;
+            const T *pg = pts + g * stride;
+            for (int i = 0; i < L; ++i) {
+                T lo[3], hi[3];
+#pragma unroll
+                for (int k = 0; k < 3; ++k) {
+                    const T a = pg[3 * i + k], b = pg[3 * i + 3 + k];
+                    lo[k] = a < b ? a : b;
+                    hi[k] = a < b ? b : a;
+                }
+                const bool gskip = i < rb.ground_included;
+                T gb = inf;
+                int lb = 0x7fffffff;
+                for (int l = lane; l < ob.nb; l += 32) {
+                    if (gskip && ob.ground_leaf(l)) continue;
+                    T o[6];
+                    ob.leaf(l, o);
+                    const T gg = gap2_bb(lo, hi, o);
+                    if (gg < gb || lb == 0x7fffffff) { gb = gg; lb = l; }
+                }
+#pragma unroll
+                for (int off = 16; off > 0; off >>= 1) {
+                    const T og = __shfl_xor_sync(full, gb, off);
+                    const int ol = __shfl_xor_sync(full, lb, off);
+                    if (og < gb || (!(gb < og) && ol < lb)) { gb = og; lb = ol; }
+                }
+                if (lb == 0x7fffffff) continue;
+                const int sidx = lb * kLeaf + (lane & (kLeaf - 1));
+                const uint32_t id = ob.idx[sidx];
+                T gg = inf;
+                if (id != kPadIdx && !(gskip && (id & kGroundBit))) {
+                    T o[6];
+                    ob.box(sidx, o);
+                    gg = gap2_bb(lo, hi, o);
+                }
+                int sb = (gg < inf) ? sidx : 0x7fffffff;
+#pragma unroll
+                for (int off = kLeaf / 2; off > 0; off >>= 1) {
+                    const T og = __shfl_xor_sync(full, gg, off);
+                    const int os = __shfl_xor_sync(full, sb, off);
+                    if (og < gg || (!(gg < og) && os < sb)) { gg = og; sb = os; }
+                }
+                if (sb == 0x7fffffff) continue;
+                wide_push<MODE, T>(ms.qd, nqd, lane == 0, ((uint32_t)g << 21) | ((uint32_t)i << 16) | (uint32_t)sb);
+                if (nqd >= 32) {
+                    multi_drain_dist<MODE, T>(ms, 32, rb, ob, nm, pts, stride, ps);
+                    wide_pop32(ms.qd, nqd);
+                }
+            }
+        }
+        if (nqd > 0) multi_drain_dist<MODE, T>(ms, nqd, rb, ob, nm, pts, stride, ps);
+        nqd = 0;
+        __syncwarp();
+    }
+    // -------------------------------------------------------------- main
+    for (int g = 0; g < G; ++g) {
+        if (!((live >> g) & 1u)) continue;
+        const T *pg = pts + g * stride;
         for (int i = 0; i < L; ++i) {
+            const bool need_b = w.valid && !(ms.flags[g] & 1);
+            const bool need_d = w.dist && ms.hit_link[g] < 0;
+            if (!need_b && !need_d) break;
             T lo[3], hi[3];
 #pragma unroll
             for (int k = 0; k < 3; ++k) {
-                const T a = pts[3 * i + k], b = pts[3 * i + 3 + k];
+                const T a = pg[3 * i + k], b = pg[3 * i + 3 + k];
                 lo[k] = a < b ? a : b;
                 hi[k] = a < b ? b : a;
             }
+            const T r = LinkConst<T>::r(rb, i);
             const bool gskip = i < rb.ground_included;
-            T gb = inf;
-            int lb = 0x7fffffff;
-            for (int l = lane; l < ob.nb; l += 32) {
-                if (gskip && ob.ground_leaf(l)) continue;
-                T o[6];
-                ob.leaf(l, o);
-                const T g = gap2_bb(lo, hi, o);
-                if (g < gb || lb == 0x7fffffff) { gb = g; lb = l; }
-            }
-#pragma unroll
-            for (int off = 16; off > 0; off >>= 1) {
-                const T og = __shfl_xor_sync(full, gb, off);
-                const int ol = __shfl_xor_sync(full, lb, off);
-                if (og < gb || (!(gb < og) && ol < lb)) { gb = og; lb = ol; }
-            }
-            if (lb == 0x7fffffff) continue;
-            // the obstacle of that leaf with the smallest gap (lanes 0-7 of each octet agree)
-            const int s = lb * kLeaf + (lane & (kLeaf - 1));
-            const uint32_t id = ob.idx[s];
-            T g = inf;
-            if (id != kPadIdx && !(gskip && (id & kGroundBit))) {
-                T o[6];
-                ob.box(s, o);
-                g = gap2_bb(lo, hi, o);
-            }
-            int sb = (g < inf) ? s : 0x7fffffff;
-#pragma unroll
-            for (int off = kLeaf / 2; off > 0; off >>= 1) {
-                const T og = __shfl_xor_sync(full, g, off);
-                const int os = __shfl_xor_sync(full, sb, off);
-                if (og < g || (!(g < og) && os < sb)) { g = og; sb = os; }
-            }
-            if (lane == i && sb != 0x7fffffff) seed = ((uint32_t)i << 16) | (uint32_t)sb;
-        }
-        const bool has = seed != 0xffffffffu;
-        const unsigned m = __ballot_sync(full, has);
-        if (has) qd[__popc(m & ((1u << lane) - 1u))] = seed;
-        __syncwarp();
-        if (m) np_drain_dist<MODE, T>(qd, __popc(m), rb, ob, nm, pts, sk, best, hit_link, hit_j, unc_d);
-        __syncwarp();
-        if (hit_link >= 0) need_d = false;   // a settled hit: the distance is 0
-    }
-    // -------------------------------------------------------------- main
-    int nqb = 0, nqd = 0;
-    for (int i = 0; i < L && (need_b || need_d); ++i) {
-        T lo[3], hi[3];
-#pragma unroll
-        for (int k = 0; k < 3; ++k) {
-            const T a = pts[3 * i + k], b = pts[3 * i + 3 + k];
-            lo[k] = a < b ? a : b;
-            hi[k] = a < b ? b : a;
-        }
-        const T r = LinkConst<T>::r(rb, i);
-        const bool gskip = i < rb.ground_included;
-        const T tb = r * T(1.41421356237309515) + BoolMargin<MODE, T>::m();
-        const T tb2 = tb * tb;
-        const T slack = r + nm.eq + dmargin;
-        for (int l0 = 0; l0 < ob.nb && (need_b || need_d); l0 += 32) {
-            const int l = l0 + lane;
-            bool cl = false;
-            if (l < ob.nb && !(gskip && ob.ground_leaf(l))) {
-                T o[6];
-                ob.leaf(l, o);
-                const T g = gap2_bb(lo, hi, o);
-                const bool cb = need_b && !(g > tb2);
-                bool cd = false;
-                if (need_d) {
-                    const T smax = smin(best, (T)ob.blk[l * kBlkRec + 6]) + slack;
-                    const T slo = smin(best, (T)ob.blk[l * kBlkRec + 7]) + slack;
-                    cd = !(slo > T(0) && g > smax * smax);
+            const T tb = r * T(1.41421356237309515) + BoolMargin<MODE, T>::m();
+            const T tb2 = tb * tb;
+            const T slack = r + nm.eq + dmargin;
+            const T best = Key<T>::value(ms.best[g]);
+            for (int l0 = 0; l0 < ob.nb; l0 += 32) {
+                const int l = l0 + lane;
+                bool cl = false;
+                if (l < ob.nb && !(gskip && ob.ground_leaf(l))) {
+                    T o[6];
+                    ob.leaf(l, o);
+                    const T gg = gap2_bb(lo, hi, o);
+                    const bool cb = need_b && !(gg > tb2);
+                    bool cd = false;
+                    if (need_d) {
+                        const T smax = smin(best, (T)ob.blk[l * kBlkRec + 6]) + slack;
+                        const T slo = smin(best, (T)ob.blk[l * kBlkRec + 7]) + slack;
+                        cd = !(slo > T(0) && gg > smax * smax);
+                    }
+                    cl = cb || cd;
                 }
-                cl = cb || cd;
-            }
-            unsigned ml = __ballot_sync(full, cl);
-            while (ml != 0u && (need_b || need_d)) {
-                const int bit = nth_bit(ml, lane >> 3);
-                ml = drop4(ml);
-                bool pb = false, pd = false;
-                uint32_t item = 0u;
-                if (bit >= 0) {
-                    const int s = (l0 + bit) * kLeaf + (lane & (kLeaf - 1));
-                    const uint32_t id = ob.idx[s];
-                    item = ((uint32_t)i << 16) | (uint32_t)s;
-                    if (id != kPadIdx && !(gskip && (id & kGroundBit))) {
-                        T o[6];
-                        ob.box(s, o);
-                        const T g2 = gap2_bb(lo, hi, o);
-                        pb = need_b && !(g2 > tb2);
-                        if (need_d) {
-                            const T sv = smin(best, ob.tol(s)) + slack;
-                            pd = !(sv > T(0) && g2 > sv * sv);
+                unsigned ml = __ballot_sync(full, cl);
+                while (ml != 0u) {
+                    const int bit = nth_bit(ml, lane >> 3);
+                    ml = drop4(ml);
+                    bool pb = false, pd = false;
+                    uint32_t item = 0u;
+                    if (bit >= 0) {
+                        const int sidx = (l0 + bit) * kLeaf + (lane & (kLeaf - 1));
+                        const uint32_t id = ob.idx[sidx];
+                        item = ((uint32_t)g << 21) | ((uint32_t)i << 16) | (uint32_t)sidx;
+                        if (id != kPadIdx && !(gskip && (id & kGroundBit))) {
+                            T o[6];
+                            ob.box(sidx, o);
+                            const T g2 = gap2_bb(lo, hi, o);
+                            pb = need_b && !(g2 > tb2);
+                            if (need_d) {
+                                const T sv = smin(best, ob.tol(sidx)) + slack;
+                                pd = !(sv > T(0) && g2 > sv * sv);
+                            }
+                        }
+                    }
+                    if (need_b) {
+                        wide_push<MODE, T>(ms.qb, nqb, pb, item);
+                        if (nqb >= 32) {
+                            multi_drain_bool<MODE, T>(ms, 32, rb, ob, nm, pts, stride, ps);
+                            wide_pop32(ms.qb, nqb);
+                        }
+                    }
+                    if (need_d) {
+                        wide_push<MODE, T>(ms.qd, nqd, pd, item);
+                        if (nqd >= 32) {
+                            multi_drain_dist<MODE, T>(ms, 32, rb, ob, nm, pts, stride, ps);
+                            wide_pop32(ms.qd, nqd);
                         }
                     }
                 }
-                if (need_b) {
-                    wide_push<MODE, T>(qb, nqb, pb, item);
-                    if (nqb >= 32) {
-                        np_drain_bool<MODE, T>(qb, 32, rb, ob, nm, pts, sk, collided, unc_b);
-                        wide_pop32(qb, nqb);
-                        if (collided) { need_b = false; nqb = 0; }
-                    }
-                }
-                if (need_d) {
-                    wide_push<MODE, T>(qd, nqd, pd, item);
-                    if (nqd >= 32) {
-                        np_drain_dist<MODE, T>(qd, 32, rb, ob, nm, pts, sk, best, hit_link, hit_j, unc_d);
-                        wide_pop32(qd, nqd);
-                        if (hit_link >= 0) { need_d = false; nqd = 0; }
-                    }
-                }
             }
         }
     }
-    if (need_b && nqb > 0) np_drain_bool<MODE, T>(qb, nqb, rb, ob, nm, pts, sk, collided, unc_b);
-    if (need_d && nqd > 0) np_drain_dist<MODE, T>(qd, nqd, rb, ob, nm, pts, sk, best, hit_link, hit_j, unc_d);
+    if (nqb > 0) multi_drain_bool<MODE, T>(ms, nqb, rb, ob, nm, pts, stride, ps);
+    if (nqd > 0) multi_drain_dist<MODE, T>(ms, nqd, rb, ob, nm, pts, stride, ps);
     __syncwarp();
-    const bool hit = hit_link >= 0;
-    if (lane == 0) {
-        if (w.valid) *valid_out = collided ? 0 : 1;
-        if (w.dist) *dist_out = hit ? 0.0 : (double)best;
-    }
-    const bool bad_b = w.valid && !collided && unc_b;
-    const bool bad_d = w.dist && unc_d && !hit;
-    if (!(bad_b || bad_d)) return kSettled;
-    return (sk.ps && sk.slot >= 0 && !sk.full) ? kPairs : kFull;
+    // ---- results of configuration 'lane'
+    const int fl = ms.flags[lane];
+    const bool collided = fl & 1;
+    hit_link = ms.hit_link[lane];
+    hit_j = ms.hit_j[lane];
+    slot = ms.slot[lane];
+    valid = collided ? 0 : 1;
+    dist = hit_link >= 0 ? 0.0 : (double)Key<T>::value(ms.best[lane]);
+    const bool bad_b = w.valid && !collided && (fl & 2);
+    const bool bad_d = w.dist && (fl & 4) && hit_link < 0;
+    status = !(bad_b || bad_d) ? kSettled : ((ps && slot >= 0 && !(fl & 8)) ? kPairs : kFull);
+    (void)sizeof(K);
 }
 
 // One configuration, the whole warp.  pts = skeleton points [(D+1)][3];
@@ -657,7 +712,8 @@ __device__ __forceinline__ bool wide_stage(const Seg &sg, const WideLayout &L, u
 // consecutive configurations of one segment.
 template <int MODE>
 __device__ __forceinline__ void wide_kernel_body(const KParams &P, unsigned char *smem, uint64_t *bar,
-                                                 uint32_t (*wq)[128], int s) {
+                                                 MultiState<typename std::conditional<MODE == 0, double, float>::type> *ms,
+                                                 int s) {
     typedef typename std::conditional<MODE == 0, double, float>::type T;
     const Seg &sg = P.segs[s];
     const WideLayout L = WideLayout::of(MODE == 0 ? RPM_PREC_FP64 : RPM_PREC_FP32_REF, sg.ns, sg.nb);
@@ -665,6 +721,7 @@ __device__ __forceinline__ void wide_kernel_body(const KParams &P, unsigned char
     const DevRobot &rb = *reinterpret_cast<const DevRobot *>(smem);
     SortedView<T> ob{reinterpret_cast<const T *>(smem + L.rows), reinterpret_cast<const uint32_t *>(smem + L.idx),
                      reinterpret_cast<const float *>(smem + L.blk), sg.ns, sg.nb};
+    const unsigned full = 0xffffffffu;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int G = P.wide_g;
     const int D = rb.D;
@@ -685,18 +742,33 @@ __device__ __forceinline__ void wide_kernel_body(const KParams &P, unsigned char
     if (MODE == 0) { nm.eq = (T)P.nmd.eq; nm.maxd = (T)P.nmd.maxd; }
     else { nm.eq = (T)P.nmf.eq; nm.maxd = (T)P.nmf.maxd; }
     const Want w{sg.valid != nullptr, sg.dist != nullptr, sg.profile != nullptr};
+    if (!w.profile) {
+        const int n = (int)min((int64_t)G, sg.count - c0);
+        uint8_t v;
+        double d;
+        int st, slot, hl, hj;
+        wide_multi_np<MODE, T>(ms[warp], rb, ob, pts, (D + 1) * 3, n, n >= 32 ? full : ((1u << n) - 1u), nm, w,
+                               MODE == 2 ? &P.ps : nullptr, v, d, st, slot, hl, hj);
+        if (lane < n) {
+            const int64_t c = c0 + lane;
+            if (w.valid) sg.valid[c] = v;
+            if (w.dist) sg.dist[c] = d;
+            if (MODE == 2) {
+                complete_record(&P.ps, slot, st, s, c, hl, hj);
+                if (st == kFull) recheck_whole(P, s, c);
+            }
+        }
+        return;
+    }
+    uint32_t *wq = ms[warp].qb;   // 128 contiguous entries: qb then qd
     for (int g = 0; g < G; ++g) {
         const int64_t c = c0 + g;
         if (c >= sg.count) break;
         WideSink sk{MODE == 2 ? &P.ps : nullptr, -1, false};
         int hl, hj;
         const T *pc = pts + g * (D + 1) * 3;
-        const int st = w.profile
-                           ? wide_config<MODE, T>(wq[warp], gl, rb, ob, pc, nm, w, w.valid ? sg.valid + c : nullptr,
-                                                  w.dist ? sg.dist + c : nullptr, sg.profile + c * D, sk, hl, hj)
-                           : wide_config_np<MODE, T>(wq[warp], wq[warp] + 64, rb, ob, pc, nm, w,
-                                                     w.valid ? sg.valid + c : nullptr, w.dist ? sg.dist + c : nullptr,
-                                                     sk, hl, hj);
+        const int st = wide_config<MODE, T>(wq, gl, rb, ob, pc, nm, w, w.valid ? sg.valid + c : nullptr,
+                                            w.dist ? sg.dist + c : nullptr, sg.profile + c * D, sk, hl, hj);
         if (MODE == 2 && lane == 0) {
             complete_record(&P.ps, sk.slot, st, s, c, hl, hj);
             if (st == kFull) recheck_whole(P, s, c);
@@ -710,7 +782,7 @@ __device__ __forceinline__ void wide_kernel_body(const KParams &P, unsigned char
 // check at or below its edge's largest colliding k.
 template <int MODE>
 __device__ __forceinline__ void edge_wide_body(const EdgeParams &P, unsigned char *smem, uint64_t *bar,
-                                               uint32_t (*wq)[128]) {
+                                               MultiState<typename std::conditional<MODE == 0, double, float>::type> *ms) {
     typedef typename std::conditional<MODE == 0, double, float>::type T;
     const Seg &sg = P.seg;
     const WideLayout L = WideLayout::of(MODE == 0 ? RPM_PREC_FP64 : RPM_PREC_FP32_REF, sg.ns, sg.nb);
@@ -741,7 +813,7 @@ __device__ __forceinline__ void edge_wide_body(const EdgeParams &P, unsigned cha
             const int64_t first = P.bprefix[e / kEdgeScanBlock] + P.local[e];
             const int n = P.n_e[e];
             k = n - (int)(idx - first);
-            act = k > *(volatile int32_t *)&P.kmax[e];
+            act = k > *(volatile int32_t *)&P.kmax[e];   // a check nearer q2 already collides
             if (act) {
                 float dist, q[kMaxDof];
                 edge_count(P.q1 + e * D, P.q2 + e * D, D, P.step, P.num_checks, dist);
@@ -753,22 +825,15 @@ __device__ __forceinline__ void edge_wide_body(const EdgeParams &P, unsigned cha
             }
         }
         __syncwarp();
-        const unsigned am = __ballot_sync(full, act);
-        for (int g = 0; g < G; ++g) {
-            if (!((am >> g) & 1u)) continue;
-            const int64_t eg = __shfl_sync(full, e, g);
-            const int kg = __shfl_sync(full, k, g);
-            int km = 0;
-            if (lane == 0) km = *(volatile int32_t *)&P.kmax[eg];
-            if (kg <= __shfl_sync(full, km, 0)) continue;   // a check nearer q2 already collides
-            WideSink sk{MODE == 2 ? &P.ps : nullptr, -1, false};
-            uint8_t v = 1;
-            int hl, hj;
-            const int st = wide_config_np<MODE, T>(wq[warp], wq[warp] + 64, rb, ob, pts + g * (D + 1) * 3, nm,
-                                                   Want{true, false, false}, &v, nullptr, sk, hl, hj);
-            if (lane == 0) edge_outcome<MODE>(P, eg, kg, st, sk.slot, v);
-            __syncwarp();
-        }
+        const unsigned live = __ballot_sync(full, act);
+        if (live == 0u) continue;
+        uint8_t v;
+        double d;
+        int st, slot, hl, hj;
+        wide_multi_np<MODE, T>(ms[warp], rb, ob, pts, (D + 1) * 3, G, live, nm, Want{true, false, false},
+                               MODE == 2 ? &P.ps : nullptr, v, d, st, slot, hl, hj);
+        if (act) edge_outcome<MODE>(P, e, k, st, slot, v);
+        __syncwarp();
     }
 }
 #endif
