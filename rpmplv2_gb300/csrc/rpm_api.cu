@@ -50,6 +50,21 @@ void prune_users(rpm_ctx *ctx, SceneBuf &b) {
     b.users.swap(keep);
 }
 
+void stream_wait_users(rpm_ctx *ctx, SceneBuf &b, cudaStream_t st) {
+    for (cudaEvent_t e : b.users) {
+        // the wait binds to the event's current record, so the event can be reused at once
+        cudaStreamWaitEvent(st, e, 0);
+        ctx->event_pool.push_back(e);
+    }
+    b.users.clear();
+}
+
+int scene_dofs(rpm_ctx *ctx, int scene_id) {
+    std::lock_guard<std::mutex> lk(ctx->dof_mu);
+    auto it = ctx->scene_dofs.find(scene_id);
+    return it == ctx->scene_dofs.end() ? -1 : it->second;
+}
+
 void wait_users(rpm_ctx *ctx, SceneBuf &b) {
     for (cudaEvent_t e : b.users) {
         cudaEventSynchronize(e);
@@ -533,6 +548,8 @@ int enqueue_edges(rpm_ctx *ctx, Scratch *sc, SceneRec *s, int prec, const float 
     if (wide) {
         // persistent: as many CTAs as fit (two per SM for the FP32 forms)
         const int grid = ctx->num_sms * (prec == RPM_PREC_FP64 ? 1 : 2);
+        // edge streams pay off once every stream has a couple of edges to walk
+        p.streams = E >= 2 * (int64_t)grid * kWideWarps * p.wide_g ? 1 : 0;
         CK(launch_edges_wide(prec, p, grid, wide_smem_bytes(prec, s->ns, s->nb), st));
     } else {
         const int grid = ctx->num_sms * std::max(1, ctas_per_sm);
@@ -646,6 +663,10 @@ int rpm_scene_create(rpm_ctx *ctx, int32_t robot_id, const float *aabb_host, con
     s->version = 1;
     *scene_id = ctx->next_scene++;
     ctx->scenes[*scene_id] = s;
+    {
+        std::lock_guard<std::mutex> dl(ctx->dof_mu);
+        ctx->scene_dofs[*scene_id] = ctx->robots[robot_id].desc.num_dofs;
+    }
     return RPM_OK;
 }
 
@@ -677,6 +698,10 @@ int rpm_scene_destroy(rpm_ctx *ctx, int32_t scene_id) {
         if (b.upd_dev) cudaFree(b.upd_dev);
     }
     ctx->scenes.erase(scene_id);
+    {
+        std::lock_guard<std::mutex> dl(ctx->dof_mu);
+        ctx->scene_dofs.erase(scene_id);
+    }
     delete s;
     return RPM_OK;
 }

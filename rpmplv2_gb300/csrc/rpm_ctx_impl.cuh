@@ -140,6 +140,9 @@ struct rpm_ctx {
     bool use_graphs = false;
     int layout = RPM_LAYOUT_AUTO;    // lane- or warp-per-configuration checks
     std::map<std::pair<int, int>, int> edge_ctas;   // (robot, precision) -> CTAs per SM of the edge kernel
+    // degrees of freedom per scene, readable without 'mu' (the server's submit path)
+    std::mutex dof_mu;
+    std::map<int, int> scene_dofs;
 };
 
 namespace rpm {
@@ -149,6 +152,9 @@ int set_device(rpm_ctx *ctx);
 cudaEvent_t get_event(rpm_ctx *ctx);
 void prune_users(rpm_ctx *ctx, SceneBuf &b);
 void wait_users(rpm_ctx *ctx, SceneBuf &b);
+// Make stream 'st' wait (on the device) for every check still reading 'b'.
+void stream_wait_users(rpm_ctx *ctx, SceneBuf &b, cudaStream_t st);
+int scene_dofs(rpm_ctx *ctx, int scene_id);   // -1: unknown scene
 int get_scratch(rpm_ctx *ctx, cudaStream_t st, int64_t need, Scratch **out);
 void free_scratch(Scratch *sc);   // stream work using it must be complete
 SceneRec *find_scene(rpm_ctx *ctx, int id);

@@ -189,7 +189,9 @@ template <int IA, int IB> RPM_HD void rot_cols_f(float *R, float c, float s) {
     }
 }
 
-RPM_HD void fk_step_d(Fk<double> &f, const DevRobot &rb, int k, double q) {
+// sc (nullable): sin / cos of every joint angle, computed ahead (in parallel)
+// with taylor_sincos, so the serial chain holds only the rigid transforms.
+RPM_HD void fk_step_d(Fk<double> &f, const DevRobot &rb, int k, double q, const double *sc = nullptr) {
     const double *o = rb.oxyz[k];
     double np[3];
 #pragma unroll
@@ -212,7 +214,8 @@ RPM_HD void fk_step_d(Fk<double> &f, const DevRobot &rb, int k, double q) {
         for (int i = 0; i < 9; ++i) f.R[i] = nR[i];
     }
     double s, c;
-    taylor_sincos(q, &s, &c);
+    if (sc) { s = sc[2 * k]; c = sc[2 * k + 1]; }
+    else taylor_sincos(q, &s, &c);
     switch (rb.axis[k]) {   // columns (a, b) <- (a c + b s, b c - a s)
         case 0: rot_cols_d<1, 2>(f.R, c, s); break;
         case 1: rot_cols_d<2, 0>(f.R, c, s); break;
@@ -258,11 +261,12 @@ template <int MODE> struct SkelWalker;
 
 template <> struct SkelWalker<0> {
     Fk<double> f;
+    const double *sc = nullptr;   // precomputed joint sin / cos (nullable)
     RPM_HD void begin() { f.init(); }
     RPM_HD void point(const DevRobot &rb, const float *q, int k, double *out) {
         if (rb.kind == RPM_ROBOT_CHAIN) {
             if (k < rb.D) {
-                fk_step_d(f, rb, k, (double)q[k]);
+                fk_step_d(f, rb, k, (double)q[k], sc);
                 out[0] = f.p[0]; out[1] = f.p[1]; out[2] = f.p[2];
             } else {
                 const double *o = rb.oxyz[rb.D];
@@ -276,20 +280,20 @@ template <> struct SkelWalker<0> {
         }
         switch (k) {
             case 0: out[0] = out[1] = out[2] = 0.0; break;
-            case 1: fk_step_d(f, rb, 0, (double)q[0]); fk_step_d(f, rb, 1, (double)q[1]);
+            case 1: fk_step_d(f, rb, 0, (double)q[0], sc); fk_step_d(f, rb, 1, (double)q[1], sc);
                     out[0] = f.p[0]; out[1] = f.p[1]; out[2] = f.p[2]; break;
-            case 2: fk_step_d(f, rb, 2, (double)q[2]); out[0] = f.p[0]; out[1] = f.p[1]; out[2] = f.p[2]; break;
-            case 3: fk_step_d(f, rb, 3, (double)q[3]);
+            case 2: fk_step_d(f, rb, 2, (double)q[2], sc); out[0] = f.p[0]; out[1] = f.p[1]; out[2] = f.p[2]; break;
+            case 3: fk_step_d(f, rb, 3, (double)q[3], sc);
 #pragma unroll
                     for (int i = 0; i < 3; ++i) out[i] = dadd(f.p[i], -dmul(f.R[3 * i + 2], 0.25));
                     break;
-            case 4: fk_step_d(f, rb, 4, (double)q[4]); out[0] = f.p[0]; out[1] = f.p[1]; out[2] = f.p[2]; break;
+            case 4: fk_step_d(f, rb, 4, (double)q[4], sc); out[0] = f.p[0]; out[1] = f.p[1]; out[2] = f.p[2]; break;
             case 5:
 #pragma unroll
                     for (int i = 0; i < 3; ++i) out[i] = dadd(f.p[i], dmul(f.R[3 * i + 0], 0.076));
                     break;
             default: {
-                fk_step_d(f, rb, 5, (double)q[5]);
+                fk_step_d(f, rb, 5, (double)q[5], sc);
                 const double g = rb.gripper_d, g3 = dmul(0.3, rb.gripper_d);
 #pragma unroll
                 for (int i = 0; i < 3; ++i) {

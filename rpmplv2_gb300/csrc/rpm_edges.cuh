@@ -44,6 +44,7 @@ struct EdgeParams {
     Num<float> nmf;
     PairSink ps;             // FP32 pass -> pair-level FP64 recheck (records: seg = k, config = edge)
     int32_t wide_g;          // warp-per-check kernels: checks taken per warp
+    int32_t streams;         // warp-per-check kernels: 1 = edge streams, 0 = flat checks
 };
 
 RPM_HD void edge_point(const float *a, const float *b, int D, float ratio, float *out) {

@@ -153,9 +153,53 @@ __device__ __forceinline__ bool decode_pair(const PairSink &ps, uint32_t k, uint
     return slot < ncfg && ps.cfgs[slot].status == kPairs;
 }
 
+// FP64 skeleton with the whole warp: the joints' sines and cosines in
+// parallel (the same taylor_sincos values), then the serial chain in lane 0.
+__device__ __forceinline__ void pair_skel_warp(const DevRobot &rb, const float *q, double *out, PairAcc &a,
+                                               double *sc) {
+    const int lane = threadIdx.x & 31;
+    if (lane < rb.D) taylor_sincos((double)q[lane], &sc[2 * lane], &sc[2 * lane + 1]);
+    a.lkey[lane] = 0x7fffffff;
+    a.hkey[lane] = ~0ull;
+    if (lane == 0) {
+        a.dkey = 0x7fffffffffffffffLL;
+        a.coll = 0;
+    }
+    __syncwarp();
+    if (lane == 0) {
+        SkelWalker<0> sw;
+        sw.sc = sc;
+        sw.begin();
+        for (int i = 0; i <= rb.D; ++i) sw.point(rb, q, i, out + 3 * i);
+    }
+    __syncwarp();
+}
+
+// Work item of this warp when there are at most as many items as warps:
+// consecutive items go to different CTAs, so they run on different SMs
+// (each FP64 warp instruction costs an SM the same time however few lanes
+// are active).  -1: this warp has none.
+__device__ __forceinline__ int64_t spread_item(uint32_t n) {
+    const uint32_t wpb = blockDim.x / 32;
+    const uint32_t w = (threadIdx.x / 32) * gridDim.x + blockIdx.x;
+    return w < n && n <= gridDim.x * wpb ? (int64_t)w : -1;
+}
+
 // 1. FP64 skeleton of each recorded configuration.
 __global__ void k_pair_skel(const __grid_constant__ KParams P) {
+    __shared__ double sc[kThreads / 32][2 * kMaxDof];
     const uint32_t n = min(*P.ps.cfg_count, P.ps.cfg_cap);
+    if (n <= gridDim.x * (blockDim.x / 32)) {   // few records: a warp each
+        const int64_t k = spread_item(n);
+        if (k < 0) return;
+        const PairCfg c = P.ps.cfgs[k];
+        if (c.status != kPairs) return;
+        const Seg &sg = P.segs[c.seg];
+        const DevRobot &rb = *sg.robot;
+        pair_skel_warp(rb, sg.q + c.config * rb.D, P.ps.skel + (size_t)k * (kMaxDof + 1) * 3, P.ps.acc[k],
+                       sc[threadIdx.x / 32]);
+        return;
+    }
     for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
         const PairCfg c = P.ps.cfgs[k];
         if (c.status != kPairs) continue;
@@ -172,6 +216,17 @@ __global__ void k_pair_skel(const __grid_constant__ KParams P) {
 __global__ void k_pair_eval(const __grid_constant__ KParams P) {
     const uint32_t n = min(*P.ps.pair_count, P.ps.pair_cap);
     const uint32_t ncfg = min(*P.ps.cfg_count, P.ps.cfg_cap);
+    if (n <= gridDim.x * (blockDim.x / 32)) {   // few pairs: a warp each (lane 0), spread over the SMs
+        const int64_t k = spread_item(n);
+        if (k < 0 || (threadIdx.x & 31) != 0) return;
+        uint32_t slot;
+        int link, j, kind;
+        if (!decode_pair(P.ps, (uint32_t)k, ncfg, slot, link, j, kind)) return;
+        const Seg &sg = P.segs[P.ps.cfgs[slot].seg];
+        ObsView<double> ob{sg.obs_d, sg.obs_f + (size_t)kRowGround * sg.n_pad, sg.n, sg.n_pad};
+        pair_eval_one(*sg.robot, ob, P.nmd, P.ps.skel + (size_t)slot * (kMaxDof + 1) * 3, link, j, kind, P.ps.acc[slot]);
+        return;
+    }
     for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
         uint32_t slot;
         int link, j, kind;
@@ -185,9 +240,26 @@ __global__ void k_pair_eval(const __grid_constant__ KParams P) {
 // Edge checks: the same three steps; a record is check k (seg) of an edge
 // (config), and an FP64 collision raises the edge's largest colliding k.
 __global__ void k_edge_pair_skel(const __grid_constant__ EdgeParams P) {
+    __shared__ double sc[kThreads / 32][2 * kMaxDof];
+    __shared__ float qs[kThreads / 32][kMaxDof];
     const uint32_t n = min(*P.ps.cfg_count, P.ps.cfg_cap);
     const DevRobot &rb = *P.seg.robot;
     const int D = rb.D;
+    if (n <= gridDim.x * (blockDim.x / 32)) {   // few records: a warp each
+        const int64_t k = spread_item(n);
+        if (k < 0) return;
+        const PairCfg c = P.ps.cfgs[k];
+        if (c.status != kPairs) return;
+        const int w = threadIdx.x / 32;
+        if ((threadIdx.x & 31) == 0) {
+            float dist;
+            const int N = edge_count(P.q1 + c.config * D, P.q2 + c.config * D, D, P.step, P.num_checks, dist);
+            edge_config(P.q1 + c.config * D, P.q2 + c.config * D, D, N, c.seg, dist, qs[w]);
+        }
+        __syncwarp();
+        pair_skel_warp(rb, qs[w], P.ps.skel + (size_t)k * (kMaxDof + 1) * 3, P.ps.acc[k], sc[w]);
+        return;
+    }
     for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
         const PairCfg c = P.ps.cfgs[k];
         if (c.status != kPairs) continue;
@@ -203,6 +275,16 @@ __global__ void k_edge_pair_eval(const __grid_constant__ EdgeParams P) {
     const uint32_t n = min(*P.ps.pair_count, P.ps.pair_cap);
     const uint32_t ncfg = min(*P.ps.cfg_count, P.ps.cfg_cap);
     ObsView<double> ob{P.seg.obs_d, P.seg.obs_f + (size_t)kRowGround * P.seg.n_pad, P.seg.n, P.seg.n_pad};
+    if (n <= gridDim.x * (blockDim.x / 32)) {   // few pairs: a warp each (lane 0), spread over the SMs
+        const int64_t k = spread_item(n);
+        if (k < 0 || (threadIdx.x & 31) != 0) return;
+        uint32_t slot;
+        int link, j, kind;
+        if (!decode_pair(P.ps, (uint32_t)k, ncfg, slot, link, j, kind)) return;
+        pair_eval_one(*P.seg.robot, ob, P.nmd, P.ps.skel + (size_t)slot * (kMaxDof + 1) * 3, link, j, kind,
+                      P.ps.acc[slot]);
+        return;
+    }
     for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
         uint32_t slot;
         int link, j, kind;

@@ -57,8 +57,12 @@ int scene_update(rpm_ctx *ctx, SceneRec *s, const int32_t *idx, const float *aab
     const int nxt = (s->cur + 1) % kRing;
     SceneBuf &cur = s->bufs[s->cur];
     SceneBuf &b = s->bufs[nxt];
-    wait_users(ctx, b);
-    if (b.ready) CK(cudaEventSynchronize(b.ready));   // its staging may be reused now
+    // checks still reading the version about to be overwritten finish first
+    // (ordered on the device: the host never blocks here)
+    stream_wait_users(ctx, b, ctx->upd_stream);
+    // the pinned staging of this buffer is free once its last update ran;
+    // otherwise this update copies from pageable memory
+    const bool staging_free = !b.ready || cudaEventQuery(b.ready) == cudaSuccess;
     const size_t bytes = scene_bytes(*s);
     if (!b.mem) {
         if (cudaMalloc(&b.mem, bytes) != cudaSuccess) return fail(RPM_ERR_NOMEM, "scene version allocation failed");
@@ -66,6 +70,7 @@ int scene_update(rpm_ctx *ctx, SceneRec *s, const int32_t *idx, const float *aab
     }
     if (!b.ready) CK(cudaEventCreateWithFlags(&b.ready, cudaEventDisableTiming));
     if (b.upd_cap < m) {
+        if (b.ready) CK(cudaEventSynchronize(b.ready));   // growing the staging (rare): its last copy must be done
         if (b.upd_host) cudaFreeHost(b.upd_host);
         if (b.upd_dev) cudaFree(b.upd_dev);
         b.upd_cap = std::max(m, 64);
@@ -73,14 +78,20 @@ int scene_update(rpm_ctx *ctx, SceneRec *s, const int32_t *idx, const float *aab
             cudaMalloc(&b.upd_dev, (size_t)b.upd_cap * 7 * sizeof(float)) != cudaSuccess)
             return fail(RPM_ERR_NOMEM, "update staging allocation failed");
     }
+    std::vector<float> pageable;
+    float *stage = b.upd_host;
+    if (!staging_free) {
+        pageable.resize((size_t)m * 7);
+        stage = pageable.data();
+    }
     for (int k = 0; k < m; ++k) {
         int32_t j = idx[k];
-        std::memcpy(&b.upd_host[7 * k], &j, sizeof j);
-        for (int c = 0; c < 6; ++c) b.upd_host[7 * k + 1 + c] = aabb[6 * (size_t)k + c];
+        std::memcpy(&stage[7 * k], &j, sizeof j);
+        for (int c = 0; c < 6; ++c) stage[7 * k + 1 + c] = aabb[6 * (size_t)k + c];
     }
     CK(cudaMemcpyAsync(b.mem, cur.mem, bytes, cudaMemcpyDeviceToDevice, ctx->upd_stream));
     if (m > 0) {
-        CK(cudaMemcpyAsync(b.upd_dev, b.upd_host, (size_t)m * 7 * sizeof(float), cudaMemcpyHostToDevice, ctx->upd_stream));
+        CK(cudaMemcpyAsync(b.upd_dev, stage, (size_t)m * 7 * sizeof(float), cudaMemcpyHostToDevice, ctx->upd_stream));
         k_obstacle_update<<<(m + 127) / 128, 128, 0, ctx->upd_stream>>>(b.f, b.d, s->n_pad, b.upd_dev, m);
         CK(cudaGetLastError());
         CK(launch_scene_sort(*s, b, ctx->upd_stream));   // same order, new contents and block bounds
@@ -221,17 +232,15 @@ DevBufs layout(rpm_server *srv, const Req *q) {
     return d;
 }
 
-// Launch one batch on a free slot: copies in, the checks, copies out.  Caller
-// holds srv->mu; takes ctx->mu for the enqueue.
-int launch_batch(rpm_server *srv, Slot &slot, std::vector<Req *> &batch) {
+// Launch one batch on a reserved slot: copies in, the checks, copies out.
+// Called by the worker without srv->mu (the batch and the slot are its own);
+// takes ctx->mu for the enqueue.
+int launch_batch(rpm_server *srv, Slot &slot, const std::vector<Req *> &batch) {
     rpm_ctx *ctx = srv->ctx;
-    const double t = now_s();
     std::lock_guard<std::mutex> lk(ctx->mu);
     if (set_device(ctx)) return RPM_ERR_CUDA;
     std::vector<SegReq> segs;
     for (Req *q : batch) {
-        q->t.t_launch = t;
-        q->t.batch_size = (int32_t)batch.size();
         const DevBufs d = layout(srv, q);
         const size_t n = (size_t)q->r.count;
         if (q->r.kind == RPM_REQ_EDGES) {
@@ -282,9 +291,6 @@ int launch_batch(rpm_server *srv, Slot &slot, std::vector<Req *> &batch) {
         }
     }
     CK(cudaEventRecord(slot.done, slot.st));
-    slot.reqs = batch;
-    slot.busy = true;
-    srv->batches++;
     return RPM_OK;
 }
 
@@ -358,11 +364,23 @@ void worker_loop(rpm_server *srv) {
                 if (edge) break;   // an edge pipeline takes the slot to itself
             }
             if (batch.empty()) continue;
+            sl.busy = true;   // reserved: only this thread touches the slot
+            const double t = now_s();
+            lk.unlock();      // submissions and polls proceed while the batch is enqueued
             const int rc = launch_batch(srv, sl, batch);
+            lk.lock();
+            for (Req *q : batch) {
+                q->t.t_launch = t;
+                q->t.batch_size = (int32_t)batch.size();
+            }
             if (rc) {
-                const double t = now_s();
-                for (Req *q : batch) { q->t.status = rc; q->t.t_done = t; srv->arena.release(q->off, q->bytes); }
+                const double te = now_s();
+                for (Req *q : batch) { q->t.status = rc; q->t.t_done = te; srv->arena.release(q->off, q->bytes); }
+                sl.busy = false;
                 srv->cv_done.notify_all();
+            } else {
+                sl.reqs = batch;
+                srv->batches++;
             }
             progress = true;
         }
@@ -429,15 +447,12 @@ int rpm_server_submit(rpm_server *srv, const rpm_request *r, uint64_t *ticket) {
     if (r->kind != RPM_REQ_CONFIGS && r->kind != RPM_REQ_EDGES) return fail(RPM_ERR_INVALID, "unknown request kind");
     if (r->count > 0 && (r->kind == RPM_REQ_CONFIGS ? !r->q_host : (!r->q1_host || !r->q2_host || !r->valid_host)))
         return fail(RPM_ERR_INVALID, "missing request buffers");
+    const int dofs = scene_dofs(srv->ctx, r->scene_id);
+    if (dofs < 0) return fail(RPM_ERR_INVALID, "unknown scene %d", r->scene_id);
     Req *q = new Req();
     q->r = *r;
-    {
-        std::lock_guard<std::mutex> lk(srv->ctx->mu);
-        SceneRec *s = find_scene(srv->ctx, r->scene_id);
-        if (!s) { delete q; return fail(RPM_ERR_INVALID, "unknown scene %d", r->scene_id); }
-        q->D = srv->ctx->robots[s->robot].desc.num_dofs;
-        q->L = q->D;
-    }
+    q->D = dofs;
+    q->L = dofs;
     q->bytes = request_bytes(q->r, q->D, q->L);
     q->t.status = 1;
     q->t.t_submit = now_s();

@@ -776,10 +776,16 @@ __device__ __forceinline__ void wide_kernel_body(const KParams &P, unsigned char
     }
 }
 
-// Body of k_edges_wide<MODE>: persistent warps take G consecutive flat checks
-// at a time (edge-major, k descending), run their forward kinematics lane =
-// check, then check them one at a time with the whole warp, skipping every
-// check at or below its edge's largest colliding k.
+// Body of k_edges_wide<MODE>.  Batches with fewer edges than about two per
+// stream check all their checks in parallel (flat mode below); larger ones
+// run edge streams: each warp runs G edge streams.  A stream owns
+// one edge and walks its checks in the reference's order (k = n_e down to 1);
+// every round the warp checks the current check of all its streams together
+// (one forward kinematics per lane, shared queues).  A settled collision at k
+// sets the edge's largest colliding k and ends the stream (the reference
+// stops there); a check left to the FP64 recheck does not stop it, since a
+// collision further down still has to be found.  Finished streams take the
+// next edge from a global counter.
 template <int MODE>
 __device__ __forceinline__ void edge_wide_body(const EdgeParams &P, unsigned char *smem, uint64_t *bar,
                                                MultiState<typename std::conditional<MODE == 0, double, float>::type> *ms) {
@@ -798,41 +804,93 @@ __device__ __forceinline__ void edge_wide_body(const EdgeParams &P, unsigned cha
     Num<T> nm;
     if (MODE == 0) { nm.eq = (T)P.nmd.eq; nm.maxd = (T)P.nmd.maxd; }
     else { nm.eq = (T)P.nmf.eq; nm.maxd = (T)P.nmf.maxd; }
-    const int64_t total = P.bprefix[(P.E + kEdgeScanBlock - 1) / kEdgeScanBlock];
-    for (;;) {
-        unsigned long long base = 0;
-        if (lane == 0) base = atomicAdd(P.work, (unsigned long long)G);
-        base = __shfl_sync(full, base, 0);
-        if ((int64_t)base >= total) break;
-        int64_t e = 0;
-        int k = 0;
-        bool act = false;
-        if (lane < G && (int64_t)base + lane < total) {
-            const int64_t idx = (int64_t)base + lane;
-            e = edge_of_flat(P, idx);
-            const int64_t first = P.bprefix[e / kEdgeScanBlock] + P.local[e];
-            const int n = P.n_e[e];
-            k = n - (int)(idx - first);
-            act = k > *(volatile int32_t *)&P.kmax[e];   // a check nearer q2 already collides
-            if (act) {
-                float dist, q[kMaxDof];
-                edge_count(P.q1 + e * D, P.q2 + e * D, D, P.step, P.num_checks, dist);
-                edge_config(P.q1 + e * D, P.q2 + e * D, D, n, k, dist, q);
-                SkelWalker<MODE> sw;
-                sw.begin();
-                T *p = pts + lane * (D + 1) * 3;
-                for (int t = 0; t <= D; ++t) sw.point(rb, q, t, p + 3 * t);
+    if (!P.streams) {
+        // small batches: every check of every edge in parallel, G consecutive
+        // flat checks (edge-major, k descending) per warp at a time
+        const int64_t total = P.bprefix[(P.E + kEdgeScanBlock - 1) / kEdgeScanBlock];
+        for (;;) {
+            unsigned long long base = 0;
+            if (lane == 0) base = atomicAdd(P.work, (unsigned long long)G);
+            base = __shfl_sync(full, base, 0);
+            if ((int64_t)base >= total) break;
+            int64_t e = 0;
+            int k = 0;
+            bool act = false;
+            if (lane < G && (int64_t)base + lane < total) {
+                const int64_t idx = (int64_t)base + lane;
+                e = edge_of_flat(P, idx);
+                const int64_t first = P.bprefix[e / kEdgeScanBlock] + P.local[e];
+                const int n = P.n_e[e];
+                k = n - (int)(idx - first);
+                act = k > *(volatile int32_t *)&P.kmax[e];   // a check nearer q2 already collides
+                if (act) {
+                    float dist, q[kMaxDof];
+                    edge_count(P.q1 + e * D, P.q2 + e * D, D, P.step, P.num_checks, dist);
+                    edge_config(P.q1 + e * D, P.q2 + e * D, D, n, k, dist, q);
+                    SkelWalker<MODE> sw;
+                    sw.begin();
+                    T *p = pts + lane * (D + 1) * 3;
+                    for (int t = 0; t <= D; ++t) sw.point(rb, q, t, p + 3 * t);
+                }
             }
+            __syncwarp();
+            const unsigned live = __ballot_sync(full, act);
+            if (live == 0u) continue;
+            uint8_t v;
+            double dd;
+            int st, slot, hl, hj;
+            wide_multi_np<MODE, T>(ms[warp], rb, ob, pts, (D + 1) * 3, G, live, nm, Want{true, false, false},
+                                   MODE == 2 ? &P.ps : nullptr, v, dd, st, slot, hl, hj);
+            if (act) edge_outcome<MODE>(P, e, k, st, slot, v);
+            __syncwarp();
+        }
+        return;
+    }
+    int64_t e = -1;      // this lane's edge (-1: none)
+    int k = 0, n = 0;    // its current check and check count
+    float dist = 0.f;
+    bool more = true;    // edges left to take (warp-uniform)
+    for (;;) {
+        const bool need = lane < G && e < 0 && more;
+        const unsigned nmask = __ballot_sync(full, need);
+        if (nmask) {
+            unsigned long long base = 0;
+            if (lane == 0) base = atomicAdd(P.work, (unsigned long long)__popc(nmask));
+            base = __shfl_sync(full, base, 0);
+            if (need) {
+                const int64_t idx = (int64_t)base + __popc(nmask & ((1u << lane) - 1u));
+                if (idx < P.E) {
+                    e = idx;
+                    n = edge_count(P.q1 + e * D, P.q2 + e * D, D, P.step, P.num_checks, dist);
+                    k = n;
+                }
+            }
+            if ((int64_t)base + __popc(nmask) >= P.E) more = false;
+        }
+        const unsigned live = __ballot_sync(full, lane < G && e >= 0);
+        if (live == 0u) {
+            if (!more) break;
+            continue;
+        }
+        if (e >= 0) {
+            float q[kMaxDof];
+            edge_config(P.q1 + e * D, P.q2 + e * D, D, n, k, dist, q);
+            SkelWalker<MODE> sw;
+            sw.begin();
+            T *p = pts + lane * (D + 1) * 3;
+            for (int t = 0; t <= D; ++t) sw.point(rb, q, t, p + 3 * t);
         }
         __syncwarp();
-        const unsigned live = __ballot_sync(full, act);
-        if (live == 0u) continue;
         uint8_t v;
-        double d;
+        double dd;
         int st, slot, hl, hj;
         wide_multi_np<MODE, T>(ms[warp], rb, ob, pts, (D + 1) * 3, G, live, nm, Want{true, false, false},
-                               MODE == 2 ? &P.ps : nullptr, v, d, st, slot, hl, hj);
-        if (act) edge_outcome<MODE>(P, e, k, st, slot, v);
+                               MODE == 2 ? &P.ps : nullptr, v, dd, st, slot, hl, hj);
+        if (e >= 0) {
+            edge_outcome<MODE>(P, e, k, st, slot, v);
+            if (st == kSettled && v == 0) e = -1;    // the reference's first collision: the edge is done
+            else if (--k < 1) e = -1;                // every check clear (or left to the recheck)
+        }
         __syncwarp();
     }
 }
