@@ -45,7 +45,9 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--configs", type=int, default=NUM_CONFIGS)
-    ap.add_argument("--no-extra", action="store_true", help="skip the edge, mixed-DOF and serving measurements")
+    ap.add_argument("--no-extra", action="store_true", help="skip the edge, mixed-DOF, large-scene and serving measurements")
+    ap.add_argument("--extra", default="edges,mixed,large,serve",
+                    help="comma list of extra measurements: edges, mixed, large, serve")
     return ap.parse_args()
 
 
@@ -156,7 +158,21 @@ def extra_workloads(eng, args):
             ms.append(a.elapsed_time(b))
         return statistics.median(ms)
 
-    # ---- edges (BASELINE config 2)
+    which = set(args.extra.split(","))
+    if "edges" in which:
+        out["edges"] = edges_line(eng, scenes, timed)
+    if "mixed" in which:
+        out["mixed_dof"] = mixed_line(eng, scenes, timed)
+    if "large" in which:
+        out["large_scene"] = large_line(eng, scenes, timed)
+    if "serve" in which:
+        out["serve"] = serve_line(eng, serve)
+    return out
+
+
+def edges_line(eng, scenes, timed):
+    """262,144 spatial_10dof edges at 0.05 rad steps against 200 boxes."""
+    import torch
     robot, scene, q1, q2, step = scenes.spatial10_edge_workload(1 << 18, seed=2)
     sid = eng.create_scene(eng.upload_robot(robot), scene)
     q1d, q2d = torch.from_numpy(q1).cuda(), torch.from_numpy(q2).cuda()
@@ -167,12 +183,17 @@ def extra_workloads(eng, args):
     ms = timed(lambda: eng.check_edges(sid, q1d, q2d, v, k, step=float(step), precision="fp32_recheck"))
     eng.set_graphs(False)
     checks = int(k.sum().item())
-    out["edges"] = {"workload": "spatial_10dof (r 0.03) vs 200 rotated boxes as fcl AABBs, 262,144 edges, 0.05 rad",
-                    "edges_per_s": q1.shape[0] / (ms / 1e3), "checks_per_s": checks / (ms / 1e3),
-                    "ms_per_step": ms, "checks_reference_order": checks, "valid_fraction": float(v.float().mean()),
-                    "ctas_per_sm": ctas, "cuda_graph": True, "precision": "fp32_recheck"}
+    line = {"workload": "spatial_10dof (r 0.03) vs 200 rotated boxes as fcl AABBs, 262,144 edges, 0.05 rad",
+            "edges_per_s": q1.shape[0] / (ms / 1e3), "checks_per_s": checks / (ms / 1e3),
+            "ms_per_step": ms, "checks_reference_order": checks, "valid_fraction": float(v.float().mean()),
+            "ctas_per_sm": ctas, "cuda_graph": True, "precision": "fp32_recheck"}
     eng.destroy_scene(sid)
-    # ---- mixed-DOF profile launch (BASELINE config 3)
+    return line
+
+
+def mixed_line(eng, scenes, timed):
+    """Per-link distance profiles of spatial 14/18/22-DOF chains against 500 AABBs in one launch."""
+    import torch
     scene, parts = scenes.mixed_dof_workload(seed=3)
     items = []
     for robot, q in parts:
@@ -182,12 +203,35 @@ def extra_workloads(eng, args):
                       torch.zeros((C, L), device="cuda")))
     total = sum(it[1].shape[0] for it in items)
     ms = timed(lambda: eng.check_batch(items, "fp32_recheck"))
-    out["mixed_dof"] = {"workload": "spatial 14/18/22 DOF (r 0.03), 32,768/49,152/49,152 configs, 500 AABBs, "
+    line = {"workload": "spatial 14/18/22 DOF (r 0.03), 32,768/49,152/49,152 configs, 500 AABBs, "
                         "per-link distance + global min in one launch",
-                        "configs_per_s": total / (ms / 1e3), "ms_per_step": ms, "precision": "fp32_recheck"}
+            "configs_per_s": total / (ms / 1e3), "ms_per_step": ms, "precision": "fp32_recheck"}
     for it in items:
         eng.destroy_scene(it[0])
-    # ---- serving replay (BASELINE config 4)
+    return line
+
+
+def large_line(eng, scenes, timed):
+    """isValid + computeDistance of 65,536 spatial_22dof configurations against 1000 boxes (the
+    warp-per-configuration layout), the size of the largest serving requests."""
+    import torch
+    robot, scene, q = scenes.large_scene_workload(65536, seed=6)
+    sid = eng.create_scene(eng.upload_robot(robot), scene)
+    qd = torch.from_numpy(q).cuda()
+    C = q.shape[0]
+    v = torch.zeros(C, dtype=torch.uint8, device="cuda")
+    d = torch.zeros(C, dtype=torch.float64, device="cuda")
+    ms = timed(lambda: eng.check_configs(sid, qd, "fp32_recheck", v, d, None), steps=5, warmup=2)
+    line = {"workload": "spatial_22dof (r 0.03) vs 1000 boxes (dims U[0.02, 0.15] m, 1.5 m ball), 65,536 configs, "
+                        "isValid + computeDistance",
+            "configs_per_s": C / (ms / 1e3), "ms_per_step": ms, "valid_fraction": float(v.float().mean()),
+            "layout": "auto (warp per configuration)", "precision": "fp32_recheck"}
+    eng.destroy_scene(sid)
+    return line
+
+
+def serve_line(eng, serve):
+    """The serving replay: 20,000 requests/s for 0.5 s over 64 resident scenes."""
     wl = serve.serving_workload(eng, seed=4, rate=20000.0, duration=0.5)
     srv = serve.Server(eng, num_slots=6)
     srv.replay(wl["requests"][:200], [0.0] * 200)
@@ -197,11 +241,10 @@ def extra_workloads(eng, args):
                              "boxes moving up to 1.6 m/s updated every 1 ms), Poisson 20,000 req/s for 0.5 s, "
                              "sizes log-uniform 1-65,536, isValid / distance / edge in equal shares",
                  "memory_budget_bytes": 8 << 30, "slots": 6})
-    out["serve"] = summ
     srv.close()
     for sid in wl["scene_ids"]:
         eng.destroy_scene(sid)
-    return out
+    return summ
 
 
 def run_reference(args, ws, rank):

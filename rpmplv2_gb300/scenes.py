@@ -171,6 +171,15 @@ def spatial10_edge_workload(num_edges=1 << 18, seed=2, step=0.05):
     return robot, scene, q1, q2, np.float32(step)
 
 
+def large_scene_workload(num_configs=65536, seed=6, num_obstacles=1000, dofs=22):
+    """A spatial chain against a large obstacle set: boxes with dims U[0.02, 0.15] m,
+    centres uniform in a 1.5 m ball (no rejection), configurations uniform in limits."""
+    rng = np.random.default_rng(seed)
+    robot = _robots.spatial(dofs, radius=0.03)
+    boxes = [box_aabb(rng.uniform(0.02, 0.15, 3), c) for c in _ball(rng, num_obstacles, SPATIAL_WS_CENTER, 1.5)]
+    return robot, Scene(np.array(boxes)), uniform_configs(rng, num_configs, dofs)
+
+
 def mixed_dof_workload(counts=(32768, 49152, 49152), seed=3):
     rng = np.random.default_rng(seed)
     scene = random_obb_scene(rng, 500, 0.02, 0.15, SPATIAL_WS_CENTER, 1.5, rotated=False,
