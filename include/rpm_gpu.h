@@ -197,6 +197,29 @@ int rpm_set_edge_ctas(rpm_ctx *ctx, int32_t scene_id, int32_t precision, int32_t
  * addition with no reference counterpart; outputs do not depend on it. */
 int rpm_ctx_set_layout(rpm_ctx *ctx, int32_t layout);
 
+/* computeDistance(q, true) with the nearest points (RealVectorSpace.cpp:318-392)
+ * for the single-state adapter path: every (link, obstacle) pair is evaluated.
+ * dist_dev[c] (double); profile_dev[c][L] (float, the early-exit profile);
+ * nearest_dev[c][n][6][L] (float; rows 0-2 the robot point, rows 3-5 the
+ * obstacle point, one column per link: the reference's vector<MatrixXf(6, L)>);
+ * nearest_valid_dev[c] = 0 where the reference sets the nearest points to
+ * nullptr (some link at distance <= 0).  precision RPM_PREC_FP64 or
+ * RPM_PREC_FP32_REF (bit-equal to the reference's numerics);
+ * RPM_PREC_FP32_RECHECK is served by the FP64 form. */
+int rpm_distance_nearest(rpm_ctx *ctx, int32_t scene_id, int32_t precision, const float *q_dev, int64_t num_configs,
+                         double *dist_dev, float *profile_dev, float *nearest_dev, uint8_t *nearest_valid_dev,
+                         void *stream);
+/* computeDistanceUnderestimation (RealVectorSpace.cpp:402-446): per link, the
+ * smallest distance of its skeleton points to the planes through the obstacle
+ * points O of nearest_dev (layout as above) with normals (R - O)/|R - O|,
+ * minus the radius.  complete_dev[c] = 0 where the reference returns 0 at the
+ * first negative value without updating the state (dist 0, profile not
+ * written); otherwise dist_dev[c] and profile_dev[c][L] are the reference's
+ * d_c and profile.  Same precisions as rpm_distance_nearest. */
+int rpm_distance_underestimation(rpm_ctx *ctx, int32_t scene_id, int32_t precision, const float *q_dev,
+                                 int64_t num_configs, const float *nearest_dev, double *dist_dev, float *profile_dev,
+                                 uint8_t *complete_dev, void *stream);
+
 /* Skeleton points (L+1 points x 3) per configuration, widened to double
  * (computeSkeleton; xArm6.cpp:209-235, Planar2DOF.cpp:117-130): RPM_PREC_FP64
  * gives the FP64 points, RPM_PREC_FP32_REF the reference's float skeleton,

@@ -39,6 +39,8 @@ def lib():
         L.orc_prim_segseg.argtypes = [_f, _f, _f, _f, ctypes.c_int, _vp]
         L.orc_prim_segseg.restype = ctypes.c_double
         L.orc_box_aabb.argtypes = [_f, _f, _f, _f]
+        L.orc_distance_underest.argtypes = [_vp, ctypes.c_int, _f, ctypes.c_int64, ctypes.c_int, ctypes.c_int, _vp, _f,
+                                            _d, _f, _u8]
         _lib = L
     return _lib
 
@@ -114,6 +116,20 @@ def distance_nearest(robot, scene, q, prec="ref64", trig=0):
                                n, _p(q, _f), C, _prec(prec), trig, None, _p(dist, _d), _p(prof, _f), _p(near, _f),
                                _p(nv, _u8))
     return dist, prof, near, nv
+
+
+def distance_underestimation(robot, scene_n, q, nearest, prec="ref64", trig=0):
+    """computeDistanceUnderestimation from nearest points (C x n x 6 x L float32).
+    Returns (dist, profile, complete)."""
+    q = np.ascontiguousarray(q, np.float32)
+    nearest = np.ascontiguousarray(nearest, np.float32)
+    C, L = q.shape[0], robot.num_links
+    dist = np.zeros(C, np.float64)
+    prof = np.zeros((C, L), np.float32)
+    comp = np.zeros(C, np.uint8)
+    lib().orc_distance_underest(ctypes.byref(robot.desc), int(scene_n), _p(q, _f), C, _prec(prec), trig, None,
+                                _p(nearest, _f), _p(dist, _d), _p(prof, _f), _p(comp, _u8))
+    return dist, prof, comp
 
 
 def sincos(x, trig=0):

@@ -396,7 +396,7 @@ template <typename T> struct CapsuleBox {
             T tp[6];
             bool hp;
             T dt = seg_seg(nm, A, B, seg[k], seg[k + 1], tp, &hp);
-            if (dt <= 0) { d_c = 0; has_pts = false; return; }
+            if (dt <= 0) { d_c = 0; return; }   // the reference keeps its point matrix as it is
             else if (dt < d_c) { d_c = dt; std::memcpy(pts, tp, sizeof pts); has_pts = true; }
         }
     }
@@ -407,7 +407,7 @@ template <typename T> struct CapsuleBox {
         int face = -1;
         for (int f : order) if (proj[f][idx]) { face = f; break; }
         if (face < 0) return;
-        if (coll_rect(nm, A, B, T(0), obs, face)) { d_c = 0; has_pts = false; return; }
+        if (coll_rect(nm, A, B, T(0), obs, face)) { d_c = 0; return; }   // points left as they are
         int coord = face % 3;
         int a = (coord == 0) ? 1 : 0, b = (coord == 2) ? 1 : 2;
         T p0 = point[a], p1 = point[b];
@@ -493,7 +493,7 @@ template <typename T> struct CapsuleBox {
                 else if (A[2] > o[5] && B[2] > o[5]) { static const int c[4][3] = {{0, 1, 5}, {3, 1, 5}, {3, 4, 5}, {0, 4, 5}}; face_loop(c); }
                 else {
                     for (int kk = 0; kk < 6; ++kk)
-                        if (coll_rect(nm, A, B, T(0), obs, kk)) { d_c = 0; has_pts = false; return; }
+                        if (coll_rect(nm, A, B, T(0), obs, kk)) { d_c = 0; return; }   // points left as they are
                     // the 12 box edges: bottom loop, top loop, four verticals (:747-750)
                     static const int e12[24][3] = {
                         {0, 1, 2}, {3, 1, 2}, {3, 1, 2}, {3, 4, 2}, {3, 4, 2}, {0, 4, 2}, {0, 4, 2}, {0, 1, 2},
@@ -635,6 +635,50 @@ void config_one(const Num<T> &nm, const rpm_robot_desc &rb, const Scene<T> &sc, 
 
 }  // namespace
 
+// RealVectorSpace::computeDistanceUnderestimation (RealVectorSpace.cpp:402-446)
+// from given nearest points (n x 6 x L, the reference's vector<MatrixXf(6, L)>):
+// the distance of each link to the plane through the obstacle point O with
+// normal (R - O) / |R - O| (Eigen's normalized(): unchanged when |R - O| = 0),
+// minus the radius.  Pairs whose O has norm MAX_DISTANCE (the ground pairs the
+// ground rule skips) are passed over.  *complete is false when the reference
+// returns 0 at the first negative value without updating the state.
+template <typename T>
+T distance_underest(const Num<T> &nm, const rpm_robot_desc &rb, int n, const T *skel, const float *near, T *profile,
+                    bool *complete) {
+    const int L = rb.num_dofs;
+    T d_c = nm.maxd;
+    for (int i = 0; i < L; ++i) profile[i] = 0;
+    for (int i = 0; i < L; ++i) {
+        profile[i] = nm.maxd;
+        for (int j = 0; j < n; ++j) {
+            T O[3], R[3];
+            for (int k = 0; k < 3; ++k) {
+                R[k] = (T)near[((size_t)j * 6 + k) * L + i];
+                O[k] = (T)near[((size_t)j * 6 + 3 + k) * L + i];
+            }
+            if (std::sqrt(dot3(O, O)) == nm.maxd) continue;
+            T u[3] = {R[0] - O[0], R[1] - O[1], R[2] - O[2]};
+            const T z = dot3(u, u);
+            if (z > T(0)) {
+                const T nz = std::sqrt(z);
+                for (int k = 0; k < 3; ++k) u[k] = u[k] / nz;
+            }
+            const T *S0 = skel + 3 * i, *S1 = skel + 3 * (i + 1);
+            T a[3] = {S0[0] - O[0], S0[1] - O[1], S0[2] - O[2]};
+            T b[3] = {S1[0] - O[0], S1[1] - O[1], S1[2] - O[2]};
+            const T d = smin(dot3(a, u), dot3(b, u)) - (T)rb.capsule_radius[i];
+            if (d < T(0)) {
+                *complete = false;
+                return 0;
+            }
+            profile[i] = smin(profile[i], d);
+        }
+        d_c = smin(d_c, profile[i]);
+    }
+    *complete = true;
+    return d_c;
+}
+
 extern "C" {
 
 int orc_version(void) { return 1; }
@@ -723,6 +767,30 @@ int orc_distance_nearest(const rpm_robot_desc *rb, const float *aabb, const floa
             for (size_t k = 0; k < NS; ++k) nearest[c * NS + k] = (float)near[k];
         }
         nearest_valid[c] = nv ? 1 : 0;
+    }
+    return 0;
+}
+
+int orc_distance_underest(const rpm_robot_desc *rb, int n, const float *q, int64_t C, int prec, int trig,
+                          const rpm_params *params, const float *nearest, double *dist, float *profile,
+                          uint8_t *complete) {
+    const int D = rb->num_dofs, L = D;
+    const size_t NS = (size_t)n * 6 * L;
+    for (int64_t c = 0; c < C; ++c) {
+        double p64[3 * (RPM_MAX_DOF + 1)];
+        float p32[3 * (RPM_MAX_DOF + 1)];
+        skeleton(*rb, q + c * D, trig, p64, p32);
+        bool ok = false;
+        if (prec == 32) {
+            float prof[RPM_MAX_DOF];
+            dist[c] = distance_underest(num_of<float>(params), *rb, n, p32, nearest + c * NS, prof, &ok);
+            for (int i = 0; i < L; ++i) profile[c * L + i] = prof[i];
+        } else {
+            double prof[RPM_MAX_DOF];
+            dist[c] = distance_underest(num_of<double>(params), *rb, n, p64, nearest + c * NS, prof, &ok);
+            for (int i = 0; i < L; ++i) profile[c * L + i] = (float)prof[i];
+        }
+        complete[c] = ok ? 1 : 0;
     }
     return 0;
 }

@@ -16,6 +16,7 @@
 #include <vector>
 
 #include "rpm_ctx_impl.cuh"
+#include "rpm_nearest.cuh"
 
 using namespace rpm;
 
@@ -823,6 +824,82 @@ int rpm_check_edges(rpm_ctx *ctx, int32_t scene_id, int32_t precision, const flo
     CK(cudaEventRecord(e, st));
     buf.users.push_back(e);
     return RPM_OK;
+}
+
+// Shared set-up of the nearest-point and underestimation calls (caller holds ctx->mu).
+static int near_setup(rpm_ctx *ctx, int32_t scene_id, int32_t precision, const float *q, int64_t C, cudaStream_t st,
+                      NearParams &p, SceneBuf **used) {
+    if (precision < RPM_PREC_FP64 || precision > RPM_PREC_FP32_REF) return fail(RPM_ERR_INVALID, "unknown precision %d", precision);
+    SceneRec *s = find_scene(ctx, scene_id);
+    if (!s) return fail(RPM_ERR_INVALID, "unknown scene %d", scene_id);
+    if (set_device(ctx)) return RPM_ERR_CUDA;
+    SceneBuf &buf = s->bufs[s->cur];
+    if (buf.pending) {
+        if (cudaEventQuery(buf.ready) == cudaSuccess) buf.pending = false;
+        else CK(cudaStreamWaitEvent(st, buf.ready, 0));
+    }
+    std::memset(&p, 0, sizeof p);
+    p.robot = ctx->robots[s->robot].dev;
+    p.obs_f = buf.f;
+    p.obs_d = buf.d;
+    p.n = s->n;
+    p.n_pad = s->n_pad;
+    p.q = q;
+    p.C = C;
+    p.nmd.eq = ctx->params.equality_threshold;
+    p.nmd.maxd = ctx->params.max_distance;
+    p.nmf.eq = (float)ctx->params.equality_threshold;
+    p.nmf.maxd = (float)ctx->params.max_distance;
+    *used = &buf;
+    return RPM_OK;
+}
+
+static int near_done(rpm_ctx *ctx, SceneBuf *buf, cudaStream_t st) {
+    prune_users(ctx, *buf);
+    cudaEvent_t e = get_event(ctx);
+    CK(cudaEventRecord(e, st));
+    buf->users.push_back(e);
+    return RPM_OK;
+}
+
+int rpm_distance_nearest(rpm_ctx *ctx, int32_t scene_id, int32_t precision, const float *q_dev, int64_t num_configs,
+                         double *dist_dev, float *profile_dev, float *nearest_dev, uint8_t *nearest_valid_dev,
+                         void *stream) {
+    if (!ctx || num_configs < 0 || (num_configs > 0 && (!q_dev || !dist_dev || !profile_dev || !nearest_valid_dev)))
+        return fail(RPM_ERR_INVALID, "bad arguments");
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    cudaStream_t st = (cudaStream_t)stream;
+    NearParams p;
+    SceneBuf *buf = nullptr;
+    int rc = near_setup(ctx, scene_id, precision, q_dev, num_configs, st, p, &buf);
+    if (rc) return rc;
+    if (num_configs > 0 && p.n > 0 && !nearest_dev) return fail(RPM_ERR_INVALID, "NULL nearest-point buffer");
+    p.dist = dist_dev;
+    p.profile = profile_dev;
+    p.nearest = nearest_dev;
+    p.flag = nearest_valid_dev;
+    CK(launch_distance_nearest(precision == RPM_PREC_FP32_REF ? RPM_PREC_FP32_REF : RPM_PREC_FP64, p, st));
+    return near_done(ctx, buf, st);
+}
+
+int rpm_distance_underestimation(rpm_ctx *ctx, int32_t scene_id, int32_t precision, const float *q_dev,
+                                 int64_t num_configs, const float *nearest_dev, double *dist_dev, float *profile_dev,
+                                 uint8_t *complete_dev, void *stream) {
+    if (!ctx || num_configs < 0 || (num_configs > 0 && (!q_dev || !dist_dev || !profile_dev || !complete_dev)))
+        return fail(RPM_ERR_INVALID, "bad arguments");
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    cudaStream_t st = (cudaStream_t)stream;
+    NearParams p;
+    SceneBuf *buf = nullptr;
+    int rc = near_setup(ctx, scene_id, precision, q_dev, num_configs, st, p, &buf);
+    if (rc) return rc;
+    if (num_configs > 0 && p.n > 0 && !nearest_dev) return fail(RPM_ERR_INVALID, "NULL nearest-point buffer");
+    p.dist = dist_dev;
+    p.profile = profile_dev;
+    p.nearest = const_cast<float *>(nearest_dev);
+    p.flag = complete_dev;
+    CK(launch_distance_underest(precision == RPM_PREC_FP32_REF ? RPM_PREC_FP32_REF : RPM_PREC_FP64, p, st));
+    return near_done(ctx, buf, st);
 }
 
 int rpm_ctx_set_layout(rpm_ctx *ctx, int32_t layout) {

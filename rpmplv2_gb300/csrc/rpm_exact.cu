@@ -7,6 +7,7 @@
 #include "rpm_check.cuh"
 #include "rpm_edges.cuh"
 #include "rpm_launch.cuh"
+#include "rpm_nearest.cuh"
 #include "rpm_wide.cuh"
 
 namespace rpm {
@@ -593,6 +594,166 @@ cudaError_t launch_check_wide(int mode, const KParams &p, int64_t blocks, size_t
         if (!attr) { cudaFuncSetAttribute(k_check_wide<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024); attr = true; }
         k_check_wide<1><<<(unsigned)blocks, kWideThreads, smem, st>>>(p);
     }
+    return cudaGetLastError();
+}
+
+// ------------------------------------------------------ nearest points --
+// computeDistance(q, true) with nearest points (RealVectorSpace.cpp:318-392),
+// one warp per configuration: links in order, lanes over the obstacles, every
+// pair evaluated; the link minimum and the first hit (lowest obstacle index
+// with d <= 0 after the min_dist_tol clamp) are warp reductions.
+template <int MODE>
+__global__ void __launch_bounds__(kThreads) k_distance_nearest(const __grid_constant__ NearParams P) {
+    typedef typename std::conditional<MODE == 0, double, float>::type T;
+    __shared__ T skel[kThreads / 32][(kMaxDof + 1) * 3];
+    const unsigned full = 0xffffffffu;
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int64_t c = (int64_t)blockIdx.x * (kThreads / 32) + w;
+    if (c >= P.C) return;
+    const DevRobot &rb = *P.robot;
+    const int D = rb.D, L = D;
+    if (lane == 0) {
+        SkelWalker<MODE> sw;
+        sw.begin();
+        for (int k = 0; k <= D; ++k) sw.point(rb, P.q + c * D, k, skel[w] + 3 * k);
+    }
+    __syncwarp();
+    Num<T> nm;
+    if (MODE == 0) { nm.eq = (T)P.nmd.eq; nm.maxd = (T)P.nmd.maxd; }
+    else { nm.eq = (T)P.nmf.eq; nm.maxd = (T)P.nmf.maxd; }
+    const float *ground = P.obs_f + (size_t)kRowGround * P.n_pad;
+    float *near = P.nearest + (size_t)c * P.n * 6 * L;
+    T d_c = nm.maxd;
+    int hit = -1;
+    for (int i = 0; i < L && hit < 0; ++i) {
+        const T *A = skel[w] + 3 * i, *B = A + 3;
+        const T r = MODE == 0 ? (T)rb.radius_d[i] : (T)rb.radius_f[i];
+        T lmin = nm.maxd, hv = T(0);
+        int hj = 0x7fffffff;
+        for (int j = lane; j < P.n; j += 32) {
+            T d, pts[6];
+            bool has = true;
+            T tol;
+            if (ground[j] != 0.f && i < rb.ground_included) {
+                d = nm.maxd;
+                pts[0] = pts[1] = pts[2] = pts[3] = pts[4] = T(0);
+                pts[5] = -nm.maxd;
+                tol = MODE == 0 ? (T)P.obs_d[(size_t)kRowTol * P.n_pad + j] : (T)P.obs_f[(size_t)kRowTol * P.n_pad + j];
+            } else {
+                T o[6];
+                for (int k = 0; k < 6; ++k)
+                    o[k] = MODE == 0 ? (T)P.obs_d[(size_t)k * P.n_pad + j] : (T)P.obs_f[(size_t)k * P.n_pad + j];
+                tol = MODE == 0 ? (T)P.obs_d[(size_t)kRowTol * P.n_pad + j] : (T)P.obs_f[(size_t)kRowTol * P.n_pad + j];
+                d = capsule_box_pts(nm, A, B, r, o, pts, has);
+            }
+            if (d > tol) d = nm.maxd;   // :367-368
+            for (int k = 0; k < 6; ++k) near[((size_t)j * 6 + k) * L + i] = (float)pts[k];
+            lmin = smin(lmin, d);
+            if (d <= T(0) && j < hj) { hj = j; hv = d; }
+        }
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) {
+            lmin = smin(lmin, __shfl_xor_sync(full, lmin, off));
+            const int oj = __shfl_xor_sync(full, hj, off);
+            const T ov = __shfl_xor_sync(full, hv, off);
+            if (oj < hj) { hj = oj; hv = ov; }
+        }
+        if (hj != 0x7fffffff) {   // the reference returns at its first hit
+            hit = i;
+            if (lane == 0) P.profile[c * L + i] = (float)hv;
+        } else {
+            if (lane == 0) P.profile[c * L + i] = (float)lmin;
+            d_c = smin(d_c, lmin);
+        }
+    }
+    if (lane == 0) {
+        if (hit >= 0)
+            for (int k = hit + 1; k < L; ++k) P.profile[c * L + k] = 0.f;
+        P.dist[c] = hit >= 0 ? 0.0 : (double)d_c;
+        P.flag[c] = hit >= 0 ? 0 : 1;
+    }
+}
+
+// computeDistanceUnderestimation (RealVectorSpace.cpp:402-446) from the
+// nearest points in P.nearest: per link the smallest distance of its two
+// skeleton points to the planes through the obstacle points O with normals
+// (R - O) / |R - O| (Eigen's normalized(): unchanged when |R - O| = 0), minus
+// the radius; pairs whose O has norm MAX_DISTANCE are passed over.  The
+// reference returns 0 at the first negative value without updating the
+// state: flag 0, distance 0, profile not written.
+template <int MODE>
+__global__ void __launch_bounds__(kThreads) k_distance_underest(const __grid_constant__ NearParams P) {
+    typedef typename std::conditional<MODE == 0, double, float>::type T;
+    __shared__ T skel[kThreads / 32][(kMaxDof + 1) * 3];
+    __shared__ T prof[kThreads / 32][kMaxDof];
+    const unsigned full = 0xffffffffu;
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int64_t c = (int64_t)blockIdx.x * (kThreads / 32) + w;
+    if (c >= P.C) return;
+    const DevRobot &rb = *P.robot;
+    const int D = rb.D, L = D;
+    if (lane == 0) {
+        SkelWalker<MODE> sw;
+        sw.begin();
+        for (int k = 0; k <= D; ++k) sw.point(rb, P.q + c * D, k, skel[w] + 3 * k);
+    }
+    __syncwarp();
+    const T maxd = MODE == 0 ? (T)P.nmd.maxd : (T)P.nmf.maxd;
+    const float *near = P.nearest + (size_t)c * P.n * 6 * L;
+    T d_c = maxd;
+    bool negative = false;
+    for (int i = 0; i < L && !negative; ++i) {
+        const T *S0 = skel[w] + 3 * i, *S1 = S0 + 3;
+        const T r = MODE == 0 ? (T)rb.radius_d[i] : (T)rb.radius_f[i];
+        T lmin = maxd;
+        bool neg = false;
+        for (int j = lane; j < P.n; j += 32) {
+            T O[3], R[3];
+            for (int k = 0; k < 3; ++k) {
+                R[k] = (T)near[((size_t)j * 6 + k) * L + i];
+                O[k] = (T)near[((size_t)j * 6 + 3 + k) * L + i];
+            }
+            if (sqrtT(dot3(O, O)) == maxd) continue;
+            T u[3] = {R[0] - O[0], R[1] - O[1], R[2] - O[2]};
+            const T z = dot3(u, u);
+            if (z > T(0)) {
+                const T nz = sqrtT(z);
+                for (int k = 0; k < 3; ++k) u[k] = u[k] / nz;
+            }
+            T a[3] = {S0[0] - O[0], S0[1] - O[1], S0[2] - O[2]};
+            T b[3] = {S1[0] - O[0], S1[1] - O[1], S1[2] - O[2]};
+            const T d = smin(dot3(a, u), dot3(b, u)) - r;
+            if (d < T(0)) neg = true;
+            lmin = smin(lmin, d);
+        }
+        negative = __any_sync(full, neg);
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) lmin = smin(lmin, __shfl_xor_sync(full, lmin, off));
+        if (lane == 0) prof[w][i] = lmin;
+        d_c = smin(d_c, lmin);
+    }
+    __syncwarp();
+    if (negative) {
+        if (lane == 0) { P.dist[c] = 0.0; P.flag[c] = 0; }
+        return;
+    }
+    for (int i = lane; i < L; i += 32) P.profile[c * L + i] = (float)prof[w][i];
+    if (lane == 0) { P.dist[c] = (double)d_c; P.flag[c] = 1; }
+}
+
+cudaError_t launch_distance_nearest(int mode, const NearParams &p, cudaStream_t st) {
+    const unsigned grid = (unsigned)((p.C + kThreads / 32 - 1) / (kThreads / 32));
+    if (grid == 0) return cudaSuccess;
+    if (mode == RPM_PREC_FP32_REF) k_distance_nearest<1><<<grid, kThreads, 0, st>>>(p);
+    else k_distance_nearest<0><<<grid, kThreads, 0, st>>>(p);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_distance_underest(int mode, const NearParams &p, cudaStream_t st) {
+    const unsigned grid = (unsigned)((p.C + kThreads / 32 - 1) / (kThreads / 32));
+    if (grid == 0) return cudaSuccess;
+    if (mode == RPM_PREC_FP32_REF) k_distance_underest<1><<<grid, kThreads, 0, st>>>(p);
+    else k_distance_underest<0><<<grid, kThreads, 0, st>>>(p);
     return cudaGetLastError();
 }
 

@@ -57,6 +57,8 @@ def load(build_if_missing=False):
     L.rpm_check_edges.argtypes = [_vp, _i32, _i32, _vp, _vp, _i64, ctypes.c_float, _i32, _vp, _vp, _vp]
     L.rpm_ctx_set_graphs.argtypes = [_vp, ctypes.c_int]
     L.rpm_ctx_set_layout.argtypes = [_vp, ctypes.c_int32]
+    L.rpm_distance_nearest.argtypes = [_vp, _i32, _i32, _vp, _i64, _vp, _vp, _vp, _vp, _vp]
+    L.rpm_distance_underestimation.argtypes = [_vp, _i32, _i32, _vp, _i64, _vp, _vp, _vp, _vp, _vp]
     L.rpm_autotune_edges.argtypes = [_vp, _i32, _i32, _vp, _vp, _i64, ctypes.c_float, _i32, _vp, _pi32]
     L.rpm_set_edge_ctas.argtypes = [_vp, _i32, _i32, _i32]
     L.rpm_check_configs_host.argtypes = [_vp, _i32, _i32, _vp, _i64, _vp, _vp, _vp]
@@ -164,6 +166,19 @@ class Engine:
     def set_graphs(self, enable=True):
         _check(self.lib.rpm_ctx_set_graphs(self.ctx, 1 if enable else 0))
 
+    def distance_nearest(self, scene_id, q, dist, profile, nearest, nearest_valid, precision="fp64", stream=None):
+        """computeDistance with nearest points (torch CUDA tensors: q [C][D] float32, dist [C] float64,
+        profile [C][L] float32, nearest [C][n][6][L] float32, nearest_valid [C] uint8)."""
+        prec = PRECISIONS[precision] if isinstance(precision, str) else int(precision)
+        _check(self.lib.rpm_distance_nearest(self.ctx, scene_id, prec, _ptr(q), int(q.shape[0]), _ptr(dist),
+                                             _ptr(profile), _ptr(nearest), _ptr(nearest_valid), stream))
+
+    def distance_underestimation(self, scene_id, q, nearest, dist, profile, complete, precision="fp64", stream=None):
+        """computeDistanceUnderestimation from nearest points ([C][n][6][L] float32)."""
+        prec = PRECISIONS[precision] if isinstance(precision, str) else int(precision)
+        _check(self.lib.rpm_distance_underestimation(self.ctx, scene_id, prec, _ptr(q), int(q.shape[0]), _ptr(nearest),
+                                                     _ptr(dist), _ptr(profile), _ptr(complete), stream))
+
     def set_layout(self, layout="auto"):
         """Spread configuration checks one lane ('lane') or one warp ('warp')
         per configuration, or choose per segment ('auto').  Outputs do not
@@ -236,6 +251,7 @@ ABI_SYMBOLS = [
     "rpm_box_aabb", "rpm_check_configs", "rpm_check_configs_host", "rpm_skeleton", "rpm_last_stats", "rpm_sync",
     "rpm_ctx_set_timing", "rpm_last_timing", "rpm_probe_fp32_peak", "rpm_check_configs_noalloc", "rpm_check_batch",
     "rpm_check_edges", "rpm_ctx_set_graphs", "rpm_autotune_edges", "rpm_set_edge_ctas", "rpm_ctx_set_layout",
+    "rpm_distance_nearest", "rpm_distance_underestimation",
     "rpm_server_create", "rpm_server_submit", "rpm_server_poll", "rpm_server_wait", "rpm_server_release",
     "rpm_server_replay", "rpm_server_stats", "rpm_server_destroy",
 ]

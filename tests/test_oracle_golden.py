@@ -89,6 +89,12 @@ def test_primitives_against_reference_source():
         r = float(rng.choice([0.0, 0.03, 0.1]))
         P = lambda x: np.ascontiguousarray(x).ctypes.data_as(fp)
         assert R.ref_collision(P(a), P(b), r, P(o)) == O.prim_collision(a, b, r, o, "ref32")
-        rd = np.float32(R.ref_distance(P(a), P(b), r, P(o), None, None))
-        od = np.float32(O.prim_distance(a, b, r, o, "ref32")[0])
-        assert rd.tobytes() == od.tobytes()
+        rpts = np.zeros(6, np.float32)
+        rhas = ctypes.c_int()
+        rd = np.float32(R.ref_distance(P(a), P(b), r, P(o), P(rpts), ctypes.byref(rhas)))
+        od, opts, ohas = O.prim_distance(a, b, r, o, "ref32")
+        assert rd.tobytes() == np.float32(od).tobytes()
+        # the nearest points (robot point, obstacle point) of CapsuleToBox, or none
+        assert bool(rhas.value) == ohas
+        if ohas:
+            assert rpts.tobytes() == opts.tobytes(), (it, rpts, opts)
