@@ -41,8 +41,35 @@ def nvcc():
     return "nvcc"
 
 
+ADAPTER_DIR = os.path.join(HERE, "adapter")
+ADAPTER_LIB = os.path.join(OUT_DIR, "librpm_adapter.so")
+
+
+def adapter_flags():
+    """Include flags for code built on the RealVectorSpaceGPU adapter (its
+    StateSpace / State / Eigen stand-ins, the adapter and the C ABI)."""
+    return ["-I", os.path.join(ADAPTER_DIR, "shim"), "-I", ADAPTER_DIR, "-I", os.path.join(HERE, "..", "include")]
+
+
+def build_adapter(force=False):
+    """The C++ RealVectorSpaceGPU adapter as librpm_adapter.so (host code on the C ABI)."""
+    src = os.path.join(ADAPTER_DIR, "RealVectorSpaceGPU.cpp")
+    deps = [src, os.path.join(ADAPTER_DIR, "RealVectorSpaceGPU.h"), LIB]
+    if not force and os.path.exists(ADAPTER_LIB) and all(os.path.getmtime(f) <= os.path.getmtime(ADAPTER_LIB) for f in deps):
+        return ADAPTER_LIB
+    tmp = ADAPTER_LIB + ".tmp%d" % os.getpid()
+    cmd = [nvcc(), "-std=c++17", "-O2", "-Xcompiler", "-fPIC", "-shared", "-x", "c++", src, *adapter_flags(),
+           "-L", OUT_DIR, "-lrpm_gb300", "-Xlinker", "-rpath=" + OUT_DIR, "-lcudart", "-o", tmp]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("adapter build failed:\n%s%s" % (r.stdout, r.stderr))
+    os.replace(tmp, ADAPTER_LIB)
+    return ADAPTER_LIB
+
+
 def build(force=False, verbose=False):
     if not force and _up_to_date():
+        build_adapter()
         return LIB
     os.makedirs(OUT_DIR, exist_ok=True)
 
@@ -68,6 +95,7 @@ def build(force=False, verbose=False):
     if r.returncode != 0:
         raise RuntimeError("link failed:\n%s%s" % (r.stdout, r.stderr))
     os.replace(tmp, LIB)
+    build_adapter(force=True)
     return LIB
 
 

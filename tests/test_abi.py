@@ -59,3 +59,25 @@ def test_no_cpu_fallback_without_gpu():
     from rpmplv2_gb300.engine import Engine
     with pytest.raises(Exception):
         Engine(0)
+
+
+def test_adapter_library_defines_the_space(lib):
+    """librpm_adapter.so (base::RealVectorSpaceGPU over the StateSpace shim)
+    loads and defines the four overriding virtuals and the batched forms."""
+    from rpmplv2_gb300 import build
+    path = build.build_adapter()
+    ctypes.CDLL(path)
+    nm = shutil.which("nm")
+    if nm is None:
+        pytest.skip("nm not available")
+    import subprocess
+    syms = subprocess.run([nm, "-D", "-C", "--defined-only", path], capture_output=True, text=True, check=True).stdout
+    for name in ("RealVectorSpaceGPU::isValid(std::shared_ptr<base::State>)",
+                 "RealVectorSpaceGPU::isValid(std::shared_ptr<base::State>, std::shared_ptr<base::State>)",
+                 "RealVectorSpaceGPU::computeDistance(", "RealVectorSpaceGPU::computeDistanceUnderestimation(",
+                 "RealVectorSpaceGPU::isValidBatch(", "RealVectorSpaceGPU::computeDistanceBatch(",
+                 "RealVectorSpaceGPU::isValidEdgesBatch(", "RealVectorSpaceGPU::updateObstacles(",
+                 "vtable for base::RealVectorSpaceGPU"):
+        assert name in syms, name
+    undef = subprocess.run([nm, "-D", "--undefined-only", path], capture_output=True, text=True, check=True).stdout
+    assert "rpm_distance_nearest" in undef and "rpm_check_configs" in undef
