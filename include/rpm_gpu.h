@@ -186,6 +186,23 @@ int rpm_check_edges(rpm_ctx *ctx, int32_t scene_id, int32_t precision, const flo
                     int64_t num_edges, float step, int32_t num_checks, uint8_t *valid_dev, int32_t *checks_dev,
                     void *stream);
 int rpm_ctx_set_graphs(rpm_ctx *ctx, int enable);
+/* rpm_check_edges for several edge sets in one pipeline: each item has its
+ * own scene (and so robot, DOF count and obstacles), edges, discretisation
+ * and outputs, as rpm_check_edges.  Items are checked together (the
+ * batching form for uneven discretisations and mixed-DOF robots); each
+ * item's outputs equal what rpm_check_edges gives for it alone. */
+typedef struct rpm_edge_batch_item {
+    int32_t scene_id;
+    int32_t num_checks;
+    int64_t num_edges;
+    const float *q1_dev;      /* num_edges x D of the scene's robot */
+    const float *q2_dev;
+    float step;
+    uint8_t *valid_dev;
+    int32_t *checks_dev;      /* nullable */
+} rpm_edge_batch_item;
+int rpm_check_edges_batch(rpm_ctx *ctx, int32_t precision, const rpm_edge_batch_item *items, int32_t n_items,
+                          void *stream);
 /* Times the edge pipeline on the given batch for several persistent-grid
  * sizes (CTAs per SM) and keeps the fastest for this scene's robot and
  * precision; *ctas_out receives it.  rpm_set_edge_ctas sets it directly. */
@@ -232,8 +249,10 @@ int rpm_skeleton(rpm_ctx *ctx, int32_t robot_id, int32_t precision, const float 
  * against resident scenes while obstacles move (the DRGBT replanning shape,
  * DRGBT.cpp:79-176 with MotionValidity.cpp:30-53).  A worker thread admits
  * requests as device memory of the budget frees up, packs waiting
- * configuration requests from any scenes into one launch per free slot
- * (stream), so batches overlap on the device, and time-stamps each request.
+ * configuration and edge requests from any scenes and robots into one batch
+ * per free slot (stream): one launch for the configuration requests and one
+ * edge pipeline for the edge requests, so batches overlap on the device; it
+ * time-stamps each request.
  * Smaller requests are served first (requests waiting over 50 ms are served
  * as small); half of the slots are high-priority streams reserved for batches
  * of small requests, so a replanning query is not held behind a bulk batch.
@@ -243,8 +262,8 @@ typedef struct rpm_server_config {
     int32_t num_slots;           /* concurrent batches (streams), default 4 */
     int32_t precision;           /* RPM_PREC_* of every request */
     int64_t memory_budget;       /* device bytes for request buffers (admission), default 8 GiB */
-    int32_t max_batch_segments;  /* requests per launch, <= 32 */
-    int32_t max_batch_configs;   /* configurations per launch */
+    int32_t max_batch_segments;  /* configuration requests and edge requests per batch, each <= 32 */
+    int32_t max_batch_configs;   /* work per batch: configurations + 8 x edges (1/8 on high-priority slots) */
 } rpm_server_config;
 
 enum rpm_request_kind { RPM_REQ_CONFIGS = 0, RPM_REQ_EDGES = 1 };

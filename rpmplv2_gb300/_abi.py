@@ -68,3 +68,17 @@ class BatchItem(ctypes.Structure):
         ("dist_dev", ctypes.c_void_p),
         ("profile_dev", ctypes.c_void_p),
     ]
+
+
+class EdgeBatchItem(ctypes.Structure):
+    """rpm_edge_batch_item."""
+    _fields_ = [
+        ("scene_id", ctypes.c_int32),
+        ("num_checks", ctypes.c_int32),
+        ("num_edges", ctypes.c_int64),
+        ("q1_dev", ctypes.c_void_p),
+        ("q2_dev", ctypes.c_void_p),
+        ("step", ctypes.c_float),
+        ("valid_dev", ctypes.c_void_p),
+        ("checks_dev", ctypes.c_void_p),
+    ]

@@ -501,64 +501,107 @@ int edge_scratch(rpm_ctx *ctx, Scratch *sc, int64_t E, cudaStream_t st) {
     return RPM_OK;
 }
 
-// Queue the edge pipeline (counts + scan, persistent checks, recheck, final).
+// Queue the edge pipeline (counts + scan, the lane- and warp-layout passes,
+// recheck, final) for a batch of edge requests, kMaxSegs requests per launch.
+// The scratch must hold the batch's edges (edge_scratch).
+int enqueue_edge_batch(rpm_ctx *ctx, Scratch *sc, int prec, const std::vector<EdgeReq> &reqs, int ctas_per_sm,
+                       cudaStream_t st) {
+    std::vector<const EdgeReq *> order;   // lane-layout requests first
+    for (int wide = 0; wide < 2; ++wide)
+        for (const EdgeReq &r : reqs)
+            if (r.E > 0 && edge_warp_layout(ctx, r.scene) == (wide == 1)) order.push_back(&r);
+    const size_t tsz = prec == RPM_PREC_FP64 ? sizeof(double) : sizeof(float);
+    for (size_t first = 0; first < order.size(); first += kMaxSegs) {
+        const size_t last = std::min(order.size(), first + (size_t)kMaxSegs);
+        EdgeParams p;
+        std::memset(&p, 0, sizeof p);
+        int64_t E = 0, E_wide = 0;
+        int gmax = 32;
+        for (size_t i = first; i < last; ++i) {
+            const EdgeReq &r = *order[i];
+            SceneRec *s = r.scene;
+            SceneBuf &buf = s->bufs[s->cur];
+            if (buf.pending) {   // an incremental update still writing this version
+                if (cudaEventQuery(buf.ready) == cudaSuccess) buf.pending = false;
+                else CK(cudaStreamWaitEvent(st, buf.ready, 0));
+            }
+            const bool wide = edge_warp_layout(ctx, s);
+            EdgeSeg &es = p.segs[p.nseg];
+            if (!wide) p.nseg_lane = p.nseg + 1;
+            p.nseg++;
+            const int D = ctx->robots[s->robot].desc.num_dofs;
+            es.seg.robot = ctx->robots[s->robot].dev;
+            es.seg.obs_f = buf.f;
+            es.seg.obs_d = buf.d;
+            es.seg.n = s->n;
+            es.seg.n_pad = s->n_pad;
+            es.seg.srt_f = buf.sf;
+            es.seg.srt_d = buf.sd;
+            es.seg.blk = buf.blk;
+            es.seg.ns = s->ns;
+            es.seg.nb = s->nb;
+            es.seg.q = r.q1;
+            es.seg.count = r.E;
+            es.seg.valid = r.valid;
+            es.q2 = r.q2;
+            es.checks_out = r.checks;
+            es.e0 = E;
+            es.step = r.step;
+            es.num_checks = r.num_checks;
+            es.D = D;
+            E += r.E;
+            if (wide) {
+                E_wide += r.E;
+                gmax = std::min(gmax, kWidePtsBytes / ((D + 1) * 3 * (int)tsz));
+            }
+        }
+        if ((int64_t)sc->ecap < E) return fail(RPM_ERR_INVALID, "edge scratch below the batch's %lld edges", (long long)E);
+        p.E = E;
+        p.n_e = sc->n_e; p.local = sc->local; p.bprefix = sc->bprefix; p.kmax = sc->kmax; p.work = sc->work;
+        p.full = sc->full;
+        p.recheck = sc->erecheck;
+        p.recheck_cap = (uint32_t)std::min<size_t>(sc->erecheck_cap, 0xffffffffu);
+        p.recheck_count = sc->counters;
+        p.overflow = sc->counters + 1;
+        p.counters = sc->counters;
+        p.status = sc->status;
+        p.nmd.eq = ctx->params.equality_threshold; p.nmd.maxd = ctx->params.max_distance;
+        p.nmf.eq = (float)ctx->params.equality_threshold; p.nmf.maxd = (float)ctx->params.max_distance;
+        p.ps.pairs = sc->pairs;
+        p.ps.pair_count = sc->counters + 3;
+        p.ps.pair_cap = (uint32_t)sc->ppair_cap;
+        p.ps.cfg_cap = (uint32_t)sc->pcfg_cap;
+        p.ps.cfgs = sc->pcfgs;
+        p.ps.cfg_count = sc->counters + 2;
+        p.ps.skel = sc->pskel;
+        p.ps.acc = sc->pacc;
+        p.wide_g = std::max(1, gmax);
+        CK(launch_edge_prep(p, st));   // also zeroes the counters
+        if (p.nseg_lane > 0) {
+            const int grid = ctx->num_sms * std::max(1, ctas_per_sm);
+            const size_t smem = p.nseg_lane == 1
+                ? smem_bytes(prec == RPM_PREC_FP32_RECHECK ? RPM_PREC_FP32_REF : prec, p.segs[0].seg.n_pad) : 0;
+            if (prec == RPM_PREC_FP32_RECHECK) CK(launch_edges_fp32(p, grid, smem, st));
+            else CK(launch_edges(prec, p, grid, smem, st));
+        }
+        if (p.nseg_lane < p.nseg) {
+            // persistent: as many CTAs as fit (two per SM for the FP32 forms)
+            const int grid = ctx->num_sms * (prec == RPM_PREC_FP64 ? 1 : 2);
+            // edge streams pay off once every stream has a couple of edges to walk
+            p.streams = E_wide >= 2 * (int64_t)grid * kWideWarps * p.wide_g ? 1 : 0;
+            const Seg &sg = p.segs[p.nseg_lane].seg;
+            const size_t smem = p.nseg - p.nseg_lane == 1 ? wide_smem_bytes(prec, sg.ns, sg.nb)
+                                                          : (size_t)kWideWarps * kWidePtsBytes;
+            CK(launch_edges_wide(prec, p, grid, smem, st));
+        }
+        CK(launch_edge_recheck_final(p, ctx->num_sms * 4, prec == RPM_PREC_FP32_RECHECK, st));
+    }
+    return RPM_OK;
+}
+
 int enqueue_edges(rpm_ctx *ctx, Scratch *sc, SceneRec *s, int prec, const float *q1, const float *q2, int64_t E,
                   float step, int32_t num_checks, uint8_t *valid, int32_t *checks, int ctas_per_sm, cudaStream_t st) {
-    SceneBuf &buf = s->bufs[s->cur];
-    if (buf.pending) {
-        if (cudaEventQuery(buf.ready) == cudaSuccess) buf.pending = false;
-        else CK(cudaStreamWaitEvent(st, buf.ready, 0));
-    }
-    EdgeParams p;
-    std::memset(&p, 0, sizeof p);
-    p.seg.robot = ctx->robots[s->robot].dev;
-    p.seg.obs_f = buf.f;
-    p.seg.obs_d = buf.d;
-    p.seg.n = s->n;
-    p.seg.n_pad = s->n_pad;
-    p.seg.srt_f = buf.sf;
-    p.seg.srt_d = buf.sd;
-    p.seg.blk = buf.blk;
-    p.seg.ns = s->ns;
-    p.seg.nb = s->nb;
-    p.q1 = q1; p.q2 = q2; p.E = E; p.step = step; p.num_checks = num_checks;
-    p.n_e = sc->n_e; p.local = sc->local; p.bprefix = sc->bprefix; p.kmax = sc->kmax; p.work = sc->work;
-    p.full = sc->full;
-    p.recheck = sc->erecheck;
-    p.recheck_cap = (uint32_t)std::min<size_t>(sc->erecheck_cap, 0xffffffffu);
-    p.recheck_count = sc->counters;
-    p.overflow = sc->counters + 1;
-    p.valid = valid; p.checks_out = checks; p.status = sc->status;
-    p.nmd.eq = ctx->params.equality_threshold; p.nmd.maxd = ctx->params.max_distance;
-    p.nmf.eq = (float)ctx->params.equality_threshold; p.nmf.maxd = (float)ctx->params.max_distance;
-    p.ps.pairs = sc->pairs;
-    p.ps.pair_count = sc->counters + 3;
-    p.ps.pair_cap = (uint32_t)sc->ppair_cap;
-    p.ps.cfg_cap = (uint32_t)sc->pcfg_cap;
-    p.ps.cfgs = sc->pcfgs;
-    p.ps.cfg_count = sc->counters + 2;
-    p.ps.skel = sc->pskel;
-    p.ps.acc = sc->pacc;
-    const int D = ctx->robots[s->robot].desc.num_dofs;
-    const size_t tsz = prec == RPM_PREC_FP64 ? sizeof(double) : sizeof(float);
-    p.wide_g = std::max(1, std::min(32, kWidePtsBytes / ((D + 1) * 3 * (int)tsz)));
-    CK(cudaMemsetAsync(sc->counters, 0, 4 * sizeof(uint32_t), st));
-    if (E == 0) return RPM_OK;
-    CK(launch_edge_prep(p, st));
-    const bool wide = edge_warp_layout(ctx, s);
-    if (wide) {
-        // persistent: as many CTAs as fit (two per SM for the FP32 forms)
-        const int grid = ctx->num_sms * (prec == RPM_PREC_FP64 ? 1 : 2);
-        // edge streams pay off once every stream has a couple of edges to walk
-        p.streams = E >= 2 * (int64_t)grid * kWideWarps * p.wide_g ? 1 : 0;
-        CK(launch_edges_wide(prec, p, grid, wide_smem_bytes(prec, s->ns, s->nb), st));
-    } else {
-        const int grid = ctx->num_sms * std::max(1, ctas_per_sm);
-        if (prec == RPM_PREC_FP32_RECHECK) CK(launch_edges_fp32(p, grid, smem_bytes(RPM_PREC_FP32_REF, s->n_pad), st));
-        else CK(launch_edges(prec, p, grid, smem_bytes(prec, s->n_pad), st));
-    }
-    CK(launch_edge_recheck_final(p, ctx->num_sms * 4, prec == RPM_PREC_FP32_RECHECK, st));
-    return RPM_OK;
+    return enqueue_edge_batch(ctx, sc, prec, {EdgeReq{s, q1, q2, E, step, num_checks, valid, checks}}, ctas_per_sm, st);
 }
 
 int enqueue_check(rpm_ctx *ctx, SceneRec *s, int prec, const float *q, int64_t C, uint8_t *valid, double *dist,
@@ -763,6 +806,51 @@ int rpm_check_batch(rpm_ctx *ctx, int32_t precision, const rpm_batch_item *items
     }
     if (total >= (int64_t)1 << 40) return fail(RPM_ERR_RANGE, "too many configurations in one batch");
     return enqueue_segments(ctx, precision, reqs, (cudaStream_t)stream);
+}
+
+int rpm_check_edges_batch(rpm_ctx *ctx, int32_t precision, const rpm_edge_batch_item *items, int32_t n_items,
+                          void *stream) {
+    if (!ctx || (n_items > 0 && !items) || n_items < 0) return fail(RPM_ERR_INVALID, "bad edge batch");
+    if (precision < RPM_PREC_FP64 || precision > RPM_PREC_FP32_REF) return fail(RPM_ERR_INVALID, "unknown precision %d", precision);
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    if (set_device(ctx)) return RPM_ERR_CUDA;
+    std::vector<EdgeReq> reqs;
+    int64_t total = 0;
+    for (int k = 0; k < n_items; ++k) {
+        const rpm_edge_batch_item &it = items[k];
+        SceneRec *s = find_scene(ctx, it.scene_id);
+        if (!s) return fail(RPM_ERR_INVALID, "edge batch item %d: unknown scene %d", k, it.scene_id);
+        if (it.num_edges < 0 || (it.num_edges > 0 && (!it.q1_dev || !it.q2_dev || !it.valid_dev)))
+            return fail(RPM_ERR_INVALID, "edge batch item %d: bad edge buffers", k);
+        if (!(it.step > 0.f) && it.num_checks < 1)
+            return fail(RPM_ERR_INVALID, "edge batch item %d: need step > 0 or num_checks >= 1", k);
+        total += it.num_edges;
+        reqs.push_back(EdgeReq{s, it.q1_dev, it.q2_dev, it.num_edges, it.step, it.num_checks, it.valid_dev, it.checks_dev});
+    }
+    if (total >= (int64_t)1 << 40) return fail(RPM_ERR_RANGE, "too many edges in one batch");
+    if (total == 0) return RPM_OK;
+    cudaStream_t st = (cudaStream_t)stream;
+    Scratch *sc = nullptr;
+    int rc = get_scratch(ctx, st, total, &sc);
+    if (!rc) rc = edge_scratch(ctx, sc, total, st);
+    if (rc) return rc;
+    sc->last_configs = total;
+    sc->timed = false;
+    auto it = ctx->edge_ctas.find({reqs[0].scene->robot, precision});
+    rc = enqueue_edge_batch(ctx, sc, precision, reqs, it == ctx->edge_ctas.end() ? 4 : it->second, st);
+    if (rc) return rc;
+    std::vector<SceneBuf *> used;
+    for (const EdgeReq &r : reqs) {
+        SceneBuf *b = &r.scene->bufs[r.scene->cur];
+        if (std::find(used.begin(), used.end(), b) == used.end()) used.push_back(b);
+    }
+    for (SceneBuf *b : used) {
+        prune_users(ctx, *b);
+        cudaEvent_t e = get_event(ctx);
+        CK(cudaEventRecord(e, st));
+        b->users.push_back(e);
+    }
+    return RPM_OK;
 }
 
 int rpm_check_edges(rpm_ctx *ctx, int32_t scene_id, int32_t precision, const float *q1_dev, const float *q2_dev,

@@ -160,6 +160,18 @@ void free_scratch(Scratch *sc);   // stream work using it must be complete
 SceneRec *find_scene(rpm_ctx *ctx, int id);
 int enqueue_segments(rpm_ctx *ctx, int prec, const std::vector<SegReq> &reqs, cudaStream_t st);
 int edge_scratch(rpm_ctx *ctx, Scratch *sc, int64_t E, cudaStream_t st);
+// One edge request of a batched edge launch.
+struct EdgeReq {
+    SceneRec *scene;
+    const float *q1, *q2;
+    int64_t E;
+    float step;
+    int32_t num_checks;
+    uint8_t *valid;
+    int32_t *checks;
+};
+int enqueue_edge_batch(rpm_ctx *ctx, Scratch *sc, int prec, const std::vector<EdgeReq> &reqs, int ctas_per_sm,
+                       cudaStream_t st);
 int enqueue_edges(rpm_ctx *ctx, Scratch *sc, SceneRec *s, int prec, const float *q1, const float *q2, int64_t E,
                   float step, int32_t num_checks, uint8_t *valid, int32_t *checks, int ctas_per_sm, cudaStream_t st);
 int scene_update(rpm_ctx *ctx, SceneRec *s, const int32_t *idx, const float *aabb, int32_t m);

@@ -8,6 +8,10 @@
 // interpolation is an explicit round-to-nearest float op, so all arithmetic
 // forms check exactly the same configurations as the CPU restatement.
 //
+// A launch takes the edges of up to kMaxSegs requests (segments), each with
+// its own robot and scene; edges are numbered globally, segment-major, the
+// lane-layout segments first.
+//
 // Work: the checks of all edges are flattened (edge-major, k descending) and
 // taken 32 at a time by persistent warps from a global atomic counter.  Early
 // exit: each edge keeps kmax, the largest colliding k found so far; a check
@@ -16,29 +20,42 @@
 // number of checks the reference evaluates is n_e - kmax + 1.
 #pragma once
 #include "rpm_check.cuh"
+#include "rpm_launch.cuh"
 
 namespace rpm {
 
 constexpr int kEdgeScanBlock = 1024;   // edges per block of the count/scan pass
 
-struct EdgeParams {
-    Seg seg;                 // robot, scene rows, n, n_pad (q/count/outputs unused)
-    const float *q1, *q2;    // [E][D]
-    int64_t E;
+// One edge request of a launch: its robot and scene, its edges and outputs.
+// Edges of all segments are numbered globally (segment-major); segment s
+// holds the global edges [e0, e0 + seg.count).
+struct EdgeSeg {
+    Seg seg;                 // robot, scene rows; seg.q = q1 [E][D], seg.count = E, seg.valid = output
+    const float *q2;         // [E][D]
+    int32_t *checks_out;     // [E] checks in the reference's order (nullable)
+    int64_t e0;              // first global edge
     float step;              // > 0: n_e = max(1, ceil(dist / step))
     int32_t num_checks;      // step <= 0: fixed count per edge
+    int32_t D;
+    int32_t pad;
+};
+
+struct EdgeParams {
+    EdgeSeg segs[kMaxSegs];
+    int32_t nseg;
+    int32_t nseg_lane;       // segments [0, nseg_lane) run the lane layout, the rest the warp layout
+    int64_t E;               // edges of all segments
     int32_t *n_e;            // [E] checks per edge
     int32_t *local;          // [E] exclusive offset within its block of kEdgeScanBlock edges
     int64_t *bprefix;        // [blocks + 1] exclusive prefix of block totals; [blocks] = total
     int32_t *kmax;           // [E] largest colliding k (0 = none)
-    unsigned long long *work;    // flat-check work counter
+    unsigned long long *work;    // [2] work counters of the lane- and warp-layout passes
     uint64_t *recheck;       // unsettled checks (FP32 form): edge << 20 | k
     uint32_t *recheck_count;
     uint32_t recheck_cap;
     uint32_t *overflow;
+    uint32_t *counters;      // [4] zeroed by the count pass
     uint8_t *full;           // [E] edges whose unsettled checks did not fit the list: all rechecked in FP64
-    uint8_t *valid;          // [E] output
-    int32_t *checks_out;     // [E] checks in the reference's order (nullable)
     int32_t *status;
     Num<double> nmd;
     Num<float> nmf;
@@ -46,6 +63,22 @@ struct EdgeParams {
     int32_t wide_g;          // warp-per-check kernels: checks taken per warp
     int32_t streams;         // warp-per-check kernels: 1 = edge streams, 0 = flat checks
 };
+
+// Segment of global edge g (segments are few: a binary search over e0).
+RPM_HD int edge_seg(const EdgeParams &P, int64_t g) {
+    int lo = 0, hi = P.nseg - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (P.segs[mid].e0 <= g) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
+
+// First global edge of the warp-layout segments.
+RPM_HD int64_t edge_split(const EdgeParams &P) {
+    return P.nseg_lane < P.nseg ? P.segs[P.nseg_lane].e0 : P.E;
+}
 
 RPM_HD void edge_point(const float *a, const float *b, int D, float ratio, float *out) {
     for (int i = 0; i < D; ++i) out[i] = fadd(a[i], fmul(fadd(b[i], -a[i]), ratio));
@@ -78,6 +111,32 @@ RPM_HD void edge_config(const float *a, const float *b, int D, int N, int k, flo
     }
 }
 
+// Endpoints and check count of global edge g of segment s.
+struct EdgeGeom {
+    const float *a, *b;
+    int D, n;
+    float dist;
+};
+RPM_HD EdgeGeom edge_geom(const EdgeParams &P, int s, int64_t g) {
+    const EdgeSeg &es = P.segs[s];
+    EdgeGeom r;
+    r.D = es.D;
+    r.a = es.seg.q + (g - es.e0) * es.D;
+    r.b = es.q2 + (g - es.e0) * es.D;
+    r.n = edge_count(r.a, r.b, r.D, es.step, es.num_checks, r.dist);
+    return r;
+}
+
+// Views of a segment's robot and scene in global memory (launches of several
+// segments read them through L1 instead of staging one scene per CTA).
+template <typename T> RPM_HD ObsView<T> global_obs(const Seg &sg);
+template <> RPM_HD ObsView<double> global_obs<double>(const Seg &sg) {
+    return ObsView<double>{sg.obs_d, sg.obs_f + (size_t)kRowGround * sg.n_pad, sg.n, sg.n_pad};
+}
+template <> RPM_HD ObsView<float> global_obs<float>(const Seg &sg) {
+    return ObsView<float>{sg.obs_f, sg.obs_f + (size_t)kRowGround * sg.n_pad, sg.n, sg.n_pad};
+}
+
 #ifdef __CUDACC__
 // A check the FP32 pass could not settle through the pair recheck: recheck it
 // whole in FP64, or, when that list is full, every check of its edge.
@@ -95,54 +154,70 @@ __device__ __forceinline__ void edge_outcome(const EdgeParams &P, int64_t e, int
     else if (st == kSettled && v == 0) atomicMax(&P.kmax[e], k);
 }
 
-// Edge index of flat check 'idx': the last edge whose global offset <= idx.
-__device__ __forceinline__ int64_t edge_of_flat(const EdgeParams &P, int64_t idx) {
-    int64_t lo = 0, hi = P.E - 1;
+// Flat offset of global edge e's first check (e = E: the total).
+__device__ __forceinline__ int64_t flat_off(const EdgeParams &P, int64_t e) {
+    if (e >= P.E) return P.bprefix[(P.E + kEdgeScanBlock - 1) / kEdgeScanBlock];
+    return P.bprefix[e / kEdgeScanBlock] + P.local[e];
+}
+
+// Edge index of flat check 'idx': the last edge in [lo, hi] whose offset <= idx.
+__device__ __forceinline__ int64_t edge_of_flat(const EdgeParams &P, int64_t idx, int64_t lo, int64_t hi) {
     while (lo < hi) {
         const int64_t mid = (lo + hi + 1) >> 1;
-        const int64_t off = P.bprefix[mid / kEdgeScanBlock] + P.local[mid];
-        if (off <= idx) lo = mid;
+        if (flat_off(P, mid) <= idx) lo = mid;
         else hi = mid - 1;
     }
     return lo;
 }
 
-// The persistent edge kernel body for one arithmetic form.
+// The persistent lane-per-check pass over the lane-layout segments.  rb_st /
+// ob_st: the robot and scene staged in shared memory when the pass has one
+// segment, else null (each segment read from global memory).  A warp's 32
+// checks may span segments: they are checked one segment at a time.
 template <int MODE, typename T>
-__device__ void edge_warps(const EdgeParams &P, const DevRobot &rb, const ObsView<T> &ob, const Num<T> &nm,
+__device__ void edge_warps(const EdgeParams &P, const DevRobot *rb_st, const ObsView<T> *ob_st, const Num<T> &nm,
                            WarpShared<T> &sh, float *qbuf /* 32 x kMaxDof */) {
+    const unsigned full = 0xffffffffu;
     const int lane = threadIdx.x & 31;
-    const int D = rb.D;
-    const int64_t total = P.bprefix[(P.E + kEdgeScanBlock - 1) / kEdgeScanBlock];
+    const int64_t split = edge_split(P);
+    const int64_t total = flat_off(P, split);
     for (;;) {
         unsigned long long base = 0;
-        if (lane == 0) base = atomicAdd(P.work, 32ull);
-        base = __shfl_sync(0xffffffffu, base, 0);
+        if (lane == 0) base = atomicAdd(&P.work[0], 32ull);
+        base = __shfl_sync(full, base, 0);
         if ((int64_t)base >= total) break;
         const int64_t idx = (int64_t)base + lane;
         bool active = idx < total;
         int64_t e = 0;
-        int k = 0;
+        int k = 0, s = 0;
         if (active) {
-            e = edge_of_flat(P, idx);
-            const int64_t first = P.bprefix[e / kEdgeScanBlock] + P.local[e];
+            e = edge_of_flat(P, idx, 0, split - 1);
+            s = edge_seg(P, e);
             const int n = P.n_e[e];
-            k = n - (int)(idx - first);
+            k = n - (int)(idx - flat_off(P, e));
             if (k <= *(volatile int32_t *)&P.kmax[e]) active = false;   // a check nearer q2 already collides
             if (active) {
-                float dist;
-                edge_count(P.q1 + e * D, P.q2 + e * D, D, P.step, P.num_checks, dist);
-                edge_config(P.q1 + e * D, P.q2 + e * D, D, n, k, dist, qbuf + lane * kMaxDof);
+                const EdgeGeom gm = edge_geom(P, s, e);
+                edge_config(gm.a, gm.b, gm.D, n, k, gm.dist, qbuf + lane * kMaxDof);
             }
         }
         __syncwarp();
-        const Want w{true, false, false};
-        uint8_t v = 1;
-        int slot = -1;
-        const int st = warp_check<MODE, T>(sh, rb, ob, qbuf + lane * kMaxDof, active, nm, w, &v, nullptr, nullptr,
-                                           MODE == 2 ? &P.ps : nullptr, &slot);
-        if (active) edge_outcome<MODE>(P, e, k, st, slot, v);
-        __syncwarp();
+        unsigned todo = __ballot_sync(full, active);
+        while (todo) {
+            const int cur = __shfl_sync(full, s, __ffs(todo) - 1);
+            const bool mine = active && s == cur;
+            const unsigned m = __ballot_sync(full, mine);
+            const DevRobot &rb = rb_st ? *rb_st : *P.segs[cur].seg.robot;
+            const ObsView<T> ob = ob_st ? *ob_st : global_obs<T>(P.segs[cur].seg);
+            const Want w{true, false, false};
+            uint8_t v = 1;
+            int slot = -1;
+            const int st = warp_check<MODE, T>(sh, rb, ob, qbuf + lane * kMaxDof, mine, nm, w, &v, nullptr, nullptr,
+                                               MODE == 2 ? &P.ps : nullptr, &slot);
+            if (mine) edge_outcome<MODE>(P, e, k, st, slot, v);
+            todo &= ~m;
+            __syncwarp();
+        }
     }
 }
 #endif

@@ -244,54 +244,53 @@ __global__ void k_edge_pair_skel(const __grid_constant__ EdgeParams P) {
     __shared__ double sc[kThreads / 32][2 * kMaxDof];
     __shared__ float qs[kThreads / 32][kMaxDof];
     const uint32_t n = min(*P.ps.cfg_count, P.ps.cfg_cap);
-    const DevRobot &rb = *P.seg.robot;
-    const int D = rb.D;
     if (n <= gridDim.x * (blockDim.x / 32)) {   // few records: a warp each
         const int64_t k = spread_item(n);
         if (k < 0) return;
         const PairCfg c = P.ps.cfgs[k];
         if (c.status != kPairs) return;
+        const int s = edge_seg(P, c.config);
         const int w = threadIdx.x / 32;
         if ((threadIdx.x & 31) == 0) {
-            float dist;
-            const int N = edge_count(P.q1 + c.config * D, P.q2 + c.config * D, D, P.step, P.num_checks, dist);
-            edge_config(P.q1 + c.config * D, P.q2 + c.config * D, D, N, c.seg, dist, qs[w]);
+            const EdgeGeom gm = edge_geom(P, s, c.config);
+            edge_config(gm.a, gm.b, gm.D, gm.n, c.seg, gm.dist, qs[w]);
         }
         __syncwarp();
-        pair_skel_warp(rb, qs[w], P.ps.skel + (size_t)k * (kMaxDof + 1) * 3, P.ps.acc[k], sc[w]);
+        pair_skel_warp(*P.segs[s].seg.robot, qs[w], P.ps.skel + (size_t)k * (kMaxDof + 1) * 3, P.ps.acc[k], sc[w]);
         return;
     }
     for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
         const PairCfg c = P.ps.cfgs[k];
         if (c.status != kPairs) continue;
-        const int64_t e = c.config;
-        float dist, q[kMaxDof];
-        const int N = edge_count(P.q1 + e * D, P.q2 + e * D, D, P.step, P.num_checks, dist);
-        edge_config(P.q1 + e * D, P.q2 + e * D, D, N, c.seg, dist, q);
-        pair_skel_one(rb, q, P.ps.skel + (size_t)k * (kMaxDof + 1) * 3, P.ps.acc[k]);
+        const int s = edge_seg(P, c.config);
+        const EdgeGeom gm = edge_geom(P, s, c.config);
+        float q[kMaxDof];
+        edge_config(gm.a, gm.b, gm.D, gm.n, c.seg, gm.dist, q);
+        pair_skel_one(*P.segs[s].seg.robot, q, P.ps.skel + (size_t)k * (kMaxDof + 1) * 3, P.ps.acc[k]);
     }
 }
 
 __global__ void k_edge_pair_eval(const __grid_constant__ EdgeParams P) {
     const uint32_t n = min(*P.ps.pair_count, P.ps.pair_cap);
     const uint32_t ncfg = min(*P.ps.cfg_count, P.ps.cfg_cap);
-    ObsView<double> ob{P.seg.obs_d, P.seg.obs_f + (size_t)kRowGround * P.seg.n_pad, P.seg.n, P.seg.n_pad};
     if (n <= gridDim.x * (blockDim.x / 32)) {   // few pairs: a warp each (lane 0), spread over the SMs
         const int64_t k = spread_item(n);
         if (k < 0 || (threadIdx.x & 31) != 0) return;
         uint32_t slot;
         int link, j, kind;
         if (!decode_pair(P.ps, (uint32_t)k, ncfg, slot, link, j, kind)) return;
-        pair_eval_one(*P.seg.robot, ob, P.nmd, P.ps.skel + (size_t)slot * (kMaxDof + 1) * 3, link, j, kind,
-                      P.ps.acc[slot]);
+        const Seg &sg = P.segs[edge_seg(P, P.ps.cfgs[slot].config)].seg;
+        pair_eval_one(*sg.robot, global_obs<double>(sg), P.nmd, P.ps.skel + (size_t)slot * (kMaxDof + 1) * 3, link, j,
+                      kind, P.ps.acc[slot]);
         return;
     }
     for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
         uint32_t slot;
         int link, j, kind;
         if (!decode_pair(P.ps, k, ncfg, slot, link, j, kind)) continue;
-        pair_eval_one(*P.seg.robot, ob, P.nmd, P.ps.skel + (size_t)slot * (kMaxDof + 1) * 3, link, j, kind,
-                      P.ps.acc[slot]);
+        const Seg &sg = P.segs[edge_seg(P, P.ps.cfgs[slot].config)].seg;
+        pair_eval_one(*sg.robot, global_obs<double>(sg), P.nmd, P.ps.skel + (size_t)slot * (kMaxDof + 1) * 3, link, j,
+                      kind, P.ps.acc[slot]);
     }
 }
 
@@ -304,13 +303,13 @@ __global__ void k_edge_pair_fold(const __grid_constant__ EdgeParams P) {
 }
 
 // Warp-per-check edge pass (rpm_wide.cuh).
-template <int MODE>
+template <int MODE, bool MULTI>
 __global__ void __launch_bounds__(kWideThreads, MODE == 0 ? 1 : 2) k_edges_wide(const __grid_constant__ EdgeParams P) {
     extern __shared__ __align__(128) unsigned char smem[];
     __shared__ uint64_t bar;
     __shared__ MultiState<typename std::conditional<MODE == 0, double, float>::type> ms[kWideWarps];
     bulk_init(&bar);
-    edge_wide_body<MODE>(P, smem, &bar, ms);
+    edge_wide_body<MODE, MULTI>(P, smem, &bar, ms);
 }
 
 // 3. Fold per recorded configuration in the reference's link order: the
@@ -382,15 +381,16 @@ __global__ void k_skeleton(const DevRobot *rbp, const float *q, int64_t C, doubl
 
 // ---------------------------------------------------------------- edges --
 // Checks per edge and their exclusive offsets within blocks of kEdgeScanBlock
-// edges; block totals go to bprefix[b + 1] for the block scan.
+// edges; block totals go to bprefix[b + 1] for the block scan.  With a single
+// block the prefix is final here (no scan pass).  Zeroes the launch's counters.
 __global__ void __launch_bounds__(kEdgeScanBlock) k_edge_prep(const __grid_constant__ EdgeParams P) {
     __shared__ int32_t warp_sum[kEdgeScanBlock / 32];
     const int64_t e = (int64_t)blockIdx.x * kEdgeScanBlock + threadIdx.x;
-    const int D = P.seg.robot->D;
+    if (blockIdx.x == 0 && threadIdx.x < 4) P.counters[threadIdx.x] = 0u;
+    if (blockIdx.x == 0 && threadIdx.x < 2) P.work[threadIdx.x] = 0ull;
     int n = 0;
     if (e < P.E) {
-        float dist;
-        n = edge_count(P.q1 + e * D, P.q2 + e * D, D, P.step, P.num_checks, dist);
+        n = edge_geom(P, edge_seg(P, e), e).n;
         P.n_e[e] = n;
         P.kmax[e] = 0;
         P.full[e] = 0;
@@ -416,7 +416,10 @@ __global__ void __launch_bounds__(kEdgeScanBlock) k_edge_prep(const __grid_const
     __syncthreads();
     const int excl = x - n + (wid > 0 ? warp_sum[wid - 1] : 0);
     if (e < P.E) P.local[e] = excl;
-    if (threadIdx.x == kEdgeScanBlock - 1) P.bprefix[blockIdx.x + 1] = warp_sum[31];
+    if (threadIdx.x == kEdgeScanBlock - 1) {
+        P.bprefix[blockIdx.x + 1] = warp_sum[31];
+        if (gridDim.x == 1) P.bprefix[0] = 0;
+    }
 }
 
 // Exclusive scan of the block totals (one CTA; bprefix[0] = 0).
@@ -428,7 +431,6 @@ __global__ void k_edge_scan(const __grid_constant__ EdgeParams P, int nblocks) {
             acc += P.bprefix[b];
             P.bprefix[b] = acc;
         }
-        *P.work = 0ull;
     }
 }
 
@@ -439,17 +441,22 @@ __global__ void __launch_bounds__(kThreads) k_edges_exact(const __grid_constant_
     __shared__ uint64_t bar;
     __shared__ WarpShared<T> wsh[kThreads / 32];
     __shared__ float qbuf[kThreads / 32][32 * kMaxDof];
-    bulk_init(&bar);
-    if (!stage<MODE>(P.seg, smem, &bar, P.status)) return;
-    const DevRobot &rb = *reinterpret_cast<const DevRobot *>(smem);
-    const T *rows = reinterpret_cast<const T *>(smem + sizeof(DevRobot));
-    const float *ground = (MODE == 0) ? reinterpret_cast<const float *>(smem + sizeof(DevRobot) + kDRows * P.seg.n_pad * sizeof(double))
-                                      : reinterpret_cast<const float *>(rows) + (size_t)kRowGround * P.seg.n_pad;
-    ObsView<T> ob{rows, ground, P.seg.n, P.seg.n_pad};
     Num<T> nm;
     if (MODE == 0) { nm.eq = (T)P.nmd.eq; nm.maxd = (T)P.nmd.maxd; }
     else { nm.eq = (T)P.nmf.eq; nm.maxd = (T)P.nmf.maxd; }
-    edge_warps<MODE, T>(P, rb, ob, nm, wsh[threadIdx.x >> 5], qbuf[threadIdx.x >> 5]);
+    if (P.nseg_lane != 1) {   // several segments: robots and scenes from global memory
+        edge_warps<MODE, T>(P, nullptr, nullptr, nm, wsh[threadIdx.x >> 5], qbuf[threadIdx.x >> 5]);
+        return;
+    }
+    const Seg &sg = P.segs[0].seg;
+    bulk_init(&bar);
+    if (!stage<MODE>(sg, smem, &bar, P.status)) return;
+    const DevRobot &rb = *reinterpret_cast<const DevRobot *>(smem);
+    const T *rows = reinterpret_cast<const T *>(smem + sizeof(DevRobot));
+    const float *ground = (MODE == 0) ? reinterpret_cast<const float *>(smem + sizeof(DevRobot) + kDRows * sg.n_pad * sizeof(double))
+                                      : reinterpret_cast<const float *>(rows) + (size_t)kRowGround * sg.n_pad;
+    const ObsView<T> ob{rows, ground, sg.n, sg.n_pad};
+    edge_warps<MODE, T>(P, &rb, &ob, nm, wsh[threadIdx.x >> 5], qbuf[threadIdx.x >> 5]);
 }
 
 // FP64 recheck of the checks the FP32 edge pass left unsettled (one warp each).
@@ -458,22 +465,21 @@ __global__ void __launch_bounds__(kThreads) k_edge_recheck(const __grid_constant
     const uint32_t n = min(*P.recheck_count, P.recheck_cap);
     const uint32_t warps = gridDim.x * (blockDim.x / 32);
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    const DevRobot &rb = *P.seg.robot;
-    const int D = rb.D;
-    ObsView<double> ob{P.seg.obs_d, P.seg.obs_f + (size_t)kRowGround * P.seg.n_pad, P.seg.n, P.seg.n_pad};
     for (uint32_t it = blockIdx.x * (blockDim.x / 32) + wid; it < n; it += warps) {
         const uint64_t ent = P.recheck[it];
         const int64_t e = (int64_t)(ent >> 20);
         const int k = (int)(ent & 0xfffff);
         if (k <= *(volatile int32_t *)&P.kmax[e]) continue;
+        const int s = edge_seg(P, e);
         if (lane == 0) {
-            float dist;
-            const int N = edge_count(P.q1 + e * D, P.q2 + e * D, D, P.step, P.num_checks, dist);
-            edge_config(P.q1 + e * D, P.q2 + e * D, D, N, k, dist, qbuf[wid]);
+            const EdgeGeom gm = edge_geom(P, s, e);
+            edge_config(gm.a, gm.b, gm.D, gm.n, k, gm.dist, qbuf[wid]);
         }
         __syncwarp();
+        const Seg &sg = P.segs[s].seg;
         uint8_t v = 1;
-        config_exact_warp<0, double>(rb, ob, qbuf[wid], P.nmd, Want{true, false, false}, &v, nullptr, nullptr);
+        config_exact_warp<0, double>(*sg.robot, global_obs<double>(sg), qbuf[wid], P.nmd, Want{true, false, false}, &v,
+                                     nullptr, nullptr);
         v = (uint8_t)__shfl_sync(0xffffffffu, (int)v, 0);
         if (lane == 0 && v == 0) atomicMax(&P.kmax[e], k);
         __syncwarp();
@@ -487,21 +493,17 @@ __global__ void __launch_bounds__(kThreads) k_edge_full(const __grid_constant__ 
     if (*P.overflow == 0) return;
     const int64_t warps = (int64_t)gridDim.x * (blockDim.x / 32);
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    const DevRobot &rb = *P.seg.robot;
-    const int D = rb.D;
-    ObsView<double> ob{P.seg.obs_d, P.seg.obs_f + (size_t)kRowGround * P.seg.n_pad, P.seg.n, P.seg.n_pad};
     for (int64_t e = (int64_t)blockIdx.x * (blockDim.x / 32) + wid; e < P.E; e += warps) {
         if (!P.full[e]) continue;
-        const int N = P.n_e[e];
-        for (int k = N; k > P.kmax[e]; --k) {
-            if (lane == 0) {
-                float dist;
-                edge_count(P.q1 + e * D, P.q2 + e * D, D, P.step, P.num_checks, dist);
-                edge_config(P.q1 + e * D, P.q2 + e * D, D, N, k, dist, qbuf[wid]);
-            }
+        const int s = edge_seg(P, e);
+        const Seg &sg = P.segs[s].seg;
+        const EdgeGeom gm = edge_geom(P, s, e);
+        for (int k = gm.n; k > P.kmax[e]; --k) {
+            if (lane == 0) edge_config(gm.a, gm.b, gm.D, gm.n, k, gm.dist, qbuf[wid]);
             __syncwarp();
             uint8_t v = 1;
-            config_exact_warp<0, double>(rb, ob, qbuf[wid], P.nmd, Want{true, false, false}, &v, nullptr, nullptr);
+            config_exact_warp<0, double>(*sg.robot, global_obs<double>(sg), qbuf[wid], P.nmd, Want{true, false, false},
+                                         &v, nullptr, nullptr);
             v = (uint8_t)__shfl_sync(0xffffffffu, (int)v, 0);
             __syncwarp();
             if (v == 0) {
@@ -515,16 +517,18 @@ __global__ void __launch_bounds__(kThreads) k_edge_full(const __grid_constant__ 
 __global__ void k_edge_final(const __grid_constant__ EdgeParams P) {
     const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (e >= P.E) return;
+    const EdgeSeg &es = P.segs[edge_seg(P, e)];
+    const int64_t le = e - es.e0;
     const int km = P.kmax[e];
-    P.valid[e] = km == 0 ? 1 : 0;
-    if (P.checks_out) P.checks_out[e] = km == 0 ? P.n_e[e] : P.n_e[e] - km + 1;
+    es.seg.valid[le] = km == 0 ? 1 : 0;
+    if (es.checks_out) es.checks_out[le] = km == 0 ? P.n_e[e] : P.n_e[e] - km + 1;
 }
 
 cudaError_t launch_edge_prep(const EdgeParams &p, cudaStream_t st) {
     const int nb = (int)((p.E + kEdgeScanBlock - 1) / kEdgeScanBlock);
     if (nb == 0) return cudaSuccess;
     k_edge_prep<<<nb, kEdgeScanBlock, 0, st>>>(p);
-    k_edge_scan<<<1, 32, 0, st>>>(p, nb);
+    if (nb > 1) k_edge_scan<<<1, 32, 0, st>>>(p, nb);
     return cudaGetLastError();
 }
 
@@ -541,18 +545,19 @@ cudaError_t launch_edges(int mode, const EdgeParams &p, int grid, size_t smem, c
     return cudaGetLastError();
 }
 
-cudaError_t launch_edges_wide(int mode, const EdgeParams &p, int grid, size_t smem, cudaStream_t st) {
-    if (mode == RPM_PREC_FP32_RECHECK) return launch_edges_wide_fp32(p, grid, smem, st);
-    if (mode == RPM_PREC_FP64) {
-        static bool attr = false;
-        if (!attr) { cudaFuncSetAttribute(k_edges_wide<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024); attr = true; }
-        k_edges_wide<0><<<grid, kWideThreads, smem, st>>>(p);
-    } else {
-        static bool attr = false;
-        if (!attr) { cudaFuncSetAttribute(k_edges_wide<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024); attr = true; }
-        k_edges_wide<1><<<grid, kWideThreads, smem, st>>>(p);
-    }
+template <int MODE, bool MULTI>
+static cudaError_t launch_wide_edges(const EdgeParams &p, int grid, size_t smem, cudaStream_t st) {
+    static bool attr = false;
+    if (!attr) { cudaFuncSetAttribute(k_edges_wide<MODE, MULTI>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024); attr = true; }
+    k_edges_wide<MODE, MULTI><<<grid, kWideThreads, smem, st>>>(p);
     return cudaGetLastError();
+}
+
+cudaError_t launch_edges_wide(int mode, const EdgeParams &p, int grid, size_t smem, cudaStream_t st) {
+    const bool multi = p.nseg - p.nseg_lane > 1;
+    if (mode == RPM_PREC_FP32_RECHECK) return launch_edges_wide_fp32(p, grid, smem, st);
+    if (mode == RPM_PREC_FP64) return multi ? launch_wide_edges<0, true>(p, grid, smem, st) : launch_wide_edges<0, false>(p, grid, smem, st);
+    return multi ? launch_wide_edges<1, true>(p, grid, smem, st) : launch_wide_edges<1, false>(p, grid, smem, st);
 }
 
 cudaError_t launch_edge_recheck_final(const EdgeParams &p, int grid, bool pairs, cudaStream_t st) {

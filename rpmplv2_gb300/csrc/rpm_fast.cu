@@ -65,19 +65,25 @@ cudaError_t launch_check_wide_fp32(const KParams &p, int64_t blocks, size_t smem
     return cudaGetLastError();
 }
 
-// FP32 pass of the warp-per-check edge form.
+// FP32 pass of the warp-per-check edge form (MULTI: several segments).
+template <bool MULTI>
 __global__ void __launch_bounds__(kWideThreads, 2) k_edges_wide_fp32(const __grid_constant__ EdgeParams P) {
     extern __shared__ __align__(128) unsigned char smem[];
     __shared__ uint64_t bar;
     __shared__ MultiState<float> ms[kWideWarps];
     bulk_init(&bar);
-    edge_wide_body<2>(P, smem, &bar, ms);
+    edge_wide_body<2, MULTI>(P, smem, &bar, ms);
 }
 
 cudaError_t launch_edges_wide_fp32(const EdgeParams &p, int grid, size_t smem, cudaStream_t st) {
-    static bool attr = false;
-    if (!attr) { cudaFuncSetAttribute(k_edges_wide_fp32, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024); attr = true; }
-    k_edges_wide_fp32<<<grid, kWideThreads, smem, st>>>(p);
+    static bool attr[2] = {false, false};
+    if (p.nseg - p.nseg_lane > 1) {
+        if (!attr[1]) { cudaFuncSetAttribute(k_edges_wide_fp32<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024); attr[1] = true; }
+        k_edges_wide_fp32<true><<<grid, kWideThreads, smem, st>>>(p);
+    } else {
+        if (!attr[0]) { cudaFuncSetAttribute(k_edges_wide_fp32<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024); attr[0] = true; }
+        k_edges_wide_fp32<false><<<grid, kWideThreads, smem, st>>>(p);
+    }
     return cudaGetLastError();
 }
 
@@ -87,19 +93,24 @@ __global__ void __launch_bounds__(kThreads) k_edges_fp32(const __grid_constant__
     __shared__ uint64_t bar;
     __shared__ WarpShared<float> wsh[kThreads / 32];
     __shared__ float qbuf[kThreads / 32][32 * kMaxDof];
+    if (P.nseg_lane != 1) {   // several segments: robots and scenes from global memory
+        edge_warps<2, float>(P, nullptr, nullptr, P.nmf, wsh[threadIdx.x >> 5], qbuf[threadIdx.x >> 5]);
+        return;
+    }
+    const Seg &sg = P.segs[0].seg;
     bulk_init(&bar);
     if (threadIdx.x == 0) {
         const uint32_t rb = (uint32_t)sizeof(DevRobot);
-        const uint32_t rows = (uint32_t)(kFRows * P.seg.n_pad * sizeof(float));
+        const uint32_t rows = (uint32_t)(kFRows * sg.n_pad * sizeof(float));
         bulk_expect(&bar, rb + rows);
-        bulk_copy(&bar, smem, P.seg.robot, rb);
-        bulk_copy(&bar, smem + rb, P.seg.obs_f, rows);
+        bulk_copy(&bar, smem, sg.robot, rb);
+        bulk_copy(&bar, smem + rb, sg.obs_f, rows);
     }
     if (!bulk_wait(&bar, 0, P.status)) return;
     const DevRobot &rb = *reinterpret_cast<const DevRobot *>(smem);
     const float *rows = reinterpret_cast<const float *>(smem + sizeof(DevRobot));
-    ObsView<float> ob{rows, rows + (size_t)kRowGround * P.seg.n_pad, P.seg.n, P.seg.n_pad};
-    edge_warps<2, float>(P, rb, ob, P.nmf, wsh[threadIdx.x >> 5], qbuf[threadIdx.x >> 5]);
+    const ObsView<float> ob{rows, rows + (size_t)kRowGround * sg.n_pad, sg.n, sg.n_pad};
+    edge_warps<2, float>(P, &rb, &ob, P.nmf, wsh[threadIdx.x >> 5], qbuf[threadIdx.x >> 5]);
 }
 
 cudaError_t launch_edges_fp32(const EdgeParams &p, int grid, size_t smem, cudaStream_t st) {

@@ -8,11 +8,13 @@
 //   * admits requests in arrival order as device memory of the budget frees up
 //     (a request larger than the whole budget is rejected), skipping over
 //     requests that do not fit yet so small ones are not held behind large ones;
-//   * packs admitted configuration requests -- from any scenes and robots --
-//     into one multi-segment launch per free slot (a slot is a stream), so new
-//     requests join the next batch while earlier batches still run and batches
-//     overlap on the device;
-//   * runs edge requests as their own pipeline on a slot;
+//   * packs admitted requests -- from any scenes and robots, configuration and
+//     edge requests alike -- into one batch per free slot (a slot is a
+//     stream): one multi-segment launch for the configuration requests and one
+//     multi-segment edge pipeline for the edge requests, so new requests join
+//     the next batch while earlier batches still run and batches overlap on
+//     the device.  A batch holds at most max_batch_configs units of work (an
+//     edge counts 8), an eighth of that on the high-priority slots;
 //   * retires batches by CUDA events, frees their memory and time-stamps every
 //     request (submit, admit, launch, done).
 // Each request's result is what the same check gives alone: configurations are
@@ -240,16 +242,20 @@ int launch_batch(rpm_server *srv, Slot &slot, const std::vector<Req *> &batch) {
     std::lock_guard<std::mutex> lk(ctx->mu);
     if (set_device(ctx)) return RPM_ERR_CUDA;
     std::vector<SegReq> segs;
+    std::vector<EdgeReq> edges;
+    int64_t n_edges = 0;
     for (Req *q : batch) {
         const DevBufs d = layout(srv, q);
         const size_t n = (size_t)q->r.count;
+        SceneRec *s = find_scene(ctx, q->r.scene_id);
+        if (!s) return fail(RPM_ERR_INVALID, "unknown scene %d", q->r.scene_id);
         if (q->r.kind == RPM_REQ_EDGES) {
             CK(cudaMemcpyAsync(d.q1, q->r.q1_host, n * q->D * sizeof(float), cudaMemcpyHostToDevice, slot.st));
             CK(cudaMemcpyAsync(d.q2, q->r.q2_host, n * q->D * sizeof(float), cudaMemcpyHostToDevice, slot.st));
+            edges.push_back(EdgeReq{s, d.q1, d.q2, (int64_t)n, q->r.step, q->r.num_checks, d.valid, d.checks});
+            n_edges += (int64_t)n;
         } else {
             CK(cudaMemcpyAsync(d.q, q->r.q_host, n * q->D * sizeof(float), cudaMemcpyHostToDevice, slot.st));
-            SceneRec *s = find_scene(ctx, q->r.scene_id);
-            if (!s) return fail(RPM_ERR_INVALID, "unknown scene %d", q->r.scene_id);
             segs.push_back(SegReq{s, d.q, (int64_t)n, d.valid, d.dist, d.profile});
         }
     }
@@ -257,25 +263,28 @@ int launch_batch(rpm_server *srv, Slot &slot, const std::vector<Req *> &batch) {
         const int rc = enqueue_segments(ctx, srv->cfg.precision, segs, slot.st);
         if (rc) return rc;
     }
-    for (Req *q : batch) {
-        if (q->r.kind != RPM_REQ_EDGES) continue;
-        SceneRec *s = find_scene(ctx, q->r.scene_id);
-        if (!s) return fail(RPM_ERR_INVALID, "unknown scene %d", q->r.scene_id);
-        const DevBufs d = layout(srv, q);
+    if (n_edges > 0) {
+        // every edge request of the batch in one pipeline (up to kMaxSegs requests per launch)
         Scratch *sc = nullptr;
         int rc = get_scratch(ctx, slot.st, 0, &sc);
-        if (!rc) rc = edge_scratch(ctx, sc, q->r.count, slot.st);
+        if (!rc) rc = edge_scratch(ctx, sc, n_edges, slot.st);
         if (!rc) {
-            auto it = ctx->edge_ctas.find({s->robot, srv->cfg.precision});
-            rc = enqueue_edges(ctx, sc, s, srv->cfg.precision, d.q1, d.q2, q->r.count, q->r.step, q->r.num_checks, d.valid,
-                               d.checks, it == ctx->edge_ctas.end() ? 4 : it->second, slot.st);
+            auto it = ctx->edge_ctas.find({edges[0].scene->robot, srv->cfg.precision});
+            rc = enqueue_edge_batch(ctx, sc, srv->cfg.precision, edges, it == ctx->edge_ctas.end() ? 4 : it->second,
+                                    slot.st);
         }
         if (rc) return rc;
-        SceneBuf &buf = s->bufs[s->cur];
-        prune_users(ctx, buf);
-        cudaEvent_t e = get_event(ctx);
-        CK(cudaEventRecord(e, slot.st));
-        buf.users.push_back(e);
+        std::vector<SceneBuf *> used;
+        for (const EdgeReq &r : edges) {
+            SceneBuf *b = &r.scene->bufs[r.scene->cur];
+            if (std::find(used.begin(), used.end(), b) == used.end()) used.push_back(b);
+        }
+        for (SceneBuf *b : used) {
+            prune_users(ctx, *b);
+            cudaEvent_t e = get_event(ctx);
+            CK(cudaEventRecord(e, slot.st));
+            b->users.push_back(e);
+        }
     }
     for (Req *q : batch) {
         const DevBufs d = layout(srv, q);
@@ -344,24 +353,25 @@ void worker_loop(rpm_server *srv) {
         for (Slot &sl : srv->slots) {
             if (srv->ready.empty()) break;
             if (sl.busy) continue;
+            // work cap of the batch: small on the high-priority slots so their
+            // requests finish quickly; configuration and edge requests mix
+            const int64_t cap = sl.small ? std::max<int64_t>(1, srv->cfg.max_batch_configs / 8) : srv->cfg.max_batch_configs;
             std::vector<Req *> batch;
-            int64_t configs = 0;
-            int segs = 0;
+            int64_t work = 0;
+            int nseg = 0, nedge = 0;
             for (auto it = srv->ready.begin(); it != srv->ready.end();) {
                 Req *q = *it;
                 const bool edge = q->r.kind == RPM_REQ_EDGES;
                 const bool small = work_of(q) <= kSmallRequest || tnow - q->t.t_submit > kAgeBoost;
                 if (sl.small && !small) { ++it; continue; }
-                if (!batch.empty() && (segs >= srv->cfg.max_batch_segments ||
-                                       configs + q->r.count > srv->cfg.max_batch_configs || edge)) {
+                if (!batch.empty() && (work + work_of(q) > cap || (edge ? nedge : nseg) >= srv->cfg.max_batch_segments)) {
                     ++it;
                     continue;
                 }
                 batch.push_back(q);
-                configs += q->r.count;
-                segs += edge ? 0 : 1;
+                work += work_of(q);
+                (edge ? nedge : nseg) += 1;
                 it = srv->ready.erase(it);
-                if (edge) break;   // an edge pipeline takes the slot to itself
             }
             if (batch.empty()) continue;
             sl.busy = true;   // reserved: only this thread touches the slot
@@ -433,6 +443,7 @@ int rpm_server_create(rpm_ctx *ctx, const rpm_server_config *cfg, rpm_server **o
             CK(cudaEventCreateWithFlags(&sl.done, cudaEventDisableTiming));
             Scratch *sc = nullptr;   // pre-size scratch so the loop never allocates
             int rc = get_scratch(ctx, sl.st, c.max_batch_configs, &sc);
+            if (!rc) rc = edge_scratch(ctx, sc, c.max_batch_configs / 4, sl.st);
             if (rc) return rc;
         }
     }

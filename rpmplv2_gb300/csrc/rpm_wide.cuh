@@ -785,69 +785,102 @@ __device__ __forceinline__ void wide_kernel_body(const KParams &P, unsigned char
 // sets the edge's largest colliding k and ends the stream (the reference
 // stops there); a check left to the FP64 recheck does not stop it, since a
 // collision further down still has to be found.  Finished streams take the
-// next edge from a global counter.
-template <int MODE>
+// next edge from a global counter.  The pass covers the warp-layout segments
+// (edges from edge_split on); lanes of different segments are checked one
+// segment at a time, each against its own robot and sorted scene (staged in
+// shared memory when the pass has a single segment).
+template <int MODE, bool MULTI>
 __device__ __forceinline__ void edge_wide_body(const EdgeParams &P, unsigned char *smem, uint64_t *bar,
                                                MultiState<typename std::conditional<MODE == 0, double, float>::type> *ms) {
     typedef typename std::conditional<MODE == 0, double, float>::type T;
-    const Seg &sg = P.seg;
-    const WideLayout L = WideLayout::of(MODE == 0 ? RPM_PREC_FP64 : RPM_PREC_FP32_REF, sg.ns, sg.nb);
-    if (!wide_stage<MODE>(sg, L, smem, bar, P.status)) return;
-    const DevRobot &rb = *reinterpret_cast<const DevRobot *>(smem);
-    SortedView<T> ob{reinterpret_cast<const T *>(smem + L.rows), reinterpret_cast<const uint32_t *>(smem + L.idx),
-                     reinterpret_cast<const float *>(smem + L.blk), sg.ns, sg.nb};
+    const int s_lo = P.nseg_lane;
+    constexpr bool staged = !MULTI;   // one segment: its robot and sorted scene in shared memory
+    const DevRobot *rb_st = nullptr;
+    SortedView<T> ob_st{nullptr, nullptr, nullptr, 0, 0};
+    uint32_t pts_off = 0;
+    if (staged) {
+        const Seg &sg = P.segs[s_lo].seg;
+        const WideLayout L = WideLayout::of(MODE == 0 ? RPM_PREC_FP64 : RPM_PREC_FP32_REF, sg.ns, sg.nb);
+        if (!wide_stage<MODE>(sg, L, smem, bar, P.status)) return;
+        rb_st = reinterpret_cast<const DevRobot *>(smem);
+        ob_st = SortedView<T>{reinterpret_cast<const T *>(smem + L.rows), reinterpret_cast<const uint32_t *>(smem + L.idx),
+                              reinterpret_cast<const float *>(smem + L.blk), sg.ns, sg.nb};
+        pts_off = L.pts;
+    }
     const unsigned full = 0xffffffffu;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int G = P.wide_g;
-    const int D = rb.D;
-    T *pts = reinterpret_cast<T *>(smem + L.pts + warp * kWidePtsBytes);
+    T *pts = reinterpret_cast<T *>(smem + pts_off + warp * kWidePtsBytes);
     Num<T> nm;
     if (MODE == 0) { nm.eq = (T)P.nmd.eq; nm.maxd = (T)P.nmd.maxd; }
     else { nm.eq = (T)P.nmf.eq; nm.maxd = (T)P.nmf.maxd; }
+    const int64_t e_lo = edge_split(P);
+    // One segment's checks of the lanes in 'live' (skeletons first, then the
+    // joint obstacle walk); returns this lane's outcome.
+    auto check_seg = [&](int cur, bool mine, const float *q, uint8_t &v, int &st, int &slot) {
+        const unsigned live = __ballot_sync(full, mine);
+        const DevRobot &rb = staged ? *rb_st : *P.segs[cur].seg.robot;
+        const Seg &sg = P.segs[cur].seg;
+        const SortedView<T> ob = staged ? ob_st
+                                        : SortedView<T>{MODE == 0 ? reinterpret_cast<const T *>(sg.srt_d)
+                                                                  : reinterpret_cast<const T *>(sg.srt_f),
+                                                        reinterpret_cast<const uint32_t *>(sg.srt_f + (size_t)7 * sg.ns),
+                                                        sg.blk, sg.ns, sg.nb};
+        const int D = P.segs[cur].D;
+        if (mine) {
+            SkelWalker<MODE> sw;
+            sw.begin();
+            T *p = pts + lane * (D + 1) * 3;
+            for (int t = 0; t <= D; ++t) sw.point(rb, q, t, p + 3 * t);
+        }
+        __syncwarp();
+        double dd;
+        int hl, hj;
+        wide_multi_np<MODE, T>(ms[warp], rb, ob, pts, (D + 1) * 3, G, live, nm, Want{true, false, false},
+                               MODE == 2 ? &P.ps : nullptr, v, dd, st, slot, hl, hj);
+        __syncwarp();
+        return live;
+    };
     if (!P.streams) {
         // small batches: every check of every edge in parallel, G consecutive
         // flat checks (edge-major, k descending) per warp at a time
-        const int64_t total = P.bprefix[(P.E + kEdgeScanBlock - 1) / kEdgeScanBlock];
+        const int64_t f_lo = flat_off(P, e_lo), f_hi = flat_off(P, P.E);
         for (;;) {
             unsigned long long base = 0;
-            if (lane == 0) base = atomicAdd(P.work, (unsigned long long)G);
+            if (lane == 0) base = atomicAdd(&P.work[1], (unsigned long long)G);
             base = __shfl_sync(full, base, 0);
-            if ((int64_t)base >= total) break;
+            if (f_lo + (int64_t)base >= f_hi) break;
             int64_t e = 0;
-            int k = 0;
+            int k = 0, s = 0;
             bool act = false;
-            if (lane < G && (int64_t)base + lane < total) {
-                const int64_t idx = (int64_t)base + lane;
-                e = edge_of_flat(P, idx);
-                const int64_t first = P.bprefix[e / kEdgeScanBlock] + P.local[e];
+            float q[kMaxDof];
+            if (lane < G && f_lo + (int64_t)base + lane < f_hi) {
+                const int64_t idx = f_lo + (int64_t)base + lane;
+                e = edge_of_flat(P, idx, e_lo, P.E - 1);
+                s = MULTI ? edge_seg(P, e) : s_lo;
                 const int n = P.n_e[e];
-                k = n - (int)(idx - first);
+                k = n - (int)(idx - flat_off(P, e));
                 act = k > *(volatile int32_t *)&P.kmax[e];   // a check nearer q2 already collides
                 if (act) {
-                    float dist, q[kMaxDof];
-                    edge_count(P.q1 + e * D, P.q2 + e * D, D, P.step, P.num_checks, dist);
-                    edge_config(P.q1 + e * D, P.q2 + e * D, D, n, k, dist, q);
-                    SkelWalker<MODE> sw;
-                    sw.begin();
-                    T *p = pts + lane * (D + 1) * 3;
-                    for (int t = 0; t <= D; ++t) sw.point(rb, q, t, p + 3 * t);
+                    const EdgeGeom gm = edge_geom(P, s, e);
+                    edge_config(gm.a, gm.b, gm.D, n, k, gm.dist, q);
                 }
             }
-            __syncwarp();
-            const unsigned live = __ballot_sync(full, act);
-            if (live == 0u) continue;
-            uint8_t v;
-            double dd;
-            int st, slot, hl, hj;
-            wide_multi_np<MODE, T>(ms[warp], rb, ob, pts, (D + 1) * 3, G, live, nm, Want{true, false, false},
-                                   MODE == 2 ? &P.ps : nullptr, v, dd, st, slot, hl, hj);
-            if (act) edge_outcome<MODE>(P, e, k, st, slot, v);
-            __syncwarp();
+            unsigned todo = __ballot_sync(full, act);
+            while (todo) {
+                const int cur = MULTI ? __shfl_sync(full, s, __ffs(todo) - 1) : s_lo;
+                const bool mine = MULTI ? (act && s == cur) : act;
+                uint8_t v;
+                int st, slot;
+                todo &= ~check_seg(cur, mine, q, v, st, slot);
+                if (mine) edge_outcome<MODE>(P, e, k, st, slot, v);
+                if (!MULTI) break;
+            }
         }
         return;
     }
     int64_t e = -1;      // this lane's edge (-1: none)
-    int k = 0, n = 0;    // its current check and check count
+    int k = 0, n = 0, s = 0;   // its current check, check count and segment
     float dist = 0.f;
     bool more = true;    // edges left to take (warp-uniform)
     for (;;) {
@@ -855,43 +888,45 @@ __device__ __forceinline__ void edge_wide_body(const EdgeParams &P, unsigned cha
         const unsigned nmask = __ballot_sync(full, need);
         if (nmask) {
             unsigned long long base = 0;
-            if (lane == 0) base = atomicAdd(P.work, (unsigned long long)__popc(nmask));
+            if (lane == 0) base = atomicAdd(&P.work[1], (unsigned long long)__popc(nmask));
             base = __shfl_sync(full, base, 0);
             if (need) {
-                const int64_t idx = (int64_t)base + __popc(nmask & ((1u << lane) - 1u));
+                const int64_t idx = e_lo + (int64_t)base + __popc(nmask & ((1u << lane) - 1u));
                 if (idx < P.E) {
                     e = idx;
-                    n = edge_count(P.q1 + e * D, P.q2 + e * D, D, P.step, P.num_checks, dist);
+                    s = MULTI ? edge_seg(P, e) : s_lo;
+                    const EdgeGeom gm = edge_geom(P, s, e);
+                    n = gm.n;
+                    dist = gm.dist;
                     k = n;
                 }
             }
-            if ((int64_t)base + __popc(nmask) >= P.E) more = false;
+            if (e_lo + (int64_t)base + __popc(nmask) >= P.E) more = false;
         }
-        const unsigned live = __ballot_sync(full, lane < G && e >= 0);
-        if (live == 0u) {
+        const bool has = lane < G && e >= 0;
+        unsigned todo = __ballot_sync(full, has);
+        if (todo == 0u) {
             if (!more) break;
             continue;
         }
-        if (e >= 0) {
+        while (todo) {
+            const int cur = MULTI ? __shfl_sync(full, s, __ffs(todo) - 1) : s_lo;
+            const bool mine = MULTI ? (has && s == cur) : has;
             float q[kMaxDof];
-            edge_config(P.q1 + e * D, P.q2 + e * D, D, n, k, dist, q);
-            SkelWalker<MODE> sw;
-            sw.begin();
-            T *p = pts + lane * (D + 1) * 3;
-            for (int t = 0; t <= D; ++t) sw.point(rb, q, t, p + 3 * t);
+            if (mine) {
+                const EdgeSeg &es = P.segs[cur];
+                edge_config(es.seg.q + (e - es.e0) * es.D, es.q2 + (e - es.e0) * es.D, es.D, n, k, dist, q);
+            }
+            uint8_t v;
+            int st, slot;
+            todo &= ~check_seg(cur, mine, q, v, st, slot);
+            if (mine) {
+                edge_outcome<MODE>(P, e, k, st, slot, v);
+                if (st == kSettled && v == 0) e = -1;    // the reference's first collision: the edge is done
+                else if (--k < 1) e = -1;                // every check clear (or left to the recheck)
+            }
+            if (!MULTI) break;
         }
-        __syncwarp();
-        uint8_t v;
-        double dd;
-        int st, slot, hl, hj;
-        wide_multi_np<MODE, T>(ms[warp], rb, ob, pts, (D + 1) * 3, G, live, nm, Want{true, false, false},
-                               MODE == 2 ? &P.ps : nullptr, v, dd, st, slot, hl, hj);
-        if (e >= 0) {
-            edge_outcome<MODE>(P, e, k, st, slot, v);
-            if (st == kSettled && v == 0) e = -1;    // the reference's first collision: the edge is done
-            else if (--k < 1) e = -1;                // every check clear (or left to the recheck)
-        }
-        __syncwarp();
     }
 }
 #endif

@@ -9,7 +9,7 @@ import os
 import numpy as np
 
 from . import _abi
-from ._abi import BatchItem, CheckStats, LAYOUTS, Params, PRECISIONS
+from ._abi import BatchItem, CheckStats, EdgeBatchItem, LAYOUTS, Params, PRECISIONS
 
 _LIB = None
 
@@ -55,6 +55,7 @@ def load(build_if_missing=False):
     L.rpm_check_configs.argtypes = [_vp, _i32, _i32, _vp, _i64, _vp, _vp, _vp, _vp]
     L.rpm_check_batch.argtypes = [_vp, _i32, _vp, _i32, _vp]
     L.rpm_check_edges.argtypes = [_vp, _i32, _i32, _vp, _vp, _i64, ctypes.c_float, _i32, _vp, _vp, _vp]
+    L.rpm_check_edges_batch.argtypes = [_vp, _i32, _vp, _i32, _vp]
     L.rpm_ctx_set_graphs.argtypes = [_vp, ctypes.c_int]
     L.rpm_ctx_set_layout.argtypes = [_vp, ctypes.c_int32]
     L.rpm_distance_nearest.argtypes = [_vp, _i32, _i32, _vp, _i64, _vp, _vp, _vp, _vp, _vp]
@@ -163,6 +164,16 @@ class Engine:
         _check(self.lib.rpm_check_edges(self.ctx, scene_id, prec, _ptr(q1), _ptr(q2), int(q1.shape[0]), float(step),
                                         int(num_checks), _ptr(valid), _ptr(checks), stream))
 
+    def check_edges_batch(self, items, precision="fp64", stream=None):
+        """items: list of (scene_id, q1, q2, valid, checks, step, num_checks) with torch CUDA tensors
+        (checks nullable); every item's edges go through one pipeline."""
+        prec = PRECISIONS[precision] if isinstance(precision, str) else int(precision)
+        arr = (EdgeBatchItem * max(1, len(items)))()
+        for k, (sid, q1, q2, valid, checks, step, num_checks) in enumerate(items):
+            arr[k] = EdgeBatchItem(sid, int(num_checks), int(q1.shape[0]), _ptr(q1), _ptr(q2), float(step), _ptr(valid),
+                                   _ptr(checks))
+        _check(self.lib.rpm_check_edges_batch(self.ctx, prec, ctypes.addressof(arr), len(items), stream))
+
     def set_graphs(self, enable=True):
         _check(self.lib.rpm_ctx_set_graphs(self.ctx, 1 if enable else 0))
 
@@ -250,7 +261,7 @@ ABI_SYMBOLS = [
     "rpm_robot_upload", "rpm_scene_create", "rpm_scene_update", "rpm_scene_destroy", "rpm_scene_info",
     "rpm_box_aabb", "rpm_check_configs", "rpm_check_configs_host", "rpm_skeleton", "rpm_last_stats", "rpm_sync",
     "rpm_ctx_set_timing", "rpm_last_timing", "rpm_probe_fp32_peak", "rpm_check_configs_noalloc", "rpm_check_batch",
-    "rpm_check_edges", "rpm_ctx_set_graphs", "rpm_autotune_edges", "rpm_set_edge_ctas", "rpm_ctx_set_layout",
+    "rpm_check_edges", "rpm_check_edges_batch", "rpm_ctx_set_graphs", "rpm_autotune_edges", "rpm_set_edge_ctas", "rpm_ctx_set_layout",
     "rpm_distance_nearest", "rpm_distance_underestimation",
     "rpm_server_create", "rpm_server_submit", "rpm_server_poll", "rpm_server_wait", "rpm_server_release",
     "rpm_server_replay", "rpm_server_stats", "rpm_server_destroy",

@@ -97,3 +97,53 @@ def test_golden_fixtures_on_gpu(engine, prec, tag):
     assert np.array_equal(v.cpu().numpy(), G["edges_%s_valid" % tag])
     assert np.array_equal(k.cpu().numpy(), G["edges_%s_checks" % tag])
     engine.destroy_scene(sid)
+
+
+def _edge_items(engine, rng):
+    """Edge sets of several robots and scene sizes (both layouts), uneven and fixed discretisations."""
+    from rpmplv2_gb300 import serve
+    specs = [("planar_2dof", 8, 300, 0.05), ("xarm6", 40, 700, 0.05), ("spatial_10dof", 250, 900, 0.05),
+             ("spatial_14dof", 30, 1, 0.0), ("spatial_22dof", 600, 400, 0.05), ("xarm6", 150, 0, 0.05),
+             ("spatial_18dof", 120, 2500, 0.0)]
+    out = []
+    for name, n, E, step in specs:
+        robot = serve.make_robot(name)
+        scene = serve._scene_for(robot, rng, n)
+        sid = engine.create_scene(engine.upload_robot(robot), scene)
+        D = robot.num_dofs
+        q1 = scenes.uniform_configs(rng, E, D)
+        u = rng.normal(size=(E, D))
+        u /= np.maximum(np.linalg.norm(u, axis=1, keepdims=True), 1e-12)
+        q2 = (q1 + u * rng.uniform(0.01, 2.0, (E, 1))).astype(np.float32)
+        out.append((robot, scene, sid, q1, q2, step, 10))
+    return out
+
+
+@pytest.mark.parametrize("prec,oracle_prec", [("fp64", "ref64"), ("fp32_ref", "ref32"), ("fp32_recheck", "ref64")])
+def test_edges_batch_mixed_robots(engine, prec, oracle_prec):
+    """rpm_check_edges_batch: robots of 2-22 DOF, scenes of 8-600 boxes (lane and
+    warp layouts in one pipeline), uneven and fixed discretisations and an empty
+    item; each item equals the oracle and rpm_check_edges alone."""
+    rng = np.random.default_rng(35)
+    sets = _edge_items(engine, rng)
+    items, outs = [], []
+    for robot, scene, sid, q1, q2, step, nc in sets:
+        E = q1.shape[0]
+        v, k = _t(max(E, 1), torch.uint8), _t(max(E, 1), torch.int32)
+        items.append((sid, _t(q1), _t(q2), v, k, step, nc))
+        outs.append((v, k))
+    engine.check_edges_batch(items, prec)
+    engine.sync()
+    for (robot, scene, sid, q1, q2, step, nc), (v, k), it in zip(sets, outs, items):
+        E = q1.shape[0]
+        if E == 0:
+            continue
+        rv, rk = O.check_edges(robot, scene, q1, q2, step=step, num_checks=nc, prec=oracle_prec)
+        assert np.array_equal(v.cpu().numpy()[:E], rv)
+        assert np.array_equal(k.cpu().numpy()[:E], rk)
+        v1, k1 = _t(E, torch.uint8), _t(E, torch.int32)
+        engine.check_edges(sid, it[1], it[2], v1, k1, step=step, num_checks=nc, precision=prec)
+        engine.sync()
+        assert np.array_equal(v1.cpu().numpy(), rv) and np.array_equal(k1.cpu().numpy(), rk)
+    for s in sets:
+        engine.destroy_scene(s[2])
