@@ -41,12 +41,14 @@ enum rpm_status_code {
     RPM_ERR_RANGE = -6        /* size beyond a stated maximum */
 };
 
-/* Robot families of the reference.  CHAIN is robots::Planar2DOF and the
- * classes derived from it (Planar10DOF, Spatial10/14/18/22DOF): skeleton point
- * k is the origin of chain segment k, k = 0..D (Planar2DOF.cpp:125-126).
+/* Robot families of the reference.  CHAIN is robots::Planar2DOF and
+ * Planar10DOF, SPATIAL is robots::Spatial10DOF and the Spatial14/18/22DOF
+ * classes derived from it: for both, skeleton point k is the origin of chain
+ * segment k, k = 0..D (Planar2DOF.cpp:125-126); they differ only in
+ * computeEnclosingRadii (Spatial10DOF.cpp:11-30 projects row 0 on {x, y}).
  * XARM6 is robots::xArm6 with its 7-point skeleton recipe and gripper offset
  * (xArm6.cpp:130, 215-231). */
-enum rpm_robot_kind { RPM_ROBOT_CHAIN = 0, RPM_ROBOT_XARM6 = 1 };
+enum rpm_robot_kind { RPM_ROBOT_CHAIN = 0, RPM_ROBOT_XARM6 = 1, RPM_ROBOT_SPATIAL = 2 };
 
 /* Kinematic description of a serial chain as kdl_parser builds it from the
  * URDF: joint k (0-based) has a fixed origin (origin_xyz[k], origin_rot[k])
@@ -243,6 +245,48 @@ int rpm_distance_underestimation(rpm_ctx *ctx, int32_t scene_id, int32_t precisi
  * RPM_PREC_FP32_RECHECK the FP32 FK of the bulk pass. */
 int rpm_skeleton(rpm_ctx *ctx, int32_t robot_id, int32_t precision, const float *q_dev, int64_t num_configs,
                  double *points_dev, void *stream);
+
+/* ---- bubbles and spines (the RBT planners' step after the distance profile)
+ * All in the reference's float numerics (its float skeleton, IEEE float
+ * operations); xArm6 self-collision checking is off.  Status values are
+ * base::State::Status (State.h:22). */
+enum rpm_state_status { RPM_STATE_NONE = 0, RPM_STATE_ADVANCED = 1, RPM_STATE_TRAPPED = 2, RPM_STATE_REACHED = 3 };
+
+/* AbstractRobot::computeEnclosingRadii (xArm6.cpp:237-275, Spatial10DOF.cpp:11-30,
+ * Planar2DOF.cpp:132-148) for a batch: radii_dev[c] is the D x (D + 1)
+ * matrix R, row-major (R[i][j]: the radius about joint i enclosing skeleton
+ * points i+1..j and their capsules). */
+int rpm_enclosing_radii(rpm_ctx *ctx, int32_t robot_id, const float *q_dev, int64_t num_configs, float *radii_dev,
+                        void *stream);
+
+/* RBTConnect::extendSpine (RBTConnect.cpp:85-150) for a batch of spines:
+ * spine c runs from q_dev[c] towards q_e_dev[c] (num_spines x D), given the
+ * start's d_c (dist_dev, float, as computeDistance returns it) and its
+ * profile (profile_dev, num_spines x L).  num_iter = NUM_ITER_SPINE,
+ * expanded = USE_EXPANDED_BUBBLE.  q_new_dev gets each spine's end and
+ * status_dev its rpm_state_status. */
+int rpm_extend_spines(rpm_ctx *ctx, int32_t robot_id, const float *q_dev, const float *q_e_dev, const float *dist_dev,
+                      const float *profile_dev, int64_t num_spines, int32_t num_iter, int32_t expanded, float *q_new_dev,
+                      int32_t *status_dev, void *stream);
+
+/* DRGBT::computeReachedState (DRGBT.cpp:475-495) for a whole horizon in one
+ * launch (the DRGBT generalized bur, DRGBT.cpp:272-320): for every horizon
+ * state h, extendGenSpine (RGBTConnect.cpp:73-93) from q_current towards
+ * horizon_dev[h] -- computeDistance of q_current with nearest points, then
+ * up to num_layers spines, each followed by computeDistanceUnderestimation
+ * from q_current's nearest points and stopped below d_crit -- then
+ * computeDistance(q_reached, true) in 'precision' (dist_dev, nullable).
+ * q_reached_dev is horizon_size x D; status_dev per rpm_state_status
+ * (RPM_STATE_REACHED = isReached). */
+typedef struct rpm_spine_params {
+    int32_t num_layers;   /* RGBTConnectConfig::NUM_LAYERS */
+    int32_t num_iter;     /* RBTConnectConfig::NUM_ITER_SPINE */
+    int32_t expanded;     /* RBTConnectConfig::USE_EXPANDED_BUBBLE */
+    float d_crit;         /* RBTConnectConfig::D_CRIT */
+} rpm_spine_params;
+int rpm_reached_states(rpm_ctx *ctx, int32_t scene_id, int32_t precision, const float *q_current_dev,
+                       const float *horizon_dev, int64_t horizon_size, const rpm_spine_params *params,
+                       float *q_reached_dev, int32_t *status_dev, double *dist_dev, void *stream);
 
 /* ---- serving loop (continuous batching) -----------------------------------
  * Planners submit isValid / distance batches and edge batches of any size

@@ -41,6 +41,11 @@ def lib():
         L.orc_box_aabb.argtypes = [_f, _f, _f, _f]
         L.orc_distance_underest.argtypes = [_vp, ctypes.c_int, _f, ctypes.c_int64, ctypes.c_int, ctypes.c_int, _vp, _f,
                                             _d, _f, _u8]
+        L.orc_enclosing_radii.argtypes = [_vp, _f, ctypes.c_int64, ctypes.c_int, _f]
+        L.orc_extend_spines.argtypes = [_vp, _f, _f, _f, _f, ctypes.c_int64, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                        _f, _i32]
+        L.orc_reached_states.argtypes = [_vp, _f, _f, _u8, ctypes.c_int, _f, _f, ctypes.c_int64, ctypes.c_int,
+                                         ctypes.c_int, ctypes.c_int, ctypes.c_float, ctypes.c_int, _vp, _f, _i32]
         _lib = L
     return _lib
 
@@ -130,6 +135,44 @@ def distance_underestimation(robot, scene_n, q, nearest, prec="ref64", trig=0):
     lib().orc_distance_underest(ctypes.byref(robot.desc), int(scene_n), _p(q, _f), C, _prec(prec), trig, None,
                                 _p(nearest, _f), _p(dist, _d), _p(prof, _f), _p(comp, _u8))
     return dist, prof, comp
+
+
+def enclosing_radii(robot, q, trig=0):
+    """computeEnclosingRadii per configuration: (C, D, D + 1) float32."""
+    q = np.ascontiguousarray(q, np.float32)
+    C, D = q.shape
+    out = np.zeros((C, D, D + 1), np.float32)
+    lib().orc_enclosing_radii(ctypes.byref(robot.desc), _p(q, _f), C, trig, _p(out, _f))
+    return out
+
+
+def extend_spines(robot, q, qe, dist, profile, num_iter=1, expanded=True, trig=0):
+    """RBTConnect::extendSpine per row; dist (C,) and profile (C, L) float32.
+    Returns (q_new (C, D) float32, status (C,) int32)."""
+    q = np.ascontiguousarray(q, np.float32)
+    qe = np.ascontiguousarray(qe, np.float32)
+    dist = np.ascontiguousarray(dist, np.float32)
+    profile = np.ascontiguousarray(profile, np.float32)
+    C, D = q.shape
+    q_new = np.zeros((C, D), np.float32)
+    status = np.zeros(C, np.int32)
+    lib().orc_extend_spines(ctypes.byref(robot.desc), _p(q, _f), _p(qe, _f), _p(dist, _f), _p(profile, _f), C,
+                            int(num_iter), int(bool(expanded)), trig, _p(q_new, _f), _p(status, _i32))
+    return q_new, status
+
+
+def reached_states(robot, scene, q_cur, horizon, num_layers=5, num_iter=1, expanded=True, d_crit=0.05, trig=0):
+    """DRGBT::computeReachedState for every horizon state (without the final
+    computeDistance).  Returns (q_reached (H, D) float32, status (H,) int32)."""
+    q_cur = np.ascontiguousarray(q_cur, np.float32).reshape(-1)
+    horizon = np.ascontiguousarray(horizon, np.float32)
+    H, D = horizon.shape
+    q_out = np.zeros((H, D), np.float32)
+    status = np.zeros(H, np.int32)
+    lib().orc_reached_states(ctypes.byref(robot.desc), _p(scene.aabb, _f), _p(scene.tol, _f), _p(scene.flags, _u8),
+                             scene.n, _p(q_cur, _f), _p(horizon, _f), H, int(num_layers), int(num_iter),
+                             int(bool(expanded)), float(d_crit), trig, None, _p(q_out, _f), _p(status, _i32))
+    return q_out, status
 
 
 def sincos(x, trig=0):

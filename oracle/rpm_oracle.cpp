@@ -128,7 +128,7 @@ void skeleton(const rpm_robot_desc &rb, const float *q, int trig, double *p64, f
     Frame F;
     for (int i = 0; i < 9; ++i) F.R[i] = (i % 4 == 0) ? 1.0 : 0.0;
     F.p[0] = F.p[1] = F.p[2] = 0.0;
-    if (rb.kind == RPM_ROBOT_CHAIN) {
+    if (rb.kind != RPM_ROBOT_XARM6) {
         // Planar2DOF.cpp:125-126: skeleton col k = frames[k].p, k = 0..D
         for (int k = 0; k < D; ++k) {
             fk_step(F, rb, k, (double)q[k], trig);
@@ -679,6 +679,159 @@ T distance_underest(const Num<T> &nm, const rpm_robot_desc &rb, int n, const T *
     return d_c;
 }
 
+// ------------------------------------------------------------------ spines --
+// The bubble and spine steps of the RBT planners in the reference's float
+// numerics.  Sums over dynamic-size Eigen expressions (a skeleton column,
+// R->col(i).dot(delta_q)) run in index order; fixed-size 3-vector reductions
+// as x0 + (x1 + x2).  Eigen's order for dynamic sizes is not pinned by any
+// reference test.
+enum { kStNone = 0, kStAdvanced = 1, kStTrapped = 2, kStReached = 3 };   // base::State::Status (State.h:22)
+
+inline float maxf_std(float a, float b) { return (a < b) ? b : a; }   // std::max
+
+// |a - b| over dynamic 3-element columns, summed in index order.
+inline float col_dist(const float *a, const float *b) {
+    float s = 0.f;
+    for (int k = 0; k < 3; ++k) {
+        const float d = a[k] - b[k];
+        s = s + d * d;
+    }
+    return std::sqrt(s);
+}
+
+// computeEnclosingRadii from the float skeleton sk (D + 1 points): R is
+// D x (D + 1), row-major.  xArm6.cpp:237-275 (radii max(r_i, r_i+1), rows 0
+// and 3 projected), Spatial10DOF.cpp:11-30 (row 0 projected on {x, y}),
+// Planar2DOF.cpp:132-148 (no projection).
+void enclosing_radii(const rpm_robot_desc &rb, const float *sk, float *R) {
+    const int D = rb.num_dofs, W = D + 1;
+    for (int i = 0; i < D * W; ++i) R[i] = 0.f;
+    if (rb.kind == RPM_ROBOT_XARM6) {
+        float rn[RPM_MAX_DOF];
+        for (int i = 0; i < D - 1; ++i) rn[i] = maxf_std(rb.capsule_radius[i], rb.capsule_radius[i + 1]);
+        rn[D - 1] = rb.capsule_radius[D - 1];
+        for (int i = 0; i < D - 1; ++i)
+            for (int j = i + 1; j <= D; ++j) {
+                const float *pj = sk + 3 * j;
+                if (i == 0) {
+                    if (j >= 2) R[j] = maxf_std(R[j - 1], std::sqrt(pj[0] * pj[0] + pj[1] * pj[1]) + rn[j - 1]);
+                } else if (i == 3) {
+                    if (j >= 5) {
+                        const float *p3 = sk + 9, *p4 = sk + 12;
+                        float AB[3], v[3], proj[3], w[3];
+                        sub3(p4, p3, AB);
+                        sub3(pj, p3, v);
+                        const float t = dot3(v, AB) / dot3(AB, AB);
+                        for (int k = 0; k < 3; ++k) proj[k] = p3[k] + t * AB[k];
+                        sub3(pj, proj, w);
+                        R[3 * W + j] = maxf_std(R[3 * W + j - 1], norm3(w) + rn[j - 1]);
+                    }
+                } else {
+                    R[i * W + j] = maxf_std(R[i * W + j - 1], col_dist(pj, sk + 3 * i) + rn[j - 1]);
+                }
+            }
+        return;
+    }
+    const bool spatial = rb.kind == RPM_ROBOT_SPATIAL;
+    for (int i = 0; i < D; ++i)
+        for (int j = i + 1; j <= D; ++j) {
+            const float *pj = sk + 3 * j;
+            const float v = (i == 0 && spatial) ? std::sqrt(pj[0] * pj[0] + pj[1] * pj[1]) : col_dist(pj, sk + 3 * i);
+            R[i * W + j] = maxf_std(R[i * W + j - 1], v + rb.capsule_radius[j - 1]);
+        }
+}
+
+// RBTConnect::extendSpine (RBTConnect.cpp:85-150) with self-collision checking
+// off: from q (distance d, profile prof) towards qe.  Returns the status;
+// q_new is the spine's end.
+int extend_spine(const rpm_robot_desc &rb, int trig, const float *q, float d, const float *prof, const float *qe,
+                 int num_iter, bool expanded, float *q_new) {
+    const int D = rb.num_dofs, L = D, W = D + 1;
+    if (d <= 0) {
+        for (int k = 0; k < D; ++k) q_new[k] = q[k];
+        return kStTrapped;
+    }
+    double p64[3 * (RPM_MAX_DOF + 1)];
+    float sk0[3 * (RPM_MAX_DOF + 1)], skt[3 * (RPM_MAX_DOF + 1)], skn[3 * (RPM_MAX_DOF + 1)];
+    float R[RPM_MAX_DOF * (RPM_MAX_DOF + 1)];
+    float rho_profile[RPM_MAX_DOF] = {0.f}, qt[RPM_MAX_DOF], dq[RPM_MAX_DOF];
+    float rho = 0.f;
+    skeleton(rb, q, trig, p64, sk0);
+    for (int k = 0; k < D; ++k) qt[k] = q[k];
+    int status = kStAdvanced, counter = 0;
+    for (;;) {
+        skeleton(rb, qt, trig, p64, skt);
+        enclosing_radii(rb, skt, R);
+        for (int k = 0; k < D; ++k) dq[k] = std::fabs(qe[k] - qt[k]);
+        float step;
+        if (expanded) {
+            step = INFINITY;
+            for (int i = 0; i < D; ++i) {
+                float s = 0.f;
+                for (int k = 0; k < D; ++k) s = s + R[k * W + i + 1] * dq[k];
+                step = smin(step, (prof[i] - rho_profile[i]) / s);
+            }
+        } else {
+            float s = 0.f;
+            for (int k = 0; k < D; ++k) s = s + R[k * W + D] * dq[k];
+            step = (d - rho) / s;
+        }
+        if (step > 1.f) {
+            for (int k = 0; k < D; ++k) q_new[k] = qe[k];
+            status = kStReached;
+        } else {
+            for (int k = 0; k < D; ++k) q_new[k] = qt[k] + step * (qe[k] - qt[k]);
+        }
+        if (++counter == num_iter || status != kStAdvanced) return status;
+        skeleton(rb, q_new, trig, p64, skn);
+        float rk_prev = 0.f;
+        for (int k = 1; k <= L; ++k) {
+            const float rk = col_dist(sk0 + 3 * k, skn + 3 * k);
+            rho_profile[k - 1] = maxf_std(rk_prev, rk);
+            rk_prev = rk;
+            rho = maxf_std(rho, rk);
+        }
+        for (int k = 0; k < D; ++k) qt[k] = q_new[k];
+    }
+}
+
+// DRGBT::computeReachedState (DRGBT.cpp:475-495) without its final
+// computeDistance: RGBTConnect::extendGenSpine (RGBTConnect.cpp:73-93) from
+// q_cur (distance d_cur, profile prof_cur, nearest points near_cur) towards
+// qe, with computeDistanceUnderestimation from q_cur's nearest points after
+// every layer.
+int reached_state(const Num<float> &nm, const rpm_robot_desc &rb, int trig, int n, const float *q_cur, float d_cur,
+                  const float *prof_cur, const float *near_cur, const float *qe, int num_layers, int num_iter,
+                  bool expanded, float d_crit, float *q_out) {
+    const int D = rb.num_dofs, L = D;
+    for (int k = 0; k < D; ++k) q_out[k] = q_cur[k];
+    if (d_cur <= 0) return kStTrapped;
+    float qn[RPM_MAX_DOF], pn[RPM_MAX_DOF], qs[RPM_MAX_DOF];
+    for (int k = 0; k < D; ++k) qn[k] = q_cur[k];
+    for (int i = 0; i < L; ++i) pn[i] = prof_cur[i];
+    float dn = d_cur;
+    int status = kStNone;
+    for (int layer = 0; layer < num_layers; ++layer) {
+        status = extend_spine(rb, trig, qn, dn, pn, qe, num_iter, expanded, qs);
+        for (int k = 0; k < D; ++k) qn[k] = qs[k];
+        double p64[3 * (RPM_MAX_DOF + 1)];
+        float sk[3 * (RPM_MAX_DOF + 1)], p[RPM_MAX_DOF];
+        skeleton(rb, qn, trig, p64, sk);
+        bool ok = false;
+        float d = distance_underest(nm, rb, n, sk, near_cur, p, &ok);
+        if (ok) {
+            dn = d;
+            for (int i = 0; i < L; ++i) pn[i] = p[i];
+        } else {
+            d = 0.f;
+            dn = -1.f;
+        }
+        if (d < d_crit || status != kStAdvanced) break;
+    }
+    for (int k = 0; k < D; ++k) q_out[k] = qn[k];
+    return status;
+}
+
 extern "C" {
 
 int orc_version(void) { return 1; }
@@ -891,6 +1044,47 @@ void orc_box_aabb(const float *dim, const float *pos, const float *quat_xyzw, fl
         float rad = std::sqrt(h[0] * h[0] + (h[1] * h[1] + h[2] * h[2]));
         for (int k = 0; k < 3; ++k) { out[k] = pos[k] - rad; out[3 + k] = pos[k] + rad; }
     }
+}
+
+// Enclosing radii per configuration: out is C x D x (D + 1) floats.
+int orc_enclosing_radii(const rpm_robot_desc *rb, const float *q, int64_t C, int trig, float *out) {
+    const int D = rb->num_dofs;
+    for (int64_t c = 0; c < C; ++c) {
+        double p64[3 * (RPM_MAX_DOF + 1)];
+        float p32[3 * (RPM_MAX_DOF + 1)];
+        skeleton(*rb, q + c * D, trig, p64, p32);
+        enclosing_radii(*rb, p32, out + c * D * (D + 1));
+    }
+    return 0;
+}
+
+// extendSpine per row: q, qe C x D; dist C; profile C x L.
+int orc_extend_spines(const rpm_robot_desc *rb, const float *q, const float *qe, const float *dist, const float *profile,
+                      int64_t C, int num_iter, int expanded, int trig, float *q_new, int32_t *status) {
+    const int D = rb->num_dofs;
+    for (int64_t c = 0; c < C; ++c)
+        status[c] = extend_spine(*rb, trig, q + c * D, dist[c], profile + c * D, qe + c * D, num_iter, expanded != 0,
+                                 q_new + c * D);
+    return 0;
+}
+
+// computeReachedState for a horizon (H x D) from q_cur, whose computeDistance
+// with nearest points runs here in the reference's float numerics.
+int orc_reached_states(const rpm_robot_desc *rb, const float *aabb, const float *tol, const uint8_t *flags, int n,
+                       const float *q_cur, const float *qe, int64_t H, int num_layers, int num_iter, int expanded,
+                       float d_crit, int trig, const rpm_params *params, float *q_out, int32_t *status) {
+    const int D = rb->num_dofs, L = D;
+    const size_t NS = (size_t)n * 6 * L;
+    std::vector<float> near(NS > 0 ? NS : 1, 0.f);
+    float prof[RPM_MAX_DOF];
+    double d = 0.0;
+    uint8_t nv = 0;
+    orc_distance_nearest(rb, aabb, tol, flags, n, q_cur, 1, 32, trig, params, &d, prof, near.data(), &nv);
+    const Num<float> nm = num_of<float>(params);
+    for (int64_t h = 0; h < H; ++h)
+        status[h] = reached_state(nm, *rb, trig, n, q_cur, (float)d, prof, near.data(), qe + h * D, num_layers,
+                                  num_iter, expanded != 0, d_crit, q_out + h * D);
+    return 0;
 }
 
 }  // extern "C"

@@ -13,6 +13,7 @@ RPM_ERR_RANGE = -6
 
 RPM_ROBOT_CHAIN = 0
 RPM_ROBOT_XARM6 = 1
+RPM_ROBOT_SPATIAL = 2
 
 RPM_OBS_GROUND = 0x1
 RPM_OBS_DYNAMIC = 0x2
@@ -81,4 +82,14 @@ class EdgeBatchItem(ctypes.Structure):
         ("step", ctypes.c_float),
         ("valid_dev", ctypes.c_void_p),
         ("checks_dev", ctypes.c_void_p),
+    ]
+
+
+class SpineParams(ctypes.Structure):
+    """rpm_spine_params."""
+    _fields_ = [
+        ("num_layers", ctypes.c_int32),
+        ("num_iter", ctypes.c_int32),
+        ("expanded", ctypes.c_int32),
+        ("d_crit", ctypes.c_float),
     ]

@@ -17,6 +17,7 @@
 
 #include "rpm_ctx_impl.cuh"
 #include "rpm_nearest.cuh"
+#include "rpm_spine.cuh"
 
 using namespace rpm;
 
@@ -293,7 +294,7 @@ using impl::fail;
 
 int set_error(int code, const char *msg) { return fail(code, "%s", msg); }
 int build_dev_robot(const rpm_robot_desc &d, DevRobot &r) {
-    if (d.kind != RPM_ROBOT_CHAIN && d.kind != RPM_ROBOT_XARM6) return fail(RPM_ERR_INVALID, "unknown robot kind %d", d.kind);
+    if (d.kind != RPM_ROBOT_CHAIN && d.kind != RPM_ROBOT_XARM6 && d.kind != RPM_ROBOT_SPATIAL) return fail(RPM_ERR_INVALID, "unknown robot kind %d", d.kind);
     if (d.num_dofs < 1 || d.num_dofs > RPM_MAX_DOF) return fail(RPM_ERR_INVALID, "num_dofs %d out of range", d.num_dofs);
     if (d.kind == RPM_ROBOT_XARM6 && d.num_dofs != 6) return fail(RPM_ERR_INVALID, "xArm6 needs num_dofs == 6");
     std::memset(&r, 0, sizeof r);
@@ -968,6 +969,108 @@ int rpm_distance_nearest(rpm_ctx *ctx, int32_t scene_id, int32_t precision, cons
     p.flag = nearest_valid_dev;
     CK(launch_distance_nearest(precision == RPM_PREC_FP32_REF ? RPM_PREC_FP32_REF : RPM_PREC_FP64, p, st));
     return near_done(ctx, buf, st);
+}
+
+static int spine_robot(rpm_ctx *ctx, int32_t robot_id, SpineParams &p) {
+    if (robot_id < 0 || robot_id >= (int32_t)ctx->robots.size() || !ctx->robots[robot_id].dev)
+        return fail(RPM_ERR_INVALID, "unknown robot %d", robot_id);
+    std::memset(&p, 0, sizeof p);
+    p.robot = ctx->robots[robot_id].dev;
+    p.maxd = (float)ctx->params.max_distance;
+    return RPM_OK;
+}
+
+int rpm_enclosing_radii(rpm_ctx *ctx, int32_t robot_id, const float *q_dev, int64_t num_configs, float *radii_dev,
+                        void *stream) {
+    if (!ctx || num_configs < 0 || (num_configs > 0 && (!q_dev || !radii_dev))) return fail(RPM_ERR_INVALID, "bad arguments");
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    if (set_device(ctx)) return RPM_ERR_CUDA;
+    SpineParams p;
+    const int rc = spine_robot(ctx, robot_id, p);
+    if (rc) return rc;
+    p.q = q_dev;
+    p.C = num_configs;
+    p.radii = radii_dev;
+    CK(launch_enclosing_radii(p, (cudaStream_t)stream));
+    return RPM_OK;
+}
+
+int rpm_extend_spines(rpm_ctx *ctx, int32_t robot_id, const float *q_dev, const float *q_e_dev, const float *dist_dev,
+                      const float *profile_dev, int64_t num_spines, int32_t num_iter, int32_t expanded, float *q_new_dev,
+                      int32_t *status_dev, void *stream) {
+    if (!ctx || num_spines < 0 ||
+        (num_spines > 0 && (!q_dev || !q_e_dev || !dist_dev || !profile_dev || !q_new_dev || !status_dev)))
+        return fail(RPM_ERR_INVALID, "bad arguments");
+    if (num_iter < 1) return fail(RPM_ERR_INVALID, "num_iter must be >= 1");
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    if (set_device(ctx)) return RPM_ERR_CUDA;
+    SpineParams p;
+    const int rc = spine_robot(ctx, robot_id, p);
+    if (rc) return rc;
+    p.q = q_dev;
+    p.qe = q_e_dev;
+    p.dist = dist_dev;
+    p.profile = profile_dev;
+    p.C = num_spines;
+    p.num_iter = num_iter;
+    p.expanded = expanded;
+    p.q_new = q_new_dev;
+    p.status = status_dev;
+    CK(launch_extend_spines(p, (cudaStream_t)stream));
+    return RPM_OK;
+}
+
+int rpm_reached_states(rpm_ctx *ctx, int32_t scene_id, int32_t precision, const float *q_current_dev,
+                       const float *horizon_dev, int64_t horizon_size, const rpm_spine_params *params,
+                       float *q_reached_dev, int32_t *status_dev, double *dist_dev, void *stream) {
+    if (!ctx || !params || horizon_size < 0 || !q_current_dev ||
+        (horizon_size > 0 && (!horizon_dev || !q_reached_dev || !status_dev)))
+        return fail(RPM_ERR_INVALID, "bad arguments");
+    if (params->num_iter < 1 || params->num_layers < 0) return fail(RPM_ERR_INVALID, "num_iter >= 1 and num_layers >= 0");
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    cudaStream_t st = (cudaStream_t)stream;
+    NearParams np;
+    SceneBuf *buf = nullptr;
+    int rc = near_setup(ctx, scene_id, RPM_PREC_FP32_REF, q_current_dev, 1, st, np, &buf);
+    if (rc) return rc;
+    if (precision < RPM_PREC_FP64 || precision > RPM_PREC_FP32_REF) return fail(RPM_ERR_INVALID, "unknown precision %d", precision);
+    SceneRec *s = find_scene(ctx, scene_id);
+    const int L = ctx->robots[s->robot].desc.num_dofs;
+    // computeDistance of the current state with nearest points (stream-ordered scratch)
+    const size_t near_floats = (size_t)std::max(1, np.n) * 6 * L;
+    char *tmp = nullptr;
+    const size_t bytes = 16 + 4 * (size_t)L + 4 * near_floats + 16;
+    CK(cudaMallocAsync((void **)&tmp, bytes, st));
+    np.dist = reinterpret_cast<double *>(tmp);
+    np.flag = reinterpret_cast<uint8_t *>(tmp + 8);
+    np.profile = reinterpret_cast<float *>(tmp + 16);
+    np.nearest = reinterpret_cast<float *>(tmp + 16 + 4 * (size_t)L);
+    CK(launch_distance_nearest(RPM_PREC_FP32_REF, np, st));
+    SpineParams p;
+    std::memset(&p, 0, sizeof p);
+    p.robot = np.robot;
+    p.qe = horizon_dev;
+    p.C = horizon_size;
+    p.num_iter = params->num_iter;
+    p.expanded = params->expanded;
+    p.num_layers = params->num_layers;
+    p.d_crit = params->d_crit;
+    p.q_new = q_reached_dev;
+    p.status = status_dev;
+    p.q_cur = q_current_dev;
+    p.cur_dist = np.dist;
+    p.cur_prof = np.profile;
+    p.cur_near = np.nearest;
+    p.n = np.n;
+    p.maxd = np.nmf.maxd;
+    CK(launch_reached_states(p, st));
+    CK(cudaFreeAsync(tmp, st));
+    rc = near_done(ctx, buf, st);
+    if (rc) return rc;
+    // computeDistance(q_reached, true) in the requested form
+    if (dist_dev && horizon_size > 0)
+        return enqueue_check(ctx, s, precision, q_reached_dev, horizon_size, nullptr, dist_dev, nullptr, st);
+    return RPM_OK;
 }
 
 int rpm_distance_underestimation(rpm_ctx *ctx, int32_t scene_id, int32_t precision, const float *q_dev,

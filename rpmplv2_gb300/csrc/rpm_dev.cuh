@@ -264,7 +264,7 @@ template <> struct SkelWalker<0> {
     const double *sc = nullptr;   // precomputed joint sin / cos (nullable)
     RPM_HD void begin() { f.init(); }
     RPM_HD void point(const DevRobot &rb, const float *q, int k, double *out) {
-        if (rb.kind == RPM_ROBOT_CHAIN) {
+        if (rb.kind != RPM_ROBOT_XARM6) {
             if (k < rb.D) {
                 fk_step_d(f, rb, k, (double)q[k], sc);
                 out[0] = f.p[0]; out[1] = f.p[1]; out[2] = f.p[2];
@@ -331,7 +331,7 @@ template <> struct SkelWalker<2> {
     Fk<float> f;
     RPM_HD void begin() { f.init(); }
     RPM_HD void point(const DevRobot &rb, const float *q, int k, float *out) {
-        if (rb.kind == RPM_ROBOT_CHAIN) {
+        if (rb.kind != RPM_ROBOT_XARM6) {
             if (k < rb.D) {
                 fk_step_f(f, rb, k, q[k]);
                 out[0] = f.p[0]; out[1] = f.p[1]; out[2] = f.p[2];

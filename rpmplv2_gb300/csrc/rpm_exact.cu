@@ -8,6 +8,7 @@
 #include "rpm_edges.cuh"
 #include "rpm_launch.cuh"
 #include "rpm_nearest.cuh"
+#include "rpm_spine.cuh"
 #include "rpm_wide.cuh"
 
 namespace rpm {
@@ -781,6 +782,129 @@ cudaError_t launch_skeleton(int mode, const DevRobot *rb, int D, const float *q,
     if (mode == RPM_PREC_FP64) k_skeleton<0><<<grid, 128, 0, st>>>(rb, q, C, out);
     else if (mode == RPM_PREC_FP32_REF) k_skeleton<1><<<grid, 128, 0, st>>>(rb, q, C, out);
     else k_skeleton<2><<<grid, 128, 0, st>>>(rb, q, C, out);
+    return cudaGetLastError();
+}
+
+}  // namespace rpm
+
+// ----------------------------------------------------------------- spines --
+namespace rpm {
+
+// computeEnclosingRadii: one thread per configuration.
+__global__ void __launch_bounds__(kThreads) k_enclosing_radii(const __grid_constant__ SpineParams P) {
+    const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= P.C) return;
+    const DevRobot &rb = *P.robot;
+    const int D = rb.D;
+    float sk[3 * (kMaxDof + 1)], row[kMaxDof + 1];
+    skel_ref(rb, P.q + c * D, sk);
+    float *out = P.radii + c * D * (D + 1);
+    for (int i = 0; i < D; ++i) {
+        enclosing_row(rb, sk, i, row);
+        for (int j = 0; j <= D; ++j) out[i * (D + 1) + j] = row[j];
+    }
+}
+
+// extendSpine: one thread per spine.
+__global__ void __launch_bounds__(kThreads) k_extend_spines(const __grid_constant__ SpineParams P) {
+    const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= P.C) return;
+    const DevRobot &rb = *P.robot;
+    const int D = rb.D;
+    P.status[c] = extend_spine(rb, P.q + c * D, P.dist[c], P.profile + c * D, P.qe + c * D, P.num_iter, P.expanded != 0,
+                               P.q_new + c * D);
+}
+
+// computeReachedState: one warp per horizon state.  Every lane runs the spine
+// (the same arithmetic, so no broadcasts are needed); the lanes split the
+// obstacles of computeDistanceUnderestimation, whose first negative value
+// (any lane, any link) makes the reference return 0 without updating the state.
+__global__ void __launch_bounds__(kThreads) k_reached_states(const __grid_constant__ SpineParams P) {
+    const unsigned full = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    const int64_t h = (int64_t)blockIdx.x * (blockDim.x / 32) + (threadIdx.x >> 5);
+    if (h >= P.C) return;
+    const DevRobot &rb = *P.robot;
+    const int D = rb.D, L = D;
+    const float *qe = P.qe + h * D;
+    float qn[kMaxDof], pn[kMaxDof], qs[kMaxDof], sk[3 * (kMaxDof + 1)], p[kMaxDof];
+    for (int k = 0; k < D; ++k) qn[k] = P.q_cur[k];
+    const float d_cur = (float)P.cur_dist[0];
+    int status = kStTrapped;
+    if (d_cur > 0.f) {
+        for (int i = 0; i < L; ++i) pn[i] = P.cur_prof[i];
+        float dn = d_cur;
+        status = kStNone;
+        for (int layer = 0; layer < P.num_layers; ++layer) {
+            status = extend_spine(rb, qn, dn, pn, qe, P.num_iter, P.expanded != 0, qs);
+            for (int k = 0; k < D; ++k) qn[k] = qs[k];
+            skel_ref(rb, qn, sk);
+            float d_c = P.maxd;
+            bool negative = false;
+            for (int i = 0; i < L && !negative; ++i) {
+                const float *S0 = sk + 3 * i, *S1 = S0 + 3;
+                float lmin = P.maxd;
+                bool neg = false;
+                for (int j = lane; j < P.n; j += 32) {
+                    float O[3], R[3];
+#pragma unroll
+                    for (int k = 0; k < 3; ++k) {
+                        R[k] = P.cur_near[((size_t)j * 6 + k) * L + i];
+                        O[k] = P.cur_near[((size_t)j * 6 + 3 + k) * L + i];
+                    }
+                    if (sqrtf(dot3f(O, O)) == P.maxd) continue;
+                    float u[3] = {R[0] - O[0], R[1] - O[1], R[2] - O[2]};
+                    const float z = dot3f(u, u);
+                    if (z > 0.f) {
+                        const float nz = sqrtf(z);
+#pragma unroll
+                        for (int k = 0; k < 3; ++k) u[k] = u[k] / nz;
+                    }
+                    float a[3] = {S0[0] - O[0], S0[1] - O[1], S0[2] - O[2]};
+                    float b[3] = {S1[0] - O[0], S1[1] - O[1], S1[2] - O[2]};
+                    const float d = min_std(dot3f(a, u), dot3f(b, u)) - rb.radius_f[i];
+                    if (d < 0.f) neg = true;
+                    lmin = min_std(lmin, d);
+                }
+                negative = __any_sync(full, neg);
+#pragma unroll
+                for (int off = 16; off > 0; off >>= 1) lmin = min_std(lmin, __shfl_xor_sync(full, lmin, off));
+                p[i] = lmin;
+                d_c = min_std(d_c, lmin);
+            }
+            float d;
+            if (!negative) {
+                d = d_c;
+                dn = d_c;
+                for (int i = 0; i < L; ++i) pn[i] = p[i];
+            } else {
+                d = 0.f;
+                dn = -1.f;
+            }
+            if (d < P.d_crit || status != kStAdvanced) break;
+        }
+    }
+    if (lane == 0) {
+        for (int k = 0; k < D; ++k) P.q_new[h * D + k] = qn[k];
+        P.status[h] = status;
+    }
+}
+
+cudaError_t launch_enclosing_radii(const SpineParams &p, cudaStream_t st) {
+    const unsigned grid = (unsigned)((p.C + kThreads - 1) / kThreads);
+    if (grid) k_enclosing_radii<<<grid, kThreads, 0, st>>>(p);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_extend_spines(const SpineParams &p, cudaStream_t st) {
+    const unsigned grid = (unsigned)((p.C + kThreads - 1) / kThreads);
+    if (grid) k_extend_spines<<<grid, kThreads, 0, st>>>(p);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_reached_states(const SpineParams &p, cudaStream_t st) {
+    const unsigned grid = (unsigned)((p.C + kThreads / 32 - 1) / (kThreads / 32));
+    if (grid) k_reached_states<<<grid, kThreads, 0, st>>>(p);
     return cudaGetLastError();
 }
 

@@ -1,0 +1,156 @@
+// rpm_spine.cuh -- the bubble and spine steps of the RBT planners on the
+// device, in the reference's float numerics (the FP32_REF skeleton and plain
+// IEEE float operations; compiled without contracted multiply-adds):
+//   computeEnclosingRadii   xArm6.cpp:237-275, Spatial10DOF.cpp:11-30,
+//                           Planar2DOF.cpp:132-148
+//   extendSpine             RBTConnect.cpp:85-150 (self-collision checking off)
+//   computeReachedState     DRGBT.cpp:475-495 = extendGenSpine
+//                           (RGBTConnect.cpp:73-93) from the current state with
+//                           computeDistanceUnderestimation after each layer.
+// Sums over dynamic-size Eigen expressions (a skeleton column,
+// R->col(i).dot(delta_q)) run in index order; fixed-size 3-vector reductions
+// as x0 + (x1 + x2).
+#pragma once
+#include "rpm_dev.cuh"
+
+namespace rpm {
+
+enum { kStNone = 0, kStAdvanced = 1, kStTrapped = 2, kStReached = 3 };   // base::State::Status (State.h:22)
+
+struct SpineParams {
+    const DevRobot *robot;
+    const float *q;          // [C][D] spine starts (extendSpine)
+    const float *qe;         // [C][D] spine targets (the horizon for reached states)
+    const float *dist;       // [C] d_c of each start (extendSpine)
+    const float *profile;    // [C][L] its profile (extendSpine)
+    int64_t C;
+    int32_t num_iter;        // NUM_ITER_SPINE
+    int32_t expanded;        // USE_EXPANDED_BUBBLE
+    int32_t num_layers;      // NUM_LAYERS (reached states)
+    float d_crit;            // RBTConnectConfig::D_CRIT (reached states)
+    float *q_new;            // [C][D] output
+    int32_t *status;         // [C] output
+    float *radii;            // [C][D][D + 1] (enclosing radii)
+    // reached states: the current state's computeDistance (reference float numerics)
+    const float *q_cur;      // [D]
+    const double *cur_dist;  // [1]
+    const float *cur_prof;   // [L]
+    const float *cur_near;   // [n][6][L]
+    int32_t n;
+    float maxd;              // MAX_DISTANCE
+};
+
+#ifdef __CUDACC__
+__device__ __forceinline__ float max_std(float a, float b) { return (a < b) ? b : a; }   // std::max
+__device__ __forceinline__ float min_std(float a, float b) { return (b < a) ? b : a; }   // std::min
+__device__ __forceinline__ float dot3f(const float *a, const float *b) { return a[0] * b[0] + (a[1] * b[1] + a[2] * b[2]); }
+
+// |a - b| over dynamic 3-element columns, summed in index order.
+__device__ __forceinline__ float col_dist(const float *a, const float *b) {
+    float s = 0.f;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        const float d = a[k] - b[k];
+        s = s + d * d;
+    }
+    return sqrtf(s);
+}
+
+// The reference's float skeleton (D + 1 points).
+__device__ __forceinline__ void skel_ref(const DevRobot &rb, const float *q, float *sk) {
+    SkelWalker<1> sw;
+    sw.begin();
+    for (int k = 0; k <= rb.D; ++k) sw.point(rb, q, k, sk + 3 * k);
+}
+
+// Row i (D + 1 entries) of computeEnclosingRadii from the float skeleton.
+static __device__ void enclosing_row(const DevRobot &rb, const float *sk, int i, float *row) {
+    const int D = rb.D;
+    for (int j = 0; j <= D; ++j) row[j] = 0.f;
+    if (rb.kind == RPM_ROBOT_XARM6) {
+        if (i >= D - 1) return;
+        for (int j = i + 1; j <= D; ++j) {
+            const float rn = j - 1 < D - 1 ? max_std(rb.radius_f[j - 1], rb.radius_f[j]) : rb.radius_f[D - 1];
+            const float *pj = sk + 3 * j;
+            if (i == 0) {
+                if (j >= 2) row[j] = max_std(row[j - 1], sqrtf(pj[0] * pj[0] + pj[1] * pj[1]) + rn);
+            } else if (i == 3) {
+                if (j >= 5) {
+                    const float *p3 = sk + 9, *p4 = sk + 12;
+                    float AB[3], v[3], proj[3], w[3];
+#pragma unroll
+                    for (int k = 0; k < 3; ++k) { AB[k] = p4[k] - p3[k]; v[k] = pj[k] - p3[k]; }
+                    const float t = dot3f(v, AB) / dot3f(AB, AB);
+#pragma unroll
+                    for (int k = 0; k < 3; ++k) { proj[k] = p3[k] + t * AB[k]; w[k] = pj[k] - proj[k]; }
+                    row[j] = max_std(row[j - 1], sqrtf(dot3f(w, w)) + rn);
+                }
+            } else {
+                row[j] = max_std(row[j - 1], col_dist(pj, sk + 3 * i) + rn);
+            }
+        }
+        return;
+    }
+    const bool spatial = rb.kind == RPM_ROBOT_SPATIAL;
+    for (int j = i + 1; j <= D; ++j) {
+        const float *pj = sk + 3 * j;
+        const float v = (i == 0 && spatial) ? sqrtf(pj[0] * pj[0] + pj[1] * pj[1]) : col_dist(pj, sk + 3 * i);
+        row[j] = max_std(row[j - 1], v + rb.radius_f[j - 1]);
+    }
+}
+
+// extendSpine from q (distance d, profile prof) towards qe; q_new gets the end.
+static __device__ int extend_spine(const DevRobot &rb, const float *q, float d, const float *prof, const float *qe, int num_iter,
+                            bool expanded, float *q_new) {
+    const int D = rb.D, L = D;
+    if (d <= 0.f) {
+        for (int k = 0; k < D; ++k) q_new[k] = q[k];
+        return kStTrapped;
+    }
+    float sk0[3 * (kMaxDof + 1)], skt[3 * (kMaxDof + 1)];
+    float qt[kMaxDof], dq[kMaxDof], rho_profile[kMaxDof], col[kMaxDof + 1], row[kMaxDof + 1];
+    float rho = 0.f;
+    skel_ref(rb, q, sk0);
+    for (int k = 0; k < D; ++k) { qt[k] = q[k]; rho_profile[k] = 0.f; }
+    int status = kStAdvanced, counter = 0;
+    for (;;) {
+        skel_ref(rb, qt, skt);
+        for (int k = 0; k < D; ++k) dq[k] = fabsf(qe[k] - qt[k]);
+        // R->col(j).dot(delta_q) for every column j, rows in index order
+        for (int j = 0; j <= D; ++j) col[j] = 0.f;
+        for (int i = 0; i < D; ++i) {
+            enclosing_row(rb, skt, i, row);
+            for (int j = 0; j <= D; ++j) col[j] = col[j] + row[j] * dq[i];
+        }
+        float step;
+        if (expanded) {
+            step = INFINITY;
+            for (int i = 0; i < D; ++i) step = min_std(step, (prof[i] - rho_profile[i]) / col[i + 1]);
+        } else {
+            step = (d - rho) / col[D];
+        }
+        if (step > 1.f) {
+            for (int k = 0; k < D; ++k) q_new[k] = qe[k];
+            status = kStReached;
+        } else {
+            for (int k = 0; k < D; ++k) q_new[k] = qt[k] + step * (qe[k] - qt[k]);
+        }
+        if (++counter == num_iter || status != kStAdvanced) return status;
+        skel_ref(rb, q_new, skt);
+        float rk_prev = 0.f;
+        for (int k = 1; k <= L; ++k) {
+            const float rk = col_dist(sk0 + 3 * k, skt + 3 * k);
+            rho_profile[k - 1] = max_std(rk_prev, rk);
+            rk_prev = rk;
+            rho = max_std(rho, rk);
+        }
+        for (int k = 0; k < D; ++k) qt[k] = q_new[k];
+    }
+}
+#endif
+
+cudaError_t launch_enclosing_radii(const SpineParams &p, cudaStream_t st);
+cudaError_t launch_extend_spines(const SpineParams &p, cudaStream_t st);
+cudaError_t launch_reached_states(const SpineParams &p, cudaStream_t st);
+
+}  // namespace rpm

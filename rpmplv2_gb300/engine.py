@@ -9,7 +9,7 @@ import os
 import numpy as np
 
 from . import _abi
-from ._abi import BatchItem, CheckStats, EdgeBatchItem, LAYOUTS, Params, PRECISIONS
+from ._abi import BatchItem, CheckStats, EdgeBatchItem, LAYOUTS, Params, PRECISIONS, SpineParams
 
 _LIB = None
 
@@ -60,6 +60,9 @@ def load(build_if_missing=False):
     L.rpm_ctx_set_layout.argtypes = [_vp, ctypes.c_int32]
     L.rpm_distance_nearest.argtypes = [_vp, _i32, _i32, _vp, _i64, _vp, _vp, _vp, _vp, _vp]
     L.rpm_distance_underestimation.argtypes = [_vp, _i32, _i32, _vp, _i64, _vp, _vp, _vp, _vp, _vp]
+    L.rpm_enclosing_radii.argtypes = [_vp, _i32, _vp, _i64, _vp, _vp]
+    L.rpm_extend_spines.argtypes = [_vp, _i32, _vp, _vp, _vp, _vp, _i64, _i32, _i32, _vp, _vp, _vp]
+    L.rpm_reached_states.argtypes = [_vp, _i32, _i32, _vp, _vp, _i64, ctypes.POINTER(SpineParams), _vp, _vp, _vp, _vp]
     L.rpm_autotune_edges.argtypes = [_vp, _i32, _i32, _vp, _vp, _i64, ctypes.c_float, _i32, _vp, _pi32]
     L.rpm_set_edge_ctas.argtypes = [_vp, _i32, _i32, _i32]
     L.rpm_check_configs_host.argtypes = [_vp, _i32, _i32, _vp, _i64, _vp, _vp, _vp]
@@ -174,6 +177,25 @@ class Engine:
                                    _ptr(checks))
         _check(self.lib.rpm_check_edges_batch(self.ctx, prec, ctypes.addressof(arr), len(items), stream))
 
+    def enclosing_radii(self, robot_id, q, radii, stream=None):
+        """computeEnclosingRadii: q [C][D] float32, radii [C][D][D+1] float32 (torch CUDA tensors)."""
+        _check(self.lib.rpm_enclosing_radii(self.ctx, robot_id, _ptr(q), int(q.shape[0]), _ptr(radii), stream))
+
+    def extend_spines(self, robot_id, q, qe, dist, profile, q_new, status, num_iter=1, expanded=True, stream=None):
+        """extendSpine per row (torch CUDA tensors: dist [C] float32, profile [C][L], status [C] int32)."""
+        _check(self.lib.rpm_extend_spines(self.ctx, robot_id, _ptr(q), _ptr(qe), _ptr(dist), _ptr(profile),
+                                          int(q.shape[0]), int(num_iter), int(bool(expanded)), _ptr(q_new),
+                                          _ptr(status), stream))
+
+    def reached_states(self, scene_id, q_current, horizon, q_reached, status, dist=None, precision="fp32_recheck",
+                       num_layers=5, num_iter=1, expanded=True, d_crit=0.05, stream=None):
+        """DRGBT computeReachedState for a horizon [H][D] from q_current [D] (torch CUDA tensors)."""
+        prec = PRECISIONS[precision] if isinstance(precision, str) else int(precision)
+        sp = SpineParams(int(num_layers), int(num_iter), int(bool(expanded)), float(d_crit))
+        _check(self.lib.rpm_reached_states(self.ctx, scene_id, prec, _ptr(q_current), _ptr(horizon),
+                                           int(horizon.shape[0]), ctypes.byref(sp), _ptr(q_reached), _ptr(status),
+                                           _ptr(dist), stream))
+
     def set_graphs(self, enable=True):
         _check(self.lib.rpm_ctx_set_graphs(self.ctx, 1 if enable else 0))
 
@@ -262,7 +284,8 @@ ABI_SYMBOLS = [
     "rpm_box_aabb", "rpm_check_configs", "rpm_check_configs_host", "rpm_skeleton", "rpm_last_stats", "rpm_sync",
     "rpm_ctx_set_timing", "rpm_last_timing", "rpm_probe_fp32_peak", "rpm_check_configs_noalloc", "rpm_check_batch",
     "rpm_check_edges", "rpm_check_edges_batch", "rpm_ctx_set_graphs", "rpm_autotune_edges", "rpm_set_edge_ctas", "rpm_ctx_set_layout",
-    "rpm_distance_nearest", "rpm_distance_underestimation",
+    "rpm_distance_nearest", "rpm_distance_underestimation", "rpm_enclosing_radii", "rpm_extend_spines",
+    "rpm_reached_states",
     "rpm_server_create", "rpm_server_submit", "rpm_server_poll", "rpm_server_wait", "rpm_server_release",
     "rpm_server_replay", "rpm_server_stats", "rpm_server_destroy",
 ]

@@ -18,7 +18,7 @@ import math
 
 import numpy as np
 
-from ._abi import RobotDesc, RPM_MAX_DOF, RPM_ROBOT_CHAIN, RPM_ROBOT_XARM6
+from ._abi import RobotDesc, RPM_MAX_DOF, RPM_ROBOT_CHAIN, RPM_ROBOT_SPATIAL, RPM_ROBOT_XARM6
 
 PI_URDF = 3.14159
 
@@ -136,7 +136,7 @@ class Robot:
                 J = np.array([[c, -s, 0], [s, c, 0], [0, 0, 1]])
             R = R @ J
             frames.append((R.copy(), p.copy()))
-        if d.kind == RPM_ROBOT_CHAIN:
+        if d.kind != RPM_ROBOT_XARM6:
             pts = [f[1] for f in frames]
             pts.append(frames[-1][0] @ np.array(d.origin_xyz[D][:]) + frames[-1][1])
             return np.array(pts)
@@ -165,7 +165,7 @@ def spatial(dofs, radius=0.025, ground_included=0):
     h = SPATIAL_LINK_OFFSET[dofs]
     origins = [(0, 0, 0), (0, 0, 0.1)] + [(0, 0, h)] * (dofs - 2)
     axes = [2] + [0] * (dofs - 1)
-    return Robot("spatial_%ddof" % dofs, RPM_ROBOT_CHAIN, origins, [IDENTITY] * dofs, axes, (0, 0, h), radius,
+    return Robot("spatial_%ddof" % dofs, RPM_ROBOT_SPATIAL, origins, [IDENTITY] * dofs, axes, (0, 0, h), radius,
                  [(-PI_URDF, PI_URDF)] * dofs, ground_included=ground_included)
 
 
