@@ -288,6 +288,34 @@ int rpm_reached_states(rpm_ctx *ctx, int32_t scene_id, int32_t precision, const 
                        const float *horizon_dev, int64_t horizon_size, const rpm_spine_params *params,
                        float *q_reached_dev, int32_t *status_dev, double *dist_dev, void *stream);
 
+/* ---- motion validity with moving obstacles (DRGBT replanning) -------------
+ * A box of the scene that moves during a motion, by
+ * Environment::moveStraight (Environment.cpp:220-233): before each check its
+ * position x decreases by delta_time * max_vel, and its AABB is recomputed as
+ * fcl does for a box (rpm_box_aabb). */
+typedef struct rpm_moving_box {
+    int32_t index;          /* obstacle of the scene (label "dynamic_obstacle") */
+    float max_vel;          /* Object::getMaxVel, m/s */
+    float dim[3];
+    float pos[3];           /* position when the motion starts */
+    float quat_xyzw[4];
+} rpm_moving_box;
+
+/* MotionValidity::check (MotionValidity.cpp:30-53) for a batch of motions
+ * q_prev_dev[m] -> q_cur_dev[m] (num_motions x D), each checked from the
+ * scene's current obstacle state while the given boxes move:
+ * delta_time = max_iter_time / num_points (num_points =
+ * NUM_VALIDITY_POINTS_CHECK, MotionValidity.cpp:20-22); check k = 1..num_points
+ * moves the boxes k steps and tests interpolateEdge(q_prev, q_cur,
+ * dist * k / num_points, dist).  valid_dev[m] is the reference's result and
+ * checks_dev[m] (nullable) the checks it makes (the first invalid k, or
+ * num_points).  The scene itself is not changed: a caller that follows the
+ * reference moves its boxes with rpm_scene_update.  precision RPM_PREC_FP64
+ * or RPM_PREC_FP32_REF (the reference's numerics). */
+int rpm_motion_validity(rpm_ctx *ctx, int32_t scene_id, int32_t precision, const float *q_prev_dev,
+                        const float *q_cur_dev, int64_t num_motions, const rpm_moving_box *boxes, int32_t num_boxes,
+                        float max_iter_time, int32_t num_points, uint8_t *valid_dev, int32_t *checks_dev, void *stream);
+
 /* ---- serving loop (continuous batching) -----------------------------------
  * Planners submit isValid / distance batches and edge batches of any size
  * against resident scenes while obstacles move (the DRGBT replanning shape,

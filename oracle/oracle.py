@@ -41,6 +41,8 @@ def lib():
         L.orc_box_aabb.argtypes = [_f, _f, _f, _f]
         L.orc_distance_underest.argtypes = [_vp, ctypes.c_int, _f, ctypes.c_int64, ctypes.c_int, ctypes.c_int, _vp, _f,
                                             _d, _f, _u8]
+        L.orc_motion_validity.argtypes = [_vp, _f, _f, _u8, ctypes.c_int, _f, _f, ctypes.c_int64, _vp, ctypes.c_int,
+                                          ctypes.c_float, ctypes.c_int, ctypes.c_int, ctypes.c_int, _vp, _u8, _i32]
         L.orc_enclosing_radii.argtypes = [_vp, _f, ctypes.c_int64, ctypes.c_int, _f]
         L.orc_extend_spines.argtypes = [_vp, _f, _f, _f, _f, ctypes.c_int64, ctypes.c_int, ctypes.c_int, ctypes.c_int,
                                         _f, _i32]
@@ -173,6 +175,21 @@ def reached_states(robot, scene, q_cur, horizon, num_layers=5, num_iter=1, expan
                              scene.n, _p(q_cur, _f), _p(horizon, _f), H, int(num_layers), int(num_iter),
                              int(bool(expanded)), float(d_crit), trig, None, _p(q_out, _f), _p(status, _i32))
     return q_out, status
+
+
+def motion_validity(robot, scene, q_prev, q_cur, movers, max_iter_time, num_points, prec="ref32", trig=0):
+    """MotionValidity::check per motion with the boxes 'movers' (a ctypes array
+    of rpm_moving_box) moving straight.  Returns (valid (M,) uint8, checks (M,) int32)."""
+    q_prev = np.ascontiguousarray(q_prev, np.float32)
+    q_cur = np.ascontiguousarray(q_cur, np.float32)
+    M = q_prev.shape[0]
+    valid = np.zeros(M, np.uint8)
+    checks = np.zeros(M, np.int32)
+    lib().orc_motion_validity(ctypes.byref(robot.desc), _p(scene.aabb, _f), _p(scene.tol, _f), _p(scene.flags, _u8),
+                              scene.n, _p(q_prev, _f), _p(q_cur, _f), M, ctypes.addressof(movers) if len(movers) else None,
+                              len(movers), float(max_iter_time), int(num_points), _prec(prec), trig, None,
+                              _p(valid, _u8), _p(checks, _i32))
+    return valid, checks
 
 
 def sincos(x, trig=0):

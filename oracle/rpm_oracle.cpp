@@ -832,6 +832,56 @@ int reached_state(const Num<float> &nm, const rpm_robot_desc &rb, int trig, int 
     return status;
 }
 
+extern "C" void orc_box_aabb(const float *dim, const float *pos, const float *quat_xyzw, float *out);
+
+// ---------------------------------------------------------- motion validity --
+// MotionValidity::check (MotionValidity.cpp:30-53) with the boxes of 'movers'
+// moving by Environment::moveStraight (Environment.cpp:220-233): before check
+// k (1..N) every mover's position x decreases by delta_time * max_vel and its
+// AABB is recomputed as fcl does for a box.  Check k tests
+// interpolateEdge(q_prev, q_cur, dist * k / N, dist) (RealVectorSpace.cpp:75-88)
+// against the moved scene.  Returns the validity; *checks = the checks made.
+template <typename T>
+bool motion_valid(const Num<T> &nm, const rpm_robot_desc &rb, int trig, Scene<T> sc, const float *q1, const float *q2,
+                  const rpm_moving_box *movers, int n_movers, float max_iter_time, int N, int *checks) {
+    const int D = rb.num_dofs;
+    float ss = 0.f;   // getNorm in index order
+    for (int i = 0; i < D; ++i) {
+        const float df = q1[i] - q2[i];
+        ss = ss + df * df;
+    }
+    const float dist = std::sqrt(ss);
+    const float dt = max_iter_time / (float)N;
+    std::vector<rpm_moving_box> mv(movers, movers + n_movers);
+    for (int k = 1; k <= N; ++k) {
+        for (rpm_moving_box &m : mv) {
+            m.pos[0] = m.pos[0] - dt * m.max_vel;
+            float box[6];
+            orc_box_aabb(m.dim, m.pos, m.quat_xyzw, box);
+            for (int c = 0; c < 6; ++c) sc.box[6 * (size_t)m.index + c] = (T)box[c];
+        }
+        const float step = dist * (float)k / (float)N;
+        float q[RPM_MAX_DOF];
+        if (dist > 0) {
+            const float r = step / dist;
+            for (int i = 0; i < D; ++i) q[i] = q1[i] + (q2[i] - q1[i]) * r;
+        } else {
+            for (int i = 0; i < D; ++i) q[i] = q2[i];
+        }
+        double p64[3 * (RPM_MAX_DOF + 1)];
+        float p32[3 * (RPM_MAX_DOF + 1)];
+        skeleton(rb, q, trig, p64, p32);
+        T sk[3 * (RPM_MAX_DOF + 1)];
+        for (int i = 0; i < 3 * (D + 1); ++i) sk[i] = sizeof(T) == 4 ? (T)p32[i] : (T)p64[i];
+        if (!is_valid(nm, rb, sc, sk)) {
+            *checks = k;
+            return false;
+        }
+    }
+    *checks = N;
+    return true;
+}
+
 extern "C" {
 
 int orc_version(void) { return 1; }
@@ -1084,6 +1134,28 @@ int orc_reached_states(const rpm_robot_desc *rb, const float *aabb, const float 
     for (int64_t h = 0; h < H; ++h)
         status[h] = reached_state(nm, *rb, trig, n, q_cur, (float)d, prof, near.data(), qe + h * D, num_layers,
                                   num_iter, expanded != 0, d_crit, q_out + h * D);
+    return 0;
+}
+
+// MotionValidity::check per motion (q_prev, q_cur: M x D), every motion from
+// the same obstacle state.
+int orc_motion_validity(const rpm_robot_desc *rb, const float *aabb, const float *tol, const uint8_t *flags, int n,
+                        const float *q_prev, const float *q_cur, int64_t M, const rpm_moving_box *movers, int n_movers,
+                        float max_iter_time, int N, int prec, int trig, const rpm_params *params, uint8_t *valid,
+                        int32_t *checks) {
+    const int D = rb->num_dofs;
+    Obstacles ob{aabb, tol, flags, n};
+    const double maxd = params ? params->max_distance : 1000.0;
+    for (int64_t m = 0; m < M; ++m) {
+        int k = 0;
+        bool v;
+        if (prec == 32) v = motion_valid(num_of<float>(params), *rb, trig, Scene<float>(ob, maxd), q_prev + m * D,
+                                         q_cur + m * D, movers, n_movers, max_iter_time, N, &k);
+        else v = motion_valid(num_of<double>(params), *rb, trig, Scene<double>(ob, maxd), q_prev + m * D,
+                              q_cur + m * D, movers, n_movers, max_iter_time, N, &k);
+        valid[m] = v ? 1 : 0;
+        checks[m] = k;
+    }
     return 0;
 }
 

@@ -93,3 +93,14 @@ class SpineParams(ctypes.Structure):
         ("expanded", ctypes.c_int32),
         ("d_crit", ctypes.c_float),
     ]
+
+
+class MovingBox(ctypes.Structure):
+    """rpm_moving_box."""
+    _fields_ = [
+        ("index", ctypes.c_int32),
+        ("max_vel", ctypes.c_float),
+        ("dim", ctypes.c_float * 3),
+        ("pos", ctypes.c_float * 3),
+        ("quat_xyzw", ctypes.c_float * 4),
+    ]

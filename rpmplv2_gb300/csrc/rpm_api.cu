@@ -1073,6 +1073,71 @@ int rpm_reached_states(rpm_ctx *ctx, int32_t scene_id, int32_t precision, const 
     return RPM_OK;
 }
 
+int rpm_motion_validity(rpm_ctx *ctx, int32_t scene_id, int32_t precision, const float *q_prev_dev,
+                        const float *q_cur_dev, int64_t num_motions, const rpm_moving_box *boxes, int32_t num_boxes,
+                        float max_iter_time, int32_t num_points, uint8_t *valid_dev, int32_t *checks_dev, void *stream) {
+    if (!ctx || num_motions < 0 || num_boxes < 0 || (num_boxes > 0 && !boxes) ||
+        (num_motions > 0 && (!q_prev_dev || !q_cur_dev || !valid_dev)))
+        return fail(RPM_ERR_INVALID, "bad arguments");
+    if (precision != RPM_PREC_FP64 && precision != RPM_PREC_FP32_REF)
+        return fail(RPM_ERR_INVALID, "motion validity runs RPM_PREC_FP64 or RPM_PREC_FP32_REF");
+    if (num_points < 1) return fail(RPM_ERR_INVALID, "num_points must be >= 1");
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    cudaStream_t st = (cudaStream_t)stream;
+    NearParams np;
+    SceneBuf *buf = nullptr;
+    int rc = near_setup(ctx, scene_id, precision, q_prev_dev, num_motions, st, np, &buf);
+    if (rc) return rc;
+    if (num_motions == 0) return RPM_OK;
+    const int n = np.n;
+    for (int b = 0; b < num_boxes; ++b)
+        if (boxes[b].index < 0 || boxes[b].index >= n) return fail(RPM_ERR_INVALID, "moving box %d: bad index", b);
+    if ((int64_t)num_points * num_boxes > (int64_t)1 << 24) return fail(RPM_ERR_RANGE, "too many moving-box steps");
+    // the moving boxes' AABBs before each check, on the host in float as the
+    // reference's Environment::moveStraight and fcl compute them
+    const float dt = max_iter_time / (float)num_points;
+    const size_t moving_bytes = ((size_t)std::max(n, 1) + 15) & ~(size_t)15;
+    const size_t idx_bytes = (((size_t)num_boxes * 4) + 15) & ~(size_t)15;
+    std::vector<unsigned char> host(moving_bytes + idx_bytes + (size_t)num_points * num_boxes * 24, 0);
+    int32_t *hidx = reinterpret_cast<int32_t *>(host.data() + moving_bytes);
+    float *haabb = reinterpret_cast<float *>(host.data() + moving_bytes + idx_bytes);
+    for (int b = 0; b < num_boxes; ++b) {
+        host[boxes[b].index] = 1;
+        hidx[b] = boxes[b].index;
+        float pos[3] = {boxes[b].pos[0], boxes[b].pos[1], boxes[b].pos[2]};
+        for (int k = 0; k < num_points; ++k) {
+            pos[0] = pos[0] - dt * boxes[b].max_vel;
+            rpm_box_aabb(boxes[b].dim, pos, boxes[b].quat_xyzw, haabb + ((size_t)k * num_boxes + b) * 6);
+        }
+    }
+    unsigned char *dev = nullptr;
+    CK(cudaMallocAsync((void **)&dev, host.size(), st));
+    CK(cudaMemcpyAsync(dev, host.data(), host.size(), cudaMemcpyHostToDevice, st));
+    MotionParams p;
+    std::memset(&p, 0, sizeof p);
+    p.robot = np.robot;
+    p.obs_f = np.obs_f;
+    p.obs_d = np.obs_d;
+    p.n = n;
+    p.n_pad = np.n_pad;
+    p.q_prev = q_prev_dev;
+    p.q_cur = q_cur_dev;
+    p.M = num_motions;
+    p.N = num_points;
+    p.n_mov = num_boxes;
+    p.max_iter_time = max_iter_time;
+    p.moving = dev;
+    p.mov_idx = reinterpret_cast<const int32_t *>(dev + moving_bytes);
+    p.mov_aabb = reinterpret_cast<const float *>(dev + moving_bytes + idx_bytes);
+    p.nmd = np.nmd;
+    p.nmf = np.nmf;
+    p.valid = valid_dev;
+    p.checks = checks_dev;
+    CK(launch_motion_validity(precision, p, st));
+    CK(cudaFreeAsync(dev, st));
+    return near_done(ctx, buf, st);
+}
+
 int rpm_distance_underestimation(rpm_ctx *ctx, int32_t scene_id, int32_t precision, const float *q_dev,
                                  int64_t num_configs, const float *nearest_dev, double *dist_dev, float *profile_dev,
                                  uint8_t *complete_dev, void *stream) {

@@ -909,3 +909,74 @@ cudaError_t launch_reached_states(const SpineParams &p, cudaStream_t st) {
 }
 
 }  // namespace rpm
+
+namespace rpm {
+
+// MotionValidity::check: one warp per motion, checks in order with early exit;
+// the lanes split the static obstacles, then the moving boxes of the check.
+template <int MODE>
+__global__ void __launch_bounds__(kThreads) k_motion_validity(const __grid_constant__ MotionParams P) {
+    typedef typename std::conditional<MODE == 0, double, float>::type T;
+    const unsigned full = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    const int64_t m = (int64_t)blockIdx.x * (blockDim.x / 32) + (threadIdx.x >> 5);
+    if (m >= P.M) return;
+    const DevRobot &rb = *P.robot;
+    const int D = rb.D, L = D;
+    const float *q1 = P.q_prev + m * D, *q2 = P.q_cur + m * D;
+    Num<T> nm;
+    if (MODE == 0) { nm.eq = (T)P.nmd.eq; nm.maxd = (T)P.nmd.maxd; }
+    else { nm.eq = (T)P.nmf.eq; nm.maxd = (T)P.nmf.maxd; }
+    const ObsView<T> ob{MODE == 0 ? reinterpret_cast<const T *>(P.obs_d) : reinterpret_cast<const T *>(P.obs_f),
+                        P.obs_f + (size_t)kRowGround * P.n_pad, P.n, P.n_pad};
+    float dist;
+    edge_count(q1, q2, D, 1.f, 1, dist);   // getNorm in index order
+    int bad = 0;
+    for (int k = 1; k <= P.N && !bad; ++k) {
+        const float step = dist * (float)k / (float)P.N;
+        float q[kMaxDof];
+        if (dist > 0.f) edge_point(q1, q2, D, step / dist, q);
+        else for (int i = 0; i < D; ++i) q[i] = q2[i];
+        SkelWalker<MODE> sw;
+        sw.begin();
+        T A[3], B[3];
+        sw.point(rb, q, 0, A);
+        for (int i = 0; i < L; ++i) {
+            sw.point(rb, q, i + 1, B);
+            const T r = LinkConst<T>::r(rb, i), rn = LinkConst<T>::rn(rb, i);
+            const bool gskip = i < rb.ground_included;
+            bool hit = false;
+            for (int j = lane; j < P.n && !hit; j += 32) {
+                if (P.moving[j] || (gskip && ob.is_ground(j))) continue;
+                T o[6];
+                ob.box(j, o);
+                hit = coll_box_call<T, ExactPol>(nm, A, B, r, rn, o).v;
+            }
+            for (int mi = lane; mi < P.n_mov && !hit; mi += 32) {
+                if (gskip && ob.is_ground(P.mov_idx[mi])) continue;
+                T o[6];
+                const float *src = P.mov_aabb + ((size_t)(k - 1) * P.n_mov + mi) * 6;
+#pragma unroll
+                for (int c = 0; c < 6; ++c) o[c] = (T)src[c];
+                hit = coll_box_call<T, ExactPol>(nm, A, B, r, rn, o).v;
+            }
+            if (__any_sync(full, hit)) { bad = k; break; }
+#pragma unroll
+            for (int c = 0; c < 3; ++c) A[c] = B[c];
+        }
+    }
+    if (lane == 0) {
+        P.valid[m] = bad ? 0 : 1;
+        if (P.checks) P.checks[m] = bad ? bad : P.N;
+    }
+}
+
+cudaError_t launch_motion_validity(int mode, const MotionParams &p, cudaStream_t st) {
+    const unsigned grid = (unsigned)((p.M + kThreads / 32 - 1) / (kThreads / 32));
+    if (grid == 0) return cudaSuccess;
+    if (mode == RPM_PREC_FP64) k_motion_validity<0><<<grid, kThreads, 0, st>>>(p);
+    else k_motion_validity<1><<<grid, kThreads, 0, st>>>(p);
+    return cudaGetLastError();
+}
+
+}  // namespace rpm

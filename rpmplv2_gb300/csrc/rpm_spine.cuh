@@ -12,6 +12,7 @@
 // as x0 + (x1 + x2).
 #pragma once
 #include "rpm_dev.cuh"
+#include "rpm_check.cuh"
 
 namespace rpm {
 
@@ -152,5 +153,31 @@ static __device__ int extend_spine(const DevRobot &rb, const float *q, float d, 
 cudaError_t launch_enclosing_radii(const SpineParams &p, cudaStream_t st);
 cudaError_t launch_extend_spines(const SpineParams &p, cudaStream_t st);
 cudaError_t launch_reached_states(const SpineParams &p, cudaStream_t st);
+
+}  // namespace rpm
+
+namespace rpm {
+
+// MotionValidity::check for a batch of motions (rpm_motion_validity).
+struct MotionParams {
+    const DevRobot *robot;
+    const float *obs_f;      // [8][n_pad] scene rows (float), ground row
+    const double *obs_d;     // [7][n_pad]
+    int32_t n, n_pad;
+    const float *q_prev, *q_cur;   // [M][D]
+    int64_t M;
+    int32_t N;               // checks per motion
+    int32_t n_mov;           // moving boxes
+    float max_iter_time;
+    const uint8_t *moving;   // [n] 1 = a moving box (its stored AABB is replaced)
+    const int32_t *mov_idx;  // [n_mov] obstacle index
+    const float *mov_aabb;   // [N][n_mov][6] AABB of each moving box before check k
+    Num<double> nmd;
+    Num<float> nmf;
+    uint8_t *valid;
+    int32_t *checks;
+};
+
+cudaError_t launch_motion_validity(int mode, const MotionParams &p, cudaStream_t st);
 
 }  // namespace rpm

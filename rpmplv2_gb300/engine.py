@@ -9,7 +9,7 @@ import os
 import numpy as np
 
 from . import _abi
-from ._abi import BatchItem, CheckStats, EdgeBatchItem, LAYOUTS, Params, PRECISIONS, SpineParams
+from ._abi import BatchItem, CheckStats, EdgeBatchItem, LAYOUTS, MovingBox, Params, PRECISIONS, SpineParams
 
 _LIB = None
 
@@ -60,6 +60,7 @@ def load(build_if_missing=False):
     L.rpm_ctx_set_layout.argtypes = [_vp, ctypes.c_int32]
     L.rpm_distance_nearest.argtypes = [_vp, _i32, _i32, _vp, _i64, _vp, _vp, _vp, _vp, _vp]
     L.rpm_distance_underestimation.argtypes = [_vp, _i32, _i32, _vp, _i64, _vp, _vp, _vp, _vp, _vp]
+    L.rpm_motion_validity.argtypes = [_vp, _i32, _i32, _vp, _vp, _i64, _vp, _i32, ctypes.c_float, _i32, _vp, _vp, _vp]
     L.rpm_enclosing_radii.argtypes = [_vp, _i32, _vp, _i64, _vp, _vp]
     L.rpm_extend_spines.argtypes = [_vp, _i32, _vp, _vp, _vp, _vp, _i64, _i32, _i32, _vp, _vp, _vp]
     L.rpm_reached_states.argtypes = [_vp, _i32, _i32, _vp, _vp, _i64, ctypes.POINTER(SpineParams), _vp, _vp, _vp, _vp]
@@ -177,6 +178,15 @@ class Engine:
                                    _ptr(checks))
         _check(self.lib.rpm_check_edges_batch(self.ctx, prec, ctypes.addressof(arr), len(items), stream))
 
+    def motion_validity(self, scene_id, q_prev, q_cur, movers, max_iter_time, num_points, valid, checks=None,
+                        precision="fp32_ref", stream=None):
+        """MotionValidity::check per motion (torch CUDA tensors q_prev, q_cur [M][D], valid [M] uint8,
+        checks [M] int32); movers: a ctypes array of MovingBox."""
+        prec = PRECISIONS[precision] if isinstance(precision, str) else int(precision)
+        _check(self.lib.rpm_motion_validity(self.ctx, scene_id, prec, _ptr(q_prev), _ptr(q_cur), int(q_prev.shape[0]),
+                                            ctypes.addressof(movers) if len(movers) else None, len(movers),
+                                            float(max_iter_time), int(num_points), _ptr(valid), _ptr(checks), stream))
+
     def enclosing_radii(self, robot_id, q, radii, stream=None):
         """computeEnclosingRadii: q [C][D] float32, radii [C][D][D+1] float32 (torch CUDA tensors)."""
         _check(self.lib.rpm_enclosing_radii(self.ctx, robot_id, _ptr(q), int(q.shape[0]), _ptr(radii), stream))
@@ -285,7 +295,7 @@ ABI_SYMBOLS = [
     "rpm_ctx_set_timing", "rpm_last_timing", "rpm_probe_fp32_peak", "rpm_check_configs_noalloc", "rpm_check_batch",
     "rpm_check_edges", "rpm_check_edges_batch", "rpm_ctx_set_graphs", "rpm_autotune_edges", "rpm_set_edge_ctas", "rpm_ctx_set_layout",
     "rpm_distance_nearest", "rpm_distance_underestimation", "rpm_enclosing_radii", "rpm_extend_spines",
-    "rpm_reached_states",
+    "rpm_reached_states", "rpm_motion_validity",
     "rpm_server_create", "rpm_server_submit", "rpm_server_poll", "rpm_server_wait", "rpm_server_release",
     "rpm_server_replay", "rpm_server_stats", "rpm_server_destroy",
 ]
