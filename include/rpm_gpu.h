@@ -316,6 +316,40 @@ int rpm_motion_validity(rpm_ctx *ctx, int32_t scene_id, int32_t precision, const
                         const float *q_cur_dev, int64_t num_motions, const rpm_moving_box *boxes, int32_t num_boxes,
                         float max_iter_time, int32_t num_points, uint8_t *valid_dev, int32_t *checks_dev, void *stream);
 
+/* ---- scene I/O (host only) -------------------------------------------------
+ * The reference's scenario files.  rpm_scenario_read reads a scenario YAML
+ * (data/<robot>/<scenario>/*.yaml) as Environment::Environment
+ * (Environment.cpp:13-109) does: box obstacles as fcl world AABBs
+ * (rpm_box_aabb of dim, pos and rot [x, y, z, w]), their min_dist_tol
+ * (MAX_DISTANCE when absent) and flags (label "ground" -> RPM_OBS_GROUND,
+ * "dynamic_obstacle" -> RPM_OBS_DYNAMIC; the ground is left out when
+ * robot.ground_included is 0), plus the robot fields below.  Up to
+ * 'capacity' obstacles are written (outputs nullable); info->num_obstacles is
+ * the total, so a first call with capacity 0 sizes the arrays.  Spheres are
+ * skipped (the reference never constructs them); any other object type is an
+ * error. */
+typedef struct rpm_scenario_info {
+    char type[32];                       /* robot.type, e.g. "xarm6", "spatial_10dof" */
+    int32_t num_dofs;                    /* robot.num_DOFs */
+    int32_t ground_included;             /* robot.ground_included (0 when absent) */
+    int32_t num_radii;                   /* entries of robot.capsules_radius (1 = broadcast) */
+    int32_t num_obstacles;
+    float capsules_radius[RPM_MAX_DOF];
+    float gripper_length;
+    float ws_center[3];
+    float ws_radius;
+    float q_start[RPM_MAX_DOF];
+    float q_goal[RPM_MAX_DOF];
+} rpm_scenario_info;
+int rpm_scenario_read(const char *path, rpm_scenario_info *info, float *aabb_out, float *tol_out, uint8_t *flags_out,
+                      int32_t capacity);
+/* One run of a random_scenarios.yaml (apps/test_drgbt_random_obstacles.cpp:125-151):
+ * scenario_<num_obstacles>/run_<run>: start and goal (num_dofs each) and, per
+ * object_j, pos and vel (num_obstacles x 3 each).  The objects are boxes of
+ * the scenario's random_obstacles.dim with label "dynamic_obstacle". */
+int rpm_random_scenario_read(const char *path, int32_t num_obstacles, int32_t run, int32_t num_dofs, float *start,
+                             float *goal, float *pos, float *vel);
+
 /* ---- serving loop (continuous batching) -----------------------------------
  * Planners submit isValid / distance batches and edge batches of any size
  * against resident scenes while obstacles move (the DRGBT replanning shape,

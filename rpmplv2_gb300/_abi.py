@@ -104,3 +104,20 @@ class MovingBox(ctypes.Structure):
         ("pos", ctypes.c_float * 3),
         ("quat_xyzw", ctypes.c_float * 4),
     ]
+
+
+class ScenarioInfo(ctypes.Structure):
+    """rpm_scenario_info."""
+    _fields_ = [
+        ("type", ctypes.c_char * 32),
+        ("num_dofs", ctypes.c_int32),
+        ("ground_included", ctypes.c_int32),
+        ("num_radii", ctypes.c_int32),
+        ("num_obstacles", ctypes.c_int32),
+        ("capsules_radius", ctypes.c_float * RPM_MAX_DOF),
+        ("gripper_length", ctypes.c_float),
+        ("ws_center", ctypes.c_float * 3),
+        ("ws_radius", ctypes.c_float),
+        ("q_start", ctypes.c_float * RPM_MAX_DOF),
+        ("q_goal", ctypes.c_float * RPM_MAX_DOF),
+    ]

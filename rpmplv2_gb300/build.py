@@ -15,7 +15,7 @@ LIB = os.path.join(OUT_DIR, "librpm_gb300.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off"]
 UNITS = {"rpm_exact.cu": ["--fmad=false"], "rpm_fast.cu": ["--fmad=true"], "rpm_api.cu": [],
-         "rpm_noalloc.cu": ["--fmad=false"], "rpm_server.cu": []}
+         "rpm_noalloc.cu": ["--fmad=false"], "rpm_server.cu": [], "rpm_io.cu": []}
 
 
 def _deps():

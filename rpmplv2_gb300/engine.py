@@ -60,6 +60,8 @@ def load(build_if_missing=False):
     L.rpm_ctx_set_layout.argtypes = [_vp, ctypes.c_int32]
     L.rpm_distance_nearest.argtypes = [_vp, _i32, _i32, _vp, _i64, _vp, _vp, _vp, _vp, _vp]
     L.rpm_distance_underestimation.argtypes = [_vp, _i32, _i32, _vp, _i64, _vp, _vp, _vp, _vp, _vp]
+    L.rpm_scenario_read.argtypes = [ctypes.c_char_p, _vp, _vp, _vp, _vp, _i32]
+    L.rpm_random_scenario_read.argtypes = [ctypes.c_char_p, _i32, _i32, _i32, _vp, _vp, _vp, _vp]
     L.rpm_motion_validity.argtypes = [_vp, _i32, _i32, _vp, _vp, _i64, _vp, _i32, ctypes.c_float, _i32, _vp, _vp, _vp]
     L.rpm_enclosing_radii.argtypes = [_vp, _i32, _vp, _i64, _vp, _vp]
     L.rpm_extend_spines.argtypes = [_vp, _i32, _vp, _vp, _vp, _vp, _i64, _i32, _i32, _vp, _vp, _vp]
@@ -295,7 +297,7 @@ ABI_SYMBOLS = [
     "rpm_ctx_set_timing", "rpm_last_timing", "rpm_probe_fp32_peak", "rpm_check_configs_noalloc", "rpm_check_batch",
     "rpm_check_edges", "rpm_check_edges_batch", "rpm_ctx_set_graphs", "rpm_autotune_edges", "rpm_set_edge_ctas", "rpm_ctx_set_layout",
     "rpm_distance_nearest", "rpm_distance_underestimation", "rpm_enclosing_radii", "rpm_extend_spines",
-    "rpm_reached_states", "rpm_motion_validity",
+    "rpm_reached_states", "rpm_motion_validity", "rpm_scenario_read", "rpm_random_scenario_read",
     "rpm_server_create", "rpm_server_submit", "rpm_server_poll", "rpm_server_wait", "rpm_server_release",
     "rpm_server_replay", "rpm_server_stats", "rpm_server_destroy",
 ]

@@ -23,6 +23,7 @@ Every array is float32 (the reference's State coordinates are
 Eigen::VectorXf, include/state_spaces/State.h:27).
 """
 import math
+import os
 
 import numpy as np
 
@@ -189,3 +190,60 @@ def mixed_dof_workload(counts=(32768, 49152, 49152), seed=3):
         robot = _robots.spatial(dofs, radius=0.03)
         parts.append((robot, uniform_configs(rng, n, dofs)))
     return scene, parts
+
+
+# ------------------------------------------------------------ scene I/O --
+def load_scenario(path):
+    """A scenario YAML of the reference (Environment.cpp:13-109), read by the
+    library's rpm_scenario_read.  Returns (info, Scene): info is a dict of the
+    robot fields (type, num_dofs, ground_included, capsules_radius,
+    gripper_length, ws_center, ws_radius, q_start, q_goal)."""
+    import ctypes
+    from . import _abi
+    from .engine import _check, load
+    lib = load()
+    info = _abi.ScenarioInfo()
+    _check(lib.rpm_scenario_read(os.fsencode(path), ctypes.byref(info), None, None, None, 0))
+    n = info.num_obstacles
+    aabb = np.zeros((max(n, 1), 6), np.float32)
+    tol = np.zeros(max(n, 1), np.float32)
+    flags = np.zeros(max(n, 1), np.uint8)
+    _check(lib.rpm_scenario_read(os.fsencode(path), ctypes.byref(info), aabb.ctypes.data, tol.ctypes.data,
+                                 flags.ctypes.data, n))
+    D = info.num_dofs
+    out = {"type": info.type.decode(), "num_dofs": D, "ground_included": info.ground_included,
+           "capsules_radius": np.array(info.capsules_radius[:info.num_radii], np.float32),
+           "gripper_length": float(info.gripper_length), "ws_center": np.array(info.ws_center[:], np.float32),
+           "ws_radius": float(info.ws_radius), "q_start": np.array(info.q_start[:D], np.float32),
+           "q_goal": np.array(info.q_goal[:D], np.float32)}
+    return out, Scene(aabb[:n], tol[:n], flags[:n])
+
+
+def robot_of_scenario(info):
+    """The robot a scenario names, with its capsule radii, gripper and ground rule."""
+    name = info["type"]
+    radius = info["capsules_radius"] if info["capsules_radius"].size else None
+    kw = {} if radius is None else {"radius": radius}
+    if name == "xarm6":
+        return _robots.xarm6(gripper_length=info["gripper_length"], ground_included=info["ground_included"], **kw)
+    rb = _robots.by_name(name, **kw)
+    rb.set_ground_included(info["ground_included"])
+    return rb
+
+
+def load_random_scenario(path, num_obstacles, run, num_dofs, obstacle_dim):
+    """One run of random_scenarios.yaml (apps/test_drgbt_random_obstacles.cpp:125-151):
+    start, goal, the objects' positions and velocities, and the objects as a
+    Scene of "dynamic_obstacle" boxes of obstacle_dim (identity rotation)."""
+    from .engine import _check, load
+    lib = load()
+    start = np.zeros(num_dofs, np.float32)
+    goal = np.zeros(num_dofs, np.float32)
+    pos = np.zeros((max(num_obstacles, 1), 3), np.float32)
+    vel = np.zeros((max(num_obstacles, 1), 3), np.float32)
+    _check(lib.rpm_random_scenario_read(os.fsencode(path), int(num_obstacles), int(run), int(num_dofs),
+                                        start.ctypes.data, goal.ctypes.data, pos.ctypes.data, vel.ctypes.data))
+    pos, vel = pos[:num_obstacles], vel[:num_obstacles]
+    boxes = np.array([box_aabb(obstacle_dim, p) for p in pos], np.float32).reshape(-1, 6)
+    flags = np.full(num_obstacles, RPM_OBS_DYNAMIC, np.uint8)
+    return start, goal, pos, vel, Scene(boxes, flags=flags)
