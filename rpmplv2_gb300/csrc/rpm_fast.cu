@@ -10,7 +10,7 @@
 
 namespace rpm {
 
-__global__ void __launch_bounds__(kThreads) k_check_fp32(const __grid_constant__ KParams P) {
+__global__ void __launch_bounds__(kThreads, 5) k_check_fp32(const __grid_constant__ KParams P) {
     extern __shared__ __align__(128) unsigned char smem[];
     __shared__ uint64_t bar;
     __shared__ WarpShared<float> wsh[kThreads / 32];
