@@ -46,8 +46,8 @@ def parse():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--configs", type=int, default=NUM_CONFIGS)
     ap.add_argument("--no-extra", action="store_true", help="skip the edge, mixed-DOF, large-scene and serving measurements")
-    ap.add_argument("--extra", default="edges,mixed,large,serve",
-                    help="comma list of extra measurements: edges, mixed, large, serve")
+    ap.add_argument("--extra", default="edges,mixed,large,serve,planner",
+                    help="comma list of extra measurements: edges, mixed, large, serve, planner")
     return ap.parse_args()
 
 
@@ -167,6 +167,85 @@ def extra_workloads(eng, args):
         out["large_scene"] = large_line(eng, scenes, timed)
     if "serve" in which:
         out["serve"] = serve_line(eng, serve)
+    if "planner" in which:
+        out["planner"] = planner_line(eng, scenes, serve, timed)
+    return out
+
+
+def planner_line(eng, scenes, serve, timed):
+    """The planner-side steps after the distance profile, each beside the oracle
+    on one host core: the DRGBT horizon (computeReachedState of every horizon
+    state, then computeDistance), MotionValidity::check with moving boxes, and
+    RBT spines (extendSpine)."""
+    import time
+    import torch
+    from oracle import oracle as O
+    from rpmplv2_gb300 import _abi
+    out = {}
+    rng = np.random.default_rng(12)
+    # ---- DRGBT horizon on the xarm6 workload
+    robot, scene, q = scenes.xarm6_workload(4096, seed=13)
+    sid = eng.create_scene(eng.upload_robot(robot), scene)
+    _, d, _ = eng.check_configs_host(sid, q[:512], "fp32_recheck", want=("dist",))
+    qc = torch.from_numpy(np.ascontiguousarray(q[int(np.argmax(d))])).cuda()
+    for H in (10, 4096):
+        hz = torch.from_numpy(scenes.uniform_configs(rng, H, 6)).cuda()
+        qr = torch.zeros((H, 6), dtype=torch.float32, device="cuda")
+        st = torch.zeros(H, dtype=torch.int32, device="cuda")
+        dd = torch.zeros(H, dtype=torch.float64, device="cuda")
+        ms = timed(lambda: eng.reached_states(sid, qc, hz, qr, st, dd, precision="fp32_recheck"), steps=5, warmup=2)
+        out["drgbt_horizon_%d" % H] = {"ms_per_call": ms, "states_per_s": H / (ms / 1e3)}
+    hz10 = scenes.uniform_configs(rng, 10, 6)
+    t0 = time.perf_counter()
+    rq, _ = O.reached_states(robot, scene, qc.cpu().numpy(), hz10)
+    O.check_configs(robot, scene, rq, prec="ref32", want=("dist",), nthreads=1)
+    out["drgbt_horizon_10"]["cpu_ms"] = (time.perf_counter() - t0) * 1e3
+    out["drgbt_horizon_10"]["workload"] = ("xarm6, 50 cubes + ground; 5 layers, NUM_ITER_SPINE 1, expanded bubble, "
+                                           "D_CRIT 0.05, then computeDistance (FP32+recheck); cpu_ms: oracle, 1 core")
+    eng.destroy_scene(sid)
+    # ---- MotionValidity::check, spatial_10dof among 200 boxes, 5 of them moving at up to 1.6 m/s
+    rb = serve.make_robot("spatial_10dof")
+    sc = serve._scene_for(rb, rng, 200)
+    idx = rng.choice(sc.n, 5, replace=False)
+    mv = (_abi.MovingBox * 5)()
+    for k, j in enumerate(idx):
+        dim = rng.uniform(0.05, 0.2, 3).astype(np.float32)
+        pos = rng.uniform(-0.8, 0.8, 3).astype(np.float32)
+        sc.aabb[j] = scenes.box_aabb(dim, pos)
+        sc.flags[j] |= _abi.RPM_OBS_DYNAMIC
+        mv[k] = _abi.MovingBox(int(j), float(rng.uniform(0, 1.6)), tuple(dim), tuple(pos), (0.0, 0.0, 0.0, 1.0))
+    sid = eng.create_scene(eng.upload_robot(rb), sc)
+    M, N = 4096, 8   # NUM_VALIDITY_POINTS_CHECK = ceil(1.6 m/s x 0.05 s / 0.01 m)
+    q1 = scenes.uniform_configs(rng, M, 10)
+    q2 = (q1 + rng.uniform(-0.3, 0.3, q1.shape)).astype(np.float32)
+    q1d, q2d = torch.from_numpy(q1).cuda(), torch.from_numpy(q2).cuda()
+    v = torch.zeros(M, dtype=torch.uint8, device="cuda")
+    kk = torch.zeros(M, dtype=torch.int32, device="cuda")
+    ms = timed(lambda: eng.motion_validity(sid, q1d, q2d, mv, 0.05, N, v, kk, precision="fp32_ref"), steps=5, warmup=2)
+    t0 = time.perf_counter()
+    O.motion_validity(rb, sc, q1[:256], q2[:256], mv, 0.05, N, prec="ref32")
+    cpu_s = (time.perf_counter() - t0) / 256
+    out["motion_validity"] = {"workload": "spatial_10dof among 200 boxes, 5 moving straight, 4,096 motions x 8 checks, "
+                                          "reference numerics", "motions_per_s": M / (ms / 1e3), "ms_per_step": ms,
+                              "valid_fraction": float(v.float().mean()), "cpu_motions_per_s": 1.0 / cpu_s}
+    eng.destroy_scene(sid)
+    # ---- RBT spines (xarm6, 5 iterations, expanded bubble)
+    robot = serve.make_robot("xarm6")
+    C = 65536
+    qs = scenes.uniform_configs(rng, C, 6)
+    qe = scenes.uniform_configs(rng, C, 6)
+    prof = rng.uniform(0.01, 0.4, (C, 6)).astype(np.float32)
+    dist = prof.min(axis=1).astype(np.float32)
+    rid = eng.upload_robot(robot)
+    tq, te, td, tp = (torch.from_numpy(a).cuda() for a in (qs, qe, dist, prof))
+    qn = torch.zeros((C, 6), dtype=torch.float32, device="cuda")
+    stt = torch.zeros(C, dtype=torch.int32, device="cuda")
+    ms = timed(lambda: eng.extend_spines(rid, tq, te, td, tp, qn, stt, num_iter=5), steps=5, warmup=2)
+    t0 = time.perf_counter()
+    O.extend_spines(robot, qs[:4096], qe[:4096], dist[:4096], prof[:4096], num_iter=5)
+    cpu_s = (time.perf_counter() - t0) / 4096
+    out["spines"] = {"workload": "xarm6 extendSpine, 65,536 spines, NUM_ITER_SPINE 5, expanded bubble",
+                     "spines_per_s": C / (ms / 1e3), "ms_per_step": ms, "cpu_spines_per_s": 1.0 / cpu_s}
     return out
 
 
@@ -241,6 +320,17 @@ def serve_line(eng, serve):
                              "boxes moving up to 1.6 m/s updated every 1 ms), Poisson 20,000 req/s for 0.5 s, "
                              "sizes log-uniform 1-65,536, isValid / distance / edge in equal shares",
                  "memory_budget_bytes": 8 << 30, "slots": 6})
+    # capacity: the same trace submitted at once; latency at a rate the engine sustains
+    t = srv.replay(wl["requests"], [0.0] * len(wl["requests"]))
+    summ["capacity_req_per_s"] = len(t) / max(x.t_done for x in t)
+    for sid in wl["scene_ids"]:
+        eng.destroy_scene(sid)
+    wl12 = serve.serving_workload(eng, seed=5, rate=12000.0, duration=0.5)
+    t12 = srv.replay(wl12["requests"], wl12["arrivals"], wl12["motions"], period=0.001)
+    s12 = serve.latency_summary(t12, wl12["meta"])
+    summ["at_12000_req_per_s"] = {k: s12[k] for k in ("queries_per_s", "p50_ms", "p99_ms", "p50_ms_4096", "p99_ms_4096",
+                                                      "p99_ms_le4096", "median_run_ms")}
+    wl = wl12
     srv.close()
     for sid in wl["scene_ids"]:
         eng.destroy_scene(sid)
