@@ -193,7 +193,7 @@ def planner_line(eng, scenes, serve, timed):
         qr = torch.zeros((H, 6), dtype=torch.float32, device="cuda")
         st = torch.zeros(H, dtype=torch.int32, device="cuda")
         dd = torch.zeros(H, dtype=torch.float64, device="cuda")
-        ms = timed(lambda: eng.reached_states(sid, qc, hz, qr, st, dd, precision="fp32_recheck"), steps=5, warmup=2)
+        ms = timed(lambda: eng.reached_states(sid, qc, hz, qr, st, dd, precision="fp32_ref"), steps=5, warmup=2)
         out["drgbt_horizon_%d" % H] = {"ms_per_call": ms, "states_per_s": H / (ms / 1e3)}
     hz10 = scenes.uniform_configs(rng, 10, 6)
     t0 = time.perf_counter()
@@ -201,7 +201,8 @@ def planner_line(eng, scenes, serve, timed):
     O.check_configs(robot, scene, rq, prec="ref32", want=("dist",), nthreads=1)
     out["drgbt_horizon_10"]["cpu_ms"] = (time.perf_counter() - t0) * 1e3
     out["drgbt_horizon_10"]["workload"] = ("xarm6, 50 cubes + ground; 5 layers, NUM_ITER_SPINE 1, expanded bubble, "
-                                           "D_CRIT 0.05, then computeDistance (FP32+recheck); cpu_ms: oracle, 1 core")
+                                           "D_CRIT 0.05, then computeDistance, all in the reference's numerics; "
+                                           "cpu_ms: oracle, 1 core")
     eng.destroy_scene(sid)
     # ---- MotionValidity::check, spatial_10dof among 200 boxes, 5 of them moving at up to 1.6 m/s
     rb = serve.make_robot("spatial_10dof")
