@@ -19,6 +19,7 @@ template <typename T> struct ObsView {
     const T *rows;        // [>=7][n_pad] : six AABB coordinates, min_dist_tol
     const float *ground;  // [n_pad] 1.0 for "ground"
     int n, n_pad;
+    const float *frows = nullptr;   // FP64 form: the same rows in float (exact), for the float pre-test
     RPM_HD void box(int j, T *o) const {
 #pragma unroll
         for (int k = 0; k < 6; ++k) o[k] = rows[k * n_pad + j];
@@ -443,6 +444,25 @@ __device__ int warp_check(WarpShared<T> &sh, const DevRobot &rb, const ObsView<T
         sh.lmin[lane] = Key<T>::of(nm.maxd);
         sh.hitj[lane] = 0x7fffffff;
         sh.hitv[lane] = T(0);
+        // FP64 form: a float pre-test of each pair's gap, from the segment box
+        // rounded outwards and thresholds raised by 1e-5 m, so the FP64 gap and
+        // threshold arithmetic below runs only for pairs near one of its
+        // decisions.  A pair the pre-test passes over is one the FP64 test
+        // passes over too (the float gap errs by under 1e-6 m), so the queued
+        // pairs, and the outputs, are the same.
+        float lof[3] = {0.f, 0.f, 0.f}, hif[3] = {0.f, 0.f, 0.f};
+        float tbf2 = 0.f, huntf2 = 0.f, slackf = 0.f, bestf = 0.f;
+        const bool pre = (MODE == 0) && ob.frows != nullptr;
+        if constexpr (MODE == 0) {
+            if (pre) {
+#pragma unroll
+                for (int k = 0; k < 3; ++k) { lof[k] = __double2float_rd(lo[k]); hif[k] = __double2float_ru(hi[k]); }
+                tbf2 = __double2float_ru((tb + 1e-5) * (tb + 1e-5));
+                huntf2 = __double2float_ru((hunt + 1e-5) * (hunt + 1e-5));
+                slackf = __double2float_ru(r + nm.eq + dmargin + 1e-5);
+                bestf = __double2float_ru(w.profile ? nm.maxd : best);
+            }
+        }
         __syncwarp();
         int nb = 0, nd = 0;
         for (int j = 0; j < ob.n; ++j) {
@@ -450,7 +470,27 @@ __device__ int warp_check(WarpShared<T> &sh, const DevRobot &rb, const ObsView<T
             const int hj = sh.hitj[lane];
             const bool wd = need_d && (hj == 0x7fffffff || (w.profile && j < hj));
             bool qb = false, qd = false;
-            if ((wb || wd) && !(ground_skip && ob.is_ground(j))) {
+            bool near = (wb || wd) && !(ground_skip && ob.is_ground(j));
+            if constexpr (MODE == 0) {
+                if (near && pre) {
+                    float of[6];
+#pragma unroll
+                    for (int k = 0; k < 6; ++k) of[k] = ob.frows[k * ob.n_pad + j];
+                    const float g2f = gap2_bb(lof, hif, of);
+                    bool maybe = wb && !(g2f > tbf2);
+                    if (wd && !maybe) {
+                        if (hj != 0x7fffffff) {
+                            maybe = !(g2f > huntf2);
+                        } else {
+                            const float tolf = ob.frows[kRowTol * ob.n_pad + j];
+                            const float sf = (bestf < tolf ? bestf : tolf) + slackf;
+                            maybe = !(tolf > 0.f) || !(g2f > sf * sf * 1.00001f);
+                        }
+                    }
+                    near = maybe;
+                }
+            }
+            if (near) {
                 T o[6];
                 ob.box(j, o);
                 const T g2 = gap2_bb(lo, hi, o);

@@ -15,7 +15,7 @@ namespace rpm {
 
 size_t smem_bytes(int mode, int n_pad) {
     size_t rb = sizeof(DevRobot);
-    if (mode == RPM_PREC_FP64) return rb + (size_t)kDRows * n_pad * sizeof(double) + (size_t)n_pad * sizeof(float);
+    if (mode == RPM_PREC_FP64) return rb + (size_t)kDRows * n_pad * sizeof(double) + (size_t)kFRows * n_pad * sizeof(float);
     return rb + (size_t)kFRows * n_pad * sizeof(float);
 }
 
@@ -25,13 +25,13 @@ template <int MODE>
 __device__ __forceinline__ bool stage(const Seg &sg, unsigned char *smem, uint64_t *bar, int32_t *status) {
     if (threadIdx.x == 0) {
         const uint32_t rb = (uint32_t)sizeof(DevRobot);
-        if (MODE == 0) {
+        if (MODE == 0) {   // FP64 rows, then the float rows (ground row, float pre-test)
             const uint32_t rows = (uint32_t)(kDRows * sg.n_pad * sizeof(double));
-            const uint32_t gnd = (uint32_t)(sg.n_pad * sizeof(float));
-            bulk_expect(bar, rb + rows + gnd);
+            const uint32_t frows = (uint32_t)(kFRows * sg.n_pad * sizeof(float));
+            bulk_expect(bar, rb + rows + frows);
             bulk_copy(bar, smem, sg.robot, rb);
             bulk_copy(bar, smem + rb, sg.obs_d, rows);
-            bulk_copy(bar, smem + rb + rows, sg.obs_f + (size_t)kRowGround * sg.n_pad, gnd);
+            bulk_copy(bar, smem + rb + rows, sg.obs_f, frows);
         } else {
             const uint32_t rows = (uint32_t)(kFRows * sg.n_pad * sizeof(float));
             bulk_expect(bar, rb + rows);
@@ -60,13 +60,14 @@ __global__ void __launch_bounds__(kThreads) k_check_exact(const __grid_constant_
     if (!stage<MODE>(sg, smem, &bar, P.status)) return;
     const DevRobot &rb = *reinterpret_cast<const DevRobot *>(smem);
     const T *rows = reinterpret_cast<const T *>(smem + sizeof(DevRobot));
-    const float *ground = (MODE == 0) ? reinterpret_cast<const float *>(smem + sizeof(DevRobot) + kDRows * sg.n_pad * sizeof(double))
-                                      : reinterpret_cast<const float *>(rows) + (size_t)kRowGround * sg.n_pad;
+    const float *frows = (MODE == 0) ? reinterpret_cast<const float *>(smem + sizeof(DevRobot) + kDRows * sg.n_pad * sizeof(double))
+                                     : reinterpret_cast<const float *>(rows);
+    const float *ground = frows + (size_t)kRowGround * sg.n_pad;
     const int64_t c = (int64_t)(blockIdx.x - sg.first_block) * kThreads + threadIdx.x;
     const int64_t warp0 = c - (threadIdx.x & 31);
     if (warp0 >= sg.count) return;   // whole warp idle
     const bool active = c < sg.count;
-    ObsView<T> ob{rows, ground, sg.n, sg.n_pad};
+    ObsView<T> ob{rows, ground, sg.n, sg.n_pad, MODE == 0 ? frows : nullptr};
     const Want w{sg.valid != nullptr, sg.dist != nullptr, sg.profile != nullptr};
     const int D = rb.D;
     Num<T> nm;
@@ -454,9 +455,9 @@ __global__ void __launch_bounds__(kThreads) k_edges_exact(const __grid_constant_
     if (!stage<MODE>(sg, smem, &bar, P.status)) return;
     const DevRobot &rb = *reinterpret_cast<const DevRobot *>(smem);
     const T *rows = reinterpret_cast<const T *>(smem + sizeof(DevRobot));
-    const float *ground = (MODE == 0) ? reinterpret_cast<const float *>(smem + sizeof(DevRobot) + kDRows * sg.n_pad * sizeof(double))
-                                      : reinterpret_cast<const float *>(rows) + (size_t)kRowGround * sg.n_pad;
-    const ObsView<T> ob{rows, ground, sg.n, sg.n_pad};
+    const float *frows = (MODE == 0) ? reinterpret_cast<const float *>(smem + sizeof(DevRobot) + kDRows * sg.n_pad * sizeof(double))
+                                     : reinterpret_cast<const float *>(rows);
+    const ObsView<T> ob{rows, frows + (size_t)kRowGround * sg.n_pad, sg.n, sg.n_pad, MODE == 0 ? frows : nullptr};
     edge_warps<MODE, T>(P, &rb, &ob, nm, wsh[threadIdx.x >> 5], qbuf[threadIdx.x >> 5]);
 }
 
