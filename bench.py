@@ -482,7 +482,8 @@ def run_ours(args, ws, rank, local):
                     "fraction": statistics.median(rechecked) / C, "kernel_ms": statistics.median(re_ms)},
         "clocks": clocks,
         "e2e": {"value": C * args.steps / e2e_s, "unit": "configs/s", "h2d_bytes_per_step": C * D * 4,
-                "d2h_bytes_per_step": C * (1 + 8), "call": "rpm_check_configs_host", "matches_device_run": e2e_ok},
+                "d2h_bytes_per_step": C * (1 + 8), "call": "rpm_check_configs_host", "matches_device_run": e2e_ok,
+                "transfer": "pinned host buffers read and written by the kernels over NVLink-C2C (zero-copy)"},
         "gpu_launches": 2 * args.steps,
         "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak_fp32, "unit": "TFLOP/s",
                      "frac": achieved / peak_fp32 if peak_fp32 else None, "traffic": traffic_per_launch(),

@@ -169,9 +169,12 @@ typedef struct rpm_batch_item {
 } rpm_batch_item;
 int rpm_check_batch(rpm_ctx *ctx, int32_t precision, const rpm_batch_item *items, int32_t n_items, void *stream);
 
-/* Same as rpm_check_configs with host buffers: stages through context-owned
- * pinned memory, overlaps copies with compute and returns after the results
- * are in the host buffers. */
+/* Same as rpm_check_configs with host buffers; returns after the results are
+ * in the host buffers.  When every buffer is page-locked host memory
+ * (cudaHostAlloc / cudaHostRegister), the kernels read the configurations and
+ * write the outputs there directly (over NVLink-C2C on GB300) in one launch;
+ * otherwise the call stages chunks through context-owned device memory,
+ * overlapping copies with compute. */
 int rpm_check_configs_host(rpm_ctx *ctx, int32_t scene_id, int32_t precision, const float *q_host, int64_t num_configs,
                            uint8_t *valid_host, double *dist_host, float *profile_host);
 

@@ -631,6 +631,33 @@ int enqueue_check(rpm_ctx *ctx, SceneRec *s, int prec, const float *q, int64_t C
 
 using namespace rpm::impl;
 
+// Device address of a page-locked host buffer (cudaHostAlloc / cudaHostRegister,
+// mapped), or null for any other pointer.
+template <typename P> static P *mapped_ptr(P *host) {
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, (const void *)host) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    if (a.type != cudaMemoryTypeHost || !a.devicePointer) return nullptr;
+    return reinterpret_cast<P *>(a.devicePointer);
+}
+
+// The status word of a stream's scratch after its work: a bounded device-side
+// wait that gave up is reported (and the word reset).
+static int host_status(rpm_ctx *ctx, cudaStream_t st) {
+    if (!st) return RPM_OK;
+    auto it = ctx->scratch.find(st);
+    if (it == ctx->scratch.end()) return RPM_OK;
+    int32_t v = 0;
+    CK(cudaMemcpy(&v, it->second->status, sizeof v, cudaMemcpyDeviceToHost));
+    if (v) {
+        cudaMemset(it->second->status, 0, sizeof(int32_t));
+        return fail(RPM_ERR_TIMEOUT, "a bounded device-side wait gave up (status %d)", v);
+    }
+    return RPM_OK;
+}
+
 extern "C" {
 
 const char *rpm_last_error_string(void) { return g_err.c_str(); }
@@ -1248,6 +1275,21 @@ int rpm_check_configs_host(rpm_ctx *ctx, int32_t scene_id, int32_t precision, co
     if (!s) return fail(RPM_ERR_INVALID, "unknown scene %d", scene_id);
     if (set_device(ctx)) return RPM_ERR_CUDA;
     const int D = ctx->robots[s->robot].desc.num_dofs;
+    // Pinned (page-locked, mapped) host buffers: the kernels read q and write
+    // the outputs in host memory directly, over NVLink-C2C on GB300, in one
+    // launch.  Any other buffer takes the staged path below.
+    const float *zq = mapped_ptr(q_host);
+    uint8_t *zv = valid_host ? mapped_ptr(valid_host) : nullptr;
+    double *zd = dist_host ? mapped_ptr(dist_host) : nullptr;
+    float *zp = profile_host ? mapped_ptr(profile_host) : nullptr;
+    if (num_configs > 0 && zq && (!valid_host || zv) && (!dist_host || zd) && (!profile_host || zp)) {
+        if (!ctx->hs[0]) CK(cudaStreamCreateWithFlags(&ctx->hs[0], cudaStreamNonBlocking));
+        cudaStream_t st = ctx->hs[0];
+        int rc = enqueue_check(ctx, s, precision, zq, num_configs, zv, zd, zp, st);
+        if (rc) return rc;
+        CK(cudaStreamSynchronize(st));
+        return host_status(ctx, st);
+    }
     const int64_t chunk = 1 << 18;
     if (ctx->hcap_cfg < (size_t)chunk) {
         for (int i = 0; i < 2; ++i) {
@@ -1284,14 +1326,8 @@ int rpm_check_configs_host(rpm_ctx *ctx, int32_t scene_id, int32_t precision, co
     for (int i = 0; i < 2; ++i)
         if (ctx->hs[i]) CK(cudaStreamSynchronize(ctx->hs[i]));
     for (int i = 0; i < 2; ++i) {
-        auto it = ctx->scratch.find(ctx->hs[i]);
-        if (it == ctx->scratch.end()) continue;
-        int32_t st = 0;
-        CK(cudaMemcpy(&st, it->second->status, sizeof st, cudaMemcpyDeviceToHost));
-        if (st) {
-            cudaMemset(it->second->status, 0, sizeof(int32_t));
-            return fail(RPM_ERR_TIMEOUT, "a bounded device-side wait gave up (status %d)", st);
-        }
+        const int rc = host_status(ctx, ctx->hs[i]);
+        if (rc) return rc;
     }
     return RPM_OK;
 }

@@ -81,3 +81,31 @@ def test_skeleton_fp64_bits(engine):
     engine.sync()
     ref = O.skeleton(robot, q, prec="ref64")
     assert np.array_equal(out.cpu().numpy().view(np.uint64), ref.view(np.uint64))
+
+
+@pytest.mark.parametrize("prec", ["fp32_recheck", "fp64"])
+def test_host_buffers_pinned_and_pageable(engine, prec):
+    """rpm_check_configs_host: pinned buffers (read and written by the kernels in
+    host memory) and pageable ones (staged in chunks) give the device run's results."""
+    import torch
+    from rpmplv2_gb300 import serve
+    robot, scene, q = scenes.xarm6_workload(300_000, seed=57)
+    sid = engine.create_scene(engine.upload_robot(robot), scene)
+    C = q.shape[0]
+    v_dev = torch.zeros(C, dtype=torch.uint8, device="cuda")
+    d_dev = torch.zeros(C, dtype=torch.float64, device="cuda")
+    engine.check_configs(sid, torch.from_numpy(q).cuda(), prec, v_dev, d_dev, None)
+    engine.sync()
+    vp, dp, _ = engine.check_configs_host(sid, q, prec, want=("valid", "dist"))
+    assert np.array_equal(vp, v_dev.cpu().numpy()) and np.array_equal(dp.view(np.uint64), d_dev.cpu().numpy().view(np.uint64))
+    qs = serve.pinned(q.shape, np.float32)
+    qs[:] = q
+    vs = serve.pinned(C, np.uint8)
+    ds = serve.pinned(C, np.float64)
+    import ctypes
+    lib = engine.lib
+    from rpmplv2_gb300._abi import PRECISIONS
+    assert lib.rpm_check_configs_host(engine.ctx, sid, PRECISIONS[prec], qs.ctypes.data, C, vs.ctypes.data,
+                                      ds.ctypes.data, None) == 0
+    assert np.array_equal(vs, v_dev.cpu().numpy()) and np.array_equal(ds.view(np.uint64), d_dev.cpu().numpy().view(np.uint64))
+    engine.destroy_scene(sid)
