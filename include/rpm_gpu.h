@@ -318,6 +318,13 @@ typedef struct rpm_moving_box {
 int rpm_motion_validity(rpm_ctx *ctx, int32_t scene_id, int32_t precision, const float *q_prev_dev,
                         const float *q_cur_dev, int64_t num_motions, const rpm_moving_box *boxes, int32_t num_boxes,
                         float max_iter_time, int32_t num_points, uint8_t *valid_dev, int32_t *checks_dev, void *stream);
+/* The environment side of MotionValidity::check: 'steps' calls of
+ * Environment::moveStraight(delta_time) (Environment.cpp:220-233) on the
+ * given boxes -- boxes[b].pos is advanced in place, in float as the
+ * reference does -- and their new AABBs written to the device scene as one
+ * incremental update (rpm_scene_update; version in *version_out, nullable). */
+int rpm_scene_move_straight(rpm_ctx *ctx, int32_t scene_id, rpm_moving_box *boxes, int32_t num_boxes, float delta_time,
+                            int32_t steps, uint64_t *version_out);
 
 /* ---- scene I/O (host only) -------------------------------------------------
  * The reference's scenario files.  rpm_scenario_read reads a scenario YAML

@@ -1181,6 +1181,19 @@ int rpm_motion_validity(rpm_ctx *ctx, int32_t scene_id, int32_t precision, const
     return near_done(ctx, buf, st);
 }
 
+int rpm_scene_move_straight(rpm_ctx *ctx, int32_t scene_id, rpm_moving_box *boxes, int32_t num_boxes, float delta_time,
+                            int32_t steps, uint64_t *version_out) {
+    if (!ctx || num_boxes < 0 || (num_boxes > 0 && !boxes) || steps < 0) return fail(RPM_ERR_INVALID, "bad arguments");
+    std::vector<int32_t> idx((size_t)num_boxes);
+    std::vector<float> aabb((size_t)num_boxes * 6);
+    for (int b = 0; b < num_boxes; ++b) {
+        for (int k = 0; k < steps; ++k) boxes[b].pos[0] = boxes[b].pos[0] - delta_time * boxes[b].max_vel;
+        rpm_box_aabb(boxes[b].dim, boxes[b].pos, boxes[b].quat_xyzw, aabb.data() + 6 * (size_t)b);
+        idx[b] = boxes[b].index;
+    }
+    return rpm_scene_update(ctx, scene_id, idx.data(), aabb.data(), num_boxes, version_out);
+}
+
 int rpm_distance_underestimation(rpm_ctx *ctx, int32_t scene_id, int32_t precision, const float *q_dev,
                                  int64_t num_configs, const float *nearest_dev, double *dist_dev, float *profile_dev,
                                  uint8_t *complete_dev, void *stream) {

@@ -62,6 +62,7 @@ def load(build_if_missing=False):
     L.rpm_distance_underestimation.argtypes = [_vp, _i32, _i32, _vp, _i64, _vp, _vp, _vp, _vp, _vp]
     L.rpm_scenario_read.argtypes = [ctypes.c_char_p, _vp, _vp, _vp, _vp, _i32]
     L.rpm_random_scenario_read.argtypes = [ctypes.c_char_p, _i32, _i32, _i32, _vp, _vp, _vp, _vp]
+    L.rpm_scene_move_straight.argtypes = [_vp, _i32, _vp, _i32, ctypes.c_float, _i32, ctypes.POINTER(ctypes.c_uint64)]
     L.rpm_motion_validity.argtypes = [_vp, _i32, _i32, _vp, _vp, _i64, _vp, _i32, ctypes.c_float, _i32, _vp, _vp, _vp]
     L.rpm_enclosing_radii.argtypes = [_vp, _i32, _vp, _i64, _vp, _vp]
     L.rpm_extend_spines.argtypes = [_vp, _i32, _vp, _vp, _vp, _vp, _i64, _i32, _i32, _vp, _vp, _vp]
@@ -189,6 +190,14 @@ class Engine:
                                             ctypes.addressof(movers) if len(movers) else None, len(movers),
                                             float(max_iter_time), int(num_points), _ptr(valid), _ptr(checks), stream))
 
+    def move_straight(self, scene_id, movers, delta_time, steps):
+        """Environment::moveStraight 'steps' times on the movers (positions advanced in place) and the
+        device scene; returns the scene's new version."""
+        ver = ctypes.c_uint64()
+        _check(self.lib.rpm_scene_move_straight(self.ctx, scene_id, ctypes.addressof(movers) if len(movers) else None,
+                                                len(movers), float(delta_time), int(steps), ctypes.byref(ver)))
+        return ver.value
+
     def enclosing_radii(self, robot_id, q, radii, stream=None):
         """computeEnclosingRadii: q [C][D] float32, radii [C][D][D+1] float32 (torch CUDA tensors)."""
         _check(self.lib.rpm_enclosing_radii(self.ctx, robot_id, _ptr(q), int(q.shape[0]), _ptr(radii), stream))
@@ -297,7 +306,7 @@ ABI_SYMBOLS = [
     "rpm_ctx_set_timing", "rpm_last_timing", "rpm_probe_fp32_peak", "rpm_check_configs_noalloc", "rpm_check_batch",
     "rpm_check_edges", "rpm_check_edges_batch", "rpm_ctx_set_graphs", "rpm_autotune_edges", "rpm_set_edge_ctas", "rpm_ctx_set_layout",
     "rpm_distance_nearest", "rpm_distance_underestimation", "rpm_enclosing_radii", "rpm_extend_spines",
-    "rpm_reached_states", "rpm_motion_validity", "rpm_scenario_read", "rpm_random_scenario_read",
+    "rpm_reached_states", "rpm_motion_validity", "rpm_scene_move_straight", "rpm_scenario_read", "rpm_random_scenario_read",
     "rpm_server_create", "rpm_server_submit", "rpm_server_poll", "rpm_server_wait", "rpm_server_release",
     "rpm_server_replay", "rpm_server_stats", "rpm_server_destroy",
 ]

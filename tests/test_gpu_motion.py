@@ -56,3 +56,46 @@ def test_motion_validity(engine, name, n):
     if name != "planar_2dof":   # the 1 m planar links meet the sweeping boxes on every motion
         assert 0 < rv.sum() < M
     engine.destroy_scene(sid)
+
+
+def test_move_straight_updates_the_scene(engine):
+    """MotionValidity::check moves the environment once per check it makes; moving the
+    device scene by those steps leaves it equal to the oracle's moved scene."""
+    rng = np.random.default_rng(93)
+    rb = serve.make_robot("spatial_10dof")
+    scene = serve._scene_for(rb, rng, 60)
+    specs = []
+    for j in range(3):
+        dim = rng.uniform(0.05, 0.2, 3).astype(np.float32)
+        pos = rng.uniform(-0.6, 0.6, 3).astype(np.float32)
+        scene.aabb[j] = scenes.box_aabb(dim, pos)
+        scene.flags[j] |= _abi.RPM_OBS_DYNAMIC
+        specs.append((j, float(rng.uniform(5.0, 20.0)), dim, pos))
+    mv = movers_of(specs)
+    sid = engine.create_scene(engine.upload_robot(rb), scene)
+    q1 = scenes.uniform_configs(rng, 1, 10)
+    q2 = (q1 + 0.3).astype(np.float32)
+    N, T = 10, 0.05
+    k = torch.zeros(1, dtype=torch.int32, device="cuda")
+    v = torch.zeros(1, dtype=torch.uint8, device="cuda")
+    engine.motion_validity(sid, _t(q1), _t(q2), mv, T, N, v, k)
+    engine.sync()
+    steps = int(k.cpu().numpy()[0])
+    engine.move_straight(sid, mv, np.float32(T) / np.float32(N), steps)
+    # the oracle's view of the same motion of the boxes
+    dt = np.float32(np.float32(T) / np.float32(N))
+    moved = scenes.Scene(scene.aabb.copy(), scene.tol.copy(), scene.flags.copy())
+    for (j, vel, dim, pos), box in zip(specs, mv):
+        p = pos.copy()
+        for _ in range(steps):
+            p[0] = np.float32(p[0] - np.float32(dt * np.float32(vel)))
+        assert np.array_equal(np.array(box.pos[:], np.float32), p)
+        moved.aabb[j] = scenes.box_aabb(dim, p)
+    q = scenes.uniform_configs(rng, 2048, 10)
+    vd = torch.zeros(2048, dtype=torch.uint8, device="cuda")
+    dd = torch.zeros(2048, dtype=torch.float64, device="cuda")
+    engine.check_configs(sid, _t(q), "fp32_ref", vd, dd, None)
+    engine.sync()
+    rv, rd, _ = O.check_configs(rb, moved, q, prec="ref32", want=("valid", "dist"))
+    assert np.array_equal(vd.cpu().numpy(), rv) and np.array_equal(dd.cpu().numpy().view(np.uint64), rd.view(np.uint64))
+    engine.destroy_scene(sid)
