@@ -127,7 +127,9 @@ int rpm_robot_upload(rpm_ctx *ctx, const rpm_robot_desc *desc, int32_t *robot_id
  * floats (xmin, ymin, zmin, xmax, ymax, zmax) per obstacle, exactly the
  * 'obs' vector of RealVectorSpace.cpp:293-295; min_dist_tol_host is
  * Object::getMinDistTol (Box.cpp:13, YAML min_dist_tol); flags_host holds
- * RPM_OBS_* bits.  min_dist_tol_host and flags_host may be NULL (MAX_DISTANCE, 0). */
+ * RPM_OBS_* bits.  min_dist_tol_host and flags_host may be NULL (MAX_DISTANCE, 0).
+ * A scene holds at most RPM_MAX_OBSTACLES obstacles (RPM_ERR_RANGE beyond). */
+#define RPM_MAX_OBSTACLES 2048
 int rpm_scene_create(rpm_ctx *ctx, int32_t robot_id, const float *aabb_host, const float *min_dist_tol_host,
                      const uint8_t *flags_host, int32_t n, int32_t *scene_id);
 /* Replace the AABBs of obstacles idx[0..m) (Object::setPosition, Object.cpp:21-26;

@@ -51,7 +51,7 @@ RPM_HD float fadd(float a, float b) {
 }
 
 constexpr int kMaxDof = RPM_MAX_DOF;
-constexpr int kMaxObstacles = 2048;     // per scene, shared-memory resident
+constexpr int kMaxObstacles = RPM_MAX_OBSTACLES;   // per scene (the pair-recheck entry keeps 11 bits of index)
 constexpr int kFRows = 8;               // float rows per scene
 constexpr int kDRows = 7;               // double rows per scene
 constexpr int kRowTol = 6;

@@ -240,3 +240,33 @@ def test_warp_edges_big_scene_fixed_count(engine, layout):
     finally:
         engine.set_graphs(False)
         engine.destroy_scene(sid)
+
+
+def test_maximum_scene_size(engine):
+    """RPM_MAX_OBSTACLES boxes: every layout and form against the oracle (the
+    pair-recheck entries index obstacles up to 2047); one more is refused."""
+    from rpmplv2_gb300 import robots
+    from rpmplv2_gb300.engine import RpmError
+    rng = np.random.default_rng(97)
+    rb = robots.spatial(14, radius=0.03)
+    n = 2048
+    boxes = [scenes.box_aabb(rng.uniform(0.01, 0.04, 3), c) for c in scenes._ball(rng, n, scenes.SPATIAL_WS_CENTER, 1.5)]
+    sc = scenes.Scene(np.array(boxes), tol=rng.uniform(0.2, 2.0, n).astype(np.float32))
+    q = scenes.uniform_configs(rng, 3000, 14)
+    sid = engine.create_scene(engine.upload_robot(rb), sc)
+    rv64, rd64, _ = O.check_configs(rb, sc, q, prec="ref64")
+    for layout in ("lane", "warp"):
+        engine.set_layout(layout)
+        for prec in ("fp64", "fp32_recheck"):
+            v = torch.zeros(q.shape[0], dtype=torch.uint8, device="cuda")
+            d = torch.zeros(q.shape[0], dtype=torch.float64, device="cuda")
+            engine.check_configs(sid, torch.from_numpy(q).cuda(), prec, v, d, None)
+            engine.sync()
+            assert np.array_equal(v.cpu().numpy(), rv64), (layout, prec)
+            err = np.abs(d.cpu().numpy() - rd64).max()
+            assert err <= (1e-9 if prec == "fp64" else 1e-5), (layout, prec, err)
+    engine.set_layout("auto")
+    engine.destroy_scene(sid)
+    big = scenes.Scene(np.concatenate([sc.aabb, sc.aabb[:1]]))
+    with pytest.raises(RpmError):
+        engine.create_scene(engine.upload_robot(rb), big)
