@@ -381,7 +381,8 @@ typedef struct rpm_server_config {
     int32_t precision;           /* RPM_PREC_* of every request */
     int64_t memory_budget;       /* device bytes for request buffers (admission), default 8 GiB */
     int32_t max_batch_segments;  /* configuration requests and edge requests per batch, each <= 32 */
-    int32_t max_batch_configs;   /* work per batch: configurations + 8 x edges (1/8 on high-priority slots) */
+    int32_t max_batch_configs;   /* work per batch: configurations + 8 x edges (1/8 on high-priority slots);
+                                    default 32,768 (a larger request runs as a batch of its own) */
 } rpm_server_config;
 
 enum rpm_request_kind { RPM_REQ_CONFIGS = 0, RPM_REQ_EDGES = 1 };

@@ -168,6 +168,11 @@ struct Slot {
 };
 
 constexpr int64_t kSmallRequest = 8192;   // configurations (edges count x 8)
+// Work per batch: a batch completes as a whole, so its size bounds the latency
+// of every request in it.  32,768 units held p99 of requests up to 4,096
+// configurations to 3.4 ms at 12,000 req/s of the serving trace (262,144: 9.7 ms)
+// for 5 % less throughput at 20,000 req/s.
+constexpr int32_t kDefaultBatchWork = 1 << 15;
 constexpr double kAgeBoost = 0.050;       // a request waiting this long (s) is served as if small
 
 int64_t work_of(const Req *q) { return q->r.kind == RPM_REQ_EDGES ? 8 * q->r.count : q->r.count; }
@@ -414,12 +419,12 @@ extern "C" {
 
 int rpm_server_create(rpm_ctx *ctx, const rpm_server_config *cfg, rpm_server **out) {
     if (!ctx || !out) return fail(RPM_ERR_INVALID, "NULL argument");
-    rpm_server_config c{4, RPM_PREC_FP32_RECHECK, (int64_t)8 << 30, kMaxSegs, 1 << 18};
+    rpm_server_config c{4, RPM_PREC_FP32_RECHECK, (int64_t)8 << 30, kMaxSegs, kDefaultBatchWork};
     if (cfg) c = *cfg;
     if (c.num_slots < 1 || c.num_slots > 64) return fail(RPM_ERR_INVALID, "num_slots must be 1..64");
     if (c.precision < RPM_PREC_FP64 || c.precision > RPM_PREC_FP32_REF) return fail(RPM_ERR_INVALID, "unknown precision");
     if (c.max_batch_segments < 1 || c.max_batch_segments > kMaxSegs) c.max_batch_segments = kMaxSegs;
-    if (c.max_batch_configs < 1) c.max_batch_configs = 1 << 18;
+    if (c.max_batch_configs < 1) c.max_batch_configs = kDefaultBatchWork;
     if (c.memory_budget < (1 << 20)) return fail(RPM_ERR_INVALID, "memory budget below 1 MiB");
     rpm_server *srv = new rpm_server();
     srv->ctx = ctx;
@@ -442,8 +447,10 @@ int rpm_server_create(rpm_ctx *ctx, const rpm_server_config *cfg, rpm_server **o
             CK(cudaStreamCreateWithPriority(&sl.st, cudaStreamNonBlocking, sl.small ? hi_prio : lo_prio));
             CK(cudaEventCreateWithFlags(&sl.done, cudaEventDisableTiming));
             Scratch *sc = nullptr;   // pre-size scratch so the loop never allocates
-            int rc = get_scratch(ctx, sl.st, c.max_batch_configs, &sc);
-            if (!rc) rc = edge_scratch(ctx, sc, c.max_batch_configs / 4, sl.st);
+            // sized for requests up to 262,144 configurations, which run as batches of their own
+            const int64_t presize = std::max<int64_t>(c.max_batch_configs, 1 << 18);
+            int rc = get_scratch(ctx, sl.st, presize, &sc);
+            if (!rc) rc = edge_scratch(ctx, sc, presize / 4, sl.st);
             if (rc) return rc;
         }
     }

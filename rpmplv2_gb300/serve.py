@@ -69,7 +69,7 @@ def pinned(shape, dtype):
 
 class Server:
     def __init__(self, engine, num_slots=4, precision="fp32_recheck", memory_budget=8 << 30, max_batch_segments=32,
-                 max_batch_configs=1 << 18):
+                 max_batch_configs=1 << 15):
         from ._abi import PRECISIONS
         self.engine = engine
         self.lib = load()
