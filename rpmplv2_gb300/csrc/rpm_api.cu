@@ -631,6 +631,15 @@ int enqueue_check(rpm_ctx *ctx, SceneRec *s, int prec, const float *q, int64_t C
 
 using namespace rpm::impl;
 
+// Stream-ordered scratch of one call, freed on the stream however the call returns.
+struct AsyncScratch {
+    void *p = nullptr;
+    cudaStream_t st = nullptr;
+    ~AsyncScratch() {
+        if (p) cudaFreeAsync(p, st);
+    }
+};
+
 // Device address of a page-locked host buffer (cudaHostAlloc / cudaHostRegister,
 // mapped), or null for any other pointer.
 template <typename P> static P *mapped_ptr(P *host) {
@@ -1081,9 +1090,11 @@ int rpm_reached_states(rpm_ctx *ctx, int32_t scene_id, int32_t precision, const 
     const int L = ctx->robots[s->robot].desc.num_dofs;
     // computeDistance of the current state with nearest points (stream-ordered scratch)
     const size_t near_floats = (size_t)std::max(1, np.n) * 6 * L;
-    char *tmp = nullptr;
     const size_t bytes = 16 + 4 * (size_t)L + 4 * near_floats + 16;
-    CK(cudaMallocAsync((void **)&tmp, bytes, st));
+    AsyncScratch scratch;
+    scratch.st = st;
+    CK(cudaMallocAsync(&scratch.p, bytes, st));
+    char *tmp = static_cast<char *>(scratch.p);
     np.dist = reinterpret_cast<double *>(tmp);
     np.flag = reinterpret_cast<uint8_t *>(tmp + 8);
     np.profile = reinterpret_cast<float *>(tmp + 16);
@@ -1107,7 +1118,6 @@ int rpm_reached_states(rpm_ctx *ctx, int32_t scene_id, int32_t precision, const 
     p.n = np.n;
     p.maxd = np.nmf.maxd;
     CK(launch_reached_states(p, st));
-    CK(cudaFreeAsync(tmp, st));
     rc = near_done(ctx, buf, st);
     if (rc) return rc;
     // computeDistance(q_reached, true) in the requested form
@@ -1153,8 +1163,10 @@ int rpm_motion_validity(rpm_ctx *ctx, int32_t scene_id, int32_t precision, const
             rpm_box_aabb(boxes[b].dim, pos, boxes[b].quat_xyzw, haabb + ((size_t)k * num_boxes + b) * 6);
         }
     }
-    unsigned char *dev = nullptr;
-    CK(cudaMallocAsync((void **)&dev, host.size(), st));
+    AsyncScratch scratch;
+    scratch.st = st;
+    CK(cudaMallocAsync(&scratch.p, host.size(), st));
+    unsigned char *dev = static_cast<unsigned char *>(scratch.p);
     CK(cudaMemcpyAsync(dev, host.data(), host.size(), cudaMemcpyHostToDevice, st));
     MotionParams p;
     std::memset(&p, 0, sizeof p);
@@ -1177,7 +1189,6 @@ int rpm_motion_validity(rpm_ctx *ctx, int32_t scene_id, int32_t precision, const
     p.valid = valid_dev;
     p.checks = checks_dev;
     CK(launch_motion_validity(precision, p, st));
-    CK(cudaFreeAsync(dev, st));
     return near_done(ctx, buf, st);
 }
 

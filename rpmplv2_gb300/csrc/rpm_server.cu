@@ -389,6 +389,9 @@ void worker_loop(rpm_server *srv) {
                 q->t.batch_size = (int32_t)batch.size();
             }
             if (rc) {
+                // work already queued for the batch may still use its memory: let it finish first
+                cudaStreamSynchronize(sl.st);
+                cudaGetLastError();
                 const double te = now_s();
                 for (Req *q : batch) { q->t.status = rc; q->t.t_done = te; srv->arena.release(q->off, q->bytes); }
                 sl.busy = false;
