@@ -21,6 +21,7 @@ import os
 import statistics
 import subprocess
 import sys
+import tempfile
 import time
 
 import numpy as np
@@ -68,7 +69,8 @@ class ClockSampler:
     def __init__(self, index):
         self.index = index
         self.proc = None
-        self.path = os.path.join(ROOT, "gpurun_out", "clocks_bench.csv")
+        # the raw samples (the JSON line carries their summary)
+        self.path = os.environ.get("RPM_CLOCKS_CSV", os.path.join(tempfile.gettempdir(), "rpm_clocks_bench.csv"))
 
     def __enter__(self):
         try:

@@ -158,8 +158,9 @@ int rpm_check_configs(rpm_ctx *ctx, int32_t scene_id, int32_t precision, const f
                       uint8_t *valid_dev, double *dist_dev, float *profile_dev, void *stream);
 
 /* Several scenes (and robots of different DOF) in one launch: item k checks
- * num_configs configurations of its own scene (BASELINE-style mixed-DOF
- * batches, serving batches).  Same outputs as rpm_check_configs per item. */
+ * num_configs configurations of its own scene (mixed-DOF batches of
+ * spatial 14/18/22-DOF robots, serving batches).  Same outputs as
+ * rpm_check_configs per item. */
 typedef struct rpm_batch_item {
     int32_t scene_id;
     int32_t reserved;

@@ -7,7 +7,7 @@ import pytest
 
 from rpmplv2_gb300 import robots, scenes
 
-REF = os.environ.get("RPM_REFERENCE_ROOT", "/root/reference")
+from oracle.build import REF_ROOT as REF   # the reference tree the oracle recipe reads (absent on GPU hosts)
 
 
 def urdf_joints(name):
