@@ -439,6 +439,13 @@ int rpm_last_stats(rpm_ctx *ctx, void *stream, rpm_check_stats *out);
 int rpm_ctx_set_timing(rpm_ctx *ctx, int enable);
 int rpm_last_timing(rpm_ctx *ctx, void *stream, float *bulk_ms, float *recheck_ms);
 
+/* Failure detection without a fault: launches one CTA whose shared-memory
+ * staging wait can never complete (no copy is issued), bounded at 'polls'
+ * polls (1 .. 2^22).  The kernel records the timeout in a status word and
+ * returns, as every staging wait of the library does; the call then returns
+ * RPM_ERR_TIMEOUT, and the context stays usable. */
+int rpm_probe_bounded_wait(rpm_ctx *ctx, uint32_t polls);
+
 /* FP32 FMA throughput of the device (TFLOP/s), measured with independent FMA
  * chains: the denominator of the FP32 roofline. */
 int rpm_probe_fp32_peak(rpm_ctx *ctx, double *tflops);

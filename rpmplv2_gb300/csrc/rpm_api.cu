@@ -1413,6 +1413,23 @@ int rpm_last_timing(rpm_ctx *ctx, void *stream, float *bulk_ms, float *recheck_m
     return RPM_OK;
 }
 
+int rpm_probe_bounded_wait(rpm_ctx *ctx, uint32_t polls) {
+    if (!ctx) return fail(RPM_ERR_INVALID, "NULL context");
+    if (polls < 1 || polls > kWaitLimit) return fail(RPM_ERR_INVALID, "polls must be 1 .. %u", kWaitLimit);
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    if (set_device(ctx)) return RPM_ERR_CUDA;
+    int32_t *status = nullptr;
+    CK(cudaMalloc(&status, sizeof(int32_t)));
+    int32_t v = 0;
+    cudaError_t e = cudaMemset(status, 0, sizeof(int32_t));
+    if (e == cudaSuccess) e = launch_wait_probe(status, polls, 0);
+    if (e == cudaSuccess) e = cudaMemcpy(&v, status, sizeof v, cudaMemcpyDeviceToHost);
+    cudaFree(status);
+    CK(e);
+    if (v == kStatusTimeout) return fail(RPM_ERR_TIMEOUT, "a bounded device-side wait gave up after %u polls", polls);
+    return fail(RPM_ERR_CUDA, "the wait probe did not report its timeout (status %d)", v);
+}
+
 int rpm_probe_fp32_peak(rpm_ctx *ctx, double *tflops) {
     if (!ctx || !tflops) return fail(RPM_ERR_INVALID, "NULL argument");
     std::lock_guard<std::mutex> lk(ctx->mu);

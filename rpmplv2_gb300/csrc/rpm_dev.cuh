@@ -393,9 +393,10 @@ __device__ __forceinline__ void bulk_copy(uint64_t *bar, void *dst, const void *
                  : "memory");
 }
 
-__device__ __forceinline__ bool bulk_wait(uint64_t *bar, uint32_t parity, int32_t *status) {
+__device__ __forceinline__ bool bulk_wait(uint64_t *bar, uint32_t parity, int32_t *status,
+                                          unsigned limit = kWaitLimit) {
     uint32_t done = 0;
-    for (unsigned it = 0; it < kWaitLimit; ++it) {
+    for (unsigned it = 0; it < limit; ++it) {
         asm volatile(
             "{\n\t.reg .pred p;\n\t"
             "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"

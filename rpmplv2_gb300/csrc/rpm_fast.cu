@@ -120,6 +120,22 @@ cudaError_t launch_edges_fp32(const EdgeParams &p, int grid, size_t smem, cudaSt
     return cudaGetLastError();
 }
 
+// Failure-detection probe: the staging wait of a CTA whose copy is never
+// issued.  Thread 0 announces 16 bytes that no copy delivers, so the bounded
+// wait runs out after 'limit' polls, records the timeout in *status and the
+// kernel returns; nothing is left in flight.
+__global__ void k_wait_probe(int32_t *status, unsigned limit) {
+    __shared__ uint64_t bar;
+    bulk_init(&bar);
+    if (threadIdx.x == 0) bulk_expect(&bar, 16);
+    bulk_wait(&bar, 0, status, limit);
+}
+
+cudaError_t launch_wait_probe(int32_t *status, unsigned limit, cudaStream_t st) {
+    k_wait_probe<<<1, 32, 0, st>>>(status, limit);
+    return cudaGetLastError();
+}
+
 // Peak FP32 issue rate of this GPU: independent FMA chains, no memory traffic.
 __global__ void k_ffma_probe(float *out, int iters) {
     float a[kProbeChains];

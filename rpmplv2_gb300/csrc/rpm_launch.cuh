@@ -55,4 +55,6 @@ constexpr int kProbeChains = 8;
 cudaError_t launch_ffma_probe(float *out, int blocks, int threads, int iters, cudaStream_t st);
 cudaError_t launch_skeleton(int mode, const DevRobot *rb, int D, const float *q, int64_t C, double *out, cudaStream_t st);
 
+cudaError_t launch_wait_probe(int32_t *status, unsigned limit, cudaStream_t st);
+
 }  // namespace rpm
