@@ -390,16 +390,23 @@ int enqueue_segments(rpm_ctx *ctx, int prec, const std::vector<SegReq> &reqs_in,
     if (sc->timed && !sc->ev[0])
         for (int i = 0; i < 3; ++i) CK(cudaEventCreate(&sc->ev[i]));
     if (sc->timed) CK(cudaEventRecord(sc->ev[0], st));
-    // chunks of at most kMaxSegs segments of one layout
+    // chunks of at most kMaxSegs segments of one layout and, in the lane layout,
+    // of one output kind (isValid only, distance / profile only, both), so a
+    // launch runs the kernel body compiled for its outputs
+    auto kind_of = [](const SegReq &r) { return (r.dist || r.profile) ? (r.valid ? 0 : 2) : 1; };
     std::vector<std::pair<bool, std::vector<const SegReq *>>> chunks;
     for (int wide = 0; wide < 2; ++wide) {
-        std::vector<const SegReq *> cur;
-        for (const SegReq &r : reqs) {
-            if (r.count <= 0 || use_warp_layout(ctx, r, total, prec) != (wide == 1)) continue;
-            cur.push_back(&r);
-            if ((int)cur.size() == kMaxSegs) { chunks.push_back({wide == 1, cur}); cur.clear(); }
+        for (int kind = 0; kind < 3; ++kind) {
+            if (wide && kind > 0) break;   // the warp layout takes every kind in one launch
+            std::vector<const SegReq *> cur;
+            for (const SegReq &r : reqs) {
+                if (r.count <= 0 || use_warp_layout(ctx, r, total, prec) != (wide == 1)) continue;
+                if (!wide && kind_of(r) != kind) continue;
+                cur.push_back(&r);
+                if ((int)cur.size() == kMaxSegs) { chunks.push_back({wide == 1, cur}); cur.clear(); }
+            }
+            if (!cur.empty()) chunks.push_back({wide == 1, cur});
         }
-        if (!cur.empty()) chunks.push_back({wide == 1, cur});
     }
     const size_t tsz = prec == RPM_PREC_FP64 ? sizeof(double) : sizeof(float);
     std::vector<SceneBuf *> used;

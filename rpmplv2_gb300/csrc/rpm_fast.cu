@@ -10,6 +10,9 @@
 
 namespace rpm {
 
+// KIND: 1 = every segment of the launch is isValid only, 2 = distance /
+// profile only, 0 = mixed (the body compiled for the launch's outputs).
+template <int KIND>
 __global__ void __launch_bounds__(kThreads, 5) k_check_fp32(const __grid_constant__ KParams P) {
     extern __shared__ __align__(128) unsigned char smem[];
     __shared__ uint64_t bar;
@@ -36,10 +39,11 @@ __global__ void __launch_bounds__(kThreads, 5) k_check_fp32(const __grid_constan
     const Want w{sg.valid != nullptr, sg.dist != nullptr, sg.profile != nullptr};
     const int D = rb.D;
     int hl = -1, hj = 0x7fffffff, slot = -1;
-    const int st = warp_check<2, float>(wsh[threadIdx.x >> 5], rb, ob, sg.q + c * D, active, P.nmf, w,
-                                        (w.valid && active) ? sg.valid + c : nullptr,
-                                        (w.dist && active) ? sg.dist + c : nullptr,
-                                        (w.profile && active) ? sg.profile + c * D : nullptr, &P.ps, &slot, &hl, &hj);
+    uint8_t *vo = (w.valid && active) ? sg.valid + c : nullptr;
+    double *dout = (w.dist && active) ? sg.dist + c : nullptr;
+    float *po = (w.profile && active) ? sg.profile + c * D : nullptr;
+    const int st = warp_check<2, float, KIND>(wsh[threadIdx.x >> 5], rb, ob, sg.q + c * D, active, P.nmf, w, vo, dout,
+                                              po, &P.ps, &slot, &hl, &hj);
     if (active) {
         complete_record(&P.ps, slot, st, s, c, hl, hj);
         if (st == kFull) recheck_whole(P, s, c);
@@ -157,11 +161,22 @@ cudaError_t launch_ffma_probe(float *out, int blocks, int threads, int iters, cu
     return cudaGetLastError();
 }
 
-cudaError_t launch_check_fp32(const KParams &p, int64_t blocks, size_t smem, cudaStream_t st) {
+template <int KIND> static cudaError_t launch_fp32_kind(const KParams &p, int64_t blocks, size_t smem, cudaStream_t st) {
     static bool attr = false;
-    if (!attr) { cudaFuncSetAttribute(k_check_fp32, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024); attr = true; }
-    k_check_fp32<<<(unsigned)blocks, kThreads, smem, st>>>(p);
+    if (!attr) { cudaFuncSetAttribute(k_check_fp32<KIND>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024); attr = true; }
+    k_check_fp32<KIND><<<(unsigned)blocks, kThreads, smem, st>>>(p);
     return cudaGetLastError();
+}
+
+cudaError_t launch_check_fp32(const KParams &p, int64_t blocks, size_t smem, cudaStream_t st) {
+    bool any_b = false, any_d = false;
+    for (int k = 0; k < p.nseg; ++k) {
+        any_b = any_b || p.segs[k].valid;
+        any_d = any_d || p.segs[k].dist || p.segs[k].profile;
+    }
+    if (!any_d) return launch_fp32_kind<1>(p, blocks, smem, st);
+    if (!any_b) return launch_fp32_kind<2>(p, blocks, smem, st);
+    return launch_fp32_kind<0>(p, blocks, smem, st);
 }
 
 }  // namespace rpm
