@@ -391,12 +391,16 @@ int enqueue_segments(rpm_ctx *ctx, int prec, const std::vector<SegReq> &reqs_in,
         for (int i = 0; i < 3; ++i) CK(cudaEventCreate(&sc->ev[i]));
     if (sc->timed) CK(cudaEventRecord(sc->ev[0], st));
     // chunks of at most kMaxSegs segments of one layout and, in the lane layout,
-    // of one output kind (isValid only, distance / profile only, both), so a
-    // launch runs the kernel body compiled for its outputs
-    auto kind_of = [](const SegReq &r) { return (r.dist || r.profile) ? (r.valid ? 0 : 2) : 1; };
+    // of one output kind (isValid only, distance only, distance with profile,
+    // several), so a launch runs the kernel body compiled for its outputs
+    auto kind_of = [](const SegReq &r) {
+        if (!r.dist && !r.profile) return 1;
+        if (r.valid) return 0;
+        return r.profile ? 2 : 3;
+    };
     std::vector<std::pair<bool, std::vector<const SegReq *>>> chunks;
     for (int wide = 0; wide < 2; ++wide) {
-        for (int kind = 0; kind < 3; ++kind) {
+        for (int kind = 0; kind < 4; ++kind) {
             if (wide && kind > 0) break;   // the warp layout takes every kind in one launch
             std::vector<const SegReq *> cur;
             for (const SegReq &r : reqs) {

@@ -404,13 +404,15 @@ template <typename T> __device__ __forceinline__ T gap2_bb(const T *lo, const T 
 // lane has a settled hit it only looks for an earlier hit (lower obstacle
 // index), which is all the profile's first-hit semantics need.
 // KIND fixes the outputs at compile time so the unused tree and its queue
-// compile away: 0 = as 'w' says, 1 = isValid only, 2 = distance / profile only.
+// compile away: 0 = as 'w' says, 1 = isValid only, 2 = distance / profile
+// only, 3 = distance only (no profile).
 template <int MODE, typename T, int KIND = 0>
 __device__ int warp_check(WarpShared<T> &sh, const DevRobot &rb, const ObsView<T> &ob, const float *q, bool active,
                           const Num<T> &nm, Want w_in, uint8_t *valid_out, double *dist_out, float *prof_out,
                           const PairSink *ps = nullptr, int *slot = nullptr, int *hit_link = nullptr,
                           int *hit_j = nullptr) {
-    const Want w{KIND == 2 ? false : w_in.valid, KIND == 1 ? false : w_in.dist, KIND == 1 ? false : w_in.profile};
+    const Want w{(KIND == 2 || KIND == 3) ? false : w_in.valid, KIND == 1 ? false : w_in.dist,
+                 (KIND == 1 || KIND == 3) ? false : w_in.profile};
     const unsigned full = 0xffffffffu;
     const int lane = threadIdx.x & 31;
     const unsigned lt_mask = (1u << lane) - 1u;

@@ -11,7 +11,8 @@
 namespace rpm {
 
 // KIND: 1 = every segment of the launch is isValid only, 2 = distance /
-// profile only, 0 = mixed (the body compiled for the launch's outputs).
+// profile only, 3 = distance only, 0 = mixed (the body compiled for the
+// launch's outputs).
 template <int KIND>
 __global__ void __launch_bounds__(kThreads, 5) k_check_fp32(const __grid_constant__ KParams P) {
     extern __shared__ __align__(128) unsigned char smem[];
@@ -169,12 +170,14 @@ template <int KIND> static cudaError_t launch_fp32_kind(const KParams &p, int64_
 }
 
 cudaError_t launch_check_fp32(const KParams &p, int64_t blocks, size_t smem, cudaStream_t st) {
-    bool any_b = false, any_d = false;
+    bool any_b = false, any_d = false, any_p = false;
     for (int k = 0; k < p.nseg; ++k) {
         any_b = any_b || p.segs[k].valid;
-        any_d = any_d || p.segs[k].dist || p.segs[k].profile;
+        any_d = any_d || p.segs[k].dist;
+        any_p = any_p || p.segs[k].profile;
     }
-    if (!any_d) return launch_fp32_kind<1>(p, blocks, smem, st);
+    if (!any_d && !any_p) return launch_fp32_kind<1>(p, blocks, smem, st);
+    if (!any_b && !any_p) return launch_fp32_kind<3>(p, blocks, smem, st);
     if (!any_b) return launch_fp32_kind<2>(p, blocks, smem, st);
     return launch_fp32_kind<0>(p, blocks, smem, st);
 }
