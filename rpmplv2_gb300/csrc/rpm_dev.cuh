@@ -311,7 +311,7 @@ template <> struct SkelWalker<1> {
     RPM_HD void begin() { w.begin(); }
     RPM_HD void point(const DevRobot &rb, const float *q, int k, float *out) {
         if (rb.kind == RPM_ROBOT_XARM6 && k == 6) {
-            fk_step_d(w.f, rb, 5, (double)q[5]);
+            fk_step_d(w.f, rb, 5, (double)q[5], w.sc);
             const double g = rb.gripper_d;
 #pragma unroll
             for (int i = 0; i < 3; ++i) {

@@ -812,8 +812,10 @@ __global__ void __launch_bounds__(kThreads) k_extend_spines(const __grid_constan
     if (c >= P.C) return;
     const DevRobot &rb = *P.robot;
     const int D = rb.D;
-    P.status[c] = extend_spine(rb, P.q + c * D, P.dist[c], P.profile + c * D, P.qe + c * D, P.num_iter, P.expanded != 0,
-                               P.q_new + c * D);
+    float sk[3 * (kMaxDof + 1)], sk_end[3 * (kMaxDof + 1)];
+    skel_ref(rb, P.q + c * D, sk);
+    P.status[c] = extend_spine(rb, P.q + c * D, sk, P.dist[c], P.profile + c * D, P.qe + c * D, P.num_iter,
+                               P.expanded != 0, P.q_new + c * D, sk_end);
 }
 
 // computeReachedState: one warp per horizon state.  Every lane runs the spine
@@ -823,12 +825,16 @@ __global__ void __launch_bounds__(kThreads) k_extend_spines(const __grid_constan
 __global__ void __launch_bounds__(kThreads) k_reached_states(const __grid_constant__ SpineParams P) {
     const unsigned full = 0xffffffffu;
     const int lane = threadIdx.x & 31;
+    __shared__ double scw[kThreads / 32][2 * kMaxDof];
     const int64_t h = (int64_t)blockIdx.x * (blockDim.x / 32) + (threadIdx.x >> 5);
     if (h >= P.C) return;
+    double *sc = scw[threadIdx.x >> 5];
     const DevRobot &rb = *P.robot;
     const int D = rb.D, L = D;
     const float *qe = P.qe + h * D;
-    float qn[kMaxDof], pn[kMaxDof], qs[kMaxDof], sk[3 * (kMaxDof + 1)], p[kMaxDof];
+    float qn[kMaxDof], pn[kMaxDof], qs[kMaxDof], p[kMaxDof];
+    float skn[3 * (kMaxDof + 1)], sk[3 * (kMaxDof + 1)];   // skeletons of the layer's start and end
+    const int NP = 3 * (D + 1);
     for (int k = 0; k < D; ++k) qn[k] = P.q_cur[k];
     const float d_cur = (float)P.cur_dist[0];
     int status = kStTrapped;
@@ -836,10 +842,11 @@ __global__ void __launch_bounds__(kThreads) k_reached_states(const __grid_consta
         for (int i = 0; i < L; ++i) pn[i] = P.cur_prof[i];
         float dn = d_cur;
         status = kStNone;
+        skel_ref_warp(rb, qn, skn, sc);
         for (int layer = 0; layer < P.num_layers; ++layer) {
-            status = extend_spine(rb, qn, dn, pn, qe, P.num_iter, P.expanded != 0, qs);
+            status = extend_spine(rb, qn, skn, dn, pn, qe, P.num_iter, P.expanded != 0, qs, sk, sc);
             for (int k = 0; k < D; ++k) qn[k] = qs[k];
-            skel_ref(rb, qn, sk);
+            for (int k = 0; k < NP; ++k) skn[k] = sk[k];
             float d_c = P.maxd;
             bool negative = false;
             for (int i = 0; i < L && !negative; ++i) {

@@ -64,6 +64,21 @@ __device__ __forceinline__ void skel_ref(const DevRobot &rb, const float *q, flo
     for (int k = 0; k <= rb.D; ++k) sw.point(rb, q, k, sk + 3 * k);
 }
 
+// The same skeleton with the whole warp (every lane passes the same q): lane
+// k computes joint k's sine and cosine -- the values the chain would compute
+// itself -- and every lane then runs the chain.  sc: 2 * kMaxDof doubles of
+// the warp's shared memory.
+__device__ __forceinline__ void skel_ref_warp(const DevRobot &rb, const float *q, float *sk, double *sc) {
+    const int lane = threadIdx.x & 31;
+    __syncwarp();
+    if (lane < rb.D) taylor_sincos((double)q[lane], &sc[2 * lane], &sc[2 * lane + 1]);
+    __syncwarp();
+    SkelWalker<1> sw;
+    sw.begin();
+    sw.w.sc = sc;
+    for (int k = 0; k <= rb.D; ++k) sw.point(rb, q, k, sk + 3 * k);
+}
+
 // Row i (D + 1 entries) of computeEnclosingRadii from the float skeleton.
 static __device__ void enclosing_row(const DevRobot &rb, const float *sk, int i, float *row) {
     const int D = rb.D;
@@ -100,22 +115,28 @@ static __device__ void enclosing_row(const DevRobot &rb, const float *sk, int i,
     }
 }
 
-// extendSpine from q (distance d, profile prof) towards qe; q_new gets the end.
-static __device__ int extend_spine(const DevRobot &rb, const float *q, float d, const float *prof, const float *qe, int num_iter,
-                            bool expanded, float *q_new) {
-    const int D = rb.D, L = D;
+// extendSpine from q (its skeleton sk_q, distance d, profile prof) towards
+// qe; q_new gets the end and sk_new its skeleton.  Each iteration computes
+// one forward kinematics, of its new state: the skeleton of the state an
+// iteration starts from is the previous iteration's (or sk_q).
+// sc: the warp's shared sincos scratch when the whole warp runs this spine
+// (every lane the same arguments), null for one spine per lane.
+static __device__ int extend_spine(const DevRobot &rb, const float *q, const float *sk_q, float d, const float *prof,
+                                   const float *qe, int num_iter, bool expanded, float *q_new, float *sk_new,
+                                   double *sc = nullptr) {
+    const int D = rb.D, L = D, NP = 3 * (D + 1);
     if (d <= 0.f) {
         for (int k = 0; k < D; ++k) q_new[k] = q[k];
+        for (int k = 0; k < NP; ++k) sk_new[k] = sk_q[k];
         return kStTrapped;
     }
-    float sk0[3 * (kMaxDof + 1)], skt[3 * (kMaxDof + 1)];
+    float skt[3 * (kMaxDof + 1)];
     float qt[kMaxDof], dq[kMaxDof], rho_profile[kMaxDof], col[kMaxDof + 1], row[kMaxDof + 1];
     float rho = 0.f;
-    skel_ref(rb, q, sk0);
+    for (int k = 0; k < NP; ++k) skt[k] = sk_q[k];
     for (int k = 0; k < D; ++k) { qt[k] = q[k]; rho_profile[k] = 0.f; }
     int status = kStAdvanced, counter = 0;
     for (;;) {
-        skel_ref(rb, qt, skt);
         for (int k = 0; k < D; ++k) dq[k] = fabsf(qe[k] - qt[k]);
         // R->col(j).dot(delta_q) for every column j, rows in index order
         for (int j = 0; j <= D; ++j) col[j] = 0.f;
@@ -136,16 +157,18 @@ static __device__ int extend_spine(const DevRobot &rb, const float *q, float d, 
         } else {
             for (int k = 0; k < D; ++k) q_new[k] = qt[k] + step * (qe[k] - qt[k]);
         }
+        if (sc) skel_ref_warp(rb, q_new, sk_new, sc);
+        else skel_ref(rb, q_new, sk_new);
         if (++counter == num_iter || status != kStAdvanced) return status;
-        skel_ref(rb, q_new, skt);
         float rk_prev = 0.f;
         for (int k = 1; k <= L; ++k) {
-            const float rk = col_dist(sk0 + 3 * k, skt + 3 * k);
+            const float rk = col_dist(sk_q + 3 * k, sk_new + 3 * k);
             rho_profile[k - 1] = max_std(rk_prev, rk);
             rk_prev = rk;
             rho = max_std(rho, rk);
         }
         for (int k = 0; k < D; ++k) qt[k] = q_new[k];
+        for (int k = 0; k < NP; ++k) skt[k] = sk_new[k];
     }
 }
 #endif
