@@ -20,6 +20,8 @@ template <typename T> struct ObsView {
     const float *ground;  // [n_pad] 1.0 for "ground"
     int n, n_pad;
     const float *frows = nullptr;   // FP64 form: the same rows in float (exact), for the float pre-test
+    const float4 *aos = nullptr;    // FP32 pass: the float rows per obstacle as [n][8] (six coordinates,
+                                    // min_dist_tol, ground), two 16-byte loads per obstacle
     RPM_HD void box(int j, T *o) const {
 #pragma unroll
         for (int k = 0; k < 6; ++k) o[k] = rows[k * n_pad + j];
@@ -381,19 +383,24 @@ template <typename T> __device__ __forceinline__ T gap2_bb(const T *lo, const T 
 }
 
 // Append this lane's item to a warp queue (positions by ballot rank) and
-// drain the queue 32 entries at a time.
-#define RPM_PUSH_AND_DRAIN(Q, N, want, item, DRAIN)                                    \
+// drain the queue 32 entries at a time.  The ballot gates the rest: for most
+// obstacles no lane of the warp queues a pair.  REFRESH reloads the lane's
+// register copies of what the drain changes.
+#define RPM_PUSH_AND_DRAIN(Q, N, want, item, DRAIN, REFRESH)                           \
     do {                                                                               \
         const unsigned m_ = __ballot_sync(0xffffffffu, (want));                         \
-        if (want) sh.Q[(N) + __popc(m_ & lt_mask)] = (item);                           \
-        (N) += __popc(m_);                                                             \
-        __syncwarp();                                                                  \
-        if ((N) >= 32) {                                                               \
-            DRAIN<MODE, T>(sh, rb, ob, nm, i, 32, ps);                                 \
-            __syncwarp();                                                              \
-            if (lane < (N) - 32) sh.Q[lane] = sh.Q[32 + lane];                         \
-            (N) -= 32;                                                                 \
-            __syncwarp();                                                              \
+        if (m_ != 0u) {                                                                \
+            if (want) sh.Q[(N) + __popc(m_ & lt_mask)] = (item);                       \
+            (N) += __popc(m_);                                                         \
+            if ((N) >= 32) {                                                           \
+                __syncwarp();                                                          \
+                DRAIN<MODE, T>(sh, rb, ob, nm, i, 32, ps);                             \
+                __syncwarp();                                                          \
+                if (lane < (N) - 32) sh.Q[lane] = sh.Q[32 + lane];                     \
+                (N) -= 32;                                                             \
+                REFRESH;                                                               \
+                __syncwarp();                                                          \
+            }                                                                          \
         }                                                                              \
     } while (0)
 
@@ -436,6 +443,7 @@ __device__ int warp_check(WarpShared<T> &sh, const DevRobot &rb, const ObsView<T
         const T tb = r * T(1.41421356237309515) + BoolMargin<MODE, T>::m();
         const T tb2 = tb * tb;
         const T hunt = r + nm.eq + dmargin;          // a gap above this cannot be a hit
+        const T hunt2 = hunt * hunt;
         const bool ground_skip = i < rb.ground_included;
         const bool dist_link = need_d;
         T lo[3], hi[3];
@@ -469,13 +477,31 @@ __device__ int warp_check(WarpShared<T> &sh, const DevRobot &rb, const ObsView<T
             }
         }
         __syncwarp();
+        // Register copies of the lane's per-link state that only the drains
+        // change: a settled collision (flags bit 0), the first settled hit
+        // (hitj) and the link minimum (lmin).
+        bool hitb = false;
+        int hj = 0x7fffffff;
+        T cur = nm.maxd;
         int nb = 0, nd = 0;
         for (int j = 0; j < ob.n; ++j) {
-            const bool wb = need_b && !(sh.flags[lane] & 1);
-            const int hj = sh.hitj[lane];
+            const bool wb = need_b && !hitb;
             const bool wd = need_d && (hj == 0x7fffffff || (w.profile && j < hj));
             bool qb = false, qd = false;
-            bool near = (wb || wd) && !(ground_skip && ob.is_ground(j));
+            bool near = wb || wd;
+            T o[6];
+            T tj = T(0);
+            bool have = false;   // o and tj loaded from the per-obstacle copy
+            if constexpr (MODE == 2) {
+                if (ob.aos != nullptr) {
+                    const float4 a = ob.aos[2 * j], b = ob.aos[2 * j + 1];
+                    o[0] = a.x; o[1] = a.y; o[2] = a.z; o[3] = a.w; o[4] = b.x; o[5] = b.y;
+                    tj = b.z;
+                    near = near && !(ground_skip && b.w != 0.f);
+                    have = true;
+                }
+            }
+            if (!have) near = near && !(ground_skip && ob.is_ground(j));
             if constexpr (MODE == 0) {
                 if (near && pre) {
                     float of[6];
@@ -496,26 +522,27 @@ __device__ int warp_check(WarpShared<T> &sh, const DevRobot &rb, const ObsView<T
                 }
             }
             if (near) {
-                T o[6];
-                ob.box(j, o);
+                if (!have) ob.box(j, o);
                 const T g2 = gap2_bb(lo, hi, o);
                 qb = wb && !(g2 > tb2);
                 if (wd) {
                     if (hj != 0x7fffffff) {
-                        qd = !(g2 > hunt * hunt);
+                        qd = !(g2 > hunt2);
                     } else {
-                        const T cur = Key<T>::value(sh.lmin[lane]);
                         T thr = w.profile ? cur : smin(best, cur);
-                        thr = smin(thr, ob.tol(j));
+                        thr = smin(thr, have ? tj : ob.tol(j));
                         const T s = thr + r + nm.eq + dmargin;
                         qd = !(s > T(0) && g2 > s * s);
                     }
                 }
             }
             const uint32_t item = (uint32_t)lane | ((uint32_t)j << 5);
-            RPM_PUSH_AND_DRAIN(qb, nb, qb, item, drain_bool);
-            RPM_PUSH_AND_DRAIN(qd, nd, qd, item, drain_dist);
+            if constexpr (KIND != 2 && KIND != 3)
+                RPM_PUSH_AND_DRAIN(qb, nb, qb, item, drain_bool, hitb = (sh.flags[lane] & 1) != 0);
+            if constexpr (KIND != 1)
+                RPM_PUSH_AND_DRAIN(qd, nd, qd, item, drain_dist, (hj = sh.hitj[lane], cur = Key<T>::value(sh.lmin[lane])));
         }
+        __syncwarp();
         if (nb > 0) drain_bool<MODE, T>(sh, rb, ob, nm, i, nb, ps);
         if (nd > 0) drain_dist<MODE, T>(sh, rb, ob, nm, i, nd, ps);
         __syncwarp();

@@ -56,6 +56,9 @@ constexpr int kFRows = 8;               // float rows per scene
 constexpr int kDRows = 7;               // double rows per scene
 constexpr int kRowTol = 6;
 constexpr int kRowGround = 7;
+// Scenes of at most this many padded obstacles also get a per-obstacle copy of
+// their float rows ([n_pad][8] floats) in the FP32 lane kernel's shared memory.
+constexpr int kAosMaxPad = 512;
 // FP32 + FP64-recheck thresholds.  The FP32 skeleton differs from the FP64
 // one by at most ~2e-7 m on the reference's robots, so an FP32 branch decision
 // whose (error-amplification-scaled) margin is at least kDecide = 1e-5 m takes

@@ -3,6 +3,8 @@
 // kBand of a boundary are listed and re-evaluated in FP64 by the pair recheck
 // (rpm_exact.cu), or, when the lists are full, their configurations are
 // recomputed whole by k_recheck.
+#include <algorithm>
+
 #include "rpm_check.cuh"
 #include "rpm_edges.cuh"
 #include "rpm_launch.cuh"
@@ -32,11 +34,24 @@ __global__ void __launch_bounds__(kThreads, 5) k_check_fp32(const __grid_constan
     if (!bulk_wait(&bar, 0, P.status)) return;
     const DevRobot &rb = *reinterpret_cast<const DevRobot *>(smem);
     const float *rows = reinterpret_cast<const float *>(smem + sizeof(DevRobot));
+    // The obstacle loop reads each obstacle's rows as two 16-byte words.
+    float4 *aos = nullptr;
+    if (sg.n_pad <= kAosMaxPad) {
+        aos = reinterpret_cast<float4 *>(smem + sizeof(DevRobot) + (size_t)kFRows * sg.n_pad * sizeof(float));
+        for (int t = threadIdx.x; t < sg.n; t += kThreads) {
+            const int np = sg.n_pad;
+            aos[2 * t] = make_float4(rows[t], rows[np + t], rows[2 * np + t], rows[3 * np + t]);
+            aos[2 * t + 1] = make_float4(rows[4 * np + t], rows[5 * np + t], rows[kRowTol * np + t],
+                                         rows[kRowGround * np + t]);
+        }
+        __syncthreads();
+    }
     const int64_t c = (int64_t)(blockIdx.x - sg.first_block) * kThreads + threadIdx.x;
     const int64_t warp0 = c - (threadIdx.x & 31);
     if (warp0 >= sg.count) return;   // whole warp idle
     const bool active = c < sg.count;
     ObsView<float> ob{rows, rows + (size_t)kRowGround * sg.n_pad, sg.n, sg.n_pad};
+    ob.aos = aos;
     const Want w{sg.valid != nullptr, sg.dist != nullptr, sg.profile != nullptr};
     const int D = rb.D;
     int hl = -1, hj = 0x7fffffff, slot = -1;
@@ -171,11 +186,14 @@ template <int KIND> static cudaError_t launch_fp32_kind(const KParams &p, int64_
 
 cudaError_t launch_check_fp32(const KParams &p, int64_t blocks, size_t smem, cudaStream_t st) {
     bool any_b = false, any_d = false, any_p = false;
+    int aos_pad = 0;   // room for the per-obstacle copy of the largest scene that gets one
     for (int k = 0; k < p.nseg; ++k) {
         any_b = any_b || p.segs[k].valid;
         any_d = any_d || p.segs[k].dist;
         any_p = any_p || p.segs[k].profile;
+        if (p.segs[k].n_pad <= kAosMaxPad) aos_pad = std::max(aos_pad, p.segs[k].n_pad);
     }
+    smem += (size_t)aos_pad * kFRows * sizeof(float);
     if (!any_d && !any_p) return launch_fp32_kind<1>(p, blocks, smem, st);
     if (!any_b && !any_p) return launch_fp32_kind<3>(p, blocks, smem, st);
     if (!any_b) return launch_fp32_kind<2>(p, blocks, smem, st);
