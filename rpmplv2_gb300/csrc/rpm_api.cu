@@ -353,6 +353,11 @@ static bool use_warp_layout(const rpm_ctx *ctx, const SegReq &r, int64_t total, 
     if (ctx->layout == RPM_LAYOUT_WARP) return true;
     const int n = r.scene->n;
     if (n >= kWideMinObstacles) return !(r.profile != nullptr && total > kWideMaxProfileBatch);
+    if (prec == RPM_PREC_FP32_RECHECK && r.profile == nullptr && n >= 20) {
+        if (n >= 80) return total <= kWide32Batch80;
+        if (n >= 40) return total <= kWide32Batch40;
+        return total <= kWide32Batch20;
+    }
     if (n >= kWideMidObstacles) return total <= kWideMidBatch;
     const int64_t small = (prec == RPM_PREC_FP64) ? kWideSmallBatch : kWideSmallBatch32;
     return n >= kWideSmallObstacles && r.profile == nullptr && total <= small;

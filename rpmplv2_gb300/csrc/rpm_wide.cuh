@@ -43,9 +43,10 @@ constexpr uint32_t kPadIdx = 0x7fffffffu;           // idx row: padding slot (bo
 static_assert(kMaxLeaves * kLeaf >= kMaxObstacles + 3 * (kLeaf - 1), "sorted layout too small");
 // Automatic layout (rpm_api.cu): warp-per-configuration for scenes of at
 // least kWideMinObstacles obstacles (profiles: batches up to
-// kWideMaxProfileBatch), of kWideMidObstacles with batches up to
-// kWideMidBatch, and of kWideSmallObstacles with batches up to kWideSmallBatch
-// (FP64) or kWideSmallBatch32 (FP32 forms) without profiles.
+// kWideMaxProfileBatch), by the kWide32Batch* thresholds below in the
+// FP32+recheck form without profiles, otherwise for kWideMidObstacles with
+// batches up to kWideMidBatch, and for kWideSmallObstacles with batches up to
+// kWideSmallBatch (FP64) or kWideSmallBatch32 (FP32 forms) without profiles.
 constexpr int kWideMinObstacles = 150;
 constexpr int64_t kWideMaxProfileBatch = 16384;
 constexpr int kWideMidObstacles = 40;
@@ -53,6 +54,13 @@ constexpr int64_t kWideMidBatch = 8192;
 constexpr int kWideSmallObstacles = 8;
 constexpr int64_t kWideSmallBatch = 512;
 constexpr int64_t kWideSmallBatch32 = 4096;
+// FP32+recheck form without profiles: warp-per-configuration while the batch
+// holds at most this many configurations, for scenes of at least 80 / 40 / 20
+// obstacles (below 20, the small-scene rule above).  Measured crossovers of
+// the two layouts for xarm6 and spatial 10- and 22-DOF robots.
+constexpr int64_t kWide32Batch80 = 32768;
+constexpr int64_t kWide32Batch40 = 16384;
+constexpr int64_t kWide32Batch20 = 8192;
 // Edge batches (rpm_api.cu): warp-per-check for scenes of at least this many obstacles.
 constexpr int kWideEdgeObstacles = 100;
 
