@@ -212,8 +212,8 @@ __device__ void edge_warps(const EdgeParams &P, const DevRobot *rb_st, const Obs
             const Want w{true, false, false};
             uint8_t v = 1;
             int slot = -1;
-            const int st = warp_check<MODE, T>(sh, rb, ob, qbuf + lane * kMaxDof, mine, nm, w, &v, nullptr, nullptr,
-                                               MODE == 2 ? &P.ps : nullptr, &slot);
+            const int st = warp_check<MODE, T, 1>(sh, rb, ob, qbuf + lane * kMaxDof, mine, nm, w, &v, nullptr, nullptr,
+                                                  MODE == 2 ? &P.ps : nullptr, &slot);
             if (mine) edge_outcome<MODE>(P, e, k, st, slot, v);
             todo &= ~m;
             __syncwarp();

@@ -129,11 +129,23 @@ __global__ void __launch_bounds__(kThreads) k_edges_fp32(const __grid_constant__
     if (!bulk_wait(&bar, 0, P.status)) return;
     const DevRobot &rb = *reinterpret_cast<const DevRobot *>(smem);
     const float *rows = reinterpret_cast<const float *>(smem + sizeof(DevRobot));
-    const ObsView<float> ob{rows, rows + (size_t)kRowGround * sg.n_pad, sg.n, sg.n_pad};
+    ObsView<float> ob{rows, rows + (size_t)kRowGround * sg.n_pad, sg.n, sg.n_pad};
+    if (sg.n_pad <= kAosMaxPad) {   // the per-obstacle copy of the rows (room reserved by the launcher)
+        float4 *aos = reinterpret_cast<float4 *>(smem + sizeof(DevRobot) + (size_t)kFRows * sg.n_pad * sizeof(float));
+        for (int t = threadIdx.x; t < sg.n; t += kThreads) {
+            const int np = sg.n_pad;
+            aos[2 * t] = make_float4(rows[t], rows[np + t], rows[2 * np + t], rows[3 * np + t]);
+            aos[2 * t + 1] = make_float4(rows[4 * np + t], rows[5 * np + t], rows[kRowTol * np + t],
+                                         rows[kRowGround * np + t]);
+        }
+        __syncthreads();
+        ob.aos = aos;
+    }
     edge_warps<2, float>(P, &rb, &ob, P.nmf, wsh[threadIdx.x >> 5], qbuf[threadIdx.x >> 5]);
 }
 
 cudaError_t launch_edges_fp32(const EdgeParams &p, int grid, size_t smem, cudaStream_t st) {
+    if (p.nseg_lane == 1 && p.segs[0].seg.n_pad <= kAosMaxPad) smem += (size_t)p.segs[0].seg.n_pad * kFRows * sizeof(float);
     static bool attr = false;
     if (!attr) { cudaFuncSetAttribute(k_edges_fp32, cudaFuncAttributeMaxDynamicSharedMemorySize, 160 * 1024); attr = true; }
     k_edges_fp32<<<grid, kThreads, smem, st>>>(p);
