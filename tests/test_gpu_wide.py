@@ -217,6 +217,30 @@ def test_warp_edges_match_oracle_and_lane(engine, layout, prec, oprec):
     assert np.array_equal(outs["lane"][0], rv) and np.array_equal(outs["lane"][1], rk)
 
 
+@pytest.mark.parametrize("prec,oprec", FORMS)
+@pytest.mark.parametrize("n", [100, 700])
+def test_lane_edges_staged_rows(engine, layout, prec, oprec, n):
+    """The lane edge pass with one scene staged in shared memory: read through
+    the per-obstacle copy of the rows (100 boxes) and through the plain rows
+    (700 boxes, beyond the copy's size limit)."""
+    robot = robots.spatial(10, radius=0.03)
+    scene = _big_scene(61 + n, n, 0.02, 0.08, 1.4)
+    rng = np.random.default_rng(62)
+    q1 = scenes.uniform_configs(rng, 400, 10)
+    q2 = (q1 + rng.uniform(-0.6, 0.6, q1.shape)).astype(np.float32)
+    sid = engine.create_scene(engine.upload_robot(robot), scene)
+    layout("lane")
+    v = torch.zeros(400, dtype=torch.uint8, device="cuda")
+    k = torch.zeros(400, dtype=torch.int32, device="cuda")
+    engine.check_edges(sid, torch.from_numpy(q1).cuda(), torch.from_numpy(q2).cuda(), v, k, step=0.05,
+                       precision=prec)
+    engine.sync()
+    engine.destroy_scene(sid)
+    rv, rk = O.check_edges(robot, scene, q1, q2, step=0.05, prec=oprec)
+    assert np.array_equal(v.cpu().numpy(), rv) and np.array_equal(k.cpu().numpy(), rk)
+    assert 0 < int(rv.sum()) < 400
+
+
 def test_warp_edges_big_scene_fixed_count(engine, layout):
     """22 links against 1000 boxes with the fixed NUM_INTERPOLATION_VALIDITY_CHECKS
     discretisation (step <= 0), FP32 + FP64 recheck, with CUDA-graph replay."""
