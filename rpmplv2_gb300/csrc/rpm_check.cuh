@@ -294,7 +294,9 @@ template <int MODE> struct BoolMargin<MODE, float> { __device__ static float m()
 
 // flags bits: 1 settled collision, 2 unsettled isValid pair, 4 unsettled
 // distance pair (bits 1-4 per link), 8 pair list full (per configuration).
-template <int MODE, typename T>
+// FLAT: the isValid tree with its rectangle test inlined (coll_box), for
+// kernels that run no distance tree.
+template <int MODE, typename T, bool FLAT = false>
 __device__ __forceinline__ void drain_bool(WarpShared<T> &sh, const DevRobot &rb, const ObsView<T> &ob, const Num<T> &nm,
                                            int i, int nitems, const PairSink *ps) {
     typedef typename PolOf<MODE>::type P;
@@ -305,7 +307,8 @@ __device__ __forceinline__ void drain_bool(WarpShared<T> &sh, const DevRobot &rb
         const int owner = (int)(e & 31u), j = (int)(e >> 5);
         T o[6];
         ob.box(j, o);
-        const RB rr = coll_box_call<T, P>(nm, sh.a[owner], sh.b[owner], LinkConst<T>::r(rb, i), LinkConst<T>::rn(rb, i), o);
+        const RB rr = coll_box_call<T, P, FLAT>(nm, sh.a[owner], sh.b[owner], LinkConst<T>::r(rb, i),
+                                                LinkConst<T>::rn(rb, i), o);
         const bool c = rr.v;
         if (P::robust && rr.m < kDecide) {
             atomicOr(&sh.flags[owner], 2);
@@ -341,7 +344,7 @@ __device__ __forceinline__ T pair_distance(const DevRobot &rb, const V &ob, cons
     return d;
 }
 
-template <int MODE, typename T>
+template <int MODE, typename T, bool FLAT = false>
 __device__ __forceinline__ void drain_dist(WarpShared<T> &sh, const DevRobot &rb, const ObsView<T> &ob, const Num<T> &nm,
                                            int i, int nitems, const PairSink *ps) {
     const int lane = threadIdx.x & 31;
@@ -394,7 +397,7 @@ template <typename T> __device__ __forceinline__ T gap2_bb(const T *lo, const T 
             (N) += __popc(m_);                                                         \
             if ((N) >= 32) {                                                           \
                 __syncwarp();                                                          \
-                DRAIN<MODE, T>(sh, rb, ob, nm, i, 32, ps);                             \
+                DRAIN<MODE, T, kFlat>(sh, rb, ob, nm, i, 32, ps);                      \
                 __syncwarp();                                                          \
                 if (lane < (N) - 32) sh.Q[lane] = sh.Q[32 + lane];                     \
                 (N) -= 32;                                                             \
@@ -420,6 +423,7 @@ __device__ int warp_check(WarpShared<T> &sh, const DevRobot &rb, const ObsView<T
                           int *hit_j = nullptr) {
     const Want w{(KIND == 2 || KIND == 3) ? false : w_in.valid, KIND == 1 ? false : w_in.dist,
                  (KIND == 1 || KIND == 3) ? false : w_in.profile};
+    constexpr bool kFlat = KIND == 1;   // the isValid tree alone: its rectangle test inlined
     const unsigned full = 0xffffffffu;
     const int lane = threadIdx.x & 31;
     const unsigned lt_mask = (1u << lane) - 1u;
@@ -543,7 +547,7 @@ __device__ int warp_check(WarpShared<T> &sh, const DevRobot &rb, const ObsView<T
                 RPM_PUSH_AND_DRAIN(qd, nd, qd, item, drain_dist, (hj = sh.hitj[lane], cur = Key<T>::value(sh.lmin[lane])));
         }
         __syncwarp();
-        if (nb > 0) drain_bool<MODE, T>(sh, rb, ob, nm, i, nb, ps);
+        if (nb > 0) drain_bool<MODE, T, kFlat>(sh, rb, ob, nm, i, nb, ps);
         if (nd > 0) drain_dist<MODE, T>(sh, rb, ob, nm, i, nd, ps);
         __syncwarp();
         // ---- fold this link's results into the lane's configuration

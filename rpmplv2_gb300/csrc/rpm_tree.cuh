@@ -389,8 +389,10 @@ __host__ __device__ __noinline__ RB coll_rect_call(const Num<T> nm, const T *A, 
 // collisionCapsuleToBox (:4-42).  r_new = radius * sqrt(3) / 3 comes
 // precomputed per link with the reference's rounding.  The face tests of
 // :19-40 run as one loop over the axes (x, then y, then z), stopping at the
-// first collision.
-template <typename T, typename P>
+// first collision.  FLAT inlines the rectangle test: for a kernel that runs
+// this tree alone, a nested out-of-line call costs more in saved registers
+// than the shared copy saves in instruction cache.
+template <typename T, typename P, bool FLAT = false>
 RPM_HD bool coll_box(P &pol, const Num<T> &nm, const T *A, const T *B, T radius, T r_new, const T *o) {
     auto inA = P::all6(P::gt(A[0], o[0] - r_new), P::gt(A[1], o[1] - r_new), P::gt(A[2], o[2] - r_new),
                        P::lt(A[0], o[3] + r_new), P::lt(A[1], o[4] + r_new), P::lt(A[2], o[5] + r_new));
@@ -411,9 +413,13 @@ RPM_HD bool coll_box(P &pol, const Num<T> &nm, const T *A, const T *B, T radius,
         if (RPM_TAKE(pol, P::lt(a, sel6(o, ax)))) face = ax;
         else if (RPM_TAKE(pol, P::gt(a, sel6(o, ax + 3)))) face = ax + 3;
         if (face >= 0) {
-            const RB rr = coll_rect_call<T, P>(nm, A, B, radius, o, face);
-            RPM_NOTE(pol, rr.m);
-            if (rr.v) return true;
+            if constexpr (FLAT) {
+                if (coll_rect(pol, nm, A, B, radius, o, face)) return true;
+            } else {
+                const RB rr = coll_rect_call<T, P>(nm, A, B, radius, o, face);
+                RPM_NOTE(pol, rr.m);
+                if (rr.v) return true;
+            }
         }
     }
     return false;
@@ -585,11 +591,11 @@ template <typename T> struct ValM {
     float ia, m;
 };
 
-template <typename T, typename P>
+template <typename T, typename P, bool FLAT = false>
 __host__ __device__ __noinline__ RB coll_box_call(const Num<T> nm, const T *A, const T *B, T radius, T r_new,
                                                   const T *o) {
     P pol;
-    const bool v = coll_box(pol, nm, A, B, radius, r_new, o);
+    const bool v = coll_box<T, P, FLAT>(pol, nm, A, B, radius, r_new, o);
     return RB{v, pol.m};
 }
 
