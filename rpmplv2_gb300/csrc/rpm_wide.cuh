@@ -258,7 +258,8 @@ __device__ __forceinline__ void multi_flush(MultiState<T> &ms, const PairSink *p
     __syncwarp();
 }
 
-template <int MODE, typename T>
+// FLAT: the collision tree with its rectangle test inlined (kernels without the distance tree).
+template <int MODE, typename T, bool FLAT = false>
 __device__ __forceinline__ void multi_drain_bool(MultiState<T> &ms, int nitems, const DevRobot &rb,
                                                  const SortedView<T> &ob, const Num<T> &nm, const T *pts, int stride,
                                                  const PairSink *ps) {
@@ -271,7 +272,7 @@ __device__ __forceinline__ void multi_drain_bool(MultiState<T> &ms, int nitems, 
         const T *A = pts + g * stride + 3 * link;
         T o[6];
         ob.box(s, o);
-        const RB rr = coll_box_call<T, P>(nm, A, A + 3, LinkConst<T>::r(rb, link), LinkConst<T>::rn(rb, link), o);
+        const RB rr = coll_box_call<T, P, FLAT>(nm, A, A + 3, LinkConst<T>::r(rb, link), LinkConst<T>::rn(rb, link), o);
         if (P::robust && rr.m < kDecide) {
             atomicOr(&ms.flags[g], 2);
             pe = 0x80000000u | ((ob.idx[s] & 2047u) << 10) | ((uint32_t)link << 5) | (uint32_t)g;
@@ -320,10 +321,14 @@ __device__ __forceinline__ void multi_drain_dist(MultiState<T> &ms, int nitems, 
 // and / or the distance; 'live' marks the configurations to check.  On return
 // lane g < G holds configuration g's results: *valid (0 / 1), *dist, the
 // status (kSettled / kPairs / kFull), its record and first settled hit.
-template <int MODE, typename T>
+// KIND 1: isValid only, fixed at compile time (the edge checks), so the
+// distance tree and its queue compile away and the collision tree is FLAT.
+template <int MODE, typename T, int KIND = 0>
 __device__ void wide_multi_np(MultiState<T> &ms, const DevRobot &rb, const SortedView<T> &ob, const T *pts,
-                              int stride, int G, unsigned live, const Num<T> &nm, Want w, const PairSink *ps,
+                              int stride, int G, unsigned live, const Num<T> &nm, Want w_in, const PairSink *ps,
                               uint8_t &valid, double &dist, int &status, int &slot, int &hit_link, int &hit_j) {
+    const Want w{w_in.valid, KIND == 1 ? false : w_in.dist, w_in.profile};
+    constexpr bool kFlat = KIND == 1;
     typedef typename Key<T>::type K;
     const unsigned full = 0xffffffffu;
     const int lane = threadIdx.x & 31;
@@ -457,7 +462,7 @@ __device__ void wide_multi_np(MultiState<T> &ms, const DevRobot &rb, const Sorte
                     if (need_b) {
                         wide_push<MODE, T>(ms.qb, nqb, pb, item);
                         if (nqb >= 32) {
-                            multi_drain_bool<MODE, T>(ms, 32, rb, ob, nm, pts, stride, ps);
+                            multi_drain_bool<MODE, T, kFlat>(ms, 32, rb, ob, nm, pts, stride, ps);
                             wide_pop32(ms.qb, nqb);
                         }
                     }
@@ -472,7 +477,7 @@ __device__ void wide_multi_np(MultiState<T> &ms, const DevRobot &rb, const Sorte
             }
         }
     }
-    if (nqb > 0) multi_drain_bool<MODE, T>(ms, nqb, rb, ob, nm, pts, stride, ps);
+    if (nqb > 0) multi_drain_bool<MODE, T, kFlat>(ms, nqb, rb, ob, nm, pts, stride, ps);
     if (nqd > 0) multi_drain_dist<MODE, T>(ms, nqd, rb, ob, nm, pts, stride, ps);
     __syncwarp();
     // ---- results of configuration 'lane'
@@ -846,7 +851,7 @@ __device__ __forceinline__ void edge_wide_body(const EdgeParams &P, unsigned cha
         __syncwarp();
         double dd;
         int hl, hj;
-        wide_multi_np<MODE, T>(ms[warp], rb, ob, pts, (D + 1) * 3, G, live, nm, Want{true, false, false},
+        wide_multi_np<MODE, T, 1>(ms[warp], rb, ob, pts, (D + 1) * 3, G, live, nm, Want{true, false, false},
                                MODE == 2 ? &P.ps : nullptr, v, dd, st, slot, hl, hj);
         __syncwarp();
         return live;
