@@ -536,12 +536,12 @@ cudaError_t launch_edge_prep(const EdgeParams &p, cudaStream_t st) {
 
 cudaError_t launch_edges(int mode, const EdgeParams &p, int grid, size_t smem, cudaStream_t st) {
     if (mode == RPM_PREC_FP64) {
-        static bool attr = false;
-        if (!attr) { cudaFuncSetAttribute(k_edges_exact<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, 160 * 1024); attr = true; }
+        static std::atomic<uint64_t> attr{0};
+        ensure_smem_limit(k_edges_exact<0>, 160 * 1024, attr);
         k_edges_exact<0><<<grid, kThreads, smem, st>>>(p);
     } else {
-        static bool attr = false;
-        if (!attr) { cudaFuncSetAttribute(k_edges_exact<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, 160 * 1024); attr = true; }
+        static std::atomic<uint64_t> attr{0};
+        ensure_smem_limit(k_edges_exact<1>, 160 * 1024, attr);
         k_edges_exact<1><<<grid, kThreads, smem, st>>>(p);
     }
     return cudaGetLastError();
@@ -549,8 +549,8 @@ cudaError_t launch_edges(int mode, const EdgeParams &p, int grid, size_t smem, c
 
 template <int MODE, bool MULTI>
 static cudaError_t launch_wide_edges(const EdgeParams &p, int grid, size_t smem, cudaStream_t st) {
-    static bool attr = false;
-    if (!attr) { cudaFuncSetAttribute(k_edges_wide<MODE, MULTI>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024); attr = true; }
+    static std::atomic<uint64_t> attr{0};
+    ensure_smem_limit(k_edges_wide<MODE, MULTI>, 200 * 1024, attr);
     k_edges_wide<MODE, MULTI><<<grid, kWideThreads, smem, st>>>(p);
     return cudaGetLastError();
 }
@@ -577,12 +577,12 @@ cudaError_t launch_edge_recheck_final(const EdgeParams &p, int grid, bool pairs,
 
 cudaError_t launch_check_exact(int mode, const KParams &p, int64_t blocks, size_t smem, cudaStream_t st) {
     if (mode == RPM_PREC_FP64) {
-        static bool attr = false;
-        if (!attr) { cudaFuncSetAttribute(k_check_exact<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024); attr = true; }
+        static std::atomic<uint64_t> attr{0};
+        ensure_smem_limit(k_check_exact<0>, 200 * 1024, attr);
         k_check_exact<0><<<(unsigned)blocks, kThreads, smem, st>>>(p);
     } else {
-        static bool attr = false;
-        if (!attr) { cudaFuncSetAttribute(k_check_exact<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024); attr = true; }
+        static std::atomic<uint64_t> attr{0};
+        ensure_smem_limit(k_check_exact<1>, 200 * 1024, attr);
         k_check_exact<1><<<(unsigned)blocks, kThreads, smem, st>>>(p);
     }
     return cudaGetLastError();
@@ -593,12 +593,12 @@ size_t wide_smem_bytes(int mode, int ns, int nb) { return WideLayout::of(mode, n
 cudaError_t launch_check_wide(int mode, const KParams &p, int64_t blocks, size_t smem, cudaStream_t st) {
     if (mode == RPM_PREC_FP32_RECHECK) return launch_check_wide_fp32(p, blocks, smem, st);
     if (mode == RPM_PREC_FP64) {
-        static bool attr = false;
-        if (!attr) { cudaFuncSetAttribute(k_check_wide<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024); attr = true; }
+        static std::atomic<uint64_t> attr{0};
+        ensure_smem_limit(k_check_wide<0>, 200 * 1024, attr);
         k_check_wide<0><<<(unsigned)blocks, kWideThreads, smem, st>>>(p);
     } else {
-        static bool attr = false;
-        if (!attr) { cudaFuncSetAttribute(k_check_wide<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024); attr = true; }
+        static std::atomic<uint64_t> attr{0};
+        ensure_smem_limit(k_check_wide<1>, 200 * 1024, attr);
         k_check_wide<1><<<(unsigned)blocks, kWideThreads, smem, st>>>(p);
     }
     return cudaGetLastError();

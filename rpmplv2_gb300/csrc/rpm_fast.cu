@@ -79,8 +79,8 @@ __global__ void __launch_bounds__(kWideThreads, 2) k_check_wide_fp32(const __gri
 }
 
 cudaError_t launch_check_wide_fp32(const KParams &p, int64_t blocks, size_t smem, cudaStream_t st) {
-    static bool attr = false;
-    if (!attr) { cudaFuncSetAttribute(k_check_wide_fp32, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024); attr = true; }
+    static std::atomic<uint64_t> attr{0};
+    ensure_smem_limit(k_check_wide_fp32, 200 * 1024, attr);
     k_check_wide_fp32<<<(unsigned)blocks, kWideThreads, smem, st>>>(p);
     return cudaGetLastError();
 }
@@ -96,12 +96,12 @@ __global__ void __launch_bounds__(kWideThreads, 2) k_edges_wide_fp32(const __gri
 }
 
 cudaError_t launch_edges_wide_fp32(const EdgeParams &p, int grid, size_t smem, cudaStream_t st) {
-    static bool attr[2] = {false, false};
+    static std::atomic<uint64_t> attr[2] = {{0}, {0}};
     if (p.nseg - p.nseg_lane > 1) {
-        if (!attr[1]) { cudaFuncSetAttribute(k_edges_wide_fp32<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024); attr[1] = true; }
+        ensure_smem_limit(k_edges_wide_fp32<true>, 200 * 1024, attr[1]);
         k_edges_wide_fp32<true><<<grid, kWideThreads, smem, st>>>(p);
     } else {
-        if (!attr[0]) { cudaFuncSetAttribute(k_edges_wide_fp32<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024); attr[0] = true; }
+        ensure_smem_limit(k_edges_wide_fp32<false>, 200 * 1024, attr[0]);
         k_edges_wide_fp32<false><<<grid, kWideThreads, smem, st>>>(p);
     }
     return cudaGetLastError();
@@ -146,8 +146,8 @@ __global__ void __launch_bounds__(kThreads) k_edges_fp32(const __grid_constant__
 
 cudaError_t launch_edges_fp32(const EdgeParams &p, int grid, size_t smem, cudaStream_t st) {
     if (p.nseg_lane == 1 && p.segs[0].seg.n_pad <= kAosMaxPad) smem += (size_t)p.segs[0].seg.n_pad * kFRows * sizeof(float);
-    static bool attr = false;
-    if (!attr) { cudaFuncSetAttribute(k_edges_fp32, cudaFuncAttributeMaxDynamicSharedMemorySize, 160 * 1024); attr = true; }
+    static std::atomic<uint64_t> attr{0};
+    ensure_smem_limit(k_edges_fp32, 160 * 1024, attr);
     k_edges_fp32<<<grid, kThreads, smem, st>>>(p);
     return cudaGetLastError();
 }
@@ -190,8 +190,8 @@ cudaError_t launch_ffma_probe(float *out, int blocks, int threads, int iters, cu
 }
 
 template <int KIND> static cudaError_t launch_fp32_kind(const KParams &p, int64_t blocks, size_t smem, cudaStream_t st) {
-    static bool attr = false;
-    if (!attr) { cudaFuncSetAttribute(k_check_fp32<KIND>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024); attr = true; }
+    static std::atomic<uint64_t> attr{0};
+    ensure_smem_limit(k_check_fp32<KIND>, 200 * 1024, attr);
     k_check_fp32<KIND><<<(unsigned)blocks, kThreads, smem, st>>>(p);
     return cudaGetLastError();
 }

@@ -1,5 +1,6 @@
 // rpm_launch.cuh -- kernel parameter block and host-side launchers.
 #pragma once
+#include <atomic>
 #include <cstdint>
 #include <cuda_runtime.h>
 
@@ -11,6 +12,19 @@ namespace rpm {
 
 constexpr int kThreads = 128;     // configurations per CTA
 constexpr int kMaxSegs = 32;      // segments per launch (passed by value)
+
+// Raise a kernel's dynamic shared-memory limit once per device.  'done'
+// holds one bit per device (the attribute belongs to the device's context);
+// concurrent callers may both set it, which is harmless.
+template <typename K>
+inline void ensure_smem_limit(K kernel, int bytes, std::atomic<uint64_t> &done) {
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return;
+    const uint64_t bit = 1ull << (dev & 63);
+    if (done.load(std::memory_order_acquire) & bit) return;
+    if (cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes) == cudaSuccess)
+        done.fetch_or(bit, std::memory_order_acq_rel);
+}
 
 struct KParams {
     Seg segs[kMaxSegs];

@@ -164,12 +164,9 @@ extern "C" int rpm_check_configs_noalloc(const rpm_robot_desc *robot, const floa
         return set_error(RPM_ERR_CUDA, "rpm_check_configs_noalloc: device query failed");
     const size_t smem32 = (size_t)kFRows * P.n_pad * sizeof(float);
     const size_t smem64 = (size_t)kDRows * P.n_pad * sizeof(double) + (size_t)P.n_pad * sizeof(float);
-    static bool attr[kNoAllocMaxDevices] = {false};
-    if (!attr[dev]) {
-        cudaFuncSetAttribute(k_noalloc_fp32, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-        cudaFuncSetAttribute(k_noalloc_recheck, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-        attr[dev] = true;
-    }
+    static std::atomic<uint64_t> attr32{0}, attr64{0};
+    ensure_smem_limit(k_noalloc_fp32, 200 * 1024, attr32);
+    ensure_smem_limit(k_noalloc_recheck, 200 * 1024, attr64);
     const unsigned blocks = (unsigned)((num_configs + kThreads - 1) / kThreads);
     k_noalloc_fp32<<<blocks, kThreads, smem32, st>>>(P);
     k_noalloc_recheck<<<sms * 2, kThreads, smem64, st>>>(P);
