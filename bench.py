@@ -486,9 +486,10 @@ def run_ours(args, ws, rank, local):
         "e2e": {"value": C * args.steps / e2e_s, "unit": "configs/s", "h2d_bytes_per_step": C * D * 4,
                 "d2h_bytes_per_step": C * (1 + 8), "call": "rpm_check_configs_host", "matches_device_run": e2e_ok,
                 "transfer": "pinned host buffers read and written by the kernels over NVLink-C2C (zero-copy)"},
-        # per step: k_check_fp32 (isValid and distance as two segments of one launch), then the pair
-        # recheck k_pair_skel / k_pair_eval / k_pair_fold and the whole-configuration k_recheck
-        "gpu_launches": 5 * args.steps,
+        # per step, for each of the two outputs (isValid, distance): k_check_fp32 compiled for that
+        # output, then the pair recheck k_pair_skel / k_pair_eval / k_pair_fold and the
+        # whole-configuration k_recheck
+        "gpu_launches": 10 * args.steps,
         "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak_fp32, "unit": "TFLOP/s",
                      "frac": achieved / peak_fp32 if peak_fp32 else None, "traffic": traffic_per_launch(),
                      "kernel": "k_check_fp32", "kernel_ms": statistics.median(bulk_ms),
