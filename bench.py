@@ -114,16 +114,75 @@ class ClockSampler:
 
 
 def cpu_baseline(robot, scene, q, sample):
-    """The oracle (a restatement of the reference's FP32 path) on every host core."""
+    """The oracle (a restatement of the reference's FP32 path) on every host
+    core.  Returns the baseline line and the oracle's outputs (ref32 valid,
+    distance) on the sample, which the parity accounting then uses."""
     from oracle import oracle as O
     cores = os.cpu_count() or 1
     qs = np.ascontiguousarray(q[:sample])
     O.check_configs(robot, scene, qs[:4096], prec="ref32", nthreads=cores)   # warm-up
     t0 = time.perf_counter()
-    O.check_configs(robot, scene, qs, prec="ref32", nthreads=cores)
+    rv, rd, _ = O.check_configs(robot, scene, qs, prec="ref32", nthreads=cores)
     dt = time.perf_counter() - t0
-    return {"value": sample / dt, "unit": "configs/s", "cores": cores, "kind": "port",
-            "sample": "%d configs of the same workload, isValid + computeDistance, ref32 oracle, OpenMP" % sample}
+    t1 = time.perf_counter()
+    O.check_configs(robot, scene, qs[:65536], prec="ref32", nthreads=1)
+    dt1 = time.perf_counter() - t1
+    line = {"value": sample / dt, "unit": "configs/s", "cores": cores, "kind": "port",
+            "sample": "%d configs of the same workload, isValid + computeDistance, ref32 oracle, OpenMP" % sample,
+            "one_core": {"value": 65536 / dt1, "unit": "configs/s", "cores": 1,
+                         "sample": "the first 65,536 of those configs"}}
+    return line, rv, rd
+
+
+BAND_M = 1e-5   # FP32 rounding band of a decision margin (metres over error amplification)
+
+
+def parity_accounting(eng, sid, robot, scene, q, outs, ref32):
+    """Headline-size parity against the oracle (the checker, not the thing
+    measured): the FP64 form against ref64, and every form against ref32, the
+    reference's own FP32 numerics.  Each isValid flip and each distance
+    difference above 1e-5 m against ref32 is listed with its FP64 decision
+    margin (rpm_decision_margins), which must lie inside the FP32 rounding
+    band."""
+    import torch
+    from oracle import oracle as O
+    cores = os.cpu_count() or 1
+    rv32, rd32 = ref32
+    rv64, rd64, _ = O.check_configs(robot, scene, q, prec="ref64", want=("valid", "dist"), nthreads=cores)
+    out = {"configs": int(q.shape[0]), "band_m": BAND_M}
+    v64, d64 = outs["fp64"]
+    out["fp64_vs_ref64"] = {"isvalid_mismatches": int((v64 != rv64).sum()),
+                            "distance_bit_mismatches": int((d64.view(np.uint64) != rd64.view(np.uint64)).sum())}
+    v32, d32 = outs["fp32_recheck"]
+    out["fp32_recheck_vs_ref64"] = {"isvalid_flips": int((v32 != rv64).sum()),
+                                    "max_distance_error_m": float(np.abs(d32 - rd64).max())}
+    vr, dr = outs["fp32_ref"]
+    out["fp32_ref_vs_ref32"] = {"isvalid_mismatches": int((vr != rv32).sum()),
+                                "distance_bit_mismatches": int((dr.view(np.uint64) != rd32.view(np.uint64)).sum())}
+    for form in ("fp64", "fp32_recheck"):
+        v, d = outs[form]
+        flips = np.nonzero(v != rv32)[0]
+        dflips = np.nonzero(np.abs(d - rd32) > 1e-5)[0]
+        sel = np.union1d(flips, dflips)
+        mv = md = np.zeros(0)
+        if sel.size:
+            qd = torch.from_numpy(np.ascontiguousarray(q[sel])).cuda()
+            tv = torch.zeros(sel.size, dtype=torch.float64, device="cuda")
+            tdm = torch.zeros(sel.size, dtype=torch.float64, device="cuda")
+            eng.decision_margins(sid, qd, tv, tdm)
+            eng.sync()
+            mv, md = tv.cpu().numpy(), tdm.cpu().numpy()
+        fm = mv[np.isin(sel, flips)]
+        dm = md[np.isin(sel, dflips)]
+        rest = np.setdiff1d(np.arange(q.shape[0]), dflips)
+        out["%s_vs_ref32" % form] = {
+            "isvalid_flips": int(flips.size), "max_flip_margin_m": float(fm.max()) if fm.size else None,
+            "distance_diffs_gt_1e-5_m": int(dflips.size), "max_diff_margin_m": float(dm.max()) if dm.size else None,
+            "all_inside_band": bool(np.all(fm < BAND_M) and np.all(dm < BAND_M)),
+            "max_distance_diff_elsewhere_m": float(np.abs(d[rest] - rd32[rest]).max()) if rest.size else None,
+            "flips": [{"config": int(c), "ours": int(v[c]), "ref32": int(rv32[c]), "margin_m": float(m)}
+                      for c, m in zip(flips[:8], fm[:8])]}
+    return out
 
 
 def traffic_per_launch():
@@ -428,6 +487,10 @@ def run_ours(args, ws, rank, local):
     v64, d64 = valid.clone(), distv.clone()
     flips = int((v32 != v64).sum().item())
     max_derr = float((d32 - d64).abs().max().item())
+    # ---- the reference-numerics form on the same batch (bit-equal to ref32)
+    stepref, _, _, _ = timed("fp32_ref", 2, 1)
+    outs = {"fp32_recheck": (v32.cpu().numpy(), d32.cpu().numpy()), "fp64": (v64.cpu().numpy(), d64.cpu().numpy()),
+            "fp32_ref": (valid.cpu().numpy(), distv.cpu().numpy())}
 
     t_local = sum(step_ms) / 1e3
     if dist is not None:
@@ -500,8 +563,13 @@ def run_ours(args, ws, rank, local):
                              "bytes_per_config": BYTES_PER_CONFIG, "peak_source": "MEASURED_PEAKS.json hbm_gbs"}},
     }
     line.update(extra)
+    line["fp32_ref_form"] = {"value": C / (statistics.median(stepref) / 1e3), "unit": "configs/s",
+                             "note": "the reference's own numerics on the device (FP64 FK rounded to FP32, FP32 trees)"}
     if ws == 1 or rank == 0:
-        line["cpu_baseline"] = cpu_baseline(robot, scene, q, min(C, 1 << 20))
+        line["cpu_baseline"], rv32, rd32 = cpu_baseline(robot, scene, q, min(C, 1 << 20))
+        n = rv32.shape[0]
+        line["parity"] = parity_accounting(eng, sid, robot, scene, q[:n], {k: (a[:n], b[:n]) for k, (a, b) in outs.items()},
+                                           (rv32, rd32))
     print(json.dumps(line), flush=True)
     if dist is not None:
         dist.destroy_process_group()

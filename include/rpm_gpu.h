@@ -245,6 +245,21 @@ int rpm_distance_underestimation(rpm_ctx *ctx, int32_t scene_id, int32_t precisi
                                  int64_t num_configs, const float *nearest_dev, double *dist_dev, float *profile_dev,
                                  uint8_t *complete_dev, void *stream);
 
+/* How close each configuration's answers lie to a decision boundary of the
+ * reference's trees (RealVectorSpace.cpp:277-309, 318-392 with
+ * CollisionAndDistance.cpp:4-755), in metres over the error amplification of
+ * the compared quantities, evaluated in FP64 on the FP64 skeleton.  The
+ * isValid margin is that of the OR over the pairs (a collision as robust as
+ * its most robust colliding pair, a free configuration as its least robust
+ * pair); the distance margin is the smallest among the pairs that can set d_c
+ * (within 1e-3 m of it), including the contact band and min_dist_tol rules,
+ * or for a collision the largest among the pairs at distance 0.  Where the
+ * reference's FP32 numerics and FP64 disagree on a configuration, its margin
+ * lies inside the FP32 rounding band (about 1e-5 m): the diagnostic that
+ * explains such flips. */
+int rpm_decision_margins(rpm_ctx *ctx, int32_t scene_id, const float *q_dev, int64_t num_configs,
+                         double *margin_valid_dev, double *margin_dist_dev, void *stream);
+
 /* Skeleton points (L+1 points x 3) per configuration, widened to double
  * (computeSkeleton; xArm6.cpp:209-235, Planar2DOF.cpp:117-130): RPM_PREC_FP64
  * gives the FP64 points, RPM_PREC_FP32_REF the reference's float skeleton,
@@ -407,6 +422,7 @@ typedef struct rpm_request_timing {
     int32_t status;              /* 0 done, 1 pending, < 0 error (RPM_ERR_ADMISSION: larger than the budget) */
     int32_t batch_size;          /* requests in the launch it ran in */
     double t_submit, t_admit, t_launch, t_done;   /* seconds (monotonic; relative to the start in a replay) */
+    uint64_t scene_version;      /* the version of the request's scene its checks read (rpm_scene_update) */
 } rpm_request_timing;
 
 /* A moving obstacle of a replay: AABB(t) = AABB(0) + velocity * t. */
@@ -446,14 +462,31 @@ int rpm_last_timing(rpm_ctx *ctx, void *stream, float *bulk_ms, float *recheck_m
  * RPM_ERR_TIMEOUT, and the context stays usable. */
 int rpm_probe_bounded_wait(rpm_ctx *ctx, uint32_t polls);
 
+/* The decision trees on single primitives, for parity tests against the
+ * reference's own CollisionAndDistance.cpp on directed edge cases.  Case i
+ * evaluates, by kind_dev[i]:
+ *   0  collisionCapsuleToBox(a, b, r, aabb)    CollisionAndDistance.cpp:4-42   (value 1 = collision)
+ *   1  distanceCapsuleToBox(a, b, r, aabb)     :208-214, 409-755 (d_c, radius subtracted)
+ *   2  distanceLineSegToLineSeg(a, b, c, d)    :217-320
+ * a_dev, b_dev: n x 3; x_dev: n x 6 (the AABB, or c then d); r_dev: n.
+ * RPM_PREC_FP64 and RPM_PREC_FP32_REF evaluate the FP64 and the reference's
+ * FP32 trees.  RPM_PREC_FP32_RECHECK evaluates the FP32 pass's trees with
+ * their margins: settled_dev[i] = 1 where the pass settles the case, 0 where
+ * it leaves it to the FP64 recheck (value_dev then holds the FP64 value, as
+ * the form's outputs do), 2 if the pass's two compilations of the collision
+ * tree disagree (never expected). */
+int rpm_probe_primitives(rpm_ctx *ctx, int32_t precision, const int32_t *kind_dev, const float *a_dev,
+                         const float *b_dev, const float *x_dev, const float *r_dev, int64_t n, double *value_dev,
+                         uint8_t *settled_dev, void *stream);
+
 /* FP32 FMA throughput of the device (TFLOP/s), measured with independent FMA
  * chains: the denominator of the FP32 roofline. */
 int rpm_probe_fp32_peak(rpm_ctx *ctx, double *tflops);
 
 /* The FP32 + FP64-recheck check of rpm_check_configs for callers that cannot
- * allocate device memory (a CUDA graph being captured by someone else, a
- * real-time loop that forbids allocator calls after start-up, a framework that
- * owns all device memory).  No counterpart in the reference: it adds a calling
+ * allocate device memory (a real-time loop that forbids allocator calls after
+ * start-up, a framework that owns all device memory and hands out only its
+ * own buffers).  No counterpart in the reference: it adds a calling
  * convention, not a reference operation.  Everything is passed in: the robot
  * as a host descriptor, obstacles as the caller's device arrays (aabb_dev n x 6
  * floats as in rpm_scene_create, min_dist_tol_dev and flags_dev nullable),
@@ -462,8 +495,10 @@ int rpm_probe_fp32_peak(rpm_ctx *ctx, double *tflops);
  * static device array of 65,536 entries (~512 KB held on every GPU that loads
  * the library), so num_configs above 65,536 returns RPM_ERR_RANGE.  The first
  * call on each device looks up the array's address and should come before any
- * stream capture.  All calls share the array: calls that overlap on the GPU
- * race and must be serialised by the caller. */
+ * stream capture; a call that finds another context current on the device
+ * (after cudaDeviceReset) looks it up again.  All calls share the array and
+ * keep the last call's contents: calls that overlap on the GPU race and must
+ * be serialised by the caller. */
 int rpm_check_configs_noalloc(const rpm_robot_desc *robot, const float *aabb_dev, const float *min_dist_tol_dev,
                               const uint8_t *flags_dev, int32_t n, const rpm_params *params, const float *q_dev,
                               int64_t num_configs, uint8_t *valid_dev, double *dist_dev, float *profile_dev,

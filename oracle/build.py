@@ -15,7 +15,10 @@ import subprocess
 import sys
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REF_ROOT = os.environ.get("RPM_REFERENCE_ROOT", "/root/reference")
+# The reference tree: RPM_REFERENCE_ROOT, else a "reference" directory beside
+# this repository.  Where it is absent the reference build is skipped.
+REF_ROOT = os.environ.get("RPM_REFERENCE_ROOT",
+                          os.path.join(os.path.dirname(os.path.dirname(HERE)), "reference"))
 ORACLE_SO = os.path.join(HERE, "_build", "librpm_oracle.so")
 REF_SO = os.path.join(HERE, "_ref", "libref_cad.so")
 

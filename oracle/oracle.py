@@ -39,6 +39,7 @@ def lib():
         L.orc_prim_segseg.argtypes = [_f, _f, _f, _f, ctypes.c_int, _vp]
         L.orc_prim_segseg.restype = ctypes.c_double
         L.orc_box_aabb.argtypes = [_f, _f, _f, _f]
+        L.orc_undefined_hits.restype = ctypes.c_int64
         L.orc_distance_underest.argtypes = [_vp, ctypes.c_int, _f, ctypes.c_int64, ctypes.c_int, ctypes.c_int, _vp, _f,
                                             _d, _f, _u8]
         L.orc_motion_validity.argtypes = [_vp, _f, _f, _u8, ctypes.c_int, _f, _f, ctypes.c_int64, _vp, ctypes.c_int,
@@ -212,6 +213,12 @@ def prim_distance(A, B, r, obs, prec="ref32"):
     d = lib().orc_prim_distance(_p(A, _f), _p(B, _f), float(r), _p(obs, _f), _prec(prec), None, _p(pts, _f),
                                 ctypes.byref(hp))
     return d, pts, bool(hp.value)
+
+
+def undefined_hits():
+    """Evaluations on this thread that reached the reference's uninitialised
+    edge matrix (getLineSegments selecting no edge) since the last call."""
+    return int(lib().orc_undefined_hits())
 
 
 def box_aabb(dim, pos, quat_xyzw):

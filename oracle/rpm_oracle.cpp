@@ -359,6 +359,11 @@ template <typename T> bool coll_box(const Num<T> &nm, const T *A, const T *B, T 
 }
 
 // CapsuleToBox (CollisionAndDistance.cpp:395-755)
+// Evaluations that reached the reference's uninitialised-matrix branch of
+// getLineSegments (CollisionAndDistance.cpp:542-574 with no edge selected),
+// per host thread.
+thread_local int64_t g_undefined_hits = 0;
+
 template <typename T> struct CapsuleBox {
     const Num<T> &nm;
     T A[3], B[3], radius, obs[6];
@@ -420,7 +425,10 @@ template <typename T> struct CapsuleBox {
         else if (p1 > max2) { pt3(min1, max2, cv, coord, seg[n]); pt3(max1, max2, cv, coord, seg[n + 1]); n += 2; }
         // n == 0 leaves the reference's 3x2 matrix uninitialised (undefined); it is
         // reachable only when the segment meets the face rectangle exactly on its
-        // border, and is treated here as "no edge".
+        // border, and is treated here as "no edge".  g_undefined_hits counts it so
+        // fixtures can leave such cases out (the reference's answer there is heap
+        // garbage, not a value to match).
+        if (n == 0) ++g_undefined_hits;
         more_segments(seg, n);
     }
 
@@ -1072,6 +1080,14 @@ double orc_prim_distance(const float *A, const float *B, float r, const float *o
     if (pts_out) for (int k = 0; k < 6; ++k) pts_out[k] = (float)cb.pts[k];
     if (has_pts) *has_pts = cb.has_pts;
     return cb.d_c;
+}
+
+// Number of evaluations on this thread that reached the undefined branch of
+// getLineSegments since the last call (then reset).
+int64_t orc_undefined_hits(void) {
+    const int64_t n = g_undefined_hits;
+    g_undefined_hits = 0;
+    return n;
 }
 
 double orc_prim_segseg(const float *A, const float *B, const float *C, const float *D, int prec, const rpm_params *params) {

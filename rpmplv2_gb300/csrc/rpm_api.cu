@@ -1039,6 +1039,22 @@ int rpm_distance_nearest(rpm_ctx *ctx, int32_t scene_id, int32_t precision, cons
     return near_done(ctx, buf, st);
 }
 
+int rpm_decision_margins(rpm_ctx *ctx, int32_t scene_id, const float *q_dev, int64_t num_configs,
+                         double *margin_valid_dev, double *margin_dist_dev, void *stream) {
+    if (!ctx || num_configs < 0 || (num_configs > 0 && (!q_dev || !margin_valid_dev || !margin_dist_dev)))
+        return fail(RPM_ERR_INVALID, "bad arguments");
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    cudaStream_t st = (cudaStream_t)stream;
+    NearParams p;
+    SceneBuf *buf = nullptr;
+    int rc = near_setup(ctx, scene_id, RPM_PREC_FP64, q_dev, num_configs, st, p, &buf);
+    if (rc) return rc;
+    p.margin_valid = margin_valid_dev;
+    p.margin_dist = margin_dist_dev;
+    CK(launch_decision_margins(p, st));
+    return near_done(ctx, buf, st);
+}
+
 static int spine_robot(rpm_ctx *ctx, int32_t robot_id, SpineParams &p) {
     if (robot_id < 0 || robot_id >= (int32_t)ctx->robots.size() || !ctx->robots[robot_id].dev)
         return fail(RPM_ERR_INVALID, "unknown robot %d", robot_id);
@@ -1471,6 +1487,32 @@ int rpm_probe_fp32_peak(rpm_ctx *ctx, double *tflops) {
     cudaEventDestroy(b);
     cudaFree(buf);
     *tflops = best;
+    return RPM_OK;
+}
+
+int rpm_probe_primitives(rpm_ctx *ctx, int32_t precision, const int32_t *kind_dev, const float *a_dev,
+                         const float *b_dev, const float *x_dev, const float *r_dev, int64_t n, double *value_dev,
+                         uint8_t *settled_dev, void *stream) {
+    if (!ctx || n < 0 || (n > 0 && (!kind_dev || !a_dev || !b_dev || !x_dev || !r_dev || !value_dev)))
+        return fail(RPM_ERR_INVALID, "NULL argument");
+    if (precision < RPM_PREC_FP64 || precision > RPM_PREC_FP32_REF) return fail(RPM_ERR_INVALID, "unknown precision %d", precision);
+    if (precision == RPM_PREC_FP32_RECHECK && n > 0 && !settled_dev)
+        return fail(RPM_ERR_INVALID, "the FP32 + recheck form needs settled_dev");
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    if (set_device(ctx)) return RPM_ERR_CUDA;
+    ProbeParams p{};
+    p.kind = kind_dev; p.a = a_dev; p.b = b_dev; p.x = x_dev; p.r = r_dev; p.n = n;
+    p.nmd.eq = ctx->params.equality_threshold; p.nmd.maxd = ctx->params.max_distance;
+    p.nmf.eq = (float)ctx->params.equality_threshold; p.nmf.maxd = (float)ctx->params.max_distance;
+    p.value = value_dev;
+    p.settled = settled_dev;
+    cudaStream_t st = (cudaStream_t)stream;
+    if (precision == RPM_PREC_FP32_RECHECK) {
+        CK(launch_probe_fp32(p, st));
+        CK(launch_probe_exact(0, p, true, st));   // the FP64 recheck of what the FP32 pass left open
+    } else {
+        CK(launch_probe_exact(precision == RPM_PREC_FP64 ? 0 : 1, p, false, st));
+    }
     return RPM_OK;
 }
 

@@ -987,4 +987,140 @@ cudaError_t launch_motion_validity(int mode, const MotionParams &p, cudaStream_t
     return cudaGetLastError();
 }
 
+// ------------------------------------------------------------- primitive probe --
+// One case per thread through the same tree instances the check kernels use.
+template <int MODE>
+__global__ void k_probe_exact(const __grid_constant__ ProbeParams P, bool only_unsettled) {
+    typedef typename std::conditional<MODE == 0, double, float>::type T;
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= P.n) return;
+    if (only_unsettled && P.settled[i] != 0) return;
+    Num<T> nm;
+    if (MODE == 0) { nm.eq = (T)P.nmd.eq; nm.maxd = (T)P.nmd.maxd; }
+    else { nm.eq = (T)P.nmf.eq; nm.maxd = (T)P.nmf.maxd; }
+    T A[3], B[3], X[6];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) { A[k] = (T)P.a[3 * i + k]; B[k] = (T)P.b[3 * i + k]; }
+#pragma unroll
+    for (int k = 0; k < 6; ++k) X[k] = (T)P.x[6 * i + k];
+    const float rf = P.r[i];
+    const T r = (T)rf;
+    // r * sqrt(3) / 3 with sqrt(3) in double, as CollisionAndDistance.cpp:7 and the robot upload compute it
+    const double rn_d = (double)rf * sqrt(3.0) / 3;
+    const T rn = (T)rn_d;
+    double v;
+    const int kind = P.kind[i];
+    if (kind == 0) v = coll_box_call<T, ExactPol>(nm, A, B, r, rn, X).v ? 1.0 : 0.0;
+    else if (kind == 1) v = (double)capsule_box_call<T, ExactPol>(nm, A, B, r, X).v;
+    else {
+        ExactPol pol;
+        v = (double)seg_seg(pol, nm, A, B, X, X + 3).v;
+    }
+    P.value[i] = v;
+    if (P.settled && !only_unsettled) P.settled[i] = 1;
+}
+
+cudaError_t launch_probe_exact(int mode, const ProbeParams &p, bool only_unsettled, cudaStream_t st) {
+    const unsigned grid = (unsigned)((p.n + 127) / 128);
+    if (grid == 0) return cudaSuccess;
+    if (mode == 0) k_probe_exact<0><<<grid, 128, 0, st>>>(p, only_unsettled);
+    else k_probe_exact<1><<<grid, 128, 0, st>>>(p, only_unsettled);
+    return cudaGetLastError();
+}
+
+// ---------------------------------------------------- decision margins --
+// How close each configuration's FP64 answers lie to a decision boundary of
+// the reference's trees: the margins of RobustPol (metres over the error
+// amplification of the compared quantities) evaluated in FP64 on the FP64
+// skeleton, one warp per configuration, lanes over the obstacles.
+//   margin_valid: isValid is an OR over the pairs, so a collision is as
+//     robust as its most robust colliding pair and a free configuration as
+//     its least robust pair;
+//   margin_dist: the smallest margin among the pairs that can set d_c
+//     (clamped distance within 1e-3 m of the minimum; with the min_dist_tol
+//     and contact-band rules of the FP32 pass), or for a collision the
+//     largest margin among the pairs at distance 0 or below.
+// A configuration on which FP32 and FP64 arithmetic disagree must have a
+// margin inside the FP32 rounding band.
+__global__ void __launch_bounds__(kThreads) k_decision_margins(const __grid_constant__ NearParams P) {
+    __shared__ double skel[kThreads / 32][(kMaxDof + 1) * 3];
+    const unsigned full = 0xffffffffu;
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int64_t c = (int64_t)blockIdx.x * (kThreads / 32) + w;
+    if (c >= P.C) return;
+    const DevRobot &rb = *P.robot;
+    const int D = rb.D, L = D;
+    if (lane == 0) {
+        SkelWalker<0> sw;
+        sw.begin();
+        for (int k = 0; k <= D; ++k) sw.point(rb, P.q + c * D, k, skel[w] + 3 * k);
+    }
+    __syncwarp();
+    const Num<double> nm = P.nmd;
+    const float *ground = P.obs_f + (size_t)kRowGround * P.n_pad;
+    const double inf = 1e300;
+    // isValid: robust OR over the pairs; distance: pass 1 finds d_c
+    bool coll = false;
+    double m_true = 0.0, m_all = inf, dmin = nm.maxd, m_hit = 0.0;
+    bool hit = false;
+    for (int pass = 0; pass < 2; ++pass) {
+        double m_near = inf;
+        for (int i = 0; i < L; ++i) {
+            const double *A = skel[w] + 3 * i, *B = A + 3;
+            const double r = rb.radius_d[i], rn = rb.rnew_d[i];
+            for (int j = lane; j < P.n; j += 32) {
+                if (ground[j] != 0.f && i < rb.ground_included) continue;
+                double o[6];
+                for (int k = 0; k < 6; ++k) o[k] = P.obs_d[(size_t)k * P.n_pad + j];
+                const double tol = P.obs_d[(size_t)kRowTol * P.n_pad + j];
+                if (pass == 0) {
+                    const RB rr = coll_box_call<double, RobustPol>(nm, A, B, r, rn, o);
+                    if (rr.v) { coll = true; m_true = fmax(m_true, (double)rr.m); }
+                    m_all = fmin(m_all, (double)rr.m);
+                }
+                const ValM<double> dv = capsule_box_call<double, RobustPol>(nm, A, B, r, o);
+                double d = dv.v;
+                float m = dv.m;
+                const float band = dv.ia * (kDecide / kBand);
+                m = fminf(m, fabsf((float)(d - tol)) * band);
+                if (d != 0.0) m = fminf(m, fabsf((float)(d > tol ? nm.maxd : d)) * band);
+                if (d > tol) d = nm.maxd;
+                if (pass == 0) {
+                    if (d == d) dmin = fmin(dmin, d);
+                    if (d <= 0.0) { hit = true; m_hit = fmax(m_hit, (double)m); }
+                } else if (d <= dmin + 1e-3) {
+                    m_near = fmin(m_near, (double)m);
+                }
+            }
+        }
+        if (pass == 0) {
+#pragma unroll
+            for (int off = 16; off > 0; off >>= 1) {
+                coll = __shfl_xor_sync(full, (int)coll, off) != 0 || coll;
+                m_true = fmax(m_true, __shfl_xor_sync(full, m_true, off));
+                m_all = fmin(m_all, __shfl_xor_sync(full, m_all, off));
+                dmin = fmin(dmin, __shfl_xor_sync(full, dmin, off));
+                hit = __shfl_xor_sync(full, (int)hit, off) != 0 || hit;
+                m_hit = fmax(m_hit, __shfl_xor_sync(full, m_hit, off));
+            }
+            if (hit) break;   // d_c = 0: the margin is that of the most robust hit
+        } else {
+#pragma unroll
+            for (int off = 16; off > 0; off >>= 1) m_near = fmin(m_near, __shfl_xor_sync(full, m_near, off));
+            m_hit = m_near;
+        }
+    }
+    if (lane == 0) {
+        P.margin_valid[c] = coll ? m_true : m_all;
+        P.margin_dist[c] = m_hit;
+    }
+}
+
+cudaError_t launch_decision_margins(const NearParams &p, cudaStream_t st) {
+    const unsigned grid = (unsigned)((p.C + kThreads / 32 - 1) / (kThreads / 32));
+    if (grid == 0) return cudaSuccess;
+    k_decision_margins<<<grid, kThreads, 0, st>>>(p);
+    return cudaGetLastError();
+}
+
 }  // namespace rpm

@@ -212,4 +212,55 @@ cudaError_t launch_check_fp32(const KParams &p, int64_t blocks, size_t smem, cud
     return launch_fp32_kind<0>(p, blocks, smem, st);
 }
 
+// ------------------------------------------------------------- primitive probe --
+// The FP32 pass's decisions on single cases: the value in FP32 and whether the
+// pass would settle it (every decision margin at least kDecide, and for
+// distances the contact-band rule of pair_distance with min_dist_tol =
+// MAX_DISTANCE).  Unsettled cases are left to the FP64 recheck.
+__global__ void k_probe_fp32(const __grid_constant__ ProbeParams P) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= P.n) return;
+    const Num<float> nm = P.nmf;
+    float A[3], B[3], X[6];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) { A[k] = P.a[3 * i + k]; B[k] = P.b[3 * i + k]; }
+#pragma unroll
+    for (int k = 0; k < 6; ++k) X[k] = P.x[6 * i + k];
+    const float r = P.r[i];
+    const float rn = (float)((double)r * sqrt(3.0) / 3);
+    const int kind = P.kind[i];
+    double v;
+    uint8_t settled;
+    if (kind == 0) {
+        // the inlined (isValid-only kernels) and out-of-line rectangle tests must agree
+        const RB flat = coll_box_call<float, RobustPol, true>(nm, A, B, r, rn, X);
+        const RB call = coll_box_call<float, RobustPol, false>(nm, A, B, r, rn, X);
+        v = flat.v ? 1.0 : 0.0;
+        settled = (flat.v != call.v || flat.m != call.m) ? 2 : (flat.m >= kDecide ? 1 : 0);
+    } else if (kind == 1) {
+        const ValM<float> dv = capsule_box_call<float, RobustPol>(nm, A, B, r, X);
+        const float tol = nm.maxd;
+        float d = dv.v, m = dv.m;
+        const float band = dv.ia * (kDecide / kBand);
+        m = fminf(m, fabsf(d - tol) * band);
+        if (d != 0.f) m = fminf(m, fabsf(d > tol ? nm.maxd : d) * band);
+        if (d > tol) d = nm.maxd;
+        v = (double)d;
+        settled = m >= kDecide ? 1 : 0;
+    } else {
+        RobustPol pol;
+        v = (double)seg_seg(pol, nm, A, B, X, X + 3).v;
+        settled = pol.m >= kDecide ? 1 : 0;
+    }
+    P.value[i] = v;
+    P.settled[i] = settled;
+}
+
+cudaError_t launch_probe_fp32(const ProbeParams &p, cudaStream_t st) {
+    const unsigned grid = (unsigned)((p.n + 127) / 128);
+    if (grid == 0) return cudaSuccess;
+    k_probe_fp32<<<grid, 128, 0, st>>>(p);
+    return cudaGetLastError();
+}
+
 }  // namespace rpm

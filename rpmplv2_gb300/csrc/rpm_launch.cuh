@@ -71,4 +71,23 @@ cudaError_t launch_skeleton(int mode, const DevRobot *rb, int D, const float *q,
 
 cudaError_t launch_wait_probe(int32_t *status, unsigned limit, cudaStream_t st);
 
+// Primitive probe: the device trees on single (segment, box) or (segment,
+// segment) cases.  kind[i]: 0 collisionCapsuleToBox, 1 distanceCapsuleToBox,
+// 2 distanceLineSegToLineSeg.  x holds the AABB (kinds 0, 1) or C, D (kind 2).
+struct ProbeParams {
+    const int32_t *kind;
+    const float *a, *b, *x, *r;
+    int64_t n;
+    Num<double> nmd;
+    Num<float> nmf;
+    double *value;
+    uint8_t *settled;   // FP32 pass: 1 settled, 0 left to the FP64 recheck, 2 tree variants disagree
+};
+// MODE 0: FP64 trees (with only_unsettled, only where settled[i] == 0, as
+// the FP64 recheck does); MODE 1: the reference's FP32 numerics.
+cudaError_t launch_probe_exact(int mode, const ProbeParams &p, bool only_unsettled, cudaStream_t st);
+// The FP32 pass's trees with margins (contracted multiply-adds, as the bulk
+// kernels are compiled).
+cudaError_t launch_probe_fp32(const ProbeParams &p, cudaStream_t st);
+
 }  // namespace rpm

@@ -226,9 +226,12 @@ struct NearParams {
     float *profile;          // [C][L]
     float *nearest;          // [C][n][6][L] (output of the first kernel, input of the second)
     uint8_t *flag;           // [C] nearest points valid / underestimation complete
+    double *margin_valid;    // [C] decision margins (rpm_decision_margins)
+    double *margin_dist;     // [C]
 };
 
 cudaError_t launch_distance_nearest(int mode, const NearParams &p, cudaStream_t st);
 cudaError_t launch_distance_underest(int mode, const NearParams &p, cudaStream_t st);
+cudaError_t launch_decision_margins(const NearParams &p, cudaStream_t st);
 
 }  // namespace rpm

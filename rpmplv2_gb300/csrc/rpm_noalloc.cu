@@ -1,26 +1,31 @@
 // rpm_noalloc.cu -- rpm_check_configs_noalloc: the FP32 + FP64-recheck check
 // for callers that must not allocate device memory.
 //
-// Who needs it: code that runs where cudaMalloc is off limits -- inside a
-// CUDA-graph capture owned by someone else, in a real-time control loop that
-// forbids allocator calls (and their implicit synchronisation) after start-up,
-// or inside a host framework that owns all device memory itself.  Such a caller
+// Who needs it: code that runs where cudaMalloc is off limits -- a real-time
+// control loop that forbids allocator calls (and their implicit
+// synchronisation) after start-up, or a host framework that owns all device
+// memory itself and hands out only the buffers it manages.  Such a caller
 // already holds its inputs and outputs in device memory; this entry point
 // needs nothing else.
 //
 // Scratch: the FP32 pass lists the configurations it could not settle for the
 // FP64 recheck.  Here that list lives in a file-scope static __device__ array
-// (g_noalloc_scratch, 65,536 entries plus a counter and a status word, about
-// 512 KB), which every GPU that loads this library holds until the process
-// exits.  Host code cannot use the array's name as a device address, so the
-// first call on each device looks the address up with cudaGetSymbolAddress
-// (with that device current) and caches it; make that first call before any
-// stream capture.  Every call shares the one array and clears its counter and
-// status word first, so calls that overlap on the GPU (different streams, or
-// host threads) race on it and must be serialised by the caller.
+// (g_noalloc_scratch, 65,536 entries plus a counter, about 512 KB), which
+// every GPU that loads this library holds until the process exits.  Host code
+// cannot use the array's name as a device address, so the first call on each
+// device looks the address up with cudaGetSymbolAddress (with that device
+// current) and caches it with the device's current context; a call that finds
+// another context current (after cudaDeviceReset, or under a context the
+// caller made current through the driver API) looks it up again.  Make the
+// first call on a device before any stream capture.  Every call shares the one
+// array and clears its counter first, so calls that overlap on the GPU
+// (different streams, or host threads) race on it and must be serialised by
+// the caller.
 //
 // This translation unit is built with --fmad=false like rpm_exact.cu, so its
 // FP64 recheck rounds exactly as the FP64 form does.
+#include <cuda.h>   // CUcontext / CUresult types only; the driver is reached through the runtime
+
 #include <mutex>
 
 #include "rpm_check.cuh"
@@ -31,9 +36,8 @@ namespace rpm {
 constexpr int64_t kNoAllocMaxConfigs = 1 << 16;   // configurations per call
 constexpr int kNoAllocMaxDevices = 64;
 
-// [0, kNoAllocMaxConfigs): recheck list; [kNoAllocMaxConfigs]: counter;
-// [kNoAllocMaxConfigs + 1]: device status word.
-static __device__ __align__(256) uint64_t g_noalloc_scratch[kNoAllocMaxConfigs + 2];
+// [0, kNoAllocMaxConfigs): recheck list; [kNoAllocMaxConfigs]: counter.
+static __device__ __align__(256) uint64_t g_noalloc_scratch[kNoAllocMaxConfigs + 1];
 
 struct NoAllocParams {
     DevRobot rb;
@@ -105,6 +109,25 @@ __global__ void __launch_bounds__(kThreads) k_noalloc_recheck(const __grid_const
     }
 }
 
+// The calling thread's current driver context (nullptr if none is bound yet),
+// through the runtime's driver entry point so the library needs no link
+// against the driver.
+static void *current_context() {
+    typedef CUresult (*CtxGetCurrent)(CUcontext *);
+    static std::once_flag once;
+    static CtxGetCurrent fn = nullptr;
+    std::call_once(once, [] {
+        void *f = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<CtxGetCurrent>(f);
+    });
+    CUcontext c = nullptr;
+    if (!fn || fn(&c) != CUDA_SUCCESS) return nullptr;
+    return c;
+}
+
 }  // namespace rpm
 
 using namespace rpm;
@@ -127,16 +150,20 @@ extern "C" int rpm_check_configs_noalloc(const rpm_robot_desc *robot, const floa
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kNoAllocMaxDevices)
         return set_error(RPM_ERR_CUDA, "rpm_check_configs_noalloc: no usable current device");
-    // once per device, with that device current: the array's device address
+    // once per device (and again if the device's current context changed),
+    // with that device current: the array's device address
     static std::mutex mu;
     static uint64_t *addr[kNoAllocMaxDevices] = {nullptr};
+    static void *addr_ctx[kNoAllocMaxDevices] = {nullptr};
     {
         std::lock_guard<std::mutex> lk(mu);
-        if (!addr[dev]) {
+        void *cur = current_context();
+        if (!addr[dev] || !cur || cur != addr_ctx[dev]) {
             void *p = nullptr;
             const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
             if (e != cudaSuccess) return set_error(RPM_ERR_CUDA, cudaGetErrorString(e));
             addr[dev] = static_cast<uint64_t *>(p);
+            addr_ctx[dev] = current_context();   // bound by the lookup if it was not before
         }
     }
     P.scratch = addr[dev];
@@ -155,8 +182,8 @@ extern "C" int rpm_check_configs_noalloc(const rpm_robot_desc *robot, const floa
     P.nmd.eq = params->equality_threshold;
     P.nmd.maxd = params->max_distance;
     cudaStream_t st = (cudaStream_t)stream;
-    // the shared array keeps the previous call's contents: clear the counter and status word
-    if (cudaMemsetAsync(P.scratch + kNoAllocMaxConfigs, 0, 2 * sizeof(uint64_t), st) != cudaSuccess)
+    // the shared array keeps the previous call's contents: clear the counter
+    if (cudaMemsetAsync(P.scratch + kNoAllocMaxConfigs, 0, sizeof(uint64_t), st) != cudaSuccess)
         return set_error(RPM_ERR_CUDA, "rpm_check_configs_noalloc: clearing the scratch counter failed");
     if (num_configs == 0) return RPM_OK;
     int sms = 0;

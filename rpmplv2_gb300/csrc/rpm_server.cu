@@ -242,18 +242,22 @@ DevBufs layout(rpm_server *srv, const Req *q) {
 // Launch one batch on a reserved slot: copies in, the checks, copies out.
 // Called by the worker without srv->mu (the batch and the slot are its own);
 // takes ctx->mu for the enqueue.
-int launch_batch(rpm_server *srv, Slot &slot, const std::vector<Req *> &batch) {
+// versions[k] receives the scene version batch[k] reads.
+int launch_batch(rpm_server *srv, Slot &slot, const std::vector<Req *> &batch, std::vector<uint64_t> &versions) {
     rpm_ctx *ctx = srv->ctx;
     std::lock_guard<std::mutex> lk(ctx->mu);
     if (set_device(ctx)) return RPM_ERR_CUDA;
     std::vector<SegReq> segs;
     std::vector<EdgeReq> edges;
     int64_t n_edges = 0;
-    for (Req *q : batch) {
+    versions.assign(batch.size(), 0);
+    for (size_t k = 0; k < batch.size(); ++k) {
+        Req *q = batch[k];
         const DevBufs d = layout(srv, q);
         const size_t n = (size_t)q->r.count;
         SceneRec *s = find_scene(ctx, q->r.scene_id);
         if (!s) return fail(RPM_ERR_INVALID, "unknown scene %d", q->r.scene_id);
+        versions[k] = s->version;   // the launch reads s->cur, made current with this version
         if (q->r.kind == RPM_REQ_EDGES) {
             CK(cudaMemcpyAsync(d.q1, q->r.q1_host, n * q->D * sizeof(float), cudaMemcpyHostToDevice, slot.st));
             CK(cudaMemcpyAsync(d.q2, q->r.q2_host, n * q->D * sizeof(float), cudaMemcpyHostToDevice, slot.st));
@@ -382,11 +386,14 @@ void worker_loop(rpm_server *srv) {
             sl.busy = true;   // reserved: only this thread touches the slot
             const double t = now_s();
             lk.unlock();      // submissions and polls proceed while the batch is enqueued
-            const int rc = launch_batch(srv, sl, batch);
+            std::vector<uint64_t> versions;
+            const int rc = launch_batch(srv, sl, batch, versions);
             lk.lock();
-            for (Req *q : batch) {
+            for (size_t k = 0; k < batch.size(); ++k) {
+                Req *q = batch[k];
                 q->t.t_launch = t;
                 q->t.batch_size = (int32_t)batch.size();
+                q->t.scene_version = k < versions.size() ? versions[k] : 0;
             }
             if (rc) {
                 // work already queued for the batch may still use its memory: let it finish first

@@ -29,7 +29,8 @@ class Request(ctypes.Structure):
 
 class Timing(ctypes.Structure):
     _fields_ = [("status", ctypes.c_int32), ("batch_size", ctypes.c_int32), ("t_submit", ctypes.c_double),
-                ("t_admit", ctypes.c_double), ("t_launch", ctypes.c_double), ("t_done", ctypes.c_double)]
+                ("t_admit", ctypes.c_double), ("t_launch", ctypes.c_double), ("t_done", ctypes.c_double),
+                ("scene_version", ctypes.c_uint64)]
 
 
 class Motion(ctypes.Structure):

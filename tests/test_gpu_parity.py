@@ -109,3 +109,41 @@ def test_host_buffers_pinned_and_pageable(engine, prec):
                                       ds.ctypes.data, None) == 0
     assert np.array_equal(vs, v_dev.cpu().numpy()) and np.array_equal(ds.view(np.uint64), d_dev.cpu().numpy().view(np.uint64))
     engine.destroy_scene(sid)
+
+
+BAND_M = 1e-5   # FP32 rounding band of a decision margin (metres over error amplification)
+
+
+@pytest.mark.parametrize("prec", ["fp64", "fp32_recheck"])
+def test_flips_against_reference_numerics(engine, prec):
+    """Flip accounting against ref32, the reference's own FP32 numerics: the
+    FP64-pinned forms may answer differently from it only where the FP64
+    decision margin (rpm_decision_margins) lies inside the FP32 rounding
+    band; isValid flips and distance differences above 1e-5 m are counted and
+    each must have such a margin.  The reference-numerics form has none."""
+    robot, scene, q = scenes.xarm6_workload(262144, seed=31)
+    v, d, _, _ = run_gpu(engine, robot, scene, q, prec, profile=False)
+    rv, rd, _ = O.check_configs(robot, scene, q, prec="ref32", want=("valid", "dist"))
+    sid = engine.create_scene(engine.upload_robot(robot), scene)
+    C = q.shape[0]
+    mv = torch.zeros(C, dtype=torch.float64, device="cuda")
+    md = torch.zeros(C, dtype=torch.float64, device="cuda")
+    engine.decision_margins(sid, torch.from_numpy(q).cuda(), mv, md)
+    engine.sync()
+    engine.destroy_scene(sid)
+    mv, md = mv.cpu().numpy(), md.cpu().numpy()
+    flips = np.nonzero(v != rv)[0]
+    dflips = np.nonzero(np.abs(d - rd) > 1e-5)[0]
+    print("%s vs ref32: %d isValid flips, %d distance differences > 1e-5 m; %d configurations inside the band"
+          % (prec, flips.size, dflips.size, int((mv < BAND_M).sum())))
+    assert np.all(mv[flips] < BAND_M), mv[flips]
+    assert np.all(md[dflips] < BAND_M), md[dflips]
+    # the band is narrow: almost every configuration is decided far from it
+    assert (mv < BAND_M).sum() < 1e-3 * C
+
+
+def test_reference_numerics_form_has_no_flips(engine):
+    robot, scene, q = scenes.xarm6_workload(262144, seed=31)
+    v, d, _, _ = run_gpu(engine, robot, scene, q, "fp32_ref", profile=False)
+    rv, rd, _ = O.check_configs(robot, scene, q, prec="ref32", want=("valid", "dist"))
+    assert np.array_equal(v, rv) and np.array_equal(d.view(np.uint64), rd.view(np.uint64))

@@ -80,4 +80,80 @@ def test_moving_obstacles_replay(engine):
     v1 = ctypes.c_uint64()
     lib.rpm_scene_info(engine.ctx, sid, None, None, ctypes.byref(v1))
     assert v1.value - v0.value >= 20   # ~1 ms updates during a >= 100 ms replay
+    assert all(v0.value <= t.scene_version <= v1.value for t, m in zip(timings, wl["meta"])
+               if wl["scene_ids"][m[3]] == sid)
     srv.close()
+
+
+def test_results_under_moving_obstacles_match_the_oracle(engine):
+    """Requests submitted while their scenes' boxes move (DRGBT replanning with
+    dynamic obstacles): every result equals the oracle on the scene version the
+    request read (rpm_request_timing.scene_version), with versions changing
+    between and during the requests' batches."""
+    import time
+    import torch  # noqa: F401  (pinned buffers)
+    from oracle import oracle as O
+    from rpmplv2_gb300 import scenes, serve
+    rng = np.random.default_rng(44)
+    srv = serve.Server(engine, num_slots=4)
+    setups = []
+    for name, n in (("xarm6", 50), ("spatial_10dof", 120), ("planar_2dof", 12)):
+        robot = serve.make_robot(name)
+        sc = serve._scene_for(robot, rng, n)
+        first = 1 if name == "xarm6" else 0
+        mov = rng.choice(np.arange(first, sc.n), size=5, replace=False)
+        sc.flags[mov] |= scenes.RPM_OBS_DYNAMIC
+        sid = engine.create_scene(engine.upload_robot(robot), sc)
+        vel = rng.normal(size=(5, 3)).astype(np.float32)
+        vel *= (rng.uniform(0.2, 1.6, (5, 1)) / np.linalg.norm(vel, axis=1, keepdims=True)).astype(np.float32)
+        ver = ctypes.c_uint64()
+        engine.lib.rpm_scene_info(engine.ctx, sid, None, None, ctypes.byref(ver))
+        setups.append({"robot": robot, "scene": sc, "sid": sid, "mov": mov, "vel": vel,
+                       "versions": {ver.value: sc.aabb.copy()}})
+    pending = []
+    for rnd in range(40):
+        for st in setups:   # every 1 ms of planner time the dynamic boxes move
+            moved = st["scene"].aabb[st["mov"]] + np.tile(st["vel"] * 0.001, 2)
+            st["scene"].aabb[st["mov"]] = moved
+            ver = engine.update_scene(st["sid"], st["mov"], moved)
+            st["versions"][ver] = st["scene"].aabb.copy()
+        for _ in range(3):
+            st = setups[int(rng.integers(len(setups)))]
+            D = st["robot"].num_dofs
+            kind = int(rng.integers(3))
+            cnt = int(rng.integers(1, 512))
+            q = serve.pinned((cnt, D), np.float32)
+            q[:] = rng.uniform(-np.pi, np.pi, (cnt, D))
+            v = serve.pinned(cnt, np.uint8)
+            if kind == 2:
+                q2 = serve.pinned((cnt, D), np.float32)
+                q2[:] = q + rng.uniform(-0.5, 0.5, (cnt, D))
+                k = serve.pinned(cnt, np.int32)
+                req = serve.edges_request(st["sid"], q, q2, v, k, step=0.05)
+                pending.append((srv.submit(req), st, kind, (q, q2, v, k)))
+            else:
+                d = serve.pinned(cnt, np.float64) if kind == 1 else None
+                req = serve.configs_request(st["sid"], q, v, d)
+                pending.append((srv.submit(req), st, kind, (q, v, d)))
+        time.sleep(0.0005)
+    seen = set()
+    for ticket, st, kind, bufs in pending:
+        t = srv.wait(ticket)
+        assert t.status == 0
+        assert t.scene_version in st["versions"], "request read an unknown version"
+        seen.add((st["sid"], t.scene_version))
+        scene = scenes.Scene(st["versions"][t.scene_version], st["scene"].tol, st["scene"].flags)
+        if kind == 2:
+            q, q2, v, k = bufs
+            rv, rk = O.check_edges(st["robot"], scene, q, q2, step=np.float32(0.05), prec="ref64")
+            assert np.array_equal(v, rv) and np.array_equal(k, rk)
+        else:
+            q, v, d = bufs
+            rv, rd, _ = O.check_configs(st["robot"], scene, q, prec="ref64", want=("valid", "dist"))
+            assert np.array_equal(v, rv)
+            if d is not None:
+                assert np.abs(d - rd).max() <= 1e-5
+    assert len(seen) >= 10   # requests read many different versions
+    srv.close()
+    for st in setups:
+        engine.destroy_scene(st["sid"])

@@ -98,3 +98,35 @@ def test_primitives_against_reference_source():
         assert bool(rhas.value) == ohas
         if ohas:
             assert rpts.tobytes() == opts.tobytes(), (it, rpts, opts)
+
+
+def test_adversarial_primitives_against_fixture():
+    """The directed edge cases (parallel, degenerate, on-plane, snap-distance):
+    the oracle reproduces its committed answers in both numerics, and its FP32
+    restatement equals the reference's own source wherever that source is
+    defined (adv_undefined marks its uninitialised-matrix reads)."""
+    import ctypes
+    A, B, X, r, kind = (G[k] for k in ("adv_A", "adv_B", "adv_X", "adv_r", "adv_kind"))
+    fp = ctypes.POINTER(ctypes.c_float)
+    P = lambda a: np.ascontiguousarray(a).ctypes.data_as(fp)
+    L = O.lib()
+    n = len(r)
+    v32, v64, und = np.zeros(n), np.zeros(n), np.zeros(n, np.uint8)
+    O.undefined_hits()
+    for i in range(n):
+        if kind[i] == 0:
+            v32[i] = O.prim_collision(A[i], B[i], r[i], X[i], "ref32")
+            v64[i] = O.prim_collision(A[i], B[i], r[i], X[i], "ref64")
+        elif kind[i] == 1:
+            v32[i] = O.prim_distance(A[i], B[i], r[i], X[i], "ref32")[0]
+            v64[i] = O.prim_distance(A[i], B[i], r[i], X[i], "ref64")[0]
+            und[i] = 1 if O.undefined_hits() else 0
+        else:
+            v32[i] = L.orc_prim_segseg(P(A[i]), P(B[i]), P(X[i][:3]), P(X[i][3:]), 32, None)
+            v64[i] = L.orc_prim_segseg(P(A[i]), P(B[i]), P(X[i][:3]), P(X[i][3:]), 64, None)
+    nan_eq = lambda a, b: np.all((np.isnan(a) & np.isnan(b)) | (a == b))
+    assert nan_eq(v32, G["adv_ref32"]) and nan_eq(v64, G["adv_ref64"])
+    assert np.array_equal(und, G["adv_undefined"])
+    if "adv_reference" in G:
+        d = und == 0
+        assert nan_eq(v32[d].astype(np.float32), G["adv_reference"][d].astype(np.float32))
