@@ -120,6 +120,17 @@ int rpm_ctx_set_params(rpm_ctx *ctx, const rpm_params *params);
  * Replaces the robot construction from URDF (xArm6.cpp:7-76, Planar2DOF.cpp:7-64,
  * Spatial10DOF.cpp:5-9) plus AbstractRobot::setCapsulesRadius / setGroundIncluded. */
 int rpm_robot_upload(rpm_ctx *ctx, const rpm_robot_desc *desc, int32_t *robot_id);
+/* The kinematic table of one of the reference's robots by its type name, as
+ * robots::AbstractRobot::getType() returns it (the URDF robot name): "2dof",
+ * "10dof" (also "planar_2dof", "planar_10dof"), "spatial_10dof",
+ * "spatial_14dof", "spatial_18dof", "spatial_22dof", "xarm6" -- the joint
+ * origins, axes and limits of data/<robot>/<robot>.urdf as kdl_parser chains
+ * them (Planar2DOF.cpp:7-64, Spatial10DOF.cpp:5-9, xArm6.cpp:7-76).  Capsule
+ * radii default to the URDF link boxes' dim.y / 2 (0.025; 0 for xarm6, whose
+ * radii come from the scenario), ground_included and gripper_length to 0: a
+ * caller overrides them from its robot (setCapsulesRadius, setGroundIncluded,
+ * setGripperLength).  Host only. */
+int rpm_robot_builtin(const char *type, rpm_robot_desc *out);
 
 /* ---- scenes (device-resident obstacle sets) ----------------------------------
  * Replaces env::Environment's object list as the hot path sees it

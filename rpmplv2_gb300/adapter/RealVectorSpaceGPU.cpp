@@ -3,6 +3,7 @@
 
 #include <cuda_runtime.h>
 
+#include <cstring>
 #include <stdexcept>
 #include <string>
 
@@ -18,25 +19,118 @@ void RealVectorSpaceGPU::check(int rc) const {
     if (rc != RPM_OK) throw std::runtime_error(std::string("rpm: ") + rpm_last_error_string());
 }
 
+rpm_robot_desc RealVectorSpaceGPU::describe(const robots::AbstractRobot &robot) {
+    rpm_robot_desc d;
+    if (rpm_robot_builtin(robot.getType().c_str(), &d) != RPM_OK)
+        throw std::invalid_argument(std::string("RealVectorSpaceGPU: ") + rpm_last_error_string());
+    if (robot.getNumDOFs() != (size_t)d.num_dofs)
+        throw std::invalid_argument("RealVectorSpaceGPU: the robot's DOF count differs from its type's URDF");
+    for (int i = 0; i < d.num_dofs; ++i) d.capsule_radius[i] = robot.getCapsuleRadius((size_t)i);
+    d.ground_included = (int32_t)robot.getGroundIncluded();
+    d.gripper_length = robot.getGripperLength();
+    const auto &lim = robot.getLimits();
+    for (int i = 0; i < d.num_dofs && i < (int)lim.size(); ++i) {
+        d.limits[i][0] = lim[i].first;
+        d.limits[i][1] = lim[i].second;
+    }
+    return d;
+}
+
+// The objects as RealVectorSpace.cpp:285-295 and :344-346 read them: the fcl
+// world AABB (min_, max_), the "ground" label for the ground rule, the
+// "dynamic_obstacle" label for moving boxes, and Object::getMinDistTol.
+RealVectorSpaceGPU::Obstacles RealVectorSpaceGPU::obstaclesOf(const env::Environment &env) {
+    Obstacles o;
+    const size_t n = env.getNumObjects();
+    o.aabb.resize(6 * n);
+    o.min_dist_tol.resize(n);
+    o.flags.resize(n);
+    for (size_t j = 0; j < n; ++j) {
+        const auto &box = env.getCollObject(j)->getAABB();
+        for (int k = 0; k < 3; ++k) {
+            o.aabb[6 * j + k] = box.min_[k];
+            o.aabb[6 * j + 3 + k] = box.max_[k];
+        }
+        const std::string &label = env.getObject(j)->getLabel();
+        o.min_dist_tol[j] = env.getObject(j)->getMinDistTol();
+        o.flags[j] = (uint8_t)((label == "ground" ? RPM_OBS_GROUND : 0u) | (label == "dynamic_obstacle" ? RPM_OBS_DYNAMIC : 0u));
+    }
+    return o;
+}
+
+RealVectorSpaceGPU::RealVectorSpaceGPU(size_t num_dimensions, const std::shared_ptr<robots::AbstractRobot> robot,
+                                       const std::shared_ptr<env::Environment> env, int32_t precision, int device,
+                                       int32_t num_interpolation_validity_checks)
+    : RealVectorSpace(num_dimensions, robot, env), prec_(precision), checks_(num_interpolation_validity_checks) {
+    if (!robot || !env) throw std::invalid_argument("RealVectorSpaceGPU: robot and environment are required");
+    const rpm_robot_desc desc = describe(*robot);
+    if ((size_t)desc.num_dofs != num_dimensions)
+        throw std::invalid_argument("RealVectorSpaceGPU: num_dimensions differs from the robot's DOF count");
+    init(desc, obstaclesOf(*env), device);
+}
+
 RealVectorSpaceGPU::RealVectorSpaceGPU(const rpm_robot_desc &robot, const Obstacles &obstacles, int32_t precision,
                                        int device, int32_t num_interpolation_validity_checks)
     : RealVectorSpace((size_t)robot.num_dofs), prec_(precision), checks_(num_interpolation_validity_checks) {
-    const int n = (int)(obstacles.aabb.size() / 6);
-    if (obstacles.aabb.size() != 6 * (size_t)n || (!obstacles.min_dist_tol.empty() && obstacles.min_dist_tol.size() != (size_t)n) ||
-        (!obstacles.flags.empty() && obstacles.flags.size() != (size_t)n))
-        throw std::invalid_argument("RealVectorSpaceGPU: obstacle arrays of inconsistent sizes");
+    init(robot, obstacles, device);
+}
+
+void RealVectorSpaceGPU::init(const rpm_robot_desc &robot, const Obstacles &obstacles, int device) {
     check(rpm_ctx_create(device, &ctx_));
     check(rpm_robot_upload(ctx_, &robot, &robot_));
-    check(rpm_scene_create(ctx_, robot_, n ? obstacles.aabb.data() : nullptr,
-                           obstacles.min_dist_tol.empty() ? nullptr : obstacles.min_dist_tol.data(),
-                           obstacles.flags.empty() ? nullptr : obstacles.flags.data(), n, &scene_));
     D_ = robot.num_dofs;
-    n_ = n;
+    createScene(obstacles);
     cudaStream_t st;
     cuda_check(cudaSetDevice(device), "cudaSetDevice");
     cuda_check(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking), "cudaStreamCreate");
     stream_ = st;
     reserve(1);
+}
+
+void RealVectorSpaceGPU::createScene(const Obstacles &obstacles) {
+    const int n = (int)(obstacles.aabb.size() / 6);
+    if (obstacles.aabb.size() != 6 * (size_t)n || (!obstacles.min_dist_tol.empty() && obstacles.min_dist_tol.size() != (size_t)n) ||
+        (!obstacles.flags.empty() && obstacles.flags.size() != (size_t)n))
+        throw std::invalid_argument("RealVectorSpaceGPU: obstacle arrays of inconsistent sizes");
+    if (scene_ >= 0) {
+        check(rpm_sync(ctx_, stream_));   // checks still reading the old scene finish first
+        check(rpm_scene_destroy(ctx_, scene_));
+        scene_ = -1;
+    }
+    check(rpm_scene_create(ctx_, robot_, n ? obstacles.aabb.data() : nullptr,
+                           obstacles.min_dist_tol.empty() ? nullptr : obstacles.min_dist_tol.data(),
+                           obstacles.flags.empty() ? nullptr : obstacles.flags.data(), n, &scene_));
+    check(rpm_scene_info(ctx_, scene_, nullptr, nullptr, &version_));
+    const bool grew = n > n_;
+    n_ = n;
+    scene_obs_ = obstacles;
+    if (grew && cap_ > 0) {   // the nearest-point buffer is sized by the obstacle count
+        const size_t c = cap_;
+        cap_ = 0;
+        reserve(c);
+    }
+}
+
+uint64_t RealVectorSpaceGPU::syncEnvironment() {
+    if (!env) return version_;
+    const Obstacles cur = obstaclesOf(*env);
+    const size_t n = cur.min_dist_tol.size();
+    if (n != (size_t)n_ || cur.min_dist_tol != scene_obs_.min_dist_tol || cur.flags != scene_obs_.flags) {
+        createScene(cur);
+        return version_;
+    }
+    std::vector<int32_t> idx;
+    std::vector<float> rows;
+    for (size_t j = 0; j < n; ++j) {
+        if (std::memcmp(&cur.aabb[6 * j], &scene_obs_.aabb[6 * j], 6 * sizeof(float)) == 0) continue;
+        idx.push_back((int32_t)j);
+        rows.insert(rows.end(), cur.aabb.begin() + 6 * j, cur.aabb.begin() + 6 * (j + 1));
+    }
+    if (!idx.empty()) {
+        check(rpm_scene_update(ctx_, scene_, idx.data(), rows.data(), (int32_t)idx.size(), &version_));
+        scene_obs_.aabb = cur.aabb;
+    }
+    return version_;
 }
 
 RealVectorSpaceGPU::~RealVectorSpaceGPU() {
@@ -86,6 +180,7 @@ bool RealVectorSpaceGPU::isValid(const std::shared_ptr<base::State> q1, const st
 // otherwise).
 float RealVectorSpaceGPU::computeDistance(const std::shared_ptr<base::State> q, bool compute_again) {
     if (!compute_again && q->getDistance() > 0 && q->getIsRealDistance()) return q->getDistance();
+    syncEnvironment();
     upload({q}, dq_);
     cudaStream_t st = (cudaStream_t)stream_;
     const int32_t form = prec_ == RPM_PREC_FP32_REF ? RPM_PREC_FP32_REF : RPM_PREC_FP64;
@@ -138,6 +233,7 @@ float RealVectorSpaceGPU::computeDistanceUnderestimation(const std::shared_ptr<b
         for (int k = 0; k < 6; ++k)
             for (int i = 0; i < D_; ++i) near[((size_t)j * 6 + k) * D_ + i] = m(k, i);
     }
+    syncEnvironment();
     cudaStream_t st = (cudaStream_t)stream_;
     upload({q}, dq_);
     if (!near.empty())
@@ -163,6 +259,7 @@ float RealVectorSpaceGPU::computeDistanceUnderestimation(const std::shared_ptr<b
 std::vector<bool> RealVectorSpaceGPU::isValidBatch(const std::vector<std::shared_ptr<base::State>> &qs) {
     std::vector<bool> out(qs.size());
     if (qs.empty()) return out;
+    syncEnvironment();
     reserve(qs.size());
     upload(qs, dq_);
     cudaStream_t st = (cudaStream_t)stream_;
@@ -177,6 +274,7 @@ std::vector<bool> RealVectorSpaceGPU::isValidBatch(const std::vector<std::shared
 std::vector<float> RealVectorSpaceGPU::computeDistanceBatch(const std::vector<std::shared_ptr<base::State>> &qs) {
     std::vector<float> out(qs.size());
     if (qs.empty()) return out;
+    syncEnvironment();
     reserve(qs.size());
     upload(qs, dq_);
     cudaStream_t st = (cudaStream_t)stream_;
@@ -202,6 +300,7 @@ std::vector<bool> RealVectorSpaceGPU::isValidEdgesBatch(const std::vector<std::s
     if (q1s.size() != q2s.size()) throw std::invalid_argument("RealVectorSpaceGPU: edge lists of different lengths");
     std::vector<bool> out(q1s.size());
     if (q1s.empty()) return out;
+    syncEnvironment();
     reserve(q1s.size());
     upload(q1s, dq_);
     upload(q2s, dq2_);
@@ -216,9 +315,12 @@ std::vector<bool> RealVectorSpaceGPU::isValidEdgesBatch(const std::vector<std::s
 
 uint64_t RealVectorSpaceGPU::updateObstacles(const std::vector<int32_t> &idx, const std::vector<float> &aabb) {
     if (aabb.size() != 6 * idx.size()) throw std::invalid_argument("RealVectorSpaceGPU: 6 AABB values per obstacle");
-    uint64_t version = 0;
-    check(rpm_scene_update(ctx_, scene_, idx.data(), aabb.data(), (int32_t)idx.size(), &version));
-    return version;
+    for (int32_t j : idx)
+        if (j < 0 || j >= n_) throw std::invalid_argument("RealVectorSpaceGPU: obstacle index out of range");
+    check(rpm_scene_update(ctx_, scene_, idx.data(), aabb.data(), (int32_t)idx.size(), &version_));
+    for (size_t k = 0; k < idx.size(); ++k)
+        std::memcpy(&scene_obs_.aabb[6 * (size_t)idx[k]], &aabb[6 * k], 6 * sizeof(float));
+    return version_;
 }
 
 }  // namespace base

@@ -15,11 +15,22 @@
 // the virtuals and need no change.  The space owns one engine context, one
 // robot, one device-resident scene and a small set of device staging buffers,
 // and runs every call on its own stream.
+//
+// Built with the reference's constructor (robot and environment), the space
+// keeps StateSpace::robot and StateSpace::env set, as planners expect
+// (DRGBT.cpp:15, 31; MotionValidity.cpp:12-15), and follows the environment:
+// before every check it compares each object's fcl world AABB with the device
+// scene and sends what moved as one incremental update, so a planner that
+// moves obstacles in place (env->updateEnvironment(dt) before ss->isValid(q),
+// MotionValidity.cpp:39-42) is checked against the moved scene.  Objects added
+// or removed, or a label or min_dist_tol changed, rebuild the scene.
 #pragma once
 #include <cstdint>
 #include <memory>
 #include <vector>
 
+#include <environments/Environment.h>
+#include <robots/AbstractRobot.h>
 #include <state_spaces/real_vector_space/RealVectorSpace.h>
 
 #include "rpm_gpu.h"
@@ -36,8 +47,18 @@ public:
         std::vector<uint8_t> flags;
     };
 
-    // 'robot' is the kinematic table the reference's robot builds from its
-    // URDF (rpm_robot_desc); 'precision' is an RPM_PREC_* form for the checks.
+    // The reference's constructor (RealVectorSpace.h:21-22): the robot is
+    // described by its type's URDF table (rpm_robot_builtin) with its own
+    // capsule radii, ground rule and gripper length; the obstacles are the
+    // environment's objects as RealVectorSpace.cpp:285-295 reads them (fcl
+    // world AABB, label "ground" / "dynamic_obstacle", min_dist_tol).
+    // 'precision' is an RPM_PREC_* form for the checks.
+    RealVectorSpaceGPU(size_t num_dimensions, const std::shared_ptr<robots::AbstractRobot> robot,
+                       const std::shared_ptr<env::Environment> env, int32_t precision = RPM_PREC_FP32_RECHECK,
+                       int device = 0, int32_t num_interpolation_validity_checks = 10);
+    // Without robot and environment objects: 'robot' is the kinematic table
+    // the reference's robot builds from its URDF (rpm_robot_desc), and the
+    // obstacles change only through updateObstacles.
     RealVectorSpaceGPU(const rpm_robot_desc &robot, const Obstacles &obstacles,
                        int32_t precision = RPM_PREC_FP32_RECHECK, int device = 0,
                        int32_t num_interpolation_validity_checks = 10);
@@ -62,10 +83,21 @@ public:
     // obstacles 'idx' (m x 6); returns the scene's new version.
     uint64_t updateObstacles(const std::vector<int32_t> &idx, const std::vector<float> &aabb);
 
+    // Bring the device scene up to date with 'env' (every check does this
+    // first); returns the scene's version.  No-op without an environment.
+    uint64_t syncEnvironment();
+
+    // The descriptor and obstacle arrays the constructor derives from the
+    // reference's robot and environment objects.
+    static rpm_robot_desc describe(const robots::AbstractRobot &robot);
+    static Obstacles obstaclesOf(const env::Environment &env);
+
     inline rpm_ctx *context() const { return ctx_; }
     inline int32_t sceneId() const { return scene_; }
 
 private:
+    void init(const rpm_robot_desc &robot, const Obstacles &obstacles, int device);
+    void createScene(const Obstacles &obstacles);
     void reserve(size_t configs);
     void upload(const std::vector<std::shared_ptr<base::State>> &qs, float *dst);
     void check(int rc) const;   // throws std::runtime_error with rpm_last_error_string()
@@ -73,6 +105,8 @@ private:
     rpm_ctx *ctx_ = nullptr;
     int32_t robot_ = -1, scene_ = -1, prec_ = RPM_PREC_FP32_RECHECK, checks_ = 10;
     int D_ = 0, n_ = 0;
+    Obstacles scene_obs_;       // what the device scene holds (syncEnvironment compares against it)
+    uint64_t version_ = 0;
     void *stream_ = nullptr;
     size_t cap_ = 0;
     float *dq_ = nullptr, *dq2_ = nullptr, *dprof_ = nullptr, *dnear_ = nullptr;

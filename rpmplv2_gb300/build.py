@@ -55,10 +55,13 @@ def build_adapter(force=False):
     """The C++ RealVectorSpaceGPU adapter as librpm_adapter.so (host code on the C ABI)."""
     src = os.path.join(ADAPTER_DIR, "RealVectorSpaceGPU.cpp")
     deps = [src, os.path.join(ADAPTER_DIR, "RealVectorSpaceGPU.h"), LIB]
+    for d, _, files in os.walk(os.path.join(ADAPTER_DIR, "shim")):
+        deps += [os.path.join(d, f) for f in files]
     if not force and os.path.exists(ADAPTER_LIB) and all(os.path.getmtime(f) <= os.path.getmtime(ADAPTER_LIB) for f in deps):
         return ADAPTER_LIB
     tmp = ADAPTER_LIB + ".tmp%d" % os.getpid()
-    cmd = [nvcc(), "-std=c++17", "-O2", "-Xcompiler", "-fPIC", "-shared", "-x", "c++", src, *adapter_flags(),
+    cmd = [nvcc(), "-std=c++17", "-O2", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off", "-shared", "-x", "c++",
+           src, *adapter_flags(),
            "-L", OUT_DIR, "-lrpm_gb300", "-Xlinker", "-rpath=" + OUT_DIR, "-lcudart", "-o", tmp]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:

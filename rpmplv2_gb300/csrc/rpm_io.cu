@@ -12,6 +12,8 @@
 //                             (apps/test_drgbt_random_obstacles.cpp:125-151):
 //                             start, goal and the objects' positions and
 //                             velocities.
+//   rpm_robot_builtin         the kinematic table of each of the reference's
+//                             robots, by its type name (the URDF robot name).
 //
 // The files use a small part of YAML: block mappings and sequences by
 // indentation, "- key: value" items, one-line flow sequences of scalars,
@@ -314,6 +316,110 @@ int rpm_random_scenario_read(const char *path, int32_t num_obstacles, int32_t ru
         if (!o || !as_floats(o->get("pos"), pos + 3 * j, 3) || !as_floats(o->get("vel"), vel + 3 * j, 3))
             return fail(RPM_ERR_INVALID, "%s: run %d object_%d needs pos and vel", path, run, j);
     }
+    return RPM_OK;
+}
+
+// ---- the reference's robots ------------------------------------------------
+// Joint tables of the URDFs under data/ as kdl_parser chains them: joint k is
+// its fixed origin (xyz, rpy -> quaternion -> rotation) then a revolute joint
+// about one axis of its frame; entry D is the fixed tool joint.
+namespace {
+
+// URDF rpy (fixed axes x, y, z) -> unit quaternion -> row-major rotation.
+void rpy_rotation(double roll, double pitch, double yaw, double *m) {
+    const double sphi = std::sin(roll / 2.0), cphi = std::cos(roll / 2.0);
+    const double sthe = std::sin(pitch / 2.0), cthe = std::cos(pitch / 2.0);
+    const double spsi = std::sin(yaw / 2.0), cpsi = std::cos(yaw / 2.0);
+    double x = sphi * cthe * cpsi - cphi * sthe * spsi;
+    double y = cphi * sthe * cpsi + sphi * cthe * spsi;
+    double z = cphi * cthe * spsi - sphi * sthe * cpsi;
+    double w = cphi * cthe * cpsi + sphi * sthe * spsi;
+    const double n = std::sqrt(x * x + y * y + z * z + w * w);
+    x /= n; y /= n; z /= n; w /= n;
+    const double x2 = x * x, y2 = y * y, z2 = z * z, w2 = w * w;
+    const double r[9] = {w2 + x2 - y2 - z2, 2 * x * y - 2 * w * z, 2 * x * z + 2 * w * y,
+                         2 * x * y + 2 * w * z, w2 - x2 + y2 - z2, 2 * y * z - 2 * w * x,
+                         2 * x * z - 2 * w * y, 2 * y * z + 2 * w * x, w2 - x2 - y2 + z2};
+    std::memcpy(m, r, sizeof r);
+}
+
+void identity_rotation(double *m) {
+    const double r[9] = {1, 0, 0, 0, 1, 0, 0, 0, 1};
+    std::memcpy(m, r, sizeof r);
+}
+
+constexpr double kPiUrdf = 3.14159;                 // joint limits of the planar and spatial URDFs
+constexpr double kPiXarm = 3.14159265359;           // joint limits of xarm6.urdf
+
+}  // namespace
+
+extern "C" int rpm_robot_builtin(const char *type, rpm_robot_desc *out) {
+    if (!type || !out) return fail(RPM_ERR_INVALID, "NULL argument");
+    rpm_robot_desc d;
+    std::memset(&d, 0, sizeof d);
+    const std::string t(type);
+    if (t == "2dof" || t == "planar_2dof" || t == "10dof" || t == "planar_10dof") {
+        // data/planar_2dof/planar_2dof.urdf, data/planar_10dof/planar_10dof.urdf: z axes, links of 1 m / 0.2 m
+        const bool two = t == "2dof" || t == "planar_2dof";
+        const int D = two ? 2 : 10;
+        const double len = two ? 1.0 : 0.2;
+        d.kind = RPM_ROBOT_CHAIN;
+        d.num_dofs = D;
+        for (int k = 0; k <= D; ++k) {
+            d.origin_xyz[k][0] = k == 0 ? 0.0 : len;
+            identity_rotation(d.origin_rot[k]);
+        }
+        for (int k = 0; k < D; ++k) {
+            d.joint_axis[k] = 2;
+            d.limits[k][0] = (float)-kPiUrdf;
+            d.limits[k][1] = (float)kPiUrdf;
+            d.capsule_radius[k] = 0.025f;   // URDF link box dim.y / 2 (Planar2DOF.cpp:51)
+        }
+    } else if (t.rfind("spatial_", 0) == 0) {
+        // data/spatial_{10,14,18,22}dof/*.urdf: joint 1 about z at the base, the
+        // rest about x, 0.1 m then h apart; the tool h beyond the last joint
+        int D = 0;
+        double h = 0;
+        if (t == "spatial_10dof") { D = 10; h = 0.1; }
+        else if (t == "spatial_14dof") { D = 14; h = 0.0692; }
+        else if (t == "spatial_18dof") { D = 18; h = 0.05294; }
+        else if (t == "spatial_22dof") { D = 22; h = 0.042857; }
+        else return fail(RPM_ERR_INVALID, "unknown robot type '%s'", type);
+        d.kind = RPM_ROBOT_SPATIAL;
+        d.num_dofs = D;
+        for (int k = 0; k <= D; ++k) {
+            d.origin_xyz[k][2] = k == 0 ? 0.0 : (k == 1 ? 0.1 : h);
+            identity_rotation(d.origin_rot[k]);
+        }
+        for (int k = 0; k < D; ++k) {
+            d.joint_axis[k] = k == 0 ? 2 : 0;
+            d.limits[k][0] = (float)-kPiUrdf;
+            d.limits[k][1] = (float)kPiUrdf;
+            d.capsule_radius[k] = 0.025f;
+        }
+    } else if (t == "xarm6") {
+        // data/xarm6/xarm6.urdf joint1..joint6 (xyz, rpy as written, limits); the
+        // capsule radii, gripper and ground rule come from the scenario
+        static const double xyz[6][3] = {{0, 0, 0.267}, {0, 0, 0}, {0.0535, -0.2845, 0},
+                                         {0.0775, 0.3425, 0}, {0, 0, 0}, {0.076, 0.097, 0}};
+        static const double rpy[6][3] = {{0, 0, 0}, {-1.5708, 0, 0}, {0, 0, 0},
+                                         {-1.5708, 0, 0}, {1.5708, 0, 0}, {-1.5708, 0, 0}};
+        static const double lim[6][2] = {{-kPiXarm, kPiXarm}, {-2.059, 2.0944}, {-3.927, 0.19198},
+                                         {-kPiXarm, kPiXarm}, {-1.69297, kPiXarm}, {-kPiXarm, kPiXarm}};
+        d.kind = RPM_ROBOT_XARM6;
+        d.num_dofs = 6;
+        for (int k = 0; k < 6; ++k) {
+            for (int i = 0; i < 3; ++i) d.origin_xyz[k][i] = xyz[k][i];
+            rpy_rotation(rpy[k][0], rpy[k][1], rpy[k][2], d.origin_rot[k]);
+            d.joint_axis[k] = 2;
+            d.limits[k][0] = (float)lim[k][0];
+            d.limits[k][1] = (float)lim[k][1];
+        }
+        identity_rotation(d.origin_rot[6]);
+    } else {
+        return fail(RPM_ERR_INVALID, "unknown robot type '%s'", type);
+    }
+    *out = d;
     return RPM_OK;
 }
 

@@ -77,6 +77,7 @@ def load(build_if_missing=False):
     L.rpm_last_timing.argtypes = [_vp, _vp, ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_float)]
     L.rpm_probe_fp32_peak.argtypes = [_vp, ctypes.POINTER(ctypes.c_double)]
     L.rpm_probe_bounded_wait.argtypes = [_vp, ctypes.c_uint32]
+    L.rpm_robot_builtin.argtypes = [ctypes.c_char_p, _vp]
     L.rpm_decision_margins.argtypes = [_vp, _i32, _vp, _i64, _vp, _vp, _vp]
     L.rpm_probe_primitives.argtypes = [_vp, _i32, _vp, _vp, _vp, _vp, _vp, _i64, _vp, _vp, _vp]
     L.rpm_check_configs_noalloc.argtypes = [_vp, _vp, _vp, _vp, _i32, ctypes.POINTER(Params), _vp, _i64, _vp, _vp,
@@ -319,7 +320,7 @@ ABI_SYMBOLS = [
     "rpm_last_error_string", "rpm_version", "rpm_ctx_create", "rpm_ctx_destroy", "rpm_ctx_set_params",
     "rpm_robot_upload", "rpm_scene_create", "rpm_scene_update", "rpm_scene_destroy", "rpm_scene_info",
     "rpm_box_aabb", "rpm_check_configs", "rpm_check_configs_host", "rpm_skeleton", "rpm_last_stats", "rpm_sync",
-    "rpm_ctx_set_timing", "rpm_last_timing", "rpm_probe_fp32_peak", "rpm_probe_bounded_wait", "rpm_probe_primitives", "rpm_decision_margins", "rpm_check_configs_noalloc", "rpm_check_batch",
+    "rpm_ctx_set_timing", "rpm_last_timing", "rpm_probe_fp32_peak", "rpm_probe_bounded_wait", "rpm_probe_primitives", "rpm_decision_margins", "rpm_robot_builtin", "rpm_check_configs_noalloc", "rpm_check_batch",
     "rpm_check_edges", "rpm_check_edges_batch", "rpm_ctx_set_graphs", "rpm_autotune_edges", "rpm_set_edge_ctas", "rpm_ctx_set_layout",
     "rpm_distance_nearest", "rpm_distance_underestimation", "rpm_enclosing_radii", "rpm_extend_spines",
     "rpm_reached_states", "rpm_motion_validity", "rpm_scene_move_straight", "rpm_scenario_read", "rpm_random_scenario_read",

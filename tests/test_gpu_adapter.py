@@ -119,3 +119,83 @@ def test_adapter_fp32_recheck_booleans(driver):
     assert _bits(out["near"][sel], nnear[sel])
     ev, _ = O.check_edges(robot, scene, q1, q2, step=0.0, num_checks=10, prec="ref64")
     assert np.array_equal(out["edge"], ev) and np.array_equal(out["edge_b"], ev)
+
+
+@pytest.fixture(scope="module")
+def env_driver():
+    import torch
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    build.build()
+    exe = os.path.join(build.OUT_DIR, "adapter_env_driver")
+    cmd = [build.nvcc(), "-std=c++17", "-O2", "-Xcompiler", "-ffp-contract=off", "-x", "c++",
+           os.path.join(HERE, "adapter_env_driver.cpp"), *build.adapter_flags(), "-L", build.OUT_DIR,
+           "-lrpm_adapter", "-lrpm_gb300", "-Xlinker", "-rpath=" + build.OUT_DIR, "-lcudart", "-o", exe]
+    subprocess.run(cmd, check=True)
+    return exe
+
+
+def _quat(rng):
+    u = rng.normal(size=4)
+    return (u / np.linalg.norm(u)).astype(np.float32)
+
+
+@pytest.mark.parametrize("prec", [_abi.RPM_PREC_FP32_REF, _abi.RPM_PREC_FP32_RECHECK])
+def test_adapter_follows_the_environment(env_driver, prec):
+    """The reference's constructor RealVectorSpaceGPU(D, robot, env): the space
+    keeps ss->robot and ss->env, describes the robot by its type, reads the
+    obstacles as fcl world AABBs with their labels and tolerances, and follows
+    the environment as MotionValidity::check moves it in place
+    (env->updateEnvironment(dt), then ss->isValid(q) and computeDistance);
+    removing and adding an object rebuilds the scene.  Every step's results
+    equal the oracle on the AABBs the environment held at that step."""
+    rng = np.random.default_rng(91)
+    D, S, K, dt = 6, 6, 64, 0.05
+    robot = robots.xarm6(radius=0.05, gripper_length=0.1, ground_included=2)
+    recs = [[1.5, 1.5, 0.1, 0, 0, -0.05, 0, 0, 0, 1, 1, 0.05]]   # the ground (label, min_dist_tol 0.05)
+    for j in range(36):
+        c = np.array([0, 0, 0.267]) + rng.uniform(-0.8, 0.8, 3)
+        dim = rng.uniform(0.04, 0.12, 3)
+        quat = _quat(rng) if j % 6 == 0 else np.array([0, 0, 0, 1], np.float32)
+        code, last = (2, rng.uniform(0.5, 1.6)) if j % 7 == 0 else (0, 0.0)
+        recs.append([*dim, *c, *quat, code, last])
+    boxes = np.array(recs, np.float32)
+    extra = np.array([0.1, 0.1, 0.1, 0.3, -0.3, 0.5, 0, 0, 0, 1, 0, 0], np.float32)
+    q = scenes.uniform_configs(rng, (S + 1) * K, D)
+    with tempfile.TemporaryDirectory() as d:
+        fin, fout = os.path.join(d, "in.bin"), os.path.join(d, "out.bin")
+        with open(fin, "wb") as f:
+            f.write(np.array([prec, S, K, len(boxes), D, 2], np.int32).tobytes())
+            f.write(b"xarm6".ljust(32, b"\0"))
+            f.write(robot.capsule_radius.tobytes())
+            f.write(np.array([0.1, dt], np.float32).tobytes())
+            f.write(boxes.tobytes()); f.write(extra.tobytes()); f.write(q.tobytes())
+        subprocess.run([env_driver, fin, fout], check=True)
+        raw = open(fout, "rb").read()
+    code = boxes[:, 10].astype(int)
+    tol = np.where(code == 1, boxes[:, 11], 1000.0).astype(np.float32)
+    flags = np.where(code == 1, _abi.RPM_OBS_GROUND, np.where(code == 2, _abi.RPM_OBS_DYNAMIC, 0)).astype(np.uint8)
+    off, moved = 0, 0
+    prev = None
+    oracle = "ref32" if prec == _abi.RPM_PREC_FP32_REF else "ref64"
+    for s in range(S + 2):
+        cnt = int(np.frombuffer(raw[off:off + 4], np.int32)[0]); off += 4
+        aabb = np.frombuffer(raw[off:off + 24 * cnt], np.float32).reshape(cnt, 6).copy(); off += 24 * cnt
+        res = np.frombuffer(raw[off:off + 5 * K], np.uint8).reshape(K, 5); off += 5 * K
+        v = res[:, 0].copy()
+        dist = res[:, 1:].copy().view(np.float32).reshape(K)
+        if s == S + 1:   # object 0 removed, one static box added
+            tol = np.concatenate([tol[1:], [1000.0]]).astype(np.float32)
+            flags = np.concatenate([flags[1:], [0]]).astype(np.uint8)
+        elif prev is not None:
+            moved += int((aabb != prev).any(axis=1).sum())
+        prev = aabb
+        scene = scenes.Scene(aabb, tol, flags)
+        row = min(s, S)
+        qs = q[row * K:(row + 1) * K]
+        rv, rd, _ = O.check_configs(robot, scene, qs, prec=oracle, want=("valid", "dist"))
+        assert np.array_equal(v, rv), "step %d" % s
+        nd, _, _, _ = O.distance_nearest(robot, scene, qs, prec=oracle)
+        assert _bits(dist, nd.astype(np.float32)), "step %d" % s
+    assert off == len(raw)
+    assert moved >= S * 5   # the dynamic boxes moved every step

@@ -58,3 +58,22 @@ def test_workloads_are_seeded_and_shaped():
     assert L.min() >= 0.0099 and L.max() <= 2.0001
     sc3, parts = scenes.mixed_dof_workload(counts=(10, 20, 30), seed=3)
     assert sc3.n == 500 and [p[1].shape for p in parts] == [(10, 14), (20, 18), (30, 22)]
+
+
+@pytest.mark.parametrize("name,type_name", [("planar_2dof", "2dof"), ("planar_10dof", "10dof"), ("xarm6", "xarm6"),
+                                            ("spatial_10dof", "spatial_10dof"), ("spatial_14dof", "spatial_14dof"),
+                                            ("spatial_18dof", "spatial_18dof"), ("spatial_22dof", "spatial_22dof")])
+def test_builtin_robot_tables_match(name, type_name):
+    """rpm_robot_builtin (the C library's URDF tables, used by the C++ adapter
+    to describe a robots::AbstractRobot by its getType()) equals the Python
+    tables byte for byte once radii, ground rule and gripper are set alike."""
+    import ctypes
+    from rpmplv2_gb300 import _abi, engine, robots
+    lib = engine.load()
+    d = _abi.RobotDesc()
+    assert lib.rpm_robot_builtin(type_name.encode(), ctypes.byref(d)) == 0
+    r = robots.by_name(name) if name != "xarm6" else robots.xarm6(radius=0.0, gripper_length=0.0, ground_included=0)
+    if name != "xarm6":
+        r.set_capsule_radius(0.025)
+    assert bytes(d) == bytes(r.desc)
+    assert lib.rpm_robot_builtin(b"no_such_robot", ctypes.byref(d)) != 0
