@@ -26,6 +26,9 @@ import time
 
 import numpy as np
 
+# separate hardware queues for the serving loop's streams (before any CUDA context exists)
+os.environ.setdefault("CUDA_DEVICE_MAX_CONNECTIONS", "32")
+
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
@@ -374,14 +377,15 @@ def large_line(eng, scenes, timed):
 def serve_line(eng, serve):
     """The serving replay: 20,000 requests/s for 0.5 s over 64 resident scenes."""
     wl = serve.serving_workload(eng, seed=4, rate=20000.0, duration=0.5)
-    srv = serve.Server(eng, num_slots=6)
+    srv = serve.Server(eng)   # the library's defaults: 3 bulk streams, 8 express streams
     srv.replay(wl["requests"][:200], [0.0] * 200)
     tim = srv.replay(wl["requests"], wl["arrivals"], wl["motions"], period=0.001)
     summ = serve.latency_summary(tim, wl["meta"])
     summ.update({"workload": "64 resident scenes (robots of configs 0-3, 10-1000 boxes log-uniform, 20% with 5 "
                              "boxes moving up to 1.6 m/s updated every 1 ms), Poisson 20,000 req/s for 0.5 s, "
                              "sizes log-uniform 1-65,536, isValid / distance / edge in equal shares",
-                 "memory_budget_bytes": 8 << 30, "slots": 6})
+                 "memory_budget_bytes": 8 << 30, "bulk_slots": 3, "express_slots": 8, "express_work": 8192,
+                 "chunk_work": 16384})
     # capacity: the same trace submitted at once; latency at a rate the engine sustains
     t = srv.replay(wl["requests"], [0.0] * len(wl["requests"]))
     summ["capacity_req_per_s"] = len(t) / max(x.t_done for x in t)

@@ -150,6 +150,14 @@ int rpm_scene_create(rpm_ctx *ctx, int32_t robot_id, const float *aabb_host, con
  * call returns; checks already issued keep the version they started with. */
 int rpm_scene_update(rpm_ctx *ctx, int32_t scene_id, const int32_t *idx_host, const float *aabb_host, int32_t m,
                      uint64_t *version_out);
+/* rpm_scene_update for several scenes at once (each at most once): scene k
+ * takes counts[k] rows, consecutive in idx_host (indices) and aabb_host (six
+ * floats each).  All the new versions are written by one launch, so moving the
+ * dynamic obstacles of many scenes every few milliseconds (the reference's
+ * Environment::updateEnvironment per environment) costs one update.
+ * versions_out[k] (nullable) receives scene k's new version. */
+int rpm_scene_update_many(rpm_ctx *ctx, int32_t n_scenes, const int32_t *scene_ids, const int32_t *counts,
+                          const int32_t *idx_host, const float *aabb_host, uint64_t *versions_out);
 int rpm_scene_destroy(rpm_ctx *ctx, int32_t scene_id);
 int rpm_scene_info(rpm_ctx *ctx, int32_t scene_id, int32_t *robot_id, int32_t *num_obstacles, uint64_t *version);
 
@@ -393,23 +401,37 @@ int rpm_random_scenario_read(const char *path, int32_t num_obstacles, int32_t ru
  * Planners submit isValid / distance batches and edge batches of any size
  * against resident scenes while obstacles move (the DRGBT replanning shape,
  * DRGBT.cpp:79-176 with MotionValidity.cpp:30-53).  A worker thread admits
- * requests as device memory of the budget frees up, packs waiting
- * configuration and edge requests from any scenes and robots into one batch
- * per free slot (stream): one launch for the configuration requests and one
- * edge pipeline for the edge requests, so batches overlap on the device; it
- * time-stamps each request.
- * Smaller requests are served first (requests waiting over 50 ms are served
- * as small); half of the slots are high-priority streams reserved for batches
- * of small requests, so a replanning query is not held behind a bulk batch.
- * Host buffers should be pinned for copies to overlap. */
+ * requests as device memory of the budget frees up and serves them in two
+ * classes, each in arrival order:
+ *   express  requests of at most express_work units (a configuration counts
+ *            1, an edge 8) on high-priority streams; a request of 1,024 units
+ *            or more runs as a batch of its own, smaller ones share batches of
+ *            up to 1,024 units, so a replanning query never waits behind bulk
+ *            work or behind another query;
+ *   bulk     larger requests on low-priority streams, packed up to
+ *            max_batch_configs units per batch and run as chains of launches
+ *            of at most chunk_work units, so every bulk CTA is short and the
+ *            block scheduler gives SMs to express kernels quickly.
+ * A batch packs configuration and edge requests from any scenes and robots
+ * into multi-segment launches; batches overlap on the device; every request
+ * is time-stamped.  Host buffers should be pinned for copies to overlap.
+ * Processes that set CUDA_DEVICE_MAX_CONNECTIONS to 32 before creating their
+ * CUDA context (the Python package does) keep the streams on separate
+ * hardware queues. */
 typedef struct rpm_server rpm_server;
 typedef struct rpm_server_config {
-    int32_t num_slots;           /* concurrent batches (streams), default 4 */
+    int32_t num_slots;           /* bulk streams (concurrent bulk batches); 0: 3 */
     int32_t precision;           /* RPM_PREC_* of every request */
     int64_t memory_budget;       /* device bytes for request buffers (admission), default 8 GiB */
     int32_t max_batch_segments;  /* configuration requests and edge requests per batch, each <= 32 */
-    int32_t max_batch_configs;   /* work per batch: configurations + 8 x edges (1/8 on high-priority slots);
-                                    default 32,768 (a larger request runs as a batch of its own) */
+    int32_t max_batch_configs;   /* work per bulk batch; 0: 65,536 (a larger request runs as a batch of its own) */
+    int32_t express_slots;       /* high-priority streams for express requests; 0: 8 */
+    int32_t express_work;        /* largest express request; 0: 8,192 */
+    int32_t chunk_work;          /* work per bulk launch; 0: 16,384 */
+    int32_t bulk_sms;            /* > 0: the bulk streams run in an SM partition (a green context) of this
+                                    many SMs (rounded up to the driver's granularity, 8 on GB300), so the
+                                    other SMs only run express work; 0: bulk uses every SM */
+    int32_t reserved;
 } rpm_server_config;
 
 enum rpm_request_kind { RPM_REQ_CONFIGS = 0, RPM_REQ_EDGES = 1 };
@@ -434,6 +456,11 @@ typedef struct rpm_request_timing {
     int32_t batch_size;          /* requests in the launch it ran in */
     double t_submit, t_admit, t_launch, t_done;   /* seconds (monotonic; relative to the start in a replay) */
     uint64_t scene_version;      /* the version of the request's scene its checks read (rpm_scene_update) */
+    /* device-side trace of the request's batch (CUDA events on its stream):
+     * copies in, checks and copies out, each from the end of the previous
+     * step (so a step's time includes waiting for copy engines or SMs) */
+    float h2d_ms, kernel_ms, d2h_ms;
+    float enqueue_ms;            /* host time the worker spent enqueueing the batch */
 } rpm_request_timing;
 
 /* A moving obstacle of a replay: AABB(t) = AABB(0) + velocity * t. */

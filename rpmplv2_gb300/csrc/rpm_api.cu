@@ -150,9 +150,8 @@ void bind_scene_buf(const SceneRec &s, SceneBuf &b) {
 // kLeaf slots (four leaves per warp).  Padding slots get bounds +inf / -inf so
 // no gap test passes them; a leaf holding a NaN coordinate gets infinite
 // bounds so it is never skipped.
-__global__ void k_scene_sort(const float *f, const double *d, int n_pad, const int32_t *perm, int ns, float *sf,
-                             double *sd, float *blk) {
-    const int s = blockIdx.x * 32 + threadIdx.x;
+__device__ __forceinline__ void sort_slots(const float *f, const double *d, int n_pad, const int32_t *perm, int ns,
+                                           float *sf, double *sd, float *blk, int s) {
     const bool in = s < ns;
     const int j = in ? perm[s] : -1;
     const float inf = __int_as_float(0x7f800000);
@@ -203,7 +202,7 @@ __global__ void k_scene_sort(const float *f, const double *d, int n_pad, const i
         nan = nan || __shfl_xor_sync(full, (int)nan, off);
     }
     const int leaf = s / kLeaf;
-    if ((threadIdx.x % kLeaf) == 0 && in) {
+    if ((s % kLeaf) == 0 && in) {
         float *r = blk + (size_t)leaf * kBlkRec;
         for (int c = 0; c < 3; ++c) {
             r[c] = nan ? -inf : lo[c];
@@ -212,6 +211,43 @@ __global__ void k_scene_sort(const float *f, const double *d, int n_pad, const i
         r[6] = (tmax == -inf) ? 0.f : tmax;   // an all-padding leaf
         r[7] = (tmin == inf) ? 0.f : tmin;
     }
+}
+
+__global__ void k_scene_sort(const float *f, const double *d, int n_pad, const int32_t *perm, int ns, float *sf,
+                             double *sd, float *blk) {
+    sort_slots(f, d, n_pad, perm, ns, sf, sd, blk, blockIdx.x * 32 + threadIdx.x);
+}
+
+// The fused incremental update: one CTA per scene writes its next version
+// (rows and permutation copied from the current version, the updated rows
+// scattered in, then the sorted copy and leaf bounds rebuilt by its warps).
+// Descriptors and rows are read from pinned host memory in place.
+__global__ void __launch_bounds__(256) k_scene_update_many(const UpdDesc *descs) {
+    const UpdDesc u = descs[blockIdx.x];
+    const int np = u.n_pad;
+    for (int i = threadIdx.x; i < kFRows * np; i += blockDim.x) u.f[i] = u.src_f[i];
+    for (int i = threadIdx.x; i < kDRows * np; i += blockDim.x) u.d[i] = u.src_d[i];
+    for (int i = threadIdx.x; i < u.ns; i += blockDim.x) u.perm[i] = u.src_perm[i];
+    __syncthreads();
+    for (int k = threadIdx.x; k < u.m; k += blockDim.x) {
+        const int j = __float_as_int(u.rows[7 * k]);
+#pragma unroll
+        for (int c = 0; c < 6; ++c) {
+            const float v = u.rows[7 * k + 1 + c];
+            u.f[c * np + j] = v;
+            u.d[c * np + j] = (double)v;
+        }
+    }
+    __syncthreads();
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, warps = blockDim.x >> 5;
+    for (int s0 = warp * 32; s0 < u.ns; s0 += warps * 32)
+        sort_slots(u.f, u.d, np, u.perm, u.ns, u.sf, u.sd, u.blk, s0 + lane);
+}
+
+cudaError_t launch_scene_update_many(const UpdDesc *descs, int count, cudaStream_t st) {
+    if (count <= 0) return cudaSuccess;
+    k_scene_update_many<<<count, 256, 0, st>>>(descs);
+    return cudaGetLastError();
 }
 
 cudaError_t launch_scene_sort(const SceneRec &s, const SceneBuf &b, cudaStream_t st) {
@@ -721,6 +757,11 @@ int rpm_ctx_destroy(rpm_ctx *ctx) {
         cudaFree(ctx->hq[i]); cudaFree(ctx->hv[i]); cudaFree(ctx->hd[i]); cudaFree(ctx->hp[i]);
     }
     for (cudaEvent_t e : ctx->event_pool) cudaEventDestroy(e);
+    for (int i = 0; i < rpm_ctx::kUpdRing; ++i) {
+        if (ctx->upd_stage[i]) cudaFreeHost(ctx->upd_stage[i]);
+        if (ctx->upd_done[i]) cudaEventDestroy(ctx->upd_done[i]);
+    }
+    if (ctx->upd_stream) cudaStreamDestroy(ctx->upd_stream);
     delete ctx;
     return RPM_OK;
 }
@@ -798,6 +839,31 @@ int rpm_scene_update(rpm_ctx *ctx, int32_t scene_id, const int32_t *idx_host, co
     return RPM_OK;
 }
 
+int rpm_scene_update_many(rpm_ctx *ctx, int32_t n_scenes, const int32_t *scene_ids, const int32_t *counts,
+                          const int32_t *idx_host, const float *aabb_host, uint64_t *versions_out) {
+    if (!ctx || n_scenes < 0 || (n_scenes > 0 && (!scene_ids || !counts))) return fail(RPM_ERR_INVALID, "bad update arguments");
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    std::vector<SceneUpd> ups;
+    size_t off = 0;
+    for (int k = 0; k < n_scenes; ++k) {
+        SceneRec *s = find_scene(ctx, scene_ids[k]);
+        if (!s) return fail(RPM_ERR_INVALID, "unknown scene %d", scene_ids[k]);
+        const int32_t m = counts[k];
+        if (m < 0 || (m > 0 && (!idx_host || !aabb_host))) return fail(RPM_ERR_INVALID, "bad update count %d", m);
+        for (int i = 0; i < m; ++i)
+            if (idx_host[off + i] < 0 || idx_host[off + i] >= s->n)
+                return fail(RPM_ERR_INVALID, "obstacle index %d out of range", idx_host[off + i]);
+        ups.push_back(SceneUpd{s, m ? idx_host + off : nullptr, m ? aabb_host + 6 * off : nullptr, m});
+        off += (size_t)m;
+    }
+    if (set_device(ctx)) return RPM_ERR_CUDA;
+    const int rc = scene_update_many(ctx, ups);
+    if (rc) return rc;
+    if (versions_out)
+        for (int k = 0; k < n_scenes; ++k) versions_out[k] = ups[k].s->version;
+    return RPM_OK;
+}
+
 int rpm_scene_destroy(rpm_ctx *ctx, int32_t scene_id) {
     if (!ctx) return fail(RPM_ERR_INVALID, "NULL argument");
     std::lock_guard<std::mutex> lk(ctx->mu);
@@ -807,8 +873,6 @@ int rpm_scene_destroy(rpm_ctx *ctx, int32_t scene_id) {
         wait_users(ctx, b);
         if (b.ready) { cudaEventSynchronize(b.ready); cudaEventDestroy(b.ready); }
         if (b.mem) cudaFree(b.mem);
-        if (b.upd_host) cudaFreeHost(b.upd_host);
-        if (b.upd_dev) cudaFree(b.upd_dev);
     }
     ctx->scenes.erase(scene_id);
     {

@@ -58,10 +58,23 @@ struct SceneBuf {
     std::vector<cudaEvent_t> users;   // checks that may still read this buffer
     cudaEvent_t ready = nullptr;      // end of the incremental update that wrote this version
     bool pending = false;             // 'ready' must be waited on before reading
-    // staging of the incremental update list that produced this version
-    float *upd_host = nullptr;        // pinned, [m][7]: index (as bits) + six AABB values
-    float *upd_dev = nullptr;
-    int32_t upd_cap = 0;
+};
+
+// One scene version written by the fused update kernel: the current
+// version's rows and permutation copied, m updated rows ([m][7]: index as
+// bits, six AABB values) scattered in, the sorted copy and leaf bounds rebuilt.
+struct UpdDesc {
+    const float *src_f;
+    const double *src_d;
+    const int32_t *src_perm;
+    float *f;
+    double *d;
+    float *sf;
+    double *sd;
+    float *blk;
+    int32_t *perm;
+    const float *rows;   // pinned host memory, read in place by the kernel
+    int32_t n_pad, ns, m, pad;
 };
 
 struct SceneRec {
@@ -129,6 +142,13 @@ struct rpm_ctx {
     std::map<cudaStream_t, rpm::impl::Scratch *> scratch;
     std::vector<cudaEvent_t> event_pool;
     cudaStream_t upd_stream = nullptr;    // incremental scene updates
+    // pinned staging ring of incremental updates (descriptors and rows, read in
+    // place by the update kernel); a slot is reused once its kernel has run
+    static constexpr int kUpdRing = 4;
+    unsigned char *upd_stage[kUpdRing] = {};
+    size_t upd_cap[kUpdRing] = {};
+    cudaEvent_t upd_done[kUpdRing] = {};
+    int upd_next = 0;
     // host-buffer pipeline
     cudaStream_t hs[2] = {nullptr, nullptr};
     float *hq[2] = {nullptr, nullptr};
@@ -174,7 +194,17 @@ int enqueue_edge_batch(rpm_ctx *ctx, Scratch *sc, int prec, const std::vector<Ed
                        cudaStream_t st);
 int enqueue_edges(rpm_ctx *ctx, Scratch *sc, SceneRec *s, int prec, const float *q1, const float *q2, int64_t E,
                   float step, int32_t num_checks, uint8_t *valid, int32_t *checks, int ctas_per_sm, cudaStream_t st);
+// Incremental updates of several scenes at once: one kernel launch writes the
+// next version of every scene (UpdDesc).  Caller holds ctx->mu.
+struct SceneUpd {
+    SceneRec *s;
+    const int32_t *idx;
+    const float *aabb;   // m x 6
+    int32_t m;
+};
+int scene_update_many(rpm_ctx *ctx, const std::vector<SceneUpd> &u);
 int scene_update(rpm_ctx *ctx, SceneRec *s, const int32_t *idx, const float *aabb, int32_t m);
+cudaError_t launch_scene_update_many(const UpdDesc *descs, int count, cudaStream_t st);
 // Spatially sorted copy: Morton order of the obstacle centres (fixed for the
 // scene's lifetime), its size, and the kernel that rebuilds it in a version.
 void sorted_layout(SceneRec &s);

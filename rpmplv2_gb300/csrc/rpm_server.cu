@@ -8,26 +8,38 @@
 //   * admits requests in arrival order as device memory of the budget frees up
 //     (a request larger than the whole budget is rejected), skipping over
 //     requests that do not fit yet so small ones are not held behind large ones;
-//   * packs admitted requests -- from any scenes and robots, configuration and
-//     edge requests alike -- into one batch per free slot (a slot is a
-//     stream): one multi-segment launch for the configuration requests and one
-//     multi-segment edge pipeline for the edge requests, so new requests join
-//     the next batch while earlier batches still run and batches overlap on
-//     the device.  A batch holds at most max_batch_configs units of work (an
-//     edge counts 8), an eighth of that on the high-priority slots;
+//   * sorts them into two classes.  Express requests (at most express_work
+//     units of work; an edge counts 8) run on high-priority streams, in
+//     arrival order, each in a batch of its own unless it is below
+//     kExpressShared units (those share batches up to that size); they carry
+//     a small share of the work, so they find a stream and the SMs free.
+//     Bulk requests run on low-priority streams, in arrival order, packed up
+//     to max_batch_configs units per batch, and every batch runs as a chain
+//     of launches of at most chunk_work units: short launches keep each CTA
+//     short, so the block scheduler hands SMs to express kernels quickly.
+//     Optionally the bulk streams live in an SM partition (a green context)
+//     so some SMs only ever run express work;
+//   * packs the requests of a batch -- from any scenes and robots,
+//     configuration and edge requests alike -- into multi-segment launches
+//     (configurations) and multi-segment edge pipelines (edges);
 //   * retires batches by CUDA events, frees their memory and time-stamps every
-//     request (submit, admit, launch, done).
+//     request (submit, admit, launch, done, and a device-side trace of the
+//     batch's copies and checks).
 // Each request's result is what the same check gives alone: configurations are
 // evaluated independently, and a batch reads one consistent version of each
-// scene.
+// scene (the version current when the batch was enqueued, kept for all its
+// launches).
 #include <algorithm>
 #include <atomic>
 #include <chrono>
 #include <condition_variable>
 #include <deque>
+#include <limits>
 #include <list>
 #include <thread>
 #include <unordered_map>
+
+#include <cuda.h>   // driver types only: the green-context calls go through the runtime's entry points
 
 #include "rpm_ctx_impl.cuh"
 
@@ -35,74 +47,79 @@ namespace rpm {
 namespace impl {
 
 // ------------------------------------------------------ incremental update --
-// Rows of m updated obstacles: [k][0] = index (bits), [k][1..6] = AABB.
-__global__ void k_obstacle_update(float *rows_f, double *rows_d, int n_pad, const float *upd, int m) {
-    const int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= m) return;
-    const int j = __float_as_int(upd[7 * k]);
-#pragma unroll
-    for (int c = 0; c < 6; ++c) {
-        const float v = upd[7 * k + 1 + c];
-        rows_f[c * n_pad + j] = v;
-        rows_d[c * n_pad + j] = (double)v;
+// The next version of each listed scene: one kernel (k_scene_update_many)
+// copies the current version, scatters the updated AABBs and rebuilds the
+// sorted copy, one CTA per scene; 'ready' of each new version is recorded
+// after it.  Checks issued afterwards wait on 'ready'; checks already issued
+// keep reading the versions they started on, and the update stream first waits
+// (on the device) for the checks still reading the buffers it overwrites.
+// Descriptors and rows go through a pinned staging ring read by the kernel in
+// place, so an update costs one launch plus an event per scene.  Caller holds
+// ctx->mu.
+int scene_update_many(rpm_ctx *ctx, const std::vector<SceneUpd> &ups) {
+    if (ups.empty()) return RPM_OK;
+    for (size_t a = 0; a < ups.size(); ++a)
+        for (size_t b = a + 1; b < ups.size(); ++b)
+            if (ups[a].s == ups[b].s) return fail(RPM_ERR_INVALID, "a scene appears twice in one update");
+    if (!ctx->upd_stream) CK(cudaStreamCreateWithFlags(&ctx->upd_stream, cudaStreamNonBlocking));
+    // staging: descriptors, then each scene's rows
+    size_t bytes = ups.size() * sizeof(UpdDesc);
+    for (const SceneUpd &u : ups) bytes += ((size_t)u.m * 7 * sizeof(float) + 15) & ~(size_t)15;
+    const int slot = ctx->upd_next;
+    ctx->upd_next = (slot + 1) % rpm_ctx::kUpdRing;
+    if (!ctx->upd_done[slot]) CK(cudaEventCreateWithFlags(&ctx->upd_done[slot], cudaEventDisableTiming));
+    else CK(cudaEventSynchronize(ctx->upd_done[slot]));   // its last kernel has read it (normally long done)
+    if (ctx->upd_cap[slot] < bytes) {
+        if (ctx->upd_stage[slot]) cudaFreeHost(ctx->upd_stage[slot]);
+        ctx->upd_cap[slot] = std::max<size_t>(bytes * 2, 4096);
+        if (cudaMallocHost(&ctx->upd_stage[slot], ctx->upd_cap[slot]) != cudaSuccess) {
+            ctx->upd_stage[slot] = nullptr;
+            ctx->upd_cap[slot] = 0;
+            return fail(RPM_ERR_NOMEM, "update staging allocation failed");
+        }
     }
+    UpdDesc *descs = reinterpret_cast<UpdDesc *>(ctx->upd_stage[slot]);
+    unsigned char *rows = ctx->upd_stage[slot] + ups.size() * sizeof(UpdDesc);
+    for (size_t k = 0; k < ups.size(); ++k) {
+        const SceneUpd &u = ups[k];
+        SceneRec *s = u.s;
+        for (int i = 0; i < u.m; ++i)
+            for (int c = 0; c < 6; ++c) s->aabb[6 * (size_t)u.idx[i] + c] = u.aabb[6 * (size_t)i + c];
+        const int nxt = (s->cur + 1) % kRing;
+        SceneBuf &cur = s->bufs[s->cur];
+        SceneBuf &b = s->bufs[nxt];
+        // checks still reading the version about to be overwritten finish first
+        stream_wait_users(ctx, b, ctx->upd_stream);
+        if (!b.mem) {
+            if (cudaMalloc(&b.mem, scene_bytes(*s)) != cudaSuccess) return fail(RPM_ERR_NOMEM, "scene version allocation failed");
+            bind_scene_buf(*s, b);
+        }
+        if (!b.ready) CK(cudaEventCreateWithFlags(&b.ready, cudaEventDisableTiming));
+        float *r = reinterpret_cast<float *>(rows);
+        for (int i = 0; i < u.m; ++i) {
+            const int32_t j = u.idx[i];
+            std::memcpy(&r[7 * i], &j, sizeof j);
+            for (int c = 0; c < 6; ++c) r[7 * i + 1 + c] = u.aabb[6 * (size_t)i + c];
+        }
+        descs[k] = UpdDesc{cur.f, cur.d, cur.perm, b.f, b.d, b.sf, b.sd, b.blk, b.perm, r, s->n_pad, s->ns, u.m, 0};
+        rows += ((size_t)u.m * 7 * sizeof(float) + 15) & ~(size_t)15;
+    }
+    CK(launch_scene_update_many(descs, (int)ups.size(), ctx->upd_stream));
+    CK(cudaEventRecord(ctx->upd_done[slot], ctx->upd_stream));
+    for (const SceneUpd &u : ups) {
+        SceneRec *s = u.s;
+        const int nxt = (s->cur + 1) % kRing;
+        SceneBuf &b = s->bufs[nxt];
+        CK(cudaEventRecord(b.ready, ctx->upd_stream));
+        b.pending = true;
+        s->cur = nxt;
+        s->version++;
+    }
+    return RPM_OK;
 }
 
-// The next version of a scene: copy the current version device-to-device,
-// scatter the m updated AABBs, rebuild the sorted copy, record 'ready'.  Checks issued afterwards wait
-// on 'ready'; checks already issued keep reading the version they started on.
-// Caller holds ctx->mu.
 int scene_update(rpm_ctx *ctx, SceneRec *s, const int32_t *idx, const float *aabb, int32_t m) {
-    for (int k = 0; k < m; ++k)
-        for (int c = 0; c < 6; ++c) s->aabb[6 * (size_t)idx[k] + c] = aabb[6 * (size_t)k + c];
-    if (!ctx->upd_stream) CK(cudaStreamCreateWithFlags(&ctx->upd_stream, cudaStreamNonBlocking));
-    const int nxt = (s->cur + 1) % kRing;
-    SceneBuf &cur = s->bufs[s->cur];
-    SceneBuf &b = s->bufs[nxt];
-    // checks still reading the version about to be overwritten finish first
-    // (ordered on the device: the host never blocks here)
-    stream_wait_users(ctx, b, ctx->upd_stream);
-    // the pinned staging of this buffer is free once its last update ran;
-    // otherwise this update copies from pageable memory
-    const bool staging_free = !b.ready || cudaEventQuery(b.ready) == cudaSuccess;
-    const size_t bytes = scene_bytes(*s);
-    if (!b.mem) {
-        if (cudaMalloc(&b.mem, bytes) != cudaSuccess) return fail(RPM_ERR_NOMEM, "scene version allocation failed");
-        bind_scene_buf(*s, b);
-    }
-    if (!b.ready) CK(cudaEventCreateWithFlags(&b.ready, cudaEventDisableTiming));
-    if (b.upd_cap < m) {
-        if (b.ready) CK(cudaEventSynchronize(b.ready));   // growing the staging (rare): its last copy must be done
-        if (b.upd_host) cudaFreeHost(b.upd_host);
-        if (b.upd_dev) cudaFree(b.upd_dev);
-        b.upd_cap = std::max(m, 64);
-        if (cudaMallocHost(&b.upd_host, (size_t)b.upd_cap * 7 * sizeof(float)) != cudaSuccess ||
-            cudaMalloc(&b.upd_dev, (size_t)b.upd_cap * 7 * sizeof(float)) != cudaSuccess)
-            return fail(RPM_ERR_NOMEM, "update staging allocation failed");
-    }
-    std::vector<float> pageable;
-    float *stage = b.upd_host;
-    if (!staging_free) {
-        pageable.resize((size_t)m * 7);
-        stage = pageable.data();
-    }
-    for (int k = 0; k < m; ++k) {
-        int32_t j = idx[k];
-        std::memcpy(&stage[7 * k], &j, sizeof j);
-        for (int c = 0; c < 6; ++c) stage[7 * k + 1 + c] = aabb[6 * (size_t)k + c];
-    }
-    CK(cudaMemcpyAsync(b.mem, cur.mem, bytes, cudaMemcpyDeviceToDevice, ctx->upd_stream));
-    if (m > 0) {
-        CK(cudaMemcpyAsync(b.upd_dev, stage, (size_t)m * 7 * sizeof(float), cudaMemcpyHostToDevice, ctx->upd_stream));
-        k_obstacle_update<<<(m + 127) / 128, 128, 0, ctx->upd_stream>>>(b.f, b.d, s->n_pad, b.upd_dev, m);
-        CK(cudaGetLastError());
-        CK(launch_scene_sort(*s, b, ctx->upd_stream));   // same order, new contents and block bounds
-    }
-    CK(cudaEventRecord(b.ready, ctx->upd_stream));
-    b.pending = true;
-    s->cur = nxt;
-    s->version++;
-    return RPM_OK;
+    return scene_update_many(ctx, {SceneUpd{s, idx, aabb, m}});
 }
 
 }  // namespace impl
@@ -162,20 +179,69 @@ struct Req {
 struct Slot {
     cudaStream_t st = nullptr;
     cudaEvent_t done = nullptr;
+    cudaEvent_t trace[3] = {nullptr, nullptr, nullptr};   // batch start, copies in done, checks done
     std::vector<Req *> reqs;
     bool busy = false;
-    bool small = false;   // high-priority stream for batches of small requests
+    bool express = false;   // high-priority stream for small requests
 };
 
-constexpr int64_t kSmallRequest = 8192;   // configurations (edges count x 8)
-// Work per batch: a batch completes as a whole, so its size bounds the latency
-// of every request in it.  32,768 units held p99 of requests up to 4,096
-// configurations to 3.4 ms at 12,000 req/s of the serving trace (262,144: 9.7 ms)
-// for 5 % less throughput at 20,000 req/s.
-constexpr int32_t kDefaultBatchWork = 1 << 15;
-constexpr double kAgeBoost = 0.050;       // a request waiting this long (s) is served as if small
+// Defaults of rpm_server_config (a field of 0 takes its default).
+constexpr int32_t kDefaultBulkSlots = 3;
+constexpr int32_t kDefaultExpressSlots = 8;
+constexpr int32_t kDefaultExpressWork = 8192;   // units: configurations, an edge counting 8
+constexpr int32_t kDefaultBatchWork = 1 << 16;  // bulk batch
+constexpr int32_t kDefaultChunkWork = 1 << 14;  // bulk launch
+constexpr int64_t kExpressShared = 1024;        // express requests below this share batches
 
 int64_t work_of(const Req *q) { return q->r.kind == RPM_REQ_EDGES ? 8 * q->r.count : q->r.count; }
+
+// An SM partition for the bulk streams (a green context of the device's
+// primary context).  Its driver calls are reached through the runtime's driver
+// entry points, so the library needs no link against the driver.
+struct GreenPartition {
+    CUgreenCtx g = nullptr;
+    unsigned sms = 0;
+    CUresult (*stream_create)(CUstream *, CUgreenCtx, unsigned, int) = nullptr;
+    CUresult (*stream_destroy)(CUstream) = nullptr;
+    CUresult (*destroy)(CUgreenCtx) = nullptr;
+};
+
+template <typename F> bool driver_fn(const char *name, F &fn) {
+    void *p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion(name, &p, CUDART_VERSION, cudaEnableDefault, &q) != cudaSuccess ||
+        q != cudaDriverEntryPointSuccess || !p)
+        return false;
+    fn = reinterpret_cast<F>(p);
+    return true;
+}
+
+// A green context of at least 'want' SMs of 'device' (rounded as the driver
+// requires).  Returns RPM_OK or an error with a message.
+int make_partition(int device, unsigned want, GreenPartition &gp) {
+    CUresult (*device_get)(CUdevice *, int) = nullptr;
+    CUresult (*get_resource)(CUdevice, CUdevResource *, CUdevResourceType) = nullptr;
+    CUresult (*split)(CUdevResource *, unsigned *, const CUdevResource *, CUdevResource *, unsigned, unsigned) = nullptr;
+    CUresult (*gen_desc)(CUdevResourceDesc *, CUdevResource *, unsigned) = nullptr;
+    CUresult (*create)(CUgreenCtx *, CUdevResourceDesc, CUdevice, unsigned) = nullptr;
+    if (!driver_fn("cuDeviceGet", device_get) || !driver_fn("cuDeviceGetDevResource", get_resource) ||
+        !driver_fn("cuDevSmResourceSplitByCount", split) || !driver_fn("cuDevResourceGenerateDesc", gen_desc) ||
+        !driver_fn("cuGreenCtxCreate", create) || !driver_fn("cuGreenCtxStreamCreate", gp.stream_create) ||
+        !driver_fn("cuStreamDestroy", gp.stream_destroy) || !driver_fn("cuGreenCtxDestroy", gp.destroy))
+        return fail(RPM_ERR_CUDA, "green contexts are not available from this driver");
+    CUdevice dev;
+    CUdevResource all, part, rest;
+    unsigned groups = 1;
+    CUdevResourceDesc desc;
+    if (device_get(&dev, device) != CUDA_SUCCESS || get_resource(dev, &all, CU_DEV_RESOURCE_TYPE_SM) != CUDA_SUCCESS)
+        return fail(RPM_ERR_CUDA, "querying the device's SMs failed");
+    if (want >= all.sm.smCount) return fail(RPM_ERR_INVALID, "bulk_sms %u leaves no SM of %u to express work", want, all.sm.smCount);
+    if (split(&part, &groups, &all, &rest, 0, want) != CUDA_SUCCESS || groups != 1 ||
+        gen_desc(&desc, &part, 1) != CUDA_SUCCESS || create(&gp.g, desc, dev, CU_GREEN_CTX_DEFAULT_STREAM) != CUDA_SUCCESS)
+        return fail(RPM_ERR_CUDA, "creating an SM partition of %u SMs failed", want);
+    gp.sms = part.sm.smCount;
+    return RPM_OK;
+}
 
 }  // namespace
 
@@ -187,13 +253,15 @@ struct rpm_server {
     std::mutex mu;
     std::condition_variable cv_work, cv_done;
     std::deque<Req *> incoming;   // submitted, not yet admitted
-    std::deque<Req *> ready;      // admitted, waiting for a slot
+    std::deque<Req *> express;    // admitted small requests, in arrival order
+    std::deque<Req *> bulk;       // admitted large requests, in arrival order
     std::vector<Slot> slots;
     std::unordered_map<uint64_t, Req *> reqs;
     uint64_t next_ticket = 1;
     std::thread worker;
     bool stop = false;
     int64_t batches = 0;
+    GreenPartition bulk_part;   // bulk streams' SMs (when cfg.bulk_sms > 0)
 };
 
 namespace {
@@ -239,54 +307,99 @@ DevBufs layout(rpm_server *srv, const Req *q) {
     return d;
 }
 
-// Launch one batch on a reserved slot: copies in, the checks, copies out.
-// Called by the worker without srv->mu (the batch and the slot are its own);
-// takes ctx->mu for the enqueue.
-// versions[k] receives the scene version batch[k] reads.
-int launch_batch(rpm_server *srv, Slot &slot, const std::vector<Req *> &batch, std::vector<uint64_t> &versions) {
+// Launch one batch on a reserved slot: copies in, the checks as launches of at
+// most 'chunk' units of work each, copies out.  Every launch of the batch is
+// enqueued here under ctx->mu, so all of them read the scene versions current
+// now.  Called by the worker without srv->mu (the batch and the slot are its
+// own).  versions[k] receives the scene version batch[k] reads.
+int launch_batch(rpm_server *srv, Slot &slot, const std::vector<Req *> &batch, int64_t chunk,
+                 std::vector<uint64_t> &versions) {
     rpm_ctx *ctx = srv->ctx;
     std::lock_guard<std::mutex> lk(ctx->mu);
     if (set_device(ctx)) return RPM_ERR_CUDA;
-    std::vector<SegReq> segs;
-    std::vector<EdgeReq> edges;
-    int64_t n_edges = 0;
+    std::vector<SceneRec *> scene(batch.size(), nullptr);
     versions.assign(batch.size(), 0);
+    CK(cudaEventRecord(slot.trace[0], slot.st));
     for (size_t k = 0; k < batch.size(); ++k) {
         Req *q = batch[k];
         const DevBufs d = layout(srv, q);
         const size_t n = (size_t)q->r.count;
         SceneRec *s = find_scene(ctx, q->r.scene_id);
         if (!s) return fail(RPM_ERR_INVALID, "unknown scene %d", q->r.scene_id);
-        versions[k] = s->version;   // the launch reads s->cur, made current with this version
+        scene[k] = s;
+        versions[k] = s->version;   // the launches read s->cur, made current with this version
         if (q->r.kind == RPM_REQ_EDGES) {
             CK(cudaMemcpyAsync(d.q1, q->r.q1_host, n * q->D * sizeof(float), cudaMemcpyHostToDevice, slot.st));
             CK(cudaMemcpyAsync(d.q2, q->r.q2_host, n * q->D * sizeof(float), cudaMemcpyHostToDevice, slot.st));
-            edges.push_back(EdgeReq{s, d.q1, d.q2, (int64_t)n, q->r.step, q->r.num_checks, d.valid, d.checks});
-            n_edges += (int64_t)n;
         } else {
             CK(cudaMemcpyAsync(d.q, q->r.q_host, n * q->D * sizeof(float), cudaMemcpyHostToDevice, slot.st));
-            segs.push_back(SegReq{s, d.q, (int64_t)n, d.valid, d.dist, d.profile});
         }
     }
-    if (!segs.empty()) {
+    CK(cudaEventRecord(slot.trace[1], slot.st));
+    // configuration requests, cut into launches of at most 'chunk' configurations
+    std::vector<SegReq> segs;
+    int64_t segw = 0;
+    auto flush_segs = [&]() -> int {
+        if (segs.empty()) return RPM_OK;
         const int rc = enqueue_segments(ctx, srv->cfg.precision, segs, slot.st);
-        if (rc) return rc;
-    }
-    if (n_edges > 0) {
-        // every edge request of the batch in one pipeline (up to kMaxSegs requests per launch)
-        Scratch *sc = nullptr;
-        int rc = get_scratch(ctx, slot.st, 0, &sc);
-        if (!rc) rc = edge_scratch(ctx, sc, n_edges, slot.st);
-        if (!rc) {
-            auto it = ctx->edge_ctas.find({edges[0].scene->robot, srv->cfg.precision});
-            rc = enqueue_edge_batch(ctx, sc, srv->cfg.precision, edges, it == ctx->edge_ctas.end() ? 4 : it->second,
-                                    slot.st);
+        segs.clear();
+        segw = 0;
+        return rc;
+    };
+    for (size_t k = 0; k < batch.size(); ++k) {
+        const Req *q = batch[k];
+        if (q->r.kind == RPM_REQ_EDGES) continue;
+        const DevBufs d = layout(srv, q);
+        for (int64_t first = 0; first < q->r.count;) {
+            const int64_t cnt = std::min(q->r.count - first, chunk - segw);
+            segs.push_back(SegReq{scene[k], d.q + first * q->D, cnt, d.valid ? d.valid + first : nullptr,
+                                  d.dist ? d.dist + first : nullptr, d.profile ? d.profile + first * q->L : nullptr});
+            segw += cnt;
+            first += cnt;
+            if (segw >= chunk || (int)segs.size() == kMaxSegs) {
+                const int rc = flush_segs();
+                if (rc) return rc;
+            }
         }
+    }
+    int rc = flush_segs();
+    if (rc) return rc;
+    // edge requests, cut into pipelines of at most 'chunk' units (8 per edge)
+    const int64_t echunk = std::max<int64_t>(1, chunk / 8);
+    std::vector<std::vector<EdgeReq>> groups(1);
+    int64_t ew = 0, emax = 0;
+    for (size_t k = 0; k < batch.size(); ++k) {
+        const Req *q = batch[k];
+        if (q->r.kind != RPM_REQ_EDGES) continue;
+        const DevBufs d = layout(srv, q);
+        for (int64_t first = 0; first < q->r.count;) {
+            const int64_t cnt = std::min(q->r.count - first, echunk - ew);
+            groups.back().push_back(EdgeReq{scene[k], d.q1 + first * q->D, d.q2 + first * q->D, cnt, q->r.step,
+                                            q->r.num_checks, d.valid + first, d.checks + first});
+            ew += cnt;
+            first += cnt;
+            emax = std::max(emax, ew);
+            if (ew >= echunk || (int)groups.back().size() == kMaxSegs) {
+                groups.emplace_back();
+                ew = 0;
+            }
+        }
+    }
+    if (emax > 0) {
+        Scratch *sc = nullptr;
+        rc = get_scratch(ctx, slot.st, 0, &sc);
+        if (!rc) rc = edge_scratch(ctx, sc, emax, slot.st);
         if (rc) return rc;
         std::vector<SceneBuf *> used;
-        for (const EdgeReq &r : edges) {
-            SceneBuf *b = &r.scene->bufs[r.scene->cur];
-            if (std::find(used.begin(), used.end(), b) == used.end()) used.push_back(b);
+        for (const auto &g : groups) {
+            if (g.empty()) continue;
+            auto it = ctx->edge_ctas.find({g[0].scene->robot, srv->cfg.precision});
+            rc = enqueue_edge_batch(ctx, sc, srv->cfg.precision, g, it == ctx->edge_ctas.end() ? 4 : it->second, slot.st);
+            if (rc) return rc;
+            for (const EdgeReq &r : g) {
+                SceneBuf *b = &r.scene->bufs[r.scene->cur];
+                if (std::find(used.begin(), used.end(), b) == used.end()) used.push_back(b);
+            }
         }
         for (SceneBuf *b : used) {
             prune_users(ctx, *b);
@@ -295,6 +408,7 @@ int launch_batch(rpm_server *srv, Slot &slot, const std::vector<Req *> &batch, s
             b->users.push_back(e);
         }
     }
+    CK(cudaEventRecord(slot.trace[2], slot.st));
     for (Req *q : batch) {
         const DevBufs d = layout(srv, q);
         const size_t n = (size_t)q->r.count;
@@ -321,7 +435,14 @@ void worker_loop(rpm_server *srv) {
         for (Slot &sl : srv->slots) {
             if (!sl.busy || cudaEventQuery(sl.done) != cudaSuccess) continue;
             const double t = now_s();
+            float ms[3] = {0.f, 0.f, 0.f};
+            cudaEventElapsedTime(&ms[0], sl.trace[0], sl.trace[1]);
+            cudaEventElapsedTime(&ms[1], sl.trace[1], sl.trace[2]);
+            cudaEventElapsedTime(&ms[2], sl.trace[2], sl.done);
             for (Req *q : sl.reqs) {
+                q->t.h2d_ms = ms[0];
+                q->t.kernel_ms = ms[1];
+                q->t.d2h_ms = ms[2];
                 q->t.t_done = t;
                 q->t.status = 0;
                 srv->arena.release(q->off, q->bytes);
@@ -331,7 +452,7 @@ void worker_loop(rpm_server *srv) {
             progress = true;
             srv->cv_done.notify_all();
         }
-        // ---- admit in arrival order as memory frees up
+        // ---- admit in arrival order as memory frees up, into the two classes
         for (auto it = srv->incoming.begin(); it != srv->incoming.end();) {
             Req *q = *it;
             if (q->bytes > srv->arena.size) {
@@ -345,53 +466,48 @@ void worker_loop(rpm_server *srv) {
             if (srv->arena.alloc(q->bytes, off)) {
                 q->off = off;
                 q->t.t_admit = now_s();
-                srv->ready.push_back(q);
+                (work_of(q) <= srv->cfg.express_work ? srv->express : srv->bulk).push_back(q);
                 it = srv->incoming.erase(it);
                 progress = true;
             } else {
                 ++it;
             }
         }
-        // ---- launch batches on free slots: smallest requests first; the
-        //      high-priority slots take batches of small (or long-waiting) requests
-        if (!srv->ready.empty()) {
-            std::stable_sort(srv->ready.begin(), srv->ready.end(),
-                             [](const Req *a, const Req *b) { return work_of(a) < work_of(b); });
-        }
-        const double tnow = now_s();
+        // ---- launch: express slots take express requests, bulk slots bulk
+        //      requests, each class in arrival order
         for (Slot &sl : srv->slots) {
-            if (srv->ready.empty()) break;
             if (sl.busy) continue;
-            // work cap of the batch: small on the high-priority slots so their
-            // requests finish quickly; configuration and edge requests mix
-            const int64_t cap = sl.small ? std::max<int64_t>(1, srv->cfg.max_batch_configs / 8) : srv->cfg.max_batch_configs;
+            std::deque<Req *> &queue = sl.express ? srv->express : srv->bulk;
+            if (queue.empty()) continue;
+            // an express batch is one request, or several requests smaller than
+            // kExpressShared units: a batch completes as a whole, so sharing one
+            // would add the others' work to a request's latency
+            const int64_t cap = sl.express ? kExpressShared : srv->cfg.max_batch_configs;
             std::vector<Req *> batch;
             int64_t work = 0;
             int nseg = 0, nedge = 0;
-            for (auto it = srv->ready.begin(); it != srv->ready.end();) {
-                Req *q = *it;
+            while (!queue.empty()) {
+                Req *q = queue.front();
                 const bool edge = q->r.kind == RPM_REQ_EDGES;
-                const bool small = work_of(q) <= kSmallRequest || tnow - q->t.t_submit > kAgeBoost;
-                if (sl.small && !small) { ++it; continue; }
-                if (!batch.empty() && (work + work_of(q) > cap || (edge ? nedge : nseg) >= srv->cfg.max_batch_segments)) {
-                    ++it;
-                    continue;
-                }
+                if (!batch.empty() && (work + work_of(q) > cap || (edge ? nedge : nseg) >= srv->cfg.max_batch_segments))
+                    break;
                 batch.push_back(q);
                 work += work_of(q);
                 (edge ? nedge : nseg) += 1;
-                it = srv->ready.erase(it);
+                queue.pop_front();
             }
-            if (batch.empty()) continue;
             sl.busy = true;   // reserved: only this thread touches the slot
             const double t = now_s();
             lk.unlock();      // submissions and polls proceed while the batch is enqueued
             std::vector<uint64_t> versions;
-            const int rc = launch_batch(srv, sl, batch, versions);
+            const int64_t chunk = sl.express ? std::numeric_limits<int64_t>::max() / 16 : (int64_t)srv->cfg.chunk_work;
+            const int rc = launch_batch(srv, sl, batch, chunk, versions);
+            const float enq_ms = (float)((now_s() - t) * 1e3);
             lk.lock();
             for (size_t k = 0; k < batch.size(); ++k) {
                 Req *q = batch[k];
                 q->t.t_launch = t;
+                q->t.enqueue_ms = enq_ms;
                 q->t.batch_size = (int32_t)batch.size();
                 q->t.scene_version = k < versions.size() ? versions[k] : 0;
             }
@@ -429,13 +545,20 @@ extern "C" {
 
 int rpm_server_create(rpm_ctx *ctx, const rpm_server_config *cfg, rpm_server **out) {
     if (!ctx || !out) return fail(RPM_ERR_INVALID, "NULL argument");
-    rpm_server_config c{4, RPM_PREC_FP32_RECHECK, (int64_t)8 << 30, kMaxSegs, kDefaultBatchWork};
+    rpm_server_config c{kDefaultBulkSlots, RPM_PREC_FP32_RECHECK, (int64_t)8 << 30, kMaxSegs, kDefaultBatchWork,
+                        kDefaultExpressSlots, kDefaultExpressWork, kDefaultChunkWork, 0, 0};
     if (cfg) c = *cfg;
-    if (c.num_slots < 1 || c.num_slots > 64) return fail(RPM_ERR_INVALID, "num_slots must be 1..64");
+    if (c.num_slots == 0) c.num_slots = kDefaultBulkSlots;
+    if (c.express_slots == 0) c.express_slots = kDefaultExpressSlots;
+    if (c.num_slots < 1 || c.num_slots > 64 || c.express_slots < 1 || c.express_slots > 64)
+        return fail(RPM_ERR_INVALID, "num_slots and express_slots must be 1..64");
     if (c.precision < RPM_PREC_FP64 || c.precision > RPM_PREC_FP32_REF) return fail(RPM_ERR_INVALID, "unknown precision");
     if (c.max_batch_segments < 1 || c.max_batch_segments > kMaxSegs) c.max_batch_segments = kMaxSegs;
     if (c.max_batch_configs < 1) c.max_batch_configs = kDefaultBatchWork;
+    if (c.express_work < 1) c.express_work = kDefaultExpressWork;
+    if (c.chunk_work < 8) c.chunk_work = kDefaultChunkWork;
     if (c.memory_budget < (1 << 20)) return fail(RPM_ERR_INVALID, "memory budget below 1 MiB");
+    if (c.bulk_sms < 0) return fail(RPM_ERR_INVALID, "negative bulk_sms");
     rpm_server *srv = new rpm_server();
     srv->ctx = ctx;
     srv->cfg = c;
@@ -447,20 +570,31 @@ int rpm_server_create(rpm_ctx *ctx, const rpm_server_config *cfg, rpm_server **o
             return fail(RPM_ERR_NOMEM, "server arena of %lld bytes could not be allocated", (long long)c.memory_budget);
         }
         srv->arena.init((size_t)c.memory_budget);
-        srv->slots.resize(c.num_slots);
+        if (c.bulk_sms > 0) {
+            const int rc = make_partition(ctx->device, (unsigned)c.bulk_sms, srv->bulk_part);
+            if (rc) { cudaFree(srv->arena_mem); delete srv; return rc; }
+        }
+        srv->slots.resize(c.express_slots + c.num_slots);
         int lo_prio = 0, hi_prio = 0;
         CK(cudaDeviceGetStreamPriorityRange(&lo_prio, &hi_prio));
-        const int n_small = std::max(1, c.num_slots / 2);
-        for (int k = 0; k < c.num_slots; ++k) {
+        for (int k = 0; k < (int)srv->slots.size(); ++k) {
             Slot &sl = srv->slots[k];
-            sl.small = k < n_small && c.num_slots > 1;
-            CK(cudaStreamCreateWithPriority(&sl.st, cudaStreamNonBlocking, sl.small ? hi_prio : lo_prio));
-            CK(cudaEventCreateWithFlags(&sl.done, cudaEventDisableTiming));
+            sl.express = k < c.express_slots;
+            if (!sl.express && srv->bulk_part.g) {
+                CUstream cs = nullptr;
+                if (srv->bulk_part.stream_create(&cs, srv->bulk_part.g, CU_STREAM_NON_BLOCKING, lo_prio) != CUDA_SUCCESS)
+                    return fail(RPM_ERR_CUDA, "creating a stream in the bulk partition failed");
+                sl.st = (cudaStream_t)cs;
+            } else {
+                CK(cudaStreamCreateWithPriority(&sl.st, cudaStreamNonBlocking, sl.express ? hi_prio : lo_prio));
+            }
+            CK(cudaEventCreate(&sl.done));   // timed: the batch trace ends on it
+            for (cudaEvent_t &e : sl.trace) CK(cudaEventCreate(&e));
             Scratch *sc = nullptr;   // pre-size scratch so the loop never allocates
-            // sized for requests up to 262,144 configurations, which run as batches of their own
-            const int64_t presize = std::max<int64_t>(c.max_batch_configs, 1 << 18);
+            // express batches hold up to express_work units; bulk launches chunk_work units
+            const int64_t presize = sl.express ? c.express_work : c.chunk_work;
             int rc = get_scratch(ctx, sl.st, presize, &sc);
-            if (!rc) rc = edge_scratch(ctx, sc, presize / 4, sl.st);
+            if (!rc) rc = edge_scratch(ctx, sc, std::max<int64_t>(1, presize / 8), sl.st);
             if (rc) return rc;
         }
     }
@@ -559,16 +693,29 @@ int rpm_server_replay(rpm_server *srv, const rpm_request *reqs, const double *ar
             while (!done_submitting.load()) {
                 while (now_s() < next && !done_submitting.load()) std::this_thread::sleep_for(std::chrono::microseconds(50));
                 const float t = (float)(now_s() - t0);
+                // every moving scene of the period in one fused update
+                idx.clear();
+                ab.clear();
+                std::vector<std::pair<int32_t, int32_t>> spans;   // (scene, movers)
                 for (auto &kv : by_scene) {
-                    idx.clear();
-                    ab.clear();
                     for (const Mover *m : kv.second) {   // constant velocity (Environment::updateEnvironment, straight lines)
                         idx.push_back(m->idx);
                         for (int c = 0; c < 6; ++c) ab.push_back(m->a0[c] + m->v[c % 3] * t);
                     }
+                    spans.push_back({kv.first, (int32_t)kv.second.size()});
+                }
+                {
                     std::lock_guard<std::mutex> lk(srv->ctx->mu);
-                    SceneRec *s = find_scene(srv->ctx, kv.first);
-                    const int rc = s ? scene_update(srv->ctx, s, idx.data(), ab.data(), (int32_t)idx.size()) : RPM_ERR_INVALID;
+                    std::vector<SceneUpd> ups;
+                    size_t off = 0;
+                    int rc = RPM_OK;
+                    for (const auto &sp : spans) {
+                        SceneRec *s = find_scene(srv->ctx, sp.first);
+                        if (!s) { rc = RPM_ERR_INVALID; break; }
+                        ups.push_back(SceneUpd{s, idx.data() + off, ab.data() + 6 * off, sp.second});
+                        off += (size_t)sp.second;
+                    }
+                    if (!rc) rc = scene_update_many(srv->ctx, ups);
                     if (rc) upd_rc.store(rc);
                 }
                 next += period_s;
@@ -601,7 +748,7 @@ int rpm_server_stats(rpm_server *srv, int64_t *batches, int64_t *pending) {
     if (!srv) return fail(RPM_ERR_INVALID, "NULL argument");
     std::lock_guard<std::mutex> lk(srv->mu);
     if (batches) *batches = srv->batches;
-    if (pending) *pending = (int64_t)(srv->incoming.size() + srv->ready.size());
+    if (pending) *pending = (int64_t)(srv->incoming.size() + srv->express.size() + srv->bulk.size());
     return RPM_OK;
 }
 
@@ -625,10 +772,13 @@ int rpm_server_destroy(rpm_server *srv) {
                 free_scratch(it->second);
                 srv->ctx->scratch.erase(it);
             }
-            cudaStreamDestroy(sl.st);
+            if (!sl.express && srv->bulk_part.g) srv->bulk_part.stream_destroy((CUstream)sl.st);
+            else cudaStreamDestroy(sl.st);
             cudaEventDestroy(sl.done);
+            for (cudaEvent_t e : sl.trace) cudaEventDestroy(e);
         }
     }
+    if (srv->bulk_part.g) srv->bulk_part.destroy(srv->bulk_part.g);
     cudaFree(srv->arena_mem);
     for (auto &kv : srv->reqs) delete kv.second;
     delete srv;

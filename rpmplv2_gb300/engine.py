@@ -50,6 +50,7 @@ def load(build_if_missing=False):
     L.rpm_scene_create.argtypes = [_vp, _i32, _vp, _vp, _vp, _i32, _pi32]
     L.rpm_scene_update.argtypes = [_vp, _i32, _vp, _vp, _i32, ctypes.POINTER(ctypes.c_uint64)]
     L.rpm_scene_destroy.argtypes = [_vp, _i32]
+    L.rpm_scene_update_many.argtypes = [_vp, _i32, _vp, _vp, _vp, _vp, _vp]
     L.rpm_scene_info.argtypes = [_vp, _i32, _pi32, _pi32, ctypes.POINTER(ctypes.c_uint64)]
     L.rpm_box_aabb.argtypes = [_vp, _vp, _vp, _vp]
     L.rpm_check_configs.argtypes = [_vp, _i32, _i32, _vp, _i64, _vp, _vp, _vp, _vp]
@@ -147,6 +148,20 @@ class Engine:
         _check(self.lib.rpm_scene_update(self.ctx, scene_id, idx.ctypes.data, aabb.ctypes.data, idx.size,
                                          ctypes.byref(ver)))
         return ver.value
+
+    def update_scenes(self, updates):
+        """rpm_scene_update_many: updates is a list of (scene_id, idx, aabb);
+        returns the new versions."""
+        sids = np.array([u[0] for u in updates], np.int32)
+        counts = np.array([len(u[1]) for u in updates], np.int32)
+        idx = np.ascontiguousarray(np.concatenate([np.asarray(u[1], np.int32) for u in updates]) if updates else
+                                   np.zeros(0, np.int32), np.int32)
+        aabb = np.ascontiguousarray(np.concatenate([np.asarray(u[2], np.float32).reshape(-1, 6) for u in updates])
+                                    if updates else np.zeros((0, 6), np.float32), np.float32)
+        ver = np.zeros(len(updates), np.uint64)
+        _check(self.lib.rpm_scene_update_many(self.ctx, len(updates), sids.ctypes.data, counts.ctypes.data,
+                                              idx.ctypes.data, aabb.ctypes.data, ver.ctypes.data))
+        return [int(v) for v in ver]
 
     def destroy_scene(self, scene_id):
         _check(self.lib.rpm_scene_destroy(self.ctx, scene_id))
@@ -318,7 +333,7 @@ def box_aabb(dim, pos, quat_xyzw=(0.0, 0.0, 0.0, 1.0)):
 
 ABI_SYMBOLS = [
     "rpm_last_error_string", "rpm_version", "rpm_ctx_create", "rpm_ctx_destroy", "rpm_ctx_set_params",
-    "rpm_robot_upload", "rpm_scene_create", "rpm_scene_update", "rpm_scene_destroy", "rpm_scene_info",
+    "rpm_robot_upload", "rpm_scene_create", "rpm_scene_update", "rpm_scene_update_many", "rpm_scene_destroy", "rpm_scene_info",
     "rpm_box_aabb", "rpm_check_configs", "rpm_check_configs_host", "rpm_skeleton", "rpm_last_stats", "rpm_sync",
     "rpm_ctx_set_timing", "rpm_last_timing", "rpm_probe_fp32_peak", "rpm_probe_bounded_wait", "rpm_probe_primitives", "rpm_decision_margins", "rpm_robot_builtin", "rpm_check_configs_noalloc", "rpm_check_batch",
     "rpm_check_edges", "rpm_check_edges_batch", "rpm_ctx_set_graphs", "rpm_autotune_edges", "rpm_set_edge_ctas", "rpm_ctx_set_layout",

@@ -17,7 +17,9 @@ RPM_REQ_EDGES = 1
 
 class ServerConfig(ctypes.Structure):
     _fields_ = [("num_slots", ctypes.c_int32), ("precision", ctypes.c_int32), ("memory_budget", ctypes.c_int64),
-                ("max_batch_segments", ctypes.c_int32), ("max_batch_configs", ctypes.c_int32)]
+                ("max_batch_segments", ctypes.c_int32), ("max_batch_configs", ctypes.c_int32),
+                ("express_slots", ctypes.c_int32), ("express_work", ctypes.c_int32), ("chunk_work", ctypes.c_int32),
+                ("bulk_sms", ctypes.c_int32), ("reserved", ctypes.c_int32)]
 
 
 class Request(ctypes.Structure):
@@ -30,7 +32,8 @@ class Request(ctypes.Structure):
 class Timing(ctypes.Structure):
     _fields_ = [("status", ctypes.c_int32), ("batch_size", ctypes.c_int32), ("t_submit", ctypes.c_double),
                 ("t_admit", ctypes.c_double), ("t_launch", ctypes.c_double), ("t_done", ctypes.c_double),
-                ("scene_version", ctypes.c_uint64)]
+                ("scene_version", ctypes.c_uint64), ("h2d_ms", ctypes.c_float), ("kernel_ms", ctypes.c_float),
+                ("d2h_ms", ctypes.c_float), ("enqueue_ms", ctypes.c_float)]
 
 
 class Motion(ctypes.Structure):
@@ -69,13 +72,17 @@ def pinned(shape, dtype):
 
 
 class Server:
-    def __init__(self, engine, num_slots=4, precision="fp32_recheck", memory_budget=8 << 30, max_batch_segments=32,
-                 max_batch_configs=1 << 15):
+    def __init__(self, engine, num_slots=0, precision="fp32_recheck", memory_budget=8 << 30, max_batch_segments=32,
+                 max_batch_configs=0, express_slots=0, express_work=0, chunk_work=0, bulk_sms=0):
+        """num_slots bulk streams, express_slots high-priority streams, and
+        optionally an SM partition of bulk_sms SMs for the bulk streams; 0
+        takes the library's defaults (rpm_server_config)."""
         from ._abi import PRECISIONS
         self.engine = engine
         self.lib = load()
         _bind(self.lib)
-        cfg = ServerConfig(num_slots, PRECISIONS[precision], memory_budget, max_batch_segments, max_batch_configs)
+        cfg = ServerConfig(num_slots, PRECISIONS[precision], memory_budget, max_batch_segments, max_batch_configs,
+                           express_slots, express_work, chunk_work, bulk_sms, 0)
         self.srv = _vp()
         _check(self.lib.rpm_server_create(engine.ctx, ctypes.byref(cfg), ctypes.byref(self.srv)))
 

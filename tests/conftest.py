@@ -3,6 +3,9 @@ import sys
 
 import pytest
 
+# separate hardware queues for the serving loop's streams (before any CUDA context exists)
+os.environ.setdefault("CUDA_DEVICE_MAX_CONNECTIONS", "32")
+
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 if ROOT not in sys.path:
     sys.path.insert(0, ROOT)
