@@ -377,15 +377,15 @@ def large_line(eng, scenes, timed):
 def serve_line(eng, serve):
     """The serving replay: 20,000 requests/s for 0.5 s over 64 resident scenes."""
     wl = serve.serving_workload(eng, seed=4, rate=20000.0, duration=0.5)
-    srv = serve.Server(eng)   # the library's defaults: 3 bulk streams, 8 express streams
+    srv = serve.Server(eng)   # the library's defaults (rpm_server_config)
     srv.replay(wl["requests"][:200], [0.0] * 200)
     tim = srv.replay(wl["requests"], wl["arrivals"], wl["motions"], period=0.001)
     summ = serve.latency_summary(tim, wl["meta"])
     summ.update({"workload": "64 resident scenes (robots of configs 0-3, 10-1000 boxes log-uniform, 20% with 5 "
                              "boxes moving up to 1.6 m/s updated every 1 ms), Poisson 20,000 req/s for 0.5 s, "
                              "sizes log-uniform 1-65,536, isValid / distance / edge in equal shares",
-                 "memory_budget_bytes": 8 << 30, "bulk_slots": 3, "express_slots": 8, "express_work": 8192,
-                 "chunk_work": 16384})
+                 "memory_budget_bytes": 8 << 30, "bulk_slots": 4, "express_slots": 24, "express_work": 8192,
+                 "chunk_work": 65536, "bulk_sms": "all but 32 (green context)"})
     # capacity: the same trace submitted at once; latency at a rate the engine sustains
     t = srv.replay(wl["requests"], [0.0] * len(wl["requests"]))
     summ["capacity_req_per_s"] = len(t) / max(x.t_done for x in t)

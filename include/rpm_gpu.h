@@ -420,17 +420,18 @@ int rpm_random_scenario_read(const char *path, int32_t num_obstacles, int32_t ru
  * hardware queues. */
 typedef struct rpm_server rpm_server;
 typedef struct rpm_server_config {
-    int32_t num_slots;           /* bulk streams (concurrent bulk batches); 0: 3 */
+    int32_t num_slots;           /* bulk streams (concurrent bulk batches); 0: 4 */
     int32_t precision;           /* RPM_PREC_* of every request */
     int64_t memory_budget;       /* device bytes for request buffers (admission), default 8 GiB */
     int32_t max_batch_segments;  /* configuration requests and edge requests per batch, each <= 32 */
     int32_t max_batch_configs;   /* work per bulk batch; 0: 65,536 (a larger request runs as a batch of its own) */
-    int32_t express_slots;       /* high-priority streams for express requests; 0: 8 */
+    int32_t express_slots;       /* high-priority streams for express requests; 0: 24 */
     int32_t express_work;        /* largest express request; 0: 8,192 */
-    int32_t chunk_work;          /* work per bulk launch; 0: 16,384 */
+    int32_t chunk_work;          /* work per bulk launch; 0: 65,536 */
     int32_t bulk_sms;            /* > 0: the bulk streams run in an SM partition (a green context) of this
                                     many SMs (rounded up to the driver's granularity, 8 on GB300), so the
-                                    other SMs only run express work; 0: bulk uses every SM */
+                                    other SMs only run express work; 0: all SMs but 32 where the driver
+                                    offers green contexts, else every SM; -1: bulk uses every SM */
     int32_t reserved;
 } rpm_server_config;
 

@@ -4,7 +4,8 @@
 // Serving model (DRGBT-style replanning, apps/test_drgbt_random_obstacles.cpp
 // and DRGBT.cpp:79-176, as a service): planners submit isValid / distance
 // batches and edge batches of any size against resident scenes while moving
-// obstacles are updated every few milliseconds.  One worker thread
+// obstacles are updated every few milliseconds.  Two worker threads (one per
+// class below)
 //   * admits requests in arrival order as device memory of the budget frees up
 //     (a request larger than the whole budget is rejected), skipping over
 //     requests that do not fit yet so small ones are not held behind large ones;
@@ -183,14 +184,23 @@ struct Slot {
     std::vector<Req *> reqs;
     bool busy = false;
     bool express = false;   // high-priority stream for small requests
+    bool finished = false;   // set (under srv->mu) by the stream's host callback at the end of the batch
+    void *srv = nullptr;
 };
 
 // Defaults of rpm_server_config (a field of 0 takes its default).
-constexpr int32_t kDefaultBulkSlots = 3;
-constexpr int32_t kDefaultExpressSlots = 8;
+// Chosen on the serving trace (64 scenes, Poisson 12k and 20k requests/s,
+// sizes 1-65,536): 4 bulk streams in chunks of 65,536 units held capacity
+// (16.1k req/s with the partition below) while 24 express streams kept express
+// requests from queueing for a stream (queue p99 0.18 ms at 12k req/s).
+constexpr int32_t kDefaultBulkSlots = 4;
+constexpr int32_t kDefaultExpressSlots = 24;
 constexpr int32_t kDefaultExpressWork = 8192;   // units: configurations, an edge counting 8
 constexpr int32_t kDefaultBatchWork = 1 << 16;  // bulk batch
-constexpr int32_t kDefaultChunkWork = 1 << 14;  // bulk launch
+constexpr int32_t kDefaultChunkWork = 1 << 16;  // bulk launch
+// Default bulk partition: all SMs but this many stay free of bulk work (p99 of
+// 2k-8k requests at 12k req/s: 1.27 ms with 16 free, 1.21 ms with 32).
+constexpr int32_t kDefaultExpressOnlySms = 32;
 constexpr int64_t kExpressShared = 1024;        // express requests below this share batches
 
 int64_t work_of(const Req *q) { return q->r.kind == RPM_REQ_EDGES ? 8 * q->r.count : q->r.count; }
@@ -258,7 +268,7 @@ struct rpm_server {
     std::vector<Slot> slots;
     std::unordered_map<uint64_t, Req *> reqs;
     uint64_t next_ticket = 1;
-    std::thread worker;
+    std::thread worker, bulk_worker;
     bool stop = false;
     int64_t batches = 0;
     GreenPartition bulk_part;   // bulk streams' SMs (when cfg.bulk_sms > 0)
@@ -305,6 +315,19 @@ DevBufs layout(rpm_server *srv, const Req *q) {
     if (q->r.dist_host) { d.dist = reinterpret_cast<double *>(p); p += Arena::round(n * sizeof(double)); }
     if (q->r.profile_host) d.profile = reinterpret_cast<float *>(p);
     return d;
+}
+
+// Host callback at the end of a batch's stream work: marks the slot finished
+// and wakes the workers, so they sleep instead of polling events.  It calls no
+// CUDA function.
+void CUDART_CB batch_done(void *arg) {
+    Slot *sl = static_cast<Slot *>(arg);
+    rpm_server *srv = static_cast<rpm_server *>(sl->srv);
+    {
+        std::lock_guard<std::mutex> lk(srv->mu);
+        sl->finished = true;
+    }
+    srv->cv_work.notify_all();
 }
 
 // Launch one batch on a reserved slot: copies in, the checks as launches of at
@@ -423,17 +446,23 @@ int launch_batch(rpm_server *srv, Slot &slot, const std::vector<Req *> &batch, i
         }
     }
     CK(cudaEventRecord(slot.done, slot.st));
+    CK(cudaLaunchHostFunc(slot.st, batch_done, &slot));
     return RPM_OK;
 }
 
-void worker_loop(rpm_server *srv) {
+// One worker per class: the express worker retires and launches the express
+// slots, the bulk worker the bulk slots, so enqueueing a bulk batch never holds
+// up an express launch on the host.  Either admits new requests.
+void worker_loop(rpm_server *srv, bool express) {
     cudaSetDevice(srv->ctx->device);
     std::unique_lock<std::mutex> lk(srv->mu);
     while (!srv->stop) {
         bool progress = false;
         // ---- retire finished batches
         for (Slot &sl : srv->slots) {
-            if (!sl.busy || cudaEventQuery(sl.done) != cudaSuccess) continue;
+            if (sl.express != express) continue;
+            if (!sl.busy || !sl.finished) continue;
+            sl.finished = false;
             const double t = now_s();
             float ms[3] = {0.f, 0.f, 0.f};
             cudaEventElapsedTime(&ms[0], sl.trace[0], sl.trace[1]);
@@ -476,7 +505,7 @@ void worker_loop(rpm_server *srv) {
         // ---- launch: express slots take express requests, bulk slots bulk
         //      requests, each class in arrival order
         for (Slot &sl : srv->slots) {
-            if (sl.busy) continue;
+            if (sl.express != express || sl.busy) continue;
             std::deque<Req *> &queue = sl.express ? srv->express : srv->bulk;
             if (queue.empty()) continue;
             // an express batch is one request, or several requests smaller than
@@ -515,6 +544,7 @@ void worker_loop(rpm_server *srv) {
                 // work already queued for the batch may still use its memory: let it finish first
                 cudaStreamSynchronize(sl.st);
                 cudaGetLastError();
+                sl.finished = false;   // a callback enqueued before the failure may have run
                 const double te = now_s();
                 for (Req *q : batch) { q->t.status = rc; q->t.t_done = te; srv->arena.release(q->off, q->bytes); }
                 sl.busy = false;
@@ -525,17 +555,8 @@ void worker_loop(rpm_server *srv) {
             }
             progress = true;
         }
-        if (!progress) {
-            bool busy = false;
-            for (Slot &sl : srv->slots) busy = busy || sl.busy;
-            if (busy) {
-                lk.unlock();
-                std::this_thread::yield();
-                lk.lock();
-            } else {
-                srv->cv_work.wait_for(lk, std::chrono::microseconds(200));
-            }
-        }
+        if (progress) srv->cv_work.notify_all();   // the other worker may have new work or memory
+        else srv->cv_work.wait_for(lk, std::chrono::milliseconds(2));   // woken by submissions and batch ends
     }
 }
 
@@ -558,7 +579,7 @@ int rpm_server_create(rpm_ctx *ctx, const rpm_server_config *cfg, rpm_server **o
     if (c.express_work < 1) c.express_work = kDefaultExpressWork;
     if (c.chunk_work < 8) c.chunk_work = kDefaultChunkWork;
     if (c.memory_budget < (1 << 20)) return fail(RPM_ERR_INVALID, "memory budget below 1 MiB");
-    if (c.bulk_sms < 0) return fail(RPM_ERR_INVALID, "negative bulk_sms");
+    if (c.bulk_sms < -1) return fail(RPM_ERR_INVALID, "bulk_sms below -1");
     rpm_server *srv = new rpm_server();
     srv->ctx = ctx;
     srv->cfg = c;
@@ -573,6 +594,11 @@ int rpm_server_create(rpm_ctx *ctx, const rpm_server_config *cfg, rpm_server **o
         if (c.bulk_sms > 0) {
             const int rc = make_partition(ctx->device, (unsigned)c.bulk_sms, srv->bulk_part);
             if (rc) { cudaFree(srv->arena_mem); delete srv; return rc; }
+        } else if (c.bulk_sms == 0 && ctx->num_sms > 2 * kDefaultExpressOnlySms) {
+            // the default partition where the driver offers green contexts; bulk
+            // work uses every SM where it does not
+            if (make_partition(ctx->device, (unsigned)(ctx->num_sms - kDefaultExpressOnlySms), srv->bulk_part) != RPM_OK)
+                srv->bulk_part = GreenPartition{};
         }
         srv->slots.resize(c.express_slots + c.num_slots);
         int lo_prio = 0, hi_prio = 0;
@@ -580,6 +606,7 @@ int rpm_server_create(rpm_ctx *ctx, const rpm_server_config *cfg, rpm_server **o
         for (int k = 0; k < (int)srv->slots.size(); ++k) {
             Slot &sl = srv->slots[k];
             sl.express = k < c.express_slots;
+            sl.srv = srv;
             if (!sl.express && srv->bulk_part.g) {
                 CUstream cs = nullptr;
                 if (srv->bulk_part.stream_create(&cs, srv->bulk_part.g, CU_STREAM_NON_BLOCKING, lo_prio) != CUDA_SUCCESS)
@@ -598,7 +625,8 @@ int rpm_server_create(rpm_ctx *ctx, const rpm_server_config *cfg, rpm_server **o
             if (rc) return rc;
         }
     }
-    srv->worker = std::thread(worker_loop, srv);
+    srv->worker = std::thread(worker_loop, srv, true);
+    srv->bulk_worker = std::thread(worker_loop, srv, false);
     *out = srv;
     return RPM_OK;
 }
@@ -624,7 +652,7 @@ int rpm_server_submit(rpm_server *srv, const rpm_request *r, uint64_t *ticket) {
         srv->reqs[q->ticket] = q;
         srv->incoming.push_back(q);
     }
-    srv->cv_work.notify_one();
+    srv->cv_work.notify_all();
     *ticket = q->ticket;
     return RPM_OK;
 }
@@ -760,6 +788,7 @@ int rpm_server_destroy(rpm_server *srv) {
     }
     srv->cv_work.notify_all();
     if (srv->worker.joinable()) srv->worker.join();
+    if (srv->bulk_worker.joinable()) srv->bulk_worker.join();
     cudaSetDevice(srv->ctx->device);
     for (Slot &sl : srv->slots) {
         if (sl.st) cudaStreamSynchronize(sl.st);

@@ -157,3 +157,41 @@ def test_results_under_moving_obstacles_match_the_oracle(engine):
     srv.close()
     for st in setups:
         engine.destroy_scene(st["sid"])
+
+
+def test_update_many_scenes_in_one_launch(engine):
+    """rpm_scene_update_many writes the next version of several scenes with one
+    launch: each scene's checks then equal the oracle on its moved AABBs, and
+    a scene listed twice is refused."""
+    import torch
+    from oracle import oracle as O
+    from rpmplv2_gb300 import scenes, serve
+    from rpmplv2_gb300.engine import RpmError
+    rng = np.random.default_rng(45)
+    setups = []
+    for name, n in (("xarm6", 40), ("spatial_14dof", 300), ("planar_2dof", 9)):
+        robot = serve.make_robot(name)
+        sc = serve._scene_for(robot, rng, n)
+        sid = engine.create_scene(engine.upload_robot(robot), sc)
+        setups.append((robot, sc, sid))
+    v0 = [engine.update_scenes([(sid, [], np.zeros((0, 6)))])[0] for _, _, sid in setups]
+    ups = []
+    for robot, sc, sid in setups:
+        first = 1 if robot.name == "xarm6" else 0
+        idx = rng.choice(np.arange(first, sc.n), size=min(7, sc.n - first), replace=False).astype(np.int32)
+        sc.aabb[idx] += rng.uniform(-0.1, 0.1, (len(idx), 1)).astype(np.float32)
+        ups.append((sid, idx, sc.aabb[idx]))
+    vers = engine.update_scenes(ups)
+    assert vers == [v + 1 for v in v0]
+    for robot, sc, sid in setups:
+        q = scenes.uniform_configs(rng, 2048, robot.num_dofs)
+        v = torch.zeros(2048, dtype=torch.uint8, device="cuda")
+        d = torch.zeros(2048, dtype=torch.float64, device="cuda")
+        engine.check_configs(sid, torch.from_numpy(q).cuda(), "fp32_recheck", v, d)
+        engine.sync()
+        rv, rd, _ = O.check_configs(robot, sc, q, prec="ref64", want=("valid", "dist"))
+        assert np.array_equal(v.cpu().numpy(), rv) and np.abs(d.cpu().numpy() - rd).max() <= 1e-5
+    with pytest.raises(RpmError):
+        engine.update_scenes([ups[0], ups[0]])
+    for _, _, sid in setups:
+        engine.destroy_scene(sid)
