@@ -383,7 +383,8 @@ def serve_line(eng, serve):
     summ = serve.latency_summary(tim, wl["meta"])
     summ.update({"workload": "64 resident scenes (robots of configs 0-3, 10-1000 boxes log-uniform, 20% with 5 "
                              "boxes moving up to 1.6 m/s updated every 1 ms), Poisson 20,000 req/s for 0.5 s, "
-                             "sizes log-uniform 1-65,536, isValid / distance / edge in equal shares",
+                             "sizes log-uniform 1-65,536, isValid / distance / edge in equal shares, of which 10% "
+                             "replaced by DRGBT steps (horizon of reached states, MotionValidity with moving boxes)",
                  "memory_budget_bytes": 8 << 30, "bulk_slots": 4, "express_slots": 24, "express_work": 8192,
                  "chunk_work": 65536, "bulk_sms": "all but 32 (green context)"})
     # capacity: the same trace submitted at once; latency at a rate the engine sustains
@@ -395,7 +396,8 @@ def serve_line(eng, serve):
     t12 = srv.replay(wl12["requests"], wl12["arrivals"], wl12["motions"], period=0.001)
     s12 = serve.latency_summary(t12, wl12["meta"])
     summ["at_12000_req_per_s"] = {k: s12[k] for k in ("queries_per_s", "p50_ms", "p99_ms", "p50_ms_4096", "p99_ms_4096",
-                                                      "p99_ms_le4096", "median_run_ms")}
+                                                      "p99_ms_le4096", "median_run_ms", "drgbt_horizon",
+                                                      "motion_validity")}
     wl = wl12
     srv.close()
     for sid in wl["scene_ids"]:

@@ -435,7 +435,10 @@ typedef struct rpm_server_config {
     int32_t reserved;
 } rpm_server_config;
 
-enum rpm_request_kind { RPM_REQ_CONFIGS = 0, RPM_REQ_EDGES = 1 };
+/* Request kinds: configuration checks, edge checks, and the two DRGBT
+ * replanning steps (DRGBT.cpp:272-320, 475-495; MotionValidity.cpp:30-53),
+ * which go through the same admission, classes and streams. */
+enum rpm_request_kind { RPM_REQ_CONFIGS = 0, RPM_REQ_EDGES = 1, RPM_REQ_REACHED = 2, RPM_REQ_MOTION = 3 };
 
 typedef struct rpm_request {
     int32_t kind;                /* enum rpm_request_kind */
@@ -449,7 +452,22 @@ typedef struct rpm_request {
     uint8_t *valid_host;         /* isValid (required for EDGES) */
     double *dist_host;           /* CONFIGS, nullable */
     float *profile_host;         /* CONFIGS, nullable */
-    int32_t *checks_host;        /* EDGES, nullable */
+    int32_t *checks_host;        /* EDGES, MOTION: nullable */
+    /* REACHED (rpm_reached_states over a horizon of count states): q_host is
+     * q_current (1 x D), q1_host the horizon (count x D); outputs q_out_host
+     * (count x D), status_host (count) and dist_host (nullable; in the
+     * server's precision) */
+    const rpm_spine_params *spine;
+    float *q_out_host;
+    int32_t *status_host;
+    /* MOTION (rpm_motion_validity of count motions q1_host -> q2_host while
+     * the boxes move; FP64, or the reference's numerics when the server runs
+     * RPM_PREC_FP32_REF): outputs valid_host, checks_host */
+    const rpm_moving_box *boxes;
+    int32_t num_boxes;
+    int32_t num_points;
+    float max_iter_time;
+    int32_t reserved;
 } rpm_request;
 
 typedef struct rpm_request_timing {

@@ -1168,15 +1168,19 @@ int rpm_extend_spines(rpm_ctx *ctx, int32_t robot_id, const float *q_dev, const 
     return RPM_OK;
 }
 
-int rpm_reached_states(rpm_ctx *ctx, int32_t scene_id, int32_t precision, const float *q_current_dev,
-                       const float *horizon_dev, int64_t horizon_size, const rpm_spine_params *params,
-                       float *q_reached_dev, int32_t *status_dev, double *dist_dev, void *stream) {
+}  // extern "C"
+
+namespace rpm {
+namespace impl {
+// rpm_reached_states with ctx->mu held (the C entry point and the server's
+// DRGBT requests).
+int reached_states_locked(rpm_ctx *ctx, int32_t scene_id, int32_t precision, const float *q_current_dev,
+                          const float *horizon_dev, int64_t horizon_size, const rpm_spine_params *params,
+                          float *q_reached_dev, int32_t *status_dev, double *dist_dev, cudaStream_t st) {
     if (!ctx || !params || horizon_size < 0 || !q_current_dev ||
         (horizon_size > 0 && (!horizon_dev || !q_reached_dev || !status_dev)))
         return fail(RPM_ERR_INVALID, "bad arguments");
     if (params->num_iter < 1 || params->num_layers < 0) return fail(RPM_ERR_INVALID, "num_iter >= 1 and num_layers >= 0");
-    std::lock_guard<std::mutex> lk(ctx->mu);
-    cudaStream_t st = (cudaStream_t)stream;
     NearParams np;
     SceneBuf *buf = nullptr;
     int rc = near_setup(ctx, scene_id, RPM_PREC_FP32_REF, q_current_dev, 1, st, np, &buf);
@@ -1221,18 +1225,36 @@ int rpm_reached_states(rpm_ctx *ctx, int32_t scene_id, int32_t precision, const 
         return enqueue_check(ctx, s, precision, q_reached_dev, horizon_size, nullptr, dist_dev, nullptr, st);
     return RPM_OK;
 }
+}  // namespace impl
+}  // namespace rpm
 
-int rpm_motion_validity(rpm_ctx *ctx, int32_t scene_id, int32_t precision, const float *q_prev_dev,
-                        const float *q_cur_dev, int64_t num_motions, const rpm_moving_box *boxes, int32_t num_boxes,
-                        float max_iter_time, int32_t num_points, uint8_t *valid_dev, int32_t *checks_dev, void *stream) {
+extern "C" {
+
+int rpm_reached_states(rpm_ctx *ctx, int32_t scene_id, int32_t precision, const float *q_current_dev,
+                       const float *horizon_dev, int64_t horizon_size, const rpm_spine_params *params,
+                       float *q_reached_dev, int32_t *status_dev, double *dist_dev, void *stream) {
+    if (!ctx) return fail(RPM_ERR_INVALID, "bad arguments");
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    return reached_states_locked(ctx, scene_id, precision, q_current_dev, horizon_dev, horizon_size, params,
+                                 q_reached_dev, status_dev, dist_dev, (cudaStream_t)stream);
+}
+
+}  // extern "C"
+
+namespace rpm {
+namespace impl {
+// rpm_motion_validity with ctx->mu held (the C entry point and the server's
+// DRGBT requests).
+int motion_validity_locked(rpm_ctx *ctx, int32_t scene_id, int32_t precision, const float *q_prev_dev,
+                           const float *q_cur_dev, int64_t num_motions, const rpm_moving_box *boxes, int32_t num_boxes,
+                           float max_iter_time, int32_t num_points, uint8_t *valid_dev, int32_t *checks_dev,
+                           cudaStream_t st) {
     if (!ctx || num_motions < 0 || num_boxes < 0 || (num_boxes > 0 && !boxes) ||
         (num_motions > 0 && (!q_prev_dev || !q_cur_dev || !valid_dev)))
         return fail(RPM_ERR_INVALID, "bad arguments");
     if (precision != RPM_PREC_FP64 && precision != RPM_PREC_FP32_REF)
         return fail(RPM_ERR_INVALID, "motion validity runs RPM_PREC_FP64 or RPM_PREC_FP32_REF");
     if (num_points < 1) return fail(RPM_ERR_INVALID, "num_points must be >= 1");
-    std::lock_guard<std::mutex> lk(ctx->mu);
-    cudaStream_t st = (cudaStream_t)stream;
     NearParams np;
     SceneBuf *buf = nullptr;
     int rc = near_setup(ctx, scene_id, precision, q_prev_dev, num_motions, st, np, &buf);
@@ -1286,6 +1308,19 @@ int rpm_motion_validity(rpm_ctx *ctx, int32_t scene_id, int32_t precision, const
     p.checks = checks_dev;
     CK(launch_motion_validity(precision, p, st));
     return near_done(ctx, buf, st);
+}
+}  // namespace impl
+}  // namespace rpm
+
+extern "C" {
+
+int rpm_motion_validity(rpm_ctx *ctx, int32_t scene_id, int32_t precision, const float *q_prev_dev,
+                        const float *q_cur_dev, int64_t num_motions, const rpm_moving_box *boxes, int32_t num_boxes,
+                        float max_iter_time, int32_t num_points, uint8_t *valid_dev, int32_t *checks_dev, void *stream) {
+    if (!ctx) return fail(RPM_ERR_INVALID, "bad arguments");
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    return motion_validity_locked(ctx, scene_id, precision, q_prev_dev, q_cur_dev, num_motions, boxes, num_boxes,
+                                  max_iter_time, num_points, valid_dev, checks_dev, (cudaStream_t)stream);
 }
 
 int rpm_scene_move_straight(rpm_ctx *ctx, int32_t scene_id, rpm_moving_box *boxes, int32_t num_boxes, float delta_time,

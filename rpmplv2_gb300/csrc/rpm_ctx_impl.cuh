@@ -205,6 +205,14 @@ struct SceneUpd {
 int scene_update_many(rpm_ctx *ctx, const std::vector<SceneUpd> &u);
 int scene_update(rpm_ctx *ctx, SceneRec *s, const int32_t *idx, const float *aabb, int32_t m);
 cudaError_t launch_scene_update_many(const UpdDesc *descs, int count, cudaStream_t st);
+// The DRGBT steps with ctx->mu held (rpm_reached_states, rpm_motion_validity).
+int reached_states_locked(rpm_ctx *ctx, int32_t scene_id, int32_t precision, const float *q_current_dev,
+                          const float *horizon_dev, int64_t horizon_size, const rpm_spine_params *params,
+                          float *q_reached_dev, int32_t *status_dev, double *dist_dev, cudaStream_t st);
+int motion_validity_locked(rpm_ctx *ctx, int32_t scene_id, int32_t precision, const float *q_prev_dev,
+                           const float *q_cur_dev, int64_t num_motions, const rpm_moving_box *boxes, int32_t num_boxes,
+                           float max_iter_time, int32_t num_points, uint8_t *valid_dev, int32_t *checks_dev,
+                           cudaStream_t st);
 // Spatially sorted copy: Morton order of the obstacle centres (fixed for the
 // scene's lifetime), its size, and the kernel that rebuilds it in a version.
 void sorted_layout(SceneRec &s);

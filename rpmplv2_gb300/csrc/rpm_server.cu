@@ -203,7 +203,16 @@ constexpr int32_t kDefaultChunkWork = 1 << 16;  // bulk launch
 constexpr int32_t kDefaultExpressOnlySms = 32;
 constexpr int64_t kExpressShared = 1024;        // express requests below this share batches
 
-int64_t work_of(const Req *q) { return q->r.kind == RPM_REQ_EDGES ? 8 * q->r.count : q->r.count; }
+// Units of work: a configuration 1, an edge 8, a horizon state (spines,
+// underestimations and a distance) 64, a motion one per validity point.
+int64_t work_of(const Req *q) {
+    switch (q->r.kind) {
+    case RPM_REQ_EDGES: return 8 * q->r.count;
+    case RPM_REQ_REACHED: return 64 * q->r.count;
+    case RPM_REQ_MOTION: return (int64_t)std::max(1, q->r.num_points) * q->r.count;
+    default: return q->r.count;
+    }
+}
 
 // An SM partition for the bulk streams (a green context of the device's
 // primary context).  Its driver calls are reached through the runtime's driver
@@ -278,8 +287,11 @@ namespace {
 
 size_t request_bytes(const rpm_request &r, int D, int L) {
     const size_t n = (size_t)r.count;
-    if (r.kind == RPM_REQ_EDGES)
+    if (r.kind == RPM_REQ_EDGES || r.kind == RPM_REQ_MOTION)
         return Arena::round(2 * n * D * sizeof(float)) + Arena::round(n) + Arena::round(n * sizeof(int32_t));
+    if (r.kind == RPM_REQ_REACHED)
+        return Arena::round(D * sizeof(float)) + 2 * Arena::round(n * D * sizeof(float)) +
+               Arena::round(n * sizeof(int32_t)) + (r.dist_host ? Arena::round(n * sizeof(double)) : 0);
     size_t b = Arena::round(n * D * sizeof(float));
     if (r.valid_host) b += Arena::round(n);
     if (r.dist_host) b += Arena::round(n * sizeof(double));
@@ -289,24 +301,36 @@ size_t request_bytes(const rpm_request &r, int D, int L) {
 
 // Device pointers of a request's buffers inside the arena.
 struct DevBufs {
-    float *q = nullptr, *q1 = nullptr, *q2 = nullptr;
+    float *q = nullptr, *q1 = nullptr, *q2 = nullptr, *q_out = nullptr;
     uint8_t *valid = nullptr;
     double *dist = nullptr;
     float *profile = nullptr;
-    int32_t *checks = nullptr;
+    int32_t *checks = nullptr, *status = nullptr;
 };
 
 DevBufs layout(rpm_server *srv, const Req *q) {
     char *p = srv->arena_mem + q->off;
     const size_t n = (size_t)q->r.count;
     DevBufs d;
-    if (q->r.kind == RPM_REQ_EDGES) {
+    if (q->r.kind == RPM_REQ_EDGES || q->r.kind == RPM_REQ_MOTION) {
         d.q1 = reinterpret_cast<float *>(p);
         d.q2 = d.q1 + n * q->D;
         p += Arena::round(2 * n * q->D * sizeof(float));
         d.valid = reinterpret_cast<uint8_t *>(p);
         p += Arena::round(n);
         d.checks = reinterpret_cast<int32_t *>(p);
+        return d;
+    }
+    if (q->r.kind == RPM_REQ_REACHED) {
+        d.q = reinterpret_cast<float *>(p);   // q_current
+        p += Arena::round(q->D * sizeof(float));
+        d.q1 = reinterpret_cast<float *>(p);  // horizon
+        p += Arena::round(n * q->D * sizeof(float));
+        d.q_out = reinterpret_cast<float *>(p);
+        p += Arena::round(n * q->D * sizeof(float));
+        d.status = reinterpret_cast<int32_t *>(p);
+        p += Arena::round(n * sizeof(int32_t));
+        if (q->r.dist_host) d.dist = reinterpret_cast<double *>(p);
         return d;
     }
     d.q = reinterpret_cast<float *>(p);
@@ -351,9 +375,12 @@ int launch_batch(rpm_server *srv, Slot &slot, const std::vector<Req *> &batch, i
         if (!s) return fail(RPM_ERR_INVALID, "unknown scene %d", q->r.scene_id);
         scene[k] = s;
         versions[k] = s->version;   // the launches read s->cur, made current with this version
-        if (q->r.kind == RPM_REQ_EDGES) {
+        if (q->r.kind == RPM_REQ_EDGES || q->r.kind == RPM_REQ_MOTION) {
             CK(cudaMemcpyAsync(d.q1, q->r.q1_host, n * q->D * sizeof(float), cudaMemcpyHostToDevice, slot.st));
             CK(cudaMemcpyAsync(d.q2, q->r.q2_host, n * q->D * sizeof(float), cudaMemcpyHostToDevice, slot.st));
+        } else if (q->r.kind == RPM_REQ_REACHED) {
+            CK(cudaMemcpyAsync(d.q, q->r.q_host, q->D * sizeof(float), cudaMemcpyHostToDevice, slot.st));
+            CK(cudaMemcpyAsync(d.q1, q->r.q1_host, n * q->D * sizeof(float), cudaMemcpyHostToDevice, slot.st));
         } else {
             CK(cudaMemcpyAsync(d.q, q->r.q_host, n * q->D * sizeof(float), cudaMemcpyHostToDevice, slot.st));
         }
@@ -371,7 +398,7 @@ int launch_batch(rpm_server *srv, Slot &slot, const std::vector<Req *> &batch, i
     };
     for (size_t k = 0; k < batch.size(); ++k) {
         const Req *q = batch[k];
-        if (q->r.kind == RPM_REQ_EDGES) continue;
+        if (q->r.kind != RPM_REQ_CONFIGS) continue;
         const DevBufs d = layout(srv, q);
         for (int64_t first = 0; first < q->r.count;) {
             const int64_t cnt = std::min(q->r.count - first, chunk - segw);
@@ -431,12 +458,32 @@ int launch_batch(rpm_server *srv, Slot &slot, const std::vector<Req *> &batch, i
             b->users.push_back(e);
         }
     }
+    // the DRGBT steps, one call per request
+    for (size_t k = 0; k < batch.size(); ++k) {
+        const Req *q = batch[k];
+        const DevBufs d = layout(srv, q);
+        if (q->r.kind == RPM_REQ_REACHED) {
+            rc = reached_states_locked(ctx, q->r.scene_id, srv->cfg.precision, d.q, d.q1, q->r.count, q->r.spine,
+                                       d.q_out, d.status, d.dist, slot.st);
+        } else if (q->r.kind == RPM_REQ_MOTION) {
+            const int32_t prec = srv->cfg.precision == RPM_PREC_FP32_REF ? RPM_PREC_FP32_REF : RPM_PREC_FP64;
+            rc = motion_validity_locked(ctx, q->r.scene_id, prec, d.q1, d.q2, q->r.count, q->r.boxes, q->r.num_boxes,
+                                        q->r.max_iter_time, q->r.num_points, d.valid, d.checks, slot.st);
+        }
+        if (rc) return rc;
+    }
     CK(cudaEventRecord(slot.trace[2], slot.st));
     for (Req *q : batch) {
         const DevBufs d = layout(srv, q);
         const size_t n = (size_t)q->r.count;
+        if (q->r.kind == RPM_REQ_REACHED) {
+            CK(cudaMemcpyAsync(q->r.q_out_host, d.q_out, n * q->D * sizeof(float), cudaMemcpyDeviceToHost, slot.st));
+            CK(cudaMemcpyAsync(q->r.status_host, d.status, n * sizeof(int32_t), cudaMemcpyDeviceToHost, slot.st));
+            if (q->r.dist_host) CK(cudaMemcpyAsync(q->r.dist_host, d.dist, n * sizeof(double), cudaMemcpyDeviceToHost, slot.st));
+            continue;
+        }
         if (q->r.valid_host) CK(cudaMemcpyAsync(q->r.valid_host, d.valid, n, cudaMemcpyDeviceToHost, slot.st));
-        if (q->r.kind == RPM_REQ_EDGES) {
+        if (q->r.kind == RPM_REQ_EDGES || q->r.kind == RPM_REQ_MOTION) {
             if (q->r.checks_host)
                 CK(cudaMemcpyAsync(q->r.checks_host, d.checks, n * sizeof(int32_t), cudaMemcpyDeviceToHost, slot.st));
         } else {
@@ -634,9 +681,18 @@ int rpm_server_create(rpm_ctx *ctx, const rpm_server_config *cfg, rpm_server **o
 int rpm_server_submit(rpm_server *srv, const rpm_request *r, uint64_t *ticket) {
     if (!srv || !r || !ticket) return fail(RPM_ERR_INVALID, "NULL argument");
     if (r->count < 0) return fail(RPM_ERR_INVALID, "negative count");
-    if (r->kind != RPM_REQ_CONFIGS && r->kind != RPM_REQ_EDGES) return fail(RPM_ERR_INVALID, "unknown request kind");
-    if (r->count > 0 && (r->kind == RPM_REQ_CONFIGS ? !r->q_host : (!r->q1_host || !r->q2_host || !r->valid_host)))
-        return fail(RPM_ERR_INVALID, "missing request buffers");
+    if (r->kind < RPM_REQ_CONFIGS || r->kind > RPM_REQ_MOTION) return fail(RPM_ERR_INVALID, "unknown request kind");
+    bool ok = true;
+    if (r->count > 0) {
+        switch (r->kind) {
+        case RPM_REQ_CONFIGS: ok = r->q_host != nullptr; break;
+        case RPM_REQ_EDGES: ok = r->q1_host && r->q2_host && r->valid_host; break;
+        case RPM_REQ_REACHED: ok = r->q_host && r->q1_host && r->q_out_host && r->status_host && r->spine; break;
+        default: ok = r->q1_host && r->q2_host && r->valid_host && r->num_points >= 1 && r->num_boxes >= 0 &&
+                      (r->num_boxes == 0 || r->boxes);
+        }
+    }
+    if (!ok) return fail(RPM_ERR_INVALID, "missing request buffers or parameters");
     const int dofs = scene_dofs(srv->ctx, r->scene_id);
     if (dofs < 0) return fail(RPM_ERR_INVALID, "unknown scene %d", r->scene_id);
     Req *q = new Req();

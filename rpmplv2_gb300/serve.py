@@ -7,12 +7,15 @@ import math
 
 import numpy as np
 
+from . import _abi  # noqa: F401
 from . import robots as _robots
 from . import scenes as _scenes
 from .engine import _check, _i32, _i64, _vp, load
 
 RPM_REQ_CONFIGS = 0
 RPM_REQ_EDGES = 1
+RPM_REQ_REACHED = 2
+RPM_REQ_MOTION = 3
 
 
 class ServerConfig(ctypes.Structure):
@@ -26,7 +29,10 @@ class Request(ctypes.Structure):
     _fields_ = [("kind", ctypes.c_int32), ("scene_id", ctypes.c_int32), ("count", ctypes.c_int64),
                 ("q_host", ctypes.c_void_p), ("q1_host", ctypes.c_void_p), ("q2_host", ctypes.c_void_p),
                 ("step", ctypes.c_float), ("num_checks", ctypes.c_int32), ("valid_host", ctypes.c_void_p),
-                ("dist_host", ctypes.c_void_p), ("profile_host", ctypes.c_void_p), ("checks_host", ctypes.c_void_p)]
+                ("dist_host", ctypes.c_void_p), ("profile_host", ctypes.c_void_p), ("checks_host", ctypes.c_void_p),
+                ("spine", ctypes.c_void_p), ("q_out_host", ctypes.c_void_p), ("status_host", ctypes.c_void_p),
+                ("boxes", ctypes.c_void_p), ("num_boxes", ctypes.c_int32), ("num_points", ctypes.c_int32),
+                ("max_iter_time", ctypes.c_float), ("reserved", ctypes.c_int32)]
 
 
 class Timing(ctypes.Structure):
@@ -130,6 +136,21 @@ def edges_request(scene_id, q1, q2, valid, checks=None, step=0.05, num_checks=10
                    None, None, _addr(checks))
 
 
+def reached_request(scene_id, q_current, horizon, q_out, status, spine, dist=None):
+    """DRGBT::computeReachedState over a horizon (rpm_reached_states); spine
+    is an rpm_spine_params (kept alive by the caller)."""
+    return Request(RPM_REQ_REACHED, scene_id, horizon.shape[0], _addr(q_current), _addr(horizon), None, 0.0, 0,
+                   None, _addr(dist), None, None, ctypes.addressof(spine), _addr(q_out), _addr(status))
+
+
+def motion_request(scene_id, q_prev, q_cur, valid, boxes, max_iter_time, num_points, checks=None):
+    """MotionValidity::check with moving boxes (rpm_motion_validity); boxes is
+    a ctypes array of rpm_moving_box (kept alive by the caller)."""
+    return Request(RPM_REQ_MOTION, scene_id, q_prev.shape[0], None, _addr(q_prev), _addr(q_cur), 0.0, 0,
+                   _addr(valid), None, None, _addr(checks), None, None, None,
+                   ctypes.addressof(boxes) if len(boxes) else None, len(boxes), int(num_points), float(max_iter_time))
+
+
 # ----------------------------------------------------------------- workload --
 def reject_touching(robot, aabbs, margin=0.01, samples=33):
     """Mask of boxes that stay clear of the capsule skeleton at q = 0 (the
@@ -187,19 +208,25 @@ def make_robot(name):
 
 
 def serving_workload(engine, seed=4, n_scenes=64, rate=20000.0, duration=0.5, max_size=65536, dynamic_frac=0.2,
-                     n_dynamic=5, max_speed=1.6, edge_divisor=16, pool=65536, distinct_outputs=False):
+                     n_dynamic=5, max_speed=1.6, edge_divisor=16, pool=65536, distinct_outputs=False, drgbt_frac=0.1):
     """Scenes on the device, a Poisson request trace and the moving obstacles.
 
     Request sizes are log-uniform in [1, max_size]; kinds are isValid,
     isValid + computeDistance and edge checks in equal shares.  An edge
     request of size s carries max(1, s // edge_divisor) edges at 0.05 rad
     steps (about 12 checks each), so its work is near a configuration
-    request of the same size.  Inputs are slices of per-DOF pinned pools;
-    outputs alias shared pinned pools unless distinct_outputs is set."""
+    request of the same size.  A drgbt_frac share of the requests are DRGBT
+    replanning steps instead (DRGBT.cpp:79-176): half a horizon of reached
+    states (10 + 2D - 2 states, DRGBT.cpp:24-25; 5 layers, NUM_ITER_SPINE 1,
+    expanded bubble, D_CRIT 0.05) with the reached states' distances, half a
+    MotionValidity::check of 1-16 motions at 8 points while the scene's
+    dynamic boxes move straight (MotionValidity.cpp:30-53).  Inputs are
+    slices of per-DOF pinned pools; outputs alias shared pinned pools unless
+    distinct_outputs is set."""
     rng = np.random.default_rng(seed)
     robots = {name: make_robot(name) for name in SERVE_ROBOTS}
     rids = {name: engine.upload_robot(r) for name, r in robots.items()}
-    scene_ids, scene_robot, scene_n, motions = [], [], [], []
+    scene_ids, scene_robot, scene_n, motions, sc_aabb = [], [], [], [], []
     for s in range(n_scenes):
         name = SERVE_ROBOTS[rng.integers(len(SERVE_ROBOTS))]
         n = int(round(math.exp(rng.uniform(math.log(10), math.log(1000)))))
@@ -213,6 +240,7 @@ def serving_workload(engine, seed=4, n_scenes=64, rate=20000.0, duration=0.5, ma
         scene_ids.append(sid)
         scene_robot.append(name)
         scene_n.append(sc.n)
+        sc_aabb.append(_scenes.Scene(sc.aabb.copy(), sc.tol.copy(), sc.flags.copy()))
         for j in moving:
             u = rng.normal(size=3)
             u = u / np.linalg.norm(u) * rng.uniform(0, max_speed)
@@ -230,13 +258,54 @@ def serving_workload(engine, seed=4, n_scenes=64, rate=20000.0, duration=0.5, ma
     n_req = rng.poisson(rate * duration)
     arrivals = np.sort(rng.uniform(0, duration, n_req))
     reqs, meta, keep = [], [], []
+    from ._abi import MovingBox, SpineParams
+    spine = SpineParams(5, 1, 1, 0.05)
+    keep.append(spine)
+    movers = {}   # scene index -> rpm_moving_box array of its dynamic boxes (straight motion along -x)
+    for s in range(n_scenes):
+        sid = scene_ids[s]
+        mv = [m for m in motions if m.scene_id == sid]
+        arr = (MovingBox * max(1, len(mv)))()
+        for k, m in enumerate(mv):
+            lo, hi = sc_aabb[s].aabb[m.index, :3], sc_aabb[s].aabb[m.index, 3:]
+            arr[k] = MovingBox(m.index, float(np.linalg.norm(np.array(m.velocity[:]))), tuple((hi - lo).tolist()),
+                               tuple(((lo + hi) / 2).tolist()), (0.0, 0.0, 0.0, 1.0))
+        movers[s] = (arr, len(mv))
+        keep.append(arr)
     for i in range(n_req):
         s = int(rng.integers(n_scenes))
         name = scene_robot[s]
         d = robots[name].num_dofs
         size = int(min(max_size, round(math.exp(rng.uniform(0, math.log(max_size))))))
         kind = int(rng.integers(3))
+        if rng.uniform() < drgbt_frac:
+            kind = 3 + int(rng.integers(2))
         off = int(rng.integers(0, pool - size + 1))
+        if kind == 3:   # a DRGBT horizon
+            H = 10 + 2 * d - 2
+            off = int(rng.integers(0, pool - H - 1))
+            qc, hz = qpool[d][off:off + 1], qpool[d][off + 1:off + 1 + H]
+            qo = pinned((H, d), np.float32)
+            st = pinned(H, np.int32)
+            dd = pinned(H, np.float64)
+            reqs.append(reached_request(scene_ids[s], qc, hz, qo, st, spine, dd))
+            keep += [qo, st, dd]
+            meta.append(("reached", 64 * H, 64 * H, s, qc, hz, st, dd, qo))
+            continue
+        if kind == 4:   # MotionValidity::check while the dynamic boxes move
+            M = int(rng.integers(1, 17))
+            off = int(rng.integers(0, pool - M + 1))
+            arr, nb = movers[s]
+            q1 = qpool[d][off:off + M]
+            q2 = (q1 + rng.uniform(-0.3, 0.3, q1.shape)).astype(np.float32)
+            q2p = pinned((M, d), np.float32)
+            q2p[:] = q2
+            v = pinned(M, np.uint8)
+            k = pinned(M, np.int32)
+            reqs.append(motion_request(scene_ids[s], q1, q2p, v, arr if nb else (MovingBox * 0)(), 0.05, 8, k))
+            keep += [q2p, v, k]
+            meta.append(("motion", 8 * M, 8 * M, s, q1, q2p, v, k))
+            continue
         if kind == 2:
             ne = max(1, size // edge_divisor)
             off = int(rng.integers(0, pool - ne + 1))
@@ -256,15 +325,20 @@ def serving_workload(engine, seed=4, n_scenes=64, rate=20000.0, duration=0.5, ma
             keep += [v, dd]
             meta.append(("valid" if kind == 0 else "distance", size, size, s, q, None, v, dd))
     return {"scene_ids": scene_ids, "scene_robot": scene_robot, "scene_n": scene_n, "robots": robots, "requests": reqs,
-            "arrivals": arrivals, "meta": meta, "motions": motions, "pools": (qpool, q2pool, shared), "keep": keep}
+            "arrivals": arrivals, "meta": meta, "motions": motions, "pools": (qpool, q2pool, shared), "keep": keep,
+            "scenes": sc_aabb}
 
 
 def latency_summary(timings, meta, bucket=(2048, 8192)):
+    """Latency percentiles; the size buckets hold the configuration and edge
+    requests (the DRGBT steps are reported on their own)."""
     lat = np.array([t.t_done - t.t_submit for t in timings])
     ok = np.array([t.status == 0 for t in timings])
     sizes = np.array([m[1] for m in meta])
-    sel = ok & (sizes >= bucket[0]) & (sizes <= bucket[1])
-    small = ok & (sizes <= 4096)
+    checks = np.array([m[0] in ("valid", "distance", "edges") for m in meta])
+    sel = ok & checks & (sizes >= bucket[0]) & (sizes <= bucket[1])
+    small = ok & checks & (sizes <= 4096)
+    kinds = np.array([m[0] for m in meta])
     pct = lambda a, p: float(np.percentile(a, p)) * 1e3 if a.size else None
     work = sum(m[2] for m, o in zip(meta, ok) if o)
     span = max(t.t_done for t in timings) - min(t.t_submit for t in timings) if timings else 0.0
@@ -277,4 +351,10 @@ def latency_summary(timings, meta, bucket=(2048, 8192)):
             "configs_or_edges_per_s": float(work / span) if span > 0 else None,
             "mean_batch": float(np.mean([t.batch_size for t in timings])) if timings else None,
             "median_queue_ms": pct(np.array([t.t_launch - t.t_submit for t in timings])[ok], 50),
-            "median_run_ms": pct(np.array([t.t_done - t.t_launch for t in timings])[ok], 50)}
+            "median_run_ms": pct(np.array([t.t_done - t.t_launch for t in timings])[ok], 50),
+            "drgbt_horizon": {"requests": int((ok & (kinds == "reached")).sum()),
+                              "p50_ms": pct(lat[ok & (kinds == "reached")], 50),
+                              "p99_ms": pct(lat[ok & (kinds == "reached")], 99)},
+            "motion_validity": {"requests": int((ok & (kinds == "motion")).sum()),
+                                "p50_ms": pct(lat[ok & (kinds == "motion")], 50),
+                                "p99_ms": pct(lat[ok & (kinds == "motion")], 99)}}

@@ -10,13 +10,17 @@ pytestmark = pytest.mark.gpu
 
 
 def _fresh_outputs(meta):
-    return [(m[6].copy(), None if m[7] is None else m[7].copy()) for m in meta]
+    return [tuple(None if a is None else a.copy() for a in m[6:]) for m in meta]
 
 
 def test_alone_equals_mixed(engine):
-    from rpmplv2_gb300 import serve
+    """Every kind, DRGBT horizons and motion checks included, gives the same
+    bits alone and batched with the others; the DRGBT kinds also equal the
+    oracle."""
+    from oracle import oracle as O
+    from rpmplv2_gb300 import scenes, serve
     wl = serve.serving_workload(engine, seed=41, n_scenes=8, rate=2000.0, duration=0.15, max_size=4096,
-                                dynamic_frac=0.0, distinct_outputs=True)
+                                dynamic_frac=0.5, distinct_outputs=True, drgbt_frac=0.3)
     srv = serve.Server(engine, num_slots=4)
     reqs, meta = wl["requests"], wl["meta"]
     assert len(reqs) > 100
@@ -25,18 +29,36 @@ def test_alone_equals_mixed(engine):
         t = srv.wait(srv.submit(r))
         assert t.status == 0 and t.batch_size == 1
     alone = _fresh_outputs(meta)
+    kinds = {m[0] for m in meta}
+    assert {"valid", "distance", "edges", "reached", "motion"} <= kinds
+    # the DRGBT kinds against the oracle (spines in the reference's numerics, motions in FP64)
+    checked = 0
+    for r, m in zip(reqs, meta):
+        if m[0] not in ("reached", "motion") or checked >= 12:
+            continue
+        robot = wl["robots"][wl["scene_robot"][m[3]]]
+        sc = wl["scenes"][m[3]]
+        if m[0] == "reached":
+            qo, st = O.reached_states(robot, sc, m[4], m[5])
+            assert np.array_equal(qo.view(np.uint32), m[8].view(np.uint32)) and np.array_equal(st, m[6])
+        else:
+            box = (serve._abi.MovingBox * max(1, r.num_boxes)).from_address(r.boxes) if r.num_boxes else []
+            rv, rk = O.motion_validity(robot, sc, m[4], m[5], box, 0.05, 8, prec="ref64")
+            assert np.array_equal(rv, m[6]) and np.array_equal(rk, m[7])
+        checked += 1
+    assert checked >= 4
     for m in meta:
-        m[6][:] = 9
-        if m[7] is not None:
-            m[7][:] = -1
+        for a in m[6:]:
+            if a is not None:
+                a[:] = 7
     # mixed: all submitted at once, batched and overlapped
     timings = srv.replay(reqs, np.zeros(len(reqs)))
     assert all(t.status == 0 for t in timings)
     assert max(t.batch_size for t in timings) > 1
-    for (v0, d0), m in zip(alone, meta):
-        assert np.array_equal(v0, m[6])
-        if d0 is not None:
-            assert np.array_equal(d0.view(np.uint8), m[7].view(np.uint8))
+    for outs, m in zip(alone, meta):
+        for a0, a in zip(outs, m[6:]):
+            if a0 is not None:
+                assert np.array_equal(a0.view(np.uint8), a.view(np.uint8)), m[0]
     srv.close()
 
 
