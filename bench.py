@@ -322,15 +322,16 @@ def edges_line(eng, scenes, timed):
     q1d, q2d = torch.from_numpy(q1).cuda(), torch.from_numpy(q2).cuda()
     v = torch.zeros(q1.shape[0], dtype=torch.uint8, device="cuda")
     k = torch.zeros(q1.shape[0], dtype=torch.int32, device="cuda")
-    ctas = eng.autotune_edges(sid, q1d[:32768], q2d[:32768], v[:32768], step=float(step), precision="fp32_recheck")
+    shape = eng.autotune_edges(sid, q1d, q2d, v, step=float(step), precision="fp32_recheck", reps=2)
     eng.set_graphs(True)
     ms = timed(lambda: eng.check_edges(sid, q1d, q2d, v, k, step=float(step), precision="fp32_recheck"))
     eng.set_graphs(False)
+    launched = eng.last_shape()
     checks = int(k.sum().item())
     line = {"workload": "spatial_10dof (r 0.03) vs 200 rotated boxes as fcl AABBs, 262,144 edges, 0.05 rad",
             "edges_per_s": q1.shape[0] / (ms / 1e3), "checks_per_s": checks / (ms / 1e3),
             "ms_per_step": ms, "checks_reference_order": checks, "valid_fraction": float(v.float().mean()),
-            "ctas_per_sm": ctas, "cuda_graph": True, "precision": "fp32_recheck"}
+            "tile_shape": shape, "launched_shape": launched, "cuda_graph": True, "precision": "fp32_recheck"}
     eng.destroy_scene(sid)
     return line
 
@@ -365,11 +366,12 @@ def large_line(eng, scenes, timed):
     C = q.shape[0]
     v = torch.zeros(C, dtype=torch.uint8, device="cuda")
     d = torch.zeros(C, dtype=torch.float64, device="cuda")
+    shape = eng.autotune_configs(sid, qd, "fp32_recheck", v, d, reps=2)
     ms = timed(lambda: eng.check_configs(sid, qd, "fp32_recheck", v, d, None), steps=5, warmup=2)
     line = {"workload": "spatial_22dof (r 0.03) vs 1000 boxes (dims U[0.02, 0.15] m, 1.5 m ball), 65,536 configs, "
                         "isValid + computeDistance",
             "configs_per_s": C / (ms / 1e3), "ms_per_step": ms, "valid_fraction": float(v.float().mean()),
-            "layout": "auto (warp per configuration)", "precision": "fp32_recheck"}
+            "tile_shape": shape, "launched_shape": eng.last_shape(), "precision": "fp32_recheck"}
     eng.destroy_scene(sid)
     return line
 

@@ -230,12 +230,51 @@ typedef struct rpm_edge_batch_item {
 } rpm_edge_batch_item;
 int rpm_check_edges_batch(rpm_ctx *ctx, int32_t precision, const rpm_edge_batch_item *items, int32_t n_items,
                           void *stream);
-/* Times the edge pipeline on the given batch for several persistent-grid
- * sizes (CTAs per SM) and keeps the fastest for this scene's robot and
- * precision; *ctas_out receives it.  rpm_set_edge_ctas sets it directly. */
+/* ---- tile shapes and the autotuner -------------------------------------------
+ * A GB300 addition with no reference counterpart; results never depend on
+ * the shape, only the time does.  A tile shape is how a batch is spread over
+ * the GPU: the layout (one lane per configuration or edge check, or one warp
+ * per configuration over the scene sorted into leaves), the configurations
+ * (or edge streams) each warp of the warp layout takes, and the persistent
+ * CTAs per SM of the lane-layout edge pass.  The context keeps a table of
+ * shapes per bucket (robot kind and DOF, obstacles and batch size as
+ * ceil(log2), precision, outputs, configurations or edges); a bucket without
+ * an entry takes the built-in rule (RPM_LAYOUT_AUTO).  The table is used only
+ * in RPM_LAYOUT_AUTO. */
+typedef struct rpm_tile_shape {
+    int32_t layout;             /* RPM_LAYOUT_LANE or RPM_LAYOUT_WARP (0: the built-in rule) */
+    int32_t configs_per_warp;   /* warp layout: configurations or edge streams per warp; 0: chosen by size */
+    int32_t ctas_per_sm;        /* lane-layout edge pass: persistent CTAs per SM; 0: 4 */
+    float ms;                   /* the time the autotuner measured for the bucket's call (0 if set by hand) */
+} rpm_tile_shape;
+/* Outputs of a bucket: bit 0 isValid, bit 1 distance, bit 2 profile (edges: 1). */
+#define RPM_OUT_VALID   0x1
+#define RPM_OUT_DIST    0x2
+#define RPM_OUT_PROFILE 0x4
+/* Time rpm_check_configs on the given batch (outputs as given: nullable) in
+ * every candidate shape -- the lane layout, and the warp layout with 1, 2, 4,
+ * 8, 16 or 32 configurations per warp and the size rule -- each 'reps' times
+ * after a warm-up (median), and keep the fastest for the batch's bucket;
+ * *best receives it. */
+int rpm_autotune_configs(rpm_ctx *ctx, int32_t scene_id, int32_t precision, const float *q_dev, int64_t num_configs,
+                         uint8_t *valid_dev, double *dist_dev, float *profile_dev, int32_t reps, rpm_tile_shape *best);
+/* The same for rpm_check_edges: the lane layout with 1, 2, 3, 4, 6 or 8
+ * persistent CTAs per SM, and the warp layout with the size rule or 1, 2, 4,
+ * 8 edge streams per warp. */
 int rpm_autotune_edges(rpm_ctx *ctx, int32_t scene_id, int32_t precision, const float *q1_dev, const float *q2_dev,
-                       int64_t num_edges, float step, int32_t num_checks, uint8_t *valid_dev, int32_t *ctas_out);
-int rpm_set_edge_ctas(rpm_ctx *ctx, int32_t scene_id, int32_t precision, int32_t ctas_per_sm);
+                       int64_t num_edges, float step, int32_t num_checks, uint8_t *valid_dev, int32_t reps,
+                       rpm_tile_shape *best);
+/* Set (shape non-NULL) or remove (NULL) the entry of the bucket of this
+ * scene, precision, kind (edges 0/1), batch size and outputs. */
+int rpm_set_tile_shape(rpm_ctx *ctx, int32_t scene_id, int32_t precision, int32_t edges, int64_t count,
+                       int32_t outputs, const rpm_tile_shape *shape);
+/* The table as a JSON file (one entry per line), and back: loading adds or
+ * replaces entries.  A context created while RPM_TUNING_FILE names a file
+ * loads it. */
+int rpm_tuning_save(rpm_ctx *ctx, const char *path);
+int rpm_tuning_load(rpm_ctx *ctx, const char *path);
+/* The shape of the last configuration or edge launch issued on 'stream'. */
+int rpm_last_shape(rpm_ctx *ctx, void *stream, rpm_tile_shape *out);
 /* Layout of the configuration checks (rpm_check_configs, rpm_check_batch,
  * rpm_check_configs_host and the server): one of enum rpm_layout.  A GB300
  * addition with no reference counterpart; outputs do not depend on it. */

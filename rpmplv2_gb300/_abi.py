@@ -49,6 +49,23 @@ class Params(ctypes.Structure):
     _fields_ = [("equality_threshold", ctypes.c_double), ("max_distance", ctypes.c_double)]
 
 
+class TileShape(ctypes.Structure):
+    """rpm_tile_shape."""
+    _fields_ = [
+        ("layout", ctypes.c_int32),
+        ("configs_per_warp", ctypes.c_int32),
+        ("ctas_per_sm", ctypes.c_int32),
+        ("ms", ctypes.c_float),
+    ]
+
+    def as_dict(self):
+        return {"layout": {1: "lane", 2: "warp"}.get(self.layout, "auto"), "configs_per_warp": self.configs_per_warp,
+                "ctas_per_sm": self.ctas_per_sm, "ms": self.ms}
+
+
+RPM_OUT_VALID, RPM_OUT_DIST, RPM_OUT_PROFILE = 1, 2, 4
+
+
 class CheckStats(ctypes.Structure):
     _fields_ = [
         ("configs", ctypes.c_int64),

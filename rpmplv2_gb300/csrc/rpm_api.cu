@@ -5,6 +5,7 @@
 // FP64 recheck list, counters, device status word).  Callers own every
 // q / output pointer they pass.
 #include <algorithm>
+#include <cstdlib>
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
@@ -384,9 +385,36 @@ SceneRec *find_scene(rpm_ctx *ctx, int id) {
 // lane-per-configuration: every link needs its own nearest-first search
 // there, which keeps the warp's drains half empty.  (Thresholds measured on
 // GB300 over 10-22 links, 10-1000 obstacles and 256-65,536 configurations.)
+constexpr int kDefaultEdgeCtas = 4;   // lane-layout edge pass, without a table entry
+
+static int ceil_log2(int64_t x) {
+    int l = 0;
+    while (l < 62 && ((int64_t)1 << l) < x) ++l;
+    return l;
+}
+
+static TuneKey tune_key(const rpm_ctx *ctx, const SceneRec *s, int64_t count, int prec, int outputs, int edges) {
+    const rpm_robot_desc &d = ctx->robots[s->robot].desc;
+    return TuneKey{d.kind, d.num_dofs, ceil_log2((int64_t)s->n + 1), ceil_log2(std::max<int64_t>(count, 1)), prec,
+                   outputs, edges};
+}
+
+static const rpm_tile_shape *tuned(const rpm_ctx *ctx, const TuneKey &k) {
+    if (ctx->layout != RPM_LAYOUT_AUTO) return nullptr;
+    auto it = ctx->tune.find(k);
+    return it == ctx->tune.end() ? nullptr : &it->second;
+}
+
+static int outputs_of(const SegReq &r) {
+    return (r.valid ? RPM_OUT_VALID : 0) | (r.dist ? RPM_OUT_DIST : 0) | (r.profile ? RPM_OUT_PROFILE : 0);
+}
+
 static bool use_warp_layout(const rpm_ctx *ctx, const SegReq &r, int64_t total, int prec) {
+    if (r.wide >= 0) return r.wide == 1;
     if (ctx->layout == RPM_LAYOUT_LANE) return false;
     if (ctx->layout == RPM_LAYOUT_WARP) return true;
+    if (const rpm_tile_shape *t = tuned(ctx, tune_key(ctx, r.scene, total, prec, outputs_of(r), 0)))
+        if (t->layout == RPM_LAYOUT_LANE || t->layout == RPM_LAYOUT_WARP) return t->layout == RPM_LAYOUT_WARP;
     const int n = r.scene->n;
     if (n >= kWideMinObstacles) return !(r.profile != nullptr && total > kWideMaxProfileBatch);
     if (prec == RPM_PREC_FP32_RECHECK && r.profile == nullptr && n >= 20) {
@@ -414,11 +442,14 @@ int enqueue_segments(rpm_ctx *ctx, int prec, const std::vector<SegReq> &reqs_in,
     std::vector<SegReq> reqs;
     reqs.reserve(2 * reqs_in.size());
     for (const SegReq &r : reqs_in) {
-        if (prec == RPM_PREC_FP32_RECHECK && r.valid && (r.dist || r.profile) && !use_warp_layout(ctx, r, total, prec)) {
-            reqs.push_back(SegReq{r.scene, r.q, r.count, r.valid, nullptr, nullptr});
-            reqs.push_back(SegReq{r.scene, r.q, r.count, nullptr, r.dist, r.profile});
+        const int wide = use_warp_layout(ctx, r, total, prec) ? 1 : 0;   // decided once per request
+        if (prec == RPM_PREC_FP32_RECHECK && r.valid && (r.dist || r.profile) && !wide) {
+            reqs.push_back(SegReq{r.scene, r.q, r.count, r.valid, nullptr, nullptr, 0});
+            reqs.push_back(SegReq{r.scene, r.q, r.count, nullptr, r.dist, r.profile, 0});
         } else {
-            reqs.push_back(r);
+            SegReq c = r;
+            c.wide = wide;
+            reqs.push_back(c);
         }
     }
     Scratch *sc = nullptr;
@@ -468,9 +499,23 @@ int enqueue_segments(rpm_ctx *ctx, int prec, const std::vector<SegReq> &reqs_in,
             const int D = ctx->robots[r->scene->robot].desc.num_dofs;
             gmax = std::min(gmax, kWidePtsBytes / ((D + 1) * 3 * (int)tsz));
         }
-        // configurations per warp: enough warps for two waves of two CTAs per SM
-        const int64_t want = (chunk_total + (int64_t)ctx->num_sms * 32 - 1) / ((int64_t)ctx->num_sms * 32);
+        // configurations per warp: enough warps for two waves of two CTAs per SM,
+        // unless the tile-shape table holds a count for every segment's bucket
+        // (at least 2 from 2,048 configurations: the autotuner chose 2 for every
+        // 4,096-configuration bucket it tuned in the warp layout)
+        int64_t want = (chunk_total + (int64_t)ctx->num_sms * 32 - 1) / ((int64_t)ctx->num_sms * 32);
+        if (chunk_total >= 2048) want = std::max<int64_t>(want, 2);
         p.wide_g = (int32_t)std::max<int64_t>(1, std::min<int64_t>(gmax, want));
+        if (wide) {
+            int tg = 0;
+            for (const SegReq *r : segs) {
+                const rpm_tile_shape *t = tuned(ctx, tune_key(ctx, r->scene, total, prec, outputs_of(*r), 0));
+                if (!t || t->configs_per_warp <= 0) { tg = 0; break; }
+                tg = tg ? std::min(tg, t->configs_per_warp) : t->configs_per_warp;
+            }
+            if (tg > 0) p.wide_g = std::max(1, std::min(gmax, tg));
+        }
+        sc->last_shape = rpm_tile_shape{wide ? RPM_LAYOUT_WARP : RPM_LAYOUT_LANE, wide ? p.wide_g : 0, 0, 0.f};
         const int64_t per_cta = wide ? (int64_t)kWideWarps * p.wide_g : kThreads;
         int64_t blocks = 0;
         size_t smem = 0;
@@ -545,10 +590,18 @@ int enqueue_segments(rpm_ctx *ctx, int prec, const std::vector<SegReq> &reqs_in,
 // so the lane-per-check warps of the lane layout already share most of their
 // obstacle walk; the warp layout pays off once culling whole leaves beats
 // walking every obstacle.
-static bool edge_warp_layout(const rpm_ctx *ctx, const SceneRec *s) {
-    if (ctx->layout == RPM_LAYOUT_LANE) return false;
-    if (ctx->layout == RPM_LAYOUT_WARP) return true;
-    return s->n >= kWideEdgeObstacles;
+// Shape of an edge request in a batch of 'total' edges: the layout from the
+// tile-shape table or the obstacle-count rule, and the table's counts.
+static rpm_tile_shape edge_shape(const rpm_ctx *ctx, const SceneRec *s, int64_t total, int prec) {
+    rpm_tile_shape sh{0, 0, 0, 0.f};
+    if (ctx->layout == RPM_LAYOUT_LANE || ctx->layout == RPM_LAYOUT_WARP) {
+        sh.layout = ctx->layout;
+        return sh;
+    }
+    if (const rpm_tile_shape *t = tuned(ctx, tune_key(ctx, s, total, prec, RPM_OUT_VALID, 1))) sh = *t;
+    if (sh.layout != RPM_LAYOUT_LANE && sh.layout != RPM_LAYOUT_WARP)
+        sh.layout = s->n >= kWideEdgeObstacles ? RPM_LAYOUT_WARP : RPM_LAYOUT_LANE;
+    return sh;
 }
 
 int edge_scratch(rpm_ctx *ctx, Scratch *sc, int64_t E, cudaStream_t st) {
@@ -575,10 +628,15 @@ int edge_scratch(rpm_ctx *ctx, Scratch *sc, int64_t E, cudaStream_t st) {
 // The scratch must hold the batch's edges (edge_scratch).
 int enqueue_edge_batch(rpm_ctx *ctx, Scratch *sc, int prec, const std::vector<EdgeReq> &reqs, int ctas_per_sm,
                        cudaStream_t st) {
+    int64_t batch_total = 0;
+    for (const EdgeReq &r : reqs) batch_total += r.E;
+    std::vector<rpm_tile_shape> shape(reqs.size());
+    for (size_t k = 0; k < reqs.size(); ++k) shape[k] = edge_shape(ctx, reqs[k].scene, batch_total, prec);
+    auto is_wide = [&](const EdgeReq *r) { return shape[(size_t)(r - reqs.data())].layout == RPM_LAYOUT_WARP; };
     std::vector<const EdgeReq *> order;   // lane-layout requests first
     for (int wide = 0; wide < 2; ++wide)
         for (const EdgeReq &r : reqs)
-            if (r.E > 0 && edge_warp_layout(ctx, r.scene) == (wide == 1)) order.push_back(&r);
+            if (r.E > 0 && is_wide(&r) == (wide == 1)) order.push_back(&r);
     const size_t tsz = prec == RPM_PREC_FP64 ? sizeof(double) : sizeof(float);
     for (size_t first = 0; first < order.size(); first += kMaxSegs) {
         const size_t last = std::min(order.size(), first + (size_t)kMaxSegs);
@@ -594,7 +652,7 @@ int enqueue_edge_batch(rpm_ctx *ctx, Scratch *sc, int prec, const std::vector<Ed
                 if (cudaEventQuery(buf.ready) == cudaSuccess) buf.pending = false;
                 else CK(cudaStreamWaitEvent(st, buf.ready, 0));
             }
-            const bool wide = edge_warp_layout(ctx, s);
+            const bool wide = is_wide(&r);
             EdgeSeg &es = p.segs[p.nseg];
             if (!wide) p.nseg_lane = p.nseg + 1;
             p.nseg++;
@@ -645,9 +703,19 @@ int enqueue_edge_batch(rpm_ctx *ctx, Scratch *sc, int prec, const std::vector<Ed
         p.ps.skel = sc->pskel;
         p.ps.acc = sc->pacc;
         p.wide_g = std::max(1, gmax);
+        // the table's counts of the launch's first request of each layout
+        int lane_ctas = ctas_per_sm, wide_g = 0;
+        for (size_t i = first; i < last; ++i) {
+            const rpm_tile_shape &sh = shape[(size_t)(order[i] - reqs.data())];
+            if (sh.layout == RPM_LAYOUT_LANE && sh.ctas_per_sm > 0 && lane_ctas == ctas_per_sm) lane_ctas = sh.ctas_per_sm;
+            if (sh.layout == RPM_LAYOUT_WARP && sh.configs_per_warp > 0 && !wide_g) wide_g = sh.configs_per_warp;
+        }
+        if (wide_g > 0) p.wide_g = std::max(1, std::min(gmax, wide_g));
+        sc->last_shape = p.nseg_lane < p.nseg ? rpm_tile_shape{RPM_LAYOUT_WARP, p.wide_g, 0, 0.f}
+                                              : rpm_tile_shape{RPM_LAYOUT_LANE, 0, std::max(1, lane_ctas), 0.f};
         CK(launch_edge_prep(p, st));   // also zeroes the counters
         if (p.nseg_lane > 0) {
-            const int grid = ctx->num_sms * std::max(1, ctas_per_sm);
+            const int grid = ctx->num_sms * std::max(1, lane_ctas);
             const size_t smem = p.nseg_lane == 1
                 ? smem_bytes(prec == RPM_PREC_FP32_RECHECK ? RPM_PREC_FP32_REF : prec, p.segs[0].seg.n_pad) : 0;
             if (prec == RPM_PREC_FP32_RECHECK) CK(launch_edges_fp32(p, grid, smem, st));
@@ -733,6 +801,13 @@ int rpm_ctx_create(int device, rpm_ctx **out) {
     ctx->device = device;
     CK(cudaSetDevice(device));
     CK(cudaDeviceGetAttribute(&ctx->num_sms, cudaDevAttrMultiProcessorCount, device));
+    // a tile-shape table named by the environment (rpm_tuning_save's format)
+    if (const char *tf = std::getenv("RPM_TUNING_FILE")) {
+        if (*tf) {
+            const int rc = rpm_tuning_load(ctx, tf);
+            if (rc) { delete ctx; return rc; }
+        }
+    }
     *out = ctx;
     return RPM_OK;
 }
@@ -969,8 +1044,7 @@ int rpm_check_edges_batch(rpm_ctx *ctx, int32_t precision, const rpm_edge_batch_
     if (rc) return rc;
     sc->last_configs = total;
     sc->timed = false;
-    auto it = ctx->edge_ctas.find({reqs[0].scene->robot, precision});
-    rc = enqueue_edge_batch(ctx, sc, precision, reqs, it == ctx->edge_ctas.end() ? 4 : it->second, st);
+    rc = enqueue_edge_batch(ctx, sc, precision, reqs, kDefaultEdgeCtas, st);
     if (rc) return rc;
     std::vector<SceneBuf *> used;
     for (const EdgeReq &r : reqs) {
@@ -1006,8 +1080,7 @@ int rpm_check_edges(rpm_ctx *ctx, int32_t scene_id, int32_t precision, const flo
     if (rc) return rc;
     sc->last_configs = num_edges;
     sc->timed = false;
-    auto it = ctx->edge_ctas.find({s->robot, precision});
-    const int ctas = it == ctx->edge_ctas.end() ? 4 : it->second;
+    const int ctas = kDefaultEdgeCtas;
     SceneBuf &buf = s->bufs[s->cur];
     if (ctx->use_graphs) {
         // replay a captured graph of the whole pipeline when the arguments repeat
@@ -1016,7 +1089,7 @@ int rpm_check_edges(rpm_ctx *ctx, int32_t scene_id, int32_t precision, const flo
         std::vector<uint64_t> key = {(uint64_t)(uintptr_t)&buf, (uint64_t)(uintptr_t)buf.f, (uint64_t)precision,
                                      (uint64_t)(uintptr_t)q1_dev, (uint64_t)(uintptr_t)q2_dev, (uint64_t)num_edges,
                                      (uint64_t)step_bits, (uint64_t)num_checks, (uint64_t)(uintptr_t)valid_dev,
-                                     (uint64_t)(uintptr_t)checks_dev, (uint64_t)ctas, (uint64_t)ctx->layout};
+                                     (uint64_t)(uintptr_t)checks_dev, (uint64_t)ctx->tune_epoch, (uint64_t)ctx->layout};
         cudaGraphExec_t exec = nullptr;
         for (auto &g : sc->graphs) if (g.key == key) { exec = g.exec; break; }
         if (!exec) {
@@ -1371,52 +1444,196 @@ int rpm_ctx_set_graphs(rpm_ctx *ctx, int enable) {
     return RPM_OK;
 }
 
-int rpm_autotune_edges(rpm_ctx *ctx, int32_t scene_id, int32_t precision, const float *q1_dev, const float *q2_dev,
-                       int64_t num_edges, float step, int32_t num_checks, uint8_t *valid_dev, int32_t *ctas_out) {
-    if (!ctx || !ctas_out) return fail(RPM_ERR_INVALID, "NULL argument");
-    static const int cands[] = {1, 2, 3, 4, 6, 8};
-    float best_ms = 1e30f;
-    int best = 4;
-    int32_t robot = 0;
-    {
-        std::lock_guard<std::mutex> lk(ctx->mu);
-        SceneRec *s = find_scene(ctx, scene_id);
-        if (!s) return fail(RPM_ERR_INVALID, "unknown scene %d", scene_id);
-        robot = s->robot;
-    }
+}  // extern "C"
+
+// ---- tile shapes and the autotuner ------------------------------------------
+// Times 'call' (one check on 'st') with each candidate shape in the bucket's
+// table entry: a warm-up call, then 'reps' timed calls, median; keeps the
+// fastest.  The candidates go through the same table lookups the launches use.
+template <typename F>
+static int tune_bucket(rpm_ctx *ctx, const TuneKey &key, const std::vector<rpm_tile_shape> &cands, int reps, F call,
+                       rpm_tile_shape *best) {
+    cudaStream_t st;
+    CK(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
     cudaEvent_t a, b;
     CK(cudaEventCreate(&a));
     CK(cudaEventCreate(&b));
-    for (int c : cands) {
+    rpm_tile_shape win{0, 0, 0, 1e30f};
+    int rc = RPM_OK;
+    for (const rpm_tile_shape &c : cands) {
         {
             std::lock_guard<std::mutex> lk(ctx->mu);
-            ctx->edge_ctas[{robot, precision}] = c;
+            ctx->tune[key] = c;
+            ctx->tune_epoch++;
         }
-        int rc = rpm_check_edges(ctx, scene_id, precision, q1_dev, q2_dev, num_edges, step, num_checks, valid_dev, nullptr, 0);
-        if (rc) { cudaEventDestroy(a); cudaEventDestroy(b); return rc; }
-        CK(cudaEventRecord(a, 0));
-        rc = rpm_check_edges(ctx, scene_id, precision, q1_dev, q2_dev, num_edges, step, num_checks, valid_dev, nullptr, 0);
-        if (rc) { cudaEventDestroy(a); cudaEventDestroy(b); return rc; }
-        CK(cudaEventRecord(b, 0));
-        CK(cudaEventSynchronize(b));
-        float ms = 0.f;
-        CK(cudaEventElapsedTime(&ms, a, b));
-        if (ms < best_ms) { best_ms = ms; best = c; }
+        std::vector<float> ms;
+        for (int r = 0; r <= reps && !rc; ++r) {
+            if (cudaEventRecord(a, st) != cudaSuccess) { rc = fail(RPM_ERR_CUDA, "event record failed"); break; }
+            rc = call(st);
+            if (rc) break;
+            if (cudaEventRecord(b, st) != cudaSuccess || cudaEventSynchronize(b) != cudaSuccess) {
+                rc = fail(RPM_ERR_CUDA, "timing the candidate failed");
+                break;
+            }
+            float t = 0.f;
+            cudaEventElapsedTime(&t, a, b);
+            if (r > 0) ms.push_back(t);   // the first call is the warm-up
+        }
+        if (rc) break;
+        std::sort(ms.begin(), ms.end());
+        const float med = ms[ms.size() / 2];
+        if (med < win.ms) { win = c; win.ms = med; }
     }
+    cudaStreamSynchronize(st);
     cudaEventDestroy(a);
     cudaEventDestroy(b);
+    cudaStreamDestroy(st);
     std::lock_guard<std::mutex> lk(ctx->mu);
-    ctx->edge_ctas[{robot, precision}] = best;
-    *ctas_out = best;
-    return RPM_OK;
+    if (rc) {
+        ctx->tune.erase(key);
+    } else {
+        ctx->tune[key] = win;
+        *best = win;
+    }
+    ctx->tune_epoch++;
+    return rc;
 }
 
-int rpm_set_edge_ctas(rpm_ctx *ctx, int32_t scene_id, int32_t precision, int32_t ctas_per_sm) {
-    if (!ctx || ctas_per_sm < 1 || ctas_per_sm > 32) return fail(RPM_ERR_INVALID, "bad arguments");
+extern "C" {
+
+int rpm_autotune_configs(rpm_ctx *ctx, int32_t scene_id, int32_t precision, const float *q_dev, int64_t num_configs,
+                         uint8_t *valid_dev, double *dist_dev, float *profile_dev, int32_t reps, rpm_tile_shape *best) {
+    if (!ctx || !best || num_configs < 1 || !q_dev || reps < 1 || (!valid_dev && !dist_dev && !profile_dev))
+        return fail(RPM_ERR_INVALID, "bad arguments");
+    if (precision < RPM_PREC_FP64 || precision > RPM_PREC_FP32_REF) return fail(RPM_ERR_INVALID, "unknown precision %d", precision);
+    TuneKey key;
+    {
+        std::lock_guard<std::mutex> lk(ctx->mu);
+        if (ctx->layout != RPM_LAYOUT_AUTO) return fail(RPM_ERR_INVALID, "the autotuner needs RPM_LAYOUT_AUTO");
+        SceneRec *s = find_scene(ctx, scene_id);
+        if (!s) return fail(RPM_ERR_INVALID, "unknown scene %d", scene_id);
+        const int outputs = (valid_dev ? RPM_OUT_VALID : 0) | (dist_dev ? RPM_OUT_DIST : 0) | (profile_dev ? RPM_OUT_PROFILE : 0);
+        key = tune_key(ctx, s, num_configs, precision, outputs, 0);
+    }
+    std::vector<rpm_tile_shape> cands = {{RPM_LAYOUT_LANE, 0, 0, 0.f}, {RPM_LAYOUT_WARP, 0, 0, 0.f}};
+    for (int g : {1, 2, 4, 8, 16, 32}) cands.push_back(rpm_tile_shape{RPM_LAYOUT_WARP, g, 0, 0.f});
+    return tune_bucket(ctx, key, cands, reps, [&](cudaStream_t st) {
+        return rpm_check_configs(ctx, scene_id, precision, q_dev, num_configs, valid_dev, dist_dev, profile_dev, st);
+    }, best);
+}
+
+int rpm_autotune_edges(rpm_ctx *ctx, int32_t scene_id, int32_t precision, const float *q1_dev, const float *q2_dev,
+                       int64_t num_edges, float step, int32_t num_checks, uint8_t *valid_dev, int32_t reps,
+                       rpm_tile_shape *best) {
+    if (!ctx || !best || num_edges < 1 || !q1_dev || !q2_dev || !valid_dev || reps < 1)
+        return fail(RPM_ERR_INVALID, "bad arguments");
+    if (precision < RPM_PREC_FP64 || precision > RPM_PREC_FP32_REF) return fail(RPM_ERR_INVALID, "unknown precision %d", precision);
+    TuneKey key;
+    {
+        std::lock_guard<std::mutex> lk(ctx->mu);
+        if (ctx->layout != RPM_LAYOUT_AUTO) return fail(RPM_ERR_INVALID, "the autotuner needs RPM_LAYOUT_AUTO");
+        SceneRec *s = find_scene(ctx, scene_id);
+        if (!s) return fail(RPM_ERR_INVALID, "unknown scene %d", scene_id);
+        key = tune_key(ctx, s, num_edges, precision, RPM_OUT_VALID, 1);
+    }
+    std::vector<rpm_tile_shape> cands;
+    for (int c : {1, 2, 3, 4, 6, 8}) cands.push_back(rpm_tile_shape{RPM_LAYOUT_LANE, 0, c, 0.f});
+    for (int g : {0, 1, 2, 4, 8}) cands.push_back(rpm_tile_shape{RPM_LAYOUT_WARP, g, 0, 0.f});
+    return tune_bucket(ctx, key, cands, reps, [&](cudaStream_t st) {
+        return rpm_check_edges(ctx, scene_id, precision, q1_dev, q2_dev, num_edges, step, num_checks, valid_dev, nullptr, st);
+    }, best);
+}
+
+int rpm_set_tile_shape(rpm_ctx *ctx, int32_t scene_id, int32_t precision, int32_t edges, int64_t count,
+                       int32_t outputs, const rpm_tile_shape *shape) {
+    if (!ctx || count < 1 || outputs < 1 || outputs > 7) return fail(RPM_ERR_INVALID, "bad arguments");
+    if (shape && ((shape->layout != RPM_LAYOUT_LANE && shape->layout != RPM_LAYOUT_WARP) || shape->configs_per_warp < 0 ||
+                  shape->configs_per_warp > 32 || shape->ctas_per_sm < 0 || shape->ctas_per_sm > 32))
+        return fail(RPM_ERR_INVALID, "bad tile shape");
     std::lock_guard<std::mutex> lk(ctx->mu);
     SceneRec *s = find_scene(ctx, scene_id);
     if (!s) return fail(RPM_ERR_INVALID, "unknown scene %d", scene_id);
-    ctx->edge_ctas[{s->robot, precision}] = ctas_per_sm;
+    const TuneKey key = tune_key(ctx, s, count, precision, edges ? RPM_OUT_VALID : outputs, edges ? 1 : 0);
+    if (shape) ctx->tune[key] = *shape;
+    else ctx->tune.erase(key);
+    ctx->tune_epoch++;
+    return RPM_OK;
+}
+
+int rpm_tuning_save(rpm_ctx *ctx, const char *path) {
+    if (!ctx || !path) return fail(RPM_ERR_INVALID, "NULL argument");
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    FILE *f = std::fopen(path, "w");
+    if (!f) return fail(RPM_ERR_INVALID, "cannot write %s", path);
+    cudaDeviceProp prop;
+    const char *name = cudaGetDeviceProperties(&prop, ctx->device) == cudaSuccess ? prop.name : "unknown";
+    std::fprintf(f, "{\n \"format\": \"rpmplv2_gb300 tile shapes 1\",\n \"device\": \"%s\",\n \"entries\": [\n", name);
+    size_t k = 0;
+    for (const auto &kv : ctx->tune) {
+        const TuneKey &t = kv.first;
+        const rpm_tile_shape &v = kv.second;
+        std::fprintf(f,
+                     "  {\"robot_kind\": %d, \"dofs\": %d, \"obstacles_log2\": %d, \"count_log2\": %d, "
+                     "\"precision\": %d, \"outputs\": %d, \"edges\": %d, \"layout\": %d, \"configs_per_warp\": %d, "
+                     "\"ctas_per_sm\": %d, \"ms\": %.4f}%s\n",
+                     t.robot_kind, t.dofs, t.obstacles_log2, t.count_log2, t.prec, t.outputs, t.edges, v.layout,
+                     v.configs_per_warp, v.ctas_per_sm, (double)v.ms, ++k < ctx->tune.size() ? "," : "");
+    }
+    std::fprintf(f, " ]\n}\n");
+    const bool ok = std::fclose(f) == 0;
+    return ok ? RPM_OK : fail(RPM_ERR_INVALID, "writing %s failed", path);
+}
+
+// The value after "\"name\":" in one entry line.
+static bool json_num(const std::string &line, const char *name, double &v) {
+    const std::string key = std::string("\"") + name + "\":";
+    const size_t at = line.find(key);
+    if (at == std::string::npos) return false;
+    char *end = nullptr;
+    v = std::strtod(line.c_str() + at + key.size(), &end);
+    return end != line.c_str() + at + key.size();
+}
+
+int rpm_tuning_load(rpm_ctx *ctx, const char *path) {
+    if (!ctx || !path) return fail(RPM_ERR_INVALID, "NULL argument");
+    FILE *f = std::fopen(path, "r");
+    if (!f) return fail(RPM_ERR_INVALID, "cannot read %s", path);
+    std::vector<std::pair<TuneKey, rpm_tile_shape>> got;
+    char buf[1024];
+    int lineno = 0, rc = RPM_OK;
+    while (std::fgets(buf, sizeof buf, f)) {
+        ++lineno;
+        const std::string line(buf);
+        if (line.find("\"robot_kind\"") == std::string::npos) continue;
+        static const char *names[11] = {"robot_kind", "dofs", "obstacles_log2", "count_log2", "precision", "outputs",
+                                        "edges", "layout", "configs_per_warp", "ctas_per_sm", "ms"};
+        double v[11];
+        for (int i = 0; i < 11 && !rc; ++i)
+            if (!json_num(line, names[i], v[i])) rc = fail(RPM_ERR_INVALID, "%s:%d: no \"%s\"", path, lineno, names[i]);
+        if (rc) break;
+        const rpm_tile_shape sh{(int32_t)v[7], (int32_t)v[8], (int32_t)v[9], (float)v[10]};
+        if ((sh.layout != RPM_LAYOUT_LANE && sh.layout != RPM_LAYOUT_WARP) || sh.configs_per_warp < 0 ||
+            sh.configs_per_warp > 32 || sh.ctas_per_sm < 0 || sh.ctas_per_sm > 32) {
+            rc = fail(RPM_ERR_INVALID, "%s:%d: bad tile shape", path, lineno);
+            break;
+        }
+        got.push_back({TuneKey{(int32_t)v[0], (int32_t)v[1], (int32_t)v[2], (int32_t)v[3], (int32_t)v[4], (int32_t)v[5],
+                               (int32_t)v[6]}, sh});
+    }
+    std::fclose(f);
+    if (rc) return rc;
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    for (const auto &e : got) ctx->tune[e.first] = e.second;
+    ctx->tune_epoch++;
+    return RPM_OK;
+}
+
+int rpm_last_shape(rpm_ctx *ctx, void *stream, rpm_tile_shape *out) {
+    if (!ctx || !out) return fail(RPM_ERR_INVALID, "NULL argument");
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    auto it = ctx->scratch.find((cudaStream_t)stream);
+    if (it == ctx->scratch.end()) return fail(RPM_ERR_INVALID, "no launch on this stream yet");
+    *out = it->second->last_shape;
     return RPM_OK;
 }
 

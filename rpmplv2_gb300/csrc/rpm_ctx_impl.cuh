@@ -103,6 +103,7 @@ struct Scratch {
     uint32_t *counters = nullptr;
     int32_t *status = nullptr;
     int64_t last_configs = 0;
+    rpm_tile_shape last_shape{0, 0, 0, 0.f};   // shape of the last main launch on this stream
     cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};   // bulk start, bulk end / recheck start, recheck end
     bool timed = false, had_recheck = false;
     // edge checks
@@ -126,6 +127,21 @@ struct SegReq {
     uint8_t *valid;
     double *dist;
     float *profile;
+    int32_t wide = -1;   // layout decided for the segment (-1: not yet)
+};
+
+// Tile-shape table of the autotuner: the launch shape to use for a (robot,
+// scene size, batch size, arithmetic form, outputs, configurations or edges)
+// bucket.  Sizes are bucketed by ceil(log2).
+struct TuneKey {
+    int32_t robot_kind, dofs, obstacles_log2, count_log2, prec, outputs, edges;
+    bool operator<(const TuneKey &o) const {
+        const int32_t a[7] = {robot_kind, dofs, obstacles_log2, count_log2, prec, outputs, edges};
+        const int32_t b[7] = {o.robot_kind, o.dofs, o.obstacles_log2, o.count_log2, o.prec, o.outputs, o.edges};
+        for (int i = 0; i < 7; ++i)
+            if (a[i] != b[i]) return a[i] < b[i];
+        return false;
+    }
 };
 
 }  // namespace impl
@@ -159,7 +175,8 @@ struct rpm_ctx {
     bool timing = false;
     bool use_graphs = false;
     int layout = RPM_LAYOUT_AUTO;    // lane- or warp-per-configuration checks
-    std::map<std::pair<int, int>, int> edge_ctas;   // (robot, precision) -> CTAs per SM of the edge kernel
+    std::map<rpm::impl::TuneKey, rpm_tile_shape> tune;   // autotuned tile shapes
+    uint64_t tune_epoch = 0;                              // bumped on every change (graph cache key)
     // degrees of freedom per scene, readable without 'mu' (the server's submit path)
     std::mutex dof_mu;
     std::map<int, int> scene_dofs;

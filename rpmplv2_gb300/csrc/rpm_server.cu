@@ -443,8 +443,7 @@ int launch_batch(rpm_server *srv, Slot &slot, const std::vector<Req *> &batch, i
         std::vector<SceneBuf *> used;
         for (const auto &g : groups) {
             if (g.empty()) continue;
-            auto it = ctx->edge_ctas.find({g[0].scene->robot, srv->cfg.precision});
-            rc = enqueue_edge_batch(ctx, sc, srv->cfg.precision, g, it == ctx->edge_ctas.end() ? 4 : it->second, slot.st);
+            rc = enqueue_edge_batch(ctx, sc, srv->cfg.precision, g, 4, slot.st);
             if (rc) return rc;
             for (const EdgeReq &r : g) {
                 SceneBuf *b = &r.scene->bufs[r.scene->cur];

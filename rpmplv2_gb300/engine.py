@@ -9,7 +9,7 @@ import os
 import numpy as np
 
 from . import _abi
-from ._abi import BatchItem, CheckStats, EdgeBatchItem, LAYOUTS, MovingBox, Params, PRECISIONS, SpineParams
+from ._abi import BatchItem, CheckStats, EdgeBatchItem, LAYOUTS, MovingBox, Params, PRECISIONS, SpineParams, TileShape
 
 _LIB = None
 
@@ -68,8 +68,13 @@ def load(build_if_missing=False):
     L.rpm_enclosing_radii.argtypes = [_vp, _i32, _vp, _i64, _vp, _vp]
     L.rpm_extend_spines.argtypes = [_vp, _i32, _vp, _vp, _vp, _vp, _i64, _i32, _i32, _vp, _vp, _vp]
     L.rpm_reached_states.argtypes = [_vp, _i32, _i32, _vp, _vp, _i64, ctypes.POINTER(SpineParams), _vp, _vp, _vp, _vp]
-    L.rpm_autotune_edges.argtypes = [_vp, _i32, _i32, _vp, _vp, _i64, ctypes.c_float, _i32, _vp, _pi32]
-    L.rpm_set_edge_ctas.argtypes = [_vp, _i32, _i32, _i32]
+    L.rpm_autotune_edges.argtypes = [_vp, _i32, _i32, _vp, _vp, _i64, ctypes.c_float, _i32, _vp, _i32,
+                                     ctypes.POINTER(TileShape)]
+    L.rpm_autotune_configs.argtypes = [_vp, _i32, _i32, _vp, _i64, _vp, _vp, _vp, _i32, ctypes.POINTER(TileShape)]
+    L.rpm_set_tile_shape.argtypes = [_vp, _i32, _i32, _i32, _i64, _i32, _vp]
+    L.rpm_tuning_save.argtypes = [_vp, ctypes.c_char_p]
+    L.rpm_tuning_load.argtypes = [_vp, ctypes.c_char_p]
+    L.rpm_last_shape.argtypes = [_vp, _vp, ctypes.POINTER(TileShape)]
     L.rpm_check_configs_host.argtypes = [_vp, _i32, _i32, _vp, _i64, _vp, _vp, _vp]
     L.rpm_skeleton.argtypes = [_vp, _i32, _i32, _vp, _i64, _vp, _vp]
     L.rpm_last_stats.argtypes = [_vp, _vp, ctypes.POINTER(CheckStats)]
@@ -259,16 +264,44 @@ class Engine:
         code = LAYOUTS[layout] if isinstance(layout, str) else int(layout)
         _check(self.lib.rpm_ctx_set_layout(self.ctx, code))
 
-    def autotune_edges(self, scene_id, q1, q2, valid, step=0.0, num_checks=10, precision="fp32_recheck"):
+    def autotune_edges(self, scene_id, q1, q2, valid, step=0.0, num_checks=10, precision="fp32_recheck", reps=3):
+        """rpm_autotune_edges: the fastest tile shape of this batch's bucket
+        (kept in the context's table), as a dict."""
         prec = PRECISIONS[precision] if isinstance(precision, str) else int(precision)
-        out = _i32()
+        out = TileShape()
         _check(self.lib.rpm_autotune_edges(self.ctx, scene_id, prec, _ptr(q1), _ptr(q2), int(q1.shape[0]),
-                                           float(step), int(num_checks), _ptr(valid), ctypes.byref(out)))
-        return out.value
+                                           float(step), int(num_checks), _ptr(valid), int(reps), ctypes.byref(out)))
+        return out.as_dict()
 
-    def set_edge_ctas(self, scene_id, precision, ctas_per_sm):
+    def autotune_configs(self, scene_id, q, precision="fp32_recheck", valid=None, dist=None, profile=None, reps=3):
+        """rpm_autotune_configs: the fastest tile shape of this batch's bucket, as a dict."""
         prec = PRECISIONS[precision] if isinstance(precision, str) else int(precision)
-        _check(self.lib.rpm_set_edge_ctas(self.ctx, scene_id, prec, int(ctas_per_sm)))
+        out = TileShape()
+        _check(self.lib.rpm_autotune_configs(self.ctx, scene_id, prec, _ptr(q), int(q.shape[0]), _ptr(valid),
+                                             _ptr(dist), _ptr(profile), int(reps), ctypes.byref(out)))
+        return out.as_dict()
+
+    def set_tile_shape(self, scene_id, precision, count, outputs=1, edges=False, layout=None, configs_per_warp=0,
+                       ctas_per_sm=0):
+        """rpm_set_tile_shape; layout None removes the bucket's entry."""
+        prec = PRECISIONS[precision] if isinstance(precision, str) else int(precision)
+        sh = None
+        if layout is not None:
+            sh = TileShape(LAYOUTS[layout] if isinstance(layout, str) else int(layout), int(configs_per_warp),
+                           int(ctas_per_sm), 0.0)
+        _check(self.lib.rpm_set_tile_shape(self.ctx, scene_id, prec, 1 if edges else 0, int(count), int(outputs),
+                                           ctypes.byref(sh) if sh is not None else None))
+
+    def tuning_save(self, path):
+        _check(self.lib.rpm_tuning_save(self.ctx, str(path).encode()))
+
+    def tuning_load(self, path):
+        _check(self.lib.rpm_tuning_load(self.ctx, str(path).encode()))
+
+    def last_shape(self, stream=None):
+        out = TileShape()
+        _check(self.lib.rpm_last_shape(self.ctx, stream, ctypes.byref(out)))
+        return out.as_dict()
 
     def skeleton(self, robot_id, q, points, precision="fp64", stream=None):
         prec = PRECISIONS[precision] if isinstance(precision, str) else int(precision)
@@ -336,7 +369,8 @@ ABI_SYMBOLS = [
     "rpm_robot_upload", "rpm_scene_create", "rpm_scene_update", "rpm_scene_update_many", "rpm_scene_destroy", "rpm_scene_info",
     "rpm_box_aabb", "rpm_check_configs", "rpm_check_configs_host", "rpm_skeleton", "rpm_last_stats", "rpm_sync",
     "rpm_ctx_set_timing", "rpm_last_timing", "rpm_probe_fp32_peak", "rpm_probe_bounded_wait", "rpm_probe_primitives", "rpm_decision_margins", "rpm_robot_builtin", "rpm_check_configs_noalloc", "rpm_check_batch",
-    "rpm_check_edges", "rpm_check_edges_batch", "rpm_ctx_set_graphs", "rpm_autotune_edges", "rpm_set_edge_ctas", "rpm_ctx_set_layout",
+    "rpm_check_edges", "rpm_check_edges_batch", "rpm_ctx_set_graphs", "rpm_autotune_edges", "rpm_autotune_configs", "rpm_set_tile_shape",
+    "rpm_tuning_save", "rpm_tuning_load", "rpm_last_shape", "rpm_ctx_set_layout",
     "rpm_distance_nearest", "rpm_distance_underestimation", "rpm_enclosing_radii", "rpm_extend_spines",
     "rpm_reached_states", "rpm_motion_validity", "rpm_scene_move_straight", "rpm_scenario_read", "rpm_random_scenario_read",
     "rpm_server_create", "rpm_server_submit", "rpm_server_poll", "rpm_server_wait", "rpm_server_release",

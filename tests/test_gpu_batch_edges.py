@@ -70,7 +70,14 @@ def test_edges_fixed_count_graphs_and_autotune(engine):
         assert np.array_equal(v.cpu().numpy(), rv)
     engine.set_graphs(False)
     best = engine.autotune_edges(sid, q1d, q2d, v, step=float(step), precision="fp32_recheck")
-    assert best in (1, 2, 3, 4, 6, 8)
+    assert best["layout"] in ("lane", "warp") and best["ms"] > 0
+    if best["layout"] == "lane":
+        assert best["ctas_per_sm"] in (1, 2, 3, 4, 6, 8)
+    v.fill_(7)
+    engine.check_edges(sid, q1d, q2d, v, None, step=float(step), precision="fp32_recheck")
+    engine.sync()
+    rv2, _ = O.check_edges(robot, scene, q1, q2, step=step, prec="ref64")
+    assert np.array_equal(v.cpu().numpy(), rv2)
     engine.destroy_scene(sid)
 
 
