@@ -253,7 +253,8 @@ typedef struct rpm_tile_shape {
 #define RPM_OUT_PROFILE 0x4
 /* Time rpm_check_configs on the given batch (outputs as given: nullable) in
  * every candidate shape -- the lane layout, and the warp layout with 1, 2, 4,
- * 8, 16 or 32 configurations per warp and the size rule -- each 'reps' times
+ * 8, 16 or 32 configurations per warp (up to what the warp's skeleton buffer
+ * holds for the robot, and that bound itself) and the size rule -- each 'reps' times
  * after a warm-up (median), and keep the fastest for the batch's bucket;
  * *best receives it. */
 int rpm_autotune_configs(rpm_ctx *ctx, int32_t scene_id, int32_t precision, const float *q_dev, int64_t num_configs,
@@ -500,8 +501,8 @@ typedef struct rpm_request {
     float *q_out_host;
     int32_t *status_host;
     /* MOTION (rpm_motion_validity of count motions q1_host -> q2_host while
-     * the boxes move; FP64, or the reference's numerics when the server runs
-     * RPM_PREC_FP32_REF): outputs valid_host, checks_host */
+     * the boxes move; in the reference's own numerics, or FP64 when the
+     * server runs RPM_PREC_FP64): outputs valid_host, checks_host */
     const rpm_moving_box *boxes;
     int32_t num_boxes;
     int32_t num_points;

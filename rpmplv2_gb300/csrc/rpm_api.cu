@@ -1507,6 +1507,7 @@ int rpm_autotune_configs(rpm_ctx *ctx, int32_t scene_id, int32_t precision, cons
         return fail(RPM_ERR_INVALID, "bad arguments");
     if (precision < RPM_PREC_FP64 || precision > RPM_PREC_FP32_REF) return fail(RPM_ERR_INVALID, "unknown precision %d", precision);
     TuneKey key;
+    int gmax = 32;
     {
         std::lock_guard<std::mutex> lk(ctx->mu);
         if (ctx->layout != RPM_LAYOUT_AUTO) return fail(RPM_ERR_INVALID, "the autotuner needs RPM_LAYOUT_AUTO");
@@ -1514,9 +1515,14 @@ int rpm_autotune_configs(rpm_ctx *ctx, int32_t scene_id, int32_t precision, cons
         if (!s) return fail(RPM_ERR_INVALID, "unknown scene %d", scene_id);
         const int outputs = (valid_dev ? RPM_OUT_VALID : 0) | (dist_dev ? RPM_OUT_DIST : 0) | (profile_dev ? RPM_OUT_PROFILE : 0);
         key = tune_key(ctx, s, num_configs, precision, outputs, 0);
+        const int D = ctx->robots[s->robot].desc.num_dofs;   // the warp's skeleton buffer bounds its configurations
+        gmax = std::max(1, kWidePtsBytes / ((D + 1) * 3 * (int)(precision == RPM_PREC_FP64 ? sizeof(double) : sizeof(float))));
     }
     std::vector<rpm_tile_shape> cands = {{RPM_LAYOUT_LANE, 0, 0, 0.f}, {RPM_LAYOUT_WARP, 0, 0, 0.f}};
-    for (int g : {1, 2, 4, 8, 16, 32}) cands.push_back(rpm_tile_shape{RPM_LAYOUT_WARP, g, 0, 0.f});
+    for (int g : {1, 2, 4, 8, 16, 32})
+        if (g <= gmax) cands.push_back(rpm_tile_shape{RPM_LAYOUT_WARP, g, 0, 0.f});
+    if (gmax < 32 && gmax != 1 && gmax != 2 && gmax != 4 && gmax != 8 && gmax != 16)
+        cands.push_back(rpm_tile_shape{RPM_LAYOUT_WARP, gmax, 0, 0.f});
     return tune_bucket(ctx, key, cands, reps, [&](cudaStream_t st) {
         return rpm_check_configs(ctx, scene_id, precision, q_dev, num_configs, valid_dev, dist_dev, profile_dev, st);
     }, best);

@@ -465,7 +465,8 @@ int launch_batch(rpm_server *srv, Slot &slot, const std::vector<Req *> &batch, i
             rc = reached_states_locked(ctx, q->r.scene_id, srv->cfg.precision, d.q, d.q1, q->r.count, q->r.spine,
                                        d.q_out, d.status, d.dist, slot.st);
         } else if (q->r.kind == RPM_REQ_MOTION) {
-            const int32_t prec = srv->cfg.precision == RPM_PREC_FP32_REF ? RPM_PREC_FP32_REF : RPM_PREC_FP64;
+            // the reference's own numerics unless the server runs the FP64 form
+            const int32_t prec = srv->cfg.precision == RPM_PREC_FP64 ? RPM_PREC_FP64 : RPM_PREC_FP32_REF;
             rc = motion_validity_locked(ctx, q->r.scene_id, prec, d.q1, d.q2, q->r.count, q->r.boxes, q->r.num_boxes,
                                         q->r.max_iter_time, q->r.num_points, d.valid, d.checks, slot.st);
         }

@@ -16,7 +16,7 @@ def _fresh_outputs(meta):
 def test_alone_equals_mixed(engine):
     """Every kind, DRGBT horizons and motion checks included, gives the same
     bits alone and batched with the others; the DRGBT kinds also equal the
-    oracle."""
+    oracle (spines and motions in the reference's numerics)."""
     from oracle import oracle as O
     from rpmplv2_gb300 import scenes, serve
     wl = serve.serving_workload(engine, seed=41, n_scenes=8, rate=2000.0, duration=0.15, max_size=4096,
@@ -31,7 +31,7 @@ def test_alone_equals_mixed(engine):
     alone = _fresh_outputs(meta)
     kinds = {m[0] for m in meta}
     assert {"valid", "distance", "edges", "reached", "motion"} <= kinds
-    # the DRGBT kinds against the oracle (spines in the reference's numerics, motions in FP64)
+    # the DRGBT kinds against the oracle (the reference's numerics)
     checked = 0
     for r, m in zip(reqs, meta):
         if m[0] not in ("reached", "motion") or checked >= 12:
@@ -43,7 +43,7 @@ def test_alone_equals_mixed(engine):
             assert np.array_equal(qo.view(np.uint32), m[8].view(np.uint32)) and np.array_equal(st, m[6])
         else:
             box = (serve._abi.MovingBox * max(1, r.num_boxes)).from_address(r.boxes) if r.num_boxes else []
-            rv, rk = O.motion_validity(robot, sc, m[4], m[5], box, 0.05, 8, prec="ref64")
+            rv, rk = O.motion_validity(robot, sc, m[4], m[5], box, 0.05, 8, prec="ref32")
             assert np.array_equal(rv, m[6]) and np.array_equal(rk, m[7])
         checked += 1
     assert checked >= 4
