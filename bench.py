@@ -50,8 +50,8 @@ def parse():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--configs", type=int, default=NUM_CONFIGS)
     ap.add_argument("--no-extra", action="store_true", help="skip the edge, mixed-DOF, large-scene and serving measurements")
-    ap.add_argument("--extra", default="edges,mixed,large,serve,planner",
-                    help="comma list of extra measurements: edges, mixed, large, serve, planner")
+    ap.add_argument("--extra", default="planar,edges,mixed,large,serve,planner",
+                    help="comma list of extra measurements: planar, edges, mixed, large, serve, planner")
     return ap.parse_args()
 
 
@@ -223,6 +223,8 @@ def extra_workloads(eng, args):
         return statistics.median(ms)
 
     which = set(args.extra.split(","))
+    if "planar" in which:
+        out["planar_2dof"] = planar_line(eng, scenes, timed)
     if "edges" in which:
         out["edges"] = edges_line(eng, scenes, timed)
     if "mixed" in which:
@@ -314,9 +316,50 @@ def planner_line(eng, scenes, serve, timed):
     return out
 
 
+def cpu_rates(run, total, n1, nall, unit, what):
+    """CPU baseline columns: the oracle timed on the host, one core on the
+    first n1 units and every core on the first nall units (bounded samples of
+    the same workload)."""
+    cores = os.cpu_count() or 1
+    n1, nall = min(n1, total), min(nall, total)
+    run(0, min(64, n1), 1)   # warm-up
+    t0 = time.perf_counter()
+    run(0, n1, 1)
+    t1 = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    run(0, nall, cores)
+    ta = time.perf_counter() - t0
+    return {"one_core": n1 / t1, "all_cores": nall / ta, "cores": cores, "unit": unit,
+            "sample": "%s; %d units on 1 core, %d on %d cores" % (what, n1, nall, cores)}
+
+
+def planar_line(eng, scenes, timed):
+    """planar_2dof, the plain FP64 form: 65,536 configurations against 4 AABBs, isValid + distance."""
+    import torch
+    from oracle import oracle as O
+    robot, scene, q = scenes.planar_2dof_workload(65536, seed=0)
+    sid = eng.create_scene(eng.upload_robot(robot), scene)
+    qd = torch.from_numpy(q).cuda()
+    C = q.shape[0]
+    v = torch.zeros(C, dtype=torch.uint8, device="cuda")
+    d = torch.zeros(C, dtype=torch.float64, device="cuda")
+    ms = timed(lambda: eng.check_configs(sid, qd, "fp64", v, d, None), steps=5, warmup=3)
+    rv, rd, _ = O.check_configs(robot, scene, q, prec="ref64", want=("valid", "dist"), nthreads=os.cpu_count() or 1)
+    line = {"workload": "planar_2dof (r 0) vs 4 AABBs in a 2 m disk, 65,536 configs, isValid + computeDistance",
+            "configs_per_s": C / (ms / 1e3), "ms_per_step": ms, "precision": "fp64",
+            "isvalid_mismatches_vs_ref64": int((v.cpu().numpy() != rv).sum()),
+            "distance_bit_mismatches_vs_ref64": int((d.cpu().numpy().view(np.uint64) != rd.view(np.uint64)).sum())}
+    line["cpu"] = cpu_rates(lambda a, b, nt: O.check_configs(robot, scene, q[a:b], prec="ref64",
+                                                             want=("valid", "dist"), nthreads=nt),
+                            C, 65536, 65536, "configs/s", "isValid + distance, ref64 oracle")
+    eng.destroy_scene(sid)
+    return line
+
+
 def edges_line(eng, scenes, timed):
     """262,144 spatial_10dof edges at 0.05 rad steps against 200 boxes."""
     import torch
+    from oracle import oracle as O
     robot, scene, q1, q2, step = scenes.spatial10_edge_workload(1 << 18, seed=2)
     sid = eng.create_scene(eng.upload_robot(robot), scene)
     q1d, q2d = torch.from_numpy(q1).cuda(), torch.from_numpy(q2).cuda()
@@ -332,6 +375,9 @@ def edges_line(eng, scenes, timed):
             "edges_per_s": q1.shape[0] / (ms / 1e3), "checks_per_s": checks / (ms / 1e3),
             "ms_per_step": ms, "checks_reference_order": checks, "valid_fraction": float(v.float().mean()),
             "tile_shape": shape, "launched_shape": launched, "cuda_graph": True, "precision": "fp32_recheck"}
+    line["cpu"] = cpu_rates(lambda a, b, nt: O.check_edges(robot, scene, q1[a:b], q2[a:b], step=float(step), prec="ref32",
+                                                           nthreads=nt),
+                            q1.shape[0], 2048, 32768, "edges/s", "edge checks in reference order, ref32 oracle")
     eng.destroy_scene(sid)
     return line
 
@@ -339,6 +385,7 @@ def edges_line(eng, scenes, timed):
 def mixed_line(eng, scenes, timed):
     """Per-link distance profiles of spatial 14/18/22-DOF chains against 500 AABBs in one launch."""
     import torch
+    from oracle import oracle as O
     scene, parts = scenes.mixed_dof_workload(seed=3)
     items = []
     for robot, q in parts:
@@ -351,6 +398,11 @@ def mixed_line(eng, scenes, timed):
     line = {"workload": "spatial 14/18/22 DOF (r 0.03), 32,768/49,152/49,152 configs, 500 AABBs, "
                         "per-link distance + global min in one launch",
             "configs_per_s": total / (ms / 1e3), "ms_per_step": ms, "precision": "fp32_recheck"}
+    # the CPU columns on the 18-DOF part, the middle of the three
+    robot18, q18 = parts[1]
+    line["cpu"] = cpu_rates(lambda a, b, nt: O.check_configs(robot18, scene, q18[a:b], prec="ref32",
+                                                             want=("dist", "profile"), nthreads=nt),
+                            q18.shape[0], 256, 4096, "configs/s", "spatial_18dof part, distance + profile, ref32 oracle")
     for it in items:
         eng.destroy_scene(it[0])
     return line

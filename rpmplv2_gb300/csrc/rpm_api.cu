@@ -498,6 +498,7 @@ int enqueue_segments(rpm_ctx *ctx, int prec, const std::vector<SegReq> &reqs_in,
             chunk_total += r->count;
             const int D = ctx->robots[r->scene->robot].desc.num_dofs;
             gmax = std::min(gmax, kWidePtsBytes / ((D + 1) * 3 * (int)tsz));
+            p.skel_pts = std::max(p.skel_pts, D + 1);
         }
         // configurations per warp: enough warps for two waves of two CTAs per SM,
         // unless the tile-shape table holds a count for every segment's bucket

@@ -255,18 +255,25 @@ template <typename T> struct WarpShared {
     int flags[32];                       // bit0 collision, bit1 isValid unsettled, bit2 distance unsettled
     int slot[32];                        // pair-recheck record per owner (-1: none yet)
     int need[32];                        // owner has pairs waiting for a record
-    uint32_t pend[32];                   // drain lane's unsettled pair: 1 << 31 | kind << 16 | j << 5 | owner
-    uint32_t qb[64], qd[64];             // queues: owner | j << 5
+    uint32_t pend[32];                   // drain lane's unsettled pair (pend_of)
+    uint32_t qb[64], qd[64];             // queues: owner | j << 5 (| link << 16 in warp_check_any)
 };
+
+// Queue items and pending pairs: owner (bits 0-4) | obstacle << 5 (bits 5-15)
+// | link << 16 (bits 16-20); a pending pair adds kind << 30 and bit 31.
+__device__ __forceinline__ uint32_t pend_of(uint32_t item, int link, int kind) {
+    return 0x80000000u | ((uint32_t)kind << 30) | ((uint32_t)link << 16) | (item & 0xffffu);
+}
 
 // After a drain: give every owner with waiting pairs a record, then list the
 // pairs (an owner without a record, or a full pair list, marks bit 8).
 template <typename T>
-__device__ __forceinline__ void flush_pending(WarpShared<T> &sh, const PairSink *ps, int link) {
+__device__ __forceinline__ void flush_pending(WarpShared<T> &sh, const PairSink *ps) {
     const unsigned full = 0xffffffffu;
     const int lane = threadIdx.x & 31;
     const uint32_t pe = sh.pend[lane];
-    const Pend pp{pe != 0u, (int)(pe & 31u), (int)((pe >> 5) & 2047u), (int)((pe >> 16) & 1u)};
+    const Pend pp{pe != 0u, (int)(pe & 31u), (int)((pe >> 5) & 2047u), (int)((pe >> 30) & 1u)};
+    const int link = (int)((pe >> 16) & 31u);
     if (pp.on) sh.need[pp.owner] = 1;
     __syncwarp();
     if (sh.need[lane]) {
@@ -312,14 +319,14 @@ __device__ __forceinline__ void drain_bool(WarpShared<T> &sh, const DevRobot &rb
         const bool c = rr.v;
         if (P::robust && rr.m < kDecide) {
             atomicOr(&sh.flags[owner], 2);
-            pe = 0x80000000u | e;
+            pe = pend_of(e, i, 0);
         } else if (c) {
             atomicOr(&sh.flags[owner], 1);
         }
     }
     if (ps) {
         sh.pend[lane] = pe;
-        if (__any_sync(0xffffffffu, pe != 0u)) flush_pending(sh, ps, i);
+        if (__any_sync(0xffffffffu, pe != 0u)) flush_pending(sh, ps);
     }
 }
 
@@ -356,7 +363,7 @@ __device__ __forceinline__ void drain_dist(WarpShared<T> &sh, const DevRobot &rb
         const T d = pair_distance<MODE, T>(rb, ob, nm, sh.a[owner], sh.b[owner], i, j, settled);
         if (!settled) {
             atomicOr(&sh.flags[owner], 4);
-            pe = 0x80000000u | (1u << 16) | e;
+            pe = pend_of(e, i, 1);
         } else if (d == d) {   // the reference's std::min ignores NaN
             atomicMin(&sh.lmin[owner], Key<T>::of(d));
             if (d <= T(0)) atomicMin(&sh.hitj[owner], j);
@@ -366,7 +373,7 @@ __device__ __forceinline__ void drain_dist(WarpShared<T> &sh, const DevRobot &rb
     }
     if (ps) {
         sh.pend[lane] = pe;
-        if (__any_sync(0xffffffffu, pe != 0u)) flush_pending(sh, ps, i);
+        if (__any_sync(0xffffffffu, pe != 0u)) flush_pending(sh, ps);
     }
 }
 
@@ -587,6 +594,183 @@ __device__ int warp_check(WarpShared<T> &sh, const DevRobot &rb, const ObsView<T
     const bool bad_d = (w.dist || w.profile) && unc_d && (w.profile || hit < 0);
     if (!(bad_b || bad_d)) return kSettled;
     return (ps && sh.slot[lane] >= 0 && !(sh.flags[lane] & 8)) ? kPairs : kFull;
+}
+
+// ---------------------------------------------------------------------------
+// Order-free kinds of the FP32 pass: isValid alone (KIND 1) and the distance
+// alone, without a profile (KIND 3).  Both outputs are folds over all (link,
+// obstacle) pairs that do not depend on the pairs' order: isValid is the OR
+// of the pair tests (RealVectorSpace.cpp:277-309), and the distance is 0 if
+// some pair has d <= 0, else the minimum over all pairs (:318-392; the early
+// exits and the per-link profile change only which pairs the reference
+// evaluates, not these two values).  So this driver
+//   * runs the lane's whole FP32 forward kinematics first and keeps the
+//     skeleton in shared memory ([3 * point + coordinate][NT] floats);
+//   * visits the links in an order that meets collisions and small distances
+//     early (xArm6: links 2-5, then the base links 0 and 1; serial chains: the
+//     distal link first);
+//   * keeps one queue of (owner, link, obstacle) items across links, drained
+//     when 32 items wait, so almost every drain runs a full warp; the
+//     distance's pruning threshold is the lane's running minimum over all
+//     links so far.
+// A lane stops at its first settled collision (KIND 1) or settled hit
+// (KIND 3).  Outputs and pair records are the same as warp_check's.
+__device__ __forceinline__ int any_order_link(const DevRobot &rb, int k) {
+    if (rb.kind == RPM_ROBOT_XARM6) return k + 2 < 6 ? k + 2 : k - 4;
+    return rb.D - 1 - k;
+}
+
+template <int KIND, int NT>
+__device__ __forceinline__ void drain_any(WarpShared<float> &sh, const float *skel, const DevRobot &rb,
+                                          const ObsView<float> &ob, const Num<float> &nm, const uint32_t *queue,
+                                          int nitems, const PairSink *ps) {
+    const int lane = threadIdx.x & 31;
+    uint32_t pe = 0u;
+    if (lane < nitems) {
+        const uint32_t e = queue[lane];
+        const int owner = (int)(e & 31u), j = (int)((e >> 5) & 2047u), li = (int)((e >> 16) & 31u);
+        const float *sk = skel + (threadIdx.x & ~31) + owner;
+        float A[3], B[3];
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            A[k] = sk[(3 * li + k) * NT];
+            B[k] = sk[(3 * li + 3 + k) * NT];
+        }
+        if constexpr (KIND == 1) {
+            float o[6];
+            ob.box(j, o);
+            const RB rr = coll_box_call<float, RobustPol, true>(nm, A, B, rb.radius_f[li], rb.rnew_f[li], o);
+            if (rr.m < kDecide) {
+                atomicOr(&sh.flags[owner], 2);
+                pe = pend_of(e, li, 0);
+            } else if (rr.v) {
+                atomicOr(&sh.flags[owner], 1);
+            }
+        } else {
+            bool settled;
+            const float d = pair_distance<2, float>(rb, ob, nm, A, B, li, j, settled);
+            if (!settled) {
+                atomicOr(&sh.flags[owner], 4);
+                pe = pend_of(e, li, 1);
+            } else if (d == d) {   // the reference's std::min ignores NaN
+                atomicMin(&sh.lmin[owner], Key<float>::of(d));
+                if (d <= 0.f) atomicOr(&sh.flags[owner], 1);
+            }
+        }
+    }
+    if (ps) {
+        sh.pend[lane] = pe;
+        if (__any_sync(0xffffffffu, pe != 0u)) flush_pending(sh, ps);
+    }
+}
+
+// Returns kSettled, kPairs or kFull per lane, as warp_check does; *slot
+// receives the lane's pair-recheck record (-1: none).  skel points to this
+// CTA's skeleton buffer of (rb.D + 1) * 3 * NT floats.
+template <int KIND, int NT>
+__device__ int warp_check_any(WarpShared<float> &sh, float *skel, const DevRobot &rb, const ObsView<float> &ob,
+                              const float *q, bool active, const Num<float> &nm, uint8_t *valid_out,
+                              double *dist_out, const PairSink *ps, int *slot) {
+    static_assert(KIND == 1 || KIND == 3, "isValid alone or the distance alone");
+    const unsigned full = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    const unsigned lt_mask = (1u << lane) - 1u;
+    const int L = rb.D;
+    float *mine = skel + threadIdx.x;
+    {
+        SkelWalker<2> sw;
+        sw.begin();
+        for (int p = 0; p <= L; ++p) {
+            float P[3] = {0.f, 0.f, 0.f};
+            if (active) sw.point(rb, q, p, P);
+            mine[(3 * p) * NT] = P[0];
+            mine[(3 * p + 1) * NT] = P[1];
+            mine[(3 * p + 2) * NT] = P[2];
+        }
+    }
+    sh.flags[lane] = 0;
+    sh.slot[lane] = -1;
+    sh.need[lane] = 0;
+    sh.lmin[lane] = Key<float>::of(nm.maxd);
+    __syncwarp();
+    uint32_t *queue = KIND == 1 ? sh.qb : sh.qd;
+    bool stop = !active;          // register copy of flags bit 0 (settled collision / settled hit)
+    float cur = nm.maxd;          // register copy of the running minimum (KIND 3)
+    int nq = 0;
+    for (int k = 0; k < L; ++k) {
+        if (!__any_sync(full, !stop)) break;
+        const int i = any_order_link(rb, k);
+        const float r = rb.radius_f[i];
+        const bool ground_skip = i < rb.ground_included;
+        float lo[3], hi[3];
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            const float a = mine[(3 * i + c) * NT], b = mine[(3 * i + 3 + c) * NT];
+            lo[c] = a < b ? a : b;
+            hi[c] = a < b ? b : a;
+        }
+        const float tb = r * 1.41421356237309515f + kDecide;
+        const float tb2 = tb * tb;
+        const float rs = r + nm.eq + kBand;
+        const uint32_t ibits = (uint32_t)lane | ((uint32_t)i << 16);
+        for (int j = 0; j < ob.n; ++j) {
+            float o[6], tj;
+            bool gr;
+            if (ob.aos != nullptr) {
+                const float4 a = ob.aos[2 * j], b = ob.aos[2 * j + 1];
+                o[0] = a.x; o[1] = a.y; o[2] = a.z; o[3] = a.w; o[4] = b.x; o[5] = b.y;
+                tj = b.z;
+                gr = b.w != 0.f;
+            } else {
+                ob.box(j, o);
+                tj = ob.tol(j);
+                gr = ob.is_ground(j);
+            }
+            bool qq = false;
+            if (!stop && !(ground_skip && gr)) {
+                const float g2 = gap2_bb(lo, hi, o);
+                if constexpr (KIND == 1) {
+                    qq = !(g2 > tb2);
+                } else {
+                    const float s = smin(cur, tj) + rs;
+                    qq = !(s > 0.f && g2 > s * s);
+                }
+            }
+            const unsigned m = __ballot_sync(full, qq);
+            if (m != 0u) {
+                if (qq) queue[nq + __popc(m & lt_mask)] = ibits | ((uint32_t)j << 5);
+                nq += __popc(m);
+                if (nq >= 32) {
+                    __syncwarp();
+                    drain_any<KIND, NT>(sh, skel, rb, ob, nm, queue, 32, ps);
+                    __syncwarp();
+                    if (lane < nq - 32) queue[lane] = queue[32 + lane];
+                    nq -= 32;
+                    stop = stop || (sh.flags[lane] & 1) != 0;
+                    if constexpr (KIND == 3) cur = Key<float>::value(sh.lmin[lane]);
+                    __syncwarp();
+                }
+            }
+        }
+    }
+    __syncwarp();
+    if (nq > 0) drain_any<KIND, NT>(sh, skel, rb, ob, nm, queue, nq, ps);
+    __syncwarp();
+    const int fl = sh.flags[lane];
+    if (slot) *slot = sh.slot[lane];
+    if (!active) return kSettled;
+    bool bad;
+    if constexpr (KIND == 1) {
+        const bool collided = (fl & 1) != 0;
+        if (valid_out) *valid_out = collided ? 0 : 1;
+        bad = !collided && (fl & 2);
+    } else {
+        const bool hit = (fl & 1) != 0;
+        if (dist_out) *dist_out = hit ? 0.0 : (double)Key<float>::value(sh.lmin[lane]);
+        bad = !hit && (fl & 4);
+    }
+    if (!bad) return kSettled;
+    return (ps && sh.slot[lane] >= 0 && !(fl & 8)) ? kPairs : kFull;
 }
 #endif
 

@@ -58,8 +58,17 @@ __global__ void __launch_bounds__(kThreads, 5) k_check_fp32(const __grid_constan
     uint8_t *vo = (w.valid && active) ? sg.valid + c : nullptr;
     double *dout = (w.dist && active) ? sg.dist + c : nullptr;
     float *po = (w.profile && active) ? sg.profile + c * D : nullptr;
-    const int st = warp_check<2, float, KIND>(wsh[threadIdx.x >> 5], rb, ob, sg.q + c * D, active, P.nmf, w, vo, dout,
-                                              po, &P.ps, &slot, &hl, &hj);
+    int st;
+    if constexpr (KIND == 1 || KIND == 3) {
+        // the order-free kinds: the skeleton buffer follows the rows and their per-obstacle copy
+        float *skel = reinterpret_cast<float *>(smem + sizeof(DevRobot) + (size_t)kFRows * sg.n_pad * sizeof(float) +
+                                                (aos ? (size_t)sg.n_pad * kFRows * sizeof(float) : 0));
+        st = warp_check_any<KIND, kThreads>(wsh[threadIdx.x >> 5], skel, rb, ob, sg.q + c * D, active, P.nmf, vo, dout,
+                                            &P.ps, &slot);
+    } else {
+        st = warp_check<2, float, KIND>(wsh[threadIdx.x >> 5], rb, ob, sg.q + c * D, active, P.nmf, w, vo, dout, po,
+                                        &P.ps, &slot, &hl, &hj);
+    }
     if (active) {
         complete_record(&P.ps, slot, st, s, c, hl, hj);
         if (st == kFull) recheck_whole(P, s, c);
@@ -206,8 +215,9 @@ cudaError_t launch_check_fp32(const KParams &p, int64_t blocks, size_t smem, cud
         if (p.segs[k].n_pad <= kAosMaxPad) aos_pad = std::max(aos_pad, p.segs[k].n_pad);
     }
     smem += (size_t)aos_pad * kFRows * sizeof(float);
-    if (!any_d && !any_p) return launch_fp32_kind<1>(p, blocks, smem, st);
-    if (!any_b && !any_p) return launch_fp32_kind<3>(p, blocks, smem, st);
+    const size_t skel = (size_t)kThreads * 3 * p.skel_pts * sizeof(float);   // order-free kinds
+    if (!any_d && !any_p) return launch_fp32_kind<1>(p, blocks, smem + skel, st);
+    if (!any_b && !any_p) return launch_fp32_kind<3>(p, blocks, smem + skel, st);
     if (!any_b) return launch_fp32_kind<2>(p, blocks, smem, st);
     return launch_fp32_kind<0>(p, blocks, smem, st);
 }

@@ -30,6 +30,8 @@ struct KParams {
     Seg segs[kMaxSegs];
     int32_t nseg;
     int32_t wide_g;             // warp-per-configuration kernels: configurations per warp
+    int32_t skel_pts;           // FP32 lane kernels: the most skeleton points (D + 1) of the launch's robots
+    int32_t pad;
     Num<double> nmd;
     Num<float> nmf;
     uint64_t *recheck;          // FP32 pass -> whole-configuration FP64 recheck: (segment << 40) | config
