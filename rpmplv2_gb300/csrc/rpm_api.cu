@@ -285,6 +285,7 @@ void free_scratch(Scratch *sc) {
     cudaFree(sc->n_e); cudaFree(sc->local); cudaFree(sc->kmax); cudaFree(sc->bprefix); cudaFree(sc->full);
     cudaFree(sc->work); cudaFree(sc->erecheck); cudaFree(sc->recheck); cudaFree(sc->counters); cudaFree(sc->status);
     cudaFree(sc->pairs); cudaFree(sc->pcfgs); cudaFree(sc->pskel); cudaFree(sc->pacc);
+    cudaFree(sc->perm); cudaFree(sc->bins);
     for (int i = 0; i < 3; ++i) if (sc->ev[i]) cudaEventDestroy(sc->ev[i]);
     delete sc;
 }
@@ -457,6 +458,27 @@ int enqueue_segments(rpm_ctx *ctx, int prec, const std::vector<SegReq> &reqs_in,
     if (rc) return rc;
     sc->last_configs = total;
     CK(cudaMemsetAsync(sc->counters, 0, 4 * sizeof(uint32_t), st));
+    // A large FP32 lane-layout request is checked in binned order
+    // (launch_bin_configs); its isValid and distance launches share the order.
+    if (prec == RPM_PREC_FP32_RECHECK && reqs_in.size() == 1 && reqs_in[0].count >= kBinMinConfigs &&
+        reqs_in[0].count <= INT32_MAX && !reqs.empty() && reqs[0].wide == 0) {
+        const SegReq &r0 = reqs_in[0];
+        if ((int64_t)sc->perm_cap < r0.count) {
+            if (sc->perm) {   // a launch still queued on this stream may read the old order
+                CK(cudaStreamSynchronize(st));
+                cudaFree(sc->perm);
+                sc->perm = nullptr;
+                sc->perm_cap = 0;
+            }
+            if (cudaMalloc(&sc->perm, (size_t)r0.count * sizeof(int32_t)) != cudaSuccess)
+                return fail(RPM_ERR_NOMEM, "check-order allocation failed");
+            sc->perm_cap = (size_t)r0.count;
+        }
+        if (!sc->bins && cudaMalloc(&sc->bins, 2 * kConfigBins * sizeof(int32_t)) != cudaSuccess)
+            return fail(RPM_ERR_NOMEM, "check-order allocation failed");
+        CK(launch_bin_configs(r0.q, r0.count, ctx->robots[r0.scene->robot].desc.num_dofs, sc->bins, sc->perm, st));
+        for (SegReq &r : reqs) r.perm = sc->perm;
+    }
     sc->timed = ctx->timing && total > 0;
     sc->had_recheck = prec == RPM_PREC_FP32_RECHECK;
     if (sc->timed && !sc->ev[0])
@@ -545,6 +567,7 @@ int enqueue_segments(rpm_ctx *ctx, int prec, const std::vector<SegReq> &reqs_in,
             g.blk = buf.blk;
             g.ns = r.scene->ns;
             g.nb = r.scene->nb;
+            g.perm = wide ? nullptr : r.perm;
             blocks += (r.count + per_cta - 1) / per_cta;
             smem = std::max(smem, wide ? wide_smem_bytes(prec, r.scene->ns, r.scene->nb)
                                        : smem_bytes(prec == RPM_PREC_FP32_RECHECK ? RPM_PREC_FP32_REF : prec, r.scene->n_pad));
@@ -1656,12 +1679,18 @@ int rpm_check_configs_host(rpm_ctx *ctx, int32_t scene_id, int32_t precision, co
     const int D = ctx->robots[s->robot].desc.num_dofs;
     // Pinned (page-locked, mapped) host buffers: the kernels read q and write
     // the outputs in host memory directly, over NVLink-C2C on GB300, in one
-    // launch.  Any other buffer takes the staged path below.
+    // launch.  Any other buffer takes the staged path below, and so does a
+    // batch that the FP32 lane kernel checks in binned order: its scattered
+    // row reads and output writes would cross the link line by line, while the
+    // staged path moves whole buffers by DMA.
     const float *zq = mapped_ptr(q_host);
     uint8_t *zv = valid_host ? mapped_ptr(valid_host) : nullptr;
     double *zd = dist_host ? mapped_ptr(dist_host) : nullptr;
     float *zp = profile_host ? mapped_ptr(profile_host) : nullptr;
-    if (num_configs > 0 && zq && (!valid_host || zv) && (!dist_host || zd) && (!profile_host || zp)) {
+    const bool binned = precision == RPM_PREC_FP32_RECHECK && num_configs >= kBinMinConfigs &&
+                        !use_warp_layout(ctx, SegReq{s, q_host, num_configs, valid_host, dist_host, profile_host},
+                                         num_configs, precision);
+    if (!binned && num_configs > 0 && zq && (!valid_host || zv) && (!dist_host || zd) && (!profile_host || zp)) {
         if (!ctx->hs[0]) CK(cudaStreamCreateWithFlags(&ctx->hs[0], cudaStreamNonBlocking));
         cudaStream_t st = ctx->hs[0];
         int rc = enqueue_check(ctx, s, precision, zq, num_configs, zv, zd, zp, st);

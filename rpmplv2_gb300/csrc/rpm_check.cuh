@@ -713,7 +713,57 @@ __device__ int warp_check_any(WarpShared<float> &sh, float *skel, const DevRobot
         const float tb2 = tb * tb;
         const float rs = r + nm.eq + kBand;
         const uint32_t ibits = (uint32_t)lane | ((uint32_t)i << 16);
-        for (int j = 0; j < ob.n; ++j) {
+        // The warp's cull: the bounding box of this link's segments over the lanes
+        // still working (a NaN coordinate widens it to everything), tested against 32
+        // obstacles at a time, one per lane, with the largest threshold of any working
+        // lane.  The gap to that box is at most the gap to any lane's own segment box,
+        // so an obstacle it rejects is one no lane's own test below would queue.
+        float ulo[3], uhi[3];
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            ulo[c] = stop ? INFINITY : (lo[c] == lo[c] ? lo[c] : -INFINITY);
+            uhi[c] = stop ? -INFINITY : (hi[c] == hi[c] ? hi[c] : INFINITY);
+#pragma unroll
+            for (int off = 16; off > 0; off >>= 1) {
+                ulo[c] = fminf(ulo[c], __shfl_xor_sync(full, ulo[c], off));
+                uhi[c] = fmaxf(uhi[c], __shfl_xor_sync(full, uhi[c], off));
+            }
+        }
+        for (int base = 0; base < ob.n; base += 32) {
+            float cmax = stop ? -INFINITY : cur;   // KIND 3: the largest running minimum of a working lane
+            if constexpr (KIND == 3) {
+#pragma unroll
+                for (int off = 16; off > 0; off >>= 1) cmax = fmaxf(cmax, __shfl_xor_sync(full, cmax, off));
+            }
+            bool cand = false;
+            if (base + lane < ob.n) {
+                const int jl = base + lane;
+                float o[6], tj;
+                bool gr;
+                if (ob.aos != nullptr) {
+                    const float4 a = ob.aos[2 * jl], b = ob.aos[2 * jl + 1];
+                    o[0] = a.x; o[1] = a.y; o[2] = a.z; o[3] = a.w; o[4] = b.x; o[5] = b.y;
+                    tj = b.z;
+                    gr = b.w != 0.f;
+                } else {
+                    ob.box(jl, o);
+                    tj = ob.tol(jl);
+                    gr = ob.is_ground(jl);
+                }
+                if (!(ground_skip && gr)) {
+                    const float g2 = gap2_bb(ulo, uhi, o);
+                    if constexpr (KIND == 1) {
+                        cand = !(g2 > tb2);
+                    } else {
+                        const float s = smin(cmax, tj) + rs;
+                        cand = !(s > 0.f && g2 > s * s);
+                    }
+                }
+            }
+            unsigned cm = __ballot_sync(full, cand);
+        while (cm != 0u) {
+            const int j = base + __ffs(cm) - 1;
+            cm &= cm - 1u;
             float o[6], tj;
             bool gr;
             if (ob.aos != nullptr) {
@@ -751,6 +801,7 @@ __device__ int warp_check_any(WarpShared<float> &sh, float *skel, const DevRobot
                     __syncwarp();
                 }
             }
+        }
         }
     }
     __syncwarp();

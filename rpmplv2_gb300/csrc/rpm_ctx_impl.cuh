@@ -114,6 +114,10 @@ struct Scratch {
     unsigned long long *work = nullptr;
     uint64_t *erecheck = nullptr;
     size_t erecheck_cap = 0;
+    // check order of a large FP32 lane-layout batch (binned configurations)
+    int32_t *perm = nullptr;
+    size_t perm_cap = 0;
+    int32_t *bins = nullptr;   // [2][kConfigBins]: counts, then running offsets
     // cached CUDA graphs of edge calls, keyed by their arguments
     struct Graph { std::vector<uint64_t> key; cudaGraphExec_t exec; };
     std::vector<Graph> graphs;
@@ -128,6 +132,7 @@ struct SegReq {
     double *dist;
     float *profile;
     int32_t wide = -1;   // layout decided for the segment (-1: not yet)
+    const int32_t *perm = nullptr;   // check order (FP32 lane layout), nullable
 };
 
 // Tile-shape table of the autotuner: the launch shape to use for a (robot,

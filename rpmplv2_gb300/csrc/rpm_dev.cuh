@@ -106,6 +106,10 @@ struct Seg {
     const double *srt_d;     // [7][ns]
     const float *blk;        // [nb][8]: union bounds, max tol, min tol of each block of 32 slots
     int32_t ns, nb;
+    // FP32 lane kernel: the order in which configurations are checked (binned
+    // by their first joint angles), nullable = index order.  Thread t checks
+    // configuration perm[t]; outputs and recheck records use that index.
+    const int32_t *perm;
 };
 
 struct LaunchCtl {

@@ -910,9 +910,11 @@ cudaError_t launch_extend_spines(const SpineParams &p, cudaStream_t st) {
     return cudaGetLastError();
 }
 
+// One warp per CTA: the spine's FP64 forward kinematics is bound by the SM's
+// FP64 rate, which the warps of one SM share, so each horizon state gets an
+// SM to itself while there are SMs to spare.
 cudaError_t launch_reached_states(const SpineParams &p, cudaStream_t st) {
-    const unsigned grid = (unsigned)((p.C + kThreads / 32 - 1) / (kThreads / 32));
-    if (grid) k_reached_states<<<grid, kThreads, 0, st>>>(p);
+    if (p.C > 0) k_reached_states<<<(unsigned)p.C, 32, 0, st>>>(p);
     return cudaGetLastError();
 }
 

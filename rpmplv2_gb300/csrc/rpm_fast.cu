@@ -46,10 +46,11 @@ __global__ void __launch_bounds__(kThreads, 5) k_check_fp32(const __grid_constan
         }
         __syncthreads();
     }
-    const int64_t c = (int64_t)(blockIdx.x - sg.first_block) * kThreads + threadIdx.x;
-    const int64_t warp0 = c - (threadIdx.x & 31);
+    const int64_t t = (int64_t)(blockIdx.x - sg.first_block) * kThreads + threadIdx.x;
+    const int64_t warp0 = t - (threadIdx.x & 31);
     if (warp0 >= sg.count) return;   // whole warp idle
-    const bool active = c < sg.count;
+    const bool active = t < sg.count;
+    const int64_t c = (active && sg.perm) ? (int64_t)sg.perm[t] : t;   // the configuration this thread checks
     ObsView<float> ob{rows, rows + (size_t)kRowGround * sg.n_pad, sg.n, sg.n_pad};
     ob.aos = aos;
     const Want w{sg.valid != nullptr, sg.dist != nullptr, sg.profile != nullptr};
@@ -73,6 +74,79 @@ __global__ void __launch_bounds__(kThreads, 5) k_check_fp32(const __grid_constan
         complete_record(&P.ps, slot, st, s, c, hl, hj);
         if (st == kFull) recheck_whole(P, s, c);
     }
+}
+
+// ------------------------------------------------------------ check order --
+// A large batch is checked in an order that puts configurations with similar
+// first joint angles into the same warp (the first three joints place most of
+// the arm), so a warp's skeletons span a small part of the workspace: the
+// obstacle culling of warp_check_any then skips most obstacles for the whole
+// warp, and the warp's pairs take similar branches of the trees.  A counting
+// sort over 16^3 bins; the order within a bin is whatever the atomics give,
+// which changes no output (every configuration's result depends on itself
+// alone).
+__device__ __forceinline__ int config_bin(const float *q, int D) {
+    int key = 0;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        int b = 0;
+        if (k < D) {
+            const float x = (q[k] + 3.14159265f) * (16.f / 6.28318531f);
+            b = x > 0.f ? (x < 15.f ? (int)x : 15) : 0;   // clamped; NaN -> 0
+        }
+        key = key * 16 + b;
+    }
+    return key;
+}
+
+__global__ void __launch_bounds__(1024) k_bin_count(const float *q, int64_t C, int D, int32_t *bins) {
+    __shared__ int32_t h[kConfigBins];
+    for (int k = threadIdx.x; k < kConfigBins; k += blockDim.x) h[k] = 0;
+    __syncthreads();
+    for (int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; c < C; c += (int64_t)gridDim.x * blockDim.x)
+        atomicAdd(&h[config_bin(q + c * D, D)], 1);
+    __syncthreads();
+    for (int k = threadIdx.x; k < kConfigBins; k += blockDim.x)
+        if (h[k]) atomicAdd(&bins[k], h[k]);
+}
+
+// Exclusive scan of the counts into bins[kConfigBins..] (one CTA of 1024 threads, 4 bins each).
+__global__ void __launch_bounds__(1024) k_bin_scan(int32_t *bins) {
+    __shared__ int32_t part[1024];
+    const int t = threadIdx.x;
+    int32_t v[4], sum = 0;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) { v[k] = bins[4 * t + k]; sum += v[k]; }
+    part[t] = sum;
+    __syncthreads();
+    for (int off = 1; off < 1024; off <<= 1) {
+        const int32_t x = t >= off ? part[t - off] : 0;
+        __syncthreads();
+        part[t] += x;
+        __syncthreads();
+    }
+    int32_t run = part[t] - sum;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) { bins[kConfigBins + 4 * t + k] = run; run += v[k]; }
+}
+
+__global__ void k_bin_scatter(const float *q, int64_t C, int D, int32_t *bins, int32_t *perm) {
+    for (int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; c < C; c += (int64_t)gridDim.x * blockDim.x) {
+        const int32_t pos = atomicAdd(&bins[kConfigBins + config_bin(q + c * D, D)], 1);
+        perm[pos] = (int32_t)c;
+    }
+}
+
+cudaError_t launch_bin_configs(const float *q, int64_t C, int D, int32_t *bins, int32_t *perm, cudaStream_t st) {
+    static_assert(kConfigBins == 4 * 1024, "k_bin_scan scans 4 bins per thread");
+    if (C <= 0) return cudaSuccess;
+    cudaError_t e = cudaMemsetAsync(bins, 0, kConfigBins * sizeof(int32_t), st);
+    if (e != cudaSuccess) return e;
+    const unsigned grid = (unsigned)std::min<int64_t>((C + 1023) / 1024, 256);
+    k_bin_count<<<grid, 1024, 0, st>>>(q, C, D, bins);
+    k_bin_scan<<<1, 1024, 0, st>>>(bins);
+    k_bin_scatter<<<(unsigned)std::min<int64_t>((C + 255) / 256, 4096), 256, 0, st>>>(q, C, D, bins, perm);
+    return cudaGetLastError();
 }
 
 // FP32 pass of the warp-per-configuration form; unsettled configurations go

@@ -352,6 +352,14 @@ def latency_summary(timings, meta, bucket=(2048, 8192)):
             "mean_batch": float(np.mean([t.batch_size for t in timings])) if timings else None,
             "median_queue_ms": pct(np.array([t.t_launch - t.t_submit for t in timings])[ok], 50),
             "median_run_ms": pct(np.array([t.t_done - t.t_launch for t in timings])[ok], 50),
+            # the bucket by kind: "4096-config requests" are the isValid and distance
+            # requests; an edge request of that many edges checks several
+            # configurations per edge (and counts 8 units per edge in the classes)
+            "bucket_4096_by_kind": {k: {"requests": int((sel & (kinds == k)).sum()),
+                                        "p50_ms": pct(lat[sel & (kinds == k)], 50),
+                                        "p99_ms": pct(lat[sel & (kinds == k)], 99)}
+                                    for k in ("valid", "distance", "edges")},
+            "p99_ms_4096_configs": pct(lat[sel & (kinds != "edges")], 99),
             "drgbt_horizon": {"requests": int((ok & (kinds == "reached")).sum()),
                               "p50_ms": pct(lat[ok & (kinds == "reached")], 50),
                               "p99_ms": pct(lat[ok & (kinds == "reached")], 99)},

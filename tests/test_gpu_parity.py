@@ -11,7 +11,7 @@ import pytest
 import torch
 
 from oracle import oracle as O
-from rpmplv2_gb300 import scenes
+from rpmplv2_gb300 import robots, scenes
 
 pytestmark = pytest.mark.gpu
 
@@ -62,6 +62,47 @@ def test_xarm6(engine, prec):
     st, derr = compare(engine, robot, scene, q, prec)
     if prec == "fp32_recheck":
         assert st["rechecked"] < 0.5 * q.shape[0]
+
+
+@pytest.mark.parametrize("workload", ["xarm6", "planar_2dof", "spatial_10dof"])
+def test_order_free_kinds_and_binned_order(engine, workload):
+    """isValid alone and the distance alone (no profile) in the FP32 + recheck
+    form: the kernel kinds that visit links out of order with one queue across
+    links and cull obstacles per warp.  A batch of 65,536 is checked in binned
+    order, batches of 8,192 in index order; both give the same bits, with 0
+    isValid flips and distances within 1e-5 m of ref64."""
+    if workload == "xarm6":
+        robot, scene, q = scenes.xarm6_workload(65536, seed=31)
+    elif workload == "planar_2dof":
+        robot, scene, q = scenes.planar_2dof_workload(65536, seed=32)
+    else:
+        rng = np.random.default_rng(33)
+        robot = robots.spatial(10, radius=0.03)
+        scene = scenes.random_obb_scene(rng, 30, 0.02, 0.1, scenes.SPATIAL_WS_CENTER, 1.2, rotated=True,
+                                        reject_robot=robot)
+        q = scenes.uniform_configs(rng, 65536, 10)
+    sid = engine.create_scene(engine.upload_robot(robot), scene)
+    C = q.shape[0]
+    qd = torch.from_numpy(q).cuda()
+    outs = {}
+    engine.set_layout("lane")
+    try:
+        for name, step in (("binned", C), ("index_order", 8192)):
+            v = torch.zeros(C, dtype=torch.uint8, device="cuda")
+            d = torch.zeros(C, dtype=torch.float64, device="cuda")
+            for a in range(0, C, step):
+                engine.check_configs(sid, qd[a:a + step], "fp32_recheck", v[a:a + step], None, None)
+                engine.check_configs(sid, qd[a:a + step], "fp32_recheck", None, d[a:a + step], None)
+            engine.sync()
+            outs[name] = (v.cpu().numpy(), d.cpu().numpy())
+    finally:
+        engine.set_layout("auto")
+    engine.destroy_scene(sid)
+    (vb, db), (vi, di) = outs["binned"], outs["index_order"]
+    assert np.array_equal(vb, vi) and np.array_equal(db.view(np.uint64), di.view(np.uint64))
+    rv, rd, _ = O.check_configs(robot, scene, q, prec="ref64", want=("valid", "dist"))
+    assert int((vb != rv).sum()) == 0
+    assert float(np.abs(db - rd).max()) <= 1e-5
 
 
 def test_fp64_bits(engine):
