@@ -608,8 +608,8 @@ def run_ours(args, ws, rank, local):
         "clocks": clocks,
         "e2e": {"value": C * args.steps / e2e_s, "unit": "configs/s", "h2d_bytes_per_step": C * D * 4,
                 "d2h_bytes_per_step": C * (1 + 8), "call": "rpm_check_configs_host", "matches_device_run": e2e_ok,
-                "transfer": "pinned host buffers, staged through device memory in 262,144-configuration chunks "
-                            "(DMA copies overlapped with the checks on two streams)"},
+                "transfer": "pinned host buffers, staged through device memory by DMA copies in one chunk of "
+                            "up to 1,048,576 configurations"},
         # per step: the check order (k_bin_count, k_bin_scan, k_bin_scatter), then for each of the
         # two outputs (isValid, distance): k_check_fp32 compiled for that output, the pair recheck
         # k_pair_skel / k_pair_eval / k_pair_fold and the whole-configuration k_recheck

@@ -304,8 +304,9 @@ int get_scratch(rpm_ctx *ctx, cudaStream_t st, int64_t need, Scratch **out) {
         if (s->recheck) {
             CK(cudaStreamSynchronize(st));
             cudaFree(s->recheck);
-            cudaFree(s->pairs); cudaFree(s->pcfgs); cudaFree(s->pskel); cudaFree(s->pacc);
+            cudaFree(s->pairs); cudaFree(s->pcfgs); cudaFree(s->pskel); cudaFree(s->pacc); cudaFree(s->perm);
             s->recheck = nullptr;
+            s->perm = nullptr;
         }
         const size_t cap = std::max<size_t>((size_t)need, 1u << 16);
         // records for 1/8 of the configurations (at least 4096, at most 65536),
@@ -316,9 +317,12 @@ int get_scratch(rpm_ctx *ctx, cudaStream_t st, int64_t need, Scratch **out) {
             cudaMalloc(&s->pairs, ppair * sizeof(uint64_t)) != cudaSuccess ||
             cudaMalloc(&s->pcfgs, pcfg * sizeof(PairCfg)) != cudaSuccess ||
             cudaMalloc(&s->pskel, pcfg * (kMaxDof + 1) * 3 * sizeof(double)) != cudaSuccess ||
-            cudaMalloc(&s->pacc, pcfg * sizeof(PairAcc)) != cudaSuccess)
+            cudaMalloc(&s->pacc, pcfg * sizeof(PairAcc)) != cudaSuccess ||
+            cudaMalloc(&s->perm, cap * sizeof(int32_t)) != cudaSuccess ||
+            (!s->bins && cudaMalloc(&s->bins, 2 * kConfigBins * sizeof(int32_t)) != cudaSuccess))
             return fail(RPM_ERR_NOMEM, "recheck list allocation failed");
         s->cap = cap;
+        s->perm_cap = cap;
         s->pcfg_cap = pcfg;
         s->ppair_cap = ppair;
     }
@@ -460,22 +464,12 @@ int enqueue_segments(rpm_ctx *ctx, int prec, const std::vector<SegReq> &reqs_in,
     CK(cudaMemsetAsync(sc->counters, 0, 4 * sizeof(uint32_t), st));
     // A large FP32 lane-layout request is checked in binned order
     // (launch_bin_configs); its isValid and distance launches share the order.
+    // The order lives with the recheck lists, sized for the stream's largest
+    // batch (get_scratch above), so a steady stream of requests allocates nothing.
     if (prec == RPM_PREC_FP32_RECHECK && reqs_in.size() == 1 && reqs_in[0].count >= kBinMinConfigs &&
-        reqs_in[0].count <= INT32_MAX && !reqs.empty() && reqs[0].wide == 0) {
+        reqs_in[0].count <= INT32_MAX && !reqs.empty() && reqs[0].wide == 0 &&
+        (int64_t)sc->perm_cap >= reqs_in[0].count && sc->bins) {
         const SegReq &r0 = reqs_in[0];
-        if ((int64_t)sc->perm_cap < r0.count) {
-            if (sc->perm) {   // a launch still queued on this stream may read the old order
-                CK(cudaStreamSynchronize(st));
-                cudaFree(sc->perm);
-                sc->perm = nullptr;
-                sc->perm_cap = 0;
-            }
-            if (cudaMalloc(&sc->perm, (size_t)r0.count * sizeof(int32_t)) != cudaSuccess)
-                return fail(RPM_ERR_NOMEM, "check-order allocation failed");
-            sc->perm_cap = (size_t)r0.count;
-        }
-        if (!sc->bins && cudaMalloc(&sc->bins, 2 * kConfigBins * sizeof(int32_t)) != cudaSuccess)
-            return fail(RPM_ERR_NOMEM, "check-order allocation failed");
         CK(launch_bin_configs(r0.q, r0.count, ctx->robots[r0.scene->robot].desc.num_dofs, sc->bins, sc->perm, st));
         for (SegReq &r : reqs) r.perm = sc->perm;
     }
@@ -1285,9 +1279,15 @@ int reached_states_locked(rpm_ctx *ctx, int32_t scene_id, int32_t precision, con
     if (precision < RPM_PREC_FP64 || precision > RPM_PREC_FP32_REF) return fail(RPM_ERR_INVALID, "unknown precision %d", precision);
     SceneRec *s = find_scene(ctx, scene_id);
     const int L = ctx->robots[s->robot].desc.num_dofs;
-    // computeDistance of the current state with nearest points (stream-ordered scratch)
+    // computeDistance of the current state with nearest points (stream-ordered
+    // scratch).  A short horizon's final computeDistance runs on the same
+    // CTA-per-state kernel (its points land in the scratch too), when they fit
+    // in a few megabytes; otherwise it is an ordinary check.
     const size_t near_floats = (size_t)std::max(1, np.n) * 6 * L;
-    const size_t bytes = 16 + 4 * (size_t)L + 4 * near_floats + 16;
+    const bool short_h = dist_dev && horizon_size > 0 && horizon_size <= 64 &&
+                         (size_t)horizon_size * near_floats * 4 <= ((size_t)8 << 20);
+    const size_t h_bytes = short_h ? (size_t)horizon_size * (8 + 4 * (size_t)L + 4 * near_floats) + 64 : 0;
+    const size_t bytes = 16 + 4 * (size_t)L + 4 * near_floats + 16 + h_bytes;
     AsyncScratch scratch;
     scratch.st = st;
     CK(cudaMallocAsync(&scratch.p, bytes, st));
@@ -1315,10 +1315,23 @@ int reached_states_locked(rpm_ctx *ctx, int32_t scene_id, int32_t precision, con
     p.n = np.n;
     p.maxd = np.nmf.maxd;
     CK(launch_reached_states(p, st));
+    if (short_h) {
+        // computeDistance(q_reached, true): the exact FP64 value for the FP64 and
+        // FP32 + recheck forms, the reference's numerics for RPM_PREC_FP32_REF
+        char *h = tmp + 16 + 4 * (size_t)L + 4 * near_floats + 16;
+        NearParams hp = np;
+        hp.q = q_reached_dev;
+        hp.C = horizon_size;
+        hp.dist = dist_dev;
+        hp.nearest = reinterpret_cast<float *>(h);
+        hp.profile = reinterpret_cast<float *>(h + 4 * (size_t)horizon_size * near_floats);
+        hp.flag = reinterpret_cast<uint8_t *>(h + 4 * (size_t)horizon_size * (near_floats + L));
+        CK(launch_distance_nearest(precision == RPM_PREC_FP32_REF ? RPM_PREC_FP32_REF : RPM_PREC_FP64, hp, st));
+    }
     rc = near_done(ctx, buf, st);
     if (rc) return rc;
     // computeDistance(q_reached, true) in the requested form
-    if (dist_dev && horizon_size > 0)
+    if (dist_dev && horizon_size > 0 && !short_h)
         return enqueue_check(ctx, s, precision, q_reached_dev, horizon_size, nullptr, dist_dev, nullptr, st);
     return RPM_OK;
 }
@@ -1698,24 +1711,35 @@ int rpm_check_configs_host(rpm_ctx *ctx, int32_t scene_id, int32_t precision, co
         CK(cudaStreamSynchronize(st));
         return host_status(ctx, st);
     }
-    const int64_t chunk = 1 << 18;
-    if (ctx->hcap_cfg < (size_t)chunk) {
+    // Pinned buffers move by DMA in chunks of up to 1,048,576 configurations
+    // (the copies are short next to the checks); other buffers in chunks of
+    // 262,144, two streams overlapping the copies of one chunk with the checks
+    // of the other.
+    const bool pinned = zq && (!valid_host || zv) && (!dist_host || zd) && (!profile_host || zp);
+    const int64_t chunk = pinned ? std::max<int64_t>(1 << 18, std::min<int64_t>(num_configs, 1 << 20)) : 1 << 18;
+    if (ctx->hcap_cfg < (size_t)chunk || ctx->hcap_qf < (size_t)(chunk * D)) {
         for (int i = 0; i < 2; ++i) {
             if (!ctx->hs[i]) CK(cudaStreamCreateWithFlags(&ctx->hs[i], cudaStreamNonBlocking));
             cudaFree(ctx->hq[i]); cudaFree(ctx->hv[i]); cudaFree(ctx->hd[i]);
-            if (cudaMalloc(&ctx->hq[i], chunk * RPM_MAX_DOF * sizeof(float)) != cudaSuccess ||
-                cudaMalloc(&ctx->hv[i], chunk) != cudaSuccess || cudaMalloc(&ctx->hd[i], chunk * sizeof(double)) != cudaSuccess)
-                return fail(RPM_ERR_NOMEM, "staging allocation failed");
+            ctx->hq[i] = nullptr; ctx->hv[i] = nullptr; ctx->hd[i] = nullptr;
         }
-        ctx->hcap_cfg = chunk;
+        ctx->hcap_cfg = ctx->hcap_qf = 0;
+        const size_t cfg = (size_t)chunk;
+        for (int i = 0; i < 2; ++i)
+            if (cudaMalloc(&ctx->hq[i], cfg * D * sizeof(float)) != cudaSuccess ||
+                cudaMalloc(&ctx->hv[i], cfg) != cudaSuccess || cudaMalloc(&ctx->hd[i], cfg * sizeof(double)) != cudaSuccess)
+                return fail(RPM_ERR_NOMEM, "staging allocation failed");
+        ctx->hcap_cfg = cfg;
+        ctx->hcap_qf = cfg * D;
     }
-    if (profile_host && ctx->hcap_prof < (size_t)chunk) {
+    if (profile_host && ctx->hcap_prof < (size_t)(chunk * D)) {
         for (int i = 0; i < 2; ++i) {
             cudaFree(ctx->hp[i]);
-            if (cudaMalloc(&ctx->hp[i], chunk * RPM_MAX_DOF * sizeof(float)) != cudaSuccess)
+            ctx->hp[i] = nullptr;
+            if (cudaMalloc(&ctx->hp[i], chunk * D * sizeof(float)) != cudaSuccess)
                 return fail(RPM_ERR_NOMEM, "staging allocation failed");
         }
-        ctx->hcap_prof = chunk;
+        ctx->hcap_prof = chunk * D;
     }
     int k = 0;
     for (int64_t off = 0; off < num_configs; off += chunk, ++k) {

@@ -114,7 +114,8 @@ struct Scratch {
     unsigned long long *work = nullptr;
     uint64_t *erecheck = nullptr;
     size_t erecheck_cap = 0;
-    // check order of a large FP32 lane-layout batch (binned configurations)
+    // check order of a large FP32 lane-layout batch (binned configurations),
+    // allocated with the recheck lists (cap entries)
     int32_t *perm = nullptr;
     size_t perm_cap = 0;
     int32_t *bins = nullptr;   // [2][kConfigBins]: counts, then running offsets
@@ -176,7 +177,7 @@ struct rpm_ctx {
     uint8_t *hv[2] = {nullptr, nullptr};
     double *hd[2] = {nullptr, nullptr};
     float *hp[2] = {nullptr, nullptr};
-    size_t hcap_cfg = 0, hcap_prof = 0;
+    size_t hcap_cfg = 0, hcap_qf = 0, hcap_prof = 0;   // staging capacity: configurations, q floats, profile floats
     bool timing = false;
     bool use_graphs = false;
     int layout = RPM_LAYOUT_AUTO;    // lane- or warp-per-configuration checks

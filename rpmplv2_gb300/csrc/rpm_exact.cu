@@ -605,6 +605,33 @@ cudaError_t launch_check_wide(int mode, const KParams &p, int64_t blocks, size_t
 }
 
 // ------------------------------------------------------ nearest points --
+// One (link i, obstacle j) pair of computeDistance with nearest points: the
+// distance after the min_dist_tol clamp (:367-368); with 'store' its points go
+// to near ([n][6][L] of the configuration).  Ground pairs the reference skips
+// carry (0, 0, 0), (0, 0, -MAX_DISTANCE).
+template <int MODE, typename T>
+__device__ __forceinline__ T near_pair(const NearParams &P, const DevRobot &rb, const Num<T> &nm, const T *A,
+                                       const T *B, int i, int j, const float *ground, float *near, int L, bool store) {
+    const T r = MODE == 0 ? (T)rb.radius_d[i] : (T)rb.radius_f[i];
+    T d, pts[6];
+    bool has = true;
+    const T tol = MODE == 0 ? (T)P.obs_d[(size_t)kRowTol * P.n_pad + j] : (T)P.obs_f[(size_t)kRowTol * P.n_pad + j];
+    if (ground[j] != 0.f && i < rb.ground_included) {
+        d = nm.maxd;
+        pts[0] = pts[1] = pts[2] = pts[3] = pts[4] = T(0);
+        pts[5] = -nm.maxd;
+    } else {
+        T o[6];
+        for (int k = 0; k < 6; ++k)
+            o[k] = MODE == 0 ? (T)P.obs_d[(size_t)k * P.n_pad + j] : (T)P.obs_f[(size_t)k * P.n_pad + j];
+        d = capsule_box_pts(nm, A, B, r, o, pts, has);
+    }
+    if (d > tol) d = nm.maxd;   // :367-368
+    if (store)
+        for (int k = 0; k < 6; ++k) near[((size_t)j * 6 + k) * L + i] = (float)pts[k];
+    return d;
+}
+
 // computeDistance(q, true) with nearest points (RealVectorSpace.cpp:318-392),
 // one warp per configuration: links in order, lanes over the obstacles, every
 // pair evaluated; the link minimum and the first hit (lowest obstacle index
@@ -634,27 +661,10 @@ __global__ void __launch_bounds__(kThreads) k_distance_nearest(const __grid_cons
     int hit = -1;
     for (int i = 0; i < L && hit < 0; ++i) {
         const T *A = skel[w] + 3 * i, *B = A + 3;
-        const T r = MODE == 0 ? (T)rb.radius_d[i] : (T)rb.radius_f[i];
         T lmin = nm.maxd, hv = T(0);
         int hj = 0x7fffffff;
         for (int j = lane; j < P.n; j += 32) {
-            T d, pts[6];
-            bool has = true;
-            T tol;
-            if (ground[j] != 0.f && i < rb.ground_included) {
-                d = nm.maxd;
-                pts[0] = pts[1] = pts[2] = pts[3] = pts[4] = T(0);
-                pts[5] = -nm.maxd;
-                tol = MODE == 0 ? (T)P.obs_d[(size_t)kRowTol * P.n_pad + j] : (T)P.obs_f[(size_t)kRowTol * P.n_pad + j];
-            } else {
-                T o[6];
-                for (int k = 0; k < 6; ++k)
-                    o[k] = MODE == 0 ? (T)P.obs_d[(size_t)k * P.n_pad + j] : (T)P.obs_f[(size_t)k * P.n_pad + j];
-                tol = MODE == 0 ? (T)P.obs_d[(size_t)kRowTol * P.n_pad + j] : (T)P.obs_f[(size_t)kRowTol * P.n_pad + j];
-                d = capsule_box_pts(nm, A, B, r, o, pts, has);
-            }
-            if (d > tol) d = nm.maxd;   // :367-368
-            for (int k = 0; k < 6; ++k) near[((size_t)j * 6 + k) * L + i] = (float)pts[k];
+            const T d = near_pair<MODE, T>(P, rb, nm, A, B, i, j, ground, near, L, true);
             lmin = smin(lmin, d);
             if (d <= T(0) && j < hj) { hj = j; hv = d; }
         }
@@ -674,6 +684,84 @@ __global__ void __launch_bounds__(kThreads) k_distance_nearest(const __grid_cons
         }
     }
     if (lane == 0) {
+        if (hit >= 0)
+            for (int k = hit + 1; k < L; ++k) P.profile[c * L + k] = 0.f;
+        P.dist[c] = hit >= 0 ? 0.0 : (double)d_c;
+        P.flag[c] = hit >= 0 ? 0 : 1;
+    }
+}
+
+// computeDistance(q, true) with nearest points for a few configurations: one
+// CTA per configuration and one thread per (link, obstacle) pair, so a single
+// state (the adapter's path, the current state of a DRGBT step) takes one
+// tree's latency instead of a warp walking its links in turn.  The per-link
+// minimum and first hit are shared-memory atomics on order-preserving keys,
+// which give the i-major / j-minor result; the reference's early exit then
+// decides which links the profile keeps.  Points are written for every pair:
+// where the reference stops at a hit the configuration's points are flagged
+// invalid (flag 0), as in k_distance_nearest.
+constexpr int kNearCtaThreads = 256;
+constexpr int64_t kNearCtaMaxConfigs = 64;
+
+template <int MODE>
+__global__ void __launch_bounds__(kNearCtaThreads) k_distance_nearest_cta(const __grid_constant__ NearParams P) {
+    typedef typename std::conditional<MODE == 0, double, float>::type T;
+    __shared__ T skel[(kMaxDof + 1) * 3];
+    __shared__ double sc[2 * kMaxDof];
+    __shared__ typename Key<T>::type lkey[kMaxDof];
+    __shared__ int hj[kMaxDof];
+    __shared__ T hv[kMaxDof];
+    const int64_t c = blockIdx.x;
+    const DevRobot &rb = *P.robot;
+    const int D = rb.D, L = D;
+    const float *q = P.q + c * D;
+    Num<T> nm;
+    if (MODE == 0) { nm.eq = (T)P.nmd.eq; nm.maxd = (T)P.nmd.maxd; }
+    else { nm.eq = (T)P.nmf.eq; nm.maxd = (T)P.nmf.maxd; }
+    if (threadIdx.x < 32) {   // joint sines in parallel, then the chain (the same bits as computing them in turn)
+        if ((int)threadIdx.x < D) taylor_sincos((double)q[threadIdx.x], &sc[2 * threadIdx.x], &sc[2 * threadIdx.x + 1]);
+        __syncwarp();
+        if (threadIdx.x == 0) {
+            SkelWalker<MODE> sw;
+            sw.begin();
+            if constexpr (MODE == 0) sw.sc = sc;
+            else sw.w.sc = sc;
+            for (int k = 0; k <= D; ++k) sw.point(rb, q, k, skel + 3 * k);
+        }
+    }
+    for (int i = threadIdx.x; i < L; i += blockDim.x) {
+        lkey[i] = Key<T>::of(nm.maxd);
+        hj[i] = 0x7fffffff;
+    }
+    __syncthreads();
+    const float *ground = P.obs_f + (size_t)kRowGround * P.n_pad;
+    float *near = P.nearest + (size_t)c * P.n * 6 * L;
+    const int npairs = L * P.n;
+    for (int p = threadIdx.x; p < npairs; p += blockDim.x) {
+        const int i = p / P.n, j = p - i * P.n;
+        const T d = near_pair<MODE, T>(P, rb, nm, skel + 3 * i, skel + 3 * i + 3, i, j, ground, near, L, true);
+        if (d == d) atomicMin(&lkey[i], Key<T>::of(d));   // std::min ignores NaN
+        if (d <= T(0)) atomicMin(&hj[i], j);
+    }
+    __syncthreads();
+    // each link's hit value: its lowest hitting obstacle, evaluated again (the same bits)
+    for (int i = threadIdx.x; i < L; i += blockDim.x)
+        if (hj[i] != 0x7fffffff)
+            hv[i] = near_pair<MODE, T>(P, rb, nm, skel + 3 * i, skel + 3 * i + 3, i, hj[i], ground, near, L, false);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        T d_c = nm.maxd;
+        int hit = -1;
+        for (int i = 0; i < L; ++i) {
+            if (hj[i] != 0x7fffffff) {   // the reference returns at its first hit
+                hit = i;
+                P.profile[c * L + i] = (float)hv[i];
+                break;
+            }
+            const T lm = Key<T>::value(lkey[i]);
+            P.profile[c * L + i] = (float)lm;
+            d_c = smin(d_c, lm);
+        }
         if (hit >= 0)
             for (int k = hit + 1; k < L; ++k) P.profile[c * L + k] = 0.f;
         P.dist[c] = hit >= 0 ? 0.0 : (double)d_c;
@@ -749,6 +837,11 @@ __global__ void __launch_bounds__(kThreads) k_distance_underest(const __grid_con
 }
 
 cudaError_t launch_distance_nearest(int mode, const NearParams &p, cudaStream_t st) {
+    if (p.C > 0 && p.C <= kNearCtaMaxConfigs) {   // a few states: one CTA each
+        if (mode == RPM_PREC_FP32_REF) k_distance_nearest_cta<1><<<(unsigned)p.C, kNearCtaThreads, 0, st>>>(p);
+        else k_distance_nearest_cta<0><<<(unsigned)p.C, kNearCtaThreads, 0, st>>>(p);
+        return cudaGetLastError();
+    }
     const unsigned grid = (unsigned)((p.C + kThreads / 32 - 1) / (kThreads / 32));
     if (grid == 0) return cudaSuccess;
     if (mode == RPM_PREC_FP32_REF) k_distance_nearest<1><<<grid, kThreads, 0, st>>>(p);
@@ -910,11 +1003,9 @@ cudaError_t launch_extend_spines(const SpineParams &p, cudaStream_t st) {
     return cudaGetLastError();
 }
 
-// One warp per CTA: the spine's FP64 forward kinematics is bound by the SM's
-// FP64 rate, which the warps of one SM share, so each horizon state gets an
-// SM to itself while there are SMs to spare.
 cudaError_t launch_reached_states(const SpineParams &p, cudaStream_t st) {
-    if (p.C > 0) k_reached_states<<<(unsigned)p.C, 32, 0, st>>>(p);
+    const unsigned grid = (unsigned)((p.C + kThreads / 32 - 1) / (kThreads / 32));
+    if (grid) k_reached_states<<<grid, kThreads, 0, st>>>(p);
     return cudaGetLastError();
 }
 
