@@ -196,7 +196,7 @@ int rpm_check_batch(rpm_ctx *ctx, int32_t precision, const rpm_batch_item *items
  * (cudaHostAlloc / cudaHostRegister), the kernels read the configurations and
  * write the outputs there directly (over NVLink-C2C on GB300) in one launch,
  * unless the batch is one the FP32 + recheck lane kernel checks in binned
- * order (at least 32,768 configurations); that batch, and any batch in other
+ * order (at least 2,048 configurations); that batch, and any batch in other
  * buffers, is staged in chunks through context-owned device memory, with the
  * copies overlapping the checks. */
 int rpm_check_configs_host(rpm_ctx *ctx, int32_t scene_id, int32_t precision, const float *q_host, int64_t num_configs,

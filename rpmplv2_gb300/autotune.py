@@ -49,8 +49,8 @@ def main():
 
     eng = Engine(0)
     rng = np.random.default_rng(5)
-    sizes = (10, 20, 40, 80, 150, 300) if args.crossover else (10, 40, 150, 600)
-    batches = (256, 2048, 8192, 32768) if args.crossover else (256, 4096, 65536)
+    sizes = (10, 20, 40, 80, 150, 300, 600, 1000) if args.crossover else (10, 40, 150, 600)
+    batches = (256, 2048, 8192, 32768, 65536) if args.crossover else (256, 4096, 65536)
     for name in ("xarm6", "spatial_10dof", "spatial_22dof"):
         rb = serve.make_robot(name)
         rid = eng.upload_robot(rb)

@@ -414,13 +414,18 @@ static int outputs_of(const SegReq &r) {
     return (r.valid ? RPM_OUT_VALID : 0) | (r.dist ? RPM_OUT_DIST : 0) | (r.profile ? RPM_OUT_PROFILE : 0);
 }
 
-static bool use_warp_layout(const rpm_ctx *ctx, const SegReq &r, int64_t total, int prec) {
+// 'single': the request is the whole batch, so a lane-layout launch checks it
+// in binned order (kBinMinConfigs and up).
+static bool use_warp_layout(const rpm_ctx *ctx, const SegReq &r, int64_t total, int prec, bool single) {
     if (r.wide >= 0) return r.wide == 1;
     if (ctx->layout == RPM_LAYOUT_LANE) return false;
     if (ctx->layout == RPM_LAYOUT_WARP) return true;
     if (const rpm_tile_shape *t = tuned(ctx, tune_key(ctx, r.scene, total, prec, outputs_of(r), 0)))
         if (t->layout == RPM_LAYOUT_LANE || t->layout == RPM_LAYOUT_WARP) return t->layout == RPM_LAYOUT_WARP;
     const int n = r.scene->n;
+    // binned and culled, the lane layout wins from 32,768 configurations for every
+    // scene size measured (10-1000 obstacles; xarm6, spatial 10- and 22-DOF)
+    if (prec == RPM_PREC_FP32_RECHECK && r.profile == nullptr && single && total >= kLaneBinnedBatch) return false;
     if (n >= kWideMinObstacles) return !(r.profile != nullptr && total > kWideMaxProfileBatch);
     if (prec == RPM_PREC_FP32_RECHECK && r.profile == nullptr && n >= 20) {
         if (n >= 80) return total <= kWide32Batch80;
@@ -447,7 +452,7 @@ int enqueue_segments(rpm_ctx *ctx, int prec, const std::vector<SegReq> &reqs_in,
     std::vector<SegReq> reqs;
     reqs.reserve(2 * reqs_in.size());
     for (const SegReq &r : reqs_in) {
-        const int wide = use_warp_layout(ctx, r, total, prec) ? 1 : 0;   // decided once per request
+        const int wide = use_warp_layout(ctx, r, total, prec, reqs_in.size() == 1) ? 1 : 0;   // decided once per request
         if (prec == RPM_PREC_FP32_RECHECK && r.valid && (r.dist || r.profile) && !wide) {
             reqs.push_back(SegReq{r.scene, r.q, r.count, r.valid, nullptr, nullptr, 0});
             reqs.push_back(SegReq{r.scene, r.q, r.count, nullptr, r.dist, r.profile, 0});
@@ -492,7 +497,7 @@ int enqueue_segments(rpm_ctx *ctx, int prec, const std::vector<SegReq> &reqs_in,
             if (wide && kind > 0) break;   // the warp layout takes every kind in one launch
             std::vector<const SegReq *> cur;
             for (const SegReq &r : reqs) {
-                if (r.count <= 0 || use_warp_layout(ctx, r, total, prec) != (wide == 1)) continue;
+                if (r.count <= 0 || use_warp_layout(ctx, r, total, prec, reqs_in.size() == 1) != (wide == 1)) continue;
                 if (!wide && kind_of(r) != kind) continue;
                 cur.push_back(&r);
                 if ((int)cur.size() == kMaxSegs) { chunks.push_back({wide == 1, cur}); cur.clear(); }
@@ -1702,7 +1707,7 @@ int rpm_check_configs_host(rpm_ctx *ctx, int32_t scene_id, int32_t precision, co
     float *zp = profile_host ? mapped_ptr(profile_host) : nullptr;
     const bool binned = precision == RPM_PREC_FP32_RECHECK && num_configs >= kBinMinConfigs &&
                         !use_warp_layout(ctx, SegReq{s, q_host, num_configs, valid_host, dist_host, profile_host},
-                                         num_configs, precision);
+                                         num_configs, precision, true);
     if (!binned && num_configs > 0 && zq && (!valid_host || zv) && (!dist_host || zd) && (!profile_host || zp)) {
         if (!ctx->hs[0]) CK(cudaStreamCreateWithFlags(&ctx->hs[0], cudaStreamNonBlocking));
         cudaStream_t st = ctx->hs[0];

@@ -137,9 +137,40 @@ __global__ void k_bin_scatter(const float *q, int64_t C, int D, int32_t *bins, i
     }
 }
 
+// A small batch in one CTA: count, scan and scatter in shared memory, one launch.
+__global__ void __launch_bounds__(1024) k_bin_small(const float *q, int32_t C, int D, int32_t *perm) {
+    __shared__ int32_t h[kConfigBins];
+    __shared__ int32_t part[1024];
+    const int t = threadIdx.x;
+    for (int k = t; k < kConfigBins; k += 1024) h[k] = 0;
+    __syncthreads();
+    for (int c = t; c < C; c += 1024) atomicAdd(&h[config_bin(q + (int64_t)c * D, D)], 1);
+    __syncthreads();
+    int32_t v[4], sum = 0;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) { v[k] = h[4 * t + k]; sum += v[k]; }
+    part[t] = sum;
+    __syncthreads();
+    for (int off = 1; off < 1024; off <<= 1) {
+        const int32_t x = t >= off ? part[t - off] : 0;
+        __syncthreads();
+        part[t] += x;
+        __syncthreads();
+    }
+    int32_t run = part[t] - sum;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) { h[4 * t + k] = run; run += v[k]; }
+    __syncthreads();
+    for (int c = t; c < C; c += 1024) perm[atomicAdd(&h[config_bin(q + (int64_t)c * D, D)], 1)] = c;
+}
+
 cudaError_t launch_bin_configs(const float *q, int64_t C, int D, int32_t *bins, int32_t *perm, cudaStream_t st) {
     static_assert(kConfigBins == 4 * 1024, "k_bin_scan scans 4 bins per thread");
     if (C <= 0) return cudaSuccess;
+    if (C <= kBinSmallConfigs) {
+        k_bin_small<<<1, 1024, 0, st>>>(q, (int32_t)C, D, perm);
+        return cudaGetLastError();
+    }
     cudaError_t e = cudaMemsetAsync(bins, 0, kConfigBins * sizeof(int32_t), st);
     if (e != cudaSuccess) return e;
     const unsigned grid = (unsigned)std::min<int64_t>((C + 1023) / 1024, 256);

@@ -62,7 +62,8 @@ cudaError_t launch_check_fp32(const KParams &p, int64_t blocks, size_t smem, cud
 // by their first three joint angles (16 bins each over [-pi, pi]) with a
 // counting sort; bins needs 2 * kConfigBins ints, perm C ints.
 constexpr int kConfigBins = 4096;
-constexpr int64_t kBinMinConfigs = 32768;   // smaller batches keep the index order
+constexpr int64_t kBinMinConfigs = 2048;      // smaller batches keep the index order
+constexpr int64_t kBinSmallConfigs = 16384;   // up to this many: one CTA sorts them (one launch)
 cudaError_t launch_bin_configs(const float *q, int64_t C, int D, int32_t *bins, int32_t *perm, cudaStream_t st);
 cudaError_t launch_recheck(const KParams &p, int grid, cudaStream_t st);
 // Pair-level FP64 recheck: FK of the recorded configurations, their listed

@@ -61,6 +61,10 @@ constexpr int64_t kWideSmallBatch32 = 4096;
 constexpr int64_t kWide32Batch80 = 32768;
 constexpr int64_t kWide32Batch40 = 16384;
 constexpr int64_t kWide32Batch20 = 8192;
+// ... except a single request of at least this many configurations, which the
+// lane layout checks in binned order with its per-warp culling: faster than the
+// warp layout at every scene size measured (10-1000 obstacles).
+constexpr int64_t kLaneBinnedBatch = 32768;
 // Edge batches (rpm_api.cu): warp-per-check for scenes of at least this many
 // obstacles (measured crossover for spatial 10-DOF edges at 0.05 rad: the
 // lane pass 10 % faster at 100 boxes, the warp pass 19 % faster at 130).
