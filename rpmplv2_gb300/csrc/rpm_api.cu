@@ -622,8 +622,14 @@ static rpm_tile_shape edge_shape(const rpm_ctx *ctx, const SceneRec *s, int64_t 
         return sh;
     }
     if (const rpm_tile_shape *t = tuned(ctx, tune_key(ctx, s, total, prec, RPM_OUT_VALID, 1))) sh = *t;
-    if (sh.layout != RPM_LAYOUT_LANE && sh.layout != RPM_LAYOUT_WARP)
-        sh.layout = s->n >= kWideEdgeObstacles ? RPM_LAYOUT_WARP : RPM_LAYOUT_LANE;
+    if (sh.layout != RPM_LAYOUT_LANE && sh.layout != RPM_LAYOUT_WARP) {
+        // the FP32 lane pass culls obstacles per warp (a warp's checks are neighbours on
+        // one or a few edges), which beats the warp pass except on very large scenes and batches
+        const bool wide = prec == RPM_PREC_FP32_RECHECK
+                              ? (s->n >= kWideEdgeObstacles32 && total > kWideEdgeBatch32)
+                              : s->n >= kWideEdgeObstacles;
+        sh.layout = wide ? RPM_LAYOUT_WARP : RPM_LAYOUT_LANE;
+    }
     return sh;
 }
 

@@ -173,10 +173,14 @@ __device__ __forceinline__ int64_t edge_of_flat(const EdgeParams &P, int64_t idx
 // The persistent lane-per-check pass over the lane-layout segments.  rb_st /
 // ob_st: the robot and scene staged in shared memory when the pass has one
 // segment, else null (each segment read from global memory).  A warp's 32
-// checks may span segments: they are checked one segment at a time.
+// checks may span segments: they are checked one segment at a time.  The FP32
+// pass (MODE 2) runs the order-free isValid driver (warp_check_any): a warp's
+// checks are consecutive checks of one or a few edges, so its skeletons lie
+// close together and its obstacle culling skips most obstacles; skel is the
+// CTA's skeleton buffer (kThreads x 3 x (D + 1) floats for the largest D).
 template <int MODE, typename T>
 __device__ void edge_warps(const EdgeParams &P, const DevRobot *rb_st, const ObsView<T> *ob_st, const Num<T> &nm,
-                           WarpShared<T> &sh, float *qbuf /* 32 x kMaxDof */) {
+                           WarpShared<T> &sh, float *qbuf /* 32 x kMaxDof */, float *skel = nullptr) {
     const unsigned full = 0xffffffffu;
     const int lane = threadIdx.x & 31;
     const int64_t split = edge_split(P);
@@ -212,8 +216,13 @@ __device__ void edge_warps(const EdgeParams &P, const DevRobot *rb_st, const Obs
             const Want w{true, false, false};
             uint8_t v = 1;
             int slot = -1;
-            const int st = warp_check<MODE, T, 1>(sh, rb, ob, qbuf + lane * kMaxDof, mine, nm, w, &v, nullptr, nullptr,
-                                                  MODE == 2 ? &P.ps : nullptr, &slot);
+            int st;
+            if constexpr (MODE == 2)
+                st = warp_check_any<1, kThreads>(sh, skel, rb, ob, qbuf + lane * kMaxDof, mine, nm, &v, nullptr, &P.ps,
+                                                 &slot);
+            else
+                st = warp_check<MODE, T, 1>(sh, rb, ob, qbuf + lane * kMaxDof, mine, nm, w, &v, nullptr, nullptr,
+                                            nullptr, &slot);
             if (mine) edge_outcome<MODE>(P, e, k, st, slot, v);
             todo &= ~m;
             __syncwarp();

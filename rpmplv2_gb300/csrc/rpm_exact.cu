@@ -911,39 +911,40 @@ __global__ void __launch_bounds__(kThreads) k_extend_spines(const __grid_constan
                                P.expanded != 0, P.q_new + c * D, sk_end);
 }
 
-// computeReachedState: one warp per horizon state.  Every lane runs the spine
-// (the same arithmetic, so no broadcasts are needed); the lanes split the
-// obstacles of computeDistanceUnderestimation, whose first negative value
-// (any lane, any link) makes the reference return 0 without updating the state.
+// computeReachedState: one warp per horizon state, its state in shared memory
+// (SpineWarp) and the spine spread over the lanes (extend_spine_warp); the
+// lanes split the obstacles of computeDistanceUnderestimation, whose first
+// negative value (any lane, any link) makes the reference return 0 without
+// updating the state.
 __global__ void __launch_bounds__(kThreads) k_reached_states(const __grid_constant__ SpineParams P) {
     const unsigned full = 0xffffffffu;
     const int lane = threadIdx.x & 31;
-    __shared__ double scw[kThreads / 32][2 * kMaxDof];
+    __shared__ SpineWarp sw_all[kThreads / 32];
     const int64_t h = (int64_t)blockIdx.x * (blockDim.x / 32) + (threadIdx.x >> 5);
     if (h >= P.C) return;
-    double *sc = scw[threadIdx.x >> 5];
+    SpineWarp &w = sw_all[threadIdx.x >> 5];
     const DevRobot &rb = *P.robot;
     const int D = rb.D, L = D;
-    const float *qe = P.qe + h * D;
-    float qn[kMaxDof], pn[kMaxDof], qs[kMaxDof], p[kMaxDof];
-    float skn[3 * (kMaxDof + 1)], sk[3 * (kMaxDof + 1)];   // skeletons of the layer's start and end
-    const int NP = 3 * (D + 1);
-    for (int k = 0; k < D; ++k) qn[k] = P.q_cur[k];
+    if (lane < D) {
+        w.qn[lane] = P.q_cur[lane];
+        w.qe[lane] = P.qe[h * D + lane];
+    }
     const float d_cur = (float)P.cur_dist[0];
     int status = kStTrapped;
     if (d_cur > 0.f) {
-        for (int i = 0; i < L; ++i) pn[i] = P.cur_prof[i];
+        if (lane < L) w.pn[lane] = P.cur_prof[lane];
         float dn = d_cur;
         status = kStNone;
-        skel_ref_warp(rb, qn, skn, sc);
+        skel_ref_shared(rb, w.qn, w.skn, w.sc);
         for (int layer = 0; layer < P.num_layers; ++layer) {
-            status = extend_spine(rb, qn, skn, dn, pn, qe, P.num_iter, P.expanded != 0, qs, sk, sc);
-            for (int k = 0; k < D; ++k) qn[k] = qs[k];
-            for (int k = 0; k < NP; ++k) skn[k] = sk[k];
+            status = extend_spine_warp(rb, w, dn, P.num_iter, P.expanded != 0);
+            if (lane < D) w.qn[lane] = w.qs[lane];
+            for (int k = lane; k < 3 * (D + 1); k += 32) w.skn[k] = w.sk[k];
+            __syncwarp();
             float d_c = P.maxd;
             bool negative = false;
             for (int i = 0; i < L && !negative; ++i) {
-                const float *S0 = sk + 3 * i, *S1 = S0 + 3;
+                const float *S0 = w.sk + 3 * i, *S1 = S0 + 3;
                 float lmin = P.maxd;
                 bool neg = false;
                 for (int j = lane; j < P.n; j += 32) {
@@ -970,25 +971,25 @@ __global__ void __launch_bounds__(kThreads) k_reached_states(const __grid_consta
                 negative = __any_sync(full, neg);
 #pragma unroll
                 for (int off = 16; off > 0; off >>= 1) lmin = min_std(lmin, __shfl_xor_sync(full, lmin, off));
-                p[i] = lmin;
+                if (lane == 0) w.p[i] = lmin;
                 d_c = min_std(d_c, lmin);
             }
+            __syncwarp();
             float d;
             if (!negative) {
                 d = d_c;
                 dn = d_c;
-                for (int i = 0; i < L; ++i) pn[i] = p[i];
+                if (lane < L) w.pn[lane] = w.p[lane];
             } else {
                 d = 0.f;
                 dn = -1.f;
             }
+            __syncwarp();
             if (d < P.d_crit || status != kStAdvanced) break;
         }
     }
-    if (lane == 0) {
-        for (int k = 0; k < D; ++k) P.q_new[h * D + k] = qn[k];
-        P.status[h] = status;
-    }
+    if (lane < D) P.q_new[h * D + lane] = w.qn[lane];
+    if (lane == 0) P.status[h] = status;
 }
 
 cudaError_t launch_enclosing_radii(const SpineParams &p, cudaStream_t st) {

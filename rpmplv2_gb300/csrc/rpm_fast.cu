@@ -228,7 +228,8 @@ __global__ void __launch_bounds__(kThreads) k_edges_fp32(const __grid_constant__
     __shared__ WarpShared<float> wsh[kThreads / 32];
     __shared__ float qbuf[kThreads / 32][32 * kMaxDof];
     if (P.nseg_lane != 1) {   // several segments: robots and scenes from global memory
-        edge_warps<2, float>(P, nullptr, nullptr, P.nmf, wsh[threadIdx.x >> 5], qbuf[threadIdx.x >> 5]);
+        edge_warps<2, float>(P, nullptr, nullptr, P.nmf, wsh[threadIdx.x >> 5], qbuf[threadIdx.x >> 5],
+                             reinterpret_cast<float *>(smem));
         return;
     }
     const Seg &sg = P.segs[0].seg;
@@ -255,11 +256,17 @@ __global__ void __launch_bounds__(kThreads) k_edges_fp32(const __grid_constant__
         __syncthreads();
         ob.aos = aos;
     }
-    edge_warps<2, float>(P, &rb, &ob, P.nmf, wsh[threadIdx.x >> 5], qbuf[threadIdx.x >> 5]);
+    // the skeleton buffer follows the robot, the rows and their per-obstacle copy
+    float *skel = reinterpret_cast<float *>(smem + sizeof(DevRobot) + (size_t)kFRows * sg.n_pad * sizeof(float) +
+                                            (sg.n_pad <= kAosMaxPad ? (size_t)sg.n_pad * kFRows * sizeof(float) : 0));
+    edge_warps<2, float>(P, &rb, &ob, P.nmf, wsh[threadIdx.x >> 5], qbuf[threadIdx.x >> 5], skel);
 }
 
 cudaError_t launch_edges_fp32(const EdgeParams &p, int grid, size_t smem, cudaStream_t st) {
     if (p.nseg_lane == 1 && p.segs[0].seg.n_pad <= kAosMaxPad) smem += (size_t)p.segs[0].seg.n_pad * kFRows * sizeof(float);
+    int dmax = 1;   // the skeleton buffer of the order-free driver
+    for (int k = 0; k < p.nseg_lane; ++k) dmax = std::max(dmax, (int)p.segs[k].D);
+    smem += (size_t)kThreads * 3 * (dmax + 1) * sizeof(float);
     static std::atomic<uint64_t> attr{0};
     ensure_smem_limit(k_edges_fp32, 160 * 1024, attr);
     k_edges_fp32<<<grid, kThreads, smem, st>>>(p);

@@ -171,6 +171,101 @@ static __device__ int extend_spine(const DevRobot &rb, const float *q, const flo
         for (int k = 0; k < NP; ++k) skt[k] = sk_new[k];
     }
 }
+
+// ---------------------------------------------------------------------------
+// One spine with the whole warp (DRGBT's horizon: one warp per state).  The
+// state lives in shared memory and the work is spread over the lanes: the
+// enclosing-radius rows one per lane, the column sums R->col(j).dot(delta_q)
+// one per lane (rows in index order), the joints one per lane; the step, the
+// start's radii and rho in lane 0, in index order.  Every float operation is
+// the one extend_spine performs, in its order, so the results are the same
+// bits.
+struct SpineWarp {
+    float qn[kMaxDof], pn[kMaxDof], qe[kMaxDof];   // state, its profile, the target
+    float qt[kMaxDof], qs[kMaxDof], dq[kMaxDof], rho_prof[kMaxDof], p[kMaxDof];
+    float rk[kMaxDof + 1];
+    float skn[3 * (kMaxDof + 1)], skt[3 * (kMaxDof + 1)], sk[3 * (kMaxDof + 1)];
+    float rows[kMaxDof][kMaxDof + 1];
+    float col[kMaxDof + 1];
+    double sc[2 * kMaxDof];
+};
+
+// The reference's float skeleton of q (shared memory) into sk (shared
+// memory): joint sines in parallel, then lane 0 runs the chain.
+__device__ __forceinline__ void skel_ref_shared(const DevRobot &rb, const float *q, float *sk, double *sc) {
+    const int lane = threadIdx.x & 31;
+    __syncwarp();
+    if (lane < rb.D) taylor_sincos((double)q[lane], &sc[2 * lane], &sc[2 * lane + 1]);
+    __syncwarp();
+    if (lane == 0) {
+        SkelWalker<1> sw;
+        sw.begin();
+        sw.w.sc = sc;
+        for (int k = 0; k <= rb.D; ++k) sw.point(rb, q, k, sk + 3 * k);
+    }
+    __syncwarp();
+}
+
+// extendSpine from w.qn (skeleton w.skn, distance d, profile w.pn) towards
+// w.qe; the end goes to w.qs and its skeleton to w.sk.  Returns the status
+// (the same in every lane).
+static __device__ int extend_spine_warp(const DevRobot &rb, SpineWarp &w, float d, int num_iter, bool expanded) {
+    const int lane = threadIdx.x & 31;
+    const int D = rb.D, L = D, NP = 3 * (D + 1);
+    __syncwarp();
+    if (d <= 0.f) {
+        if (lane < D) w.qs[lane] = w.qn[lane];
+        for (int k = lane; k < NP; k += 32) w.sk[k] = w.skn[k];
+        __syncwarp();
+        return kStTrapped;
+    }
+    for (int k = lane; k < NP; k += 32) w.skt[k] = w.skn[k];
+    if (lane < D) { w.qt[lane] = w.qn[lane]; w.rho_prof[lane] = 0.f; }
+    float rho = 0.f;   // lane 0's copy is the one used
+    int counter = 0;
+    __syncwarp();
+    for (;;) {
+        if (lane < D) {
+            w.dq[lane] = fabsf(w.qe[lane] - w.qt[lane]);
+            enclosing_row(rb, w.skt, lane, w.rows[lane]);
+        }
+        __syncwarp();
+        if (lane <= D) {
+            float c = 0.f;
+            for (int i = 0; i < D; ++i) c = c + w.rows[i][lane] * w.dq[i];
+            w.col[lane] = c;
+        }
+        __syncwarp();
+        float step = 0.f;
+        if (lane == 0) {
+            if (expanded) {
+                step = INFINITY;
+                for (int i = 0; i < D; ++i) step = min_std(step, (w.pn[i] - w.rho_prof[i]) / w.col[i + 1]);
+            } else {
+                step = (d - rho) / w.col[D];
+            }
+        }
+        step = __shfl_sync(0xffffffffu, step, 0);
+        const bool reached = step > 1.f;
+        if (lane < D) w.qs[lane] = reached ? w.qe[lane] : w.qt[lane] + step * (w.qe[lane] - w.qt[lane]);
+        skel_ref_shared(rb, w.qs, w.sk, w.sc);
+        if (++counter == num_iter || reached) return reached ? kStReached : kStAdvanced;
+        if (lane >= 1 && lane <= L) w.rk[lane] = col_dist(w.skn + 3 * lane, w.sk + 3 * lane);
+        __syncwarp();
+        if (lane == 0) {
+            float rk_prev = 0.f;
+            for (int k = 1; k <= L; ++k) {
+                const float rk = w.rk[k];
+                w.rho_prof[k - 1] = max_std(rk_prev, rk);
+                rk_prev = rk;
+                rho = max_std(rho, rk);
+            }
+        }
+        for (int k = lane; k < NP; k += 32) w.skt[k] = w.sk[k];
+        if (lane < D) w.qt[lane] = w.qs[lane];
+        __syncwarp();
+    }
+}
 #endif
 
 cudaError_t launch_enclosing_radii(const SpineParams &p, cudaStream_t st);

@@ -69,6 +69,13 @@ constexpr int64_t kLaneBinnedBatch = 32768;
 // obstacles (measured crossover for spatial 10-DOF edges at 0.05 rad: the
 // lane pass 10 % faster at 100 boxes, the warp pass 19 % faster at 130).
 constexpr int kWideEdgeObstacles = 110;
+// FP32+recheck edges, whose lane pass culls obstacles per warp: the warp pass
+// only from this many obstacles and batches above this many edges (measured on
+// spatial 10-DOF edges at 0.05 rad: the lane pass faster at every size up to
+// 500 boxes and up to 32,768 edges at 1000 boxes; 1.7x slower at 1000 boxes
+// and 262,144 edges).
+constexpr int kWideEdgeObstacles32 = 700;
+constexpr int64_t kWideEdgeBatch32 = 65536;
 
 // Sorted copy of one scene version: slot s holds original obstacle idx[s].
 // Static obstacles come first, then moving ones, then ground ones, each group
