@@ -373,6 +373,85 @@ template <> struct SkelWalker<2> {
     }
 };
 
+#ifdef __CUDACC__
+// ------------------------------------------------ warp forward kinematics --
+// The FP64 chain of SkelWalker<MODE> (MODE 0: FP64 points; MODE 1: the
+// reference's float skeleton) run by a whole warp: lane e < 9 holds R[e]
+// (row e / 3, column e % 3), lanes 9-11 hold p[lane - 9].  Each element is
+// computed with the operations fk_step_d and SkelWalker use, in their order,
+// so the points are the same bits; the serial chain per joint is a few
+// shuffles and three products instead of about eighty FP64 operations.
+// Every lane of the warp calls it; sc holds the joints' sines and cosines
+// (taylor_sincos, computed ahead); lanes 9-11 write the D + 1 points to out.
+template <int MODE, typename TO>
+__device__ void skel_coop(const DevRobot &rb, const double *sc, TO *out) {
+    const unsigned full = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    const bool is_r = lane < 9, is_p = lane >= 9 && lane < 12;
+    const int row = is_r ? lane / 3 : (is_p ? lane - 9 : 0);
+    const int col = is_r ? lane % 3 : 0;
+    double v = (is_r && lane % 4 == 0) ? 1.0 : 0.0;   // R = I, p = 0
+    auto rowval = [&](int t) { return __shfl_sync(full, v, 3 * row + t); };
+    auto emit = [&](int kp, double x) {
+        if (is_p) out[3 * kp + row] = (TO)x;
+    };
+    auto step = [&](int k) {
+        const double r0 = rowval(0), r1 = rowval(1), r2 = rowval(2);
+        if (is_p) {
+            const double *o = rb.oxyz[k];
+            v = dadd(dadd(dadd(dmul(r0, o[0]), dmul(r1, o[1])), dmul(r2, o[2])), v);
+        } else if (is_r && !((rb.rot_identity_mask >> k) & 1)) {
+            const double *M = rb.orot[k];
+            v = dadd(dadd(dmul(r0, M[col]), dmul(r1, M[3 + col])), dmul(r2, M[6 + col]));
+        }
+        // columns (IA, IB) <- (a c + b s, b c - a s), as rot_cols_d
+        const int ax = rb.axis[k];
+        const int ia = ax == 0 ? 1 : (ax == 1 ? 2 : 0), ib = ax == 0 ? 2 : (ax == 1 ? 0 : 1);
+        const double sn = sc[2 * k], cs = sc[2 * k + 1];
+        const double x = __shfl_sync(full, v, is_r ? 3 * row + (col == ia ? ib : ia) : lane);
+        if (is_r && col == ia) v = dadd(dmul(v, cs), dmul(x, sn));
+        else if (is_r && col == ib) v = dadd(dmul(v, cs), -dmul(x, sn));
+    };
+    const int D = rb.D;
+    if (rb.kind != RPM_ROBOT_XARM6) {
+        for (int k = 0; k < D; ++k) {
+            step(k);
+            emit(k, v);
+        }
+        const double r0 = rowval(0), r1 = rowval(1), r2 = rowval(2);
+        const double *o = rb.oxyz[D];
+        emit(D, dadd(dadd(dadd(dmul(r0, o[0]), dmul(r1, o[1])), dmul(r2, o[2])), v));
+        return;
+    }
+    emit(0, 0.0);
+    step(0);
+    step(1);
+    emit(1, v);
+    step(2);
+    emit(2, v);
+    step(3);
+    {
+        const double z = rowval(2);
+        emit(3, dadd(v, -dmul(z, 0.25)));
+    }
+    step(4);
+    emit(4, v);
+    {
+        const double x = rowval(0);
+        emit(5, dadd(v, dmul(x, 0.076)));
+    }
+    step(5);
+    const double z = rowval(2);
+    if constexpr (MODE == 0) {
+        const double g = rb.gripper_d, g3 = dmul(0.3, rb.gripper_d);
+        emit(6, dadd(dadd(v, dmul(g, z)), -dmul(g3, z)));
+    } else if (is_p) {
+        const float ps = (float)dadd(v, dmul(rb.gripper_d, z));
+        out[18 + row] = (TO)fadd(ps, -fmul(rb.grip03_f, (float)z));
+    }
+}
+#endif
+
 // --------------------------------------------------- shared-memory staging --
 __device__ __forceinline__ uint32_t smem_addr(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
 

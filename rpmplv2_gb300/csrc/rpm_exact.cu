@@ -169,12 +169,7 @@ __device__ __forceinline__ void pair_skel_warp(const DevRobot &rb, const float *
         a.coll = 0;
     }
     __syncwarp();
-    if (lane == 0) {
-        SkelWalker<0> sw;
-        sw.sc = sc;
-        sw.begin();
-        for (int i = 0; i <= rb.D; ++i) sw.point(rb, q, i, out + 3 * i);
-    }
+    skel_coop<0, double>(rb, sc, out);
     __syncwarp();
 }
 
@@ -718,16 +713,10 @@ __global__ void __launch_bounds__(kNearCtaThreads) k_distance_nearest_cta(const 
     Num<T> nm;
     if (MODE == 0) { nm.eq = (T)P.nmd.eq; nm.maxd = (T)P.nmd.maxd; }
     else { nm.eq = (T)P.nmf.eq; nm.maxd = (T)P.nmf.maxd; }
-    if (threadIdx.x < 32) {   // joint sines in parallel, then the chain (the same bits as computing them in turn)
+    if (threadIdx.x < 32) {   // joint sines in parallel, then the chain spread over the warp (the same bits)
         if ((int)threadIdx.x < D) taylor_sincos((double)q[threadIdx.x], &sc[2 * threadIdx.x], &sc[2 * threadIdx.x + 1]);
         __syncwarp();
-        if (threadIdx.x == 0) {
-            SkelWalker<MODE> sw;
-            sw.begin();
-            if constexpr (MODE == 0) sw.sc = sc;
-            else sw.w.sc = sc;
-            for (int k = 0; k <= D; ++k) sw.point(rb, q, k, skel + 3 * k);
-        }
+        skel_coop<MODE, T>(rb, sc, skel);
     }
     for (int i = threadIdx.x; i < L; i += blockDim.x) {
         lkey[i] = Key<T>::of(nm.maxd);

@@ -191,18 +191,13 @@ struct SpineWarp {
 };
 
 // The reference's float skeleton of q (shared memory) into sk (shared
-// memory): joint sines in parallel, then lane 0 runs the chain.
+// memory): joint sines in parallel, then the chain spread over the warp.
 __device__ __forceinline__ void skel_ref_shared(const DevRobot &rb, const float *q, float *sk, double *sc) {
     const int lane = threadIdx.x & 31;
     __syncwarp();
     if (lane < rb.D) taylor_sincos((double)q[lane], &sc[2 * lane], &sc[2 * lane + 1]);
     __syncwarp();
-    if (lane == 0) {
-        SkelWalker<1> sw;
-        sw.begin();
-        sw.w.sc = sc;
-        for (int k = 0; k <= rb.D; ++k) sw.point(rb, q, k, sk + 3 * k);
-    }
+    skel_coop<1, float>(rb, sc, sk);
     __syncwarp();
 }
 
