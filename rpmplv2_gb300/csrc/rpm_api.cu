@@ -467,16 +467,27 @@ int enqueue_segments(rpm_ctx *ctx, int prec, const std::vector<SegReq> &reqs_in,
     if (rc) return rc;
     sc->last_configs = total;
     CK(cudaMemsetAsync(sc->counters, 0, 4 * sizeof(uint32_t), st));
-    // A large FP32 lane-layout request is checked in binned order
-    // (launch_bin_configs); its isValid and distance launches share the order.
-    // The order lives with the recheck lists, sized for the stream's largest
-    // batch (get_scratch above), so a steady stream of requests allocates nothing.
-    if (prec == RPM_PREC_FP32_RECHECK && reqs_in.size() == 1 && reqs_in[0].count >= kBinMinConfigs &&
-        reqs_in[0].count <= INT32_MAX && !reqs.empty() && reqs[0].wide == 0 &&
-        (int64_t)sc->perm_cap >= reqs_in[0].count && sc->bins) {
-        const SegReq &r0 = reqs_in[0];
-        CK(launch_bin_configs(r0.q, r0.count, ctx->robots[r0.scene->robot].desc.num_dofs, sc->bins, sc->perm, st));
-        for (SegReq &r : reqs) r.perm = sc->perm;
+    // Every FP32 lane-layout request of at least kBinMinConfigs configurations is
+    // checked in binned order (launch_bin_configs), each with its own slice of the
+    // order; the isValid and distance launches of a request share its slice.  The
+    // order lives with the recheck lists, sized for the stream's largest batch
+    // (get_scratch above), so a steady stream of requests allocates nothing.
+    if (prec == RPM_PREC_FP32_RECHECK && sc->bins) {
+        size_t used_perm = 0;
+        for (size_t k = 0; k < reqs.size(); ++k) {
+            SegReq &r = reqs[k];
+            if (r.wide != 0 || r.count < kBinMinConfigs || r.count > INT32_MAX) continue;
+            if (k > 0 && reqs[k - 1].perm && reqs[k - 1].q == r.q && reqs[k - 1].count == r.count &&
+                reqs[k - 1].scene == r.scene) {
+                r.perm = reqs[k - 1].perm;   // the other output of the same request
+                continue;
+            }
+            if (used_perm + (size_t)r.count > sc->perm_cap) break;
+            int32_t *slice = sc->perm + used_perm;
+            CK(launch_bin_configs(r.q, r.count, ctx->robots[r.scene->robot].desc.num_dofs, sc->bins, slice, st));
+            r.perm = slice;
+            used_perm += (size_t)r.count;
+        }
     }
     sc->timed = ctx->timing && total > 0;
     sc->had_recheck = prec == RPM_PREC_FP32_RECHECK;

@@ -495,7 +495,8 @@ __device__ int warp_check(WarpShared<T> &sh, const DevRobot &rb, const ObsView<T
         int hj = 0x7fffffff;
         T cur = nm.maxd;
         int nb = 0, nd = 0;
-        for (int j = 0; j < ob.n; ++j) {
+        // the obstacle loop's body for obstacle j
+        auto obstacle = [&](const int j) {
             const bool wb = need_b && !hitb;
             const bool wd = need_d && (hj == 0x7fffffff || (w.profile && j < hj));
             bool qb = false, qd = false;
@@ -552,6 +553,69 @@ __device__ int warp_check(WarpShared<T> &sh, const DevRobot &rb, const ObsView<T
                 RPM_PUSH_AND_DRAIN(qb, nb, qb, item, drain_bool, hitb = (sh.flags[lane] & 1) != 0);
             if constexpr (KIND != 1)
                 RPM_PUSH_AND_DRAIN(qd, nd, qd, item, drain_dist, (hj = sh.hitj[lane], cur = Key<T>::value(sh.lmin[lane])));
+                };
+        if constexpr (MODE == 2) {
+            // The FP32 pass culls per warp, as warp_check_any does: the bounding box of
+            // this link's segments over the lanes still working, tested against 32
+            // obstacles at a time with the largest threshold of any lane, so an obstacle
+            // it rejects is one no lane's own test would queue.
+            float ulo[3], uhi[3];
+            const bool working = need_b || need_d;
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+                ulo[c] = !working ? INFINITY : (lo[c] == lo[c] ? (float)lo[c] : -INFINITY);
+                uhi[c] = !working ? -INFINITY : (hi[c] == hi[c] ? (float)hi[c] : INFINITY);
+#pragma unroll
+                for (int off = 16; off > 0; off >>= 1) {
+                    ulo[c] = fminf(ulo[c], __shfl_xor_sync(full, ulo[c], off));
+                    uhi[c] = fmaxf(uhi[c], __shfl_xor_sync(full, uhi[c], off));
+                }
+            }
+            for (int base = 0; base < ob.n; base += 32) {
+                const bool wb_l = need_b && !hitb;
+                const bool wd_l = need_d && (hj == 0x7fffffff || w.profile);
+                const bool hunt_l = wd_l && hj != 0x7fffffff;
+                const bool any_b = __any_sync(full, wb_l);
+                const bool any_hunt = __any_sync(full, hunt_l);
+                const bool any_d = __any_sync(full, wd_l && !hunt_l);
+                float xl = (wd_l && !hunt_l) ? (float)(w.profile ? cur : smin(best, cur)) : -INFINITY;
+#pragma unroll
+                for (int off = 16; off > 0; off >>= 1) xl = fmaxf(xl, __shfl_xor_sync(full, xl, off));
+                bool cand = false;
+                const int jl = base + lane;
+                if (jl < ob.n) {
+                    float o[6], tj;
+                    bool gr;
+                    if (ob.aos != nullptr) {
+                        const float4 a = ob.aos[2 * jl], b = ob.aos[2 * jl + 1];
+                        o[0] = a.x; o[1] = a.y; o[2] = a.z; o[3] = a.w; o[4] = b.x; o[5] = b.y;
+                        tj = b.z;
+                        gr = b.w != 0.f;
+                    } else {
+#pragma unroll
+                        for (int k = 0; k < 6; ++k) o[k] = (float)ob.rows[k * ob.n_pad + jl];
+                        tj = (float)ob.tol(jl);
+                        gr = ob.is_ground(jl);
+                    }
+                    if (!(ground_skip && gr)) {
+                        const float g2 = gap2_bb(ulo, uhi, o);
+                        cand = any_b && !(g2 > (float)tb2);
+                        if (any_hunt) cand = cand || !(g2 > (float)hunt2);
+                        if (any_d) {
+                            const float sd = smin(xl, tj) + (float)r + (float)nm.eq + (float)dmargin;
+                            cand = cand || !(sd > 0.f && g2 > sd * sd);
+                        }
+                    }
+                }
+                unsigned cm = __ballot_sync(full, cand);
+                while (cm != 0u) {
+                    const int j = base + __ffs(cm) - 1;
+                    cm &= cm - 1u;
+                    obstacle(j);
+                }
+            }
+        } else {
+            for (int j = 0; j < ob.n; ++j) obstacle(j);
         }
         __syncwarp();
         if (nb > 0) drain_bool<MODE, T, kFlat>(sh, rb, ob, nm, i, nb, ps);
