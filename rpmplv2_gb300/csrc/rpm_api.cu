@@ -1336,6 +1336,7 @@ int reached_states_locked(rpm_ctx *ctx, int32_t scene_id, int32_t precision, con
     p.cur_near = np.nearest;
     p.n = np.n;
     p.maxd = np.nmf.maxd;
+    p.L = L;
     CK(launch_reached_states(p, st));
     if (short_h) {
         // computeDistance(q_reached, true): the exact FP64 value for the FP64 and

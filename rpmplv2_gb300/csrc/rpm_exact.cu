@@ -905,10 +905,45 @@ __global__ void __launch_bounds__(kThreads) k_extend_spines(const __grid_constan
 // lanes split the obstacles of computeDistanceUnderestimation, whose first
 // negative value (any lane, any link) makes the reference return 0 without
 // updating the state.
+// The underestimation planes of the current state's nearest points, one per
+// (link i, obstacle j) at [i * n + j]: the unit normal u = normalized(R - O)
+// (unchanged when zero) and the point O, with skip = 1 where |O| is
+// MAX_DISTANCE (a pair the reference passes over).  They do not change over
+// the horizon, so a CTA computes them once (the same operations as per use).
+struct Plane {
+    float u[3], O[3];
+    int skip;
+};
+
+__device__ __forceinline__ Plane make_plane(const SpineParams &P, int L, int i, int j) {
+    Plane pl;
+    float R[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        R[k] = P.cur_near[((size_t)j * 6 + k) * L + i];
+        pl.O[k] = P.cur_near[((size_t)j * 6 + 3 + k) * L + i];
+    }
+    pl.skip = sqrtf(dot3f(pl.O, pl.O)) == P.maxd;
+    pl.u[0] = R[0] - pl.O[0]; pl.u[1] = R[1] - pl.O[1]; pl.u[2] = R[2] - pl.O[2];
+    const float z = dot3f(pl.u, pl.u);
+    if (z > 0.f) {
+        const float nz = sqrtf(z);
+#pragma unroll
+        for (int k = 0; k < 3; ++k) pl.u[k] = pl.u[k] / nz;
+    }
+    return pl;
+}
+
 __global__ void __launch_bounds__(kThreads) k_reached_states(const __grid_constant__ SpineParams P) {
     const unsigned full = 0xffffffffu;
     const int lane = threadIdx.x & 31;
     __shared__ SpineWarp sw_all[kThreads / 32];
+    extern __shared__ __align__(16) unsigned char planes_smem[];
+    Plane *planes = P.planes ? reinterpret_cast<Plane *>(planes_smem) : nullptr;
+    if (planes) {
+        for (int p = threadIdx.x; p < P.L * P.n; p += blockDim.x) planes[p] = make_plane(P, P.L, p / P.n, p % P.n);
+        __syncthreads();
+    }
     const int64_t h = (int64_t)blockIdx.x * (blockDim.x / 32) + (threadIdx.x >> 5);
     if (h >= P.C) return;
     SpineWarp &w = sw_all[threadIdx.x >> 5];
@@ -937,20 +972,9 @@ __global__ void __launch_bounds__(kThreads) k_reached_states(const __grid_consta
                 float lmin = P.maxd;
                 bool neg = false;
                 for (int j = lane; j < P.n; j += 32) {
-                    float O[3], R[3];
-#pragma unroll
-                    for (int k = 0; k < 3; ++k) {
-                        R[k] = P.cur_near[((size_t)j * 6 + k) * L + i];
-                        O[k] = P.cur_near[((size_t)j * 6 + 3 + k) * L + i];
-                    }
-                    if (sqrtf(dot3f(O, O)) == P.maxd) continue;
-                    float u[3] = {R[0] - O[0], R[1] - O[1], R[2] - O[2]};
-                    const float z = dot3f(u, u);
-                    if (z > 0.f) {
-                        const float nz = sqrtf(z);
-#pragma unroll
-                        for (int k = 0; k < 3; ++k) u[k] = u[k] / nz;
-                    }
+                    const Plane pl = planes ? planes[i * P.n + j] : make_plane(P, L, i, j);
+                    if (pl.skip) continue;
+                    const float *O = pl.O, *u = pl.u;
                     float a[3] = {S0[0] - O[0], S0[1] - O[1], S0[2] - O[2]};
                     float b[3] = {S1[0] - O[0], S1[1] - O[1], S1[2] - O[2]};
                     const float d = min_std(dot3f(a, u), dot3f(b, u)) - rb.radius_f[i];
@@ -995,7 +1019,13 @@ cudaError_t launch_extend_spines(const SpineParams &p, cudaStream_t st) {
 
 cudaError_t launch_reached_states(const SpineParams &p, cudaStream_t st) {
     const unsigned grid = (unsigned)((p.C + kThreads / 32 - 1) / (kThreads / 32));
-    if (grid) k_reached_states<<<grid, kThreads, 0, st>>>(p);
+    if (!grid) return cudaSuccess;
+    // the plane table in shared memory when it is small next to the work of the
+    // CTA's states (a few states, scenes of up to a few hundred obstacles)
+    SpineParams q = p;
+    const size_t bytes = (size_t)p.L * p.n * sizeof(Plane);
+    q.planes = (p.L > 0 && p.n > 0 && bytes <= 16384) ? 1 : 0;
+    k_reached_states<<<grid, kThreads, q.planes ? bytes : 0, st>>>(q);
     return cudaGetLastError();
 }
 

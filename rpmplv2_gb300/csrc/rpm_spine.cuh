@@ -39,6 +39,8 @@ struct SpineParams {
     const float *cur_near;   // [n][6][L]
     int32_t n;
     float maxd;              // MAX_DISTANCE
+    int32_t L;               // reached states: links (sizes the plane table below)
+    int32_t planes;          // reached states: 1 = the CTA keeps the underestimation planes in shared memory
 };
 
 #ifdef __CUDACC__
