@@ -440,7 +440,7 @@ def serve_line(eng, serve):
                              "sizes log-uniform 1-65,536, isValid / distance / edge in equal shares, of which 10% "
                              "replaced by DRGBT steps (horizon of reached states, MotionValidity with moving boxes)",
                  "memory_budget_bytes": 8 << 30, "bulk_slots": 4, "express_slots": 24, "express_work": 8192,
-                 "chunk_work": 65536, "bulk_sms": "all but 32 (green context)"})
+                 "chunk_work": 65536, "bulk_sms": "all but 48 (green context)"})
     # capacity: the same trace submitted at once; latency at a rate the engine sustains
     t = srv.replay(wl["requests"], [0.0] * len(wl["requests"]))
     summ["capacity_req_per_s"] = len(t) / max(x.t_done for x in t)

@@ -472,7 +472,7 @@ typedef struct rpm_server_config {
     int32_t chunk_work;          /* work per bulk launch; 0: 65,536 */
     int32_t bulk_sms;            /* > 0: the bulk streams run in an SM partition (a green context) of this
                                     many SMs (rounded up to the driver's granularity, 8 on GB300), so the
-                                    other SMs only run express work; 0: all SMs but 32 where the driver
+                                    other SMs only run express work; 0: all SMs but 48 where the driver
                                     offers green contexts, else every SM; -1: bulk uses every SM */
     int32_t reserved;
 } rpm_server_config;

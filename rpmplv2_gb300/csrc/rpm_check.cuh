@@ -761,6 +761,63 @@ __device__ int warp_check_any(WarpShared<float> &sh, float *skel, const DevRobot
     bool stop = !active;          // register copy of flags bit 0 (settled collision / settled hit)
     float cur = nm.maxd;          // register copy of the running minimum (KIND 3)
     int nq = 0;
+    int seed_j = -1;              // KIND 3: the obstacle every lane checked first on the first link
+    if constexpr (KIND == 3) {
+        // Seed.  Until a lane has a distance its threshold is MAX_DISTANCE, so the
+        // first link would queue every obstacle, and the warp's cull would keep
+        // them all.  So the warp first checks, on the first link it visits, the
+        // non-ground obstacle nearest to the union box of its lanes' segments (its
+        // lanes hold similar configurations); every lane's threshold then starts at
+        // a real distance.  The pair is skipped when the loop reaches it.
+        const int i0 = any_order_link(rb, 0);
+        float ulo[3], uhi[3];
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            const float a = mine[(3 * i0 + c) * NT], b = mine[(3 * i0 + 3 + c) * NT];
+            const float l = a < b ? a : b, h = a < b ? b : a;
+            ulo[c] = stop ? INFINITY : (l == l ? l : -INFINITY);
+            uhi[c] = stop ? -INFINITY : (h == h ? h : INFINITY);
+#pragma unroll
+            for (int off = 16; off > 0; off >>= 1) {
+                ulo[c] = fminf(ulo[c], __shfl_xor_sync(full, ulo[c], off));
+                uhi[c] = fmaxf(uhi[c], __shfl_xor_sync(full, uhi[c], off));
+            }
+        }
+        float bg = INFINITY;
+        int bj = 0x7fffffff;
+        for (int jl = lane; jl < ob.n; jl += 32) {
+            float o[6];
+            bool gr;
+            if (ob.aos != nullptr) {
+                const float4 a = ob.aos[2 * jl], b = ob.aos[2 * jl + 1];
+                o[0] = a.x; o[1] = a.y; o[2] = a.z; o[3] = a.w; o[4] = b.x; o[5] = b.y;
+                gr = b.w != 0.f;
+            } else {
+                ob.box(jl, o);
+                gr = ob.is_ground(jl);
+            }
+            if (gr) continue;
+            const float g2 = gap2_bb(ulo, uhi, o);
+            if (g2 < bg) { bg = g2; bj = jl; }
+        }
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) {
+            const float og = __shfl_xor_sync(full, bg, off);
+            const int oj = __shfl_xor_sync(full, bj, off);
+            if (og < bg || (og == bg && oj < bj)) { bg = og; bj = oj; }
+        }
+        if (bj != 0x7fffffff && __any_sync(full, !stop)) {
+            seed_j = bj;
+            const unsigned m = __ballot_sync(full, !stop);
+            if (!stop) queue[__popc(m & lt_mask)] = (uint32_t)lane | ((uint32_t)bj << 5) | ((uint32_t)i0 << 16);
+            __syncwarp();
+            drain_any<KIND, NT>(sh, skel, rb, ob, nm, queue, __popc(m), ps);
+            __syncwarp();
+            stop = stop || (sh.flags[lane] & 1) != 0;
+            cur = Key<float>::value(sh.lmin[lane]);
+            __syncwarp();
+        }
+    }
     for (int k = 0; k < L; ++k) {
         if (!__any_sync(full, !stop)) break;
         const int i = any_order_link(rb, k);
@@ -841,7 +898,7 @@ __device__ int warp_check_any(WarpShared<float> &sh, float *skel, const DevRobot
                 gr = ob.is_ground(j);
             }
             bool qq = false;
-            if (!stop && !(ground_skip && gr)) {
+            if (!stop && !(ground_skip && gr) && !(k == 0 && j == seed_j)) {
                 const float g2 = gap2_bb(lo, hi, o);
                 if constexpr (KIND == 1) {
                     qq = !(g2 > tb2);

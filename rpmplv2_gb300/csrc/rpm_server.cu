@@ -199,8 +199,10 @@ constexpr int32_t kDefaultExpressWork = 8192;   // units: configurations, an edg
 constexpr int32_t kDefaultBatchWork = 1 << 16;  // bulk batch
 constexpr int32_t kDefaultChunkWork = 1 << 16;  // bulk launch
 // Default bulk partition: all SMs but this many stay free of bulk work (p99 of
-// 2k-8k requests at 12k req/s: 1.27 ms with 16 free, 1.21 ms with 32).
-constexpr int32_t kDefaultExpressOnlySms = 32;
+// 2k-8k requests at 12k req/s, two runs each: 1.05 / 0.97 ms with 32 free,
+// 0.95 / 0.94 ms with 48, 1.26 / 0.98 ms with 64; capacity 24.1k, 23.0k and
+// 21.7k req/s).
+constexpr int32_t kDefaultExpressOnlySms = 48;
 constexpr int64_t kExpressShared = 1024;        // express requests below this share batches
 
 // Units of work: a configuration 1, an edge 8, a horizon state (spines,
