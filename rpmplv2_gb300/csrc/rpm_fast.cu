@@ -222,12 +222,16 @@ cudaError_t launch_edges_wide_fp32(const EdgeParams &p, int grid, size_t smem, c
 }
 
 // FP32 pass of the edge checks (unsettled checks go to the pair recheck or k_edge_recheck).
+// MULTI: several lane-layout segments, robots and scenes read from global
+// memory; otherwise one segment staged in shared memory.  Two instances, so
+// each holds one copy of the check code (the pass is fetch-bound on it).
+template <bool MULTI>
 __global__ void __launch_bounds__(kThreads) k_edges_fp32(const __grid_constant__ EdgeParams P) {
     extern __shared__ __align__(128) unsigned char smem[];
     __shared__ uint64_t bar;
     __shared__ WarpShared<float> wsh[kThreads / 32];
     __shared__ float qbuf[kThreads / 32][32 * kMaxDof];
-    if (P.nseg_lane != 1) {   // several segments: robots and scenes from global memory
+    if constexpr (MULTI) {
         edge_warps<2, float>(P, nullptr, nullptr, P.nmf, wsh[threadIdx.x >> 5], qbuf[threadIdx.x >> 5],
                              reinterpret_cast<float *>(smem));
         return;
@@ -267,9 +271,14 @@ cudaError_t launch_edges_fp32(const EdgeParams &p, int grid, size_t smem, cudaSt
     int dmax = 1;   // the skeleton buffer of the order-free driver
     for (int k = 0; k < p.nseg_lane; ++k) dmax = std::max(dmax, (int)p.segs[k].D);
     smem += (size_t)kThreads * 3 * (dmax + 1) * sizeof(float);
-    static std::atomic<uint64_t> attr{0};
-    ensure_smem_limit(k_edges_fp32, 160 * 1024, attr);
-    k_edges_fp32<<<grid, kThreads, smem, st>>>(p);
+    static std::atomic<uint64_t> attr[2] = {{0}, {0}};
+    if (p.nseg_lane != 1) {
+        ensure_smem_limit(k_edges_fp32<true>, 160 * 1024, attr[1]);
+        k_edges_fp32<true><<<grid, kThreads, smem, st>>>(p);
+    } else {
+        ensure_smem_limit(k_edges_fp32<false>, 160 * 1024, attr[0]);
+        k_edges_fp32<false><<<grid, kThreads, smem, st>>>(p);
+    }
     return cudaGetLastError();
 }
 
