@@ -444,9 +444,13 @@ def serve_line(eng, serve):
     # capacity: the same trace submitted at once; latency at a rate the engine sustains
     t = srv.replay(wl["requests"], [0.0] * len(wl["requests"]))
     summ["capacity_req_per_s"] = len(t) / max(x.t_done for x in t)
+    srv.close()
     for sid in wl["scene_ids"]:
         eng.destroy_scene(sid)
+    # the 12,000 req/s trace on a server of its own (not one just drained of a saturating burst)
     wl12 = serve.serving_workload(eng, seed=5, rate=12000.0, duration=0.5)
+    srv = serve.Server(eng)
+    srv.replay(wl12["requests"][:200], [0.0] * 200)
     t12 = srv.replay(wl12["requests"], wl12["arrivals"], wl12["motions"], period=0.001)
     s12 = serve.latency_summary(t12, wl12["meta"])
     summ["at_12000_req_per_s"] = {k: s12[k] for k in ("queries_per_s", "p50_ms", "p99_ms", "p50_ms_4096", "p99_ms_4096",
