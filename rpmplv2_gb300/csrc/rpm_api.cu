@@ -303,6 +303,9 @@ int get_scratch(rpm_ctx *ctx, cudaStream_t st, int64_t need, Scratch **out) {
     if ((int64_t)s->cap < need) {
         if (s->recheck) {
             CK(cudaStreamSynchronize(st));
+            // cached edge graphs hold the old lists' addresses: capture them again
+            for (auto &g : s->graphs) cudaGraphExecDestroy(g.exec);
+            s->graphs.clear();
             cudaFree(s->recheck);
             cudaFree(s->pairs); cudaFree(s->pcfgs); cudaFree(s->pskel); cudaFree(s->pacc); cudaFree(s->perm);
             s->recheck = nullptr;
