@@ -175,6 +175,9 @@ struct Req {
     int D = 0, L = 0;
     size_t bytes = 0, off = 0;
     rpm_request_timing t{};
+    uint64_t version = 0;           // the scene version its checks read (set before its launches)
+    bool retired = false;           // its slot's worker has read the batch trace and freed its memory
+    bool release_pending = false;   // released by the caller before that: the worker deletes it
 };
 
 struct Slot {
@@ -346,14 +349,24 @@ DevBufs layout(rpm_server *srv, const Req *q) {
 // Host callback at the end of a batch's stream work: marks the slot finished
 // and wakes the workers, so they sleep instead of polling events.  It calls no
 // CUDA function.
+// The stream has reached the end of the batch: every result is in the
+// callers' host buffers, so the requests complete now (status and t_done);
+// the worker retires the slot later (trace, memory) without holding them up.
 void CUDART_CB batch_done(void *arg) {
     Slot *sl = static_cast<Slot *>(arg);
     rpm_server *srv = static_cast<rpm_server *>(sl->srv);
     {
         std::lock_guard<std::mutex> lk(srv->mu);
         sl->finished = true;
+        const double t = now_s();
+        for (Req *q : sl->reqs) {
+            q->t.t_done = t;
+            q->t.scene_version = q->version;
+            q->t.status = 0;
+        }
     }
     srv->cv_work.notify_all();
+    srv->cv_done.notify_all();
 }
 
 // Launch one batch on a reserved slot: copies in, the checks as launches of at
@@ -377,6 +390,7 @@ int launch_batch(rpm_server *srv, Slot &slot, const std::vector<Req *> &batch, i
         if (!s) return fail(RPM_ERR_INVALID, "unknown scene %d", q->r.scene_id);
         scene[k] = s;
         versions[k] = s->version;   // the launches read s->cur, made current with this version
+        batch[k]->version = s->version;
         if (q->r.kind == RPM_REQ_EDGES || q->r.kind == RPM_REQ_MOTION) {
             CK(cudaMemcpyAsync(d.q1, q->r.q1_host, n * q->D * sizeof(float), cudaMemcpyHostToDevice, slot.st));
             CK(cudaMemcpyAsync(d.q2, q->r.q2_host, n * q->D * sizeof(float), cudaMemcpyHostToDevice, slot.st));
@@ -512,18 +526,19 @@ void worker_loop(rpm_server *srv, bool express) {
             if (sl.express != express) continue;
             if (!sl.busy || !sl.finished) continue;
             sl.finished = false;
-            const double t = now_s();
             float ms[3] = {0.f, 0.f, 0.f};
             cudaEventElapsedTime(&ms[0], sl.trace[0], sl.trace[1]);
             cudaEventElapsedTime(&ms[1], sl.trace[1], sl.trace[2]);
             cudaEventElapsedTime(&ms[2], sl.trace[2], sl.done);
-            for (Req *q : sl.reqs) {
+            const double t = now_s();
+            for (Req *q : sl.reqs) {   // status and t_done normally set by the batch's callback
+                if (q->t.status == 1) { q->t.t_done = t; q->t.status = 0; }
                 q->t.h2d_ms = ms[0];
                 q->t.kernel_ms = ms[1];
                 q->t.d2h_ms = ms[2];
-                q->t.t_done = t;
-                q->t.status = 0;
                 srv->arena.release(q->off, q->bytes);
+                q->retired = true;
+                if (q->release_pending) delete q;
             }
             sl.reqs.clear();
             sl.busy = false;
@@ -536,6 +551,7 @@ void worker_loop(rpm_server *srv, bool express) {
             if (q->bytes > srv->arena.size) {
                 q->t.status = RPM_ERR_ADMISSION;
                 q->t.t_done = now_s();
+                q->retired = true;
                 it = srv->incoming.erase(it);
                 srv->cv_done.notify_all();
                 continue;
@@ -575,19 +591,21 @@ void worker_loop(rpm_server *srv, bool express) {
                 queue.pop_front();
             }
             sl.busy = true;   // reserved: only this thread touches the slot
+            sl.reqs = batch;  // before the callback can run: it completes these requests
             const double t = now_s();
+            for (Req *q : batch) {
+                q->t.t_launch = t;
+                q->t.batch_size = (int32_t)batch.size();
+            }
             lk.unlock();      // submissions and polls proceed while the batch is enqueued
             std::vector<uint64_t> versions;
             const int64_t chunk = sl.express ? std::numeric_limits<int64_t>::max() / 16 : (int64_t)srv->cfg.chunk_work;
             const int rc = launch_batch(srv, sl, batch, chunk, versions);
             const float enq_ms = (float)((now_s() - t) * 1e3);
             lk.lock();
-            for (size_t k = 0; k < batch.size(); ++k) {
+            for (size_t k = 0; k < batch.size(); ++k) {   // (the batch may have completed already)
                 Req *q = batch[k];
-                q->t.t_launch = t;
                 q->t.enqueue_ms = enq_ms;
-                q->t.batch_size = (int32_t)batch.size();
-                q->t.scene_version = k < versions.size() ? versions[k] : 0;
             }
             if (rc) {
                 // work already queued for the batch may still use its memory: let it finish first
@@ -595,11 +613,16 @@ void worker_loop(rpm_server *srv, bool express) {
                 cudaGetLastError();
                 sl.finished = false;   // a callback enqueued before the failure may have run
                 const double te = now_s();
-                for (Req *q : batch) { q->t.status = rc; q->t.t_done = te; srv->arena.release(q->off, q->bytes); }
+                for (Req *q : batch) {
+                    q->t.status = rc;
+                    q->t.t_done = te;
+                    srv->arena.release(q->off, q->bytes);
+                    q->retired = true;
+                }
+                sl.reqs.clear();
                 sl.busy = false;
                 srv->cv_done.notify_all();
             } else {
-                sl.reqs = batch;
                 srv->batches++;
             }
             progress = true;
@@ -742,7 +765,8 @@ int rpm_server_release(rpm_server *srv, uint64_t ticket) {
     auto it = srv->reqs.find(ticket);
     if (it == srv->reqs.end()) return fail(RPM_ERR_INVALID, "unknown ticket");
     if (it->second->t.status == 1) return fail(RPM_ERR_INVALID, "request still pending");
-    delete it->second;
+    if (it->second->retired) delete it->second;
+    else it->second->release_pending = true;   // complete but not yet retired: its worker deletes it
     srv->reqs.erase(it);
     return RPM_OK;
 }
@@ -821,6 +845,22 @@ int rpm_server_replay(rpm_server *srv, const rpm_request *reqs, const double *ar
         rpm_request_timing t{};
         const int w = rpm_server_wait(srv, tickets[i], 600.0, &t);
         if (w && !rc) rc = w;
+    }
+    {   // the batch traces: wait until every request's slot has been retired
+        std::unique_lock<std::mutex> lk(srv->mu);
+        srv->cv_done.wait_for(lk, std::chrono::seconds(60), [&] {
+            for (int64_t i = 0; i < n; ++i) {
+                if (!tickets[i]) continue;
+                auto it = srv->reqs.find(tickets[i]);
+                if (it != srv->reqs.end() && !it->second->retired) return false;
+            }
+            return true;
+        });
+    }
+    for (int64_t i = 0; i < n; ++i) {
+        if (!tickets[i]) continue;
+        rpm_request_timing t{};
+        rpm_server_poll(srv, tickets[i], &t);
         t.t_submit -= t0; t.t_admit -= t0; t.t_launch -= t0; t.t_done -= t0;
         out[i] = t;
         rpm_server_release(srv, tickets[i]);
@@ -867,6 +907,9 @@ int rpm_server_destroy(rpm_server *srv) {
     }
     if (srv->bulk_part.g) srv->bulk_part.destroy(srv->bulk_part.g);
     cudaFree(srv->arena_mem);
+    for (Slot &sl : srv->slots)   // released by their callers, never retired
+        for (Req *q : sl.reqs)
+            if (q->release_pending) delete q;
     for (auto &kv : srv->reqs) delete kv.second;
     delete srv;
     return RPM_OK;
