@@ -285,7 +285,7 @@ void free_scratch(Scratch *sc) {
     cudaFree(sc->n_e); cudaFree(sc->local); cudaFree(sc->kmax); cudaFree(sc->bprefix); cudaFree(sc->full);
     cudaFree(sc->work); cudaFree(sc->erecheck); cudaFree(sc->recheck); cudaFree(sc->counters); cudaFree(sc->status);
     cudaFree(sc->pairs); cudaFree(sc->pcfgs); cudaFree(sc->pskel); cudaFree(sc->pacc);
-    cudaFree(sc->perm); cudaFree(sc->bins);
+    cudaFree(sc->perm); cudaFree(sc->bins); cudaFree(sc->aux);
     for (int i = 0; i < 3; ++i) if (sc->ev[i]) cudaEventDestroy(sc->ev[i]);
     delete sc;
 }
@@ -330,6 +330,28 @@ int get_scratch(rpm_ctx *ctx, cudaStream_t st, int64_t need, Scratch **out) {
         s->ppair_cap = ppair;
     }
     *out = s;
+    return RPM_OK;
+}
+
+// The stream's planner working memory, at least `bytes`.  Growing it waits for
+// the stream (earlier calls may still read the old block); otherwise the
+// block is reused in stream order with no allocation on the call's path.
+int get_aux(rpm_ctx *ctx, cudaStream_t st, size_t bytes, void **out) {
+    Scratch *s = nullptr;
+    int rc = get_scratch(ctx, st, 0, &s);
+    if (rc) return rc;
+    if (s->aux_cap < bytes) {
+        if (s->aux) {
+            CK(cudaStreamSynchronize(st));
+            cudaFree(s->aux);
+            s->aux = nullptr;
+            s->aux_cap = 0;
+        }
+        const size_t cap = std::max<size_t>(bytes, (size_t)1 << 20);
+        if (cudaMalloc(&s->aux, cap) != cudaSuccess) return fail(RPM_ERR_NOMEM, "planner scratch allocation failed");
+        s->aux_cap = cap;
+    }
+    *out = s->aux;
     return RPM_OK;
 }
 
@@ -1304,23 +1326,25 @@ int reached_states_locked(rpm_ctx *ctx, int32_t scene_id, int32_t precision, con
     if (precision < RPM_PREC_FP64 || precision > RPM_PREC_FP32_REF) return fail(RPM_ERR_INVALID, "unknown precision %d", precision);
     SceneRec *s = find_scene(ctx, scene_id);
     const int L = ctx->robots[s->robot].desc.num_dofs;
-    // computeDistance of the current state with nearest points (stream-ordered
-    // scratch).  A short horizon's final computeDistance runs on the same
+    // computeDistance of the current state with nearest points (the stream's
+    // planner scratch).  A short horizon's final computeDistance runs on the same
     // CTA-per-state kernel (its points land in the scratch too), when they fit
     // in a few megabytes; otherwise it is an ordinary check.
     const size_t near_floats = (size_t)std::max(1, np.n) * 6 * L;
     const bool short_h = dist_dev && horizon_size > 0 && horizon_size <= 64 &&
                          (size_t)horizon_size * near_floats * 4 <= ((size_t)8 << 20);
     const size_t h_bytes = short_h ? (size_t)horizon_size * (8 + 4 * (size_t)L + 4 * near_floats) + 64 : 0;
-    const size_t bytes = 16 + 4 * (size_t)L + 4 * near_floats + 16 + h_bytes;
-    AsyncScratch scratch;
-    scratch.st = st;
-    CK(cudaMallocAsync(&scratch.p, bytes, st));
-    char *tmp = static_cast<char *>(scratch.p);
+    const size_t skel_off = (16 + 4 * (size_t)L + 4 * near_floats + 16 + h_bytes + 15) & ~(size_t)15;
+    const size_t bytes = skel_off + 4 * 3 * ((size_t)L + 1);
+    void *aux = nullptr;
+    rc = get_aux(ctx, st, bytes, &aux);
+    if (rc) return rc;
+    char *tmp = static_cast<char *>(aux);
     np.dist = reinterpret_cast<double *>(tmp);
     np.flag = reinterpret_cast<uint8_t *>(tmp + 8);
     np.profile = reinterpret_cast<float *>(tmp + 16);
     np.nearest = reinterpret_cast<float *>(tmp + 16 + 4 * (size_t)L);
+    np.skel_out = reinterpret_cast<float *>(tmp + skel_off);   // q_cur's float skeleton, for the spines
     CK(launch_distance_nearest(RPM_PREC_FP32_REF, np, st));
     SpineParams p;
     std::memset(&p, 0, sizeof p);
@@ -1337,6 +1361,7 @@ int reached_states_locked(rpm_ctx *ctx, int32_t scene_id, int32_t precision, con
     p.cur_dist = np.dist;
     p.cur_prof = np.profile;
     p.cur_near = np.nearest;
+    p.cur_skel = np.skel_out;
     p.n = np.n;
     p.maxd = np.nmf.maxd;
     p.L = L;
@@ -1346,6 +1371,7 @@ int reached_states_locked(rpm_ctx *ctx, int32_t scene_id, int32_t precision, con
         // FP32 + recheck forms, the reference's numerics for RPM_PREC_FP32_REF
         char *h = tmp + 16 + 4 * (size_t)L + 4 * near_floats + 16;
         NearParams hp = np;
+        hp.skel_out = nullptr;
         hp.q = q_reached_dev;
         hp.C = horizon_size;
         hp.dist = dist_dev;

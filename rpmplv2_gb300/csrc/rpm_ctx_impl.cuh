@@ -119,6 +119,10 @@ struct Scratch {
     int32_t *perm = nullptr;
     size_t perm_cap = 0;
     int32_t *bins = nullptr;   // [2][kConfigBins]: counts, then running offsets
+    // the planner calls' working memory (a DRGBT step's nearest points and
+    // distances), reused in stream order; grown only between calls
+    void *aux = nullptr;
+    size_t aux_cap = 0;
     // cached CUDA graphs of edge calls, keyed by their arguments
     struct Graph { std::vector<uint64_t> key; cudaGraphExec_t exec; };
     std::vector<Graph> graphs;

@@ -374,6 +374,55 @@ template <> struct SkelWalker<2> {
 };
 
 #ifdef __CUDACC__
+// ---------------------------------------------------------- warp sincos --
+// The sines and cosines of q[0..D-1] into sc (sin, cos per joint): the values
+// taylor_sincos computes, with one warp.  Lane j evaluates joint j's sine and
+// lane 16 + j its cosine.  The two polynomials run as one instruction stream:
+// the sine's starts one Horner step earlier from 0 (z * 0 + c0 is c0), and
+// the coefficients and the final factor are selected per lane.  The quadrant
+// swap then trades the two values across the half-warps.  Each value comes
+// from taylor_sincos's operations in their order.  On this part a warp's FP64
+// instruction occupies the FP64 pipe for its whole width, so the cost goes
+// with the number of instructions issued, not with the lanes that need them.
+// Every lane calls it; more than 16 joints take one lane per joint.
+__device__ __forceinline__ void warp_sincos(const float *q, int D, double *sc) {
+    const int lane = threadIdx.x & 31;
+    if (D > 16) {
+        if (lane < D) taylor_sincos((double)q[lane], &sc[2 * lane], &sc[2 * lane + 1]);
+        return;
+    }
+    const int j = lane & 15;
+    const bool is_sin = lane < 16;
+    const double x = j < D ? (double)q[j] : 0.0;
+    const double kTwoOverPi = 0x1.45f306dc9c883p-1;
+    const double kP1 = 0x1.921fb54400000p+0;
+    const double kP2 = 0x1.0b4611a600000p-34;
+    const double kP3 = 0x1.3198a2e037073p-69;
+    const double kd = rint(dmul(x, kTwoOverPi));
+    double r = dadd(x, -dmul(kd, kP1));
+    r = dadd(r, -dmul(kd, kP2));
+    r = dadd(r, -dmul(kd, kP3));
+    const double z = dmul(r, r);
+    const double rz = dmul(r, z);
+    double p = is_sin ? 0.0 : -0x1.6827863b97d97p-53;
+    p = dadd(is_sin ? 0x1.952c77030ad4ap-49 : 0x1.ae7f3e733b81fp-45, dmul(z, p));
+    p = dadd(is_sin ? -0x1.ae7f3e733b81fp-41 : -0x1.93974a8c07c9dp-37, dmul(z, p));
+    p = dadd(is_sin ? 0x1.6124613a86d09p-33 : 0x1.1eed8eff8d898p-29, dmul(z, p));
+    p = dadd(is_sin ? -0x1.ae64567f544e4p-26 : -0x1.27e4fb7789f5cp-22, dmul(z, p));
+    p = dadd(is_sin ? 0x1.71de3a556c734p-19 : 0x1.a01a01a01a01ap-16, dmul(z, p));
+    p = dadd(is_sin ? -0x1.a01a01a01a01ap-13 : -0x1.6c16c16c16c17p-10, dmul(z, p));
+    p = dadd(is_sin ? 0x1.1111111111111p-7 : 0x1.5555555555555p-5, dmul(z, p));
+    p = dadd(is_sin ? -0x1.5555555555555p-3 : -0x1.0000000000000p-1, dmul(z, p));
+    // sine: r + (r z) ps; cosine: 1 + z pc
+    const double v = dadd(is_sin ? r : 1.0, dmul(is_sin ? rz : z, p));
+    const double o = __shfl_xor_sync(0xffffffffu, v, 16);   // the other value of the same joint
+    const int qd = (int)((long long)kd & 3);
+    // quadrant 0..3: sin = s, c, -s, -c and cos = c, -s, -c, s
+    const double base = (qd & 1) ? o : v;
+    const bool neg = is_sin ? (qd & 2) != 0 : (qd == 1 || qd == 2);
+    if (j < D) sc[2 * j + (is_sin ? 0 : 1)] = neg ? -base : base;
+}
+
 // ------------------------------------------------ warp forward kinematics --
 // The FP64 chain of SkelWalker<MODE> (MODE 0: FP64 points; MODE 1: the
 // reference's float skeleton) run by a whole warp: lane e < 9 holds R[e]
@@ -382,7 +431,7 @@ template <> struct SkelWalker<2> {
 // so the points are the same bits; the serial chain per joint is a few
 // shuffles and three products instead of about eighty FP64 operations.
 // Every lane of the warp calls it; sc holds the joints' sines and cosines
-// (taylor_sincos, computed ahead); lanes 9-11 write the D + 1 points to out.
+// (taylor_sincos or warp_sincos, computed ahead); lanes 9-11 write the D + 1 points to out.
 template <int MODE, typename TO>
 __device__ void skel_coop(const DevRobot &rb, const double *sc, TO *out) {
     const unsigned full = 0xffffffffu;
@@ -395,22 +444,27 @@ __device__ void skel_coop(const DevRobot &rb, const double *sc, TO *out) {
     auto emit = [&](int kp, double x) {
         if (is_p) out[3 * kp + row] = (TO)x;
     };
+    // One joint with no divergent FP64 code: every lane issues the same nine
+    // FP64 instructions and keeps its own result by a select.  The p lanes
+    // take p + R o_k (r0 o0 + r1 o1, + r2 o2, + p); the R lanes R M_k (the
+    // same products and sums without the last; skipped for an identity M_k).
     auto step = [&](int k) {
         const double r0 = rowval(0), r1 = rowval(1), r2 = rowval(2);
-        if (is_p) {
-            const double *o = rb.oxyz[k];
-            v = dadd(dadd(dadd(dmul(r0, o[0]), dmul(r1, o[1])), dmul(r2, o[2])), v);
-        } else if (is_r && !((rb.rot_identity_mask >> k) & 1)) {
-            const double *M = rb.orot[k];
-            v = dadd(dadd(dmul(r0, M[col]), dmul(r1, M[3 + col])), dmul(r2, M[6 + col]));
-        }
-        // columns (IA, IB) <- (a c + b s, b c - a s), as rot_cols_d
+        const double *X = is_p ? rb.oxyz[k] : rb.orot[k] + col;
+        const int sx = is_p ? 1 : 3;
+        const double t = dadd(dadd(dmul(r0, X[0]), dmul(r1, X[sx])), dmul(r2, X[2 * sx]));
+        const double tp = dadd(t, v);
+        const bool rot = is_r && !((rb.rot_identity_mask >> k) & 1);
+        v = is_p ? tp : (rot ? t : v);
+        // columns (IA, IB) <- (a c + b s, b c - a s), as rot_cols_d; x (-s)
+        // is -(x s) exactly
         const int ax = rb.axis[k];
         const int ia = ax == 0 ? 1 : (ax == 1 ? 2 : 0), ib = ax == 0 ? 2 : (ax == 1 ? 0 : 1);
         const double sn = sc[2 * k], cs = sc[2 * k + 1];
         const double x = __shfl_sync(full, v, is_r ? 3 * row + (col == ia ? ib : ia) : lane);
-        if (is_r && col == ia) v = dadd(dmul(v, cs), dmul(x, sn));
-        else if (is_r && col == ib) v = dadd(dmul(v, cs), -dmul(x, sn));
+        const bool a = is_r && col == ia, b = is_r && col == ib;
+        const double w = dadd(dmul(v, cs), dmul(x, b ? -sn : sn));
+        v = (a || b) ? w : v;
     };
     const int D = rb.D;
     if (rb.kind != RPM_ROBOT_XARM6) {

@@ -157,11 +157,12 @@ __device__ __forceinline__ bool decode_pair(const PairSink &ps, uint32_t k, uint
 }
 
 // FP64 skeleton with the whole warp: the joints' sines and cosines in
-// parallel (the same taylor_sincos values), then the serial chain in lane 0.
+// parallel (warp_sincos: the taylor_sincos values), then the chain spread
+// over the warp (skel_coop).
 __device__ __forceinline__ void pair_skel_warp(const DevRobot &rb, const float *q, double *out, PairAcc &a,
                                                double *sc) {
     const int lane = threadIdx.x & 31;
-    if (lane < rb.D) taylor_sincos((double)q[lane], &sc[2 * lane], &sc[2 * lane + 1]);
+    warp_sincos(q, rb.D, sc);
     a.lkey[lane] = 0x7fffffff;
     a.hkey[lane] = ~0ull;
     if (lane == 0) {
@@ -714,7 +715,7 @@ __global__ void __launch_bounds__(kNearCtaThreads) k_distance_nearest_cta(const 
     if (MODE == 0) { nm.eq = (T)P.nmd.eq; nm.maxd = (T)P.nmd.maxd; }
     else { nm.eq = (T)P.nmf.eq; nm.maxd = (T)P.nmf.maxd; }
     if (threadIdx.x < 32) {   // joint sines in parallel, then the chain spread over the warp (the same bits)
-        if ((int)threadIdx.x < D) taylor_sincos((double)q[threadIdx.x], &sc[2 * threadIdx.x], &sc[2 * threadIdx.x + 1]);
+        warp_sincos(q, D, sc);
         __syncwarp();
         skel_coop<MODE, T>(rb, sc, skel);
     }
@@ -723,6 +724,10 @@ __global__ void __launch_bounds__(kNearCtaThreads) k_distance_nearest_cta(const 
         hj[i] = 0x7fffffff;
     }
     __syncthreads();
+    if constexpr (MODE == 1) {
+        if (P.skel_out)
+            for (int k = threadIdx.x; k < 3 * (D + 1); k += blockDim.x) P.skel_out[c * 3 * (D + 1) + k] = skel[k];
+    }
     const float *ground = P.obs_f + (size_t)kRowGround * P.n_pad;
     float *near = P.nearest + (size_t)c * P.n * 6 * L;
     const int npairs = L * P.n;
@@ -910,9 +915,9 @@ __global__ void __launch_bounds__(kThreads) k_extend_spines(const __grid_constan
 // (unchanged when zero) and the point O, with skip = 1 where |O| is
 // MAX_DISTANCE (a pair the reference passes over).  They do not change over
 // the horizon, so a CTA computes them once (the same operations as per use).
-struct Plane {
+struct __align__(16) Plane {   // 32 bytes: two 16-byte shared-memory loads
     float u[3], O[3];
-    int skip;
+    int skip, pad;
 };
 
 __device__ __forceinline__ Plane make_plane(const SpineParams &P, int L, int i, int j) {
@@ -924,6 +929,7 @@ __device__ __forceinline__ Plane make_plane(const SpineParams &P, int L, int i, 
         pl.O[k] = P.cur_near[((size_t)j * 6 + 3 + k) * L + i];
     }
     pl.skip = sqrtf(dot3f(pl.O, pl.O)) == P.maxd;
+    pl.pad = 0;
     pl.u[0] = R[0] - pl.O[0]; pl.u[1] = R[1] - pl.O[1]; pl.u[2] = R[2] - pl.O[2];
     const float z = dot3f(pl.u, pl.u);
     if (z > 0.f) {
@@ -959,34 +965,46 @@ __global__ void __launch_bounds__(kThreads) k_reached_states(const __grid_consta
         if (lane < L) w.pn[lane] = P.cur_prof[lane];
         float dn = d_cur;
         status = kStNone;
-        skel_ref_shared(rb, w.qn, w.skn, w.sc);
+        if (P.cur_skel) {   // the skeleton of q_cur from the nearest-point kernel (the same bits)
+            for (int k = lane; k < 3 * (D + 1); k += 32) w.skn[k] = P.cur_skel[k];
+            __syncwarp();
+        } else {
+            skel_ref_shared(rb, w.qn, w.skn, w.sc);
+        }
         for (int layer = 0; layer < P.num_layers; ++layer) {
             status = extend_spine_warp(rb, w, dn, P.num_iter, P.expanded != 0);
             if (lane < D) w.qn[lane] = w.qs[lane];
             for (int k = lane; k < 3 * (D + 1); k += 32) w.skn[k] = w.sk[k];
             __syncwarp();
-            float d_c = P.maxd;
-            bool negative = false;
-            for (int i = 0; i < L && !negative; ++i) {
+            // all links at once: G lanes per link (a power of two, G L <= 32),
+            // each over a strided share of the obstacles.  Every value is the
+            // reference's; min is exact and free of order here (no NaN, no
+            // -0), and "any negative" is what its early return amounts to (on
+            // a negative value neither the minima nor the profile are used)
+            int G = 32;
+            while (G * L > 32) G >>= 1;
+            const int i = lane / G, sub = lane & (G - 1);
+            float lmin = P.maxd;
+            bool neg = false;
+            if (i < L) {
                 const float *S0 = w.sk + 3 * i, *S1 = S0 + 3;
-                float lmin = P.maxd;
-                bool neg = false;
-                for (int j = lane; j < P.n; j += 32) {
+                const float ri = rb.radius_f[i];
+                for (int j = sub; j < P.n; j += G) {
                     const Plane pl = planes ? planes[i * P.n + j] : make_plane(P, L, i, j);
                     if (pl.skip) continue;
                     const float *O = pl.O, *u = pl.u;
                     float a[3] = {S0[0] - O[0], S0[1] - O[1], S0[2] - O[2]};
                     float b[3] = {S1[0] - O[0], S1[1] - O[1], S1[2] - O[2]};
-                    const float d = min_std(dot3f(a, u), dot3f(b, u)) - rb.radius_f[i];
+                    const float d = min_std(dot3f(a, u), dot3f(b, u)) - ri;
                     if (d < 0.f) neg = true;
                     lmin = min_std(lmin, d);
                 }
-                negative = __any_sync(full, neg);
-#pragma unroll
-                for (int off = 16; off > 0; off >>= 1) lmin = min_std(lmin, __shfl_xor_sync(full, lmin, off));
-                if (lane == 0) w.p[i] = lmin;
-                d_c = min_std(d_c, lmin);
             }
+            const bool negative = __any_sync(full, neg);
+            for (int off = G >> 1; off > 0; off >>= 1) lmin = min_std(lmin, __shfl_xor_sync(full, lmin, off));
+            if (i < L && sub == 0) w.p[i] = lmin;
+            float d_c = lmin;   // the links' minimum (lanes past the links hold maxd)
+            for (int off = 16; off >= G; off >>= 1) d_c = min_std(d_c, __shfl_xor_sync(full, d_c, off));
             __syncwarp();
             float d;
             if (!negative) {

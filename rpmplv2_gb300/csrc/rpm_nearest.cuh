@@ -228,6 +228,7 @@ struct NearParams {
     uint8_t *flag;           // [C] nearest points valid / underestimation complete
     double *margin_valid;    // [C] decision margins (rpm_decision_margins)
     double *margin_dist;     // [C]
+    float *skel_out;         // [C][3 (D + 1)] the reference's float skeleton (one CTA per state), nullable
 };
 
 cudaError_t launch_distance_nearest(int mode, const NearParams &p, cudaStream_t st);

@@ -37,6 +37,7 @@ struct SpineParams {
     const double *cur_dist;  // [1]
     const float *cur_prof;   // [L]
     const float *cur_near;   // [n][6][L]
+    const float *cur_skel;   // [3 (D + 1)] its float skeleton, when the nearest-point kernel wrote it (nullable)
     int32_t n;
     float maxd;              // MAX_DISTANCE
     int32_t L;               // reached states: links (sizes the plane table below)
@@ -66,14 +67,13 @@ __device__ __forceinline__ void skel_ref(const DevRobot &rb, const float *q, flo
     for (int k = 0; k <= rb.D; ++k) sw.point(rb, q, k, sk + 3 * k);
 }
 
-// The same skeleton with the whole warp (every lane passes the same q): lane
-// k computes joint k's sine and cosine -- the values the chain would compute
-// itself -- and every lane then runs the chain.  sc: 2 * kMaxDof doubles of
-// the warp's shared memory.
+// The same skeleton with the whole warp (every lane passes the same q): the
+// warp computes the joints' sines and cosines (warp_sincos: the values the
+// chain would compute itself) and every lane then runs the chain.  sc:
+// 2 * kMaxDof doubles of the warp's shared memory.
 __device__ __forceinline__ void skel_ref_warp(const DevRobot &rb, const float *q, float *sk, double *sc) {
-    const int lane = threadIdx.x & 31;
     __syncwarp();
-    if (lane < rb.D) taylor_sincos((double)q[lane], &sc[2 * lane], &sc[2 * lane + 1]);
+    warp_sincos(q, rb.D, sc);
     __syncwarp();
     SkelWalker<1> sw;
     sw.begin();
@@ -114,6 +114,53 @@ static __device__ void enclosing_row(const DevRobot &rb, const float *sk, int i,
         const float *pj = sk + 3 * j;
         const float v = (i == 0 && spatial) ? sqrtf(pj[0] * pj[0] + pj[1] * pj[1]) : col_dist(pj, sk + 3 * i);
         row[j] = max_std(row[j - 1], v + rb.radius_f[j - 1]);
+    }
+}
+
+// The term enclosing_row adds at column j of row i (0 where it adds none).
+static __device__ __forceinline__ float enclosing_term(const DevRobot &rb, const float *sk, int i, int j) {
+    const int D = rb.D;
+    if (j <= i) return 0.f;
+    const float *pj = sk + 3 * j;
+    if (rb.kind == RPM_ROBOT_XARM6) {
+        if (i >= D - 1) return 0.f;
+        const float rn = j - 1 < D - 1 ? max_std(rb.radius_f[j - 1], rb.radius_f[j]) : rb.radius_f[D - 1];
+        if (i == 0) return j >= 2 ? sqrtf(pj[0] * pj[0] + pj[1] * pj[1]) + rn : 0.f;
+        if (i == 3) {
+            if (j < 5) return 0.f;
+            const float *p3 = sk + 9, *p4 = sk + 12;
+            float AB[3], v[3], proj[3], w[3];
+#pragma unroll
+            for (int k = 0; k < 3; ++k) { AB[k] = p4[k] - p3[k]; v[k] = pj[k] - p3[k]; }
+            const float t = dot3f(v, AB) / dot3f(AB, AB);
+#pragma unroll
+            for (int k = 0; k < 3; ++k) { proj[k] = p3[k] + t * AB[k]; w[k] = pj[k] - proj[k]; }
+            return sqrtf(dot3f(w, w)) + rn;
+        }
+        return col_dist(pj, sk + 3 * i) + rn;
+    }
+    const bool spatial = rb.kind == RPM_ROBOT_SPATIAL;
+    const float v = (i == 0 && spatial) ? sqrtf(pj[0] * pj[0] + pj[1] * pj[1]) : col_dist(pj, sk + 3 * i);
+    return v + rb.radius_f[j - 1];
+}
+
+// enclosing_row of every joint with the whole warp: each (i, j) term on a
+// lane of its own, then each row's running maximum by lane i.  The terms are
+// non-negative and max is exact, so the rows are enclosing_row's, bit for bit.
+static __device__ void enclosing_rows_warp(const DevRobot &rb, const float *sk, float (*rows)[kMaxDof + 1]) {
+    const int lane = threadIdx.x & 31;
+    const int D = rb.D, W = D + 1;
+    for (int e = lane; e < D * W; e += 32) {
+        const int i = e / W, j = e - i * W;
+        rows[i][j] = enclosing_term(rb, sk, i, j);
+    }
+    __syncwarp();
+    if (lane < D) {
+        float r = 0.f;
+        for (int j = 0; j <= D; ++j) {
+            r = max_std(r, rows[lane][j]);
+            rows[lane][j] = r;
+        }
     }
 }
 
@@ -195,9 +242,8 @@ struct SpineWarp {
 // The reference's float skeleton of q (shared memory) into sk (shared
 // memory): joint sines in parallel, then the chain spread over the warp.
 __device__ __forceinline__ void skel_ref_shared(const DevRobot &rb, const float *q, float *sk, double *sc) {
-    const int lane = threadIdx.x & 31;
     __syncwarp();
-    if (lane < rb.D) taylor_sincos((double)q[lane], &sc[2 * lane], &sc[2 * lane + 1]);
+    warp_sincos(q, rb.D, sc);
     __syncwarp();
     skel_coop<1, float>(rb, sc, sk);
     __syncwarp();
@@ -222,10 +268,8 @@ static __device__ int extend_spine_warp(const DevRobot &rb, SpineWarp &w, float 
     int counter = 0;
     __syncwarp();
     for (;;) {
-        if (lane < D) {
-            w.dq[lane] = fabsf(w.qe[lane] - w.qt[lane]);
-            enclosing_row(rb, w.skt, lane, w.rows[lane]);
-        }
+        if (lane < D) w.dq[lane] = fabsf(w.qe[lane] - w.qt[lane]);
+        enclosing_rows_warp(rb, w.skt, w.rows);
         __syncwarp();
         if (lane <= D) {
             float c = 0.f;
@@ -234,15 +278,28 @@ static __device__ int extend_spine_warp(const DevRobot &rb, SpineWarp &w, float 
         }
         __syncwarp();
         float step = 0.f;
-        if (lane == 0) {
-            if (expanded) {
-                step = INFINITY;
-                for (int i = 0; i < D; ++i) step = min_std(step, (w.pn[i] - w.rho_prof[i]) / w.col[i + 1]);
-            } else {
-                step = (d - rho) / w.col[D];
+        if (expanded) {
+            // the min over the joints of (p_i - rho_i) / col_{i+1}, a quotient
+            // per lane: the serial min keeps the first of equal values and
+            // passes over NaN, so the tree takes the lower joint on a tie and
+            // NaN as +inf
+            float x = INFINITY;
+            if (lane < D) {
+                x = (w.pn[lane] - w.rho_prof[lane]) / w.col[lane + 1];
+                if (x != x) x = INFINITY;
             }
+            int at = lane;
+#pragma unroll
+            for (int off = 16; off > 0; off >>= 1) {
+                const float y = __shfl_xor_sync(0xffffffffu, x, off);
+                const int ay = __shfl_xor_sync(0xffffffffu, at, off);
+                if (y < x || (y == x && ay < at)) { x = y; at = ay; }
+            }
+            step = x;
+        } else {
+            if (lane == 0) step = (d - rho) / w.col[D];
+            step = __shfl_sync(0xffffffffu, step, 0);
         }
-        step = __shfl_sync(0xffffffffu, step, 0);
         const bool reached = step > 1.f;
         if (lane < D) w.qs[lane] = reached ? w.qe[lane] : w.qt[lane] + step * (w.qe[lane] - w.qt[lane]);
         skel_ref_shared(rb, w.qs, w.sk, w.sc);

@@ -65,18 +65,21 @@ def test_reached_states(engine, name, n):
     H = 200
     hz = scenes.uniform_configs(rng, H, D)
     sid = engine.create_scene(engine.upload_robot(rb), scene)
-    for prec, oprec in (("fp32_ref", "ref32"), ("fp64", "ref64")):
-        qr = torch.zeros((H, D), dtype=torch.float32, device="cuda")
-        st = torch.zeros(H, dtype=torch.int32, device="cuda")
-        dist = torch.zeros(H, dtype=torch.float64, device="cuda")
-        engine.reached_states(sid, _t(q_cur), _t(hz), qr, st, dist, precision=prec, num_layers=5, num_iter=1,
-                              expanded=True, d_crit=0.05)
-        engine.sync()
-        rq, rs = O.reached_states(rb, scene, q_cur, hz, num_layers=5, num_iter=1, expanded=True, d_crit=0.05)
-        assert np.array_equal(st.cpu().numpy(), rs)
-        assert np.array_equal(qr.cpu().numpy().view(np.uint32), rq.view(np.uint32))
-        _, rd, _ = O.check_configs(rb, scene, rq, prec=oprec, want=("dist",))
-        assert np.array_equal(dist.cpu().numpy().view(np.uint64), rd.view(np.uint64))
+    rq, rs = O.reached_states(rb, scene, q_cur, hz, num_layers=5, num_iter=1, expanded=True, d_crit=0.05)
+    # a long horizon (final distances by the batch check) and a short one (by
+    # the one-CTA-per-state nearest-point kernel)
+    for h in (H, 10):
+        for prec, oprec in (("fp32_ref", "ref32"), ("fp64", "ref64")):
+            qr = torch.zeros((h, D), dtype=torch.float32, device="cuda")
+            st = torch.zeros(h, dtype=torch.int32, device="cuda")
+            dist = torch.zeros(h, dtype=torch.float64, device="cuda")
+            engine.reached_states(sid, _t(q_cur), _t(hz[:h]), qr, st, dist, precision=prec, num_layers=5,
+                                  num_iter=1, expanded=True, d_crit=0.05)
+            engine.sync()
+            assert np.array_equal(st.cpu().numpy(), rs[:h])
+            assert np.array_equal(qr.cpu().numpy().view(np.uint32), rq[:h].view(np.uint32))
+            _, rd, _ = O.check_configs(rb, scene, rq[:h], prec=oprec, want=("dist",))
+            assert np.array_equal(dist.cpu().numpy().view(np.uint64), rd.view(np.uint64))
     # a current state in collision: every horizon state is Trapped at q_current
     if n:
         v, _, _ = O.check_configs(rb, scene, qs, prec="ref32", want=("valid",))
