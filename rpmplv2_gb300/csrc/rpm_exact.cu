@@ -174,29 +174,25 @@ __device__ __forceinline__ void pair_skel_warp(const DevRobot &rb, const float *
     __syncwarp();
 }
 
-// Work item of this warp when there are at most as many items as warps:
-// consecutive items go to different CTAs, so they run on different SMs
-// (each FP64 warp instruction costs an SM the same time however few lanes
-// are active).  -1: this warp has none.
-__device__ __forceinline__ int64_t spread_item(uint32_t n) {
-    const uint32_t wpb = blockDim.x / 32;
-    const uint32_t w = (threadIdx.x / 32) * gridDim.x + blockIdx.x;
-    return w < n && n <= gridDim.x * wpb ? (int64_t)w : -1;
-}
+// Records up to this many times the warps are skeletonised a warp each, in
+// rounds, consecutive records on different CTAs so that they run on different
+// SMs (a warp's FP64 chain is latency-bound); beyond, one thread each.
+constexpr uint32_t kSkelWarpRounds = 2;
 
 // 1. FP64 skeleton of each recorded configuration.
 __global__ void k_pair_skel(const __grid_constant__ KParams P) {
     __shared__ double sc[kThreads / 32][2 * kMaxDof];
     const uint32_t n = min(*P.ps.cfg_count, P.ps.cfg_cap);
-    if (n <= gridDim.x * (blockDim.x / 32)) {   // few records: a warp each
-        const int64_t k = spread_item(n);
-        if (k < 0) return;
-        const PairCfg c = P.ps.cfgs[k];
-        if (c.status != kPairs) return;
-        const Seg &sg = P.segs[c.seg];
-        const DevRobot &rb = *sg.robot;
-        pair_skel_warp(rb, sg.q + c.config * rb.D, P.ps.skel + (size_t)k * (kMaxDof + 1) * 3, P.ps.acc[k],
-                       sc[threadIdx.x / 32]);
+    const uint32_t warps = gridDim.x * (blockDim.x / 32);
+    if (n <= kSkelWarpRounds * warps) {   // a warp each, consecutive records on different SMs
+        for (uint32_t k = (threadIdx.x / 32) * gridDim.x + blockIdx.x; k < n; k += warps) {
+            const PairCfg c = P.ps.cfgs[k];
+            if (c.status != kPairs) continue;
+            const Seg &sg = P.segs[c.seg];
+            const DevRobot &rb = *sg.robot;
+            pair_skel_warp(rb, sg.q + c.config * rb.D, P.ps.skel + (size_t)k * (kMaxDof + 1) * 3, P.ps.acc[k],
+                           sc[threadIdx.x / 32]);
+        }
         return;
     }
     for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
@@ -208,25 +204,34 @@ __global__ void k_pair_skel(const __grid_constant__ KParams P) {
     }
 }
 
-// 2. One thread per listed pair: the reference's FP64 tree on the FP64
-// skeleton (pairs of configurations that ended settled, or that were routed
-// to the whole-configuration recheck, belong to records not completed with
-// kPairs and are skipped).
+// Listed pair k of run r: each warp takes runs of `per` consecutive pairs,
+// one per lane, the runs dealt to the warps so that consecutive runs land on
+// different CTAs.  `per` is the fewest pairs per warp that covers the list
+// (at most 32), so every SM gets work and a warp diverges over a few pairs
+// only: each divergent path of an FP64 tree issues its own FP64
+// instructions, and a lone warp's FP64 chain is latency-bound.
+struct PairRuns {
+    uint32_t per, lane, first, stride;
+    __device__ PairRuns(uint32_t n) {
+        const uint32_t warps = gridDim.x * (blockDim.x / 32);
+        per = min(32u, max(1u, (n + warps - 1) / warps));
+        lane = threadIdx.x & 31;
+        first = ((threadIdx.x / 32) * gridDim.x + blockIdx.x) * per + lane;
+        stride = warps * per;
+    }
+    __device__ bool active() const { return lane < per; }
+};
+
+// 2. The reference's FP64 tree for each listed pair on the FP64 skeleton
+// (pairs of configurations that ended settled, or that were routed to the
+// whole-configuration recheck, belong to records not completed with kPairs
+// and are skipped).
 __global__ void k_pair_eval(const __grid_constant__ KParams P) {
     const uint32_t n = min(*P.ps.pair_count, P.ps.pair_cap);
     const uint32_t ncfg = min(*P.ps.cfg_count, P.ps.cfg_cap);
-    if (n <= gridDim.x * (blockDim.x / 32)) {   // few pairs: a warp each (lane 0), spread over the SMs
-        const int64_t k = spread_item(n);
-        if (k < 0 || (threadIdx.x & 31) != 0) return;
-        uint32_t slot;
-        int link, j, kind;
-        if (!decode_pair(P.ps, (uint32_t)k, ncfg, slot, link, j, kind)) return;
-        const Seg &sg = P.segs[P.ps.cfgs[slot].seg];
-        ObsView<double> ob{sg.obs_d, sg.obs_f + (size_t)kRowGround * sg.n_pad, sg.n, sg.n_pad};
-        pair_eval_one(*sg.robot, ob, P.nmd, P.ps.skel + (size_t)slot * (kMaxDof + 1) * 3, link, j, kind, P.ps.acc[slot]);
-        return;
-    }
-    for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+    const PairRuns run(n);
+    if (!run.active()) return;
+    for (uint32_t k = run.first; k < n; k += run.stride) {
         uint32_t slot;
         int link, j, kind;
         if (!decode_pair(P.ps, k, ncfg, slot, link, j, kind)) continue;
@@ -242,19 +247,22 @@ __global__ void k_edge_pair_skel(const __grid_constant__ EdgeParams P) {
     __shared__ double sc[kThreads / 32][2 * kMaxDof];
     __shared__ float qs[kThreads / 32][kMaxDof];
     const uint32_t n = min(*P.ps.cfg_count, P.ps.cfg_cap);
-    if (n <= gridDim.x * (blockDim.x / 32)) {   // few records: a warp each
-        const int64_t k = spread_item(n);
-        if (k < 0) return;
-        const PairCfg c = P.ps.cfgs[k];
-        if (c.status != kPairs) return;
-        const int s = edge_seg(P, c.config);
+    const uint32_t warps = gridDim.x * (blockDim.x / 32);
+    if (n <= kSkelWarpRounds * warps) {   // a warp each, consecutive records on different SMs
         const int w = threadIdx.x / 32;
-        if ((threadIdx.x & 31) == 0) {
-            const EdgeGeom gm = edge_geom(P, s, c.config);
-            edge_config(gm.a, gm.b, gm.D, gm.n, c.seg, gm.dist, qs[w]);
+        for (uint32_t k = (threadIdx.x / 32) * gridDim.x + blockIdx.x; k < n; k += warps) {
+            const PairCfg c = P.ps.cfgs[k];
+            if (c.status != kPairs) continue;
+            const int s = edge_seg(P, c.config);
+            __syncwarp();
+            if ((threadIdx.x & 31) == 0) {
+                const EdgeGeom gm = edge_geom(P, s, c.config);
+                edge_config(gm.a, gm.b, gm.D, gm.n, c.seg, gm.dist, qs[w]);
+            }
+            __syncwarp();
+            pair_skel_warp(*P.segs[s].seg.robot, qs[w], P.ps.skel + (size_t)k * (kMaxDof + 1) * 3, P.ps.acc[k],
+                           sc[w]);
         }
-        __syncwarp();
-        pair_skel_warp(*P.segs[s].seg.robot, qs[w], P.ps.skel + (size_t)k * (kMaxDof + 1) * 3, P.ps.acc[k], sc[w]);
         return;
     }
     for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
@@ -271,18 +279,9 @@ __global__ void k_edge_pair_skel(const __grid_constant__ EdgeParams P) {
 __global__ void k_edge_pair_eval(const __grid_constant__ EdgeParams P) {
     const uint32_t n = min(*P.ps.pair_count, P.ps.pair_cap);
     const uint32_t ncfg = min(*P.ps.cfg_count, P.ps.cfg_cap);
-    if (n <= gridDim.x * (blockDim.x / 32)) {   // few pairs: a warp each (lane 0), spread over the SMs
-        const int64_t k = spread_item(n);
-        if (k < 0 || (threadIdx.x & 31) != 0) return;
-        uint32_t slot;
-        int link, j, kind;
-        if (!decode_pair(P.ps, (uint32_t)k, ncfg, slot, link, j, kind)) return;
-        const Seg &sg = P.segs[edge_seg(P, P.ps.cfgs[slot].config)].seg;
-        pair_eval_one(*sg.robot, global_obs<double>(sg), P.nmd, P.ps.skel + (size_t)slot * (kMaxDof + 1) * 3, link, j,
-                      kind, P.ps.acc[slot]);
-        return;
-    }
-    for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+    const PairRuns run(n);
+    if (!run.active()) return;
+    for (uint32_t k = run.first; k < n; k += run.stride) {
         uint32_t slot;
         int link, j, kind;
         if (!decode_pair(P.ps, k, ncfg, slot, link, j, kind)) continue;
@@ -560,7 +559,7 @@ cudaError_t launch_edges_wide(int mode, const EdgeParams &p, int grid, size_t sm
 
 cudaError_t launch_edge_recheck_final(const EdgeParams &p, int grid, bool pairs, cudaStream_t st) {
     if (pairs) {
-        k_edge_pair_skel<<<grid, kThreads, 0, st>>>(p);
+        k_edge_pair_skel<<<grid * 4, kThreads, 0, st>>>(p);
         k_edge_pair_eval<<<grid * 2, kThreads, 0, st>>>(p);
         k_edge_pair_fold<<<grid, kThreads, 0, st>>>(p);
     }
@@ -852,7 +851,7 @@ cudaError_t launch_distance_underest(int mode, const NearParams &p, cudaStream_t
 }
 
 cudaError_t launch_pair_recheck(const KParams &p, int grid, cudaStream_t st) {
-    k_pair_skel<<<grid, kThreads, 0, st>>>(p);
+    k_pair_skel<<<grid * 4, kThreads, 0, st>>>(p);
     k_pair_eval<<<grid * 2, kThreads, 0, st>>>(p);
     k_pair_fold<<<grid, kThreads, 0, st>>>(p);
     return cudaGetLastError();
