@@ -608,7 +608,9 @@ def run_ours(args, ws, rank, local):
                  "speedup_fp32_recheck_over_fp64": value / ws / fp64_value, "isvalid_flips": flips,
                  "max_distance_diff_m": max_derr},
         "recheck": {"configs_per_step": int(statistics.median(rechecked)),
-                    "fraction": statistics.median(rechecked) / C, "kernel_ms": statistics.median(re_ms)},
+                    "fraction": statistics.median(rechecked) / C, "kernel_ms": statistics.median(re_ms),
+                    "note": "FP64 rechecks of a step, once per output pass (isValid, distance) that needed one; "
+                            "kernel_ms: the recheck round after the last main launch"},
         "clocks": clocks,
         "e2e": {"value": C * args.steps / e2e_s, "unit": "configs/s", "h2d_bytes_per_step": C * D * 4,
                 "d2h_bytes_per_step": C * (1 + 8), "call": "rpm_check_configs_host", "matches_device_run": e2e_ok,

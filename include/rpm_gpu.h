@@ -99,7 +99,8 @@ typedef struct rpm_ctx rpm_ctx;
 /* Statistics of the last check issued on a context (read after a sync). */
 typedef struct rpm_check_stats {
     int64_t configs;           /* configurations (or edge checks) in the call */
-    int64_t rechecked;         /* configurations recomputed in FP64 by the recheck pass */
+    int64_t rechecked;         /* FP64 rechecks of the call: configurations recomputed whole or through their
+                                  listed pairs, once per output pass (isValid, distance) that needed one */
     int64_t overflow;          /* recheck entries that did not fit the recheck list (must be 0) */
     int32_t device_status;     /* 0, or an RPM_ERR_* recorded by a kernel */
     int32_t pad;

@@ -316,7 +316,7 @@ int get_scratch(rpm_ctx *ctx, cudaStream_t st, int64_t need, Scratch **out) {
         // 16 listed pairs per record; what does not fit is rechecked whole
         const size_t pcfg = std::min<size_t>(cap, std::max<size_t>(4096, std::min<size_t>(cap / 8, 1u << 16)));
         const size_t ppair = 16 * pcfg;
-        if (cudaMalloc(&s->recheck, cap * sizeof(uint64_t)) != cudaSuccess ||
+        if (cudaMalloc(&s->recheck, 2 * cap * sizeof(uint64_t)) != cudaSuccess ||   // two launches per configuration
             cudaMalloc(&s->pairs, ppair * sizeof(uint64_t)) != cudaSuccess ||
             cudaMalloc(&s->pcfgs, pcfg * sizeof(PairCfg)) != cudaSuccess ||
             cudaMalloc(&s->pskel, pcfg * (kMaxDof + 1) * 3 * sizeof(double)) != cudaSuccess ||
@@ -543,6 +543,27 @@ int enqueue_segments(rpm_ctx *ctx, int prec, const std::vector<SegReq> &reqs_in,
     }
     const size_t tsz = prec == RPM_PREC_FP64 ? sizeof(double) : sizeof(float);
     std::vector<SceneBuf *> used;
+    // FP32 + recheck: the FP64 recheck of a group of launches (as many as fit
+    // kMaxSegs segments together) runs once, after the group's last launch.
+    // Their records carry the segment's index in the group (PairSink::seg_base),
+    // so the isValid and distance launches of a request share one round of the
+    // latency-bound recheck instead of two.  Each configuration is listed once
+    // per launch it is in: the whole-configuration list holds twice the
+    // configurations (get_scratch).
+    const bool recheck = prec == RPM_PREC_FP32_RECHECK;
+    KParams group, last_p;
+    int32_t group_segs = 0;
+    auto flush_group = [&]() -> int {
+        if (group_segs == 0) return RPM_OK;
+        KParams rp = last_p;
+        std::memcpy(rp.segs, group.segs, sizeof(Seg) * (size_t)group_segs);
+        rp.nseg = group_segs;
+        rp.ps.seg_base = 0;
+        group_segs = 0;
+        CK(launch_pair_recheck(rp, ctx->num_sms * 2, st));
+        CK(launch_recheck(rp, ctx->num_sms * 4, st));
+        return RPM_OK;
+    };
     for (size_t ci = 0; ci < chunks.size(); ++ci) {
         const bool wide = chunks[ci].first;
         const std::vector<const SegReq *> &segs = chunks[ci].second;
@@ -622,15 +643,27 @@ int enqueue_segments(rpm_ctx *ctx, int prec, const std::vector<SegReq> &reqs_in,
         p.ps.cfg_count = sc->counters + 2;
         p.ps.skel = sc->pskel;
         p.ps.acc = sc->pacc;
-        if (ci > 0) CK(cudaMemsetAsync(sc->counters, 0, 4 * sizeof(uint32_t), st));   // the recheck lists are per launch
+        if (recheck) {
+            if (group_segs + p.nseg > kMaxSegs) {   // the group is full: its recheck, then fresh lists
+                rc = flush_group();
+                if (rc) return rc;
+                CK(cudaMemsetAsync(sc->counters, 0, 4 * sizeof(uint32_t), st));
+            }
+            p.ps.seg_base = group_segs;
+            std::memcpy(group.segs + group_segs, p.segs, sizeof(Seg) * (size_t)p.nseg);
+            group_segs += p.nseg;
+        } else if (ci > 0) {
+            CK(cudaMemsetAsync(sc->counters, 0, 4 * sizeof(uint32_t), st));
+        }
         if (wide) CK(launch_check_wide(prec, p, blocks, smem, st));
-        else if (prec == RPM_PREC_FP32_RECHECK) CK(launch_check_fp32(p, blocks, smem, st));
+        else if (recheck) CK(launch_check_fp32(p, blocks, smem, st));
         else CK(launch_check_exact(prec, p, blocks, smem, st));
         if (sc->timed && last) CK(cudaEventRecord(sc->ev[1], st));
-        if (prec == RPM_PREC_FP32_RECHECK) {
-            CK(launch_pair_recheck(p, ctx->num_sms * 2, st));
-            CK(launch_recheck(p, ctx->num_sms * 4, st));
-        }
+        if (recheck) last_p = p;
+    }
+    if (recheck) {
+        rc = flush_group();
+        if (rc) return rc;
     }
     if (sc->timed) {
         if (chunks.empty()) CK(cudaEventRecord(sc->ev[1], st));

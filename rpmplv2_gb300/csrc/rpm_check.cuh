@@ -86,6 +86,7 @@ struct PairSink {
     uint32_t *cfg_count;
     double *skel;                // [cfg_cap][kMaxDof + 1][3]
     PairAcc *acc;                // [cfg_cap]
+    int32_t seg_base;            // added to the launch's segment index in the records (several launches, one recheck)
 };
 
 #ifdef __CUDACC__
@@ -107,7 +108,8 @@ __device__ __forceinline__ bool push_pair(const PairSink *ps, int slot, int link
 
 __device__ __forceinline__ void complete_record(const PairSink *ps, int slot, int status, int seg, int64_t config,
                                                 int hit_link, int hit_j) {
-    if (slot >= 0) ps->cfgs[slot] = PairCfg{status == kPairs ? kPairs : kSettled, seg, config, hit_link, hit_j};
+    if (slot >= 0)
+        ps->cfgs[slot] = PairCfg{status == kPairs ? kPairs : kSettled, seg + ps->seg_base, config, hit_link, hit_j};
 }
 
 // An unsettled pair found by a drain lane, waiting for its owner's record.

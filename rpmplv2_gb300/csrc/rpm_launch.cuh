@@ -45,7 +45,7 @@ struct KParams {
 // recompute it whole in FP64 (the list holds every configuration of a launch).
 __device__ __forceinline__ void recheck_whole(const KParams &P, int seg, int64_t c) {
     const uint32_t r = atomicAdd(P.recheck_count, 1u);
-    P.recheck[r] = ((uint64_t)seg << 40) | (uint64_t)c;
+    P.recheck[r] = ((uint64_t)(seg + P.ps.seg_base) << 40) | (uint64_t)c;
 }
 #endif
 

@@ -43,6 +43,26 @@ def test_mixed_dof_single_launch(engine, prec, oracle_prec):
         engine.destroy_scene(it[0])
 
 
+def test_recheck_groups_of_many_segments(engine):
+    """FP32 + recheck over 20 requests that each want isValid and a distance:
+    40 launch segments, so the launches form two recheck groups (at most 32
+    segments each) that share the recheck lists in turn.  0 flips against
+    ref64, distances within 1e-5 m."""
+    robot, scene, q = scenes.xarm6_workload(20 * 512, seed=41)
+    sid = engine.create_scene(engine.upload_robot(robot), scene)
+    items = []
+    for k in range(20):
+        items.append((sid, _t(q[k * 512:(k + 1) * 512]), _t(512, torch.uint8), _t(512, torch.float64), None))
+    engine.check_batch(items, "fp32_recheck")
+    engine.sync()
+    rv, rd, _ = O.check_configs(robot, scene, q, prec="ref64")
+    v = np.concatenate([it[2].cpu().numpy() for it in items])
+    d = np.concatenate([it[3].cpu().numpy() for it in items])
+    assert np.array_equal(v, rv)
+    assert np.abs(d - rd).max() <= 1e-5
+    engine.destroy_scene(sid)
+
+
 @pytest.mark.parametrize("prec,oracle_prec", [("fp64", "ref64"), ("fp32_ref", "ref32"), ("fp32_recheck", "ref64")])
 def test_edges_uneven(engine, prec, oracle_prec):
     robot, scene, q1, q2, step = scenes.spatial10_edge_workload(6000, seed=32)
