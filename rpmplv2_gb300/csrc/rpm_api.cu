@@ -285,6 +285,7 @@ void free_scratch(Scratch *sc) {
     cudaFree(sc->n_e); cudaFree(sc->local); cudaFree(sc->kmax); cudaFree(sc->bprefix); cudaFree(sc->full);
     cudaFree(sc->work); cudaFree(sc->erecheck); cudaFree(sc->recheck); cudaFree(sc->counters); cudaFree(sc->status);
     cudaFree(sc->pairs); cudaFree(sc->pcfgs); cudaFree(sc->pskel); cudaFree(sc->pacc);
+    cudaFree(sc->pkey); cudaFree(sc->porder); cudaFree(sc->phist);
     cudaFree(sc->perm); cudaFree(sc->bins); cudaFree(sc->aux);
     for (int i = 0; i < 3; ++i) if (sc->ev[i]) cudaEventDestroy(sc->ev[i]);
     delete sc;
@@ -308,8 +309,10 @@ int get_scratch(rpm_ctx *ctx, cudaStream_t st, int64_t need, Scratch **out) {
             s->graphs.clear();
             cudaFree(s->recheck);
             cudaFree(s->pairs); cudaFree(s->pcfgs); cudaFree(s->pskel); cudaFree(s->pacc); cudaFree(s->perm);
+            cudaFree(s->pkey); cudaFree(s->porder);
             s->recheck = nullptr;
             s->perm = nullptr;
+            s->pkey = s->porder = nullptr;
         }
         const size_t cap = std::max<size_t>((size_t)need, 1u << 16);
         // records for 1/8 of the configurations (at least 4096, at most 65536),
@@ -318,6 +321,9 @@ int get_scratch(rpm_ctx *ctx, cudaStream_t st, int64_t need, Scratch **out) {
         const size_t ppair = 16 * pcfg;
         if (cudaMalloc(&s->recheck, 2 * cap * sizeof(uint64_t)) != cudaSuccess ||   // two launches per configuration
             cudaMalloc(&s->pairs, ppair * sizeof(uint64_t)) != cudaSuccess ||
+            cudaMalloc(&s->pkey, ppair * sizeof(uint32_t)) != cudaSuccess ||
+            cudaMalloc(&s->porder, ppair * sizeof(uint32_t)) != cudaSuccess ||
+            (!s->phist && cudaMalloc(&s->phist, kPairHist * sizeof(uint32_t)) != cudaSuccess) ||
             cudaMalloc(&s->pcfgs, pcfg * sizeof(PairCfg)) != cudaSuccess ||
             cudaMalloc(&s->pskel, pcfg * (kMaxDof + 1) * 3 * sizeof(double)) != cudaSuccess ||
             cudaMalloc(&s->pacc, pcfg * sizeof(PairAcc)) != cudaSuccess ||
@@ -643,6 +649,9 @@ int enqueue_segments(rpm_ctx *ctx, int prec, const std::vector<SegReq> &reqs_in,
         p.ps.cfg_count = sc->counters + 2;
         p.ps.skel = sc->pskel;
         p.ps.acc = sc->pacc;
+        p.ps.key = sc->pkey;
+        p.ps.order = sc->porder;
+        p.ps.hist = sc->phist;
         if (recheck) {
             if (group_segs + p.nseg > kMaxSegs) {   // the group is full: its recheck, then fresh lists
                 rc = flush_group();

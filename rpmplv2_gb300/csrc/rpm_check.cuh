@@ -87,7 +87,18 @@ struct PairSink {
     double *skel;                // [cfg_cap][kMaxDof + 1][3]
     PairAcc *acc;                // [cfg_cap]
     int32_t seg_base;            // added to the launch's segment index in the records (several launches, one recheck)
+    // evaluation order of the listed pairs (nullable: list order), sorted by
+    // kind and by the regions of the segment's ends around the box (kPairKeys)
+    uint32_t *key;               // [pair_cap]
+    uint32_t *order;             // [pair_cap]
+    uint32_t *hist;              // [kPairHist]: counts, then offsets, then a CTA counter
 };
+
+// Sort keys of listed pairs: kind (isValid, distance) x region of A x region
+// of B (27 each: below, inside or above the box's slab on each axis), and a
+// last bucket for pairs the evaluation skips.
+constexpr uint32_t kPairKeys = 2 * 729 + 1;
+constexpr uint32_t kPairHist = 2 * kPairKeys + 1;
 
 #ifdef __CUDACC__
 // A new record (status kSettled until completed), or -1 when the list is full.

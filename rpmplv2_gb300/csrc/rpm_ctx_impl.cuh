@@ -95,6 +95,8 @@ struct Scratch {
     // pair-level recheck lists (see PairSink)
     size_t pcfg_cap = 0, ppair_cap = 0;
     uint64_t *pairs = nullptr;
+    uint32_t *pkey = nullptr, *porder = nullptr;   // evaluation order of the pairs (ppair_cap each)
+    uint32_t *phist = nullptr;                     // kPairHist
     PairCfg *pcfgs = nullptr;
     double *pskel = nullptr;
     PairAcc *pacc = nullptr;

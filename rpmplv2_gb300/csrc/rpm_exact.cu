@@ -182,6 +182,8 @@ constexpr uint32_t kSkelWarpRounds = 2;
 // 1. FP64 skeleton of each recorded configuration.
 __global__ void k_pair_skel(const __grid_constant__ KParams P) {
     __shared__ double sc[kThreads / 32][2 * kMaxDof];
+    if (P.ps.hist && blockIdx.x == 0)   // for k_pair_key, which runs next
+        for (uint32_t i = threadIdx.x; i < kPairHist; i += blockDim.x) P.ps.hist[i] = 0;
     const uint32_t n = min(*P.ps.cfg_count, P.ps.cfg_cap);
     const uint32_t warps = gridDim.x * (blockDim.x / 32);
     if (n <= kSkelWarpRounds * warps) {   // a warp each, consecutive records on different SMs
@@ -222,6 +224,76 @@ struct PairRuns {
     __device__ bool active() const { return lane < per; }
 };
 
+// 2a. Sort key of each listed pair (kPairKeys), counted per key; the last CTA
+// to finish turns the counts into bucket offsets.  The pairs of a warp then
+// mostly take one path through the FP64 trees, where the list order mixes
+// the two kinds and every region of both.
+__global__ void k_pair_key(const __grid_constant__ KParams P) {
+    __shared__ bool last;
+    __shared__ uint32_t wsum[kThreads / 32];
+    const uint32_t n = min(*P.ps.pair_count, P.ps.pair_cap);
+    const uint32_t ncfg = min(*P.ps.cfg_count, P.ps.cfg_cap);
+    uint32_t *hist = P.ps.hist;
+    for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+        uint32_t slot, key = kPairKeys - 1;
+        int link, j, kind;
+        if (decode_pair(P.ps, k, ncfg, slot, link, j, kind)) {
+            const Seg &sg = P.segs[P.ps.cfgs[slot].seg];
+            const double *A = P.ps.skel + (size_t)slot * (kMaxDof + 1) * 3 + 3 * link, *B = A + 3;
+            uint32_t ra = 0, rb = 0;
+#pragma unroll
+            for (int a = 0; a < 3; ++a) {
+                const double lo = sg.obs_d[a * sg.n_pad + j], hi = sg.obs_d[(a + 3) * sg.n_pad + j];
+                ra = ra * 3 + (A[a] < lo ? 0u : (A[a] > hi ? 2u : 1u));
+                rb = rb * 3 + (B[a] < lo ? 0u : (B[a] > hi ? 2u : 1u));
+            }
+            key = (uint32_t)kind * 729u + ra * 27u + rb;
+        }
+        P.ps.key[k] = key;
+        atomicAdd(&hist[key], 1u);
+    }
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) last = atomicAdd(&hist[2 * kPairKeys], 1u) == gridDim.x - 1;
+    __syncthreads();
+    if (!last) return;
+    __threadfence();
+    // exclusive scan of the counts: kPer consecutive keys per thread, then
+    // the threads' sums across the CTA
+    constexpr int kPer = (int)((kPairKeys + kThreads - 1) / kThreads);
+    uint32_t c[kPer], sum = 0;
+#pragma unroll
+    for (int i = 0; i < kPer; ++i) {
+        const uint32_t b = threadIdx.x * kPer + i;
+        c[i] = b < kPairKeys ? __ldcg(&hist[b]) : 0u;
+        sum += c[i];
+    }
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    uint32_t x = sum;
+#pragma unroll
+    for (int off = 1; off < 32; off <<= 1) {
+        const uint32_t y = __shfl_up_sync(0xffffffffu, x, off);
+        if (lane >= off) x += y;
+    }
+    if (lane == 31) wsum[warp] = x;
+    __syncthreads();
+    uint32_t run = x - sum;
+    for (int w = 0; w < warp; ++w) run += wsum[w];
+#pragma unroll
+    for (int i = 0; i < kPer; ++i) {
+        const uint32_t b = threadIdx.x * kPer + i;
+        if (b < kPairKeys) hist[kPairKeys + b] = run;
+        run += c[i];
+    }
+}
+
+// 2b. The pairs in key order.
+__global__ void k_pair_scatter(const __grid_constant__ KParams P) {
+    const uint32_t n = min(*P.ps.pair_count, P.ps.pair_cap);
+    for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x)
+        P.ps.order[atomicAdd(&P.ps.hist[kPairKeys + P.ps.key[k]], 1u)] = k;
+}
+
 // 2. The reference's FP64 tree for each listed pair on the FP64 skeleton
 // (pairs of configurations that ended settled, or that were routed to the
 // whole-configuration recheck, belong to records not completed with kPairs
@@ -234,7 +306,7 @@ __global__ void k_pair_eval(const __grid_constant__ KParams P) {
     for (uint32_t k = run.first; k < n; k += run.stride) {
         uint32_t slot;
         int link, j, kind;
-        if (!decode_pair(P.ps, k, ncfg, slot, link, j, kind)) continue;
+        if (!decode_pair(P.ps, P.ps.order ? P.ps.order[k] : k, ncfg, slot, link, j, kind)) continue;
         const Seg &sg = P.segs[P.ps.cfgs[slot].seg];
         ObsView<double> ob{sg.obs_d, sg.obs_f + (size_t)kRowGround * sg.n_pad, sg.n, sg.n_pad};
         pair_eval_one(*sg.robot, ob, P.nmd, P.ps.skel + (size_t)slot * (kMaxDof + 1) * 3, link, j, kind, P.ps.acc[slot]);
@@ -852,6 +924,10 @@ cudaError_t launch_distance_underest(int mode, const NearParams &p, cudaStream_t
 
 cudaError_t launch_pair_recheck(const KParams &p, int grid, cudaStream_t st) {
     k_pair_skel<<<grid * 4, kThreads, 0, st>>>(p);
+    if (p.ps.order) {
+        k_pair_key<<<grid, kThreads, 0, st>>>(p);
+        k_pair_scatter<<<grid, kThreads, 0, st>>>(p);
+    }
     k_pair_eval<<<grid * 2, kThreads, 0, st>>>(p);
     k_pair_fold<<<grid, kThreads, 0, st>>>(p);
     return cudaGetLastError();
