@@ -339,22 +339,31 @@ int get_scratch(rpm_ctx *ctx, cudaStream_t st, int64_t need, Scratch **out) {
     return RPM_OK;
 }
 
-// The stream's planner working memory, at least `bytes`.  Growing it waits for
-// the stream (earlier calls may still read the old block); otherwise the
-// block is reused in stream order with no allocation on the call's path.
+// The stream's planner working memory, at least `bytes`, reused in stream
+// order: no allocation on a call's path once it is large enough.  It grows
+// in stream order too (the old block is freed after the work already queued
+// on the stream, the new one is ready for the work queued next), at least
+// doubling, so a serving stream neither waits nor synchronises the device.
 int get_aux(rpm_ctx *ctx, cudaStream_t st, size_t bytes, void **out) {
     Scratch *s = nullptr;
     int rc = get_scratch(ctx, st, 0, &s);
     if (rc) return rc;
     if (s->aux_cap < bytes) {
+        cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+        CK(cudaStreamIsCapturing(st, &cs));
+        if (cs != cudaStreamCaptureStatusNone)
+            return fail(RPM_ERR_INVALID, "the stream's planner scratch grows outside stream capture: "
+                                         "make one call of this size on the stream before capturing");
+        const size_t cap = std::max<size_t>({bytes, 2 * s->aux_cap, (size_t)4 << 20});
         if (s->aux) {
-            CK(cudaStreamSynchronize(st));
-            cudaFree(s->aux);
+            CK(cudaFreeAsync(s->aux, st));
             s->aux = nullptr;
             s->aux_cap = 0;
         }
-        const size_t cap = std::max<size_t>(bytes, (size_t)1 << 20);
-        if (cudaMalloc(&s->aux, cap) != cudaSuccess) return fail(RPM_ERR_NOMEM, "planner scratch allocation failed");
+        if (cudaMallocAsync(&s->aux, cap, st) != cudaSuccess) {
+            cudaGetLastError();
+            return fail(RPM_ERR_NOMEM, "planner scratch allocation failed");
+        }
         s->aux_cap = cap;
     }
     *out = s->aux;

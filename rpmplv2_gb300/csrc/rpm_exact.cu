@@ -767,11 +767,14 @@ __global__ void __launch_bounds__(kThreads) k_distance_nearest(const __grid_cons
 // decides which links the profile keeps.  Points are written for every pair:
 // where the reference stops at a hit the configuration's points are flagged
 // invalid (flag 0), as in k_distance_nearest.
-constexpr int kNearCtaThreads = 256;
+// Threads per CTA: 512 for the reference numerics (a pair each up to 512
+// pairs, where 256 threads leave some two trees in a row), 256 for the FP64
+// form (its registers).
+template <int MODE> constexpr int near_cta_threads() { return MODE == 1 ? 512 : 256; }
 constexpr int64_t kNearCtaMaxConfigs = 64;
 
 template <int MODE>
-__global__ void __launch_bounds__(kNearCtaThreads) k_distance_nearest_cta(const __grid_constant__ NearParams P) {
+__global__ void __launch_bounds__(near_cta_threads<MODE>()) k_distance_nearest_cta(const __grid_constant__ NearParams P) {
     typedef typename std::conditional<MODE == 0, double, float>::type T;
     __shared__ T skel[(kMaxDof + 1) * 3];
     __shared__ double sc[2 * kMaxDof];
@@ -903,8 +906,8 @@ __global__ void __launch_bounds__(kThreads) k_distance_underest(const __grid_con
 
 cudaError_t launch_distance_nearest(int mode, const NearParams &p, cudaStream_t st) {
     if (p.C > 0 && p.C <= kNearCtaMaxConfigs) {   // a few states: one CTA each
-        if (mode == RPM_PREC_FP32_REF) k_distance_nearest_cta<1><<<(unsigned)p.C, kNearCtaThreads, 0, st>>>(p);
-        else k_distance_nearest_cta<0><<<(unsigned)p.C, kNearCtaThreads, 0, st>>>(p);
+        if (mode == RPM_PREC_FP32_REF) k_distance_nearest_cta<1><<<(unsigned)p.C, near_cta_threads<1>(), 0, st>>>(p);
+        else k_distance_nearest_cta<0><<<(unsigned)p.C, near_cta_threads<0>(), 0, st>>>(p);
         return cudaGetLastError();
     }
     const unsigned grid = (unsigned)((p.C + kThreads / 32 - 1) / (kThreads / 32));
