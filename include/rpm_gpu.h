@@ -361,10 +361,8 @@ int rpm_extend_spines(rpm_ctx *ctx, int32_t robot_id, const float *q_dev, const 
  * computeDistance(q_reached, true) in 'precision' (dist_dev, nullable).
  * q_reached_dev is horizon_size x D; status_dev per rpm_state_status
  * (RPM_STATE_REACHED = isReached).  Working memory is a per-stream block
- * reused in stream order; it grows (stream-ordered) when a call needs more,
- * which stream capture does not allow: before capturing a call, make one of
- * the same size on the stream (a growth under capture returns
- * RPM_ERR_INVALID). */
+ * reused in stream order; the first call on a stream, or one that needs
+ * more, grows it in stream order (cudaMallocAsync), without synchronising. */
 typedef struct rpm_spine_params {
     int32_t num_layers;   /* RGBTConnectConfig::NUM_LAYERS */
     int32_t num_iter;     /* RBTConnectConfig::NUM_ITER_SPINE */

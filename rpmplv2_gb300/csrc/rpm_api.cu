@@ -352,8 +352,7 @@ int get_aux(rpm_ctx *ctx, cudaStream_t st, size_t bytes, void **out) {
         cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
         CK(cudaStreamIsCapturing(st, &cs));
         if (cs != cudaStreamCaptureStatusNone)
-            return fail(RPM_ERR_INVALID, "the stream's planner scratch grows outside stream capture: "
-                                         "make one call of this size on the stream before capturing");
+            return fail(RPM_ERR_INVALID, "the stream's planner scratch cannot grow during stream capture");
         const size_t cap = std::max<size_t>({bytes, 2 * s->aux_cap, (size_t)4 << 20});
         if (s->aux) {
             CK(cudaFreeAsync(s->aux, st));
