@@ -657,9 +657,11 @@ int enqueue_segments(rpm_ctx *ctx, int prec, const std::vector<SegReq> &reqs_in,
         p.ps.cfg_count = sc->counters + 2;
         p.ps.skel = sc->pskel;
         p.ps.acc = sc->pacc;
-        p.ps.key = sc->pkey;
-        p.ps.order = sc->porder;
-        p.ps.hist = sc->phist;
+        if (total >= kSortPairsMinConfigs) {   // small batches list few pairs: list order, two launches fewer
+            p.ps.key = sc->pkey;
+            p.ps.order = sc->porder;
+            p.ps.hist = sc->phist;
+        }
         if (recheck) {
             if (group_segs + p.nseg > kMaxSegs) {   // the group is full: its recheck, then fresh lists
                 rc = flush_group();

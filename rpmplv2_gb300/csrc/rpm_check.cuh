@@ -99,6 +99,8 @@ struct PairSink {
 // last bucket for pairs the evaluation skips.
 constexpr uint32_t kPairKeys = 2 * 729 + 1;
 constexpr uint32_t kPairHist = 2 * kPairKeys + 1;
+// Batches from this many configurations recheck their pairs in key order.
+constexpr int64_t kSortPairsMinConfigs = 65536;
 
 #ifdef __CUDACC__
 // A new record (status kSettled until completed), or -1 when the list is full.
