@@ -4,8 +4,10 @@ recurrence starts one step earlier from 0 (z * 0 + c0 is c0), the
 coefficients and the last factor are selected per lane, and the quadrant swap
 trades the two values.  This restates both sequences in IEEE double (numpy
 float64 scalars: every product and sum rounded, no fused multiply-add, as
-dmul/dadd are on the device) and checks that they give the same bits.  The
-GPU tests check the device code itself through the skeletons built on it."""
+dmul/dadd are on the device) and checks that they give the same bits.  So
+does the warp forward kinematics' joint step (skel_coop), branchy against
+branch-free with selected operands.  The GPU tests check the device code
+itself through the skeletons built on it."""
 import numpy as np
 
 F = np.float64
@@ -71,3 +73,53 @@ def test_split_sincos_equals_per_lane_bits():
         a, b = per_lane(F(x)), split(F(x))
         assert np.float64(a[0]).tobytes() == np.float64(b[0]).tobytes(), x
         assert np.float64(a[1]).tobytes() == np.float64(b[1]).tobytes(), x
+
+
+def _joint(v, X_p, M, rot_identity, ax, sn, cs, branch_free):
+    """One skel_coop joint for the 12 lanes (R row-major on lanes 0-8, p on
+    9-11): the branchy per-lane form and the form with selected operands."""
+    ia, ib = {0: (1, 2), 1: (2, 0), 2: (0, 1)}[ax]
+    new = list(v)
+    for lane in range(12):
+        is_r, is_p = lane < 9, lane >= 9
+        row, col = (lane // 3, lane % 3) if is_r else (lane - 9, 0)
+        r0, r1, r2 = v[3 * row], v[3 * row + 1], v[3 * row + 2]
+        if branch_free:
+            X = (X_p[0], X_p[1], X_p[2]) if is_p else (M[col], M[3 + col], M[6 + col])
+            t = (r0 * X[0] + r1 * X[1]) + r2 * X[2]
+            tp = t + v[lane]
+            new[lane] = tp if is_p else (t if (is_r and not rot_identity) else v[lane])
+        elif is_p:
+            new[lane] = ((r0 * X_p[0] + r1 * X_p[1]) + r2 * X_p[2]) + v[lane]
+        elif not rot_identity:
+            new[lane] = (r0 * M[col] + r1 * M[3 + col]) + r2 * M[6 + col]
+    out = list(new)
+    for lane in range(9):
+        row, col = lane // 3, lane % 3
+        x = new[3 * row + (ib if col == ia else ia)]
+        if branch_free:
+            a, b = col == ia, col == ib
+            w = new[lane] * cs + x * (-sn if b else sn)
+            out[lane] = w if (a or b) else new[lane]
+        elif col == ia:
+            out[lane] = new[lane] * cs + x * sn
+        elif col == ib:
+            out[lane] = new[lane] * cs + -(x * sn)
+    return out
+
+
+def test_branch_free_joint_equals_branchy_bits():
+    rng = np.random.default_rng(11)
+    for _ in range(3000):
+        vals = rng.normal(size=24)
+        vals[rng.random(24) < 0.2] = 0.0
+        vals[rng.random(24) < 0.05] = -0.0
+        v = [F(x) for x in vals[:12]]
+        M = [F(x) for x in vals[12:21]]
+        Xp = [F(x) for x in vals[21:24]]
+        q = F(rng.uniform(-np.pi, np.pi)) if rng.random() < 0.9 else F(0.0)
+        sn, cs = per_lane(q)
+        ax, ident = int(rng.integers(0, 3)), bool(rng.random() < 0.3)
+        a = _joint(v, Xp, M, ident, ax, sn, cs, False)
+        b = _joint(v, Xp, M, ident, ax, sn, cs, True)
+        assert all(np.float64(p).tobytes() == np.float64(r).tobytes() for p, r in zip(a, b))
