@@ -621,10 +621,11 @@ def run_ours(args, ws, rank, local):
                 "d2h_bytes_per_step": C * (1 + 8), "call": "rpm_check_configs_host", "matches_device_run": e2e_ok,
                 "transfer": "pinned host buffers, staged through device memory by DMA copies in one chunk of "
                             "up to 1,048,576 configurations"},
-        # per step: the check order (k_bin_count, k_bin_scan, k_bin_scatter), then for each of the
-        # two outputs (isValid, distance): k_check_fp32 compiled for that output, the pair recheck
-        # k_pair_skel / k_pair_eval / k_pair_fold and the whole-configuration k_recheck
-        "gpu_launches": 13 * args.steps,
+        # per step: the check order (k_bin_count, k_bin_scan, k_bin_scatter), k_check_fp32 compiled
+        # for each of the two outputs (isValid, distance), then one recheck round for both:
+        # k_pair_skel / k_pair_key / k_pair_scatter / k_pair_eval / k_pair_fold and the
+        # whole-configuration k_recheck
+        "gpu_launches": 11 * args.steps,
         "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak_fp32, "unit": "TFLOP/s",
                      "frac": achieved / peak_fp32 if peak_fp32 else None, "traffic": traffic_per_launch(),
                      "kernel": "k_check_fp32", "kernel_ms": statistics.median(bulk_ms),
