@@ -346,12 +346,12 @@ DevBufs layout(rpm_server *srv, const Req *q) {
     return d;
 }
 
-// Host callback at the end of a batch's stream work: marks the slot finished
-// and wakes the workers, so they sleep instead of polling events.  It calls no
-// CUDA function.
-// The stream has reached the end of the batch: every result is in the
-// callers' host buffers, so the requests complete now (status and t_done);
-// the worker retires the slot later (trace, memory) without holding them up.
+// Host callback at the end of a batch's stream work.  Every result is in the
+// callers' host buffers by then, so the batch's requests complete here
+// (status, t_done, the scene version read) and their waiters wake; the slot is
+// marked finished and the workers wake too (they sleep instead of polling
+// events), and the slot's worker retires it later (trace, arena memory)
+// without holding the requests up.  It calls no CUDA function.
 void CUDART_CB batch_done(void *arg) {
     Slot *sl = static_cast<Slot *>(arg);
     rpm_server *srv = static_cast<rpm_server *>(sl->srv);
