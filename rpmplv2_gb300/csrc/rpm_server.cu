@@ -23,9 +23,10 @@
 //   * packs the requests of a batch -- from any scenes and robots,
 //     configuration and edge requests alike -- into multi-segment launches
 //     (configurations) and multi-segment edge pipelines (edges);
-//   * retires batches by CUDA events, frees their memory and time-stamps every
-//     request (submit, admit, launch, done, and a device-side trace of the
-//     batch's copies and checks).
+//   * completes a batch's requests in a host callback at the end of its
+//     stream work, then retires the batch: frees its memory and time-stamps
+//     every request (submit, admit, launch, done, and a device-side trace of
+//     the batch's copies and checks).
 // Each request's result is what the same check gives alone: configurations are
 // evaluated independently, and a batch reads one consistent version of each
 // scene (the version current when the batch was enqueued, kept for all its
